@@ -1,0 +1,544 @@
+// CPU ORACLE -- test infrastructure only (see contact_oracle.h).
+//
+// Case driver: contac / panprc (m_scontc.f90:37-553), set-up (m_sdis.f90), influence
+// coefficients (sgencr, m_visc.f90:127-376), TANG (m_stang.f90:28-951), output quantities
+// (soutpt, m_soutpt.f90:377-511) and the cntc_calculate error mapping
+// (contact_addon.f90:3870-3890).
+#include "contact_oracle.h"
+#include "orc_hertz.hpp"
+#include "orc_norm.hpp"
+#include "orc_tang.hpp"
+
+using namespace orc;
+
+namespace {
+
+constexpr int CNTC_err_norm = -27, CNTC_err_tang = -28, CNTC_err_other = -99;
+
+struct Case {
+    const orc_problem *pb;
+    // geometry
+    int mx, my, npot;
+    double dx, dy, dxdy, xl, yl, xc1, yc1;
+    Grid g;
+    // Hertz
+    double a1 = 0, b1 = 0, aa = 0, bb = 0, aob = 0, rho = 0, cp = 0, scale = 1;
+    // material
+    double ga, nu, ak;
+    // kinematics
+    double chi, dq, veloc, pen, fntrue, cksi, ceta, cphi, muscal;
+    // solver
+    TangCtx tc;
+    int maxout;
+    // state
+    Eldiv igs;
+    GF3 ps, hs, us, ss;
+    std::vector<double> mus;
+    Inflcf cs, cv, ms;
+    int itnorm = 0, ittang = 0, itcg = 0, itgs = 0, solver_eff = 0;
+    bool unsupported = false, aborted = false;
+};
+
+// set_tang_rhs, m_sdis.f90:498-583 (M=0, no extra rhs)
+void set_tang_rhs(Case &c) {
+    const orc_problem *pb = c.pb;
+    bool is_roll = pb->tang == 2 || pb->tang == 3;
+    double facphi = 1.0 / 6.0;
+    double xofs = is_roll ? std::cos(c.chi) * c.dq * facphi : 0.0;
+    double yofs = is_roll ? std::sin(c.chi) * c.dq * facphi : 0.0;
+    for (int ii = 0; ii < c.npot; ii++) {
+        c.hs.vx(ii) = 1.0 * -(c.g.y[ii] + yofs - 0.0) * c.cphi + 0.0;
+        c.hs.vy(ii) = 1.0 * (c.g.x[ii] + xofs - 0.0) * c.cphi + 0.0;
+    }
+    if (pb->force3 == 0) for (int ii = 0; ii < c.npot; ii++) c.hs.vx(ii) += c.cksi;
+    if (pb->force3 <= 1) for (int ii = 0; ii < c.npot; ii++) c.hs.vy(ii) += c.ceta;
+    for (int ii = 0; ii < c.npot; ii++) { c.hs.vx(ii) *= -c.dq; c.hs.vy(ii) *= -c.dq; }
+}
+
+// eldiv0, m_sdis.f90:818-1009 (3-D case)
+void eldiv0(Case &c) {
+    const double facpen = (double)0.60f, reltol = (double)0.01f;
+    const int maxit = 50;
+    double fnscal = c.fntrue / c.ga;
+    int imin = 0;
+    for (int ii = 1; ii < c.npot; ii++) if (c.hs.vn(ii) < c.hs.vn(imin)) imin = ii;
+    double hsmin = c.hs.vn(imin);
+    double pentru = c.pen - hsmin;
+    if (c.pb->norm == 1 && c.my == 1) {
+        double rm = 1.0;
+        double cdy = 0.35 - 0.05 * (std::log(c.dy) - std::log(200.0));
+        pentru = std::pow(fnscal / c.dy * (1.0 - c.nu) / 0.6 / cdy / std::pow(rm, 0.1), (double)0.926f);
+        c.pen = pentru + hsmin;
+    } else if (c.pb->norm == 1) {
+        double rmn = 1.0;
+        double fac = rmn * 0.75 * std::sqrt(pi) * (1.0 - c.nu);
+        double penmin = 0.0, fnmin = 0.0;
+        double penmax = fac * fnscal / std::sqrt(c.dxdy);
+        int ncnmax = 0;
+        for (int ii = 0; ii < c.npot; ii++) if (c.hs.vn(ii) - hsmin < facpen * penmax) ncnmax++;
+        double fnmax = penmax * std::sqrt(c.dxdy * ncnmax) / fac;
+        int iter = 0;
+        while (iter < maxit && std::fabs(fnmax - fnmin) > reltol * fnscal) {
+            iter++;
+            double penmid = 0.5 * (penmax + penmin);
+            int ncnmid = 0;
+            for (int ii = 0; ii < c.npot; ii++) if (c.hs.vn(ii) - hsmin < facpen * penmid) ncnmid++;
+            double fnmid = penmid * std::sqrt(c.dxdy * ncnmid) / fac;
+            if (fnmid < fnscal) { penmin = penmid; fnmin = fnmid; }
+            else { penmax = penmid; fnmax = fnmid; }
+        }
+        pentru = penmax;
+        c.pen = pentru + hsmin;
+    }
+    for (int ii = 0; ii < c.npot; ii++)
+        c.igs.el[ii] = (c.hs.vn(ii) - hsmin < facpen * pentru) ? Adhes : Exter;
+}
+
+// init_curr_data, m_sdis.f90:587-770 (B=0,2,3; I=0..3)
+void init_curr_data(Case &c, int ihertz) {
+    const orc_problem *pb = c.pb;
+    c.us.init(c.npot);
+    if (pb->iestim == 0) for (int ii = 0; ii < c.npot; ii++) c.ps.vn(ii) = 0.0;
+    if (pb->iestim == 0 || pb->iestim == 2 || pb->tang == 0)
+        for (int ii = 0; ii < c.npot; ii++) { c.ps.vx(ii) = 0.0; c.ps.vy(ii) = 0.0; }
+    bool use_hz = (pb->iestim == 0 && pb->bound == 0 && ihertz >= 1);
+    if (pb->bound == 2 || use_hz) {
+        if (ihertz <= 3) {
+            double pnmax = 3.0 * c.fntrue / (2.0 * pi * c.aa * c.bb);
+            for (int ii = 0; ii < c.npot; ii++) {
+                double f = 1.0 - (c.g.x[ii] / c.aa) * (c.g.x[ii] / c.aa) - (c.g.y[ii] / c.bb) * (c.g.y[ii] / c.bb);
+                c.ps.vn(ii) = pnmax * std::sqrt(std::max(0.0, f));
+            }
+        }
+    }
+    if (pb->bound == 3 && ihertz <= 3) {
+        double pnmax = 2.0 * c.fntrue / (pi * c.aa * c.bb);
+        for (int ii = 0; ii < c.npot; ii++) {
+            double f = 1.0 - (c.g.x[ii] / c.aa) * (c.g.x[ii] / c.aa) - (c.g.y[ii] / c.bb) * (c.g.y[ii] / c.bb);
+            c.ps.vn(ii) = pnmax * std::max(0.0, f);
+        }
+    }
+    if ((pb->bound >= 2 && pb->bound <= 4) || use_hz) {
+        for (int ii = 0; ii < c.npot; ii++) c.igs.el[ii] = (c.ps.vn(ii) > (double)1e-20f) ? Adhes : Exter;
+    } else if (pb->iestim == 0) {
+        eldiv0(c);
+    }
+    if (pb->iestim == 1) {
+        for (int ii = 0; ii < c.npot; ii++) {
+            if (c.igs.el[ii] <= Exter) { c.ps.vn(ii) = 0; c.ps.vx(ii) = 0; c.ps.vy(ii) = 0; }
+            else if (c.igs.el[ii] == Slip) {
+                double pabs = std::max(1e-10, std::sqrt(c.ps.vx(ii) * c.ps.vx(ii) + c.ps.vy(ii) * c.ps.vy(ii)));
+                c.ps.vx(ii) = c.mus[ii] * c.ps.vn(ii) * c.ps.vx(ii) / pabs;
+                c.ps.vy(ii) = c.mus[ii] * c.ps.vn(ii) * c.ps.vy(ii) / pabs;
+            }
+        }
+    }
+    if (pb->iestim == 2)
+        for (int ii = 0; ii < c.npot; ii++) if (c.igs.el[ii] >= Adhes) c.igs.el[ii] = Adhes;
+    for (int ii = 0; ii < c.npot; ii++) if (c.hs.vn(ii) > (double)1e29f) c.igs.el[ii] = Exter;
+    areas(c.igs);
+}
+
+// stang_rhs, m_stang.f90:749-951 (steady rolling / first step, pv = 0)
+void stang_rhs(Case &c, const std::vector<int> &iel, const std::vector<double> &facdt, GF3 &wsfix) {
+    const int mx = c.mx, my = c.my, n = c.npot;
+    areas(c.igs);
+    GF3 usn, uvn; usn.init(n); uvn.init(n);
+    GF3 wsrig; wsrig.init(n);
+    for (int ik = 1; ik <= 2; ik++)
+        for (int ii : iel) wsrig.c[ik - 1][ii] = -facdt[ii] * c.hs.c[ik - 1][ii];
+    vecaijpj(c.igs, AllInt, usn, ikTANG, c.ps, c.igs, ikZ, c.cs, mx, my);
+    if (c.pb->tang == 3) vecaijpj(c.igs, AllInt, uvn, ikTANG, c.ps, c.igs, ikZ, c.cv, mx, my);
+    // T=1,2 with a fresh sequence: previous tractions pv are zero, so uvn = uvt = ubnd = 0
+    for (int ik = 1; ik <= 2; ik++)
+        for (int ii : iel)
+            wsfix.c[ik - 1][ii] = wsrig.c[ik - 1][ii] + usn.c[ik - 1][ii] - uvn.c[ik - 1][ii];
+}
+
+// tang_solver, m_solvpt.f90:382-493
+int tang_solver(Case &c, const GF3 &wstot, int &info1, double &err) {
+    TangCtx &tc = c.tc;
+    int it = 0;
+    bool bad = false;
+    if (c.solver_eff == isolv_stdygs) {
+        it = stdygs(tc, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, tc.eps, tc.maxgs, tc.omegah, tc.omegas, info1, err, bad);
+    } else if (c.solver_eff == isolv_gdstdy) {
+        bool lstagn = false;
+        it = gdsteady(tc, tc.maxgs, tc.eps, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, err, lstagn, bad);
+        if (!bad && lstagn)
+            it = stdygs(tc, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, tc.eps, tc.maxgs, tc.omegah, tc.omegas, info1, err, bad);
+    } else if (c.solver_eff == isolv_tangcg) {
+        it = tangcg(tc, tc.maxgs, tc.eps, wstot, c.cs, c.ms, c.igs, c.mus, c.ps, c.ss, err, bad);
+    } else {
+        c.unsupported = true;
+        return 0;
+    }
+    if (bad) c.aborted = true;
+    return it;
+}
+
+// stang, m_stang.f90:28-746 (Coulomb friction, creepages prescribed F=0)
+int stang(Case &c) {
+    const orc_problem *pb = c.pb;
+    TangCtx &tc = c.tc;
+    const int mx = c.mx, my = c.my, npot = c.npot;
+    bool is_roll = pb->tang == 2 || pb->tang == 3, is_ssrol = pb->tang == 3;
+    std::vector<int> iel;
+    for (int ii = 0; ii < npot; ii++) if (c.igs.el[ii] >= Adhes) iel.push_back(ii);
+    int k = (int)iel.size();
+    int ixsta = (is_roll && std::fabs(c.chi - pi) < 0.01) ? mx : 1;
+    int icount = 0;
+    for (int iy = 1; iy <= my; iy++) if (c.igs.el[(ixsta - 1) + (iy - 1) * mx] >= Adhes) icount++;
+    if (is_ssrol) {
+        if (tc.gausei_eff == 5 && ixsta == 1) c.solver_eff = isolv_gdstdy;
+        else if (tc.gausei_eff != 2) c.solver_eff = isolv_stdygs;
+        else c.solver_eff = isolv_cnvxgs;
+    } else {
+        c.solver_eff = (tc.gausei_eff != 2) ? isolv_tangcg : isolv_cnvxgs;
+    }
+    if (icount > 0 && (c.solver_eff == isolv_stdygs || c.solver_eff == isolv_gdstdy)) c.solver_eff = isolv_cnvxgs;
+    if (tc.gausei_eff == 0 || tc.gausei_eff == 4 || tc.gausei_eff == 5) {
+        if (k <= 25) { tc.omegah = 1.0; tc.omegas = 1.0; }
+        else if (is_ssrol && c.solver_eff == isolv_cnvxgs) { tc.omegah = 0.5; tc.omegas = 0.5; }
+        else if (is_ssrol) {
+            if (c.dx / c.dy <= 5.0) { tc.omegah = 0.9; tc.omegas = 1.0; }
+            else if (c.dx / c.dy <= 15.0) { tc.omegah = 0.8; tc.omegas = 0.8; }
+            else { tc.omegah = 0.8; tc.omegas = 0.6; }
+        } else { tc.omegah = 0.5; tc.omegas = 0.5; }
+    }
+    if (c.solver_eff == isolv_cnvxgs) { c.unsupported = true; return -1; }
+    std::vector<double> facdt; std::vector<int> ii2j;
+    sxbnd(tc, c.solver_eff, c.igs, c.g, facdt, ii2j);
+    c.mus.assign(npot, pb->fstat);
+    GF3 wsfix; wsfix.init(npot);
+    stang_rhs(c, iel, facdt, wsfix);
+    int ittang = 0, itgs = 0;
+    bool zready = false;
+    GF3 tmp; tmp.init(npot);
+    while (!zready && ittang < tc.maxin) {
+        ittang++;
+        zready = true;
+        // solvpt, m_solvpt.f90:51-378 (F=0)
+        areas(c.igs);
+        GF3 wstot; wstot.init(npot);
+        gf_copy(AllElm, wsfix, wstot, ikTANG, c.igs);
+        int info = 0; double errpt = 0.0;
+        int it = tang_solver(c, wstot, info, errpt);
+        if (c.unsupported || c.aborted) return -1;
+        itgs += it;
+        if (info >= 3) { zready = true; ittang = -1; }
+        int newins = 0;
+        double tol = std::sqrt(2.0) * errpt;
+        for (int ii : iel) {
+            if (c.igs.el[ii] == Adhes) {
+                double pabs = std::sqrt(c.ps.vx(ii) * c.ps.vx(ii) + c.ps.vy(ii) * c.ps.vy(ii));
+                if (pabs >= c.mus[ii] * c.ps.vn(ii) + tol) {
+                    newins++;
+                    c.igs.el[ii] = Slip;
+                    c.ps.vx(ii) = c.ps.vx(ii) * c.mus[ii] * c.ps.vn(ii) / pabs;
+                    c.ps.vy(ii) = c.ps.vy(ii) * c.mus[ii] * c.ps.vn(ii) / pabs;
+                }
+            }
+        }
+        if (newins != 0) zready = false;
+        if (zready) {
+            areas(c.igs);
+            int ii0 = (std::max(1, mx / 2) - 1) + (std::max(1, my / 2) - 1) * mx;
+            gf_set(AllElm, 1.0, tmp, ikTANG, c.igs);
+            double tol1 = errpt * 2.0 * std::fabs(aijpj(ii0, ikX, tmp, c.igs, ikX, c.cs, mx, my));
+            double tol2 = errpt * 2.0 * std::fabs(aijpj(ii0, ikY, tmp, c.igs, ikY, c.cs, mx, my));
+            int newadh = 0;
+            for (int ii : iel) {
+                if (c.igs.el[ii] == Slip) {
+                    double ww = c.ss.vx(ii) * c.ps.vx(ii) + c.ss.vy(ii) * c.ps.vy(ii);
+                    double tl = tol1 * std::fabs(c.ps.vx(ii)) + tol2 * std::fabs(c.ps.vy(ii)) +
+                                errpt * (std::fabs(c.ss.vx(ii)) + std::fabs(c.ss.vy(ii)));
+                    if (ww > tl) { c.igs.el[ii] = Adhes; newadh++; }
+                }
+            }
+            if (newadh != 0) zready = false;
+            if (info > 0) zready = true;
+        }
+    }
+    if (!zready) ittang = -1;
+    c.itgs = itgs;
+    return ittang;
+}
+
+// soutpt, m_soutpt.f90:377-511 (force, moment, elastic energy, maximum pressure)
+void soutpt(Case &c, orc_result *r) {
+    const int mx = c.mx, my = c.my, npot = c.npot;
+    areas(c.igs);
+    vecaijpj(c.igs, AllInt, c.us, ikZ, c.ps, c.igs, -3, c.cs, mx, my);
+    vecaijpj(c.igs, AllInt, c.us, ikTANG, c.ps, c.igs, -3, c.cs, mx, my);
+    int nadh, nslip, nplast, nexter;
+    eldiv_count(c.igs, nadh, nslip, nplast, nexter);
+    if (c.pb->norm == 0) c.fntrue = c.dxdy * gf_sum(AllElm, c.ps, ikZ, c.igs);
+    double fxrel = c.dxdy * gf_sum(AllElm, c.ps, ikX, c.igs) / (c.fntrue * c.muscal + tiny_);
+    double fyrel = c.dxdy * gf_sum(AllElm, c.ps, ikY, c.igs) / (c.fntrue * c.muscal + tiny_);
+    double fxtrue = fxrel * (c.fntrue * c.muscal + tiny_);
+    double fytrue = fyrel * (c.fntrue * c.muscal + tiny_);
+    double dx_y = 0, dy_x = 0;
+    for (int ii = 0; ii < npot; ii++) { dx_y += c.ps.vx(ii) * c.g.y[ii]; dy_x += c.ps.vy(ii) * c.g.x[ii]; }
+    double mztrue = -c.dxdy * dx_y + c.dxdy * dy_x;
+    if (std::fabs(mztrue) < 0.5 * c.tc.eps * (c.muscal * c.fntrue + tiny_)) mztrue = 0.0;
+    double elen = 0.5 * 1e-3 * c.dxdy * gf_dot(AllInt, c.us, c.ps, ikALL, c.igs);
+    double pmax = gf_max(AllElm, c.ps, ikZ, c.igs);
+    r->fn = c.fntrue; r->fx = fxtrue; r->fy = fytrue; r->mz = mztrue;
+    r->elen = elen; r->pmax = pmax;
+    r->ncon = nadh + nslip + nplast; r->nadh = nadh; r->nslip = nslip;
+    for (int ii = 0; ii < npot; ii++) {
+        c.ss.vn(ii) = -c.pen + c.hs.vn(ii) + c.us.vn(ii);
+        if (c.igs.el[ii] != Slip) { c.ss.vx(ii) = 0.0; c.ss.vy(ii) = 0.0; }
+    }
+}
+
+} // namespace
+
+extern "C" {
+
+void orc_default_problem(orc_problem *pb) {
+    std::memset(pb, 0, sizeof(*pb));
+    pb->pvtime = 2; pb->bound = 0; pb->tang = 3; pb->norm = 1; pb->force3 = 0; pb->iestim = 0; pb->gausei = 0;
+    pb->maxgs = 999; pb->maxin = 20; pb->maxnr = 25; pb->maxout = 1; pb->eps = 1e-5;   // solv_init
+    pb->omegah = 0.9; pb->omegas = 1.0; pb->inislp = 0; pb->omgslp = 0.5;
+    pb->kdowfb = 1; pb->fdecay = 0.9; pb->betath = 0.1;
+    pb->d_ifc = 1.0; pb->d_lin = 1.0; pb->d_cns = 1.0; pb->d_slp = 1.0; pb->pow_s = 0.9;
+    pb->poiss1 = 0.28; pb->poiss2 = 0.28; pb->gg1 = 1.0; pb->gg2 = 1.0;
+    pb->fstat = 0.3; pb->fkin = 0.3;
+    pb->veloc = 1e3; pb->chi = 0.0; pb->dq = -1.0;
+    pb->ipotcn = -3; pb->ibase = 1;
+}
+
+int orc_opt_fft_size(int n) { return opt_fft_size(n); }
+
+double orc_eli(double elmodk, double *ellk, double *elle) { return eli(elmodk, *ellk, *elle); }
+
+void orc_influence_coefficients(int mx, int my, double dx, double dy, double nu, double ak, double xshft,
+                                double yshft, double *out) {
+    Inflcf c; c.alloc(mx, my, dx, dy);
+    elascf_pcwcns(ak, nu, mx, my, dx, dy, xshft, yshft, c);
+    size_t blk = (size_t)4 * mx * my;
+    for (int ik = 1; ik <= 3; ik++)
+        for (int jk = 1; jk <= 3; jk++)
+            std::memcpy(out + ((ik - 1) * 3 + (jk - 1)) * blk, c.cf[ik - 1][jk - 1].data(), blk * sizeof(double));
+}
+
+static void load_block(Inflcf &c, int mx, int my, const double *blk, double ga) {
+    c.alloc(mx, my, 1.0, 1.0);
+    std::memcpy(c.cf[2][2].data(), blk, (size_t)4 * mx * my * sizeof(double));
+    c.ga = ga; c.ga_inv = 1.0 / ga;
+}
+
+void orc_convolve(int mx, int my, const double *cf_block, double ga, const double *p, double *u) {
+    Inflcf c; load_block(c, mx, my, cf_block, ga);
+    Eldiv e; e.init(mx, my); for (int &v : e.el) v = Adhes; areas(e);
+    GF3 pp, uu; pp.init(mx * my); uu.init(mx * my);
+    std::memcpy(pp.c[2].data(), p, sizeof(double) * mx * my);
+    vecaijpj(e, AllElm, uu, ikZ, pp, e, ikZ, c, mx, my);
+    std::memcpy(u, uu.c[2].data(), sizeof(double) * mx * my);
+}
+
+void orc_convolve_direct(int mx, int my, const double *cf_block, double ga, const double *p, double *u) {
+    Inflcf c; load_block(c, mx, my, cf_block, ga);
+    Eldiv e; e.init(mx, my); for (int &v : e.el) v = Adhes; areas(e);
+    GF3 pp; pp.init(mx * my);
+    std::memcpy(pp.c[2].data(), p, sizeof(double) * mx * my);
+    for (int ii = 0; ii < mx * my; ii++) u[ii] = aijpj(ii, ikZ, pp, e, ikZ, c, mx, my);
+}
+
+int orc_calculate(const orc_problem *pb, orc_result *r) {
+    Case c;
+    c.pb = pb;
+    r->ierror = 0;
+    // combin_mater, m_hierarch_data.f90:1543-1553
+    double gg1 = pb->gg1, gg2 = pb->gg2, p1 = pb->poiss1, p2 = pb->poiss2;
+    c.ga = 2.0 / (1.0 / gg1 + 1.0 / gg2);
+    c.nu = c.ga * (p1 / gg1 + p2 / gg2) / 2.0;
+    c.ak = (c.ga / 4.0) * ((1.0 - 2.0 * p1) / gg1 - (1.0 - 2.0 * p2) / gg2);
+    c.maxout = pb->maxout;
+    if (c.maxout >= 2 && std::fabs(c.ak) < 1e-4) c.maxout = 1;
+    if (c.maxout <= 1 && std::fabs(c.ak) >= 1e-4) c.maxout = 10;
+    c.fntrue = pb->fn; c.pen = pb->pen;
+    c.cksi = pb->cksi; c.ceta = pb->ceta; c.cphi = pb->cphi;
+    c.chi = pb->chi; c.veloc = pb->veloc;
+    c.muscal = pb->fstat;
+    // Hertzian solution & potential contact (hzsol m_hertz.f90:29-93, potcon_hertz)
+    int ihertz = 0;
+    c.mx = std::max(1, (int)std::nearbyint(pb->potprm[0]));
+    c.my = std::max(1, (int)std::nearbyint(pb->potprm[1]));
+    double xl, yl, xh, yh, dx, dy;
+    if (pb->ipotcn <= -1 && pb->ipotcn >= -3) {
+        const double epshz = (double)1e-9f;
+        double e_star = c.ga / (1.0 - c.nu);
+        c.scale = pb->potprm[4];
+        if (pb->ipotcn == -3) { c.aa = pb->potprm[2]; c.bb = pb->potprm[3]; }
+        else if (pb->ipotcn == -1) { c.a1 = pb->potprm[2]; c.b1 = pb->potprm[3]; }
+        else { c.a1 = pb->potprm[2]; c.aob = pb->potprm[3]; }
+        if (pb->ipotcn == -2)
+            elliptic_to_curv(pb->norm, c.a1, c.aa, c.aob, c.b1, c.bb, c.cp, c.rho, c.fntrue, c.pen, e_star, epshz);
+        else
+            hzcalc3d(e_star, epshz, pb->ipotcn, c.a1, c.b1, c.aa, c.bb, pb->norm, c.pen, c.fntrue, c.cp, c.rho);
+        if (pb->ipotcn != -2) c.aob = (c.aa <= tiny_ && c.bb <= tiny_) ? 1.0 : c.aa / c.bb;
+        xl = -c.scale * std::max(1e-9, c.aa);
+        yl = -c.scale * std::max(1e-9, c.bb);
+        xh = -xl; yh = -yl;
+        dx = (xh - xl) / c.mx; dy = (yh - yl) / c.my;
+        ihertz = -pb->ipotcn;
+    } else if (pb->ipotcn >= 1 && pb->ipotcn <= 4) {
+        // potcon_fill, m_hierarch_data.f90:1801-1861
+        double a = pb->potprm[2], b = pb->potprm[3], cc = pb->potprm[4], d = pb->potprm[5];
+        if (pb->ipotcn == 1) { xl = a; yl = b; dx = cc; dy = d; }
+        else if (pb->ipotcn == 2) { xl = a; yl = b; dx = (cc - a) / c.mx; dy = (d - b) / c.my; }
+        else if (pb->ipotcn == 3) { dx = cc; dy = d; xl = a - 0.5 * dx; yl = b - 0.5 * dy; }
+        else { dx = (cc - a) / std::max(1, c.mx - 1); dy = (d - b) / std::max(1, c.my - 1); xl = a - 0.5 * dx; yl = b - 0.5 * dy; }
+    } else {
+        r->ierror = CNTC_err_other; return r->ierror;
+    }
+    c.dx = dx; c.dy = dy; c.dxdy = dx * dy; c.xl = xl; c.yl = yl;
+    c.xc1 = xl + 0.5 * dx; c.yc1 = yl + 0.5 * dy;
+    c.npot = c.mx * c.my;
+    c.g.create(c.mx, c.xc1, dx, c.my, c.yc1, dy);
+    // check_roll_stepsize, m_sdis.f90:125-206
+    bool is_roll = pb->tang == 2 || pb->tang == 3, is_ssrol = pb->tang == 3;
+    c.dq = (pb->dq > 0.0) ? pb->dq : dx;
+    if (is_ssrol && pb->gausei != 2) {
+        if (pb->tang >= 1 && std::fabs(c.chi) > 0.01 && std::fabs(c.chi - pi) > 0.01) c.chi = 0.0;
+        c.dq = dx;
+    }
+    if (!is_roll) { c.chi = 0.0; c.dq = 1.0; c.veloc = 1.0; }
+    // influence coefficients, sgencr m_visc.f90:127-376
+    c.cs.alloc(c.mx, c.my, dx, dy); c.ms.alloc(c.mx, c.my, dx, dy);
+    for (Inflcf *f : {&c.cs, &c.ms}) { f->ga = c.ga; f->ga_inv = 1.0 / c.ga; }
+    elascf_pcwcns(c.ak, c.nu, c.mx, c.my, dx, dy, 0.0, 0.0, c.cs);
+    bool nt_cpl = std::fabs(c.ak) >= 1e-6;
+    c.cs.nt_cpl = nt_cpl; c.ms.nt_cpl = nt_cpl;
+    if (is_roll && (nt_cpl || pb->tang == 2)) {
+        c.cv.alloc(c.mx, c.my, dx, dy); c.cv.ga = c.ga; c.cv.ga_inv = 1.0 / c.ga; c.cv.nt_cpl = nt_cpl;
+        elascf_pcwcns(c.ak, c.nu, c.mx, c.my, dx, dy, std::cos(c.chi) * c.dq, std::sin(c.chi) * c.dq, c.cv);
+        for (int jk = 1; jk <= 3; jk++)
+            for (size_t q = 0; q < c.cv.cf[0][0].size(); q++) {
+                c.cv.cf[2][jk - 1][q] = c.cs.cf[2][jk - 1][q];
+                double s1 = c.cs.cf[0][jk - 1][q] - c.cv.cf[0][jk - 1][q];
+                double s2 = c.cs.cf[1][jk - 1][q] - c.cv.cf[1][jk - 1][q];
+                c.cv.cf[0][jk - 1][q] = c.cs.cf[0][jk - 1][q] - s1;
+                c.cv.cf[1][jk - 1][q] = c.cs.cf[1][jk - 1][q] - s2;
+            }
+    } else {
+        c.cv = c.cs;
+    }
+    // undeformed distance, set_norm_rhs m_sdis.f90:321-494
+    c.hs.init(c.npot);
+    int ibase = (ihertz >= 1) ? 1 : pb->ibase;
+    if (ibase == 1) {
+        double prm[6] = {0, 0, 0, 0, 0, 0};
+        if (ihertz >= 1) { prm[0] = c.a1; prm[2] = c.b1; }
+        else for (int k = 0; k < 6 && k < pb->nprmudf; k++) prm[k] = pb->prmudf[k];
+        for (int ii = 0; ii < c.npot; ii++) {
+            double x = c.g.x[ii], y = c.g.y[ii];
+            c.hs.vn(ii) = prm[0] * x * x + prm[1] * x * y + prm[2] * y * y + prm[3] * x + prm[4] * y + prm[5];
+        }
+    } else if (ibase == 9) {
+        if (pb->nprmudf != c.npot || !pb->prmudf) { r->ierror = CNTC_err_other; return r->ierror; }
+        for (int ii = 0; ii < c.npot; ii++) c.hs.vn(ii) = pb->prmudf[ii];
+    } else {
+        r->ierror = CNTC_err_other; return r->ierror;
+    }
+    set_tang_rhs(c);
+    // initial estimate
+    c.ps.init(c.npot);
+    c.ss.init(c.npot);
+    c.igs.init(c.mx, c.my);
+    c.mus.assign(c.npot, pb->fstat);
+    if (pb->iestim != 0 && pb->igs_init) {
+        for (int ii = 0; ii < c.npot; ii++) {
+            c.igs.el[ii] = pb->igs_init[ii];
+            c.ps.vn(ii) = pb->pn_init ? pb->pn_init[ii] : 0.0;
+            c.ps.vx(ii) = pb->px_init ? pb->px_init[ii] : 0.0;
+            c.ps.vy(ii) = pb->py_init ? pb->py_init[ii] : 0.0;
+        }
+    }
+    init_curr_data(c, ihertz);
+    // solver context
+    TangCtx &tc = c.tc;
+    tc.mx = c.mx; tc.my = c.my; tc.npot = c.npot; tc.dx = dx; tc.dy = dy; tc.dxdy = c.dxdy;
+    tc.tang = pb->tang; tc.chi = c.chi; tc.dq = c.dq; tc.gausei_eff = pb->gausei;
+    tc.maxgs = pb->maxgs; tc.maxin = pb->maxin; tc.eps = pb->eps;
+    tc.omegah = pb->omegah; tc.omegas = pb->omegas;
+    tc.kdowfb = pb->kdowfb; tc.fdecay = pb->fdecay; tc.betath = pb->betath;
+    tc.d_ifc = pb->d_ifc; tc.d_lin = pb->d_lin; tc.d_cns = pb->d_cns; tc.d_slp = pb->d_slp; tc.pow_s = pb->pow_s;
+    if (tc.d_lin * (tc.d_cns - tc.d_ifc) < 0.0) { tc.d_lin = 0.0; tc.d_cns = tc.d_ifc; }
+    tc.kdown = 3;
+    if (pb->gausei == 5) {
+        if (tc.fdecay >= 0.999) tc.gd_meth = 1;
+        else if (tc.fdecay <= 0.001) { tc.gd_meth = 2; tc.kdown = std::max(1, (int)std::nearbyint(-tc.fdecay)); }
+        else tc.gd_meth = 3;
+    } else {
+        tc.gd_meth = 1;
+    }
+    // panprc, m_scontc.f90:356-553
+    NormCtx nc{c.mx, c.my, c.npot, c.dxdy, pb->norm, c.fntrue};
+    GF3 po1; po1.init(c.npot);
+    gf_copy(AllElm, c.ps, po1, ikALL, c.igs);
+    int itout = 0;
+    double difid = 1.0, dif = 200.0 * difid;
+    c.itnorm = 0; c.ittang = 0;
+    while (dif > difid && itout < c.maxout && c.itnorm >= 0 && c.ittang >= 0) {
+        itout++;
+        int it;
+        if (pb->bound >= 2 && pb->bound <= 4 && ihertz >= 1) {
+            it = 0;
+        } else {
+            int itcg = 0;
+            nc.fntrue = c.fntrue;
+            it = snorm(nc, pb->maxgs, pb->maxin, pb->eps, c.cs, c.ms, c.hs, c.pen, c.igs, c.ps, itcg);
+            c.itcg = itcg;
+            if (it == -2) { c.aborted = true; break; }
+            if (pb->norm == 0) c.fntrue = c.dxdy * gf_sum(AllElm, c.ps, ikZ, c.igs);
+        }
+        if (it >= 0) c.itnorm += it; else c.itnorm = -1;
+        int ncon = 0;
+        for (int ii = 0; ii < c.npot; ii++) {
+            if (c.igs.el[ii] <= Exter) { c.ps.vn(ii) = 0; c.ps.vx(ii) = 0; c.ps.vy(ii) = 0; }
+            else ncon++;
+        }
+        if (pb->tang == 0) {
+            dif = 0.0;
+        } else if (ncon <= 0) {
+            dif = 0.0;
+        } else {
+            int itt = stang(c);
+            if (c.unsupported || c.aborted) break;
+            if (itt >= 0) c.ittang += itt; else c.ittang = -1;
+            gf_axpy(AllElm, -1.0, c.ps, po1, ikALL, c.igs);
+            dif = gf_rms(AllInt, po1, ikALL, c.igs);
+            difid = 5.0 * pb->eps * gf_rms(AllInt, c.ps, ikALL, c.igs);
+            gf_copy(AllElm, c.ps, po1, ikALL, c.igs);
+        }
+    }
+    r->mx = c.mx; r->my = c.my; r->dx = dx; r->dy = dy; r->xc1 = c.xc1; r->yc1 = c.yc1;
+    r->a1 = c.a1; r->b1 = c.b1; r->aa = c.aa; r->bb = c.bb; r->rho = c.rho; r->cp = c.cp; r->aob = c.aob;
+    r->cksi = c.cksi; r->ceta = c.ceta; r->cphi = c.cphi;
+    r->itnorm = c.itnorm; r->ittang = c.ittang; r->itcg = c.itcg; r->itgs = c.itgs; r->solver = c.solver_eff;
+    if (c.unsupported || c.aborted) { r->ierror = CNTC_err_other; return r->ierror; }
+    soutpt(c, r);
+    r->pen = c.pen;
+    for (int ii = 0; ii < c.npot; ii++) {
+        if (r->pn) r->pn[ii] = c.ps.vn(ii);
+        if (r->px) r->px[ii] = c.ps.vx(ii);
+        if (r->py) r->py[ii] = c.ps.vy(ii);
+        if (r->un) r->un[ii] = c.us.vn(ii);
+        if (r->ux) r->ux[ii] = c.us.vx(ii);
+        if (r->uy) r->uy[ii] = c.us.vy(ii);
+        if (r->sx) r->sx[ii] = c.ss.vx(ii) / c.dq;
+        if (r->sy) r->sy[ii] = c.ss.vy(ii) / c.dq;
+        if (r->h) r->h[ii] = c.hs.vn(ii);
+        if (r->igs) r->igs[ii] = c.igs.el[ii];
+    }
+    if (c.itnorm < 0) r->ierror = CNTC_err_norm;
+    else if (c.ittang < 0) r->ierror = CNTC_err_tang;
+    else r->ierror = eldiv_count_atbnd(c.igs);
+    return r->ierror;
+}
+
+} // extern "C"

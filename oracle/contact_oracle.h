@@ -1,0 +1,99 @@
+/*
+ * CPU ORACLE -- test infrastructure only.
+ *
+ * A serial C++ restatement of CONTACT's module-3 rolling-contact solve path
+ * (eve70a/CONTACT, Fortran 90), used as the checker for the GB300 library and
+ * as the timed CPU baseline.  Nothing in the product library links or calls
+ * this code; only tests/, __graft_entry__.smoke() and bench.py's CPU legs do.
+ *
+ * Parity pinning: the oracle reproduces the reference's golden outputs
+ * testbank/test_table_mx11.ref_fx (3220 Hertzian steady-rolling cases, NormCG
+ * + SteadyGS, printed to 6 decimals) and the first series of
+ * examples/tractcurv.ref_out (48x44 grid, 4 significant digits); see
+ * tests/test_oracle_golden.py.  GDsteady (G=5) and TangCG (T=1,2) have no
+ * golden output in the reference: those paths are restated line by line but
+ * their parity is anchored only on the shared algorithms they call.
+ *
+ * One function solves one contact patch, the way cntc_calculate() does for one
+ * (ire,icp) pair in src/contact_addon.f90:3754-3900.
+ */
+#ifndef CONTACT_ORACLE_H
+#define CONTACT_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Inputs of one module-3 case, in CONTACT's internal units (mm, N, rad).
+ * Field meanings follow t_ic / t_solvers / t_kincns in src/m_hierarch_data.f90. */
+typedef struct {
+    /* control digits (t_ic, m_hierarch_data.f90:134-409) */
+    int pvtime, bound, tang, norm, force3, iestim, gausei;
+    /* solver settings (t_solvers, m_hierarch_data.f90:739-801) */
+    int maxgs, maxin, maxnr, maxout;
+    double eps;
+    double omegah, omegas;        /* G=2,3 */
+    int    inislp;  double omgslp;
+    int    kdowfb;                /* G=5 */
+    double fdecay, betath, d_ifc, d_lin, d_cns, d_slp, pow_s;
+    /* material, M=0 elastic (cntc_setmaterialparameters, contact_addon.f90:1287-1473) */
+    double poiss1, poiss2, gg1, gg2;
+    /* Coulomb friction, L=0 (contact_addon.f90:1799-1804) */
+    double fstat, fkin;
+    /* kinematics (t_kincns) */
+    double veloc, chi, dq;
+    double cksi, ceta, cphi;
+    double fn, pen;
+    double fxrel, fyrel;
+    /* potential contact: ipotcn<0 Hertzian (params mx,my,p1,p2,scale),
+     * ipotcn 1..4 explicit grid (params mx,my,p1..p4) */
+    int    ipotcn;
+    double potprm[6];
+    /* undeformed distance (ibase 1: 6 coefficients, 9: per element) */
+    int    ibase;
+    int    nprmudf;
+    const double *prmudf;
+    /* previous solution used when iestim>0 (may be NULL) */
+    const int    *igs_init;
+    const double *pn_init, *px_init, *py_init;
+} orc_problem;
+
+/* Outputs of one case.  Array pointers are caller-allocated with mx*my
+ * entries and may be NULL. */
+typedef struct {
+    int ierror;                    /* as cntc_calculate: 0 ok, <0 error, >0 elements at boundary */
+    int itnorm, ittang, itcg, itgs, solver;
+    int mx, my;
+    double dx, dy, xc1, yc1;
+    double fn, fx, fy, mz, pen, elen, pmax;
+    double cksi, ceta, cphi;
+    double a1, b1, aa, bb, rho, cp, aob;
+    int ncon, nadh, nslip;
+    double *pn, *px, *py;
+    double *un, *ux, *uy;
+    double *sx, *sy;
+    double *h;
+    int    *igs;
+} orc_result;
+
+void orc_default_problem(orc_problem *pb);
+int  orc_calculate(const orc_problem *pb, orc_result *res);
+
+/* building blocks exposed for unit tests */
+int  orc_opt_fft_size(int n);
+/* influence coefficients cf(ix,iy,ik,jk), ix in [-mx,mx-1], iy in [-my,my-1];
+ * out has 9*(2mx)*(2my) doubles, block (ik,jk) at offset ((ik-1)*3+(jk-1))*(4*mx*my) */
+void orc_influence_coefficients(int mx, int my, double dx, double dy, double nu, double ak,
+                                double xshft, double yshft, double *out);
+/* u = A_ik,jk * p on a full mx*my grid via the reference's FFT convolution
+ * (box = full grid); result scaled by 1/ga */
+void orc_convolve(int mx, int my, const double *cf_block, double ga, const double *p, double *u);
+/* same product by direct row sums (gf3_AijPj) over all elements */
+void orc_convolve_direct(int mx, int my, const double *cf_block, double ga, const double *p, double *u);
+/* complete elliptic integrals used by the Hertz solution */
+double orc_eli(double elmodk, double *ellk, double *elle);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
