@@ -1,0 +1,94 @@
+"""Extract golden vectors from the reference's own regression outputs.
+
+Reads, as text, two files of the CONTACT repository and writes compact JSON
+fixtures next to this script:
+
+* testbank/test_table_mx11.ref_fx -> test_table_mx11.json
+  output of src/test_table.f90 (3220 Hertzian steady-rolling cases through the
+  library API: 11x11 grid, NormCG + SteadyGS, eps 1e-6).  Per case the
+  normalised forces Fx/(mu Fn), Fy/(mu Fn), Mz/(mu Fn cp) to 6 decimals and the
+  slip percentage.
+* examples/tractcurv.ref_out -> tractcurv_series1.json
+  first series (cases 1-30) of examples/tractcurv.inp (Hertz a1/aob input, 48x44 grid,
+  Coulomb friction, SteadyGS): forces, energy, approach, pmax to 4 digits,
+  element counts, iteration counts and the element-division picture.
+
+Usage: python tests/golden/make_golden.py [reference_root]
+"""
+import json
+import os
+import re
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def parse_test_table(path):
+    lines = open(path).read().splitlines()
+    hertz = []
+    for ln in lines[:5]:
+        m = re.search(r"a/b=\s*([\d.]+): rho=\s*([\d.Ee+-]+)\s*, cp=\s*([\d.Ee+-]+)", ln)
+        hertz.append({"aob": float(m.group(1)), "rho": float(m.group(2)), "cp": float(m.group(3))})
+    cases = []
+    for ln in lines[5:]:
+        vals = [t.split("=")[1].strip() for t in ln.split(",")]
+        cases.append([float(vals[0]), float(vals[1]), float(vals[2]), float(vals[3])])
+    return {"source": "testbank/test_table_mx11.ref_fx", "hertz": hertz, "cases": cases}
+
+
+def parse_tractcurv(path, inp_path, ncase_max=30):
+    # exact creepages of the first series from the input file
+    cksi = [float(l.split()[1]) for l in open(inp_path) if "FN, CKSI, CETA, CPHI" in l][:ncase_max]
+    text = open(path).read()
+    blocks = re.split(r"\n Case\s+(\d+)\n", text)
+    out = []
+    for k in range(1, len(blocks), 2):
+        icase = int(blocks[k])
+        body = blocks[k + 1]
+        if icase > ncase_max:
+            break
+        rec = {"case": icase}
+        m = re.search(r"ItCG=\s*(\d+)", body)
+        rec["itcg"] = int(m.group(1)) if m else None
+        m = re.search(r"ItGS=\s*(\d+)", body)
+        rec["itgs"] = int(m.group(1)) if m else None
+        ln = body.splitlines()
+        for i, s in enumerate(ln):
+            if s.strip().startswith("FN") and "ELAST.EN." in s:
+                v = ln[i + 1].split()
+                rec.update(fn=float(v[0]), fx=float(v[1]), fy=float(v[2]), mz=float(v[3]),
+                           elen=float(v[4]), frpow=float(v[5]))
+            if s.strip().startswith("FN/G"):
+                v = ln[i + 1].split()
+                rec.update(fn_g=float(v[0]), fx_rel=float(v[1]), fy_rel=float(v[2]),
+                           approach=float(v[3]), pmax=float(v[4]))
+            if s.strip().startswith("NPOT") and "NCON" in s:
+                v = ln[i + 1].split()
+                rec.update(npot=int(v[0]), ncon=int(v[1]), nadh=int(v[2]), nslip=int(v[3]),
+                           inorm=int(v[4]), itang=int(v[5]))
+            if "FORM OF THE CONTACT" in s:
+                rows = []
+                j = i + 1
+                while re.match(r"^\s+\d+\s+\S+$", ln[j]):
+                    rows.append(ln[j].split()[1])
+                    j += 1
+                rec["picture"] = rows[::-1]     # row iy=1 first
+        rec["cksi"] = cksi[icase - 1]
+        out.append(rec)
+    return {"source": "examples/tractcurv.ref_out", "series": 1, "cases": out}
+
+
+def main():
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    tt = parse_test_table(os.path.join(root, "testbank", "test_table_mx11.ref_fx"))
+    with open(os.path.join(HERE, "test_table_mx11.json"), "w") as f:
+        json.dump(tt, f, separators=(",", ":"))
+    tc = parse_tractcurv(os.path.join(root, "examples", "tractcurv.ref_out"),
+                         os.path.join(root, "examples", "tractcurv.inp"))
+    with open(os.path.join(HERE, "tractcurv_series1.json"), "w") as f:
+        json.dump(tc, f, indent=0)
+    print("test_table cases:", len(tt["cases"]), " tractcurv cases:", len(tc["cases"]))
+
+
+if __name__ == "__main__":
+    main()
