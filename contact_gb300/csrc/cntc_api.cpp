@@ -1,0 +1,879 @@
+// C-ABI of the GB300 contact library: CONTACT's cntc_* interface for module 3
+// (src/contact_addon.f90, prototypes in matlab_intfc/contact_addon.h) on top of the
+// device engine.  All arguments are passed by pointer as in the Fortran bind(c)
+// interface; inputs are in the caller's unit convention (CNTC_if_units) and are
+// converted to CONTACT's internal units (mm, N, rad).
+//
+// Per-problem state lives on the host: one Problem per (ire, icp) holds the settings
+// staged by the setters and the results of the last cntc_calculate, read back by the
+// getters.  cntc_calculate prepares a PatchDesc (Hertz solution, grid, solver flags),
+// runs the engine on the GPU and copies the results back.  cntc_calculate_batch does the
+// same for many problems with one pass of the engine.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "../../include/contact_addon.h"
+#include "engine_api.h"
+#include "hertz.hpp"
+
+using namespace cgb;
+
+namespace {
+
+// codes of src/caddon_flags.inc
+constexpr int CNTC_if_units = 1933, CNTC_un_cntc = 1934, CNTC_un_spck = 1935, CNTC_un_si = 1936, CNTC_un_imper = 1937;
+constexpr int CNTC_ic_config = 1967, CNTC_ic_pvtime = 1970, CNTC_ic_bound = 1971, CNTC_ic_tang = 1972,
+              CNTC_ic_norm = 1973, CNTC_ic_force = 1974, CNTC_ic_frclaw = 1976, CNTC_ic_discns = 1977,
+              CNTC_ic_inflcf = 1978, CNTC_ic_mater = 1979, CNTC_ic_exrhs = 1980, CNTC_ic_xflow = 1981,
+              CNTC_ic_heat = 1982, CNTC_ic_iestim = 1983, CNTC_ic_output = 1984, CNTC_ic_flow = 1985,
+              CNTC_ic_return = 1986, CNTC_ic_matfil = 1987, CNTC_ic_sens = 1988;
+constexpr int CNTC_if_idebug = 2000, CNTC_if_wrtinp = 2002, CNTC_if_openmp = 2003, CNTC_if_timers = 2004,
+              CNTC_if_ncase = 2005;
+constexpr int CNTC_fld_h = 1, CNTC_fld_mu = 2, CNTC_fld_px = 3, CNTC_fld_py = 4, CNTC_fld_pn = 5, CNTC_fld_ux = 7,
+              CNTC_fld_uy = 8, CNTC_fld_un = 9, CNTC_fld_taucrt = 11, CNTC_fld_uplsx = 12, CNTC_fld_uplsy = 13,
+              CNTC_fld_sx = 15, CNTC_fld_sy = 16, CNTC_fld_temp1 = 20, CNTC_fld_temp2 = 21, CNTC_fld_wx = 22,
+              CNTC_fld_wy = 23;
+constexpr int CNTC_err_norm = -27, CNTC_err_tang = -28, CNTC_err_icp = -31, CNTC_err_other = -99;
+constexpr int kMaxReid = 100, kMaxCpid = 9;
+constexpr int kCaddonVersion = 100 * 25 + 10 * 2 + 0;     // version 25.2.0 of the interface
+
+struct Problem {
+    int ire = 0, icp = 0, ncase = 0;
+    // unit scaling (cntc_select_units, src/m_global_data.f90:463-526)
+    int units = CNTC_un_cntc;
+    double s_len = 1, s_area = 1, s_forc = 1, s_veloc = 1, s_angle = 1, s_body = 1;
+    // control digits (ic_init + cntc_activate_gd defaults)
+    int pvtime = 2, bound = 0, tang = 3, norm = 0, force3 = 0, iestim = 0, gausei_eff = 0;
+    int mater = 0, gencr = 2, rztang = 0, frclaw = 0, varfrc = 0, sens = 1, heat = 0, stress = 0;
+    int output = 0, flow = 1, matfil = 0, ret = 1;
+    // solver settings (solv_init, m_hierarch_data.f90:1722-1755)
+    int maxgs = 999, maxin = 20, maxnr = 25, maxout = 1, mxsens = 30, inislp = 0;
+    double eps = 1e-5, epsens = 1e-4, omegah = 0.9, omegas = 1.0, omgslp = 0.5;
+    int gd_meth = 1, kdown = 3, kdowfb = 1;
+    double fdecay = 0.9, betath = 0.1, d_ifc = 1.0, d_lin = 1.0, d_cns = 1.0, d_slp = 1.0, pow_s = 0.9;
+    // material (mater_init)
+    double poiss[2] = {0.28, 0.28}, gg[2] = {1.0, 1.0};
+    // friction (fric_init): Coulomb
+    double fstat = 0.3, fkin = 0.3, muscal = 0.3;
+    // kinematics (kincns_init)
+    double veloc = 1e3, chi = 0.0, dq = 2.0, dt = 1.0, cksi = 0, ceta = 0, cphi = 0, fn = 0, pen = 0, fxrel = 0,
+           fyrel = 0;
+    // potential contact (potcon_init) and Hertz data
+    int ipotcn = 1, mx = 1, my = 1;
+    double xl = -1, yl = -1, xc1 = 0, yc1 = 0, dx = 2, dy = 2, xh = 1, yh = 1, xcm = 0, ycm = 0;
+    double hz_a1 = 0, hz_b1 = 0, hz_aa = 0, hz_bb = 0, hz_aob = 1, hz_scale = 1, hz_rho = 0, hz_cp = 0;
+    // undeformed distance
+    int ibase = 1;
+    std::vector<double> prmudf = std::vector<double>(6, 0.0);
+    // engine settings (library extension, CNTC_if_mixedprec)
+    int mixed = 0;
+    double eps32 = 1e-5;
+    // results of the last calculation
+    bool have = false;
+    int r_mx = 0, r_my = 0, ierror = 0, itnorm = 0, ittang = 0, itcg = 0, itgs = 0, solver = 0;
+    double r_dx = 0, r_dy = 0, r_xc1 = 0, r_yc1 = 0, r_dq = 1;
+    double f_n = 0, f_x = 0, f_y = 0, m_z = 0, r_pen = 0, elen = 0, pmax = 0;
+    int ncon = 0, nadh = 0, nslip = 0;
+    std::vector<double> fields;   // W_H .. W_SN columns, npot each
+    std::vector<int> igs;
+    std::vector<double> stats;           // engine statistics: convolution counts, status, phase cycles
+    double tcpu = 0, twall = 0;
+    // device resources
+    char *d_io = nullptr, *d_work = nullptr;
+    size_t cap_io = 0, cap_work = 0;
+    PatchDesc *d_desc = nullptr;
+    int *d_list = nullptr;
+    char key[128] = {0};          // geometry key of the cached influence coefficients
+    bool ic_valid = false;
+    std::mutex busy;
+};
+
+std::mutex g_mu;
+std::map<long, std::unique_ptr<Problem>> g_problems;
+int g_initialized = -3;
+int g_debug = 0;
+
+long pkey(int ire, int icp) { return (long)ire * 100 + icp; }
+
+Problem *lookup(int ire, int icp, bool create) {
+    if (ire <= 0 || ire > 10000 || icp <= 0 || icp > kMaxCpid) return nullptr;
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_problems.find(pkey(ire, icp));
+    if (it != g_problems.end()) return it->second.get();
+    if (!create) return nullptr;
+    auto p = std::make_unique<Problem>();
+    p->ire = ire; p->icp = icp;
+    Problem *r = p.get();
+    g_problems[pkey(ire, icp)] = std::move(p);
+    return r;
+}
+
+void log_msg(const char *msg) {
+    if (g_debug >= 1) std::fprintf(stderr, "contact_gb300: %s\n", msg);
+}
+
+void select_units(Problem &p, int units) {
+    if (units == CNTC_un_spck) { p.s_len = 1e3; p.s_area = 1e6; p.s_forc = 1; p.s_veloc = 1e3; p.s_angle = 1; p.s_body = -1; }
+    else if (units == CNTC_un_si) { p.s_len = 1e3; p.s_area = 1e6; p.s_forc = 1; p.s_veloc = 1e3; p.s_angle = 1; p.s_body = 1; }
+    else if (units == CNTC_un_cntc || units == CNTC_un_imper) { p.s_len = 1; p.s_area = 1; p.s_forc = 1; p.s_veloc = 1; p.s_angle = 1; p.s_body = 1; }
+    else return;
+    p.units = units;
+}
+
+// ------------------------------------------------------------------------------------------
+// preparation of one patch: Hertz solution, potential contact, flags -> PatchDesc.
+// Returns 0 or an error code (cntc ierror convention).
+// ------------------------------------------------------------------------------------------
+struct Prep {
+    PatchDesc d;
+    bool ic_needed;
+    bool upload;          // io block carries inputs (element-wise h or warm start)
+};
+
+int prepare(Problem &p, Prep &out) {
+    std::memset(&out.d, 0, sizeof(PatchDesc));
+    PatchDesc &d = out.d;
+    // combined material constants, combin_mater (m_hierarch_data.f90:1543-1553)
+    const double ga = 2.0 / (1.0 / p.gg[0] + 1.0 / p.gg[1]);
+    const double nu = ga * (p.poiss[0] / p.gg[0] + p.poiss[1] / p.gg[1]) / 2.0;
+    const double ak = (ga / 4.0) * ((1.0 - 2.0 * p.poiss[0]) / p.gg[0] - (1.0 - 2.0 * p.poiss[1]) / p.gg[1]);
+    if (std::fabs(ak) >= 1e-6) { log_msg("non-identical materials (K != 0) are not supported"); return CNTC_err_other; }
+    if (p.mater != 0 || p.frclaw != 0 || p.force3 != 0 || p.rztang != 0 || p.varfrc != 0) {
+        log_msg("only M=0, L=0, F=0, E=0 are supported");
+        return CNTC_err_other;
+    }
+    if (!(p.bound == 0 || p.bound == 2 || p.bound == 3)) { log_msg("B digit not supported"); return CNTC_err_other; }
+    if (p.tang != 0 && p.tang != 3 && p.pvtime != 2) {
+        log_msg("transient sequences (P != 2 with T = 1, 2) are not supported");
+        return CNTC_err_other;
+    }
+    // potential contact and Hertz (hzsol m_hertz.f90:29-93, potcon_hertz, potcon_fill)
+    int ihertz = 0;
+    double xl, yl, dx, dy;
+    int mx = p.mx, my = p.my;
+    p.hz_rho = p.hz_cp = 0.0;
+    double fn = p.fn, pen = p.pen;
+    if (p.ipotcn <= -1 && p.ipotcn >= -3) {
+        hz::Result h;
+        h.a1 = p.hz_a1; h.b1 = p.hz_b1; h.aa = p.hz_aa; h.bb = p.hz_bb; h.fn = fn; h.pen = pen;
+        const double e_star = ga / (1.0 - nu);
+        if (p.ipotcn == -2) hz::calc_aob(e_star, p.norm, p.hz_aob, h);
+        else hz::calc3d(e_star, p.ipotcn, p.norm, h);
+        p.hz_a1 = h.a1; p.hz_b1 = h.b1; p.hz_aa = h.aa; p.hz_bb = h.bb; p.hz_rho = h.rho; p.hz_cp = h.cp;
+        if (p.ipotcn != -2) p.hz_aob = (h.aa <= 1e-20 && h.bb <= 1e-20) ? 1.0 : h.aa / h.bb;
+        fn = h.fn; pen = h.pen;
+        xl = -p.hz_scale * std::max(1e-9, h.aa);
+        yl = -p.hz_scale * std::max(1e-9, h.bb);
+        dx = (-2.0 * xl) / mx; dy = (-2.0 * yl) / my;
+        ihertz = -p.ipotcn;
+    } else if (p.ipotcn >= 1 && p.ipotcn <= 4) {
+        xl = p.xl; yl = p.yl; dx = p.dx; dy = p.dy;
+    } else {
+        log_msg("potential contact specification not supported");
+        return CNTC_err_other;
+    }
+    // check_roll_stepsize (m_sdis.f90:125-206)
+    double chi = p.chi, dq = p.dq, veloc = p.veloc;
+    const bool is_roll = p.tang == 2 || p.tang == 3;
+    if (p.tang == 3 && p.gausei_eff != 2) {
+        if (std::fabs(chi) > 0.01 && std::fabs(chi - M_PI) > 0.01) chi = 0.0;
+        dq = dx;
+    }
+    if (!is_roll) { chi = 0.0; dq = 1.0; veloc = 1.0; }
+    if (is_roll && std::fabs(chi) > 0.01) { log_msg("rolling direction chi != 0 is not supported"); return CNTC_err_other; }
+    p.dt = dq / std::max(1e-10, veloc);
+    if (mx < 2 || my < 2) { log_msg("grids of width 1 are not supported"); return CNTC_err_other; }
+    const int fx = cgb::opt_fft_size(mx), fy = cgb::opt_fft_size(my);
+    if (solve_smem_bytes(fx, fy) > 227 * 1024) { log_msg("patch too large for the single-block engine"); return CNTC_err_other; }
+    d.mx = mx; d.my = my; d.npot = mx * my; d.fx = fx; d.fy = fy;
+    d.dx = dx; d.dy = dy; d.dxdy = dx * dy; d.xc1 = xl + 0.5 * dx; d.yc1 = yl + 0.5 * dy;
+    d.tang = p.tang; d.norm = p.norm; d.bound = p.bound; d.iestim = p.iestim; d.force3 = p.force3;
+    d.gausei = p.gausei_eff;
+    d.maxgs = p.maxgs; d.maxin = p.maxin;
+    int maxout = p.maxout;
+    if (maxout >= 2 && std::fabs(ak) < 1e-4) maxout = 1;
+    d.maxout = maxout;
+    d.eps = p.eps;
+    d.omegah = p.omegah; d.omegas = p.omegas;
+    d.gd_meth = p.gd_meth; d.kdown = p.kdown; d.kdowfb = p.kdowfb;
+    d.fdecay = p.fdecay; d.betath = p.betath; d.d_ifc = p.d_ifc; d.d_lin = p.d_lin; d.d_cns = p.d_cns;
+    d.d_slp = p.d_slp; d.pow_s = p.pow_s;
+    d.ga = ga; d.nu = nu; d.fstat = p.fstat;
+    d.chi = chi; d.dq = dq; d.cksi = p.cksi; d.ceta = p.ceta; d.cphi = p.cphi;
+    d.fntrue = fn; d.pen = pen;
+    d.ihertz = ihertz; d.aa = p.hz_aa; d.bb = p.hz_bb;
+    if (ihertz >= 1) {
+        d.ibase = 1;
+        for (int k = 0; k < 6; k++) d.prm[k] = 0.0;
+        d.prm[0] = p.hz_a1; d.prm[2] = p.hz_b1;
+    } else {
+        d.ibase = p.ibase;
+        if (p.ibase == 1) for (int k = 0; k < 6; k++) d.prm[k] = p.prmudf[k];
+        else if (p.ibase != 9) { log_msg("undeformed distance type not supported"); return CNTC_err_other; }
+        if (p.ibase == 9 && (int)p.prmudf.size() < d.npot) return CNTC_err_other;
+    }
+    d.precision = p.mixed;
+    d.eps32 = std::max(p.eps, p.eps32);
+    // geometry key for reuse of influence coefficients and spectra
+    char key[128];
+    std::snprintf(key, sizeof(key), "%d %d %.17g %.17g %.17g %.17g", mx, my, dx, dy, ga, nu);
+    out.ic_needed = !(p.ic_valid && std::strcmp(key, p.key) == 0);
+    std::strcpy(p.key, key);
+    // warm start needs a previous solution on the same grid
+    out.upload = (d.ibase == 9);
+    if (p.iestim != 0) {
+        if (!(p.have && p.r_mx == mx && p.r_my == my)) d.iestim = 0;
+        else out.upload = true;
+    }
+    p.r_mx = mx; p.r_my = my; p.r_dx = dx; p.r_dy = dy; p.r_xc1 = d.xc1; p.r_yc1 = d.yc1; p.r_dq = dq;
+    return 0;
+}
+
+// fill the io staging block of one patch with its inputs
+void stage_inputs(Problem &p, const PatchDesc &d, double *io) {
+    const int n = d.npot;
+    if (d.ibase == 9) for (int i = 0; i < n; i++) io[(size_t)W_H * n + i] = p.prmudf[i] * 1.0;
+    if (d.iestim != 0 && p.have) {
+        int *igs = (int *)(io + (size_t)kIoCols * n + O_NSCAL);
+        double *px = io + (size_t)W_PX * n, *py = io + (size_t)W_PY * n, *pn = io + (size_t)W_PN * n;
+        for (int i = 0; i < n; i++) {
+            igs[i] = p.igs[i];
+            px[i] = p.fields[(size_t)W_PX * n + i];
+            py[i] = p.fields[(size_t)W_PY * n + i];
+            pn[i] = p.fields[(size_t)W_PN * n + i];
+            // I = 1: regularise tractions (init_curr_data, m_sdis.f90:716-729)
+            if (p.iestim == 1) {
+                if (igs[i] <= 0) { pn[i] = px[i] = py[i] = 0.0; }
+                else if (igs[i] == 2) {
+                    const double pabs = std::max(1e-10, std::sqrt(px[i] * px[i] + py[i] * py[i]));
+                    px[i] = p.fstat * pn[i] * px[i] / pabs;
+                    py[i] = p.fstat * pn[i] * py[i] / pabs;
+                }
+            }
+            if (p.iestim == 2) { if (igs[i] >= 1) igs[i] = 1; px[i] = py[i] = 0.0; }
+        }
+    }
+}
+
+// copy the results of one patch out of its io block
+void collect(Problem &p, const PatchDesc &d, const double *io) {
+    const int n = d.npot;
+    const double *o = io + (size_t)kIoCols * n;
+    p.fields.assign(io, io + (size_t)kIoCols * n);
+    const int *igs = (const int *)(o + O_NSCAL);
+    p.igs.assign(igs, igs + n);
+    p.f_n = o[O_FN]; p.f_x = o[O_FX]; p.f_y = o[O_FY]; p.m_z = o[O_MZ];
+    p.r_pen = o[O_PEN]; p.elen = o[O_ELEN]; p.pmax = o[O_PMAX];
+    p.ierror = (int)o[O_IERR]; p.itnorm = (int)o[O_ITNORM]; p.ittang = (int)o[O_ITTANG];
+    p.itcg = (int)o[O_ITCG]; p.itgs = (int)o[O_ITGS]; p.solver = (int)o[O_SOLVER];
+    p.ncon = (int)o[O_NCON]; p.nadh = (int)o[O_NADH]; p.nslip = (int)o[O_NSLIP];
+    p.stats.assign(o + O_NCONV32, o + O_NSCAL);
+    p.have = true;
+    // kinematic outputs follow the reference: fn from the solution when N = 0
+    if (p.norm == 0) p.fn = p.f_n;
+    p.pen = p.r_pen;
+}
+
+// ------------------------------------------------------------------------------------------
+// batched execution of prepared problems (one pass of the engine)
+// ------------------------------------------------------------------------------------------
+struct Batch {
+    std::vector<Problem *> probs;
+    std::vector<Prep> preps;
+    std::vector<int> status;
+};
+
+struct Arena {
+    char *d_io = nullptr, *d_work = nullptr;
+    size_t cap_io = 0, cap_work = 0;
+    PatchDesc *d_desc = nullptr;
+    size_t cap_desc = 0;
+    int *d_list = nullptr;
+    size_t cap_list = 0;
+    double *h_io = nullptr;      // pinned staging
+    size_t cap_hio = 0;
+};
+
+cudaError_t grow(void **ptr, size_t &cap, size_t need, bool pinned) {
+    if (need <= cap) return cudaSuccess;
+    if (*ptr) { if (pinned) cudaFreeHost(*ptr); else cudaFree(*ptr); *ptr = nullptr; cap = 0; }
+    size_t c = need + need / 4 + 4096;
+    cudaError_t e = pinned ? cudaMallocHost(ptr, c) : cudaMalloc(ptr, c);
+    if (e == cudaSuccess) cap = c;
+    return e;
+}
+
+thread_local Arena t_arena;
+
+// runs the engine for all prepared entries with status 0; results go to the problems
+int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
+    std::vector<int> live;
+    for (size_t i = 0; i < b.probs.size(); i++) if (b.status[i] == 0) live.push_back((int)i);
+    const int n = (int)live.size();
+    if (n == 0) return 0;
+    std::vector<size_t> off_io(n), off_work(n);
+    size_t tot_io = 0, tot_work = 0;
+    bool any_upload = false;
+    for (int k = 0; k < n; k++) {
+        const PatchDesc &d = b.preps[live[k]].d;
+        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy);
+        off_io[k] = tot_io; tot_io += s.io;
+        off_work[k] = tot_work; tot_work += s.work;
+        any_upload |= b.preps[live[k]].upload;
+    }
+    cudaError_t e;
+    if ((e = grow((void **)&A.d_io, A.cap_io, tot_io, false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_work, A.cap_work, tot_work, false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_desc, A.cap_desc, n * sizeof(PatchDesc), false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_list, A.cap_list, 2 * n * sizeof(int) + 64, false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.h_io, A.cap_hio, tot_io, true)) != cudaSuccess) return (int)e;
+    std::vector<PatchDesc> hd(n);
+    std::vector<unsigned char> need_ic(n, 1);
+    for (int k = 0; k < n; k++) {
+        hd[k] = b.preps[live[k]].d;
+        carve_patch(hd[k], A.d_io + off_io[k], A.d_work + off_work[k]);
+        (void)reuse_ic_allowed;
+        if (b.preps[live[k]].upload)
+            stage_inputs(*b.probs[live[k]], hd[k], (double *)((char *)A.h_io + off_io[k]));
+    }
+    cudaStream_t st = cudaStreamPerThread;
+    if (any_upload) {
+        if ((e = cudaMemcpyAsync(A.d_io, A.h_io, tot_io, cudaMemcpyHostToDevice, st)) != cudaSuccess) return (int)e;
+    }
+    if ((e = cudaMemcpyAsync(A.d_desc, hd.data(), n * sizeof(PatchDesc), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return (int)e;
+    int rc = engine_run(hd.data(), A.d_desc, n, need_ic.data(), A.d_list, st);
+    if (rc != 0) return rc;
+    if ((e = cudaMemcpyAsync(A.h_io, A.d_io, tot_io, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return (int)e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return (int)e;
+    for (int k = 0; k < n; k++) collect(*b.probs[live[k]], hd[k], (const double *)((const char *)A.h_io + off_io[k]));
+    return 0;
+}
+
+int calculate_many(int n, const int *ire, const int *icp, int *ierror) {
+    Batch b;
+    b.probs.resize(n); b.preps.resize(n); b.status.assign(n, 0);
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<std::unique_lock<std::mutex>> locks;
+    for (int i = 0; i < n; i++) {
+        Problem *p = lookup(ire[i], icp[i], true);
+        b.probs[i] = p;
+        if (!p) { b.status[i] = CNTC_err_icp; continue; }
+        std::unique_lock<std::mutex> lk(p->busy, std::try_to_lock);
+        if (!lk.owns_lock()) { b.status[i] = CNTC_err_other; continue; }   // same problem in use
+        locks.push_back(std::move(lk));
+        p->ncase++;
+        b.status[i] = prepare(*p, b.preps[i]);
+        if (b.status[i] != 0) p->have = false;
+    }
+    int rc = run_batch(b, t_arena, true);
+    auto t1 = std::chrono::steady_clock::now();
+    const double dt = std::chrono::duration<double>(t1 - t0).count();
+    for (int i = 0; i < n; i++) {
+        if (!b.probs[i]) { ierror[i] = b.status[i]; continue; }
+        if (b.status[i] != 0) { ierror[i] = b.status[i]; continue; }
+        ierror[i] = (rc != 0) ? CNTC_err_other : b.probs[i]->ierror;
+        b.probs[i]->twall += dt / n;
+        b.probs[i]->tcpu += dt / n;
+    }
+    if (rc != 0 && g_debug >= 1) std::fprintf(stderr, "contact_gb300: engine error %d (%s)\n", rc, cudaGetErrorString((cudaError_t)rc));
+    return rc;
+}
+
+double *field_ptr(Problem &p, int col) {
+    const int n = p.r_mx * p.r_my;
+    if (!p.have || (int)p.fields.size() < kIoCols * n) return nullptr;
+    return p.fields.data() + (size_t)col * n;
+}
+
+} // namespace
+
+// ==========================================================================================
+// exported functions
+// ==========================================================================================
+extern "C" {
+
+void cntc_initializefirst(int *ifcver, int *ierror, int *ioutput, const char *c_wrkdir, const char *c_outdir,
+                          const char *c_expnam, int *len_wrkdir, int *len_outdir, int *len_expnam) {
+    (void)ioutput; (void)c_wrkdir; (void)c_outdir; (void)c_expnam; (void)len_wrkdir; (void)len_outdir; (void)len_expnam;
+    g_initialized = 1;
+    if (ifcver) *ifcver = kCaddonVersion;
+    if (ierror) *ierror = 0;
+}
+
+void cntc_initializefirst_new(int *ifcver, int *ierror, int *ioutput, const char *c_wrkdir, const char *c_outdir,
+                              const char *c_expnam, int *len_wrkdir, int *len_outdir, int *len_expnam) {
+    cntc_initializefirst(ifcver, ierror, ioutput, c_wrkdir, c_outdir, c_expnam, len_wrkdir, len_outdir, len_expnam);
+}
+
+void cntc_initialize(int *ire, int *imodul, int *ifcver, int *ierror, const char *c_outdir, int *len_outdir) {
+    (void)c_outdir; (void)len_outdir;
+    if (g_initialized <= 0) g_initialized = 1;
+    if (ifcver) *ifcver = kCaddonVersion;
+    if (!ire || *ire <= 0 || *ire > 10000 || !imodul || *imodul != 3) { if (ierror) *ierror = CNTC_err_other; return; }
+    if (ierror) *ierror = 0;
+}
+
+void cntc_setglobalflags(int *lenflg, int *params, int *values) {
+    for (int i = 0; i < *lenflg; i++) {
+        if (params[i] == CNTC_if_idebug) g_debug = values[i];
+    }
+}
+
+void cntc_setflags(int *ire, int *icp, int *lenflg, int *params, int *values) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    for (int i = 0; i < *lenflg; i++) {
+        const int c = params[i], v = values[i];
+        switch (c) {
+            case 0: break;
+            case CNTC_if_units: select_units(*p, v); break;
+            case CNTC_ic_pvtime: p->pvtime = std::max(0, std::min(3, v)); break;
+            case CNTC_ic_bound: p->bound = std::max(0, std::min(6, v)); break;
+            case CNTC_ic_tang: p->tang = std::max(0, std::min(3, v)); break;
+            case CNTC_ic_norm: p->norm = std::max(0, std::min(1, v)); break;
+            case CNTC_ic_force: p->force3 = std::max(0, std::min(2, v)); break;
+            case CNTC_ic_sens: p->sens = std::max(0, std::min(3, v)); break;
+            case CNTC_ic_inflcf: if (v >= 0 && v <= 4) p->gencr = v; break;
+            case CNTC_ic_exrhs: p->rztang = std::max(0, std::min(3, v)); break;
+            case CNTC_ic_iestim: p->iestim = std::max(0, std::min(3, v)); break;
+            case CNTC_ic_matfil: p->matfil = (v < 0 || v > 2) ? 0 : v; break;
+            case CNTC_ic_output: p->output = std::max(0, std::min(5, v)); break;
+            case CNTC_ic_flow: p->flow = std::max(0, std::min(9, v)); break;
+            case CNTC_ic_return: p->ret = std::max(0, std::min(3, v)); break;
+            case CNTC_if_ncase: p->ncase = std::max(0, v - 1); break;
+            case CNTC_if_mixedprec: p->mixed = (v != 0) ? 1 : 0; break;
+            default: break;   // output, debugging and module-1 flags have no effect here
+        }
+    }
+}
+
+void cntc_setsolverflags(int *ire, int *icp, int *gdigit, int *nints, int *iparam, int *nreals, double *rparam) {
+    static const int nints_loc[7] = {4, 0, 5, 5, 5, 5, 1};
+    static const int nreals_loc[7] = {1, 0, 4, 4, 2, 8, 1};
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    const int g = *gdigit;
+    if (g < 0 || g > 6) return;
+    if (*nints != nints_loc[g] || *nreals != nreals_loc[g]) return;
+    if (g != 1 && g != 6) {
+        p->gausei_eff = g;
+        p->eps = std::max(1e-20, rparam[0]);
+        p->maxgs = std::max(1, iparam[0]);
+        p->maxin = std::max(1, iparam[1]);
+        p->maxnr = std::max(1, iparam[2]);
+        p->maxout = std::max(1, iparam[3]);
+        if (g == 2 || g == 3) {
+            p->inislp = iparam[4];
+            p->omegah = std::max(1e-20, rparam[1]);
+            p->omegas = std::max(1e-20, rparam[2]);
+            p->omgslp = std::max(1e-20, rparam[3]);
+        }
+        if (g == 4) { p->inislp = iparam[4]; p->omgslp = std::max(1e-20, rparam[1]); }
+        if (g == 5) {
+            p->fdecay = rparam[1];
+            p->betath = rparam[2];
+            p->kdowfb = iparam[4];
+            p->d_ifc = std::max(0.01, rparam[3]);
+            p->d_lin = rparam[4];
+            p->d_cns = std::max(0.01, rparam[5]);
+            p->d_slp = std::max(0.01, rparam[6]);
+            p->pow_s = std::max(0.01, std::min(10.0, rparam[7]));
+            if (p->d_lin * (p->d_cns - p->d_ifc) < 0.0) { p->d_lin = 0.0; p->d_cns = p->d_ifc; }
+            if (p->fdecay >= 0.999) p->gd_meth = 1;
+            else if (p->fdecay <= 0.001) { p->gd_meth = 2; p->kdown = std::max(1, (int)std::lround(-p->fdecay)); }
+            else p->gd_meth = 3;
+        }
+    } else if (g == 6) {
+        p->mxsens = std::max(1, iparam[0]);
+        p->epsens = std::max(1e-20, rparam[0]);
+    }
+}
+
+void cntc_setmaterialparameters(int *ire, int *icp, int *imeth, int *nparam, double *rparam) {
+    static const int nparam_loc[13] = {4, 8, 8, 7, 8, 7, 4, 4, 0, 0, 0, 0, 4};
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    const int m = *imeth;
+    const bool set_m = m >= 0 && m <= 7, set_m2 = m >= 10 && m <= 12;
+    if (!set_m && !set_m2) return;
+    if ((nparam_loc[m] == 0 && *nparam >= 2) || (nparam_loc[m] != 0 && *nparam != nparam_loc[m])) return;
+    if (set_m2) return;     // damping (M2 digit) does not change the solve
+    p->mater = m;
+    p->poiss[0] = rparam[0]; p->poiss[1] = rparam[1];
+    p->gg[0] = rparam[2] * p->s_forc / p->s_area;
+    p->gg[1] = rparam[3] * p->s_forc / p->s_area;
+}
+
+void cntc_settemperaturedata(int *ire, int *icp, int *imeth, int *nparam, double *rparam) {
+    (void)ire; (void)icp; (void)imeth; (void)nparam; (void)rparam;
+}
+
+void cntc_settimestep(int *ire, int *icp, double *dt) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (p) p->dt = *dt;
+}
+
+void cntc_setreferencevelocity(int *ire, int *icp, double *veloc) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (p) p->veloc = std::max(1e-9, std::fabs(*veloc) * p->s_veloc);
+}
+
+void cntc_setrollingstepsize(int *ire, int *icp, double *chi, double *dq) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    p->chi = *chi * p->s_angle;
+    p->dq = *dq * p->s_len;
+}
+
+void cntc_setfrictionmethod(int *ire, int *icp, int *imeth, int *nparam, double *params) {
+    static const int nparam_loc[7] = {2, 0, 7, 7, 7, 3, 6};
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    const int vdigit = *imeth / 10, ldigit = *imeth - 10 * vdigit;
+    if (vdigit < 0 || vdigit > 2 || ldigit < 0 || ldigit > 6) return;
+    if (ldigit == 1) return;
+    if (vdigit != 0) { p->varfrc = vdigit; return; }
+    if (*nparam != nparam_loc[ldigit]) return;
+    p->varfrc = 0;
+    p->frclaw = (ldigit == 5) ? 4 : ldigit;
+    if (ldigit == 0) {
+        p->fkin = std::max(1e-6, std::min(params[0], params[1]));
+        p->fstat = p->fkin;
+        p->muscal = p->fstat;
+    }
+}
+
+void cntc_sethertzcontact(int *ire, int *icp, int *ipotcn, int *nparam, double *params) {
+    static const int nparam_loc[6] = {6, 5, 5, 5, 5, 5};
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    const int ip = *ipotcn;
+    if (ip < -6 || ip > -1 || *nparam != nparam_loc[ip + 6]) return;
+    p->ipotcn = ip;
+    p->mx = std::max(1, (int)std::lround(params[0]));
+    p->my = std::max(1, (int)std::lround(params[1]));
+    if (ip == -3) {
+        p->hz_aa = std::max(1e-6, params[2]) * p->s_len;
+        p->hz_bb = std::max(1e-6, params[3]) * p->s_len;
+        p->hz_scale = std::max(1e-6, params[4]);
+    } else if (ip == -2) {
+        p->hz_a1 = std::max(1e-12, params[2]) / p->s_len;
+        p->hz_aob = std::max(1e-6, params[3]);
+        p->hz_scale = std::max(1e-6, params[4]);
+    } else if (ip == -1) {
+        p->hz_a1 = std::max(1e-12, params[2]) / p->s_len;
+        p->hz_b1 = std::max(1e-12, params[3]) / p->s_len;
+        p->hz_scale = std::max(1e-6, params[4]);
+    } else {
+        p->ipotcn = ip;   // 2-D and SDEC variants are stored but not solved by this engine
+    }
+}
+
+void cntc_setpotcontact(int *ire, int *icp, int *ipotcn, int *nparam, double *params) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    const int ip = *ipotcn;
+    if (ip < 1 || ip > 4 || *nparam != 6) return;
+    p->ipotcn = ip;
+    p->mx = std::max(1, (int)std::lround(params[0]));
+    p->my = std::max(1, (int)std::lround(params[1]));
+    const double a = params[2] * p->s_len, b = params[3] * p->s_len;
+    // potcon_fill, m_hierarch_data.f90:1801-1861
+    if (ip == 1) { p->xl = a; p->yl = b; p->dx = std::max(1e-12, params[4]) * p->s_len; p->dy = std::max(1e-12, params[5]) * p->s_len; }
+    else if (ip == 2) { p->xl = a; p->yl = b; p->dx = (params[4] * p->s_len - a) / p->mx; p->dy = (params[5] * p->s_len - b) / p->my; }
+    else if (ip == 3) {
+        p->dx = std::max(1e-12, params[4]) * p->s_len; p->dy = std::max(1e-12, params[5]) * p->s_len;
+        p->xl = a - 0.5 * p->dx; p->yl = b - 0.5 * p->dy;
+    } else {
+        p->dx = (params[4] * p->s_len - a) / std::max(1, p->mx - 1);
+        p->dy = (params[5] * p->s_len - b) / std::max(1, p->my - 1);
+        p->xl = a - 0.5 * p->dx; p->yl = b - 0.5 * p->dy;
+    }
+}
+
+void cntc_setpenetration(int *ire, int *icp, double *pen) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    p->norm = 0;
+    p->pen = *pen * p->s_len;
+}
+
+void cntc_setnormalforce(int *ire, int *icp, double *fn) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    p->norm = 1;
+    p->fn = *fn;
+}
+
+void cntc_setundeformeddistc(int *ire, int *icp, int *ibase, int *nparam, double *prmudf) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    const int ib = *ibase;
+    int need;
+    if (ib == 1) need = 6;
+    else if (ib == 9) need = p->mx * p->my;
+    else return;      // ibase 2, 3 are not provided by this engine
+    if (*nparam != need) return;
+    p->ibase = ib;
+    if (ib == 1) {
+        p->prmudf.assign(6, 0.0);
+        for (int k = 0; k < 3; k++) p->prmudf[k] = prmudf[k] / p->s_len;
+        for (int k = 3; k < 5; k++) p->prmudf[k] = prmudf[k];
+        p->prmudf[5] = prmudf[5] * p->s_len;
+    } else {
+        p->prmudf.assign(prmudf, prmudf + need);
+        for (auto &v : p->prmudf) v *= p->s_len;
+    }
+}
+
+void cntc_setcreepages(int *ire, int *icp, double *vx, double *vy, double *phi) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    if (p->tang == 1) { p->cksi = *vx * p->s_len; p->ceta = *vy * p->s_len; p->cphi = *phi; }
+    else { p->cksi = *vx; p->ceta = *vy; p->cphi = *phi / p->s_len; }
+}
+
+void cntc_setextrarigidslip(int *ire, int *icp, int *lenarr, double *wx, double *wy) {
+    (void)lenarr; (void)wx; (void)wy;
+    Problem *p = lookup(*ire, *icp, true);
+    if (p) p->rztang = 1;   // stored as a request; the solve reports it as unsupported
+}
+
+void cntc_settangentialforces(int *ire, int *icp, double *fx, double *fy) {
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    p->fxrel = *fx; p->fyrel = *fy;
+    const double fabs_ = std::sqrt((*fx) * (*fx) + (*fy) * (*fy));
+    if (fabs_ > 1.0) { p->fxrel /= fabs_; p->fyrel /= fabs_; }
+}
+
+void cntc_calculate(int *ire, int *icp, int *ierror) {
+    int ie = 0;
+    calculate_many(1, ire, icp, &ie);
+    *ierror = ie;
+}
+
+void cntc_calculate_batch(int *n, int *ire, int *icp, int *ierror) {
+    if (!n || *n <= 0) return;
+    calculate_many(*n, ire, icp, ierror);
+}
+
+void cntc_getflags(int *ire, int *icp, int *lenflg, int *params, int *values) {
+    Problem *p = lookup(*ire, *icp, false);
+    for (int i = 0; i < *lenflg; i++) {
+        int v = 0;
+        if (p) {
+            switch (params[i]) {
+                case CNTC_if_units: v = p->units; break;
+                case CNTC_ic_pvtime: v = p->pvtime; break;
+                case CNTC_ic_bound: v = p->bound; break;
+                case CNTC_ic_tang: v = p->tang; break;
+                case CNTC_ic_norm: v = p->norm; break;
+                case CNTC_ic_force: v = p->force3; break;
+                case CNTC_ic_frclaw: v = p->frclaw; break;
+                case CNTC_ic_mater: v = p->mater; break;
+                case CNTC_ic_iestim: v = p->iestim; break;
+                case CNTC_if_ncase: v = p->ncase; break;
+                case CNTC_if_mixedprec: v = p->mixed; break;
+                default: v = 0;
+            }
+        }
+        values[i] = v;
+    }
+}
+
+void cntc_gethertzcontact(int *ire, int *icp, int *lenarr, double *rvalues) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    const double v[10] = {p->hz_a1 * p->s_len, p->hz_b1 * p->s_len, p->hz_aa / p->s_len, p->hz_bb / p->s_len,
+                          p->hz_rho / p->s_len, p->hz_cp / p->s_len, p->hz_scale, 0.0, 0.0, p->hz_aob};
+    for (int i = 0; i < *lenarr && i < 10; i++) rvalues[i] = v[i];
+}
+
+void cntc_getnumelements(int *ire, int *icp, int *mx, int *my) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    *mx = p->have ? p->r_mx : p->mx;
+    *my = p->have ? p->r_my : p->my;
+}
+
+void cntc_getgriddiscretization(int *ire, int *icp, double *dx, double *dy) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    *dx = p->r_dx / p->s_len;
+    *dy = p->r_dy / p->s_len;
+}
+
+void cntc_getpotcontact(int *ire, int *icp, int *lenarr, double *rvalues) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    const double v[6] = {(double)p->r_mx, (double)p->r_my, p->r_xc1 / p->s_len, p->r_yc1 / p->s_len,
+                         p->r_dx / p->s_len, p->r_dy / p->s_len};
+    for (int i = 0; i < *lenarr; i++) rvalues[i] = i < 6 ? v[i] : 0.0;
+}
+
+void cntc_getpenetration(int *ire, int *icp, double *pen) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (p) *pen = p->pen / p->s_len;
+}
+
+void cntc_getcreepages(int *ire, int *icp, double *vx, double *vy, double *phi) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    if (p->tang == 1) { *vx = p->s_body * p->cksi / p->s_len; *vy = p->s_body * p->ceta / p->s_len; *phi = p->s_body * p->cphi; }
+    else { *vx = p->s_body * p->cksi; *vy = p->s_body * p->ceta; *phi = p->s_body * p->cphi * p->s_len; }
+}
+
+void cntc_getreferencevelocity(int *ire, int *icp, double *veloc) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (p) *veloc = p->veloc / p->s_veloc;
+}
+
+void cntc_getcontactforces(int *ire, int *icp, double *fn, double *tx, double *ty, double *mz) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    *fn = p->f_n;
+    *tx = p->s_body * p->f_x;
+    *ty = p->s_body * p->f_y;
+    *mz = p->s_body * p->m_z / p->s_len;
+}
+
+void cntc_getcontactpatchareas(int *ire, int *icp, double *carea, double *harea, double *sarea) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    const double dxdy = p->r_dx * p->r_dy;
+    *carea = (double)(float)p->ncon * dxdy / p->s_area;
+    *harea = (double)(float)p->nadh * dxdy / p->s_area;
+    *sarea = (double)(float)p->nslip * dxdy / p->s_area;
+}
+
+void cntc_getelementdivision(int *ire, int *icp, int *lenarr, int *eldiv) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p || !p->have) return;
+    const int n = std::min(*lenarr, (int)p->igs.size());
+    for (int i = 0; i < n; i++) eldiv[i] = p->igs[i];
+}
+
+void cntc_getmaximumpressure(int *ire, int *icp, double *pnmax) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    const double *pn = field_ptr(*p, W_PN);
+    double m = 0.0;
+    if (pn) for (int i = 0; i < p->r_mx * p->r_my; i++) m = std::max(m, std::fabs(pn[i]));
+    *pnmax = m * p->s_area;
+}
+
+void cntc_getmaximumtraction(int *ire, int *icp, double *ptmax) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    const double *px = field_ptr(*p, W_PX), *py = field_ptr(*p, W_PY);
+    double m = -1.0;
+    if (px) for (int i = 0; i < p->r_mx * p->r_my; i++) m = std::max(m, std::sqrt(px[i] * px[i] + py[i] * py[i]));
+    *ptmax = m * p->s_area;
+}
+
+void cntc_getfielddata(int *ire, int *icp, int *ifld, int *lenarr, double *fld) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p || !p->have) return;
+    const int n = p->r_mx * p->r_my;
+    int col = -1;
+    double sc = 1.0;
+    std::vector<double> tmp;
+    const double *src = nullptr;
+    switch (*ifld) {
+        case CNTC_fld_h: col = W_H; sc = 1.0 / p->s_len; break;
+        case CNTC_fld_mu: tmp.assign(n, p->fstat); src = tmp.data(); break;
+        case CNTC_fld_px: col = W_PX; sc = p->s_area * p->s_body; break;
+        case CNTC_fld_py: col = W_PY; sc = p->s_area * p->s_body; break;
+        case CNTC_fld_pn: col = W_PN; sc = p->s_area; break;
+        case CNTC_fld_ux: col = W_UX; sc = 1.0 / p->s_len; break;
+        case CNTC_fld_uy: col = W_UY; sc = 1.0 / p->s_len; break;
+        case CNTC_fld_un: col = W_UN; sc = 1.0 / p->s_len; break;
+        case CNTC_fld_sx: col = W_SX; sc = p->s_body / p->r_dq; break;
+        case CNTC_fld_sy: col = W_SY; sc = p->s_body / p->r_dq; break;
+        case CNTC_fld_wx: col = W_WX; sc = p->s_body / p->r_dq; break;
+        case CNTC_fld_wy: col = W_WY; sc = p->s_body / p->r_dq; break;
+        case CNTC_fld_taucrt: case CNTC_fld_uplsx: case CNTC_fld_uplsy: case CNTC_fld_temp1: case CNTC_fld_temp2:
+            tmp.assign(n, 0.0); src = tmp.data(); break;
+        default: return;
+    }
+    if (col >= 0) src = field_ptr(*p, col);
+    if (!src) return;
+    for (int i = 0; i < n && i < *lenarr; i++) fld[i] = sc * src[i];
+}
+
+void cntc_gettractions(int *ire, int *icp, int *lenarr, double *pn, double *px, double *py) {
+    int f;
+    f = CNTC_fld_px; cntc_getfielddata(ire, icp, &f, lenarr, px);
+    f = CNTC_fld_py; cntc_getfielddata(ire, icp, &f, lenarr, py);
+    f = CNTC_fld_pn; cntc_getfielddata(ire, icp, &f, lenarr, pn);
+}
+
+void cntc_getmicroslip(int *ire, int *icp, int *lenarr, double *sx, double *sy) {
+    int f;
+    f = CNTC_fld_sx; cntc_getfielddata(ire, icp, &f, lenarr, sx);
+    f = CNTC_fld_sy; cntc_getfielddata(ire, icp, &f, lenarr, sy);
+}
+
+void cntc_getdisplacements(int *ire, int *icp, int *lenarr, double *un, double *ux, double *uy) {
+    int f;
+    f = CNTC_fld_ux; cntc_getfielddata(ire, icp, &f, lenarr, ux);
+    f = CNTC_fld_uy; cntc_getfielddata(ire, icp, &f, lenarr, uy);
+    f = CNTC_fld_un; cntc_getfielddata(ire, icp, &f, lenarr, un);
+}
+
+void cntc_getsensitivities(int *ire, int *icp, int *lenout, int *lenin, double *sens) {
+    (void)ire; (void)icp;
+    for (int i = 0; i < (*lenout) * (*lenin); i++) sens[i] = 0.0;
+}
+
+void cntc_getcalculationtime(int *ire, int *icp, double *tcpu, double *twall) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) { *tcpu = 0; *twall = 0; return; }
+    *tcpu = p->tcpu; *twall = p->twall;
+}
+
+void cntc_resetcalculationtime(int *ire, int *icp) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (p) { p->tcpu = 0; p->twall = 0; }
+}
+
+void cntc_getiterationcounts(int *ire, int *icp, int *lenarr, int *values) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    const int v[6] = {p->itnorm, p->ittang, p->itcg, p->itgs, p->solver, p->ierror};
+    for (int i = 0; i < *lenarr && i < 6; i++) values[i] = v[i];
+}
+
+void cntc_finalize(int *ire) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (auto it = g_problems.begin(); it != g_problems.end();) {
+        if (it->second->ire == *ire) it = g_problems.erase(it);
+        else ++it;
+    }
+}
+
+void cntc_finalizelast() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_problems.clear();
+    g_initialized = -1;
+}
+
+long long cntc_gb300_kernel_launches() { return cgb::kernel_launch_count(); }
+
+void cntc_gb300_getsolverstats(int *ire, int *icp, int *lenarr, double *values) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    for (int i = 0; i < *lenarr; i++) values[i] = i < (int)p->stats.size() ? p->stats[i] : 0.0;
+}
+
+} // extern "C"

@@ -1,0 +1,74 @@
+// Host/device interface of the GB300 contact engine: one PatchDesc per contact
+// patch (one cntc_calculate of one (ire,icp) pair), filled by the host API layer and
+// read by the patch-solver kernel.  Plain C structs, no torch types.
+#pragma once
+#include <stdint.h>
+
+namespace cgb {
+
+// workspace columns (each npot doubles) of one patch
+enum WsCol {
+    W_H = 0, W_WX, W_WY,                   // undeformed distance h, rigid slip -dq*w (x,y)
+    W_PX, W_PY, W_PN,                      // tractions
+    W_UX, W_UY, W_UN,                      // displacement differences
+    W_SX, W_SY, W_SN,                      // slip (x,y) / deformed distance (n)
+    W_HSTOT, W_RHS, W_RES, W_RPRV, W_DD, W_Z, W_V, W_Q,      // NormCG
+    W_WSX, W_WSY, W_DPX, W_DPY, W_DSCL, W_NX, W_NY,          // TANG
+    W_RX, W_RY, W_DVX, W_DVY, W_VX, W_VY, W_QX, W_QY,
+    W_POX, W_POY, W_PDX, W_PDY, W_PNX, W_PNY, W_TRC, W_ZX, W_ZY, W_ONE,
+    W_NCOL
+};
+enum WsIntCol { I_IGS = 0, I_OLD, I_EXT, I_IEL, I_NCOL };
+
+// output scalars
+enum OutScalar {
+    O_FN = 0, O_FX, O_FY, O_MZ, O_PEN, O_ELEN, O_PMAX,
+    O_IERR, O_ITNORM, O_ITTANG, O_ITCG, O_ITGS, O_SOLVER, O_NCON, O_NADH, O_NSLIP,
+    O_NCONV32, O_NCONV64, O_NLS, O_STATUS,
+    O_T_TOTAL, O_T_CONV, O_T_LS, O_T_DIAG, O_T_GS, O_T_NORM, O_T_TANG, O_T_SCAN,   // SM clock cycles
+    O_NSCAL
+};
+
+// solver status bits (O_STATUS)
+constexpr int ST_OK = 0, ST_UNSUPPORTED = 1, ST_NOBRACKET = 2, ST_NORMCG_DIV = 4, ST_BADSIZE = 8;
+
+struct PatchDesc {
+    int mx, my, npot;
+    int fx, fy;                       // FFT grid NX = 2 fx, NY = 2 fy
+    double dx, dy, dxdy, xc1, yc1;
+    int tang, norm, bound, iestim, force3, gausei;
+    int maxgs, maxin, maxout;
+    double eps;
+    double omegah, omegas;
+    int gd_meth, kdown, kdowfb;
+    double fdecay, betath, d_ifc, d_lin, d_cns, d_slp, pow_s;
+    double ga, nu;
+    double fstat;
+    double chi, dq, cksi, ceta, cphi;
+    double fntrue, pen;
+    int ihertz;
+    double aa, bb;
+    int ibase;
+    double prm[6];
+    int precision;                    // 0: FP64 throughout; 1: FP32 convolutions + FP64 refinement
+    double eps32;                     // tolerance of the FP32 phase
+    int pad_;
+    // io block: columns W_H .. W_SN (kIoCols * npot doubles), then O_NSCAL output scalars,
+    // then the element division (npot ints).  Inputs (element-wise h, warm-start tractions
+    // and element division) arrive and all results leave through this block.
+    double *io;
+    double *wk;                       // work columns W_HSTOT .. (W_NCOL - kIoCols) * npot doubles
+    int *wki;                         // int columns I_OLD .. ((I_NCOL - 1) * npot ints)
+    const double *cf;                 // spatial influence coefficients [4][2my][2mx]: xx, xy, yy, zz
+    const double *spec64;             // spectra [7][fx+1][fy+1]: xx, xy, yy, zz, M_zz, M_xx, M_yy
+    const float *spec32;
+    void *rbuf;                       // 2 * (fx+1) * my complex doubles
+};
+
+constexpr int kIoCols = W_HSTOT;      // W_H .. W_SN live in the io block
+
+__host__ __device__ inline size_t io_doubles(int npot) {
+    return (size_t)kIoCols * npot + O_NSCAL + (size_t)(npot + 1) / 2;
+}
+
+} // namespace cgb

@@ -1,0 +1,1285 @@
+// Device-resident solve of one contact patch by one thread block: set-up of the
+// right-hand sides and initial estimate (m_sdis.f90), NORM + NormCG (m_snorm.f90:31-378,
+// m_solvpn.f90:24-461), TANG (m_stang.f90:28-951) with the solvers SteadyGS
+// (m_solvpt.f90:2825-3254), GDsteady (gdsteady.f90) and TangCG (m_solvpt.f90:1841-2442),
+// and the output quantities of soutpt (m_soutpt.f90:377-511).
+//
+// Every vector operation is a block-strided loop over the npot elements; every scalar
+// decision comes from a deterministic block reduction, so all threads follow the same
+// control flow.  Products with the influence-coefficient matrix use the FFT convolution of
+// fft.cuh in precision T (double, or float in the first phase of the mixed-precision form).
+#pragma once
+#include "common.cuh"
+#include "engine.h"
+#include "fft.cuh"
+
+namespace cgb {
+
+constexpr int kMaxLs = 99;   // perform_linesearch max_j, gdsteady.f90:1063
+
+struct SolverSmem {
+    RedSmem red;
+    // line search table (1-based like the reference)
+    double tbl_alpha[kMaxLs + 2], tbl_rho[kMaxLs + 2], tbl_drhoda[kMaxLs + 2];
+    double alpha_j;
+    int stop_j, nobracket, jcount;
+    // generic broadcast slots
+    double bd[8];
+    int bi[8];
+    // phase timers (SM cycles), indexed like O_T_TOTAL .. O_T_SCAN
+    long long t[8];
+};
+
+// thread 0 accumulates the cycles between a start mark and the end of a phase
+#define PHASE_START(v) long long v = clock64()
+#define PHASE_END(P, k, v) do { if (threadIdx.x == 0) (P).sm->t[(k)] += clock64() - (v); } while (0)
+
+// view of one patch's memory
+struct PView {
+    const PatchDesc *d;
+    int mx, my, n;
+    SolverSmem *sm;
+    __device__ double *c(int k) const {
+        return k < kIoCols ? d->io + (size_t)k * n : d->wk + (size_t)(k - kIoCols) * n;
+    }
+    __device__ int *ci(int k) const {
+        return k == I_IGS ? igs() : d->wki + (size_t)(k - 1) * n;
+    }
+    __device__ int *igs() const { return (int *)(d->io + (size_t)kIoCols * n + O_NSCAL); }
+    __device__ double *out() const { return d->io + (size_t)kIoCols * n; }
+};
+
+#define FOR_I(i, n) for (int i = threadIdx.x; i < (n); i += kThreads)
+
+// ------------------------------------------------------------------------------------------
+// small helpers
+// ------------------------------------------------------------------------------------------
+__device__ inline double dsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
+
+__device__ __noinline__ void count_eldiv(const PView &P, int &nadh, int &nslip, int &nplast, int &nexter) {
+    const int *igs = P.igs();
+    int v[4] = {0, 0, 0, 0};
+    FOR_I(i, P.n) {
+        int e = igs[i];
+        if (e == Adhes) v[0]++; else if (e == Slip) v[1]++; else if (e == Plast) v[2]++; else v[3]++;
+    }
+    block_sumi<4>(P.sm->red, v);
+    nadh = v[0]; nslip = v[1]; nplast = v[2]; nexter = v[3];
+}
+
+// row extents of the interior elements (Areas, m_gridfunc.f90:582-637), 1-based like the
+// reference: first = nx, last = 0 for empty rows.  Stored in int column I_EXT: row1st at
+// [iy], rowlst at [my + iy].
+__device__ __noinline__ void areas(const PView &P) {
+    const int mx = P.mx, my = P.my;
+    const int *igs = P.igs();
+    int *ext = P.ci(I_EXT);
+    __syncthreads();
+    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+        const int i0 = iy * mx;
+        int first = 1;
+        while (igs[(first - 1) + i0] <= Exter && first != mx) first++;
+        int last = 0;
+        for (int ix = first; ix <= mx; ix++) if (igs[(ix - 1) + i0] >= Adhes) last = ix;
+        ext[iy] = first;
+        ext[my + iy] = last;
+    }
+    __syncthreads();
+}
+
+// one row of A times a vector restricted to the row extents (gf3_AijPj, m_aijpj.f90:99-254):
+// returns sum over blocks (ik,jk) listed in blks/vecs for element ii, times ga_inv.
+// blk codes: 0 xx, 1 xy, 2 yy, 3 zz (xy == yx).  vec == nullptr means a vector of ones.
+__device__ __noinline__ void direct_rowsum(const PView &P, int ii, int nterm, const int *blks, const double *const *vecs,
+                                     double *res /* nres */, const int *resid, int nres) {
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx, my = P.my;
+    const int ix = ii % mx + 1, iy = ii / mx + 1;
+    const int *ext = P.ci(I_EXT);
+    const size_t bsz = (size_t)4 * mx * my;
+    double acc[2] = {0.0, 0.0};
+    // iterate over (jy, jx) pairs; each thread takes a strided subset of the flattened range
+    for (int jy = 1; jy <= my; jy++) {
+        const int j0 = max(1, ext[jy - 1] - 1), j1 = min(mx, ext[my + jy - 1] + 1);
+        for (int jx = j0 + threadIdx.x; jx <= j1; jx += kThreads) {
+            const size_t off = (size_t)(ix - jx + mx) + (size_t)(iy - jy + my) * 2 * mx;
+            const int jj = (jx - 1) + (jy - 1) * mx;
+            for (int t = 0; t < nterm; t++) {
+                const double c = d.cf[blks[t] * bsz + off];
+                const double v = vecs[t] ? vecs[t][jj] : 1.0;
+                acc[resid[t]] += c * v;
+            }
+        }
+    }
+    if (nres == 1) {
+        double s = block_sum1(P.sm->red, acc[0]);
+        res[0] = s / d.ga;
+    } else {
+        double a2[2] = {acc[0], acc[1]};
+        block_sum<2>(P.sm->red, a2);
+        res[0] = a2[0] / d.ga; res[1] = a2[1] / d.ga;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// products with A.  Spectra K[0..6] = xx, xy, yy, zz and the preconditioners zz, xx, yy.
+// ------------------------------------------------------------------------------------------
+template <typename T>
+struct Ops {
+    Conv<T> cv;
+    const T *K[7];          // xx, xy, yy, zz, M_zz, M_xx, M_yy
+};
+
+// normal product out = A_zz in (kind 3) or M in (kind 4)
+template <typename T>
+__device__ inline void prod_n(const Ops<T> &op, const double *in, double *out, int mode, const int *igs, int kind) {
+    convolve<T>(op.cv, in, nullptr, out, nullptr, 1, op.K[kind], nullptr, nullptr, mode, igs);
+}
+// tangential product (outx, outy) = A_tt (inx, iny)
+template <typename T>
+__device__ inline void prod_t(const Ops<T> &op, const double *inx, const double *iny, double *ox, double *oy,
+                              int mode, const int *igs) {
+    convolve<T>(op.cv, inx, iny, ox, oy, 2, op.K[0], op.K[1], op.K[2], mode, igs);
+}
+
+// ------------------------------------------------------------------------------------------
+// NormCG, m_solvpn.f90:24-461.  Returns itcg, or -1 when the reference would abort.
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, double eps, double &pen, double &err,
+                      int &nconv) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n;
+    RedSmem &red = P.sm->red;
+    int *igs = P.igs();
+    double *pn = P.c(W_PN), *hstot = P.c(W_HSTOT), *rhs = P.c(W_RHS), *res = P.c(W_RES), *rprv = P.c(W_RPRV);
+    double *dd = P.c(W_DD), *z = P.c(W_Z), *v = P.c(W_V), *q = P.c(W_Q);
+    const double dxdy = d.dxdy, fntrue = d.fntrue;
+    const int numinn = (n <= 150) ? 3 : (n <= 400) ? 2 : 1;
+    if (d.norm == 1) pen = 0.0;
+    FOR_I(i, n) { rhs[i] = pen - hstot[i]; }
+    double davg = 0.0;
+    int ncon = 0;
+    { int c = 0; FOR_I(i, n) if (igs[i] >= Adhes) c++; ncon = block_sumi1(red, c); }
+    if (d.norm == 0) {
+        double hmin = 1e20; FOR_I(i, n) hmin = fmin(hmin, hstot[i]);
+        hmin = block_min1(red, hmin) - pen;
+        if (hmin >= 0.0) {
+            FOR_I(i, n) { pn[i] = 0.0; igs[i] = Exter; }
+            __syncthreads();
+            err = 0.0;
+            return 0;
+        }
+    } else {
+        if (ncon <= 0) {
+            double hmin = 1e20, hmax = -1e20;
+            FOR_I(i, n) { hmin = fmin(hmin, hstot[i]); hmax = fmax(hmax, hstot[i]); }
+            hmin = block_min1(red, hmin); hmax = block_max1(red, hmax);
+            double htrsh = hmin + 0.1 * fmax(hmax - hmin, 1e-10);
+            int c = 0;
+            FOR_I(i, n) if (hstot[i] < htrsh) { igs[i] = Adhes; c++; }
+            ncon += block_sumi1(red, c);
+        }
+        double s = 0; FOR_I(i, n) s += pn[i];
+        double fk = dxdy * block_sum1(red, s);
+        if (fabs(fk) < (double)1e-3f * fntrue) {
+            double pval = fntrue / (dxdy * (double)(float)ncon);
+            FOR_I(i, n) if (igs[i] >= Adhes) pn[i] = pval;
+        } else {
+            FOR_I(i, n) if (igs[i] >= Adhes) pn[i] *= fntrue / fk;
+        }
+    }
+    // res = rhs - A ps on AllInt, then proj_avg
+    prod_n<T>(op, pn, res, OUT_INT, igs, 3); nconv++;
+    {
+        double s = 0; int c = 0;
+        FOR_I(i, n) if (igs[i] >= Adhes) { res[i] = rhs[i] - res[i]; s += res[i]; c++; }
+        if (d.norm == 1) {
+            double a[1] = {s}; block_sum<1>(red, a); int cc = block_sumi1(red, c);
+            double avg = a[0] / (double)(float)max(1, cc);
+            FOR_I(i, n) if (igs[i] >= Adhes) res[i] -= avg;
+        }
+    }
+    __syncthreads();
+    double rz1 = 0, rz2 = 0, rms_upd1 = 0, alpha = 0;
+    int itcg = 0, itinn = 0;
+    double rms_xk = 1.0, rms_upd = 2.0 * eps * rms_xk;
+    bool lchanged = false;
+    while ((lchanged || rms_upd > eps * rms_xk) && itcg < maxcg) {
+        itcg++; itinn++;
+        prod_n<T>(op, res, z, OUT_INT, igs, 4); nconv++;
+        if (d.norm == 1) {
+            double s = 0; int c = 0;
+            FOR_I(i, n) if (igs[i] >= Adhes) { s += z[i]; c++; }
+            s = block_sum1(red, s); c = block_sumi1(red, c);
+            double avg = s / (double)(float)max(1, c);
+            FOR_I(i, n) if (igs[i] >= Adhes) z[i] -= avg;
+            __syncthreads();
+        }
+        rz1 = rz2;
+        {
+            double a[2] = {0, 0};
+            FOR_I(i, n) if (igs[i] >= Adhes) { a[0] += z[i] * res[i]; a[1] += z[i] * rprv[i]; }
+            block_sum<2>(red, a);
+            rz2 = a[0];
+            if (itcg <= 1 || rz1 < 1e-20) {
+                FOR_I(i, n) if (igs[i] >= Adhes) v[i] = z[i];
+            } else {
+                double beta = fmax(0.0, (rz2 - a[1]) / fmax(1e-20, rz1));
+                FOR_I(i, n) if (igs[i] >= Adhes) v[i] = beta * v[i] + z[i];
+            }
+        }
+        if (d.norm == 1) {
+            double s = 0; int c = 0;
+            FOR_I(i, n) if (igs[i] >= Adhes) { s += v[i]; c++; }
+            s = block_sum1(red, s); c = block_sumi1(red, c);
+            double avg = s / (double)(float)max(1, c);
+            FOR_I(i, n) if (igs[i] >= Adhes) v[i] -= avg;
+        }
+        prod_n<T>(op, v, q, OUT_INT, igs, 3); nconv++;
+        if (d.norm == 1) {
+            double s = 0; int c = 0;
+            FOR_I(i, n) if (igs[i] >= Adhes) { s += q[i]; c++; }
+            s = block_sum1(red, s); c = block_sumi1(red, c);
+            double avg = s / (double)(float)max(1, c);
+            FOR_I(i, n) if (igs[i] >= Adhes) q[i] -= avg;
+            __syncthreads();
+        }
+        double rv, vav;
+        {
+            double a[2] = {0, 0};
+            FOR_I(i, n) if (igs[i] >= Adhes) { a[0] += res[i] * v[i]; a[1] += q[i] * v[i]; }
+            block_sum<2>(red, a);
+            rv = a[0]; vav = a[1];
+        }
+        if (fabs(vav) > 1e-32 && ncon == 1) alpha = rv / vav;
+        else alpha = rv / fmax(1e-20, vav);
+        {
+            double a[2] = {0, 0};
+            FOR_I(i, n) if (igs[i] >= Adhes) {
+                pn[i] += alpha * v[i];
+                a[0] += v[i] * v[i]; a[1] += pn[i] * pn[i];
+            }
+            int c = 0; FOR_I(i, n) if (igs[i] >= Adhes) c++;
+            block_sum<2>(red, a);
+            c = block_sumi1(red, c);
+            rms_upd = fabs(alpha) * sqrt(a[0] / max(1, c));
+            if (itcg == 1) rms_upd1 = rms_upd;
+            if (itcg <= 3 || itcg % 10 == 0) rms_xk = sqrt(a[1] / max(1, c));
+        }
+        FOR_I(i, n) rprv[i] = res[i];
+        if (itinn < numinn && rms_upd >= eps * rms_xk) {
+            FOR_I(i, n) if (igs[i] >= Adhes) res[i] -= alpha * q[i];
+            __syncthreads();
+        } else {
+            int chg = 0, dn = 0;
+            FOR_I(i, n) if (igs[i] >= Adhes && pn[i] < 0.0) { igs[i] = Exter; pn[i] = 0.0; chg = 1; dn++; }
+            {
+                int a[2] = {chg, dn}; block_sumi<2>(red, a);
+                chg = a[0]; ncon -= a[1];
+            }
+            bool lchg_negpn = chg > 0;
+            if (ncon <= 0) {
+                double hmin = 1e20; FOR_I(i, n) hmin = fmin(hmin, hstot[i]);
+                hmin = block_min1(red, hmin);
+                int c = 0;
+                FOR_I(i, n) if (hstot[i] <= hmin + 1e-5) { igs[i] = Adhes; pn[i] = 0.0; c++; }
+                c = block_sumi1(red, c);
+                ncon += c;
+                if (c > 0) lchg_negpn = true;
+            }
+            if (d.norm == 1 && lchg_negpn) {
+                double s = 0; FOR_I(i, n) s += pn[i];
+                double fk = dxdy * block_sum1(red, s);
+                if (fabs(fk) < (double)1e-3f * fntrue) {
+                    FOR_I(i, n) if (igs[i] >= Adhes) pn[i] = 1.0;
+                    s = 0; FOR_I(i, n) s += pn[i];
+                    fk = block_sum1(red, s);
+                }
+                FOR_I(i, n) if (igs[i] >= Adhes) pn[i] *= fntrue / fk;
+            }
+            // dd = A ps - rhs on all elements
+            prod_n<T>(op, pn, dd, OUT_ALL, igs, 3); nconv++;
+            FOR_I(i, n) dd[i] -= rhs[i];
+            if (d.norm == 1) {
+                double s = 0; FOR_I(i, n) if (igs[i] >= Adhes) s += dd[i];
+                s = block_sum1(red, s);
+                davg = s / (double)(float)ncon;
+                FOR_I(i, n) if (igs[i] >= Adhes) dd[i] -= davg;   // proj_avg over AllInt (count = ncon)
+            }
+            __syncthreads();
+            int nin = 0;
+            FOR_I(i, n) {
+                res[i] = (igs[i] >= Adhes) ? -dd[i] : 0.0;
+                if (igs[i] == Exter && dd[i] - davg < 0.0) {
+                    igs[i] = Adhes; res[i] = -(dd[i] - davg); nin++;
+                }
+                if (igs[i] == Exter) v[i] = 0.0;
+            }
+            nin = block_sumi1(red, nin);
+            ncon += nin;
+            itinn = 0;
+            lchanged = (nin > 0) || lchg_negpn;
+        }
+    }
+    if (d.norm == 1) pen = davg;
+    double conv = 1.0;
+    if (rms_upd * rms_upd1 > 0.0 && itcg > 1) conv = exp(log(rms_upd / rms_upd1) / (itcg - 1));
+    err = rms_upd;
+    if (rms_upd > rms_xk && conv > 1.0 && itcg >= maxcg) return -1;
+    return itcg;
+}
+
+// ------------------------------------------------------------------------------------------
+// snorm, m_snorm.f90:31-378.  Returns itnorm (-1 maxin, -2 NormCG divergence).
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ int snorm(const PView &P, const Ops<T> &op, int maxgs, int maxin, double eps, double &pen,
+                     int &itcg_out, int &nconv) {
+    const int n = P.n, mx = P.mx, my = P.my;
+    RedSmem &red = P.sm->red;
+    int *igs = P.igs();
+    double *pn = P.c(W_PN), *hstot = P.c(W_HSTOT), *h = P.c(W_H), *unn = P.c(W_DD), *one = P.c(W_ONE);
+    FOR_I(i, n) { hstot[i] = h[i]; one[i] = 1.0; }
+    int itnorm = 0, itcg = 0;
+    bool zready;
+    do {
+        itnorm++;
+        zready = true;
+        FOR_I(i, n) if (igs[i] < Adhes) pn[i] = 0.0;
+        __syncthreads();
+        double errpn;
+        int it = normcg<T>(P, op, maxgs, eps, pen, errpn, nconv);
+        if (it < 0) { itcg_out = itcg; return -2; }
+        itcg += it;
+        int newext = 0;
+        FOR_I(i, n) if (igs[i] >= Adhes && pn[i] < -errpn) { igs[i] = Exter; pn[i] = 0.0; newext++; }
+        newext = block_sumi1(red, newext);
+        if (newext > 0) zready = false;
+        if (zready) {
+            areas(P);
+            prod_n<T>(op, pn, unn, OUT_ALL, igs, 3); nconv++;
+            int ixc = max(1, mx / 2), iyc = max(1, my / 2);
+            int iic = (ixc - 1) + (iyc - 1) * mx;
+            int blk[1] = {3}; const double *vv[1] = {nullptr}; int rid[1] = {0}; double tolv[1];
+            direct_rowsum(P, iic, 1, blk, vv, tolv, rid, 1);
+            double tol = fabs(errpn * tolv[0]);
+            int newcon = 0;
+            FOR_I(i, n) {
+                if (igs[i] == Exter && hstot[i] - pen < 0.0) {
+                    double dd = hstot[i] - pen + unn[i];
+                    if (dd < -tol) { igs[i] = Adhes; newcon++; }
+                }
+            }
+            newcon = block_sumi1(red, newcon);
+            if (newcon != 0) zready = false;
+        }
+        if (it >= maxgs) zready = false;
+    } while (!zready && itnorm < maxin);
+    if (!zready) itnorm = -1;
+    FOR_I(i, n) if (pn[i] < 0.0 && igs[i] >= Adhes) { pn[i] = 0.0; igs[i] = Exter; }
+    __syncthreads();
+    itcg_out = itcg;
+    return itnorm;
+}
+
+// ------------------------------------------------------------------------------------------
+// single-element solver plstrc for an elastic element (m_solvpt.f90:3278-3807, no plasticity;
+// the plastic trial of the reference cannot succeed there and leaves the element in adhesion)
+// ------------------------------------------------------------------------------------------
+__device__ __noinline__ void elm_solve(int &el, const double coef[2][2], double eps, double omegah, double omegas,
+                                 double pr[3], double mus, double s[2]) {
+    const int maxnr = 10;
+    const double prc = 0.0001;
+    const double taucs = 1e20;
+    double pold1 = pr[0], pold2 = pr[1];
+    double si0[2], si[2] = {0.0, 0.0}, dp[2], fk[2], gradf[2][2];
+    si0[0] = s[0] - coef[0][0] * pr[0] - coef[0][1] * pr[1];
+    si0[1] = s[1] - coef[1][0] * pr[0] - coef[1][1] * pr[1];
+    int itry = 0, violat = 1;
+    double trc_bound = 0.0;
+    while (itry <= 3 && violat == 1) {
+        itry++;
+        if (el == Adhes) {
+            trc_bound = mus * pr[2];
+            double detinv = 1.0 / (coef[0][0] * coef[1][1] - coef[0][1] * coef[1][0]);
+            dp[0] = (-coef[1][1] * s[0] + coef[0][1] * s[1]) * detinv;
+            dp[1] = (coef[1][0] * s[0] - coef[0][0] * s[1]) * detinv;
+            pr[0] = pold1 + omegah * dp[0];
+            pr[1] = pold2 + omegah * dp[1];
+            double pabs2 = sqrt(pr[0] * pr[0] + pr[1] * pr[1]);
+            double bnd = fmin(trc_bound, taucs);
+            if (pabs2 <= bnd) violat = 0;
+            else {
+                double pabs1 = sqrt((pold1 + dp[0]) * (pold1 + dp[0]) + (pold2 + dp[1]) * (pold2 + dp[1]));
+                if (pabs1 <= bnd) { pr[0] = pr[0] * bnd / pabs2; pr[1] = pr[1] * bnd / pabs2; violat = 0; }
+                else violat = 1;
+            }
+            si[0] = si0[0] + coef[0][0] * pr[0] + coef[0][1] * pr[1];
+            si[1] = si0[1] + coef[1][0] * pr[0] + coef[1][1] * pr[1];
+        } else if (el == Slip) {
+            violat = 0;
+            trc_bound = mus * pr[2];
+            double sabs = sqrt(si0[0] * si0[0] + si0[1] * si0[1]);
+            pr[0] = -trc_bound * si0[0] / sabs;
+            pr[1] = -trc_bound * si0[1] / sabs;
+            si[0] = si0[0] + coef[0][0] * pr[0] + coef[0][1] * pr[1];
+            si[1] = si0[1] + coef[1][0] * pr[0] + coef[1][1] * pr[1];
+            fk[0] = pr[1] * si[0] - pr[0] * si[1];
+            fk[1] = pr[0] * pr[0] + pr[1] * pr[1] - trc_bound * trc_bound;
+            int itnr = 0;
+            while (itnr == 0 || (itnr < maxnr && fabs(fk[0]) + fabs(fk[1]) >= prc * eps * trc_bound)) {
+                itnr++;
+                gradf[0][0] = -2.0 * coef[1][0] * pr[0] - si0[1] + (coef[0][0] - coef[1][1]) * pr[1];
+                gradf[0][1] = 2.0 * coef[0][1] * pr[1] + si0[0] + (coef[0][0] - coef[1][1]) * pr[0];
+                gradf[1][0] = 2.0 * pr[0];
+                gradf[1][1] = 2.0 * pr[1];
+                double det = gradf[0][0] * gradf[1][1] - gradf[0][1] * gradf[1][0];
+                if (det == 0.0) itnr = maxnr;
+                else {
+                    dp[0] = -(gradf[1][1] * fk[0] - gradf[0][1] * fk[1]) / det;
+                    dp[1] = -(-gradf[1][0] * fk[0] + gradf[0][0] * fk[1]) / det;
+                    pr[0] += dp[0]; pr[1] += dp[1];
+                }
+                si[0] = si0[0] + coef[0][0] * pr[0] + coef[0][1] * pr[1];
+                si[1] = si0[1] + coef[1][0] * pr[0] + coef[1][1] * pr[1];
+                fk[0] = pr[1] * si[0] - pr[0] * si[1];
+                fk[1] = pr[0] * pr[0] + pr[1] * pr[1] - trc_bound * trc_bound;
+            }
+            double alph0 = atan2(pold2, pold1);
+            double alph1 = atan2(pr[1], pr[0]);
+            double dalph = alph1 - alph0;
+            const double pi = 3.14159265358979323846;
+            if (dalph < -pi) dalph += 2.0 * pi;
+            if (dalph > pi) dalph -= 2.0 * pi;
+            alph1 = alph0 + omegas * dalph;
+            double sn, cs;
+            sincos(alph1, &sn, &cs);
+            pr[0] = trc_bound * cs;
+            pr[1] = trc_bound * sn;
+            if (fabs(pr[0]) > fabs(pr[1])) { if (pr[0] * si[0] > 0.0) violat = 1; }
+            else { if (pr[1] * si[1] > 0.0) violat = 1; }
+        } else {
+            // plastic trial: with an infinite yield limit it is always rejected
+            trc_bound = mus * pr[2];
+            si[0] = 0.0; si[1] = 0.0;
+            violat = 1;
+        }
+        if (itry <= 3 && violat == 1) {
+            if (el == Adhes) el = (trc_bound <= taucs) ? Slip : Plast;
+            else if (el == Slip) el = Plast;
+            else el = Adhes;
+        }
+    }
+    s[0] = si[0]; s[1] = si[1];
+}
+
+struct TangState {
+    int solver;
+    double omegah, omegas;
+};
+
+// ------------------------------------------------------------------------------------------
+// SteadyGS, m_solvpt.f90:2825-3254: element-by-element Gauss-Seidel in rolling order.
+// Each element's shift is a block reduction; thread 0 solves the element and propagates.
+// ------------------------------------------------------------------------------------------
+__device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double omegah, double omegas, int &info, double &err) {
+    PHASE_START(tgs);
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx, my = P.my, n = P.n;
+    RedSmem &red = P.sm->red;
+    int *igs = P.igs();
+    double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN);
+    double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY), *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+    double *sx = P.c(W_SX), *sy = P.c(W_SY);
+    const size_t bsz = (size_t)4 * mx * my;
+    const double mus = d.fstat;
+    const int ixsta = 1, ixinc = 1, ixend = mx;
+    FOR_I(ii, n) {
+        int ix = ii % mx + 1;
+        if (ix != ixend) { dpx[ii] = px[ii] - px[ii + ixinc]; dpy[ii] = py[ii] - py[ii + ixinc]; }
+        else { dpx[ii] = px[ii]; dpy[ii] = py[ii]; }
+    }
+    int nadh, nslip, nplst, nexter;
+    count_eldiv(P, nadh, nslip, nplst, nexter);
+    int k = nadh + nslip + nplst;
+    double facnel = sqrt((double)(float)n / (double)(float)k);
+    int itgs = 0;
+    double dif = 2.0, difid = 1.0, dif1 = 0.0;
+    const int blks[4] = {0, 1, 1, 2};
+    const int rid[4] = {0, 0, 1, 1};
+    while (dif >= difid && itgs < maxgs) {
+        itgs++;
+        double difacc = 0.0;      // held by thread 0
+        for (int iy = 1; iy <= my; iy++) {
+            for (int ix = ixsta; ix <= ixend; ix++) {
+                int ii = (ix - 1) + (iy - 1) * mx;
+                if (igs[ii] < Adhes) continue;
+                const double *vecs[4] = {dpx, dpy, dpx, dpy};
+                double s[2];
+                direct_rowsum(P, ii, 4, blks, vecs, s, rid, 2);
+                if (threadIdx.x == 0 && ix > ixsta) {
+                    // the solver choice keeps the trailing column ix = 1 outside the contact area
+                    int jx = ix - ixinc;
+                    int jj = (jx - 1) + (iy - 1) * mx;
+                    while (igs[jj] == Adhes && jx != ixsta) { jx -= ixinc; jj = (jx - 1) + (iy - 1) * mx; }
+                    const size_t o0 = (size_t)(0 + mx) + (size_t)(0 + my) * 2 * mx;
+                    const size_t oj = (size_t)(jx - ix + mx) + (size_t)(0 + my) * 2 * mx;
+                    double coef[2][2];
+                    coef[0][0] = (d.cf[0 * bsz + o0] - d.cf[0 * bsz + oj]) / d.ga;
+                    coef[0][1] = (d.cf[1 * bsz + o0] - d.cf[1 * bsz + oj]) / d.ga;
+                    coef[1][0] = coef[0][1];
+                    coef[1][1] = (d.cf[2 * bsz + o0] - d.cf[2 * bsz + oj]) / d.ga;
+                    s[0] += wsx[ii]; s[1] += wsy[ii];
+                    double pr[3] = {px[ii], py[ii], pn[ii]};
+                    int el = igs[ii];
+                    elm_solve(el, coef, eps, omegah, omegas, pr, mus, s);
+                    igs[ii] = el;
+                    difacc += (pr[0] - px[ii]) * (pr[0] - px[ii]) + (pr[1] - py[ii]) * (pr[1] - py[ii]);
+                    dpx[ii] += pr[0] - px[ii];
+                    dpy[ii] += pr[1] - py[ii];
+                    px[ii] = pr[0]; py[ii] = pr[1];
+                    sx[ii] = s[0]; sy[ii] = s[1];
+                    for (int kx = ix - ixinc; kx >= ixsta; kx -= ixinc) {
+                        int kk = (kx - 1) + (iy - 1) * mx, kn = kk + ixinc;
+                        if (igs[kk] == Adhes) {
+                            px[kk] = px[kn] + dpx[kk];
+                            py[kk] = py[kn] + dpy[kk];
+                            double ptabs = sqrt(px[kk] * px[kk] + py[kk] * py[kk]);
+                            double ptbnd = mus * pn[kk];
+                            if (ptabs > ptbnd) {
+                                px[kk] = px[kk] * ptbnd / ptabs; py[kk] = py[kk] * ptbnd / ptabs;
+                                dpx[kk] = px[kk] - px[kn]; dpy[kk] = py[kk] - py[kn];
+                            }
+                        } else if (igs[kk] == Slip || igs[kk] == Plast) {
+                            dpx[kk] = px[kk] - px[kn]; dpy[kk] = py[kk] - py[kn];
+                        } else if (igs[kk] <= Exter && igs[kn] >= Adhes) {
+                            dpx[kk] = -px[kn]; dpy[kk] = -py[kn];
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        if (threadIdx.x == 0) P.sm->bd[0] = difacc;
+        __syncthreads();
+        dif = sqrt(P.sm->bd[0] / (2.0 * k));
+        double a = 0; FOR_I(i, n) a += px[i] * px[i] + py[i] * py[i];
+        a = block_sum1(red, a);
+        double rms = sqrt(a / (2 * n));
+        difid = eps * fmax(1e-6, facnel * rms);
+        if (itgs == 1) dif1 = dif;
+    }
+    double conv = 1.0;
+    if (dif * dif1 != 0.0 && itgs > 1) conv = exp(log(dif / dif1) / (itgs - 1));
+    err = dif;
+    info = 0;
+    if (itgs >= maxgs) info = 1;
+    if (itgs >= maxgs && conv > 0.997) info = 2;
+    if (itgs >= maxgs && conv > 1.0) info = 3;
+    PHASE_END(P, O_T_GS - O_T_TOTAL, tgs);
+    return itgs;
+}
+
+// ------------------------------------------------------------------------------------------
+// GDsteady helpers (gdsteady.f90:610-1462); rows are scanned from the leading edge (ix = mx)
+// towards the trailing edge, one thread per row.
+// ------------------------------------------------------------------------------------------
+__device__ __noinline__ void apply_trcbnd(const PView &P, const double *trc, double *dpx, double *dpy, double *px,
+                                    double *py) {
+    const int mx = P.mx, my = P.my;
+    const int *igs = P.igs();
+    __syncthreads();
+    PHASE_START(tsc);
+    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+        int ii = (mx - 1) + iy * mx;
+        px[ii] = 0.0; py[ii] = 0.0;
+        double pxn = 0.0, pyn = 0.0;
+        for (int ix = mx - 2; ix >= 0; ix--) {
+            ii = ix + iy * mx;
+            double qx, qy;
+            if (igs[ii] <= Exter) { qx = 0.0; qy = 0.0; }
+            else {
+                qx = pxn + dpx[ii]; qy = pyn + dpy[ii];
+                double ptabs = sqrt(qx * qx + qy * qy);
+                if (igs[ii] == Slip || ptabs >= trc[ii]) { qx = qx * trc[ii] / ptabs; qy = qy * trc[ii] / ptabs; }
+            }
+            px[ii] = qx; py[ii] = qy;
+            dpx[ii] = qx - pxn; dpy[ii] = qy - pyn;
+            pxn = qx; pyn = qy;
+        }
+    }
+    __syncthreads();
+    PHASE_END(P, O_T_SCAN - O_T_TOTAL, tsc);
+}
+
+// project_searchdir, gdsteady.f90:639-803 (variants E_trl, E_down(k), E_keep(f))
+__device__ __noinline__ void project_searchdir(const PView &P, int imeth, int kdown, const double *trc) {
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx, my = P.my;
+    const int *igs = P.igs();
+    double *dvx = P.c(W_DVX), *dvy = P.c(W_DVY), *vx = P.c(W_VX), *vy = P.c(W_VY);
+    const double *nx = P.c(W_NX), *ny = P.c(W_NY);
+    double *dxi = P.c(W_ZX), *dyi = P.c(W_ZY);   // copies of the input search direction (E_down)
+    const double fac_v = 1000.0;
+    __syncthreads();
+    if (imeth == 2) { FOR_I(i, P.n) { dxi[i] = dvx[i]; dyi[i] = dvy[i]; } __syncthreads(); }
+    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+        const int i0 = iy * mx;
+        int ii = (mx - 1) + i0;
+        vx[ii] = 0.0; vy[ii] = 0.0;
+        for (int ix = mx - 2; ix >= 0; ix--) {
+            ii = ix + i0;
+            const double tx = -ny[ii], ty = nx[ii];
+            if (imeth == 1) {
+                if (igs[ii] == Adhes) { vx[ii] = vx[ii + 1] + dvx[ii]; vy[ii] = vy[ii + 1] + dvy[ii]; }
+                else if (igs[ii] == Slip) {
+                    double vt = tx * dvx[ii] + ty * dvy[ii];
+                    vt = dsign(1.0, vt) * fmin(fabs(vt), fac_v * trc[ii]);
+                    vx[ii] = tx * vt; vy[ii] = ty * vt;
+                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                } else {
+                    vx[ii] = 0.0; vy[ii] = 0.0;
+                    dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
+                }
+            } else if (imeth == 2) {
+                if (igs[ii] == Adhes) {
+                    if (ix + 1 + kdown <= mx) {
+                        vx[ii] = vx[ii + 1] + dxi[ii] - dxi[ii + kdown];
+                        vy[ii] = vy[ii + 1] + dyi[ii] - dyi[ii + kdown];
+                    } else { vx[ii] = vx[ii + 1] + dxi[ii]; vy[ii] = vy[ii + 1] + dyi[ii]; }
+                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                } else {
+                    if (igs[ii] == Slip) {
+                        double vt = tx * dxi[ii] + ty * dyi[ii];
+                        vt = dsign(1.0, vt) * fmin(fabs(vt), fac_v * trc[ii]);
+                        vx[ii] = tx * vt; vy[ii] = ty * vt;
+                        dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                    } else {
+                        vx[ii] = 0.0; vy[ii] = 0.0;
+                        dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
+                    }
+                    for (int kk = 1; kk <= kdown; kk++) if (ix + 1 + kk <= mx) { dxi[ii + kk] = 0.0; dyi[ii + kk] = 0.0; }
+                }
+            } else {
+                if (igs[ii] == Adhes) {
+                    vx[ii] = d.fdecay * vx[ii + 1] + dvx[ii]; vy[ii] = d.fdecay * vy[ii + 1] + dvy[ii];
+                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                } else if (igs[ii] == Slip) {
+                    double vt = tx * dvx[ii] + ty * dvy[ii];
+                    vt = dsign(1.0, vt) * fmin(fabs(vt), fac_v * trc[ii]);
+                    vx[ii] = tx * vt; vy[ii] = ty * vt;
+                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                } else {
+                    vx[ii] = 0.0; vy[ii] = 0.0;
+                    dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
+                }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// unit direction of the tangential traction: (cos, sin) of atan2(py, px), with (1, 0) for p = 0
+__device__ inline void unit_dir(double px, double py, double &nx, double &ny) {
+    double r = sqrt(px * px + py * py);
+    if (r > 0.0) { nx = px / r; ny = py / r; }
+    else { nx = (px < 0.0 || (px == 0.0 && signbit(px))) ? -1.0 : 1.0; ny = 0.0; if (signbit(py) && px == 0.0) nx = 1.0; }
+}
+
+// compute_diagscaling, gdsteady.f90:901-1042.  In the reference 'elnew' and 'fac_s' carry over
+// from one element to the next.  The carried values reach (a) exterior elements, whose
+// scaling is never used (their residual and line-search terms are zero), and (b) slip
+// elements whose angle error stays below tiny_err after the perturbation.  All other
+// elements are independent and are handled in parallel; when a case (b) element exists the
+// whole pass is repeated serially with the reference's carry-over.
+__device__ inline double dscl_adhesion(const PatchDesc &d, const int *igs, int ii, int mx, double old) {
+    const int ix = ii % mx + 1;
+    int jx = ix;
+    while (jx > 1 && igs[ii - ix + jx] == Adhes) jx--;
+    double dn;
+    if (d.d_cns < d.d_ifc) dn = fmax(d.d_cns, d.d_ifc + (ix - jx - 1) * fmin(0.0, d.d_lin));
+    else dn = fmin(d.d_cns, d.d_ifc + (ix - jx - 1) * fmax(0.0, d.d_lin));
+    return fmin(50.0 * old, dn);
+}
+
+// angle error of a slip element (perturbed once when it is tiny); returns false if it stays tiny
+__device__ inline bool slip_element(const PatchDesc &d, const double coefs[2][2], double px, double py, double pn,
+                                    double sx, double sy, int &elnew, double &fac_s) {
+    const double tiny_err = 1e-6, pi = 3.14159265358979323846;
+    double pr[3] = {px, py, pn};
+    double si[2] = {sx, sy};
+    double th_p0 = atan2(pr[1], pr[0]);
+    double th_s0 = atan2(-si[1], -si[0]);
+    double err_0 = th_s0 - th_p0;
+    if (fabs(err_0) >= pi) err_0 = err_0 - rint(err_0 / (2.0 * pi)) * 2.0 * pi;
+    if (fabs(err_0) <= tiny_err) {
+        double c, s; sincos(th_p0 + 0.1, &s, &c);
+        pr[0] = d.fstat * pr[2] * c;
+        pr[1] = d.fstat * pr[2] * s;
+        si[0] = sx + coefs[0][0] * (pr[0] - px) + coefs[0][1] * (pr[1] - py);
+        si[1] = sy + coefs[1][0] * (pr[0] - px) + coefs[1][1] * (pr[1] - py);
+        th_p0 = atan2(pr[1], pr[0]);
+        th_s0 = atan2(-si[1], -si[0]);
+        err_0 = th_s0 - th_p0;
+        if (fabs(err_0) >= pi) err_0 = err_0 - rint(err_0 / (2.0 * pi)) * 2.0 * pi;
+    }
+    if (fabs(err_0) <= tiny_err) return false;
+    elnew = Slip;
+    elm_solve(elnew, coefs, 1e-6, 1.0, 1.0, pr, d.fstat, si);
+    if (elnew == Slip) {
+        const double th_s1 = atan2(-si[1], -si[0]);
+        double upd_s = th_s1 - th_s0;
+        if (fabs(upd_s) >= pi) upd_s = upd_s - rint(upd_s / (2.0 * pi)) * 2.0 * pi;
+        fac_s = fabs(upd_s) / fabs(err_0);
+    }
+    return true;
+}
+
+__device__ __noinline__ void compute_diagscaling(const PView &P, const double coefs[2][2]) {
+    const PatchDesc &d = *P.d;
+    __syncthreads();
+    PHASE_START(tdg);
+    const int mx = P.mx, n = P.n;
+    const int *igs = P.igs();
+    const double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN), *sx = P.c(W_SX), *sy = P.c(W_SY);
+    double *dscl = P.c(W_DSCL);
+    int ndeg = 0;
+    FOR_I(ii, n) {
+        const int el = igs[ii];
+        if (el == Slip) {
+            int elnew = Slip;
+            double fac_s = 0.0;
+            if (!slip_element(d, coefs, px[ii], py[ii], pn[ii], sx[ii], sy[ii], elnew, fac_s)) ndeg++;
+            else if (elnew == Slip) dscl[ii] = d.d_slp * pow(fac_s, d.pow_s);
+            else dscl[ii] = dscl_adhesion(d, igs, ii, mx, dscl[ii]);
+        } else if (el == Adhes) {
+            dscl[ii] = dscl_adhesion(d, igs, ii, mx, dscl[ii]);
+        } else {
+            dscl[ii] = 0.0;
+        }
+    }
+    ndeg = block_sumi1(P.sm->red, ndeg);
+    if (ndeg > 0 && threadIdx.x == 0) {
+        // serial pass with the reference's carry-over of elnew and fac_s (elements in order)
+        int elnew = Exter;
+        double fac_s = 0.0;
+        for (int ii = 0; ii < n; ii++) {
+            const int el = igs[ii];
+            if (el == Slip) {
+                int e2 = el;
+                double f2 = fac_s;
+                if (slip_element(d, coefs, px[ii], py[ii], pn[ii], sx[ii], sy[ii], e2, f2)) { elnew = e2; fac_s = f2; }
+            }
+            if (el == Slip && elnew == Slip) dscl[ii] = d.d_slp * pow(fac_s, d.pow_s);
+            else if (el == Adhes || elnew == Adhes) dscl[ii] = dscl_adhesion(d, igs, ii, mx, dscl[ii]);
+            else dscl[ii] = 0.0;
+        }
+    }
+    __syncthreads();
+    PHASE_END(P, O_T_DIAG - O_T_TOTAL, tdg);
+}
+
+// perform_linesearch, gdsteady.f90:1046-1462.  Evaluations of rho(alpha) are block-parallel;
+// the Brent bookkeeping runs on thread 0 with the table in shared memory.
+template <int DUMMY = 0>
+__device__ __noinline__ bool perform_linesearch(const PView &P, double alpha0, double &alpha_out, int &jout) {
+    PHASE_START(tls);
+    const int n = P.n;
+    SolverSmem &S = *P.sm;
+    RedSmem &red = S.red;
+    const int *igs = P.igs();
+    const double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY), *dvx = P.c(W_DVX), *dvy = P.c(W_DVY);
+    const double *vx = P.c(W_VX), *vy = P.c(W_VY), *qx = P.c(W_QX), *qy = P.c(W_QY);
+    const double *sx = P.c(W_SX), *sy = P.c(W_SY), *nox = P.c(W_NX), *noy = P.c(W_NY);
+    const double *dscl = P.c(W_DSCL), *trc = P.c(W_TRC);
+    double *pdx = P.c(W_PDX), *pdy = P.c(W_PDY), *pnx = P.c(W_PNX), *pny = P.c(W_PNY);
+    const double tiny = 1e-12, eps_j = 0.001;
+    // thread-0 state
+    int itb_a = 0, itb_b = 0, itb_x = 0, itb_w = 0, itb_v = 0, itb_u = 0;
+    double dst_cur = 0, dst_prv1 = 0, dst_prv2 = 0, ddrho = 0, alpha_prv = -1.0;
+    bool has_bracket = false;
+    int j = 0;
+    if (threadIdx.x == 0) { S.alpha_j = 0.0; S.stop_j = 0; S.nobracket = 0; }
+    __syncthreads();
+    for (int guard = 0; guard < kMaxLs + 1; guard++) {
+        const double alpha_j = S.alpha_j;
+        FOR_I(i, n) {
+            if (igs[i] >= Adhes) { pdx[i] = dpx[i] + alpha_j * dvx[i]; pdy[i] = dpy[i] + alpha_j * dvy[i]; }
+            else { pdx[i] = dpx[i]; pdy[i] = dpy[i]; }
+        }
+        apply_trcbnd(P, trc, pdx, pdy, pnx, pny);
+        double acc[4] = {0, 0, 0, 0};     // rho, c0, c1, c2
+        FOR_I(ii, n) {
+            const double txo = -noy[ii], tyo = nox[ii];
+            const double vt = vx[ii] * txo + vy[ii] * tyo;
+            const double tb = trc[ii];
+            const double dth_da = (tb * vt) / (fmax(tiny, tb * tb) + alpha_j * alpha_j * vt * vt);
+            double nxn, nyn;
+            unit_dir(pnx[ii], pny[ii], nxn, nyn);
+            const double txn = -nyn, tyn = nxn;
+            const double s_x = sx[ii], s_y = sy[ii], q_x = qx[ii], q_y = qy[ii];
+            const double sn = s_x * nxn + s_y * nyn;
+            int elnew = igs[ii];
+            if (elnew == Slip && sn > 0.0) elnew = Adhes;
+            const double st = s_x * txn + s_y * tyn, rt = -st;
+            const double qn = q_x * nxn + q_y * nyn, qt = q_x * txn + q_y * tyn;
+            const double d2 = dscl[ii] * dscl[ii];
+            if (elnew == Adhes) {
+                acc[1] += 2.0 * d2 * (s_x * q_x + s_y * q_y);
+                acc[2] += 2.0 * d2 * (q_x * q_x + q_y * q_y);
+                acc[0] += d2 * ((s_x + alpha_j * q_x) * (s_x + alpha_j * q_x) + (s_y + alpha_j * q_y) * (s_y + alpha_j * q_y));
+            } else if (elnew == Slip) {
+                acc[1] -= 2.0 * d2 * (rt * qt - rt * sn * dth_da);
+                acc[2] -= 2.0 * d2 * (-qt * qt + qt * sn * dth_da - rt * qn * dth_da);
+                acc[3] -= 2.0 * d2 * (qt * qn * dth_da);
+                acc[0] += d2 * (st + alpha_j * qt) * (st + alpha_j * qt);
+            }
+        }
+        block_sum<4>(red, acc);
+        if (threadIdx.x == 0) {
+            double *ta = S.tbl_alpha, *tr = S.tbl_rho, *td = S.tbl_drhoda;
+            const double rhonew = acc[0];
+            const double drho_da = acc[1] + alpha_j * acc[2] + alpha_j * alpha_j * acc[3];
+            int itb = 1;
+            while (itb <= j && alpha_j > ta[itb]) itb++;
+            itb_u = itb;
+            for (int k = j; k >= itb; k--) { ta[k + 1] = ta[k]; tr[k + 1] = tr[k]; td[k + 1] = td[k]; }
+            if (has_bracket) {
+                if (itb_a >= itb_u) itb_a++;
+                if (itb_b >= itb_u) itb_b++;
+                if (itb_x >= itb_u) itb_x++;
+                if (itb_w >= itb_u) itb_w++;
+                if (itb_v >= itb_u) itb_v++;
+            }
+            j++;
+            ta[itb] = alpha_j; tr[itb] = rhonew; td[itb] = drho_da;
+            bool prev_bracket = has_bracket;
+            has_bracket = false;
+            int ibrack = 1;
+            while (ibrack < j - 1 && !has_bracket) {
+                has_bracket = (tr[ibrack + 1] <= fmin(tr[ibrack], tr[ibrack + 2]));
+                if (!has_bracket) ibrack++;
+            }
+            if (has_bracket && !prev_bracket) {
+                itb_a = ibrack; itb_x = ibrack + 1; itb_b = ibrack + 2;
+                if (tr[itb_a] < tr[itb_b]) { itb_w = itb_a; itb_v = itb_b; }
+                else { itb_w = itb_b; itb_v = itb_a; }
+                dst_prv1 = ta[itb_x] - ta[itb_w];
+                dst_prv2 = ta[itb_w] - ta[itb_v];
+            } else if (has_bracket) {
+                if (tr[itb_u] <= tr[itb_x]) {
+                    if (ta[itb_u] >= ta[itb_x]) itb_a = itb_x; else itb_b = itb_x;
+                    itb_v = itb_w; itb_w = itb_x; itb_x = itb_u;
+                } else {
+                    if (ta[itb_u] < ta[itb_x]) itb_a = itb_u; else itb_b = itb_u;
+                    if (tr[itb_u] <= tr[itb_w] || ta[itb_w] == ta[itb_x]) { itb_v = itb_w; itb_w = itb_u; }
+                    else if (tr[itb_u] <= tr[itb_v] || ta[itb_v] == ta[itb_x] || ta[itb_v] == ta[itb_w]) itb_v = itb_u;
+                }
+                dst_prv2 = dst_prv1;
+                dst_prv1 = dst_cur;
+            }
+            alpha_prv = alpha_j;
+            double anew = alpha_j;
+            if (has_bracket) {
+                double xmid = 0.5 * (ta[itb_a] + ta[itb_b]);
+                double tolx = eps_j * fabs(ta[itb_x]) + tiny;
+                bool ldone = (fabs(ta[itb_x] - xmid) <= 2.0 * tolx - 0.5 * (ta[itb_b] - ta[itb_a]));
+                if (!ldone) {
+                    bool use_parab;
+                    if (fabs(dst_prv2) <= tolx) use_parab = false;
+                    else {
+                        double br = (ta[itb_x] - ta[itb_w]) * (tr[itb_x] - tr[itb_v]);
+                        double bq = (ta[itb_x] - ta[itb_v]) * (tr[itb_x] - tr[itb_w]);
+                        double bp = (ta[itb_x] - ta[itb_v]) * bq - (ta[itb_x] - ta[itb_w]) * br;
+                        bq = 2.0 * (bq - br);
+                        if (bq > 0.0) bp = -bp;
+                        bq = fabs(bq);
+                        if (fabs(bp) >= fabs(0.5 * bq * dst_prv2) || bp <= bq * (ta[itb_a] - ta[itb_x]) ||
+                            bp >= bq * (ta[itb_b] - ta[itb_x])) {
+                            use_parab = false;
+                        } else {
+                            use_parab = true;
+                            dst_cur = bp / bq;
+                            double at = ta[itb_x] + dst_cur;
+                            if (at - ta[itb_a] < 2.0 * tolx || ta[itb_b] - at < 2.0 * tolx)
+                                dst_cur = tolx * dsign(1.0, xmid - ta[itb_x]);
+                        }
+                    }
+                    if (!use_parab) {
+                        if (ta[itb_x] >= xmid) dst_prv1 = ta[itb_a] - ta[itb_x];
+                        else dst_prv1 = ta[itb_b] - ta[itb_x];
+                        dst_cur = 0.381966 * dst_prv1;
+                    }
+                    anew = ta[itb_x] + dst_cur;
+                }
+            } else if (j == 1) {
+                anew = alpha_j + 0.6 * alpha0;
+                ddrho = 10.0;
+            } else if (tr[j] < tr[1]) {
+                int ib = j - 1;
+                double dal = ta[ib + 1] - ta[ib];
+                if (j < 3) { ddrho = (td[ib + 1] - td[ib]) / dal; anew = ta[ib + 1] + fmin(3.0 * dal, -td[ib] / ddrho); }
+                else anew = ta[ib + 1] + 3.0 * dal;
+            } else {
+                int ib = 1;
+                double dal = ta[ib + 1] - ta[ib];
+                if (j < 3) { ddrho = (td[ib + 1] - td[ib]) / dal; anew = ta[ib] + fmin(-3.0 * dal, td[ib] / ddrho); }
+                else anew = ta[ib] - 3.0 * dal;
+            }
+            bool stop = (j >= kMaxLs || fabs(anew - alpha_prv) < eps_j * fmax(fabs(anew), fabs(alpha_prv)));
+            if (stop) {
+                if (!has_bracket) S.nobracket = 1;
+                if (j >= kMaxLs) {
+                    int best = 1;
+                    for (int k = 2; k <= kMaxLs; k++) if (tr[k] < tr[best]) best = k;
+                    anew = ta[best];
+                }
+            }
+            S.alpha_j = anew;
+            S.stop_j = stop ? 1 : 0;
+            S.jcount = j;
+        }
+        __syncthreads();
+        if (S.stop_j) break;
+    }
+    alpha_out = S.alpha_j;
+    jout = S.jcount;
+    bool ok = !S.nobracket;
+    __syncthreads();
+    PHASE_END(P, O_T_LS - O_T_TOTAL, tls);
+    return ok;
+}
+
+// slip s = A dp + ws on the interior (zero elsewhere)
+template <typename T>
+__device__ __noinline__ void compute_slip(const PView &P, const Ops<T> &op, int &nconv) {
+    const int n = P.n;
+    int *igs = P.igs();
+    double *sx = P.c(W_SX), *sy = P.c(W_SY);
+    const double *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+    FOR_I(i, n) { sx[i] = 0.0; sy[i] = 0.0; }
+    prod_t<T>(op, P.c(W_DPX), P.c(W_DPY), sx, sy, OUT_INT, igs); nconv++;
+    FOR_I(i, n) if (igs[i] >= Adhes) { sx[i] += wsx[i]; sy[i] += wsy[i]; }
+    __syncthreads();
+}
+
+__device__ __noinline__ void set_nt(const PView &P) {
+    const double *px = P.c(W_PX), *py = P.c(W_PY);
+    double *nx = P.c(W_NX), *ny = P.c(W_NY);
+    FOR_I(i, P.n) unit_dir(px[i], py[i], nx[i], ny[i]);
+    __syncthreads();
+}
+
+__device__ __noinline__ void set_residual(const PView &P) {
+    const int *igs = P.igs();
+    const double *sx = P.c(W_SX), *sy = P.c(W_SY), *nx = P.c(W_NX), *ny = P.c(W_NY), *dscl = P.c(W_DSCL);
+    double *rx = P.c(W_RX), *ry = P.c(W_RY);
+    FOR_I(i, P.n) {
+        if (igs[i] == Adhes) { rx[i] = -sx[i] * dscl[i]; ry[i] = -sy[i] * dscl[i]; }
+        else if (igs[i] == Slip) {
+            const double tx = -ny[i], ty = nx[i];
+            double st = tx * sx[i] + ty * sy[i];
+            rx[i] = -st * tx * dscl[i]; ry[i] = -st * ty * dscl[i];
+        } else { rx[i] = 0.0; ry[i] = 0.0; }
+    }
+    __syncthreads();
+}
+
+// gdsteady, gdsteady.f90:9-606 (elastic).  Returns itgd (negated on stagnation);
+// lstagn as in the reference; returns -100000 when the line search has no bracket.
+template <typename T>
+__device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd, double eps, double &err, bool &lstagn,
+                        int &nconv, int &nls) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n, mx = P.mx, my = P.my;
+    RedSmem &red = P.sm->red;
+    int *igs = P.igs(), *igsold = P.ci(I_OLD);
+    double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN);
+    double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY), *trc = P.c(W_TRC), *dscl = P.c(W_DSCL);
+    double *rx = P.c(W_RX), *ry = P.c(W_RY), *dvx = P.c(W_DVX), *dvy = P.c(W_DVY);
+    double *qx = P.c(W_QX), *qy = P.c(W_QY), *pox = P.c(W_POX), *poy = P.c(W_POY);
+    double *sx = P.c(W_SX), *sy = P.c(W_SY), *nx = P.c(W_NX), *ny = P.c(W_NY);
+    const double tiny = 1e-12;
+    const size_t bsz = (size_t)4 * mx * my;
+    const size_t o0 = (size_t)mx + (size_t)my * 2 * mx;
+    double coefs[2][2];
+    coefs[0][0] = d.cf[0 * bsz + o0] / d.ga;
+    coefs[0][1] = d.cf[1 * bsz + o0] / d.ga;
+    coefs[1][0] = coefs[0][1];
+    coefs[1][1] = d.cf[2 * bsz + o0] / d.ga;
+    int nadh, nslip, nplast, nexter;
+    count_eldiv(P, nadh, nslip, nplast, nexter);
+    const double facnel = sqrt((double)(float)n / (double)(float)(nadh + nslip + nplast));
+    FOR_I(i, n) { trc[i] = d.fstat * pn[i]; dscl[i] = 1.0; }
+    // compute_dp
+    FOR_I(ii, n) {
+        int ix = ii % mx;
+        if (ix == mx - 1) { dpx[ii] = px[ii]; dpy[ii] = py[ii]; }
+        else { dpx[ii] = px[ii] - px[ii + 1]; dpy[ii] = py[ii] - py[ii + 1]; }
+    }
+    __syncthreads();
+    int itgd = 0, it_fb = -99;
+    double dif = 2.0, difid = 1.0, dif1 = 0.0, beta = 1.0, alpha = 0.0, alpha0 = 0.0;
+    bool lchanged = false;
+    lstagn = false;
+    set_nt(P);
+    compute_slip<T>(P, op, nconv);
+    compute_diagscaling(P, coefs);
+    set_residual(P);
+    {
+        double m = 0.0; FOR_I(i, n) m = fmax(m, fmax(fabs(rx[i]), fabs(ry[i])));
+        m = block_max1(red, m);
+        if (m < tiny) dif = 0.0;
+    }
+    while ((lchanged || dif > difid) && itgd < maxgd) {
+        itgd++;
+        FOR_I(i, n) { dvx[i] = rx[i]; dvy[i] = ry[i]; }
+        int imeth, kdown;
+        if (beta > d.betath || itgd - it_fb <= 1) { imeth = d.gd_meth; kdown = d.kdown; }
+        else { imeth = 2; kdown = d.kdowfb; it_fb = itgd; }
+        project_searchdir(P, imeth, kdown, trc);
+        prod_t<T>(op, dvx, dvy, qx, qy, OUT_INT, igs); nconv++;
+        if (itgd <= 1) {
+            double a[2] = {0, 0};
+            FOR_I(i, n) { a[0] += rx[i] * rx[i] + ry[i] * ry[i]; a[1] += (rx[i] * qx[i] + ry[i] * qy[i]) * dscl[i]; }
+            block_sum<2>(red, a);
+            alpha0 = a[0] / a[1];
+        } else {
+            alpha0 = 0.5 * (alpha0 + alpha);
+        }
+        int its_j = 0;
+        if (!perform_linesearch(P, alpha0, alpha, its_j)) { err = dif; return -100000; }
+        nls += its_j;
+        {
+            double a[2] = {0, 0};
+            FOR_I(i, n) if (igs[i] >= Adhes) {
+                double a0 = dscl[i] * qx[i], a1 = dscl[i] * qy[i];
+                a[0] += a0 * a0 + a1 * a1;
+                a[1] += rx[i] * rx[i] + ry[i] * ry[i];
+            }
+            block_sum<2>(red, a);
+            beta = alpha * sqrt(a[0]) / sqrt(a[1]);
+        }
+        FOR_I(i, n) {
+            igsold[i] = igs[i];
+            pox[i] = px[i]; poy[i] = py[i];
+            if (igs[i] >= Adhes) { dpx[i] += alpha * dvx[i]; dpy[i] += alpha * dvy[i]; }
+        }
+        apply_trcbnd(P, trc, dpx, dpy, px, py);
+        set_nt(P);
+        compute_slip<T>(P, op, nconv);
+        // local optimisation (solve_elmtrc) and active-set updates
+        int chg = 0;
+        FOR_I(ii, n) {
+            if (igsold[ii] == Slip) {
+                double pr[3] = {px[ii], py[ii], pn[ii]};
+                double si[2] = {sx[ii], sy[ii]};
+                int elnew = igs[ii];
+                elm_solve(elnew, coefs, 1e-6, 1.0, 1.0, pr, d.fstat, si);
+                double snrm = nx[ii] * sx[ii] + ny[ii] * sy[ii];
+                double cosdth = (nx[ii] * pr[0] + ny[ii] * pr[1]) / trc[ii];
+                // the A->S test below only sees elements that were in adhesion
+                if ((snrm > 0.0 && (dscl[ii] >= 0.001 || elnew == Adhes)) || cosdth <= -0.5) { igs[ii] = Adhes; chg = 1; }
+            } else if (igs[ii] == Adhes) {
+                double ptabs = sqrt(px[ii] * px[ii] + py[ii] * py[ii]);
+                if (ptabs >= trc[ii] - tiny) { igs[ii] = Slip; chg = 1; }
+            }
+        }
+        chg = block_sumi1(red, chg);
+        lchanged = chg > 0;
+        compute_diagscaling(P, coefs);
+        set_residual(P);
+        double facdif;
+        if (beta >= 0.1) facdif = 1.0;
+        else if (beta >= 0.001) facdif = 0.1 / beta;
+        else facdif = 100.0;
+        {
+            double a[2] = {0, 0};
+            FOR_I(i, n) {
+                double ex = pox[i] - px[i], ey = poy[i] - py[i];
+                a[0] += ex * ex + ey * ey;
+                a[1] += px[i] * px[i] + py[i] * py[i];
+            }
+            block_sum<2>(red, a);
+            dif = facnel * sqrt(a[0] / (2 * n)) * facdif;
+            difid = eps * fmax(1e-6, facnel * sqrt(a[1] / (2 * n)));
+        }
+        if (itgd == 1) dif1 = dif;
+    }
+    double resrms;
+    {
+        double a = 0; int c = 0;
+        FOR_I(i, n) if (igs[i] >= Adhes) { a += rx[i] * rx[i] + ry[i] * ry[i]; c += 2; }
+        a = block_sum1(red, a); c = block_sumi1(red, c);
+        resrms = sqrt(a / max(1, c));
+    }
+    double res_dp = resrms / fmax(coefs[0][0], coefs[1][1]);
+    err = dif;
+    double conv = 1.0;
+    if (dif * dif1 > 0.0 && itgd > 1) conv = exp(log(dif / dif1) / (itgd - 1));
+    if (lchanged && itgd >= maxgd) lstagn = true;
+    else if (dif > difid && conv > 1.0 && itgd >= maxgd) lstagn = true;
+    else if (conv < 1.0 - tiny && res_dp > 5.0 * difid / (1.0 - conv)) { itgd = -itgd; lstagn = true; }
+    return itgd;
+}
+
+// ------------------------------------------------------------------------------------------
+// TangCG, m_solvpt.f90:1841-2442 (elastic).  The FFT preconditioner uses blocks xx, yy of
+// the preconditioner spectra, evaluated at the convolution's FFT size.
+// ------------------------------------------------------------------------------------------
+template <typename T>
+__device__ __noinline__ int tangcg(const PView &P, const Ops<T> &op, const T *Mxx, const T *Myy, int maxcg, double eps,
+                      double &err, int &nconv) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n, my = P.my, mx = P.mx;
+    RedSmem &red = P.sm->red;
+    int *igs = P.igs();
+    double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN), *g = P.c(W_TRC);
+    double *sx = P.c(W_SX), *sy = P.c(W_SY), *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+    double *nx = P.c(W_NX), *ny = P.c(W_NY), *rx = P.c(W_RX), *ry = P.c(W_RY);
+    double *zx = P.c(W_ZX), *zy = P.c(W_ZY), *vx = P.c(W_VX), *vy = P.c(W_VY);
+    double *qx = P.c(W_QX), *qy = P.c(W_QY), *pox = P.c(W_POX), *poy = P.c(W_POY);
+    const size_t bsz = (size_t)4 * mx * my;
+    const size_t o0 = (size_t)mx + (size_t)my * 2 * mx;
+    const double cxx = d.cf[0 * bsz + o0], cyy = d.cf[2 * bsz + o0], ga = d.ga;
+    const int num_inn = 4;
+    const double small = 1e-6;
+    bool use_fftprec = true;
+    int nadh, nslip, nplast, nexter;
+    count_eldiv(P, nadh, nslip, nplast, nexter);
+    const double facnel = sqrt((double)(float)n / (double)(float)(nadh + nslip + nplast));
+    FOR_I(i, n) g[i] = d.fstat * pn[i];
+    int itcg = 0, it_inn = 0;
+    double dif = 2.0, difid = 1.0, difinn = 0.0, alpha = 0.0, trsinn = 0.0;
+    bool lchanged = false;
+    set_nt(P);
+    FOR_I(i, n) { sx[i] = 0.0; sy[i] = 0.0; }
+    prod_t<T>(op, px, py, sx, sy, OUT_INT, igs); nconv++;
+    auto set_r = [&]() {
+        FOR_I(i, n) {
+            double r0 = -sx[i], r1 = -sy[i];
+            if (igs[i] == Slip) {
+                const double tx = -ny[i], ty = nx[i];
+                double perp = tx * r0 + ty * r1; r0 = perp * tx; r1 = perp * ty;
+            }
+            rx[i] = r0; ry[i] = r1;
+        }
+        __syncthreads();
+    };
+    FOR_I(i, n) if (igs[i] >= Adhes) { sx[i] += wsx[i]; sy[i] += wsy[i]; }
+    __syncthreads();
+    set_r();
+    while ((lchanged || dif > difid) && itcg < maxcg) {
+        itcg++; it_inn++;
+        if (use_fftprec) {
+            if (nslip + nplast > 3 * nadh && my > 1) use_fftprec = false;
+            if (itcg >= maxcg / 2) use_fftprec = false;
+            if (!use_fftprec) lchanged = true;
+        }
+        if (use_fftprec) {
+            convolve<T>(op.cv, rx, nullptr, zx, nullptr, 1, Mxx, nullptr, nullptr, OUT_INT, igs);
+            convolve<T>(op.cv, ry, nullptr, zy, nullptr, 1, Myy, nullptr, nullptr, OUT_INT, igs);
+            nconv++;
+        } else {
+            FOR_I(i, n) { zx[i] = rx[i]; zy[i] = ry[i]; }
+        }
+        FOR_I(i, n) {
+            double z0 = zx[i], z1 = zy[i];
+            if (igs[i] == Slip) {
+                double snrm = -sx[i] * nx[i] - sy[i] * ny[i];
+                z0 = z0 / (cxx + ga * snrm / g[i]);
+                z1 = z1 / (cyy + ga * snrm / g[i]);
+                const double tx = -ny[i], ty = nx[i];
+                double perp = tx * z0 + ty * z1; z0 = perp * tx; z1 = perp * ty;
+            } else {
+                z0 = z0 / cxx; z1 = z1 / cyy;
+            }
+            zx[i] = z0; zy[i] = z1;
+        }
+        __syncthreads();
+        if (itcg <= 1 || lchanged) {
+            FOR_I(i, n) { vx[i] = zx[i]; vy[i] = zy[i]; }
+        } else {
+            double a[2] = {0, 0};
+            FOR_I(i, n) { a[0] += zx[i] * qx[i] + zy[i] * qy[i]; a[1] += vx[i] * qx[i] + vy[i] * qy[i]; }
+            block_sum<2>(red, a);
+            double zq = a[0], vq = a[1], beta;
+            if (fabs(zq) < 1e-60 || fabs(vq) < small * fabs(zq)) beta = 0.0;
+            else beta = -zq / vq;
+            FOR_I(i, n) { vx[i] = beta * vx[i] + zx[i]; vy[i] = beta * vy[i] + zy[i]; }
+        }
+        __syncthreads();
+        prod_t<T>(op, vx, vy, qx, qy, OUT_INT, igs); nconv++;
+        FOR_I(i, n) if (igs[i] == Slip) {
+            const double tx = -ny[i], ty = nx[i];
+            double perp = tx * qx[i] + ty * qy[i];
+            double q0 = perp * tx, q1 = perp * ty;
+            double snrm = (nx[i] * sx[i] + ny[i] * sy[i]) / g[i];
+            qx[i] = q0 - snrm * vx[i]; qy[i] = q1 - snrm * vy[i];
+        }
+        double rv, vq;
+        {
+            double a[2] = {0, 0};
+            FOR_I(i, n) { a[0] += rx[i] * vx[i] + ry[i] * vy[i]; a[1] += vx[i] * qx[i] + vy[i] * qy[i]; }
+            block_sum<2>(red, a);
+            rv = a[0]; vq = a[1];
+        }
+        if (fabs(rv) < 1e-60) alpha = 0.0;
+        else if (fabs(vq) < small * fabs(rv)) alpha = 1.0;
+        else alpha = rv / vq;
+        {
+            double a[2] = {0, 0};
+            FOR_I(i, n) {
+                pox[i] = px[i]; poy[i] = py[i];
+                if (igs[i] >= Adhes) { px[i] += alpha * vx[i]; py[i] += alpha * vy[i]; }
+                if (igs[i] == Slip) {
+                    double ptabs = sqrt(px[i] * px[i] + py[i] * py[i]);
+                    px[i] = px[i] * g[i] / ptabs; py[i] = py[i] * g[i] / ptabs;
+                }
+                a[0] += vx[i] * vx[i] + vy[i] * vy[i];
+                a[1] += px[i] * px[i] + py[i] * py[i];
+            }
+            block_sum<2>(red, a);
+            dif = alpha * facnel * sqrt(a[0] / (2 * n));
+            difinn += dif;
+            if (itcg <= 5 || itcg % 5 == 1) {
+                double ptang = facnel * sqrt(a[1] / (2 * n));
+                difid = eps * fmax(1e-6, ptang);
+                trsinn = (double)0.01f * ptang;
+            }
+        }
+        if (it_inn >= num_inn || dif <= difid || difinn > trsinn) {
+            int chg = 0;
+            FOR_I(i, n) if (igs[i] == Adhes) {
+                double ptabs = sqrt(px[i] * px[i] + py[i] * py[i]);
+                if (ptabs > g[i]) {
+                    igs[i] = Slip; px[i] = px[i] * g[i] / ptabs; py[i] = py[i] * g[i] / ptabs; chg = 1;
+                }
+            }
+            prod_t<T>(op, px, py, sx, sy, OUT_INT, igs); nconv++;
+            FOR_I(i, n) if (igs[i] >= Adhes) { sx[i] += wsx[i]; sy[i] += wsy[i]; }
+            FOR_I(i, n) if (igs[i] == Slip) {
+                double snrm = sx[i] * px[i] + sy[i] * py[i];
+                if (snrm > 0.0) { igs[i] = Adhes; chg = 1; }
+            }
+            chg = block_sumi1(red, chg);
+            lchanged = chg > 0;
+            double a = 0;
+            FOR_I(i, n) { double ex = pox[i] - px[i], ey = poy[i] - py[i]; a += ex * ex + ey * ey; }
+            a = block_sum1(red, a);
+            dif = facnel * sqrt(a / (2 * n));
+            it_inn = 0;
+            difinn = 0.0;
+            if (lchanged) count_eldiv(P, nadh, nslip, nplast, nexter);
+        }
+        if ((lchanged || dif > difid) && itcg < maxcg) {
+            if (it_inn <= 0) { set_nt(P); set_r(); }
+            else { FOR_I(i, n) if (igs[i] >= Adhes) { rx[i] -= alpha * qx[i]; ry[i] -= alpha * qy[i]; } __syncthreads(); }
+        }
+    }
+    err = dif;
+    return itcg;
+}
+
+} // namespace cgb

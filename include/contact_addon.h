@@ -1,0 +1,121 @@
+/*
+ * contact_addon.h -- C-ABI of the GB300 rolling-contact library.
+ *
+ * A drop-in for the module-3 part of CONTACT's library interface: same lowercase
+ * symbol names, same argument lists (every argument by pointer, Fortran bind(c)
+ * convention), same argument meaning and units.  The reference prototypes are in
+ * matlab_intfc/contact_addon.h; the Fortran implementations are cited per function
+ * below (file:line in src/contact_addon.f90 unless stated otherwise).
+ *
+ * Additions (no counterpart in the reference):
+ *   cntc_calculate_batch        solve many (ire,icp) problems in one pass of the engine
+ *   cntc_getiterationcounts     iteration counts / solver used of the last solve
+ *   cntc_gb300_kernel_launches  number of GPU kernels this library has launched
+ *   cntc_gb300_getsolverstats   convolution counts and per-phase cycle counts of the last solve
+ *   flag CNTC_if_mixedprec      (cntc_setflags) 1: FP32 convolutions + FP64 refinement
+ */
+#ifndef CONTACT_GB300_ADDON_H
+#define CONTACT_GB300_ADDON_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* library extension flag for cntc_setflags: 0 = FP64 throughout (default), 1 = FP32 bulk
+ * convolutions followed by an FP64 refinement phase to the requested tolerance */
+#define CNTC_if_mixedprec 2010
+
+/* initialisation: cntc_initializeFirst 235-442, cntc_initializeFirst_new 446-472,
+ * cntc_initialize 476-576 */
+void cntc_initializefirst(int *ifcver, int *ierror, int *ioutput, const char *c_wrkdir,
+                          const char *c_outdir, const char *c_expnam, int *len_wrkdir,
+                          int *len_outdir, int *len_expnam);
+void cntc_initializefirst_new(int *ifcver, int *ierror, int *ioutput, const char *c_wrkdir,
+                              const char *c_outdir, const char *c_expnam, int *len_wrkdir,
+                              int *len_outdir, int *len_expnam);
+void cntc_initialize(int *ire, int *imodul, int *ifcver, int *ierror, const char *c_outdir,
+                     int *len_outdir);
+
+/* configuration: cntc_setGlobalFlags 580-725, cntc_setFlags 780-973,
+ * cntc_setSolverFlags 1128-1283, cntc_setMaterialParameters 1287-1473,
+ * cntc_setTemperatureData 1477-1550, cntc_setTimestep 1554-1583,
+ * cntc_setReferenceVelocity 1587-1615, cntc_setRollingStepsize 1619-1667,
+ * cntc_setFrictionMethod 1671-1968 */
+void cntc_setglobalflags(int *lenflg, int *params, int *values);
+void cntc_setflags(int *ire, int *icp, int *lenflg, int *params, int *values);
+void cntc_setsolverflags(int *ire, int *icp, int *gdigit, int *nints, int *iparam, int *nreals,
+                         double *rparam);
+void cntc_setmaterialparameters(int *ire, int *icp, int *mdigit, int *nparam, double *rparam);
+void cntc_settemperaturedata(int *ire, int *icp, int *imeth, int *nparam, double *rparam);
+void cntc_settimestep(int *ire, int *icp, double *dt);
+void cntc_setreferencevelocity(int *ire, int *icp, double *veloc);
+void cntc_setrollingstepsize(int *ire, int *icp, double *chi, double *dq);
+void cntc_setfrictionmethod(int *ire, int *icp, int *imeth, int *nparam, double *params);
+
+/* geometry and loading: cntc_setHertzContact 1972-2093, cntc_setPotContact 2097-2257,
+ * cntc_setPenetration 2294-2323, cntc_setNormalForce 2327-2357,
+ * cntc_setUndeformedDistc 2361-2487, cntc_setCreepages 2491-2530,
+ * cntc_setExtraRigidSlip 2534-2593, cntc_setTangentialForces 2597-2650 */
+void cntc_sethertzcontact(int *ire, int *icp, int *ipotcn, int *nparam, double *rparam);
+void cntc_setpotcontact(int *ire, int *icp, int *ipotcn, int *nparam, double *rparam);
+void cntc_setpenetration(int *ire, int *icp, double *pen);
+void cntc_setnormalforce(int *ire, int *icp, double *fn);
+void cntc_setundeformeddistc(int *ire, int *icp, int *ibase, int *nparam, double *prmudf);
+void cntc_setcreepages(int *ire, int *icp, double *vx, double *vy, double *phi);
+void cntc_setextrarigidslip(int *ire, int *icp, int *lenarr, double *wx, double *wy);
+void cntc_settangentialforces(int *ire, int *icp, double *fx, double *fy);
+
+/* computation: cntc_calculate 3519-3552 -> cntc_calculate3 3754-3900 */
+void cntc_calculate(int *ire, int *icp, int *ierror);
+/* extension: n problems (ire[i], icp[i]) solved together; ierror[i] as cntc_calculate */
+void cntc_calculate_batch(int *n, int *ire, int *icp, int *ierror);
+
+/* results: cntc_getFlags 4001-4160, cntc_getReferenceVelocity 4987-5017,
+ * cntc_getHertzContact 5021-5066, cntc_getNumElements 5070-5099,
+ * cntc_getGridDiscretization 5103-5140, cntc_getPotContact 5144-5187,
+ * cntc_getPenetration 5191-5220, cntc_getCreepages 5224-5271,
+ * cntc_getContactForces 5275-5318, cntc_getContactPatchAreas 5460-5497,
+ * cntc_getElementDivision 5501-5552, cntc_getMaximumPressure 5556-5587,
+ * cntc_getMaximumTraction 5591-5626, cntc_getFieldData 5672-5823,
+ * cntc_getTractions 5827-5855, cntc_getMicroSlip 5859-5885,
+ * cntc_getDisplacements 5889-5915, cntc_getSensitivities 5919-6007,
+ * cntc_getCalculationTime 6011-6040, cntc_resetCalculationTime 6044-6067 */
+void cntc_getflags(int *ire, int *icp, int *lenflg, int *params, int *values);
+void cntc_getreferencevelocity(int *ire, int *icp, double *veloc);
+void cntc_gethertzcontact(int *ire, int *icp, int *lenarr, double *values);
+void cntc_getnumelements(int *ire, int *icp, int *mx, int *my);
+void cntc_getgriddiscretization(int *ire, int *icp, double *dx, double *dy);
+void cntc_getpotcontact(int *ire, int *icp, int *lenarr, double *values);
+void cntc_getpenetration(int *ire, int *icp, double *pen);
+void cntc_getcreepages(int *ire, int *icp, double *vx, double *vy, double *phi);
+void cntc_getcontactforces(int *ire, int *icp, double *fn, double *tx, double *ty, double *mz);
+void cntc_getcontactpatchareas(int *ire, int *icp, double *carea, double *harea, double *sarea);
+void cntc_getelementdivision(int *ire, int *icp, int *lenarr, int *eldiv);
+void cntc_getmaximumpressure(int *ire, int *icp, double *pnmax);
+void cntc_getmaximumtraction(int *ire, int *icp, double *ptmax);
+void cntc_getfielddata(int *ire, int *icp, int *ifld, int *lenarr, double *fld);
+void cntc_gettractions(int *ire, int *icp, int *lenarr, double *pn, double *px, double *py);
+void cntc_getmicroslip(int *ire, int *icp, int *lenarr, double *sx, double *sy);
+void cntc_getdisplacements(int *ire, int *icp, int *lenarr, double *un, double *ux, double *uy);
+void cntc_getsensitivities(int *ire, int *icp, int *lenout, int *lenin, double *sens);
+void cntc_getcalculationtime(int *ire, int *icp, double *tcpu, double *twall);
+void cntc_resetcalculationtime(int *ire, int *icp);
+/* extension: [itnorm, ittang, itcg, itgs, solver id, ierror] of the last solve */
+void cntc_getiterationcounts(int *ire, int *icp, int *lenarr, int *values);
+
+/* clean-up: cntc_finalize 6243-6290, cntc_finalizeLast 6294-6375 */
+void cntc_finalize(int *ire);
+void cntc_finalizelast(void);
+
+/* extension: number of GPU kernels launched by this library since it was loaded */
+long long cntc_gb300_kernel_launches(void);
+/* extension: engine statistics of the last solve of (ire,icp): [0] FP32 convolutions,
+ * [1] FP64 convolutions, [2] line-search steps, [3] status bits, [4..11] SM clock cycles
+ * spent in: whole solve, convolutions, line search, diagonal scaling, Gauss-Seidel sweeps,
+ * normal problem, tangential problem, row scans */
+void cntc_gb300_getsolverstats(int *ire, int *icp, int *lenarr, double *values);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,167 @@
+"""Case descriptions shared by the parity tests and the benchmark.
+
+A case is a plain dict (see contact_gb300.setup_case for the keys).  The same dict
+drives the GB300 library through its C-ABI and the CPU oracle, so both solve exactly
+the same problem.
+"""
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+if os.path.join(ROOT, "oracle") not in sys.path:
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+E_STEEL = 210000.0          # N/mm^2
+NU_STEEL = 0.28
+G_STEEL = E_STEEL / (2.0 * (1.0 + NU_STEEL))
+
+
+def f32(v):
+    return float(np.float32(v))
+
+
+def config0(gausei=5, eps=1e-10, mixed=0, mx=51, my=51):
+    """Plain FP64 Hertzian steady rolling: a=6 mm, b=4 mm, 51x51 over 1.1a x 1.1b, Fn=100 kN,
+    creepage 0.001, mu=0.3, steel on steel."""
+    return dict(tang=3, norm=1, bound=0, gausei=gausei, maxgs=999, maxin=100, maxnr=30, maxout=1, eps=eps,
+                poiss=NU_STEEL, gg=G_STEEL, fstat=0.3, veloc=10000.0, fn=1e5, cksi=0.001, ceta=0.0, cphi=0.0,
+                ipotcn=-3, potprm=[mx, my, 6.0, 4.0, 1.1], mixed=mixed)
+
+
+# test_table (src/test_table.f90:60-292): 11x11 Hertz grids, SteadyGS, eps 1e-6
+TT_ELLIP = [f32(0.2), f32(0.5), 1.0, 2.0, 5.0]
+TT_AA = [4.0, 6.0, 9.0, 12.0, 20.0]
+TT_SPIN = [0.0, 0.5, 1.0, 2.0]
+TT_ANGL = [-math.pi / 2, -math.pi / 3, -math.pi / 6, 0.0, math.pi / 6, math.pi / 3, math.pi / 2]
+TT_MAGN = [f32(v) for v in (0.0, 0.1, 0.2, 0.3, 0.4, 0.5, 0.7, 0.9, 1.1, 1.4, 1.7, 2.0, 2.5, 3.0, 3.5, 4.0, 5.0,
+                            6.0, 7.0, 8.0, 9.0, 10., 12.)]
+TT_MX = 11
+TT_SCALE = f32(np.float32(TT_MX) / np.float32(TT_MX - 4))
+
+
+def test_table_base(iell):
+    return dict(tang=3, norm=1, bound=0, gausei=0, maxgs=299, maxin=1, maxnr=30, maxout=1, eps=1e-6,
+                poiss=0.28, gg=82000.0, fstat=0.3, veloc=10000.0, fn=82000.0, cksi=0.0, ceta=0.0, cphi=0.0,
+                ipotcn=-3, potprm=[TT_MX, TT_MX, TT_AA[iell], TT_AA[iell] / TT_ELLIP[iell], TT_SCALE])
+
+
+def test_table_case(icase, rho, cp):
+    """Case number icase (0-based) of test_table, with the Hertz rho, cp per ellipticity."""
+    ivmgn = icase % 23
+    irem = icase // 23
+    ivang = irem % 7
+    irem //= 7
+    ispin = irem % 4
+    irem //= 4
+    iell = irem % 5
+    c = test_table_base(iell)
+    cmgn, cang = TT_MAGN[ivmgn], TT_ANGL[ivang]
+    c["cksi"] = cmgn * 0.3 * math.cos(cang) * cp[iell] / rho[iell]
+    c["ceta"] = cmgn * 0.3 * math.sin(cang) * cp[iell] / rho[iell]
+    c["cphi"] = 0.3 * TT_SPIN[ispin] / rho[iell]
+    return c, iell
+
+
+def tractcurv_case(cksi):
+    """First series of examples/tractcurv.inp: Hertz a1=0.0008/mm, a/b=0.5, 48x44, Fn=106.7 kN."""
+    return dict(tang=3, norm=1, bound=0, gausei=0, maxgs=80, maxin=200, maxnr=5, maxout=1, eps=1e-6,
+                poiss=0.28, gg=82000.0, fstat=0.33, veloc=10000.0, fn=106700.0, cksi=cksi, ceta=0.0, cphi=0.0,
+                ipotcn=-2, potprm=[48, 44, 0.0008, 0.5, 1.1], dq=0.5)
+
+
+def rough_surface(mx, my, xl, yl, dx, dy, pen_hz, seed, rx=460.0, ry=300.0, nsin=8):
+    """Non-Hertzian undeformed distance: x^2/(2Rx) + y^2/(2Ry) + a seeded sum of 8 sinusoids
+    (wavelength 1-5 mm, total amplitude 5% of the Hertzian approach)."""
+    rng = np.random.default_rng(seed)
+    lam = rng.uniform(1.0, 5.0, nsin)
+    th = rng.uniform(0.0, math.pi, nsin)
+    ph = rng.uniform(0.0, 2 * math.pi, nsin)
+    amp = rng.uniform(0.0, 1.0, nsin)
+    amp = amp / amp.sum() * 0.05 * pen_hz
+    x = xl + (np.arange(mx) + 0.5) * dx
+    y = yl + (np.arange(my) + 0.5) * dy
+    X, Y = np.meshgrid(x, y)
+    h = X ** 2 / (2 * rx) + Y ** 2 / (2 * ry)
+    for k in range(nsin):
+        h = h + amp[k] * np.sin(2 * math.pi * (X * math.cos(th[k]) + Y * math.sin(th[k])) / lam[k] + ph[k])
+    return h
+
+
+def config1(m, seed=1, gausei=5, eps=1e-8, mixed=0, fn=1e5, cksi=0.002, ceta=0.001, cphi=2e-4, mu=0.3):
+    """Non-Hertzian grid case: square m x m grid over [-1.25a, 1.25a]^2 of the Hertz solution
+    for Rx=460, Ry=300 mm; element-wise h with seeded roughness."""
+    a_est = 7.2 * (fn / 1e5) ** (1.0 / 3.0)
+    half = 1.25 * a_est
+    dx = 2 * half / m
+    pen_hz = 0.16 * (fn / 1e5) ** (2.0 / 3.0)
+    h = rough_surface(m, m, -half, -half, dx, dx, pen_hz, seed)
+    return dict(tang=3, norm=1, bound=0, gausei=gausei, maxgs=999, maxin=100, maxnr=30, maxout=1, eps=eps,
+                poiss=NU_STEEL, gg=G_STEEL, fstat=mu, veloc=10000.0, fn=fn, cksi=cksi, ceta=ceta, cphi=cphi,
+                ipotcn=1, potprm=[m, m, -half, -half, dx, dx], h=h, mixed=mixed)
+
+
+def batch_patches(n, seed=2, mixed=1, eps=1e-8):
+    """Batched workload: n independent Hertzian patches, sides U{24..160}, semi-axes
+    log-uniform 2-10 mm, Fn U[10,150] kN, creepages U[-0.005,0.005], spin U[-0.5,0.5] rad/m,
+    mu U[0.2,0.4], GDsteady with FP32 bulk + FP64 refinement."""
+    rng = np.random.default_rng(seed)
+    cases = []
+    for i in range(n):
+        mx, my = int(rng.integers(24, 161)), int(rng.integers(24, 161))
+        a = float(np.exp(rng.uniform(math.log(2.0), math.log(10.0))))
+        b = float(np.exp(rng.uniform(math.log(2.0), math.log(10.0))))
+        fn = float(rng.uniform(10e3, 150e3))
+        cksi, ceta = float(rng.uniform(-0.005, 0.005)), float(rng.uniform(-0.005, 0.005))
+        cphi = float(rng.uniform(-0.5, 0.5)) * 1e-3            # rad/m -> rad/mm
+        mu = float(rng.uniform(0.2, 0.4))
+        cases.append(dict(tang=3, norm=1, bound=0, gausei=5, maxgs=999, maxin=100, maxnr=30, maxout=1, eps=eps,
+                          poiss=NU_STEEL, gg=G_STEEL, fstat=mu, veloc=10000.0, fn=fn, cksi=cksi, ceta=ceta,
+                          cphi=cphi, ipotcn=-3, potprm=[mx, my, a, b, 1.1], mixed=mixed))
+    return cases
+
+
+def to_oracle(case):
+    """Oracle problem for a case dict; returns (Problem, h or None)."""
+    import pyoracle as po
+    pb = po.default_problem()
+    pb.tang = case.get("tang", 3)
+    pb.norm = case.get("norm", 1)
+    pb.bound = case.get("bound", 0)
+    pb.gausei = case.get("gausei", 0)
+    pb.maxgs = case.get("maxgs", 999)
+    pb.maxin = case.get("maxin", 100)
+    pb.maxnr = case.get("maxnr", 30)
+    pb.maxout = case.get("maxout", 1)
+    pb.eps = case.get("eps", 1e-6)
+    nu = case.get("poiss", 0.28)
+    g = case.get("gg", 82000.0)
+    pb.poiss1 = pb.poiss2 = nu
+    pb.gg1 = pb.gg2 = g
+    pb.fstat = pb.fkin = case.get("fstat", 0.3)
+    pb.veloc = case.get("veloc", 10000.0)
+    if "dq" in case:
+        pb.dq = case["dq"]
+    pb.cksi, pb.ceta, pb.cphi = case.get("cksi", 0.0), case.get("ceta", 0.0), case.get("cphi", 0.0)
+    if pb.norm == 1:
+        pb.fn = case["fn"]
+    else:
+        pb.pen = case["pen"]
+    pb.ipotcn = case.get("ipotcn", -3)
+    for k, v in enumerate(case["potprm"][:6]):
+        pb.potprm[k] = v
+    if pb.gausei == 5:
+        gd = case.get("gd", dict(fdecay=0.9, betath=0.1, kdowfb=1, d_ifc=1.0, d_lin=1.0, d_cns=1.0, d_slp=1.0,
+                                 pow_s=0.9))
+        pb.fdecay, pb.betath, pb.kdowfb = gd["fdecay"], gd["betath"], gd["kdowfb"]
+        pb.d_ifc, pb.d_lin, pb.d_cns, pb.d_slp, pb.pow_s = gd["d_ifc"], gd["d_lin"], gd["d_cns"], gd["d_slp"], gd["pow_s"]
+    return pb, case.get("h")
+
+
+def oracle_solve(case):
+    import pyoracle as po
+    pb, h = to_oracle(case)
+    return po.solve(pb, h=h)
