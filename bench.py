@@ -1,0 +1,402 @@
+"""Throughput benchmark of the GB300 rolling-contact library on the batched mixed-size workload.
+
+Workload: 4096 independent Hertzian steady-rolling patches (seed 2): grid sides U{24..160},
+semi-axes log-uniform 2-10 mm, Fn U[10,150] kN, creepages U[-0.005,0.005], spin U[-0.5,0.5]
+rad/m, mu U[0.2,0.4], steel on steel; NormCG + GDsteady with FP32 convolutions and FP64
+refinement to eps 1e-8.  One step = one solve of all patches (influence coefficients,
+normal and tangential problem, force integration).
+
+  value  solves/s with inputs resident in device memory (cntc_gb300_resident_*; CUDA events
+         on the library's stream around its launches)
+  e2e    solves/s through cntc_calculate_batch from host buffers (host->device copy of the
+         inputs, device->host copy of all results inside the timed region)
+  --impl reference  the CPU oracle (serial restatement of the reference's solve path) on
+         all host cores, on a bounded sample of the same workload per step
+
+Multi-GPU: patches are independent and nothing is exchanged, so N ranks run N replicas of
+the workload (weak scaling); value = total solves / max over ranks of the timed region.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import cases as C  # noqa: E402
+
+METRIC = "solves/s & p99 latency, mixed+batched vs plain FP64 on GB300 at 1e-8 rel err"
+UNIT = "solves/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--patches", type=int, default=4096)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--plain-sample", type=int, default=608,
+                    help="patches of the same workload solved in plain FP64 for the mixed/plain ratio")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="wall-clock budget of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(n, seed, mixed=1):
+    return C.batch_patches(n, seed=seed, mixed=mixed, eps=1e-8)
+
+
+def fft_proxy(case):
+    """Cost proxy of one patch for scaling CPU samples: F log2 F with F the doubled FFT grid."""
+    from contact_gb300 import opt_fft_size as opt
+    mx, my = int(case["potprm"][0]), int(case["potprm"][1])
+    f = 4 * opt(mx) * opt(my)
+    return f * math.log2(f)
+
+
+# ------------------------------------------------------------------------------------------
+# distributed plumbing (torchrun): replicas, barrier, max over ranks
+# ------------------------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            backend = "nccl" if _cuda_ok() else "gloo"
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda" if _cuda_ok() else "cpu"
+        t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda" if _cuda_ok() else "cpu"
+        t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def _cuda_ok():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+# ------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            v = [x.strip() for x in ln.split(",")]
+            if len(v) < 9:
+                continue
+            try:
+                sm.append(float(v[1]))
+                smax.append(float(v[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, v[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------------------------------
+# CPU baseline: the oracle on all host cores, bounded sample, scaled by the FFT cost proxy
+# ------------------------------------------------------------------------------------------
+def cpu_sample_rate(cases, budget_s, seed, threads=None):
+    """Solve a seeded sample of the workload's patches with the CPU oracle on a thread pool
+    (ctypes releases the GIL).  Patches are drawn from those no larger than 64x64 so that a
+    sample ends within the budget; the measured time per unit of the FFT cost proxy is then
+    applied to the whole workload's proxy.  Returns (solves/s, threads, description)."""
+    from concurrent.futures import ThreadPoolExecutor
+    import pyoracle as po
+    po.build()
+    threads = threads or os.cpu_count() or 1
+    rng = np.random.default_rng(seed)
+    small = [i for i, c in enumerate(cases) if c["potprm"][0] <= 64 and c["potprm"][1] <= 64]
+    order = list(rng.permutation(small))
+    t_sum, p_sum, done = 0.0, 0.0, 0
+    t0 = time.perf_counter()
+
+    def one(i):
+        c = dict(cases[i], mixed=0)
+        ts = time.perf_counter()
+        C.oracle_solve(c)
+        return time.perf_counter() - ts, fft_proxy(c)
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        pending = set()
+        it = iter(order)
+        while True:
+            while len(pending) < threads and time.perf_counter() - t0 < budget_s:
+                try:
+                    pending.add(ex.submit(one, next(it)))
+                except StopIteration:
+                    break
+            if not pending:
+                break
+            fin = [f for f in pending if f.done()]
+            if not fin:
+                time.sleep(0.01)
+                continue
+            for f in fin:
+                pending.discard(f)
+                dt, px = f.result()
+                t_sum += dt
+                p_sum += px
+                done += 1
+    wall = time.perf_counter() - t0
+    mean_proxy = float(np.mean([fft_proxy(c) for c in cases]))
+    sec_per_patch = t_sum / p_sum * mean_proxy          # one core, average patch of the workload
+    rate = threads / sec_per_patch
+    desc = ("%d patches (sides <= 64) of the workload solved by the oracle in %.1f s wall on %d threads; "
+            "core-seconds per unit of F log2 F (F = doubled FFT grid) applied to the full workload's mix"
+            % (done, wall, threads))
+    return rate, threads, desc
+
+
+# ------------------------------------------------------------------------------------------
+# GB300 arm
+# ------------------------------------------------------------------------------------------
+def setup_problems(cg, cases, ire0=1):
+    ire = list(range(ire0, ire0 + len(cases)))
+    for i, c in zip(ire, cases):
+        cg.setup_case(i, 1, c)
+    return ire, [1] * len(cases)
+
+
+def run_gb300(args, dist):
+    import torch
+    import contact_gb300 as cg
+    torch.cuda.set_device(dist.local)
+    cg.load()
+    cases = workload(args.patches, args.seed, mixed=1)
+    n = len(cases)
+    ire, icp = setup_problems(cg, cases)
+    rb = cg.ResidentBatch(ire, icp)
+    bad = int((rb.setup_errors != 0).sum())
+    if bad:
+        raise RuntimeError("%d patches could not be prepared" % bad)
+    launches0 = cg.kernel_launches()
+    rb.solve(args.warmup)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    launches1 = cg.kernel_launches()
+    times = rb.solve(args.steps)
+    gpu_launches = cg.kernel_launches() - launches1
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    t_total_ms = float(times[:, 0].sum())
+    t_total_ms = dist.max(t_total_ms)
+    ms_per_step = t_total_ms / args.steps
+    value = dist.sum(n * args.steps) / (t_total_ms / 1e3)
+
+    # results and per-patch statistics of the last step
+    err = rb.collect()
+    nfail = int((err < 0).sum())
+    stats = [cg.getsolverstats(i, 1) for i in ire]
+    res_it = [cg.getiterationcounts(i, 1) for i in ire]
+    t0 = min(s["t_start_ns"] for s in stats)
+    ic_ms = float(times[-1, 2])
+    lat_ms = np.array([(s["t_end_ns"] - t0) / 1e6 for s in stats]) + ic_ms
+    # algorithmic bytes of the patch-solve kernels in one step: convolution traffic counted in
+    # the kernel, plus the vector passes of the iterations (8 N bytes per pass):
+    # NormCG 12 passes / iteration, GDsteady 20 / iteration + 16 / line-search step
+    alg = 0.0
+    for c, s, r in zip(cases, stats, res_it):
+        npot = int(c["potprm"][0]) * int(c["potprm"][1])
+        itgd = r["itgs"] if r["solver"] == 7 else 0
+        alg += s["conv_bytes"] + 8.0 * npot * (12 * r["itcg"] + 20 * itgd + 16 * s["nls"])
+    solve_ms = float(times[-1, 1])
+    nsolve_launch = int(round(times[-1, 3])) - (2 if ic_ms > 0 else 0)
+    peak, peak_kind = measured_peaks()
+    achieved = alg / (solve_ms / 1e3) / 1e9
+    rb.release()
+
+    # end to end: cntc_calculate_batch from host buffers (copies inside the timed region)
+    e2e_steps = max(1, min(args.steps, 2))
+    cg.calculate_batch(ire, icp)                       # warm the pinned staging buffers
+    dist.barrier()
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(e2e_steps):
+        e_err = cg.calculate_batch(ire, icp)
+    torch.cuda.synchronize()
+    te = dist.max(time.perf_counter() - te)
+    e2e_value = dist.sum(n * e2e_steps) / te
+    h2d_bytes, d2h_bytes = cg.lastcopybytes()
+    # plain FP64 form on a sample of the same workload
+    plain = None
+    if args.plain_sample > 0:
+        pc = [dict(c, mixed=0) for c in cases[:args.plain_sample]]
+        pire = ire[:len(pc)]
+        picp = [2] * len(pc)
+        for i, c in zip(pire, pc):
+            cg.setup_case(i, 2, c)
+        prb = cg.ResidentBatch(pire, picp)
+        prb.solve(1)
+        pt = prb.solve(1)
+        prb.release()
+        mixed_sample_ms = None
+        mrb = cg.ResidentBatch(ire[:args.plain_sample], icp[:args.plain_sample])
+        mrb.solve(1)
+        mt = mrb.solve(1)
+        mrb.release()
+        mixed_sample_ms = float(mt[0, 0])
+        plain = {"patches": len(pc), "solves_per_s": len(pc) / (float(pt[0, 0]) / 1e3),
+                 "mixed_solves_per_s_same_sample": len(pc) / (mixed_sample_ms / 1e3),
+                 "note": "first %d patches of the workload, eps 1e-8, FP64 throughout" % len(pc)}
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        rate, thr, desc = cpu_sample_rate(cases, args.cpu_seconds, args.seed)
+        cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port", "sample": desc}
+    if dist.rank != 0:
+        return None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "batched mixed-size Hertzian steady rolling, %d patches, sides 24-160, "
+                               "GDsteady, FP32 convolutions + FP64 refinement, eps 1e-8" % n,
+                   "patches": n, "seed": args.seed, "parallelism": "replicas x%d" % dist.world,
+                   "l2": "inputs larger than L2 (%.1f GB of io blocks alone)" % (d2h_bytes / 1e9)},
+        "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
+                       "definition": "completion time of each patch since the start of its step (batched)"},
+        "failed_patches": nfail,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "kernel": "k_solve",
+                     "launches_per_step": nsolve_launch, "peak_source": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
+                "errors": int((np.asarray(e_err) < 0).sum())},
+        "plain_fp64": plain,
+        "clocks": clk,
+        "gpu_launches": int(gpu_launches),
+    }
+    return out
+
+
+# ------------------------------------------------------------------------------------------
+# reference arm: the CPU oracle on the host cores
+# ------------------------------------------------------------------------------------------
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return None
+    cases = workload(args.patches, args.seed, mixed=0)
+    budget = max(5.0, min(args.cpu_seconds, 30.0))
+    for w in range(args.warmup):
+        cpu_sample_rate(cases, 1.0, args.seed + 1000 + w)
+    rates = []
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        r, thr, desc = cpu_sample_rate(cases, budget, args.seed + s)
+        rates.append(r)
+    wall = time.perf_counter() - t0
+    value = float(np.mean(rates))
+    return {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "batched mixed-size Hertzian steady rolling, %d patches, sides 24-160, "
+                               "GDsteady, FP64, eps 1e-8" % len(cases), "patches": len(cases), "seed": args.seed},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        out = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
+        if out is not None:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

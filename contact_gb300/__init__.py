@@ -82,6 +82,11 @@ _PROTOS = {
     "cntc_finalizelast": [],
     "cntc_gb300_kernel_launches": [],
     "cntc_gb300_getsolverstats": [_IP, _IP, _IP, _DP],
+    "cntc_gb300_resident_setup": [_IP, _IP, _IP, _IP],
+    "cntc_gb300_resident_solve": [_IP, _DP, _IP],
+    "cntc_gb300_resident_collect": [_IP, _IP],
+    "cntc_gb300_resident_release": [],
+    "cntc_gb300_lastcopybytes": [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
 }
 
 
@@ -303,7 +308,67 @@ def kernel_launches():
 
 
 STAT_NAMES = ("nconv32", "nconv64", "nls", "status", "t_total", "t_conv", "t_ls", "t_diag", "t_gs", "t_norm",
-              "t_tang", "t_scan")
+              "t_tang", "t_scan", "t_conv32", "conv_bytes", "t_start_ns", "t_end_ns")
+
+
+def lastcopybytes():
+    """(host->device, device->host) bytes of this thread's last calculate call."""
+    a, b = ctypes.c_longlong(), ctypes.c_longlong()
+    load().cntc_gb300_lastcopybytes(ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+def opt_fft_size(n):
+    """FFT length used for a grid side n (m_aijpj.f90:1022-1119): start from the next power of two
+    and trade factors (4 -> 3, 32 -> 27, 6 -> 5, 16 -> 15, 27 -> 25, 8 -> 7, 15 -> 14, 10 -> 9)
+    while the product stays >= n."""
+    trades = (((-2, 1, 0, 0), 4, 3), ((-5, 3, 0, 0), 32, 27), ((-1, -1, 1, 0), 6, 5), ((-4, 1, 1, 0), 16, 15),
+              ((0, -3, 2, 0), 27, 25), ((-3, 0, 0, 1), 8, 7), ((1, -1, -1, 1), 15, 14), ((-1, 2, -1, 0), 10, 9))
+    k2 = 0
+    while (1 << k2) < n:
+        k2 += 1
+    k = [k2, 0, 0, 0]
+    prod = 1 << k2
+    changed = True
+    while changed:
+        changed = False
+        for dk, den, num in trades:
+            while all(k[f] + dk[f] >= 0 for f in range(4)) and num * prod >= den * n:
+                k = [k[f] + dk[f] for f in range(4)]
+                prod = num * prod // den
+                changed = True
+    return prod
+
+
+class ResidentBatch:
+    """Problems staged in device memory once and solved repeatedly (inputs resident in HBM)."""
+
+    def __init__(self, ire_list, icp_list):
+        _require_gpu()
+        self.n = len(ire_list)
+        a, ap = _iarr(ire_list)
+        b, bp = _iarr(icp_list)
+        self._ids = (a, b)
+        self.setup_errors = np.zeros(self.n, dtype=np.int32)
+        load().cntc_gb300_resident_setup(_i(self.n), ap, bp, self.setup_errors.ctypes.data_as(_IP))
+
+    def solve(self, nrep=1):
+        """Run the engine nrep times; returns an (nrep, 4) array: device ms of the pass, ms in
+        patch solves, ms in influence/spectrum kernels, launches."""
+        t = np.zeros((nrep, 4))
+        err = ctypes.c_int(0)
+        load().cntc_gb300_resident_solve(_i(nrep), t.ctypes.data_as(_DP), ctypes.byref(err))
+        if err.value != 0:
+            raise RuntimeError("resident solve failed (%d)" % err.value)
+        return t
+
+    def collect(self):
+        err = np.zeros(self.n, dtype=np.int32)
+        load().cntc_gb300_resident_collect(_i(self.n), err.ctypes.data_as(_IP))
+        return err
+
+    def release(self):
+        load().cntc_gb300_resident_release()
 
 
 def getsolverstats(ire, icp):

@@ -190,7 +190,9 @@ int prepare(Problem &p, Prep &out) {
     if (!is_roll) { chi = 0.0; dq = 1.0; veloc = 1.0; }
     if (is_roll && std::fabs(chi) > 0.01) { log_msg("rolling direction chi != 0 is not supported"); return CNTC_err_other; }
     p.dt = dq / std::max(1e-10, veloc);
-    if (mx < 2 || my < 2) { log_msg("grids of width 1 are not supported"); return CNTC_err_other; }
+    // a single column in rolling direction: steady rolling would select ConvexGS (-99 here as
+    // well); single rows (my = 1) are solved
+    if (mx < 2 || my < 1) { log_msg("grids with mx < 2 are not supported"); return CNTC_err_other; }
     const int fx = cgb::opt_fft_size(mx), fy = cgb::opt_fft_size(my);
     if (solve_smem_bytes(fx, fy) > 227 * 1024) { log_msg("patch too large for the single-block engine"); return CNTC_err_other; }
     d.mx = mx; d.my = my; d.npot = mx * my; d.fx = fx; d.fy = fy;
@@ -312,6 +314,8 @@ cudaError_t grow(void **ptr, size_t &cap, size_t need, bool pinned) {
 }
 
 thread_local Arena t_arena;
+// bytes moved by the last host<->device batch copy of this thread
+thread_local long long t_h2d_bytes = 0, t_d2h_bytes = 0;
 
 // runs the engine for all prepared entries with status 0; results go to the problems
 int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
@@ -345,14 +349,17 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
             stage_inputs(*b.probs[live[k]], hd[k], (double *)((char *)A.h_io + off_io[k]));
     }
     cudaStream_t st = cudaStreamPerThread;
+    t_h2d_bytes = (long long)(n * sizeof(PatchDesc));
     if (any_upload) {
         if ((e = cudaMemcpyAsync(A.d_io, A.h_io, tot_io, cudaMemcpyHostToDevice, st)) != cudaSuccess) return (int)e;
+        t_h2d_bytes += (long long)tot_io;
     }
     if ((e = cudaMemcpyAsync(A.d_desc, hd.data(), n * sizeof(PatchDesc), cudaMemcpyHostToDevice, st)) != cudaSuccess)
         return (int)e;
     int rc = engine_run(hd.data(), A.d_desc, n, need_ic.data(), A.d_list, st);
     if (rc != 0) return rc;
     if ((e = cudaMemcpyAsync(A.h_io, A.d_io, tot_io, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return (int)e;
+    t_d2h_bytes = (long long)tot_io;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return (int)e;
     for (int k = 0; k < n; k++) collect(*b.probs[live[k]], hd[k], (const double *)((const char *)A.h_io + off_io[k]));
     return 0;
@@ -386,6 +393,121 @@ int calculate_many(int n, const int *ire, const int *icp, int *ierror) {
     }
     if (rc != 0 && g_debug >= 1) std::fprintf(stderr, "contact_gb300: engine error %d (%s)\n", rc, cudaGetErrorString((cudaError_t)rc));
     return rc;
+}
+
+// ------------------------------------------------------------------------------------------
+// resident batch: a set of prepared problems staged in device memory once and solved again
+// and again on the same inputs (throughput with inputs already in HBM).  Each solve runs the
+// whole engine, influence coefficients included.
+// ------------------------------------------------------------------------------------------
+struct Resident {
+    Batch b;
+    std::vector<int> live;
+    std::vector<PatchDesc> hd;
+    std::vector<unsigned char> need_ic;
+    std::vector<size_t> off_io;
+    size_t tot_io = 0;
+    Arena A;
+    EngineTimer tm;
+    bool have_events = false;
+    ~Resident() {
+        if (have_events) for (auto &e : tm.ev) cudaEventDestroy(e);
+        if (A.d_io) cudaFree(A.d_io);
+        if (A.d_work) cudaFree(A.d_work);
+        if (A.d_desc) cudaFree(A.d_desc);
+        if (A.d_list) cudaFree(A.d_list);
+        if (A.h_io) cudaFreeHost(A.h_io);
+    }
+};
+std::mutex g_res_mu;
+std::unique_ptr<Resident> g_res;
+
+int resident_setup(int n, const int *ire, const int *icp, int *ierror) {
+    g_res.reset();
+    auto R = std::make_unique<Resident>();
+    Batch &b = R->b;
+    b.probs.resize(n); b.preps.resize(n); b.status.assign(n, 0);
+    for (int i = 0; i < n; i++) {
+        Problem *p = lookup(ire[i], icp[i], true);
+        b.probs[i] = p;
+        if (!p) { b.status[i] = CNTC_err_icp; continue; }
+        b.status[i] = prepare(*p, b.preps[i]);
+    }
+    for (int i = 0; i < n; i++) { ierror[i] = b.status[i]; if (b.status[i] == 0) R->live.push_back(i); }
+    const int m = (int)R->live.size();
+    std::vector<size_t> off_work(m);
+    R->off_io.resize(m);
+    size_t tot_work = 0;
+    for (int k = 0; k < m; k++) {
+        const PatchDesc &d = b.preps[R->live[k]].d;
+        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy);
+        R->off_io[k] = R->tot_io; R->tot_io += s.io;
+        off_work[k] = tot_work; tot_work += s.work;
+    }
+    Arena &A = R->A;
+    cudaError_t e;
+    if ((e = grow((void **)&A.d_io, A.cap_io, R->tot_io, false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_work, A.cap_work, tot_work, false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_desc, A.cap_desc, m * sizeof(PatchDesc), false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_list, A.cap_list, 2 * m * sizeof(int) + 64, false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.h_io, A.cap_hio, R->tot_io, true)) != cudaSuccess) return (int)e;
+    R->hd.resize(m);
+    R->need_ic.assign(m, 1);
+    for (int k = 0; k < m; k++) {
+        R->hd[k] = b.preps[R->live[k]].d;
+        carve_patch(R->hd[k], A.d_io + R->off_io[k], A.d_work + off_work[k]);
+        stage_inputs(*b.probs[R->live[k]], R->hd[k], (double *)((char *)A.h_io + R->off_io[k]));
+    }
+    cudaStream_t st = cudaStreamPerThread;
+    if ((e = cudaMemcpyAsync(A.d_io, A.h_io, R->tot_io, cudaMemcpyHostToDevice, st)) != cudaSuccess) return (int)e;
+    if ((e = cudaMemcpyAsync(A.d_desc, R->hd.data(), m * sizeof(PatchDesc), cudaMemcpyHostToDevice, st)) != cudaSuccess)
+        return (int)e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return (int)e;
+    for (auto &ev : R->tm.ev) if ((e = cudaEventCreate(&ev)) != cudaSuccess) return (int)e;
+    R->have_events = true;
+    g_res = std::move(R);
+    return 0;
+}
+
+// one solve of the resident batch; times[0] = device time of the whole pass (first to last
+// launch), times[1] = patch-solve kernels, times[2] = influence-coefficient and spectrum
+// kernels (ms, CUDA events on the launching stream), times[3] = number of launches
+int resident_solve(double *times) {
+    Resident *R = g_res.get();
+    if (!R || R->hd.empty()) return -1;
+    cudaStream_t st = cudaStreamPerThread;
+    int rc = engine_run(R->hd.data(), R->A.d_desc, (int)R->hd.size(), R->need_ic.data(), R->A.d_list, st, &R->tm);
+    if (rc != 0) return rc;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return (int)e;
+    const EngineTimer &tm = R->tm;
+    float ms = 0.f;
+    times[0] = times[1] = times[2] = 0.0;
+    if (tm.nlaunch > 0) {
+        cudaEventElapsedTime(&ms, tm.ev[0], tm.ev[2 * tm.nlaunch - 1]);
+        times[0] = ms;
+    }
+    for (int k = 0; k < tm.nlaunch; k++) {
+        cudaEventElapsedTime(&ms, tm.ev[2 * k], tm.ev[2 * k + 1]);
+        times[tm.kind[k] == 2 ? 1 : 2] += ms;
+    }
+    times[3] = tm.nlaunch;
+    return 0;
+}
+
+int resident_collect(int *ierror) {
+    Resident *R = g_res.get();
+    if (!R) return -1;
+    cudaStream_t st = cudaStreamPerThread;
+    cudaError_t e = cudaMemcpyAsync(R->A.h_io, R->A.d_io, R->tot_io, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return (int)e;
+    for (size_t k = 0; k < R->live.size(); k++) {
+        const int i = R->live[k];
+        collect(*R->b.probs[i], R->hd[k], (const double *)((const char *)R->A.h_io + R->off_io[k]));
+        ierror[i] = R->b.probs[i]->ierror;
+    }
+    return 0;
 }
 
 double *field_ptr(Problem &p, int col) {
@@ -869,6 +991,40 @@ void cntc_finalizelast() {
 }
 
 long long cntc_gb300_kernel_launches() { return cgb::kernel_launch_count(); }
+
+void cntc_gb300_lastcopybytes(long long *h2d, long long *d2h) {
+    *h2d = t_h2d_bytes;
+    *d2h = t_d2h_bytes;
+}
+
+void cntc_gb300_resident_setup(int *n, int *ire, int *icp, int *ierror) {
+    std::lock_guard<std::mutex> lk(g_res_mu);
+    int rc = resident_setup(*n, ire, icp, ierror);
+    if (rc != 0) {
+        for (int i = 0; i < *n; i++) if (ierror[i] == 0) ierror[i] = CNTC_err_other;
+        g_res.reset();
+    }
+}
+
+void cntc_gb300_resident_solve(int *nrep, double *times, int *ierror) {
+    std::lock_guard<std::mutex> lk(g_res_mu);
+    *ierror = 0;
+    for (int r = 0; r < *nrep; r++) {
+        int rc = resident_solve(times + 4 * r);
+        if (rc != 0) { *ierror = CNTC_err_other; return; }
+    }
+}
+
+void cntc_gb300_resident_collect(int *n, int *ierror) {
+    std::lock_guard<std::mutex> lk(g_res_mu);
+    if (!g_res || (int)g_res->b.probs.size() != *n || resident_collect(ierror) != 0)
+        for (int i = 0; i < *n; i++) ierror[i] = CNTC_err_other;
+}
+
+void cntc_gb300_resident_release() {
+    std::lock_guard<std::mutex> lk(g_res_mu);
+    g_res.reset();
+}
 
 void cntc_gb300_getsolverstats(int *ire, int *icp, int *lenarr, double *values) {
     Problem *p = lookup(*ire, *icp, false);

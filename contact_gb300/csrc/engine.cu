@@ -119,6 +119,8 @@ __device__ inline Conv<T> make_conv(const PatchDesc &d, unsigned char *smraw, co
     cv.R1 = R + (size_t)cv.nkx * cv.my;
     cv.scale = 1.0 / (d.ga * (double)cv.NX * (double)cv.NY);
     cv.tacc = nullptr;
+    cv.tacc2 = nullptr;
+    cv.bacc = nullptr;
     return cv;
 }
 
@@ -378,9 +380,10 @@ __device__ __noinline__ void compute_facdt(const PView &P, int solver, double *f
 
 // TANG, m_stang.f90:28-746 for Coulomb friction and prescribed creepages.
 // Returns ittang; -1000 when the reference would pick ConvexGS, -2000 on a failed line search.
-template <typename T>
-__device__ __noinline__ int stang(const PView &P, const Ops<T> &op, double eps, int &itgs_out, int &solver_out, int &nconv,
-                     int &nls) {
+// With o32 (mixed precision): GDsteady runs once with FP32 direction products and FP64
+// residual replacement; TangCG runs an FP32 pass to eps32 followed by an FP64 pass.
+__device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const Ops<float> *o32, double eps,
+                                  double eps32, int &itgs_out, int &solver_out, int &nconv, int &nconv32, int &nls) {
     const PatchDesc &d = *P.d;
     const int mx = P.mx, my = P.my, n = P.n;
     RedSmem &red = P.sm->red;
@@ -431,11 +434,15 @@ __device__ __noinline__ int stang(const PView &P, const Ops<T> &op, double eps, 
             it = stdygs(P, eps, d.maxgs, omegah, omegas, info, errpt);
         } else if (solver == 7) {
             bool lstagn = false;
-            it = gdsteady<T>(P, op, d.maxgs, eps, errpt, lstagn, nconv, nls);
+            it = gdsteady<double>(P, op, d.maxgs, eps, errpt, lstagn, nconv, nls, o32, nconv32);
             if (it == -100000) return -2000;
             if (lstagn) it = stdygs(P, eps, d.maxgs, omegah, omegas, info, errpt);
         } else {
-            it = tangcg<T>(P, op, op.K[5], op.K[6], d.maxgs, eps, errpt, nconv);
+            if (o32) {
+                it = tangcg<float>(P, *o32, o32->K[5], o32->K[6], d.maxgs, eps32, errpt, nconv32);
+                itgs += it > 0 ? it : 0;
+            }
+            it = tangcg<double>(P, op, op.K[5], op.K[6], d.maxgs, eps, errpt, nconv);
         }
         itgs += it;
         if (info >= 3) { zready = true; ittang = -1; }
@@ -560,11 +567,15 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
     PView P;
     P.d = &d; P.mx = d.mx; P.my = d.my; P.n = d.npot; P.sm = &sm;
     double *out = P.out();
-    if (threadIdx.x < 8) sm.t[threadIdx.x] = 0;
+    if (threadIdx.x < kNumPhaseTimers) sm.t[threadIdx.x] = 0;
+    if (threadIdx.x == 0) sm.algb = 0.0;
     const long long t_start = clock64();
+    unsigned long long g_start;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g_start));
     Ops<double> op64;
     make_ops<double>(op64, d, smraw, sp);
     op64.cv.tacc = &sm.t[O_T_CONV - O_T_TOTAL];
+    op64.cv.bacc = &sm.algb;
     make_twiddles<double>(op64.cv.twx, sp.NX);
     make_twiddles<double>(op64.cv.twy, sp.NY);
     Ops<float> op32;
@@ -572,6 +583,8 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
     if (mixed) {
         make_ops<float>(op32, d, smraw, sp);
         op32.cv.tacc = &sm.t[O_T_CONV - O_T_TOTAL];
+        op32.cv.tacc2 = &sm.t[O_T_CONV32 - O_T_TOTAL];
+        op32.cv.bacc = &sm.algb;
         make_twiddles<float>(op32.cv.twx, sp.NX);
         make_twiddles<float>(op32.cv.twy, sp.NY);
     }
@@ -597,15 +610,11 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
     // NORM (skipped for Hertzian traction bounds B = 2, 3)
     long long t_norm0 = clock64();
     if (!(d.bound >= 2 && d.bound <= 4 && d.ihertz >= 1)) {
+        // the normal problem is a small part of a solve: FP64 in both forms, so that the mixed
+        // form starts its tangential iteration from exactly the same pressures
         int it = 0, itc = 0;
-        if (mixed) {
-            it = snorm<float>(P, op32, d.maxgs, d.maxin, d.eps32, pen, itc, nconv32);
-            itcg += itc;
-        }
-        if (it != -2) {
-            it = snorm<double>(P, op64, d.maxgs, d.maxin, d.eps, pen, itc, nconv64);
-            itcg += itc;
-        }
+        it = snorm<double>(P, op64, d.maxgs, d.maxin, d.eps, pen, itc, nconv64);
+        itcg += itc;
         if (it == -2) status |= ST_NORMCG_DIV;
         itnorm = it >= 0 ? it : -1;
         if (d.norm == 0) {
@@ -628,14 +637,8 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
     long long t_tang0 = clock64();
     if (d.tang != 0 && ncon > 0 && itnorm >= 0) {
         int it = 0, itg = 0;
-        if (mixed) {
-            it = stang<float>(P, op32, d.eps32, itg, solver, nconv32, nls);
-            itgs += itg;
-        }
-        if (it > -1000) {
-            it = stang<double>(P, op64, d.eps, itg, solver, nconv64, nls);
-            itgs += itg;
-        }
+        it = stang(P, op64, mixed ? &op32 : nullptr, d.eps, d.eps32, itg, solver, nconv64, nconv32, nls);
+        itgs += itg;
         if (it == -1000) status |= ST_UNSUPPORTED;
         if (it == -2000) status |= ST_NOBRACKET;
         ittang = it >= 0 ? it : -1;
@@ -660,7 +663,12 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
         out[O_NLS] = nls;
         out[O_STATUS] = status;
         sm.t[0] = clock64() - t_start;
-        for (int k = 0; k < 8; k++) out[O_T_TOTAL + k] = (double)sm.t[k];
+        for (int k = 0; k < kNumPhaseTimers; k++) out[O_T_TOTAL + k] = (double)sm.t[k];
+        out[O_ALGB] = sm.algb;
+        unsigned long long g_end;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g_end));
+        out[O_TSTART] = (double)g_start;
+        out[O_TEND] = (double)g_end;
     }
 }
 
@@ -749,8 +757,14 @@ static cudaError_t ensure_smem_attr(size_t need) {
 }
 
 int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
-               int *d_list, cudaStream_t stream) {
+               int *d_list, cudaStream_t stream, EngineTimer *timer) {
+    if (timer) timer->nlaunch = 0;
     if (n <= 0) return 0;
+    auto mark = [&](int kind, bool after) {
+        if (!timer || timer->nlaunch >= EngineTimer::kMax) return;
+        cudaEventRecord(timer->ev[2 * timer->nlaunch + (after ? 1 : 0)], stream);
+        if (after) { timer->kind[timer->nlaunch] = kind; timer->nlaunch++; }
+    };
     // order: influence list first, then patches grouped by shared-memory class, largest first
     std::vector<int> ic_list, order(n);
     for (int i = 0; i < n; i++) { order[i] = i; if (compute_ic[i]) ic_list.push_back(i); }
@@ -780,8 +794,12 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
         }
         dim3 g((maxn + kThreads - 1) / kThreads, (unsigned)ic_list.size());
         if (g.x > 64) g.x = 64;
+        mark(0, false);
         k_influence<<<g, kThreads, 0, stream>>>(ddesc, d_ic);
+        mark(0, true);
+        mark(1, false);
         k_spectra<<<(unsigned)ic_list.size(), kThreads, smax, stream>>>(ddesc, d_ic);
+        mark(1, true);
         g_launches += 2;
     }
     // one launch per shared-memory class
@@ -791,7 +809,9 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
         int end = start + 1;
         // classes: group while the requirement stays within 25% of the first member
         while (end < n && solve_smem_bytes(hdesc[order[end]].fx, hdesc[order[end]].fy) * 5 >= sm0 * 4) end++;
+        mark(2, false);
         k_solve<<<end - start, kThreads, sm0, stream>>>(ddesc, d_order + start);
+        mark(2, true);
         g_launches += 1;
         start = end;
     }

@@ -16,6 +16,7 @@ enum WsCol {
     W_WSX, W_WSY, W_DPX, W_DPY, W_DSCL, W_NX, W_NY,          // TANG
     W_RX, W_RY, W_DVX, W_DVY, W_VX, W_VY, W_QX, W_QY,
     W_POX, W_POY, W_PDX, W_PDY, W_PNX, W_PNY, W_TRC, W_ZX, W_ZY, W_ONE,
+    W_DBX, W_DBY, W_SBX, W_SBY, W_TX, W_TY,                  // mixed precision: base dp, A dp_base, change
     W_NCOL
 };
 enum WsIntCol { I_IGS = 0, I_OLD, I_EXT, I_IEL, I_NCOL };
@@ -26,6 +27,9 @@ enum OutScalar {
     O_IERR, O_ITNORM, O_ITTANG, O_ITCG, O_ITGS, O_SOLVER, O_NCON, O_NADH, O_NSLIP,
     O_NCONV32, O_NCONV64, O_NLS, O_STATUS,
     O_T_TOTAL, O_T_CONV, O_T_LS, O_T_DIAG, O_T_GS, O_T_NORM, O_T_TANG, O_T_SCAN,   // SM clock cycles
+    O_T_CONV32,                            // SM cycles in FP32 convolutions (part of O_T_CONV)
+    O_ALGB,                                // algorithmic bytes of the convolutions (inputs, spectra, outputs)
+    O_TSTART, O_TEND,                      // global timer (ns) at the start and end of the solve
     O_NSCAL
 };
 
@@ -65,6 +69,7 @@ struct PatchDesc {
     void *rbuf;                       // 2 * (fx+1) * my complex doubles
 };
 
+constexpr int kNumPhaseTimers = 9;   // O_T_TOTAL .. O_T_CONV32
 constexpr int kIoCols = W_HSTOT;      // W_H .. W_SN live in the io block
 
 __host__ __device__ inline size_t io_doubles(int npot) {

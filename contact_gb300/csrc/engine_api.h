@@ -28,8 +28,18 @@ size_t solve_smem_bytes(int fx, int fy);
 // spectra for patch i.  Patches are grouped by shared-memory class internally.
 // d_list is caller-owned device scratch for 2*n ints and must stay untouched until the
 // launched work has finished.  Returns a cudaError_t value.
+// Optional per-launch timing: when given, engine_run records ev[2k] before and ev[2k+1]
+// after its k-th kernel launch on 'stream' and sets kind[k] (0 influence coefficients,
+// 1 spectra, 2 patch solve).  The events are created by the caller.
+struct EngineTimer {
+    static constexpr int kMax = 32;
+    cudaEvent_t ev[2 * kMax];
+    int kind[kMax];
+    int nlaunch = 0;
+};
+
 int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
-               int *d_list, cudaStream_t stream);
+               int *d_list, cudaStream_t stream, EngineTimer *timer = nullptr);
 
 // smallest 2^a 3^b 5^c 7^d >= n, following opt_fft_size (src/m_aijpj.f90:1022-1119)
 int opt_fft_size(int n);

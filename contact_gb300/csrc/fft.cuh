@@ -216,6 +216,8 @@ struct Conv {
     C<T> *R0, *R1;          // global: nkx * my each, column-major [kx][iy]
     double scale;           // ga_inv / (NX NY)
     long long *tacc;        // shared accumulator of cycles spent in convolutions (may be null)
+    long long *tacc2;       // second cycle accumulator (may be null)
+    double *bacc;           // shared accumulator of algorithmic bytes (may be null)
 };
 
 // step A: forward row transforms of ncomp real inputs (element-major, mx*my doubles each)
@@ -365,7 +367,16 @@ __device__ void convolve(const Conv<T> &cv, const double *in0, const double *in1
     __syncthreads();
     conv_rows_inv<T>(cv, out0, out1, ncomp, mode, igs);
     __syncthreads();
-    if (threadIdx.x == 0 && cv.tacc) *cv.tacc += clock64() - t0;
+    if (threadIdx.x == 0) {
+        const long long dt = clock64() - t0;
+        if (cv.tacc) *cv.tacc += dt;
+        if (cv.tacc2) *cv.tacc2 += dt;
+        // algorithmic bytes: FP64 inputs and outputs, one real quadrant spectrum per block
+        if (cv.bacc) {
+            const int nblk = (K0 != nullptr) + (K1 != nullptr) + (K2 != nullptr);
+            *cv.bacc += 16.0 * ncomp * cv.mx * cv.my + (double)sizeof(T) * nblk * (cv.fx + 1) * (cv.fy + 1);
+        }
+    }
 }
 
 } // namespace cgb

@@ -26,8 +26,9 @@ struct SolverSmem {
     // generic broadcast slots
     double bd[8];
     int bi[8];
-    // phase timers (SM cycles), indexed like O_T_TOTAL .. O_T_SCAN
-    long long t[8];
+    // phase timers (SM cycles), indexed like O_T_TOTAL .. O_T_CONV32
+    long long t[kNumPhaseTimers];
+    double algb;      // algorithmic bytes of the convolutions so far
 };
 
 // thread 0 accumulates the cycles between a start mark and the end of a phase
@@ -483,6 +484,36 @@ struct TangState {
 // SteadyGS, m_solvpt.f90:2825-3254: element-by-element Gauss-Seidel in rolling order.
 // Each element's shift is a block reduction; thread 0 solves the element and propagates.
 // ------------------------------------------------------------------------------------------
+// Tangential row sum of SteadyGS: s = ga_inv * sum_j A_t(ii, j) dp(j) over the row extents of
+// the contact area (gf3_AijPj's row1st/rowlst rule).  The (jy, jx) pairs of the bounding box
+// of all row extents are spread over the whole block so that every thread loads its share of
+// coefficients and vectors independently.
+struct GsBox { int jy0, jx0, w, cnt; };
+
+__device__ inline void stdygs_rowsum(const PView &P, const GsBox &b, int ii, const double *dpx, const double *dpy,
+                                     double s[2]) {
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx, my = P.my;
+    const int ix = ii % mx + 1, iy = ii / mx + 1;
+    const int *ext = P.ci(I_EXT);
+    const size_t bsz = (size_t)4 * mx * my;
+    const double *cxx = d.cf, *cxy = d.cf + bsz, *cyy = d.cf + 2 * bsz;
+    double a[2] = {0.0, 0.0};
+    for (int k = threadIdx.x; k < b.cnt; k += kThreads) {
+        const int jy = b.jy0 + k / b.w, jx = b.jx0 + k % b.w;
+        const int j0 = max(1, ext[jy - 1] - 1), j1 = min(mx, ext[my + jy - 1] + 1);
+        if (jx < j0 || jx > j1) continue;
+        const size_t off = (size_t)(ix - jx + mx) + (size_t)(iy - jy + my) * 2 * mx;
+        const int jj = (jx - 1) + (jy - 1) * mx;
+        const double vx = dpx[jj], vy = dpy[jj], c01 = cxy[off];
+        a[0] += cxx[off] * vx + c01 * vy;
+        a[1] += c01 * vx + cyy[off] * vy;
+    }
+    block_sum<2>(P.sm->red, a);
+    s[0] = a[0] / d.ga;
+    s[1] = a[1] / d.ga;
+}
+
 __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double omegah, double omegas, int &info, double &err) {
     PHASE_START(tgs);
     const PatchDesc &d = *P.d;
@@ -504,10 +535,28 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
     count_eldiv(P, nadh, nslip, nplst, nexter);
     int k = nadh + nslip + nplst;
     double facnel = sqrt((double)(float)n / (double)(float)k);
+    // bounding box of the row extents (constant: the contact area does not change in TANG)
+    GsBox box;
+    {
+        const int *ext = P.ci(I_EXT);
+        if (threadIdx.x == 0) {
+            int jy0 = my + 1, jy1 = 0, jx0 = mx + 1, jx1 = 0;
+            for (int jy = 1; jy <= my; jy++) {
+                const int j0 = max(1, ext[jy - 1] - 1), j1 = min(mx, ext[my + jy - 1] + 1);
+                if (j0 > j1) continue;
+                jy0 = min(jy0, jy); jy1 = max(jy1, jy);
+                jx0 = min(jx0, j0); jx1 = max(jx1, j1);
+            }
+            P.sm->bi[0] = jy0; P.sm->bi[1] = jx0;
+            P.sm->bi[2] = jx1 >= jx0 ? jx1 - jx0 + 1 : 1;
+            P.sm->bi[3] = (jy1 >= jy0 && jx1 >= jx0) ? (jy1 - jy0 + 1) * (jx1 - jx0 + 1) : 0;
+        }
+        __syncthreads();
+        box.jy0 = P.sm->bi[0]; box.jx0 = P.sm->bi[1]; box.w = P.sm->bi[2]; box.cnt = P.sm->bi[3];
+        __syncthreads();
+    }
     int itgs = 0;
     double dif = 2.0, difid = 1.0, dif1 = 0.0;
-    const int blks[4] = {0, 1, 1, 2};
-    const int rid[4] = {0, 0, 1, 1};
     while (dif >= difid && itgs < maxgs) {
         itgs++;
         double difacc = 0.0;      // held by thread 0
@@ -515,9 +564,8 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
             for (int ix = ixsta; ix <= ixend; ix++) {
                 int ii = (ix - 1) + (iy - 1) * mx;
                 if (igs[ii] < Adhes) continue;
-                const double *vecs[4] = {dpx, dpy, dpx, dpy};
                 double s[2];
-                direct_rowsum(P, ii, 4, blks, vecs, s, rid, 2);
+                stdygs_rowsum(P, box, ii, dpx, dpy, s);
                 if (threadIdx.x == 0 && ix > ixsta) {
                     // the solver choice keeps the trailing column ix = 1 outside the contact area
                     int jx = ix - ixinc;
@@ -964,6 +1012,52 @@ __device__ __noinline__ void compute_slip(const PView &P, const Ops<T> &op, int 
     __syncthreads();
 }
 
+// Mixed precision slip s = ws + A dp, with A dp = A dp_b + A (dp - dp_b): the base product
+// A dp_b is an FP64 convolution, the change since the base an FP32 one.  The base is moved
+// to the current dp (and re-evaluated in FP64) when the change exceeds tau * |dp| (rms over
+// the grid); the FP32 part then carries at most ~tau times the FP32 rounding of the product.
+constexpr double kRefreshTau = 5e-5;
+
+__device__ __noinline__ void compute_slip_rr(const PView &P, const Ops<double> &op, const Ops<float> &o32,
+                                             bool &have_base, int &nconv64, int &nconv32) {
+    const int n = P.n;
+    const int *igs = P.igs();
+    const double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY);
+    double *dbx = P.c(W_DBX), *dby = P.c(W_DBY), *sbx = P.c(W_SBX), *sby = P.c(W_SBY);
+    double *tx = P.c(W_TX), *ty = P.c(W_TY);
+    double *sx = P.c(W_SX), *sy = P.c(W_SY);
+    const double *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+    bool refresh = !have_base;
+    if (have_base) {
+        double a[2] = {0.0, 0.0};
+        FOR_I(i, n) {
+            const double ex = dpx[i] - dbx[i], ey = dpy[i] - dby[i];
+            tx[i] = ex; ty[i] = ey;
+            a[0] += ex * ex + ey * ey;
+            a[1] += dpx[i] * dpx[i] + dpy[i] * dpy[i];
+        }
+        block_sum<2>(P.sm->red, a);
+        refresh = a[0] > kRefreshTau * kRefreshTau * a[1];
+    }
+    if (refresh) {
+        FOR_I(i, n) { dbx[i] = dpx[i]; dby[i] = dpy[i]; }
+        prod_t<double>(op, dbx, dby, sbx, sby, OUT_ALL, igs); nconv64++;
+        FOR_I(i, n) {
+            if (igs[i] >= Adhes) { sx[i] = sbx[i] + wsx[i]; sy[i] = sby[i] + wsy[i]; }
+            else { sx[i] = 0.0; sy[i] = 0.0; }
+        }
+        have_base = true;
+        __syncthreads();
+        return;
+    }
+    FOR_I(i, n) {
+        if (igs[i] >= Adhes) { sx[i] = sbx[i] + wsx[i]; sy[i] = sby[i] + wsy[i]; }
+        else { sx[i] = 0.0; sy[i] = 0.0; }
+    }
+    prod_t<float>(o32, tx, ty, sx, sy, OUT_ADDINT, igs); nconv32++;
+    __syncthreads();
+}
+
 __device__ __noinline__ void set_nt(const PView &P) {
     const double *px = P.c(W_PX), *py = P.c(W_PY);
     double *nx = P.c(W_NX), *ny = P.c(W_NY);
@@ -990,7 +1084,18 @@ __device__ __noinline__ void set_residual(const PView &P) {
 // lstagn as in the reference; returns -100000 when the line search has no bracket.
 template <typename T>
 __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd, double eps, double &err, bool &lstagn,
-                        int &nconv, int &nls) {
+                        int &nconv, int &nls, const Ops<float> *o32, int &nconv32) {
+    // o32 != nullptr (mixed precision, T = double): the search-direction product q = A v is an
+    // FP32 convolution and the slip s = ws + A dp is kept exact to FP64 level by an FP64 base
+    // product plus an FP32 product of the change since the base (compute_slip_rr).  The
+    // iteration itself, with all its decisions, stays the FP64 iteration from the same start.
+    bool have_base = false;
+    auto slip = [&]() {
+        if constexpr (sizeof(T) == 8) {
+            if (o32) { compute_slip_rr(P, op, *o32, have_base, nconv, nconv32); return; }
+        }
+        compute_slip<T>(P, op, nconv);
+    };
     const PatchDesc &d = *P.d;
     const int n = P.n, mx = P.mx, my = P.my;
     RedSmem &red = P.sm->red;
@@ -1024,7 +1129,7 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
     bool lchanged = false;
     lstagn = false;
     set_nt(P);
-    compute_slip<T>(P, op, nconv);
+    slip();
     compute_diagscaling(P, coefs);
     set_residual(P);
     {
@@ -1039,7 +1144,8 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
         if (beta > d.betath || itgd - it_fb <= 1) { imeth = d.gd_meth; kdown = d.kdown; }
         else { imeth = 2; kdown = d.kdowfb; it_fb = itgd; }
         project_searchdir(P, imeth, kdown, trc);
-        prod_t<T>(op, dvx, dvy, qx, qy, OUT_INT, igs); nconv++;
+        if (o32) { prod_t<float>(*o32, dvx, dvy, qx, qy, OUT_INT, igs); nconv32++; }
+        else { prod_t<T>(op, dvx, dvy, qx, qy, OUT_INT, igs); nconv++; }
         if (itgd <= 1) {
             double a[2] = {0, 0};
             FOR_I(i, n) { a[0] += rx[i] * rx[i] + ry[i] * ry[i]; a[1] += (rx[i] * qx[i] + ry[i] * qy[i]) * dscl[i]; }
@@ -1068,7 +1174,7 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
         }
         apply_trcbnd(P, trc, dpx, dpy, px, py);
         set_nt(P);
-        compute_slip<T>(P, op, nconv);
+        slip();
         // local optimisation (solve_elmtrc) and active-set updates
         int chg = 0;
         FOR_I(ii, n) {

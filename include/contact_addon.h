@@ -12,6 +12,7 @@
  *   cntc_getiterationcounts     iteration counts / solver used of the last solve
  *   cntc_gb300_kernel_launches  number of GPU kernels this library has launched
  *   cntc_gb300_getsolverstats   convolution counts and per-phase cycle counts of the last solve
+ *   cntc_gb300_resident_*       solve a staged batch repeatedly on device-resident inputs
  *   flag CNTC_if_mixedprec      (cntc_setflags) 1: FP32 convolutions + FP64 refinement
  */
 #ifndef CONTACT_GB300_ADDON_H
@@ -110,10 +111,27 @@ void cntc_finalizelast(void);
 /* extension: number of GPU kernels launched by this library since it was loaded */
 long long cntc_gb300_kernel_launches(void);
 /* extension: engine statistics of the last solve of (ire,icp): [0] FP32 convolutions,
- * [1] FP64 convolutions, [2] line-search steps, [3] status bits, [4..11] SM clock cycles
+ * [1] FP64 convolutions, [2] line-search steps, [3] status bits, [4..12] SM clock cycles
  * spent in: whole solve, convolutions, line search, diagonal scaling, Gauss-Seidel sweeps,
- * normal problem, tangential problem, row scans */
+ * normal problem, tangential problem, row scans, FP32 convolutions; [13] algorithmic bytes
+ * of the convolutions; [14], [15] GPU global timer (ns) at the start and end of the solve */
 void cntc_gb300_getsolverstats(int *ire, int *icp, int *lenarr, double *values);
+
+/* extension (no reference counterpart): resident batch for throughput measurement.
+ * setup prepares the n problems (ire[i], icp[i]) and stages their inputs in device memory
+ * (ierror[i] as cntc_calculate for problems that cannot be prepared); solve runs the whole
+ * engine nrep times on the staged inputs, influence coefficients included, and writes per
+ * run 4 values: device ms of the pass, ms in patch-solve kernels, ms in influence/spectrum
+ * kernels (CUDA events on the launching stream) and the number of launches; collect copies
+ * the results of the last run back to the problems (getters then work as after
+ * cntc_calculate); release frees the device memory. */
+void cntc_gb300_resident_setup(int *n, int *ire, int *icp, int *ierror);
+/* extension: bytes copied host->device and device->host by the calling thread's last
+ * cntc_calculate / cntc_calculate_batch */
+void cntc_gb300_lastcopybytes(long long *h2d, long long *d2h);
+void cntc_gb300_resident_solve(int *nrep, double *times, int *ierror);
+void cntc_gb300_resident_collect(int *n, int *ierror);
+void cntc_gb300_resident_release(void);
 
 #ifdef __cplusplus
 }

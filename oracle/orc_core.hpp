@@ -291,7 +291,8 @@ inline void fft2d(std::vector<cplx> &a, int nx, int ny, bool inv) {
     }
 }
 
-// opt_fft_size, m_aijpj.f90:1022-1119: smallest 2^a 3^b 5^c 7^d >= n, reached by trading factors
+// opt_fft_size, m_aijpj.f90:1022-1119: a 2^a 3^b 5^c 7^d >= n found greedily, starting from the next
+// power of two and trading factors while the product stays >= n (not always the smallest such number)
 inline int opt_fft_size(int fft_size) {
     static const int kpat[9][8] = {
         {-2, 1, 0, 0, 0, 4, 3, 3},   {-5, 3, 0, 0, 0, 32, 27, 3},  {-1, -1, 1, 0, 0, 6, 5, 5},

@@ -1,0 +1,185 @@
+"""The CPU oracle against the reference's own regression outputs (CPU only).
+
+test_table_mx11.json holds the 3220 printed lines of src/test_table.f90 (testbank/
+test_table_mx11.ref_fx); tractcurv_series1.json the first series of examples/tractcurv.inp
+(examples/tractcurv.ref_out).  The oracle has to reproduce both at their printed precision
+before any GPU result is compared with it.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import cases as C
+import contact_gb300 as cg
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _load(name):
+    with open(os.path.join(GOLD, name)) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="module")
+def tt_gold():
+    return _load("test_table_mx11.json")
+
+
+@pytest.fixture(scope="module")
+def tc_gold():
+    return _load("tractcurv_series1.json")
+
+
+@pytest.fixture(scope="module")
+def tt_hertz(oracle):
+    """rho and cp per ellipticity as test_table computes them: a first solve of the base case
+    (src/test_table.f90:150-185)."""
+    rho, cp = [], []
+    for iell in range(5):
+        r = C.oracle_solve(C.test_table_base(iell))
+        rho.append(r["rho"])
+        cp.append(r["cp"])
+    return rho, cp
+
+
+def fmt_tt(r, cp):
+    """One output line of test_table (src/test_table.f90:270-281)."""
+    fx = r["fx"] / (0.3 * r["fn"])
+    fy = r["fy"] / (0.3 * r["fn"])
+    mz = r["mz"] / (0.3 * r["fn"] * cp)
+    slip = float(np.float32(100 * r["nslip"]) / np.float32(r["ncon"]))
+    s = "Fx=%11.6f, Fy=%11.6f, Mz=%11.6f, %%Slip=%6.1f" % (fx, fy, mz, slip)
+    return s.replace("-0.000000", " 0.000000")
+
+
+def test_hertz_rho_cp(tt_gold, tt_hertz):
+    rho, cp = tt_hertz
+    for iell, h in enumerate(tt_gold["hertz"]):
+        assert float("%.4g" % rho[iell]) == pytest.approx(h["rho"], rel=1e-12)
+        assert float("%.4g" % cp[iell]) == pytest.approx(h["cp"], rel=1e-12)
+
+
+@pytest.mark.parametrize("part", range(4))
+def test_table_all_cases(oracle, tt_gold, tt_hertz, part):
+    """All 3220 lines reproduced character for character (4 parts of 805 cases)."""
+    rho, cp = tt_hertz
+    bad = []
+    for icase in range(part * 805, (part + 1) * 805):
+        case, iell = C.test_table_case(icase, rho, cp)
+        pb, _ = C.to_oracle(case)
+        r = oracle.solve(pb, fields=False)
+        g = tt_gold["cases"][icase]
+        ref = "Fx=%11.6f, Fy=%11.6f, Mz=%11.6f, %%Slip=%6.1f" % tuple(g)
+        if fmt_tt(r, cp[iell]) != ref.replace("-0.000000", " 0.000000"):
+            bad.append((icase, fmt_tt(r, cp[iell]), ref))
+    assert not bad, bad[:5]
+
+
+def _close4(a, b):
+    """Equal to the 4 significant digits printed by the reference."""
+    if b == 0:
+        return abs(a) < 5e-4
+    e = math.floor(math.log10(abs(b)))
+    return abs(a - b) <= 0.5 * 10 ** (e - 3) * 1.01
+
+
+def test_tractcurv_series(oracle, tc_gold):
+    """Forces, energy, approach, pmax at 4 digits; element counts, iteration counts and the
+    element-division picture exactly."""
+    for c in tc_gold["cases"]:
+        r = C.oracle_solve(C.tractcurv_case(c["cksi"]))
+        assert r["ierror"] == 0
+        for k_me, k_ref in (("fx", "fx"), ("elen", "elen"), ("pmax", "pmax"), ("pen", "approach"), ("fn", "fn")):
+            assert _close4(r[k_me], c[k_ref]), (c["case"], k_me, r[k_me], c[k_ref])
+        assert (r["ncon"], r["nadh"], r["nslip"]) == (c["ncon"], c["nadh"], c["nslip"]), c["case"]
+        assert (r["itcg"], r["itgs"]) == (c["itcg"], c["itgs"]), c["case"]
+        sym = np.array([".", "*", "S", "P"])[r["igs"]].reshape(44, 48)
+        pic = ["".join(row) for row in sym]
+        assert pic == [row.replace("o", ".") for row in c["picture"]], c["case"]
+
+
+def _opt_fft_size_py(n):
+    """Independent restatement of m_aijpj.f90:1022-1119: start at the next power of two and apply
+    the factor trades (e.g. 4 -> 3, 6 -> 5, 8 -> 7) while the product stays >= n."""
+    trades = [((-2, 1, 0, 0), 4, 3), ((-5, 3, 0, 0), 32, 27), ((-1, -1, 1, 0), 6, 5), ((-4, 1, 1, 0), 16, 15),
+              ((0, -3, 2, 0), 27, 25), ((-3, 0, 0, 1), 8, 7), ((1, -1, -1, 1), 15, 14), ((-1, 2, -1, 0), 10, 9)]
+    k = [max(0, math.ceil(math.log(n) / math.log(2.0) - 1e-12)), 0, 0, 0]
+    prod = 2 ** k[0]
+    changed = True
+    while changed:
+        changed = False
+        for dk, den, num in trades:
+            while all(k[f] + dk[f] >= 0 for f in range(4)) and num * prod >= den * n:
+                k = [k[f] + dk[f] for f in range(4)]
+                prod = num * prod // den
+                changed = True
+    return prod
+
+
+def test_opt_fft_size(oracle):
+    """FFT sizes of the reference (m_aijpj.f90:1022-1119): 7-smooth, >= n, the greedy choice."""
+    def smooth(v):
+        for q in (2, 3, 5, 7):
+            while v % q == 0:
+                v //= q
+        return v == 1
+    for n in list(range(1, 600)) + [1000, 1023, 1025, 2047, 2048, 4097]:
+        m = oracle.opt_fft_size(n)
+        assert m >= n and smooth(m) and m < 1.25 * n + 2
+        assert m == _opt_fft_size_py(n), n
+        assert m == cg.opt_fft_size(n), n
+    assert [oracle.opt_fft_size(n) for n in (33, 35, 51, 65, 100)] == [36, 36, 54, 72, 100]
+
+
+def test_elliptic_integrals(oracle):
+    """Complete elliptic integrals K, E of m_hertz.f90 (eli) against scipy."""
+    sp = pytest.importorskip("scipy.special")
+    for k in (0.1, 0.3, 0.5, 0.7, 0.9, 0.99):
+        r, kk, ee = oracle.eli(k)
+        # eli takes the modulus k; scipy takes the parameter m = k^2
+        m = k * k
+        assert kk == pytest.approx(sp.ellipk(m), rel=1e-12)
+        assert ee == pytest.approx(sp.ellipe(m), rel=1e-12)
+
+
+def test_convolution_fft_equals_direct(oracle):
+    """fft_VecAijPj equals the direct sum gf3_VecAijPj (m_aijpj.f90:258-451, 712-1015)."""
+    rng = np.random.default_rng(5)
+    for mx, my in ((7, 5), (11, 11), (23, 17), (51, 51)):
+        cf = oracle.influence_coefficients(mx, my, 0.3, 0.2, 0.28)
+        for ik, jk in ((0, 0), (0, 1), (1, 1), (2, 2)):
+            p = rng.standard_normal((my, mx))
+            a = oracle.convolve(cf[ik, jk], 82000.0, p)
+            b = oracle.convolve(cf[ik, jk], 82000.0, p, direct=True)
+            assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+
+
+def test_influence_coefficient_symmetry(oracle):
+    """Boussinesq-Cerruti blocks: xx, yy, zz even in x and y, xy odd in both, xy = yx,
+    zero normal-tangential coupling for identical materials."""
+    mx, my = 9, 7
+    cf = oracle.influence_coefficients(mx, my, 0.25, 0.15, 0.28)
+    core = cf[:, :, 1:, 1:]           # offsets -(m-1)..(m-1)
+    for b in ((0, 0), (1, 1), (2, 2)):
+        c = core[b]
+        tol = 1e-13 * np.abs(c).max()
+        assert np.abs(c - c[::-1, :]).max() <= tol and np.abs(c - c[:, ::-1]).max() <= tol
+    xy = core[0, 1]
+    tol = 1e-13 * np.abs(xy).max()
+    assert np.abs(xy + xy[:, ::-1]).max() <= tol and np.abs(xy + xy[::-1, :]).max() <= tol
+    assert np.array_equal(cf[0, 1], cf[1, 0])
+    assert np.abs(cf[0, 2]).max() == 0 and np.abs(cf[2, 0]).max() == 0
+
+
+def test_gdsteady_matches_steadygs(oracle):
+    """Two solvers of the same steady rolling problem (GDsteady unpinned by reference fixtures):
+    at eps 1e-10 they agree to the convergence tolerance."""
+    g0 = C.oracle_solve(C.config0(gausei=0, eps=1e-10, mx=31, my=31))
+    g5 = C.oracle_solve(C.config0(gausei=5, eps=1e-10, mx=31, my=31))
+    assert g0["ierror"] == 0 and g5["ierror"] == 0
+    assert np.array_equal(g0["igs"], g5["igs"])
+    assert abs(g5["fx"] - g0["fx"]) <= 1e-9 * abs(g0["fx"])
+    assert np.abs(g5["px"] - g0["px"]).max() <= 1e-8 * np.abs(g0["pn"]).max()
