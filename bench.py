@@ -50,11 +50,19 @@ def parse():
                     help="patches of the same workload solved in plain FP64 for the mixed/plain ratio")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="wall-clock budget of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--max-side", type=int, default=0,
+                    help="profiling aid: keep only patches with both sides <= this (0: all)")
     return ap.parse_args()
 
 
-def workload(n, seed, mixed=1):
-    return C.batch_patches(n, seed=seed, mixed=mixed, eps=1e-8)
+MIXED_TIER = 2     # FP32 convolution products, scaling and local solves; FP64 iteration path
+
+
+def workload(n, seed, mixed=MIXED_TIER, max_side=0):
+    if max_side <= 0:
+        return C.batch_patches(n, seed=seed, mixed=mixed, eps=1e-8)
+    allc = C.batch_patches(4096, seed=seed, mixed=mixed, eps=1e-8)
+    return [c for c in allc if c["potprm"][0] <= max_side and c["potprm"][1] <= max_side][:n]
 
 
 def fft_proxy(case):
@@ -250,7 +258,7 @@ def run_gb300(args, dist):
     import contact_gb300 as cg
     torch.cuda.set_device(dist.local)
     cg.load()
-    cases = workload(args.patches, args.seed, mixed=1)
+    cases = workload(args.patches, args.seed, mixed=MIXED_TIER, max_side=args.max_side)
     n = len(cases)
     ire, icp = setup_problems(cg, cases)
     rb = cg.ResidentBatch(ire, icp)
@@ -291,6 +299,7 @@ def run_gb300(args, dist):
         itgd = r["itgs"] if r["solver"] == 7 else 0
         alg += s["conv_bytes"] + 8.0 * npot * (12 * r["itcg"] + 20 * itgd + 16 * s["nls"])
     solve_ms = float(times[-1, 1])
+    sm_cycles = float(sum(s["t_total"] for s in stats))
     nsolve_launch = int(round(times[-1, 3])) - (2 if ic_ms > 0 else 0)
     peak, peak_kind = measured_peaks()
     achieved = alg / (solve_ms / 1e3) / 1e9
@@ -319,16 +328,27 @@ def run_gb300(args, dist):
         prb = cg.ResidentBatch(pire, picp)
         prb.solve(1)
         pt = prb.solve(1)
+        prb.collect()
         prb.release()
-        mixed_sample_ms = None
         mrb = cg.ResidentBatch(ire[:args.plain_sample], icp[:args.plain_sample])
         mrb.solve(1)
         mt = mrb.solve(1)
+        mrb.collect()
         mrb.release()
         mixed_sample_ms = float(mt[0, 0])
+        # force error of the mixed form against the FP64 form on the same patches
+        ferr = []
+        for i, c in zip(pire, pc):
+            a, b = cg.results(i, 1), cg.results(i, 2)
+            ft = math.hypot(b["fx"], b["fy"])
+            ferr.append(math.hypot(a["fx"] - b["fx"], a["fy"] - b["fy"]) / max(ft, 1e-3 * c["fstat"] * abs(b["fn"])))
+        ferr = np.array(ferr)
         plain = {"patches": len(pc), "solves_per_s": len(pc) / (float(pt[0, 0]) / 1e3),
                  "mixed_solves_per_s_same_sample": len(pc) / (mixed_sample_ms / 1e3),
-                 "note": "first %d patches of the workload, eps 1e-8, FP64 throughout" % len(pc)}
+                 "mixed_force_rel_err": {"max": float(ferr.max()), "p99": float(np.percentile(ferr, 99)),
+                                         "median": float(np.median(ferr)), "above_1e-8": int((ferr > 1e-8).sum())},
+                 "note": "first %d patches of the workload, eps 1e-8, FP64 throughout; force error = |dF_t| / "
+                         "max(|F_t|, 1e-3 mu Fn) of the mixed form against this FP64 form" % len(pc)}
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         rate, thr, desc = cpu_sample_rate(cases, args.cpu_seconds, args.seed)
@@ -346,6 +366,7 @@ def run_gb300(args, dist):
         "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
                        "definition": "completion time of each patch since the start of its step (batched)"},
         "failed_patches": nfail,
+        "sm_gcycles_per_step": sm_cycles / 1e9,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "kernel": "k_solve",
                      "launches_per_step": nsolve_launch, "peak_source": peak_kind},

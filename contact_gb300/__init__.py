@@ -427,7 +427,8 @@ def results(ire, icp):
     pn, px, py = gettractions(ire, icp)
     carea, harea, sarea = getcontactpatchareas(ire, icp)
     dx, dy = getgriddiscretization(ire, icp)
-    out = dict(fn=fn, fx=fx, fy=fy, mz=mz, pn=pn, px=px, py=py, pen=getpenetration(ire, icp),
+    mx, my = getnumelements(ire, icp)
+    out = dict(fn=fn, fx=fx, fy=fy, mz=mz, pn=pn, px=px, py=py, pen=getpenetration(ire, icp), mx=mx, my=my,
                pmax=getmaximumpressure(ire, icp), igs=getelementdivision(ire, icp),
                ncon=int(round(carea / (dx * dy))), nadh=int(round(harea / (dx * dy))),
                nslip=int(round(sarea / (dx * dy))), dx=dx, dy=dy)

@@ -572,7 +572,7 @@ void cntc_setflags(int *ire, int *icp, int *lenflg, int *params, int *values) {
             case CNTC_ic_flow: p->flow = std::max(0, std::min(9, v)); break;
             case CNTC_ic_return: p->ret = std::max(0, std::min(3, v)); break;
             case CNTC_if_ncase: p->ncase = std::max(0, v - 1); break;
-            case CNTC_if_mixedprec: p->mixed = (v != 0) ? 1 : 0; break;
+            case CNTC_if_mixedprec: p->mixed = (v >= 0 && v <= 3) ? v : 1; break;
             default: break;   // output, debugging and module-1 flags have no effect here
         }
     }

@@ -579,7 +579,7 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
     make_twiddles<double>(op64.cv.twx, sp.NX);
     make_twiddles<double>(op64.cv.twy, sp.NY);
     Ops<float> op32;
-    const bool mixed = d.precision == 1;
+    const bool mixed = d.precision >= 1;
     if (mixed) {
         make_ops<float>(op32, d, smraw, sp);
         op32.cv.tacc = &sm.t[O_T_CONV - O_T_TOTAL];
@@ -756,6 +756,29 @@ static cudaError_t ensure_smem_attr(size_t need) {
     return e;
 }
 
+// side streams of the calling host thread (created once, never destroyed before exit)
+struct SideStreams {
+    static constexpr int kN = 16;
+    cudaStream_t s[kN];
+    cudaEvent_t fork, join[kN];
+    bool ok = false;
+};
+
+static SideStreams &side_streams() {
+    thread_local SideStreams ss;
+    thread_local bool init = false;
+    if (!init) {
+        init = true;
+        bool ok = cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) == cudaSuccess;
+        for (int k = 0; k < SideStreams::kN && ok; k++) {
+            ok = cudaStreamCreateWithFlags(&ss.s[k], cudaStreamNonBlocking) == cudaSuccess &&
+                 cudaEventCreateWithFlags(&ss.join[k], cudaEventDisableTiming) == cudaSuccess;
+        }
+        ss.ok = ok;
+    }
+    return ss;
+}
+
 int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
                int *d_list, cudaStream_t stream, EngineTimer *timer) {
     if (timer) timer->nlaunch = 0;
@@ -802,19 +825,34 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
         mark(1, true);
         g_launches += 2;
     }
-    // one launch per shared-memory class
-    int start = 0;
-    while (start < n) {
-        size_t sm0 = solve_smem_bytes(hdesc[order[start]].fx, hdesc[order[start]].fy);
+    // one launch per shared-memory class (requirement within 25% of the class's first, largest
+    // member); the classes run concurrently on side streams so that the SMs freed by one class
+    // take CTAs of the others instead of idling until the slowest patch of a class finishes
+    std::vector<std::pair<int, int>> classes;
+    for (int start = 0; start < n;) {
+        const size_t sm0 = solve_smem_bytes(hdesc[order[start]].fx, hdesc[order[start]].fy);
         int end = start + 1;
-        // classes: group while the requirement stays within 25% of the first member
         while (end < n && solve_smem_bytes(hdesc[order[end]].fx, hdesc[order[end]].fy) * 5 >= sm0 * 4) end++;
-        mark(2, false);
-        k_solve<<<end - start, kThreads, sm0, stream>>>(ddesc, d_order + start);
-        mark(2, true);
-        g_launches += 1;
+        classes.push_back({start, end});
         start = end;
     }
+    SideStreams &ss = side_streams();
+    if (!ss.ok) return (int)cudaErrorNotReady;
+    mark(2, false);
+    if ((e = cudaEventRecord(ss.fork, stream)) != cudaSuccess) return (int)e;
+    for (size_t c = 0; c < classes.size(); c++) {
+        cudaStream_t sc = ss.s[c % SideStreams::kN];
+        if (c < (size_t)SideStreams::kN && (e = cudaStreamWaitEvent(sc, ss.fork, 0)) != cudaSuccess) return (int)e;
+        const int start = classes[c].first, cnt = classes[c].second - classes[c].first;
+        const size_t sm0 = solve_smem_bytes(hdesc[order[start]].fx, hdesc[order[start]].fy);
+        k_solve<<<cnt, kThreads, sm0, sc>>>(ddesc, d_order + start);
+        g_launches += 1;
+    }
+    for (int k = 0; k < SideStreams::kN && k < (int)classes.size(); k++) {
+        if ((e = cudaEventRecord(ss.join[k], ss.s[k])) != cudaSuccess) return (int)e;
+        if ((e = cudaStreamWaitEvent(stream, ss.join[k], 0)) != cudaSuccess) return (int)e;
+    }
+    mark(2, true);
     return (int)cudaGetLastError();
 }
 

@@ -17,7 +17,8 @@ enum WsCol {
     W_RX, W_RY, W_DVX, W_DVY, W_VX, W_VY, W_QX, W_QY,
     W_POX, W_POY, W_PDX, W_PDY, W_PNX, W_PNY, W_TRC, W_ZX, W_ZY, W_ONE,
     W_DBX, W_DBY, W_SBX, W_SBY, W_TX, W_TY,                  // mixed precision: base dp, A dp_base, change
-    W_NCOL
+    W_FLS,                                                   // 9 columns: 18 float columns of the line search
+    W_NCOL = W_FLS + 9
 };
 enum WsIntCol { I_IGS = 0, I_OLD, I_EXT, I_IEL, I_NCOL };
 
@@ -54,7 +55,7 @@ struct PatchDesc {
     double aa, bb;
     int ibase;
     double prm[6];
-    int precision;                    // 0: FP64 throughout; 1: FP32 convolutions + FP64 refinement
+    int precision;                    // 0: FP64 throughout; 1-3: mixed-precision tiers (see gdsteady)
     double eps32;                     // tolerance of the FP32 phase
     int pad_;
     // io block: columns W_H .. W_SN (kIoCols * npot doubles), then O_NSCAL output scalars,

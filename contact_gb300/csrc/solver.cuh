@@ -48,6 +48,8 @@ struct PView {
     }
     __device__ int *igs() const { return (int *)(d->io + (size_t)kIoCols * n + O_NSCAL); }
     __device__ double *out() const { return d->io + (size_t)kIoCols * n; }
+    // float columns 0..17 inside the double columns W_FLS .. W_FLS + 8
+    __device__ float *f(int k) const { return (float *)c(W_FLS) + (size_t)k * n; }
 };
 
 #define FOR_I(i, n) for (int i = threadIdx.x; i < (n); i += kThreads)
@@ -388,31 +390,32 @@ __device__ __noinline__ int snorm(const PView &P, const Ops<T> &op, int maxgs, i
 // single-element solver plstrc for an elastic element (m_solvpt.f90:3278-3807, no plasticity;
 // the plastic trial of the reference cannot succeed there and leaves the element in adhesion)
 // ------------------------------------------------------------------------------------------
-__device__ __noinline__ void elm_solve(int &el, const double coef[2][2], double eps, double omegah, double omegas,
-                                 double pr[3], double mus, double s[2]) {
+template <typename R>
+__device__ __noinline__ void elm_solve(int &el, const R coef[2][2], R eps, R omegah, R omegas, R pr[3], R mus, R s[2]) {
     const int maxnr = 10;
-    const double prc = 0.0001;
-    const double taucs = 1e20;
-    double pold1 = pr[0], pold2 = pr[1];
-    double si0[2], si[2] = {0.0, 0.0}, dp[2], fk[2], gradf[2][2];
+    const R prc = R(0.0001);
+    const R taucs = R(1e20);
+    const R zero = R(0), two = R(2);
+    R pold1 = pr[0], pold2 = pr[1];
+    R si0[2], si[2] = {zero, zero}, dp[2], fk[2], gradf[2][2];
     si0[0] = s[0] - coef[0][0] * pr[0] - coef[0][1] * pr[1];
     si0[1] = s[1] - coef[1][0] * pr[0] - coef[1][1] * pr[1];
     int itry = 0, violat = 1;
-    double trc_bound = 0.0;
+    R trc_bound = zero;
     while (itry <= 3 && violat == 1) {
         itry++;
         if (el == Adhes) {
             trc_bound = mus * pr[2];
-            double detinv = 1.0 / (coef[0][0] * coef[1][1] - coef[0][1] * coef[1][0]);
+            R detinv = R(1) / (coef[0][0] * coef[1][1] - coef[0][1] * coef[1][0]);
             dp[0] = (-coef[1][1] * s[0] + coef[0][1] * s[1]) * detinv;
             dp[1] = (coef[1][0] * s[0] - coef[0][0] * s[1]) * detinv;
             pr[0] = pold1 + omegah * dp[0];
             pr[1] = pold2 + omegah * dp[1];
-            double pabs2 = sqrt(pr[0] * pr[0] + pr[1] * pr[1]);
-            double bnd = fmin(trc_bound, taucs);
+            R pabs2 = sqrt(pr[0] * pr[0] + pr[1] * pr[1]);
+            R bnd = fmin(trc_bound, taucs);
             if (pabs2 <= bnd) violat = 0;
             else {
-                double pabs1 = sqrt((pold1 + dp[0]) * (pold1 + dp[0]) + (pold2 + dp[1]) * (pold2 + dp[1]));
+                R pabs1 = sqrt((pold1 + dp[0]) * (pold1 + dp[0]) + (pold2 + dp[1]) * (pold2 + dp[1]));
                 if (pabs1 <= bnd) { pr[0] = pr[0] * bnd / pabs2; pr[1] = pr[1] * bnd / pabs2; violat = 0; }
                 else violat = 1;
             }
@@ -421,7 +424,7 @@ __device__ __noinline__ void elm_solve(int &el, const double coef[2][2], double 
         } else if (el == Slip) {
             violat = 0;
             trc_bound = mus * pr[2];
-            double sabs = sqrt(si0[0] * si0[0] + si0[1] * si0[1]);
+            R sabs = sqrt(si0[0] * si0[0] + si0[1] * si0[1]);
             pr[0] = -trc_bound * si0[0] / sabs;
             pr[1] = -trc_bound * si0[1] / sabs;
             si[0] = si0[0] + coef[0][0] * pr[0] + coef[0][1] * pr[1];
@@ -431,12 +434,12 @@ __device__ __noinline__ void elm_solve(int &el, const double coef[2][2], double 
             int itnr = 0;
             while (itnr == 0 || (itnr < maxnr && fabs(fk[0]) + fabs(fk[1]) >= prc * eps * trc_bound)) {
                 itnr++;
-                gradf[0][0] = -2.0 * coef[1][0] * pr[0] - si0[1] + (coef[0][0] - coef[1][1]) * pr[1];
-                gradf[0][1] = 2.0 * coef[0][1] * pr[1] + si0[0] + (coef[0][0] - coef[1][1]) * pr[0];
-                gradf[1][0] = 2.0 * pr[0];
-                gradf[1][1] = 2.0 * pr[1];
-                double det = gradf[0][0] * gradf[1][1] - gradf[0][1] * gradf[1][0];
-                if (det == 0.0) itnr = maxnr;
+                gradf[0][0] = -two * coef[1][0] * pr[0] - si0[1] + (coef[0][0] - coef[1][1]) * pr[1];
+                gradf[0][1] = two * coef[0][1] * pr[1] + si0[0] + (coef[0][0] - coef[1][1]) * pr[0];
+                gradf[1][0] = two * pr[0];
+                gradf[1][1] = two * pr[1];
+                R det = gradf[0][0] * gradf[1][1] - gradf[0][1] * gradf[1][0];
+                if (det == zero) itnr = maxnr;
                 else {
                     dp[0] = -(gradf[1][1] * fk[0] - gradf[0][1] * fk[1]) / det;
                     dp[1] = -(-gradf[1][0] * fk[0] + gradf[0][0] * fk[1]) / det;
@@ -447,23 +450,23 @@ __device__ __noinline__ void elm_solve(int &el, const double coef[2][2], double 
                 fk[0] = pr[1] * si[0] - pr[0] * si[1];
                 fk[1] = pr[0] * pr[0] + pr[1] * pr[1] - trc_bound * trc_bound;
             }
-            double alph0 = atan2(pold2, pold1);
-            double alph1 = atan2(pr[1], pr[0]);
-            double dalph = alph1 - alph0;
-            const double pi = 3.14159265358979323846;
-            if (dalph < -pi) dalph += 2.0 * pi;
-            if (dalph > pi) dalph -= 2.0 * pi;
+            R alph0 = atan2(pold2, pold1);
+            R alph1 = atan2(pr[1], pr[0]);
+            R dalph = alph1 - alph0;
+            const R pi = R(3.14159265358979323846);
+            if (dalph < -pi) dalph += two * pi;
+            if (dalph > pi) dalph -= two * pi;
             alph1 = alph0 + omegas * dalph;
-            double sn, cs;
+            R sn, cs;
             sincos(alph1, &sn, &cs);
             pr[0] = trc_bound * cs;
             pr[1] = trc_bound * sn;
-            if (fabs(pr[0]) > fabs(pr[1])) { if (pr[0] * si[0] > 0.0) violat = 1; }
-            else { if (pr[1] * si[1] > 0.0) violat = 1; }
+            if (fabs(pr[0]) > fabs(pr[1])) { if (pr[0] * si[0] > zero) violat = 1; }
+            else { if (pr[1] * si[1] > zero) violat = 1; }
         } else {
             // plastic trial: with an infinite yield limit it is always rejected
             trc_bound = mus * pr[2];
-            si[0] = 0.0; si[1] = 0.0;
+            si[0] = zero; si[1] = zero;
             violat = 1;
         }
         if (itry <= 3 && violat == 1) {
@@ -633,23 +636,24 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
 // GDsteady helpers (gdsteady.f90:610-1462); rows are scanned from the leading edge (ix = mx)
 // towards the trailing edge, one thread per row.
 // ------------------------------------------------------------------------------------------
-__device__ __noinline__ void apply_trcbnd(const PView &P, const double *trc, double *dpx, double *dpy, double *px,
-                                    double *py) {
+template <typename R>
+__device__ __noinline__ void apply_trcbnd(const PView &P, const R *trc, R *dpx, R *dpy, R *px, R *py) {
     const int mx = P.mx, my = P.my;
     const int *igs = P.igs();
     __syncthreads();
     PHASE_START(tsc);
+    const R zero = R(0);
     for (int iy = threadIdx.x; iy < my; iy += kThreads) {
         int ii = (mx - 1) + iy * mx;
-        px[ii] = 0.0; py[ii] = 0.0;
-        double pxn = 0.0, pyn = 0.0;
+        px[ii] = zero; py[ii] = zero;
+        R pxn = zero, pyn = zero;
         for (int ix = mx - 2; ix >= 0; ix--) {
             ii = ix + iy * mx;
-            double qx, qy;
-            if (igs[ii] <= Exter) { qx = 0.0; qy = 0.0; }
+            R qx, qy;
+            if (igs[ii] <= Exter) { qx = zero; qy = zero; }
             else {
                 qx = pxn + dpx[ii]; qy = pyn + dpy[ii];
-                double ptabs = sqrt(qx * qx + qy * qy);
+                R ptabs = sqrt(qx * qx + qy * qy);
                 if (igs[ii] == Slip || ptabs >= trc[ii]) { qx = qx * trc[ii] / ptabs; qy = qy * trc[ii] / ptabs; }
             }
             px[ii] = qx; py[ii] = qy;
@@ -729,10 +733,11 @@ __device__ __noinline__ void project_searchdir(const PView &P, int imeth, int kd
 }
 
 // unit direction of the tangential traction: (cos, sin) of atan2(py, px), with (1, 0) for p = 0
-__device__ inline void unit_dir(double px, double py, double &nx, double &ny) {
-    double r = sqrt(px * px + py * py);
-    if (r > 0.0) { nx = px / r; ny = py / r; }
-    else { nx = (px < 0.0 || (px == 0.0 && signbit(px))) ? -1.0 : 1.0; ny = 0.0; if (signbit(py) && px == 0.0) nx = 1.0; }
+template <typename R>
+__device__ inline void unit_dir(R px, R py, R &nx, R &ny) {
+    R r = sqrt(px * px + py * py);
+    if (r > R(0)) { nx = px / r; ny = py / r; }
+    else { nx = (px < R(0) || (px == R(0) && signbit(px))) ? R(-1) : R(1); ny = R(0); if (signbit(py) && px == R(0)) nx = R(1); }
 }
 
 // compute_diagscaling, gdsteady.f90:901-1042.  In the reference 'elnew' and 'fac_s' carry over
@@ -741,50 +746,57 @@ __device__ inline void unit_dir(double px, double py, double &nx, double &ny) {
 // elements whose angle error stays below tiny_err after the perturbation.  All other
 // elements are independent and are handled in parallel; when a case (b) element exists the
 // whole pass is repeated serially with the reference's carry-over.
-__device__ inline double dscl_adhesion(const PatchDesc &d, const int *igs, int ii, int mx, double old) {
+template <typename R>
+__device__ inline R dscl_adhesion(const PatchDesc &d, const int *igs, int ii, int mx, R old) {
     const int ix = ii % mx + 1;
     int jx = ix;
     while (jx > 1 && igs[ii - ix + jx] == Adhes) jx--;
-    double dn;
-    if (d.d_cns < d.d_ifc) dn = fmax(d.d_cns, d.d_ifc + (ix - jx - 1) * fmin(0.0, d.d_lin));
-    else dn = fmin(d.d_cns, d.d_ifc + (ix - jx - 1) * fmax(0.0, d.d_lin));
-    return fmin(50.0 * old, dn);
+    const R d_cns = (R)d.d_cns, d_ifc = (R)d.d_ifc, d_lin = (R)d.d_lin;
+    R dn;
+    if (d_cns < d_ifc) dn = fmax(d_cns, d_ifc + R(ix - jx - 1) * fmin(R(0), d_lin));
+    else dn = fmin(d_cns, d_ifc + R(ix - jx - 1) * fmax(R(0), d_lin));
+    return fmin(R(50) * old, dn);
 }
 
 // angle error of a slip element (perturbed once when it is tiny); returns false if it stays tiny
-__device__ inline bool slip_element(const PatchDesc &d, const double coefs[2][2], double px, double py, double pn,
-                                    double sx, double sy, int &elnew, double &fac_s) {
-    const double tiny_err = 1e-6, pi = 3.14159265358979323846;
-    double pr[3] = {px, py, pn};
-    double si[2] = {sx, sy};
-    double th_p0 = atan2(pr[1], pr[0]);
-    double th_s0 = atan2(-si[1], -si[0]);
-    double err_0 = th_s0 - th_p0;
-    if (fabs(err_0) >= pi) err_0 = err_0 - rint(err_0 / (2.0 * pi)) * 2.0 * pi;
+template <typename R>
+__device__ inline bool slip_element(const PatchDesc &d, const R coefs[2][2], R px, R py, R pn, R sx, R sy, int &elnew,
+                                    R &fac_s) {
+    const R tiny_err = R(1e-6), pi = R(3.14159265358979323846), two = R(2);
+    const R fstat = (R)d.fstat;
+    R pr[3] = {px, py, pn};
+    R si[2] = {sx, sy};
+    R th_p0 = atan2(pr[1], pr[0]);
+    R th_s0 = atan2(-si[1], -si[0]);
+    R err_0 = th_s0 - th_p0;
+    if (fabs(err_0) >= pi) err_0 = err_0 - rint(err_0 / (two * pi)) * two * pi;
     if (fabs(err_0) <= tiny_err) {
-        double c, s; sincos(th_p0 + 0.1, &s, &c);
-        pr[0] = d.fstat * pr[2] * c;
-        pr[1] = d.fstat * pr[2] * s;
+        R c, s; sincos(th_p0 + R(0.1), &s, &c);
+        pr[0] = fstat * pr[2] * c;
+        pr[1] = fstat * pr[2] * s;
         si[0] = sx + coefs[0][0] * (pr[0] - px) + coefs[0][1] * (pr[1] - py);
         si[1] = sy + coefs[1][0] * (pr[0] - px) + coefs[1][1] * (pr[1] - py);
         th_p0 = atan2(pr[1], pr[0]);
         th_s0 = atan2(-si[1], -si[0]);
         err_0 = th_s0 - th_p0;
-        if (fabs(err_0) >= pi) err_0 = err_0 - rint(err_0 / (2.0 * pi)) * 2.0 * pi;
+        if (fabs(err_0) >= pi) err_0 = err_0 - rint(err_0 / (two * pi)) * two * pi;
     }
     if (fabs(err_0) <= tiny_err) return false;
     elnew = Slip;
-    elm_solve(elnew, coefs, 1e-6, 1.0, 1.0, pr, d.fstat, si);
+    elm_solve<R>(elnew, coefs, R(1e-6), R(1), R(1), pr, fstat, si);
     if (elnew == Slip) {
-        const double th_s1 = atan2(-si[1], -si[0]);
-        double upd_s = th_s1 - th_s0;
-        if (fabs(upd_s) >= pi) upd_s = upd_s - rint(upd_s / (2.0 * pi)) * 2.0 * pi;
+        const R th_s1 = atan2(-si[1], -si[0]);
+        R upd_s = th_s1 - th_s0;
+        if (fabs(upd_s) >= pi) upd_s = upd_s - rint(upd_s / (two * pi)) * two * pi;
         fac_s = fabs(upd_s) / fabs(err_0);
     }
     return true;
 }
 
-__device__ __noinline__ void compute_diagscaling(const PView &P, const double coefs[2][2]) {
+// R = float (mixed precision): the scaling is a preconditioner of the search direction, so
+// single precision changes the iteration path only at rounding level of the direction
+template <typename R>
+__device__ __noinline__ void compute_diagscaling(const PView &P, const double coefs_d[2][2]) {
     const PatchDesc &d = *P.d;
     __syncthreads();
     PHASE_START(tdg);
@@ -792,17 +804,19 @@ __device__ __noinline__ void compute_diagscaling(const PView &P, const double co
     const int *igs = P.igs();
     const double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN), *sx = P.c(W_SX), *sy = P.c(W_SY);
     double *dscl = P.c(W_DSCL);
+    R coefs[2][2] = {{(R)coefs_d[0][0], (R)coefs_d[0][1]}, {(R)coefs_d[1][0], (R)coefs_d[1][1]}};
+    const R d_slp = (R)d.d_slp, pow_s = (R)d.pow_s;
     int ndeg = 0;
     FOR_I(ii, n) {
         const int el = igs[ii];
         if (el == Slip) {
             int elnew = Slip;
-            double fac_s = 0.0;
-            if (!slip_element(d, coefs, px[ii], py[ii], pn[ii], sx[ii], sy[ii], elnew, fac_s)) ndeg++;
-            else if (elnew == Slip) dscl[ii] = d.d_slp * pow(fac_s, d.pow_s);
-            else dscl[ii] = dscl_adhesion(d, igs, ii, mx, dscl[ii]);
+            R fac_s = R(0);
+            if (!slip_element<R>(d, coefs, (R)px[ii], (R)py[ii], (R)pn[ii], (R)sx[ii], (R)sy[ii], elnew, fac_s)) ndeg++;
+            else if (elnew == Slip) dscl[ii] = (double)(d_slp * pow(fac_s, pow_s));
+            else dscl[ii] = (double)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
         } else if (el == Adhes) {
-            dscl[ii] = dscl_adhesion(d, igs, ii, mx, dscl[ii]);
+            dscl[ii] = (double)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
         } else {
             dscl[ii] = 0.0;
         }
@@ -811,16 +825,18 @@ __device__ __noinline__ void compute_diagscaling(const PView &P, const double co
     if (ndeg > 0 && threadIdx.x == 0) {
         // serial pass with the reference's carry-over of elnew and fac_s (elements in order)
         int elnew = Exter;
-        double fac_s = 0.0;
+        R fac_s = R(0);
         for (int ii = 0; ii < n; ii++) {
             const int el = igs[ii];
             if (el == Slip) {
                 int e2 = el;
-                double f2 = fac_s;
-                if (slip_element(d, coefs, px[ii], py[ii], pn[ii], sx[ii], sy[ii], e2, f2)) { elnew = e2; fac_s = f2; }
+                R f2 = fac_s;
+                if (slip_element<R>(d, coefs, (R)px[ii], (R)py[ii], (R)pn[ii], (R)sx[ii], (R)sy[ii], e2, f2)) {
+                    elnew = e2; fac_s = f2;
+                }
             }
-            if (el == Slip && elnew == Slip) dscl[ii] = d.d_slp * pow(fac_s, d.pow_s);
-            else if (el == Adhes || elnew == Adhes) dscl[ii] = dscl_adhesion(d, igs, ii, mx, dscl[ii]);
+            if (el == Slip && elnew == Slip) dscl[ii] = (double)(d_slp * pow(fac_s, pow_s));
+            else if (el == Adhes || elnew == Adhes) dscl[ii] = (double)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
             else dscl[ii] = 0.0;
         }
     }
@@ -828,21 +844,54 @@ __device__ __noinline__ void compute_diagscaling(const PView &P, const double co
     PHASE_END(P, O_T_DIAG - O_T_TOTAL, tdg);
 }
 
+// arrays read and written by the line search, in its working precision
+template <typename R>
+struct LsArrays {
+    const R *dpx, *dpy, *dvx, *dvy, *vx, *vy, *qx, *qy, *sx, *sy, *nox, *noy, *dscl, *trc;
+    R *pdx, *pdy, *pnx, *pny;
+};
+
+__device__ inline void ls_arrays(const PView &P, LsArrays<double> &A) {
+    A.dpx = P.c(W_DPX); A.dpy = P.c(W_DPY); A.dvx = P.c(W_DVX); A.dvy = P.c(W_DVY);
+    A.vx = P.c(W_VX); A.vy = P.c(W_VY); A.qx = P.c(W_QX); A.qy = P.c(W_QY);
+    A.sx = P.c(W_SX); A.sy = P.c(W_SY); A.nox = P.c(W_NX); A.noy = P.c(W_NY);
+    A.dscl = P.c(W_DSCL); A.trc = P.c(W_TRC);
+    A.pdx = P.c(W_PDX); A.pdy = P.c(W_PDY); A.pnx = P.c(W_PNX); A.pny = P.c(W_PNY);
+}
+
+// single-precision copies of the line-search inputs, made once per line search
+__device__ inline void ls_arrays(const PView &P, LsArrays<float> &A) {
+    const int n = P.n;
+    const int src[14] = {W_DPX, W_DPY, W_DVX, W_DVY, W_VX, W_VY, W_QX, W_QY, W_SX, W_SY, W_NX, W_NY, W_DSCL, W_TRC};
+    const float *f[18];
+    for (int k = 0; k < 14; k++) {
+        float *dst = P.f(k);
+        const double *from = P.c(src[k]);
+        FOR_I(i, n) dst[i] = (float)from[i];
+        f[k] = dst;
+    }
+    A.dpx = f[0]; A.dpy = f[1]; A.dvx = f[2]; A.dvy = f[3]; A.vx = f[4]; A.vy = f[5]; A.qx = f[6]; A.qy = f[7];
+    A.sx = f[8]; A.sy = f[9]; A.nox = f[10]; A.noy = f[11]; A.dscl = f[12]; A.trc = f[13];
+    A.pdx = P.f(14); A.pdy = P.f(15); A.pnx = P.f(16); A.pny = P.f(17);
+    __syncthreads();
+}
+
 // perform_linesearch, gdsteady.f90:1046-1462.  Evaluations of rho(alpha) are block-parallel;
 // the Brent bookkeeping runs on thread 0 with the table in shared memory.
-template <int DUMMY = 0>
+// R = float (mixed precision): the trial tractions and the terms of the merit function are
+// evaluated in single precision (sums in double); the step length only has to be found to
+// the relative tolerance eps_j = 1e-3 of the bracketing search
+template <typename R>
 __device__ __noinline__ bool perform_linesearch(const PView &P, double alpha0, double &alpha_out, int &jout) {
     PHASE_START(tls);
     const int n = P.n;
     SolverSmem &S = *P.sm;
     RedSmem &red = S.red;
     const int *igs = P.igs();
-    const double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY), *dvx = P.c(W_DVX), *dvy = P.c(W_DVY);
-    const double *vx = P.c(W_VX), *vy = P.c(W_VY), *qx = P.c(W_QX), *qy = P.c(W_QY);
-    const double *sx = P.c(W_SX), *sy = P.c(W_SY), *nox = P.c(W_NX), *noy = P.c(W_NY);
-    const double *dscl = P.c(W_DSCL), *trc = P.c(W_TRC);
-    double *pdx = P.c(W_PDX), *pdy = P.c(W_PDY), *pnx = P.c(W_PNX), *pny = P.c(W_PNY);
+    LsArrays<R> A;
+    ls_arrays(P, A);
     const double tiny = 1e-12, eps_j = 0.001;
+    const R rtiny = R(1e-12);
     // thread-0 state
     int itb_a = 0, itb_b = 0, itb_x = 0, itb_w = 0, itb_v = 0, itb_u = 0;
     double dst_cur = 0, dst_prv1 = 0, dst_prv2 = 0, ddrho = 0, alpha_prv = -1.0;
@@ -852,36 +901,37 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, double alpha0, d
     __syncthreads();
     for (int guard = 0; guard < kMaxLs + 1; guard++) {
         const double alpha_j = S.alpha_j;
+        const R aj = (R)alpha_j;
         FOR_I(i, n) {
-            if (igs[i] >= Adhes) { pdx[i] = dpx[i] + alpha_j * dvx[i]; pdy[i] = dpy[i] + alpha_j * dvy[i]; }
-            else { pdx[i] = dpx[i]; pdy[i] = dpy[i]; }
+            if (igs[i] >= Adhes) { A.pdx[i] = A.dpx[i] + aj * A.dvx[i]; A.pdy[i] = A.dpy[i] + aj * A.dvy[i]; }
+            else { A.pdx[i] = A.dpx[i]; A.pdy[i] = A.dpy[i]; }
         }
-        apply_trcbnd(P, trc, pdx, pdy, pnx, pny);
+        apply_trcbnd<R>(P, A.trc, A.pdx, A.pdy, A.pnx, A.pny);
         double acc[4] = {0, 0, 0, 0};     // rho, c0, c1, c2
         FOR_I(ii, n) {
-            const double txo = -noy[ii], tyo = nox[ii];
-            const double vt = vx[ii] * txo + vy[ii] * tyo;
-            const double tb = trc[ii];
-            const double dth_da = (tb * vt) / (fmax(tiny, tb * tb) + alpha_j * alpha_j * vt * vt);
-            double nxn, nyn;
-            unit_dir(pnx[ii], pny[ii], nxn, nyn);
-            const double txn = -nyn, tyn = nxn;
-            const double s_x = sx[ii], s_y = sy[ii], q_x = qx[ii], q_y = qy[ii];
-            const double sn = s_x * nxn + s_y * nyn;
+            const R txo = -A.noy[ii], tyo = A.nox[ii];
+            const R vt = A.vx[ii] * txo + A.vy[ii] * tyo;
+            const R tb = A.trc[ii];
+            const R dth_da = (tb * vt) / (fmax(rtiny, tb * tb) + aj * aj * vt * vt);
+            R nxn, nyn;
+            unit_dir<R>(A.pnx[ii], A.pny[ii], nxn, nyn);
+            const R txn = -nyn, tyn = nxn;
+            const R s_x = A.sx[ii], s_y = A.sy[ii], q_x = A.qx[ii], q_y = A.qy[ii];
+            const R sn = s_x * nxn + s_y * nyn;
             int elnew = igs[ii];
-            if (elnew == Slip && sn > 0.0) elnew = Adhes;
-            const double st = s_x * txn + s_y * tyn, rt = -st;
-            const double qn = q_x * nxn + q_y * nyn, qt = q_x * txn + q_y * tyn;
-            const double d2 = dscl[ii] * dscl[ii];
+            if (elnew == Slip && sn > R(0)) elnew = Adhes;
+            const R st = s_x * txn + s_y * tyn, rt = -st;
+            const R qn = q_x * nxn + q_y * nyn, qt = q_x * txn + q_y * tyn;
+            const R d2 = A.dscl[ii] * A.dscl[ii];
             if (elnew == Adhes) {
-                acc[1] += 2.0 * d2 * (s_x * q_x + s_y * q_y);
-                acc[2] += 2.0 * d2 * (q_x * q_x + q_y * q_y);
-                acc[0] += d2 * ((s_x + alpha_j * q_x) * (s_x + alpha_j * q_x) + (s_y + alpha_j * q_y) * (s_y + alpha_j * q_y));
+                acc[1] += (double)(R(2) * d2 * (s_x * q_x + s_y * q_y));
+                acc[2] += (double)(R(2) * d2 * (q_x * q_x + q_y * q_y));
+                acc[0] += (double)(d2 * ((s_x + aj * q_x) * (s_x + aj * q_x) + (s_y + aj * q_y) * (s_y + aj * q_y)));
             } else if (elnew == Slip) {
-                acc[1] -= 2.0 * d2 * (rt * qt - rt * sn * dth_da);
-                acc[2] -= 2.0 * d2 * (-qt * qt + qt * sn * dth_da - rt * qn * dth_da);
-                acc[3] -= 2.0 * d2 * (qt * qn * dth_da);
-                acc[0] += d2 * (st + alpha_j * qt) * (st + alpha_j * qt);
+                acc[1] -= (double)(R(2) * d2 * (rt * qt - rt * sn * dth_da));
+                acc[2] -= (double)(R(2) * d2 * (-qt * qt + qt * sn * dth_da - rt * qn * dth_da));
+                acc[3] -= (double)(R(2) * d2 * (qt * qn * dth_da));
+                acc[0] += (double)(d2 * (st + aj * qt) * (st + aj * qt));
             }
         }
         block_sum<4>(red, acc);
@@ -1016,7 +1066,7 @@ __device__ __noinline__ void compute_slip(const PView &P, const Ops<T> &op, int 
 // A dp_b is an FP64 convolution, the change since the base an FP32 one.  The base is moved
 // to the current dp (and re-evaluated in FP64) when the change exceeds tau * |dp| (rms over
 // the grid); the FP32 part then carries at most ~tau times the FP32 rounding of the product.
-constexpr double kRefreshTau = 5e-5;
+constexpr double kRefreshTau = 1e-3;
 
 __device__ __noinline__ void compute_slip_rr(const PView &P, const Ops<double> &op, const Ops<float> &o32,
                                              bool &have_base, int &nconv64, int &nconv32) {
@@ -1130,7 +1180,11 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
     lstagn = false;
     set_nt(P);
     slip();
-    compute_diagscaling(P, coefs);
+    // mixed-precision tiers (PatchDesc::precision): 1 FP32 products only, 2 also FP32
+    // scaling and local element solves, 3 also an FP32 line search
+    const bool f32_diag = o32 && d.precision >= 2, f32_ls = o32 && d.precision >= 3;
+    if (f32_diag) compute_diagscaling<float>(P, coefs);
+    else compute_diagscaling<double>(P, coefs);
     set_residual(P);
     {
         double m = 0.0; FOR_I(i, n) m = fmax(m, fmax(fabs(rx[i]), fabs(ry[i])));
@@ -1155,7 +1209,9 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
             alpha0 = 0.5 * (alpha0 + alpha);
         }
         int its_j = 0;
-        if (!perform_linesearch(P, alpha0, alpha, its_j)) { err = dif; return -100000; }
+        const bool ls_ok = f32_ls ? perform_linesearch<float>(P, alpha0, alpha, its_j)
+                                  : perform_linesearch<double>(P, alpha0, alpha, its_j);
+        if (!ls_ok) { err = dif; return -100000; }
         nls += its_j;
         {
             double a[2] = {0, 0};
@@ -1179,12 +1235,22 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
         int chg = 0;
         FOR_I(ii, n) {
             if (igsold[ii] == Slip) {
-                double pr[3] = {px[ii], py[ii], pn[ii]};
-                double si[2] = {sx[ii], sy[ii]};
                 int elnew = igs[ii];
-                elm_solve(elnew, coefs, 1e-6, 1.0, 1.0, pr, d.fstat, si);
+                double cosdth;
+                if (f32_diag) {
+                    // mixed precision: the local element solve only feeds the release test below
+                    float prf[3] = {(float)px[ii], (float)py[ii], (float)pn[ii]};
+                    float sif[2] = {(float)sx[ii], (float)sy[ii]};
+                    const float cf[2][2] = {{(float)coefs[0][0], (float)coefs[0][1]}, {(float)coefs[1][0], (float)coefs[1][1]}};
+                    elm_solve<float>(elnew, cf, 1e-6f, 1.0f, 1.0f, prf, (float)d.fstat, sif);
+                    cosdth = (double)(((float)nx[ii] * prf[0] + (float)ny[ii] * prf[1]) / (float)trc[ii]);
+                } else {
+                    double pr[3] = {px[ii], py[ii], pn[ii]};
+                    double si[2] = {sx[ii], sy[ii]};
+                    elm_solve<double>(elnew, coefs, 1e-6, 1.0, 1.0, pr, d.fstat, si);
+                    cosdth = (nx[ii] * pr[0] + ny[ii] * pr[1]) / trc[ii];
+                }
                 double snrm = nx[ii] * sx[ii] + ny[ii] * sy[ii];
-                double cosdth = (nx[ii] * pr[0] + ny[ii] * pr[1]) / trc[ii];
                 // the A->S test below only sees elements that were in adhesion
                 if ((snrm > 0.0 && (dscl[ii] >= 0.001 || elnew == Adhes)) || cosdth <= -0.5) { igs[ii] = Adhes; chg = 1; }
             } else if (igs[ii] == Adhes) {
@@ -1194,7 +1260,8 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
         }
         chg = block_sumi1(red, chg);
         lchanged = chg > 0;
-        compute_diagscaling(P, coefs);
+        if (f32_diag) compute_diagscaling<float>(P, coefs);
+        else compute_diagscaling<double>(P, coefs);
         set_residual(P);
         double facdif;
         if (beta >= 0.1) facdif = 1.0;

@@ -22,8 +22,9 @@
 extern "C" {
 #endif
 
-/* library extension flag for cntc_setflags: 0 = FP64 throughout (default), 1 = FP32 bulk
- * convolutions followed by an FP64 refinement phase to the requested tolerance */
+/* library extension flag for cntc_setflags: 0 = FP64 throughout (default); mixed precision,
+ * the FP64 iteration path with FP64 residual replacement: 1 = FP32 convolution products,
+ * 2 = also FP32 diagonal scaling and local element solves, 3 = also an FP32 line search */
 #define CNTC_if_mixedprec 2010
 
 /* initialisation: cntc_initializeFirst 235-442, cntc_initializeFirst_new 446-472,

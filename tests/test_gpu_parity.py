@@ -33,13 +33,15 @@ def run_gpu(cntc, case, ire=1, icp=1):
 
 
 def force_err(g, o, fstat):
-    scale_floor = 1e-3 * fstat * abs(o["fn"])
-    out = {}
-    for k in ("fn", "fx", "fy", "mz"):
-        ref = o[k]
-        floor = scale_floor if k != "mz" else 0.0
-        out[k] = abs(g[k] - ref) / max(abs(ref), floor, 1e-300)
-    return out
+    """Relative errors: Fn; the tangential force vector (Fx, Fy), relative to its magnitude or,
+    when that cancels to below a thousandth of the friction bound, to 1e-3 mu Fn; Mz relative
+    to mu Fn times the half-width of the grid."""
+    fn = abs(o["fn"])
+    ft = float(np.hypot(o["fx"], o["fy"]))
+    width = 0.5 * float(np.hypot(g["dx"] * g["mx"], g["dy"] * g["my"]))
+    return {"fn": abs(g["fn"] - o["fn"]) / max(fn, 1e-300),
+            "ft": float(np.hypot(g["fx"] - o["fx"], g["fy"] - o["fy"])) / max(ft, 1e-3 * fstat * fn, 1e-300),
+            "mz": abs(g["mz"] - o["mz"]) / max(abs(o["mz"]), fstat * fn * width, 1e-300)}
 
 
 def trac_err(g, o):
