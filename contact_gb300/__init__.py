@@ -57,6 +57,7 @@ _PROTOS = {
     "cntc_settangentialforces": [_IP, _IP, _DP, _DP],
     "cntc_calculate": [_IP, _IP, _IP],
     "cntc_calculate_batch": [_IP, _IP, _IP, _IP],
+    "cntc_calculate_noalloc": [_IP, _IP, _IP],
     "cntc_getflags": [_IP, _IP, _IP, _IP, _IP],
     "cntc_getreferencevelocity": [_IP, _IP, _DP],
     "cntc_gethertzcontact": [_IP, _IP, _IP, _DP],
@@ -213,6 +214,14 @@ def calculate(ire, icp):
     _require_gpu()
     ierr = ctypes.c_int(0)
     load().cntc_calculate(_i(ire), _i(icp), ctypes.byref(ierr))
+    return ierr.value
+
+
+def calculate_noalloc(ire, icp):
+    """cntc_calculate without device allocations (fixed 16 MiB device scratch)."""
+    _require_gpu()
+    ierr = ctypes.c_int(0)
+    load().cntc_calculate_noalloc(_i(ire), _i(icp), ctypes.byref(ierr))
     return ierr.value
 
 

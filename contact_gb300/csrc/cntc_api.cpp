@@ -510,6 +510,75 @@ int resident_collect(int *ierror) {
     return 0;
 }
 
+// ------------------------------------------------------------------------------------------
+// allocation-free solve of one problem.  Some hosts cannot have the library allocate device
+// memory once their time loop runs: a multibody code that fixes its device memory budget at
+// start-up, or a real-time co-simulation step in which the implicit device synchronisation
+// and possible failure of cudaMalloc/cudaFree are not acceptable.  For them every device
+// buffer of one solve (descriptor, launch list, io block, work area) is carved from this
+// fixed file-scope array; its address is looked up once per device.  Nothing in it has to
+// start at zero: the io block is written in full from the host before each solve and the
+// solve kernel clears its work columns itself.
+// ------------------------------------------------------------------------------------------
+constexpr size_t kNoAllocBytes = (size_t)16 << 20;          // 16 MiB: grids up to ~140 x 140
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+alignas(256) double g_noalloc_host[kNoAllocBytes / sizeof(double)];   // host staging, no allocation
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+char *g_noalloc_dev[kMaxDevices] = {};
+
+int calculate_noalloc(int ire, int icp) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    Problem *p = lookup(ire, icp, true);
+    if (!p) return CNTC_err_icp;
+    std::unique_lock<std::mutex> busy(p->busy, std::try_to_lock);
+    if (!busy.owns_lock()) return CNTC_err_other;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CNTC_err_other;
+    if (!g_noalloc_dev[dev]) {
+        void *addr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+        if (e != cudaSuccess || !addr) {
+            log_msg("cntc_calculate_noalloc: device scratch not available");
+            return CNTC_err_other;
+        }
+        g_noalloc_dev[dev] = (char *)addr;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    p->ncase++;
+    Prep prep;
+    int st = prepare(*p, prep);
+    if (st != 0) { p->have = false; return st; }
+    PatchDesc hd = prep.d;
+    const PatchSizes s = patch_sizes(hd.mx, hd.my, hd.fx, hd.fy);
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t off_list = up(sizeof(PatchDesc)), off_io = off_list + 256, off_work = off_io + up(s.io);
+    if (off_work + s.work > kNoAllocBytes || s.io > sizeof(g_noalloc_host)) {
+        char msg[160];
+        std::snprintf(msg, sizeof msg, "cntc_calculate_noalloc: problem needs %zu bytes of device scratch, limit %zu",
+                      off_work + s.work, kNoAllocBytes);
+        log_msg(msg);
+        p->have = false;
+        return CNTC_err_other;
+    }
+    char *base = g_noalloc_dev[dev];
+    carve_patch(hd, base + off_io, base + off_work);
+    stage_inputs(*p, hd, g_noalloc_host);
+    cudaStream_t stream = cudaStreamPerThread;
+    cudaError_t e = cudaMemcpyAsync(base + off_io, g_noalloc_host, s.io, cudaMemcpyHostToDevice, stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(base, &hd, sizeof(PatchDesc), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return CNTC_err_other;
+    const unsigned char need_ic = 1;
+    int rc = engine_run(&hd, (PatchDesc *)base, 1, &need_ic, (int *)(base + off_list), stream);
+    if (rc == 0) e = cudaMemcpyAsync(g_noalloc_host, base + off_io, s.io, cudaMemcpyDeviceToHost, stream);
+    if (rc == 0 && e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (rc != 0 || e != cudaSuccess) { p->have = false; return CNTC_err_other; }
+    collect(*p, hd, g_noalloc_host);
+    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    p->twall += dt; p->tcpu += dt;
+    return p->ierror;
+}
+
 double *field_ptr(Problem &p, int col) {
     const int n = p.r_mx * p.r_my;
     if (!p.have || (int)p.fields.size() < kIoCols * n) return nullptr;
@@ -782,6 +851,10 @@ void cntc_calculate(int *ire, int *icp, int *ierror) {
     int ie = 0;
     calculate_many(1, ire, icp, &ie);
     *ierror = ie;
+}
+
+void cntc_calculate_noalloc(int *ire, int *icp, int *ierror) {
+    *ierror = calculate_noalloc(*ire, *icp);
 }
 
 void cntc_calculate_batch(int *n, int *ire, int *icp, int *ierror) {

@@ -71,6 +71,14 @@ void cntc_settangentialforces(int *ire, int *icp, double *fx, double *fy);
 void cntc_calculate(int *ire, int *icp, int *ierror);
 /* extension: n problems (ire[i], icp[i]) solved together; ierror[i] as cntc_calculate */
 void cntc_calculate_batch(int *n, int *ire, int *icp, int *ierror);
+/* extension, no counterpart in the reference: cntc_calculate that allocates no device memory.
+ * All device buffers of the solve come from a fixed 16 MiB device array of the library
+ * (grids up to about 140 x 140; larger problems return CNTC_err_other with a message).  The
+ * one array serves every call of the process, so overlapping calls would race on it; the
+ * library serialises them with a lock and each call waits for its own work to finish
+ * before it returns.  The first call of a process looks up the array's device address and
+ * creates the library's streams: make it before any stream capture of the caller. */
+void cntc_calculate_noalloc(int *ire, int *icp, int *ierror);
 
 /* results: cntc_getFlags 4001-4160, cntc_getReferenceVelocity 4987-5017,
  * cntc_getHertzContact 5021-5066, cntc_getNumElements 5070-5099,
