@@ -97,14 +97,19 @@ __device__ __forceinline__ void dft_small(C<T> (&v)[8], int dir) {
         t3r = (dir < 0) ? mkc<T>(t3.y, -t3.x) : mkc<T>(-t3.y, t3.x);
         v[1] = cadd<T>(t0, t2); v[5] = csub<T>(t0, t2); v[3] = cadd<T>(t1, t3r); v[7] = csub<T>(t1, t3r);
     } else {
+        // roots are compile-time constants of type T (R and q are known after unrolling);
+        // the direction only flips the sign of the imaginary part
+        const T sd = (dir < 0) ? T(-1) : T(1);
         C<T> out[8];
 #pragma unroll
         for (int k = 0; k < R; k++) {
             C<T> acc = v[0];
 #pragma unroll
             for (int r = 1; r < R; r++) {
-                int q = (r * k) % R;
-                C<T> w = mkc<T>((T)root_cos(R, q), (T)(dir * root_sin(R, q)));
+                const int q = (r * k) % R;
+                const T wc = (T)root_cos(R, q), ws = (T)root_sin(R, q);
+                // root_sin holds sin(2 pi q / R); the root is exp(dir 2 pi i q / R)
+                C<T> w = mkc<T>(wc, sd * ws);
                 acc = cadd<T>(acc, cmul<T>(v[r], w));
             }
             out[k] = acc;
@@ -127,7 +132,7 @@ __device__ __forceinline__ void stockham_stage(const C<T> *src, C<T> *dst, int n
         for (int r = 0; r < R; r++) {
             C<T> a = src[j + r * nb];
             if (r > 0 && jm > 0) {
-                C<T> w = tw[(r * jm * tstep) % n];
+                C<T> w = tw[r * jm * tstep];          // r * jm * tstep < R * Ns * n / (Ns R) = n
                 if (dir > 0) w = cconj<T>(w);
                 a = cmul<T>(a, w);
             }

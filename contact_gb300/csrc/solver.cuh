@@ -58,6 +58,17 @@ struct PView {
 // small helpers
 // ------------------------------------------------------------------------------------------
 __device__ inline double dsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
+__device__ inline double inv_sqrt(double x) { return rsqrt(x); }
+__device__ inline float inv_sqrt(float x) { return rsqrtf(x); }
+
+// unit direction of the tangential traction p/|p| (one reciprocal square root), standing for
+// (cos, sin) of atan2(py, px); the reference's direction for p = 0
+template <typename R>
+__device__ inline void unit_dir(R px, R py, R &nx, R &ny) {
+    const R r2 = px * px + py * py;
+    if (r2 > R(0)) { const R ri = inv_sqrt(r2); nx = px * ri; ny = py * ri; }
+    else { nx = (px < R(0) || (px == R(0) && signbit(px))) ? R(-1) : R(1); ny = R(0); if (signbit(py) && px == R(0)) nx = R(1); }
+}
 
 __device__ __noinline__ void count_eldiv(const PView &P, int &nadh, int &nslip, int &nplast, int &nexter) {
     const int *igs = P.igs();
@@ -450,17 +461,26 @@ __device__ __noinline__ void elm_solve(int &el, const R coef[2][2], R eps, R ome
                 fk[0] = pr[1] * si[0] - pr[0] * si[1];
                 fk[1] = pr[0] * pr[0] + pr[1] * pr[1] - trc_bound * trc_bound;
             }
-            R alph0 = atan2(pold2, pold1);
-            R alph1 = atan2(pr[1], pr[0]);
-            R dalph = alph1 - alph0;
-            const R pi = R(3.14159265358979323846);
-            if (dalph < -pi) dalph += two * pi;
-            if (dalph > pi) dalph -= two * pi;
-            alph1 = alph0 + omegas * dalph;
-            R sn, cs;
-            sincos(alph1, &sn, &cs);
-            pr[0] = trc_bound * cs;
-            pr[1] = trc_bound * sn;
+            if (omegas == R(1)) {
+                // no under-relaxation of the angle: the rotation below reduces to scaling the
+                // Newton result onto the traction bound
+                R ux, uy;
+                unit_dir<R>(pr[0], pr[1], ux, uy);
+                pr[0] = trc_bound * ux;
+                pr[1] = trc_bound * uy;
+            } else {
+                R alph0 = atan2(pold2, pold1);
+                R alph1 = atan2(pr[1], pr[0]);
+                R dalph = alph1 - alph0;
+                const R pi = R(3.14159265358979323846);
+                if (dalph < -pi) dalph += two * pi;
+                if (dalph > pi) dalph -= two * pi;
+                alph1 = alph0 + omegas * dalph;
+                R sn, cs;
+                sincos(alph1, &sn, &cs);
+                pr[0] = trc_bound * cs;
+                pr[1] = trc_bound * sn;
+            }
             if (fabs(pr[0]) > fabs(pr[1])) { if (pr[0] * si[0] > zero) violat = 1; }
             else { if (pr[1] * si[1] > zero) violat = 1; }
         } else {
@@ -653,8 +673,8 @@ __device__ __noinline__ void apply_trcbnd(const PView &P, const R *trc, R *dpx, 
             if (igs[ii] <= Exter) { qx = zero; qy = zero; }
             else {
                 qx = pxn + dpx[ii]; qy = pyn + dpy[ii];
-                R ptabs = sqrt(qx * qx + qy * qy);
-                if (igs[ii] == Slip || ptabs >= trc[ii]) { qx = qx * trc[ii] / ptabs; qy = qy * trc[ii] / ptabs; }
+                const R qq = qx * qx + qy * qy, tb = trc[ii];
+                if (igs[ii] == Slip || qq >= tb * tb) { const R f = tb * inv_sqrt(qq); qx *= f; qy *= f; }
             }
             px[ii] = qx; py[ii] = qy;
             dpx[ii] = qx - pxn; dpy[ii] = qy - pyn;
@@ -732,14 +752,6 @@ __device__ __noinline__ void project_searchdir(const PView &P, int imeth, int kd
     __syncthreads();
 }
 
-// unit direction of the tangential traction: (cos, sin) of atan2(py, px), with (1, 0) for p = 0
-template <typename R>
-__device__ inline void unit_dir(R px, R py, R &nx, R &ny) {
-    R r = sqrt(px * px + py * py);
-    if (r > R(0)) { nx = px / r; ny = py / r; }
-    else { nx = (px < R(0) || (px == R(0) && signbit(px))) ? R(-1) : R(1); ny = R(0); if (signbit(py) && px == R(0)) nx = R(1); }
-}
-
 // compute_diagscaling, gdsteady.f90:901-1042.  In the reference 'elnew' and 'fac_s' carry over
 // from one element to the next.  The carried values reach (a) exterior elements, whose
 // scaling is never used (their residual and line-search terms are zero), and (b) slip
@@ -764,30 +776,27 @@ __device__ inline bool slip_element(const PatchDesc &d, const R coefs[2][2], R p
                                     R &fac_s) {
     const R tiny_err = R(1e-6), pi = R(3.14159265358979323846), two = R(2);
     const R fstat = (R)d.fstat;
+    // angle from a to b in (-pi, pi]: one atan2 of cross and dot product (the reference takes
+    // the difference of two atan2 values and wraps it)
+    auto angle = [](R ax, R ay, R bx, R by) { return atan2(ax * by - ay * bx, ax * bx + ay * by); };
+    (void)pi; (void)two;
     R pr[3] = {px, py, pn};
     R si[2] = {sx, sy};
-    R th_p0 = atan2(pr[1], pr[0]);
-    R th_s0 = atan2(-si[1], -si[0]);
-    R err_0 = th_s0 - th_p0;
-    if (fabs(err_0) >= pi) err_0 = err_0 - rint(err_0 / (two * pi)) * two * pi;
+    R err_0 = angle(pr[0], pr[1], -si[0], -si[1]);
     if (fabs(err_0) <= tiny_err) {
-        R c, s; sincos(th_p0 + R(0.1), &s, &c);
+        R c, s; sincos(atan2(pr[1], pr[0]) + R(0.1), &s, &c);
         pr[0] = fstat * pr[2] * c;
         pr[1] = fstat * pr[2] * s;
         si[0] = sx + coefs[0][0] * (pr[0] - px) + coefs[0][1] * (pr[1] - py);
         si[1] = sy + coefs[1][0] * (pr[0] - px) + coefs[1][1] * (pr[1] - py);
-        th_p0 = atan2(pr[1], pr[0]);
-        th_s0 = atan2(-si[1], -si[0]);
-        err_0 = th_s0 - th_p0;
-        if (fabs(err_0) >= pi) err_0 = err_0 - rint(err_0 / (two * pi)) * two * pi;
+        err_0 = angle(pr[0], pr[1], -si[0], -si[1]);
     }
     if (fabs(err_0) <= tiny_err) return false;
+    const R s0x = -si[0], s0y = -si[1];
     elnew = Slip;
     elm_solve<R>(elnew, coefs, R(1e-6), R(1), R(1), pr, fstat, si);
     if (elnew == Slip) {
-        const R th_s1 = atan2(-si[1], -si[0]);
-        R upd_s = th_s1 - th_s0;
-        if (fabs(upd_s) >= pi) upd_s = upd_s - rint(upd_s / (two * pi)) * two * pi;
+        const R upd_s = angle(s0x, s0y, -si[0], -si[1]);
         fac_s = fabs(upd_s) / fabs(err_0);
     }
     return true;
@@ -899,16 +908,50 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, double alpha0, d
     int j = 0;
     if (threadIdx.x == 0) { S.alpha_j = 0.0; S.stop_j = 0; S.nobracket = 0; }
     __syncthreads();
+    // adhesion elements keep their status during the search and their terms do not depend on
+    // the trial tractions: their part of rho is the quadratic qa0 + 2 alpha qa1 + alpha^2 qa2
+    double qa[3] = {0.0, 0.0, 0.0};
+    {
+        const double *sx = P.c(W_SX), *sy = P.c(W_SY), *qx = P.c(W_QX), *qy = P.c(W_QY), *dscl = P.c(W_DSCL);
+        FOR_I(ii, n) if (igs[ii] == Adhes) {
+            const double d2 = dscl[ii] * dscl[ii];
+            qa[0] += d2 * (sx[ii] * sx[ii] + sy[ii] * sy[ii]);
+            qa[1] += d2 * (sx[ii] * qx[ii] + sy[ii] * qy[ii]);
+            qa[2] += d2 * (qx[ii] * qx[ii] + qy[ii] * qy[ii]);
+        }
+        block_sum<3>(red, qa);
+    }
+    const int mx = P.mx, my = P.my;
     for (int guard = 0; guard < kMaxLs + 1; guard++) {
         const double alpha_j = S.alpha_j;
         const R aj = (R)alpha_j;
-        FOR_I(i, n) {
-            if (igs[i] >= Adhes) { A.pdx[i] = A.dpx[i] + aj * A.dvx[i]; A.pdy[i] = A.dpy[i] + aj * A.dvy[i]; }
-            else { A.pdx[i] = A.dpx[i]; A.pdy[i] = A.dpy[i]; }
+        // trial tractions: the traction-bound scan of dp + alpha dv along each row (apply_trcbnd)
+        {
+            PHASE_START(tsc);
+            for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+                int ii = (mx - 1) + iy * mx;
+                A.pnx[ii] = R(0); A.pny[ii] = R(0);
+                R pxn = R(0), pyn = R(0);
+                for (int ix = mx - 2; ix >= 0; ix--) {
+                    ii = ix + iy * mx;
+                    const int el = igs[ii];
+                    R qx = R(0), qy = R(0);
+                    if (el > Exter) {
+                        qx = pxn + (A.dpx[ii] + aj * A.dvx[ii]);
+                        qy = pyn + (A.dpy[ii] + aj * A.dvy[ii]);
+                        const R qq = qx * qx + qy * qy, tb = A.trc[ii];
+                        if (el == Slip || qq >= tb * tb) { const R f = tb * inv_sqrt(qq); qx *= f; qy *= f; }
+                    }
+                    A.pnx[ii] = qx; A.pny[ii] = qy;
+                    pxn = qx; pyn = qy;
+                }
+            }
+            __syncthreads();
+            PHASE_END(P, O_T_SCAN - O_T_TOTAL, tsc);
         }
-        apply_trcbnd<R>(P, A.trc, A.pdx, A.pdy, A.pnx, A.pny);
-        double acc[4] = {0, 0, 0, 0};     // rho, c0, c1, c2
+        double acc[4] = {0, 0, 0, 0};     // rho, c0, c1, c2 of the slip elements
         FOR_I(ii, n) {
+            if (igs[ii] != Slip) continue;
             const R txo = -A.noy[ii], tyo = A.nox[ii];
             const R vt = A.vx[ii] * txo + A.vy[ii] * tyo;
             const R tb = A.trc[ii];
@@ -918,16 +961,15 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, double alpha0, d
             const R txn = -nyn, tyn = nxn;
             const R s_x = A.sx[ii], s_y = A.sy[ii], q_x = A.qx[ii], q_y = A.qy[ii];
             const R sn = s_x * nxn + s_y * nyn;
-            int elnew = igs[ii];
-            if (elnew == Slip && sn > R(0)) elnew = Adhes;
-            const R st = s_x * txn + s_y * tyn, rt = -st;
-            const R qn = q_x * nxn + q_y * nyn, qt = q_x * txn + q_y * tyn;
             const R d2 = A.dscl[ii] * A.dscl[ii];
-            if (elnew == Adhes) {
+            if (sn > R(0)) {
+                // slipping along the traction: counted as adhesion for this trial
                 acc[1] += (double)(R(2) * d2 * (s_x * q_x + s_y * q_y));
                 acc[2] += (double)(R(2) * d2 * (q_x * q_x + q_y * q_y));
                 acc[0] += (double)(d2 * ((s_x + aj * q_x) * (s_x + aj * q_x) + (s_y + aj * q_y) * (s_y + aj * q_y)));
-            } else if (elnew == Slip) {
+            } else {
+                const R st = s_x * txn + s_y * tyn, rt = -st;
+                const R qn = q_x * nxn + q_y * nyn, qt = q_x * txn + q_y * tyn;
                 acc[1] -= (double)(R(2) * d2 * (rt * qt - rt * sn * dth_da));
                 acc[2] -= (double)(R(2) * d2 * (-qt * qt + qt * sn * dth_da - rt * qn * dth_da));
                 acc[3] -= (double)(R(2) * d2 * (qt * qn * dth_da));
@@ -935,6 +977,9 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, double alpha0, d
             }
         }
         block_sum<4>(red, acc);
+        acc[0] += qa[0] + alpha_j * (2.0 * qa[1] + alpha_j * qa[2]);
+        acc[1] += 2.0 * qa[1];
+        acc[2] += 2.0 * qa[2];
         if (threadIdx.x == 0) {
             double *ta = S.tbl_alpha, *tr = S.tbl_rho, *td = S.tbl_drhoda;
             const double rhonew = acc[0];
@@ -1066,7 +1111,7 @@ __device__ __noinline__ void compute_slip(const PView &P, const Ops<T> &op, int 
 // A dp_b is an FP64 convolution, the change since the base an FP32 one.  The base is moved
 // to the current dp (and re-evaluated in FP64) when the change exceeds tau * |dp| (rms over
 // the grid); the FP32 part then carries at most ~tau times the FP32 rounding of the product.
-constexpr double kRefreshTau = 1e-3;
+constexpr double kRefreshTau = 5e-3;
 
 __device__ __noinline__ void compute_slip_rr(const PView &P, const Ops<double> &op, const Ops<float> &o32,
                                              bool &have_base, int &nconv64, int &nconv32) {
