@@ -55,7 +55,7 @@ def parse():
     return ap.parse_args()
 
 
-MIXED_TIER = 2     # FP32 convolution products, scaling and local solves; FP64 iteration path
+MIXED_TIER = 1     # FP32 convolution products along the FP64 iteration path
 
 
 def workload(n, seed, mixed=MIXED_TIER, max_side=0):

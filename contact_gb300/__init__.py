@@ -58,6 +58,10 @@ _PROTOS = {
     "cntc_calculate": [_IP, _IP, _IP],
     "cntc_calculate_batch": [_IP, _IP, _IP, _IP],
     "cntc_calculate_noalloc": [_IP, _IP, _IP],
+    "cntc_calculate_async": [_IP, _IP, _IP],
+    "cntc_wait": [_IP, _IP, _IP],
+    "cntc_gb300_wait_latency": [_IP, _IP, _IP, _DP],
+    "cntc_gb300_setadmissionbudget": [_DP],
     "cntc_getflags": [_IP, _IP, _IP, _IP, _IP],
     "cntc_getreferencevelocity": [_IP, _IP, _DP],
     "cntc_gethertzcontact": [_IP, _IP, _IP, _DP],
@@ -223,6 +227,29 @@ def calculate_noalloc(ire, icp):
     ierr = ctypes.c_int(0)
     load().cntc_calculate_noalloc(_i(ire), _i(icp), ctypes.byref(ierr))
     return ierr.value
+
+
+def calculate_async(ire, icp):
+    """Queue a solve (serving); returns 0 when queued."""
+    _require_gpu()
+    ierr = ctypes.c_int(0)
+    load().cntc_calculate_async(_i(ire), _i(icp), ctypes.byref(ierr))
+    return ierr.value
+
+
+def wait(ire, icp, with_latency=False):
+    """Wait for a queued solve; returns ierror (and the queue-to-completion latency in s)."""
+    ierr = ctypes.c_int(0)
+    if with_latency:
+        lat = ctypes.c_double(0.0)
+        load().cntc_gb300_wait_latency(_i(ire), _i(icp), ctypes.byref(ierr), ctypes.byref(lat))
+        return ierr.value, lat.value
+    load().cntc_wait(_i(ire), _i(icp), ctypes.byref(ierr))
+    return ierr.value
+
+
+def setadmissionbudget(gbytes):
+    load().cntc_gb300_setadmissionbudget(ctypes.byref(ctypes.c_double(float(gbytes))))
 
 
 def calculate_batch(ire_list, icp_list):

@@ -11,8 +11,12 @@
 // same for many problems with one pass of the engine.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -579,6 +583,130 @@ int calculate_noalloc(int ire, int icp) {
     return p->ierror;
 }
 
+// ------------------------------------------------------------------------------------------
+// serving: cntc_calculate_async / cntc_wait.  Requests go to a queue served by a few worker
+// lanes.  A free lane takes every queued request that fits the device-memory admission
+// budget and solves them in one engine pass on its own stream; requests that arrive while
+// passes are running wait only for the next free lane (continuous batching), and up to
+// kLanes passes run on the device at the same time.  Each patch is solved by its own thread
+// block, so a result does not depend on which other requests shared its pass.
+// ------------------------------------------------------------------------------------------
+struct AsyncReq {
+    int ire, icp;
+    size_t bytes;
+    bool done = false;
+    int ierror = 0;
+    std::chrono::steady_clock::time_point t_submit, t_done;
+};
+
+struct Server {
+    static constexpr int kLanes = 4;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<std::shared_ptr<AsyncReq>> queue;
+    std::map<long long, std::shared_ptr<AsyncReq>> pending;    // by (ire, icp)
+    size_t budget = (size_t)40 << 30;                          // admission budget, bytes
+    size_t in_flight = 0;
+    std::vector<std::thread> lanes;
+    bool stop = false;
+    int device = 0;
+
+    void lane_main() {
+        cudaSetDevice(device);
+        for (;;) {
+            std::vector<std::shared_ptr<AsyncReq>> batch;
+            size_t bytes = 0;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                cv_work.wait(lk, [&] { return stop || (!queue.empty() && in_flight + queue.front()->bytes <= budget) ||
+                                             (!queue.empty() && in_flight == 0); });
+                if (stop && queue.empty()) return;
+                while (!queue.empty()) {
+                    const size_t b = queue.front()->bytes;
+                    // a single request larger than the budget runs alone
+                    if (in_flight + bytes + b > budget && !(batch.empty() && in_flight == 0)) break;
+                    bytes += b;
+                    batch.push_back(queue.front());
+                    queue.pop_front();
+                }
+                in_flight += bytes;
+            }
+            std::vector<int> ire(batch.size()), icp(batch.size()), err(batch.size(), 0);
+            for (size_t k = 0; k < batch.size(); k++) { ire[k] = batch[k]->ire; icp[k] = batch[k]->icp; }
+            calculate_many((int)batch.size(), ire.data(), icp.data(), err.data());
+            const auto now = std::chrono::steady_clock::now();
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                in_flight -= bytes;
+                for (size_t k = 0; k < batch.size(); k++) {
+                    batch[k]->ierror = err[k];
+                    batch[k]->done = true;
+                    batch[k]->t_done = now;
+                }
+            }
+            cv_done.notify_all();
+            cv_work.notify_all();
+        }
+    }
+
+    void ensure_started() {
+        if (!lanes.empty()) return;
+        cudaGetDevice(&device);
+        for (int k = 0; k < kLanes; k++) lanes.emplace_back([this] { lane_main(); });
+    }
+
+    ~Server() {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv_work.notify_all();
+        for (auto &t : lanes) if (t.joinable()) t.join();
+    }
+};
+
+Server &server() {
+    static Server s;
+    return s;
+}
+
+long long pkey2(int ire, int icp) { return (long long)ire * 1000003LL + icp; }
+
+int calculate_async(int ire, int icp) {
+    Problem *p = lookup(ire, icp, true);
+    if (!p) return CNTC_err_icp;
+    Server &S = server();
+    auto r = std::make_shared<AsyncReq>();
+    r->ire = ire; r->icp = icp;
+    const int fx = opt_fft_size(std::max(1, p->mx)), fy = opt_fft_size(std::max(1, p->my));
+    const PatchSizes ps = patch_sizes(std::max(1, p->mx), std::max(1, p->my), fx, fy);
+    r->bytes = ps.io + ps.work + sizeof(PatchDesc);
+    r->t_submit = std::chrono::steady_clock::now();
+    {
+        std::lock_guard<std::mutex> lk(S.mu);
+        const long long key = pkey2(ire, icp);
+        auto it = S.pending.find(key);
+        if (it != S.pending.end() && !it->second->done) return CNTC_err_other;   // already queued
+        S.ensure_started();
+        S.pending[key] = r;
+        S.queue.push_back(r);
+    }
+    S.cv_work.notify_one();
+    return 0;
+}
+
+int wait_async(int ire, int icp, double *latency_s) {
+    Server &S = server();
+    std::unique_lock<std::mutex> lk(S.mu);
+    auto it = S.pending.find(pkey2(ire, icp));
+    if (it == S.pending.end()) return CNTC_err_icp;
+    std::shared_ptr<AsyncReq> r = it->second;
+    S.cv_done.wait(lk, [&] { return r->done; });
+    S.pending.erase(it);
+    if (latency_s) *latency_s = std::chrono::duration<double>(r->t_done - r->t_submit).count();
+    return r->ierror;
+}
+
 double *field_ptr(Problem &p, int col) {
     const int n = p.r_mx * p.r_my;
     if (!p.have || (int)p.fields.size() < kIoCols * n) return nullptr;
@@ -641,7 +769,7 @@ void cntc_setflags(int *ire, int *icp, int *lenflg, int *params, int *values) {
             case CNTC_ic_flow: p->flow = std::max(0, std::min(9, v)); break;
             case CNTC_ic_return: p->ret = std::max(0, std::min(3, v)); break;
             case CNTC_if_ncase: p->ncase = std::max(0, v - 1); break;
-            case CNTC_if_mixedprec: p->mixed = (v >= 0 && v <= 3) ? v : 1; break;
+            case CNTC_if_mixedprec: p->mixed = (v >= 0 && v <= 4) ? v : 1; break;
             default: break;   // output, debugging and module-1 flags have no effect here
         }
     }
@@ -851,6 +979,24 @@ void cntc_calculate(int *ire, int *icp, int *ierror) {
     int ie = 0;
     calculate_many(1, ire, icp, &ie);
     *ierror = ie;
+}
+
+void cntc_calculate_async(int *ire, int *icp, int *ierror) {
+    *ierror = calculate_async(*ire, *icp);
+}
+
+void cntc_wait(int *ire, int *icp, int *ierror) {
+    *ierror = wait_async(*ire, *icp, nullptr);
+}
+
+void cntc_gb300_wait_latency(int *ire, int *icp, int *ierror, double *latency) {
+    *ierror = wait_async(*ire, *icp, latency);
+}
+
+void cntc_gb300_setadmissionbudget(double *gbytes) {
+    Server &S = server();
+    std::lock_guard<std::mutex> lk(S.mu);
+    S.budget = (size_t)(std::max(0.0, *gbytes) * 1e9);
 }
 
 void cntc_calculate_noalloc(int *ire, int *icp, int *ierror) {

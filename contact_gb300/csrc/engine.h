@@ -18,7 +18,8 @@ enum WsCol {
     W_POX, W_POY, W_PDX, W_PDY, W_PNX, W_PNY, W_TRC, W_ZX, W_ZY, W_ONE,
     W_DBX, W_DBY, W_SBX, W_SBY, W_TX, W_TY,                  // mixed precision: base dp, A dp_base, change
     W_FLS,                                                   // 9 columns: 18 float columns of the line search
-    W_NCOL = W_FLS + 9
+    W_FST = W_FLS + 9,                                       // 14 columns: 28 float columns of the FP32 GD state
+    W_NCOL = W_FST + 14
 };
 enum WsIntCol { I_IGS = 0, I_OLD, I_EXT, I_IEL, I_NCOL };
 

@@ -227,15 +227,15 @@ struct Conv {
 
 // step A: forward row transforms of ncomp real inputs (element-major, mx*my doubles each)
 // into R0 (and R1).  'sel' optionally zeroes inputs outside a mask (mask[i] >= sel_lo).
-template <typename T>
-__device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const double *in0, const double *in1, int ncomp) {
+template <typename T, typename IO>
+__device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, const IO *in1, int ncomp) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int NX = cv.NX, mx = cv.mx, my = cv.my, nkx = cv.nkx;
     C<T> *a = cv.wbuf + w * cv.wstride;
     C<T> *b = a + NX;
     const int npair = (my + 1) / 2;
     for (int comp = 0; comp < ncomp; comp++) {
-        const double *in = comp == 0 ? in0 : in1;
+        const IO *in = comp == 0 ? in0 : in1;
         C<T> *R = comp == 0 ? cv.R0 : cv.R1;
         for (int pr = w; pr < npair; pr += kWarps) {
             const int iy0 = 2 * pr, iy1 = 2 * pr + 1;
@@ -316,8 +316,8 @@ constexpr int OUT_INT = 1;      // u[i] = val where igs >= Adhes (AllInt), other
 constexpr int OUT_ADDINT = 2;   // u[i] += val where igs >= Adhes
 
 // step C: inverse row transforms, writes u (element-major doubles)
-template <typename T>
-__device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, double *out0, double *out1, int ncomp, int mode,
+template <typename T, typename IO>
+__device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1, int ncomp, int mode,
                               const int *igs) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int NX = cv.NX, mx = cv.mx, my = cv.my, nkx = cv.nkx;
@@ -326,7 +326,7 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, double *out0, doub
     const int npair = (my + 1) / 2;
     const T sc = (T)cv.scale;
     for (int comp = 0; comp < ncomp; comp++) {
-        double *out = comp == 0 ? out0 : out1;
+        IO *out = comp == 0 ? out0 : out1;
         const C<T> *R = comp == 0 ? cv.R0 : cv.R1;
         for (int pr = w; pr < npair; pr += kWarps) {
             const int iy0 = 2 * pr, iy1 = 2 * pr + 1;
@@ -346,12 +346,12 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, double *out0, doub
             C<T> *z = warp_fft<T>(a, b, cv.px, cv.twx, +1);
             for (int ix = lane; ix < mx; ix += 32) {
                 const int i0 = iy0 * mx + ix;
-                double v0 = (double)(z[ix].x * sc);
+                const IO v0 = (IO)(z[ix].x * sc);
                 if (mode == OUT_ALL) out[i0] = v0;
                 else if (igs[i0] >= Adhes) out[i0] = (mode == OUT_INT) ? v0 : out[i0] + v0;
                 if (has1) {
                     const int i1 = iy1 * mx + ix;
-                    double v1 = (double)(z[ix].y * sc);
+                    const IO v1 = (IO)(z[ix].y * sc);
                     if (mode == OUT_ALL) out[i1] = v1;
                     else if (igs[i1] >= Adhes) out[i1] = (mode == OUT_INT) ? v1 : out[i1] + v1;
                 }
@@ -361,25 +361,26 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, double *out0, doub
 }
 
 // full product u = A p.  Synchronises the block before and after.
-template <typename T>
-__device__ void convolve(const Conv<T> &cv, const double *in0, const double *in1, double *out0, double *out1,
+template <typename T, typename IO = double>
+__device__ void convolve(const Conv<T> &cv, const IO *in0, const IO *in1, IO *out0, IO *out1,
                          int ncomp, const T *K0, const T *K1, const T *K2, int mode, const int *igs) {
     __syncthreads();
     long long t0 = clock64();
-    conv_rows_fwd<T>(cv, in0, in1, ncomp);
+    conv_rows_fwd<T, IO>(cv, in0, in1, ncomp);
     __syncthreads();
     conv_cols<T>(cv, ncomp, K0, K1, K2);
     __syncthreads();
-    conv_rows_inv<T>(cv, out0, out1, ncomp, mode, igs);
+    conv_rows_inv<T, IO>(cv, out0, out1, ncomp, mode, igs);
     __syncthreads();
     if (threadIdx.x == 0) {
         const long long dt = clock64() - t0;
         if (cv.tacc) *cv.tacc += dt;
         if (cv.tacc2) *cv.tacc2 += dt;
-        // algorithmic bytes: FP64 inputs and outputs, one real quadrant spectrum per block
+        // algorithmic bytes: inputs and outputs in their storage type, one real quadrant
+        // spectrum per block in the working precision
         if (cv.bacc) {
             const int nblk = (K0 != nullptr) + (K1 != nullptr) + (K2 != nullptr);
-            *cv.bacc += 16.0 * ncomp * cv.mx * cv.my + (double)sizeof(T) * nblk * (cv.fx + 1) * (cv.fy + 1);
+            *cv.bacc += 2.0 * sizeof(IO) * ncomp * cv.mx * cv.my + (double)sizeof(T) * nblk * (cv.fx + 1) * (cv.fy + 1);
         }
     }
 }

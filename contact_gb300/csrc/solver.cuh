@@ -147,13 +147,12 @@ struct Ops {
 // normal product out = A_zz in (kind 3) or M in (kind 4)
 template <typename T>
 __device__ inline void prod_n(const Ops<T> &op, const double *in, double *out, int mode, const int *igs, int kind) {
-    convolve<T>(op.cv, in, nullptr, out, nullptr, 1, op.K[kind], nullptr, nullptr, mode, igs);
+    convolve<T, double>(op.cv, in, nullptr, out, nullptr, 1, op.K[kind], nullptr, nullptr, mode, igs);
 }
 // tangential product (outx, outy) = A_tt (inx, iny)
-template <typename T>
-__device__ inline void prod_t(const Ops<T> &op, const double *inx, const double *iny, double *ox, double *oy,
-                              int mode, const int *igs) {
-    convolve<T>(op.cv, inx, iny, ox, oy, 2, op.K[0], op.K[1], op.K[2], mode, igs);
+template <typename T, typename IO = double>
+__device__ inline void prod_t(const Ops<T> &op, const IO *inx, const IO *iny, IO *ox, IO *oy, int mode, const int *igs) {
+    convolve<T, IO>(op.cv, inx, iny, ox, oy, 2, op.K[0], op.K[1], op.K[2], mode, igs);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -860,14 +859,6 @@ struct LsArrays {
     R *pdx, *pdy, *pnx, *pny;
 };
 
-__device__ inline void ls_arrays(const PView &P, LsArrays<double> &A) {
-    A.dpx = P.c(W_DPX); A.dpy = P.c(W_DPY); A.dvx = P.c(W_DVX); A.dvy = P.c(W_DVY);
-    A.vx = P.c(W_VX); A.vy = P.c(W_VY); A.qx = P.c(W_QX); A.qy = P.c(W_QY);
-    A.sx = P.c(W_SX); A.sy = P.c(W_SY); A.nox = P.c(W_NX); A.noy = P.c(W_NY);
-    A.dscl = P.c(W_DSCL); A.trc = P.c(W_TRC);
-    A.pdx = P.c(W_PDX); A.pdy = P.c(W_PDY); A.pnx = P.c(W_PNX); A.pny = P.c(W_PNY);
-}
-
 // single-precision copies of the line-search inputs, made once per line search
 __device__ inline void ls_arrays(const PView &P, LsArrays<float> &A) {
     const int n = P.n;
@@ -891,14 +882,13 @@ __device__ inline void ls_arrays(const PView &P, LsArrays<float> &A) {
 // evaluated in single precision (sums in double); the step length only has to be found to
 // the relative tolerance eps_j = 1e-3 of the bracketing search
 template <typename R>
-__device__ __noinline__ bool perform_linesearch(const PView &P, double alpha0, double &alpha_out, int &jout) {
+__device__ __noinline__ bool perform_linesearch(const PView &P, const LsArrays<R> &A, double alpha0, double &alpha_out,
+                                                int &jout) {
     PHASE_START(tls);
     const int n = P.n;
     SolverSmem &S = *P.sm;
     RedSmem &red = S.red;
     const int *igs = P.igs();
-    LsArrays<R> A;
-    ls_arrays(P, A);
     const double tiny = 1e-12, eps_j = 0.001;
     const R rtiny = R(1e-12);
     // thread-0 state
@@ -912,12 +902,11 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, double alpha0, d
     // the trial tractions: their part of rho is the quadratic qa0 + 2 alpha qa1 + alpha^2 qa2
     double qa[3] = {0.0, 0.0, 0.0};
     {
-        const double *sx = P.c(W_SX), *sy = P.c(W_SY), *qx = P.c(W_QX), *qy = P.c(W_QY), *dscl = P.c(W_DSCL);
         FOR_I(ii, n) if (igs[ii] == Adhes) {
-            const double d2 = dscl[ii] * dscl[ii];
-            qa[0] += d2 * (sx[ii] * sx[ii] + sy[ii] * sy[ii]);
-            qa[1] += d2 * (sx[ii] * qx[ii] + sy[ii] * qy[ii]);
-            qa[2] += d2 * (qx[ii] * qx[ii] + qy[ii] * qy[ii]);
+            const R d2 = A.dscl[ii] * A.dscl[ii];
+            qa[0] += (double)(d2 * (A.sx[ii] * A.sx[ii] + A.sy[ii] * A.sy[ii]));
+            qa[1] += (double)(d2 * (A.sx[ii] * A.qx[ii] + A.sy[ii] * A.qy[ii]));
+            qa[2] += (double)(d2 * (A.qx[ii] * A.qx[ii] + A.qy[ii] * A.qy[ii]));
         }
         block_sum<3>(red, qa);
     }
@@ -1175,170 +1164,479 @@ __device__ __noinline__ void set_residual(const PView &P) {
     __syncthreads();
 }
 
-// gdsteady, gdsteady.f90:9-606 (elastic).  Returns itgd (negated on stagnation);
-// lstagn as in the reference; returns -100000 when the line search has no bracket.
-template <typename T>
-__device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd, double eps, double &err, bool &lstagn,
-                        int &nconv, int &nls, const Ops<float> *o32, int &nconv32) {
-    // o32 != nullptr (mixed precision, T = double): the search-direction product q = A v is an
-    // FP32 convolution and the slip s = ws + A dp is kept exact to FP64 level by an FP64 base
-    // product plus an FP32 product of the change since the base (compute_slip_rr).  The
-    // iteration itself, with all its decisions, stays the FP64 iteration from the same start.
-    bool have_base = false;
-    auto slip = [&]() {
-        if constexpr (sizeof(T) == 8) {
-            if (o32) { compute_slip_rr(P, op, *o32, have_base, nconv, nconv32); return; }
-        }
-        compute_slip<T>(P, op, nconv);
-    };
-    const PatchDesc &d = *P.d;
-    const int n = P.n, mx = P.mx, my = P.my;
-    RedSmem &red = P.sm->red;
-    int *igs = P.igs(), *igsold = P.ci(I_OLD);
-    double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN);
-    double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY), *trc = P.c(W_TRC), *dscl = P.c(W_DSCL);
-    double *rx = P.c(W_RX), *ry = P.c(W_RY), *dvx = P.c(W_DVX), *dvy = P.c(W_DVY);
-    double *qx = P.c(W_QX), *qy = P.c(W_QY), *pox = P.c(W_POX), *poy = P.c(W_POY);
-    double *sx = P.c(W_SX), *sy = P.c(W_SY), *nx = P.c(W_NX), *ny = P.c(W_NY);
-    const double tiny = 1e-12;
-    const size_t bsz = (size_t)4 * mx * my;
-    const size_t o0 = (size_t)mx + (size_t)my * 2 * mx;
-    double coefs[2][2];
-    coefs[0][0] = d.cf[0 * bsz + o0] / d.ga;
-    coefs[0][1] = d.cf[1 * bsz + o0] / d.ga;
-    coefs[1][0] = coefs[0][1];
-    coefs[1][1] = d.cf[2 * bsz + o0] / d.ga;
-    int nadh, nslip, nplast, nexter;
-    count_eldiv(P, nadh, nslip, nplast, nexter);
-    const double facnel = sqrt((double)(float)n / (double)(float)(nadh + nslip + nplast));
-    FOR_I(i, n) { trc[i] = d.fstat * pn[i]; dscl[i] = 1.0; }
-    // compute_dp
-    FOR_I(ii, n) {
-        int ix = ii % mx;
-        if (ix == mx - 1) { dpx[ii] = px[ii]; dpy[ii] = py[ii]; }
-        else { dpx[ii] = px[ii] - px[ii + 1]; dpy[ii] = py[ii] - py[ii + 1]; }
+// ------------------------------------------------------------------------------------------
+// GDsteady state in a storage precision S: the FP64 work columns, or FP32 columns for the
+// single-precision part of mixed tier 4
+// ------------------------------------------------------------------------------------------
+template <typename S>
+struct GdCols {
+    S *px, *py, *pn, *dpx, *dpy, *trc, *dscl, *rx, *ry, *dvx, *dvy, *vx, *vy, *qx, *qy;
+    S *pox, *poy, *sx, *sy, *nx, *ny, *zx, *zy, *wsx, *wsy, *pnx, *pny;
+};
+constexpr int kGdCols = 27;
+
+template <typename S>
+__device__ inline void gd_cols_assign(GdCols<S> &C, S *const (&a)[kGdCols]) {
+    S **f[kGdCols] = {&C.px, &C.py, &C.pn, &C.dpx, &C.dpy, &C.trc, &C.dscl, &C.rx, &C.ry, &C.dvx, &C.dvy, &C.vx,
+                      &C.vy, &C.qx, &C.qy, &C.pox, &C.poy, &C.sx, &C.sy, &C.nx, &C.ny, &C.zx, &C.zy, &C.wsx,
+                      &C.wsy, &C.pnx, &C.pny};
+    for (int k = 0; k < kGdCols; k++) *f[k] = a[k];
+}
+
+__device__ inline GdCols<double> gd_cols64(const PView &P) {
+    double *const a[kGdCols] = {P.c(W_PX), P.c(W_PY), P.c(W_PN), P.c(W_DPX), P.c(W_DPY), P.c(W_TRC), P.c(W_DSCL),
+                                P.c(W_RX), P.c(W_RY), P.c(W_DVX), P.c(W_DVY), P.c(W_VX), P.c(W_VY), P.c(W_QX),
+                                P.c(W_QY), P.c(W_POX), P.c(W_POY), P.c(W_SX), P.c(W_SY), P.c(W_NX), P.c(W_NY),
+                                P.c(W_ZX), P.c(W_ZY), P.c(W_WSX), P.c(W_WSY), P.c(W_PNX), P.c(W_PNY)};
+    GdCols<double> C;
+    gd_cols_assign(C, a);
+    return C;
+}
+
+// FP32 state: 27 float columns in the double columns W_FST .. W_FST + 13
+__device__ inline GdCols<float> gd_cols32(const PView &P) {
+    float *b = (float *)P.c(W_FST);
+    const size_t n = P.n;
+    float *const a[kGdCols] = {b, b + n, b + 2 * n, b + 3 * n, b + 4 * n, b + 5 * n, b + 6 * n, b + 7 * n, b + 8 * n,
+                               b + 9 * n, b + 10 * n, b + 11 * n, b + 12 * n, b + 13 * n, b + 14 * n, b + 15 * n,
+                               b + 16 * n, b + 17 * n, b + 18 * n, b + 19 * n, b + 20 * n, b + 21 * n, b + 22 * n,
+                               b + 23 * n, b + 24 * n, b + 25 * n, b + 26 * n};
+    GdCols<float> C;
+    gd_cols_assign(C, a);
+    return C;
+}
+
+template <typename S>
+__device__ inline LsArrays<S> ls_from_cols(const GdCols<S> &C) {
+    LsArrays<S> A;
+    A.dpx = C.dpx; A.dpy = C.dpy; A.dvx = C.dvx; A.dvy = C.dvy; A.vx = C.vx; A.vy = C.vy; A.qx = C.qx; A.qy = C.qy;
+    A.sx = C.sx; A.sy = C.sy; A.nox = C.nx; A.noy = C.ny; A.dscl = C.dscl; A.trc = C.trc;
+    A.pdx = nullptr; A.pdy = nullptr; A.pnx = C.pnx; A.pny = C.pny;
+    return A;
+}
+
+template <typename S>
+__device__ __noinline__ void gd_set_nt(const PView &P, const GdCols<S> &C) {
+    FOR_I(i, P.n) unit_dir<S>(C.px[i], C.py[i], C.nx[i], C.ny[i]);
+    __syncthreads();
+}
+
+// residual of the scaled gradient: -dscl s (adhesion), its tangential part (slip)
+template <typename S>
+__device__ __noinline__ void gd_set_residual(const PView &P, const GdCols<S> &C) {
+    const int *igs = P.igs();
+    FOR_I(i, P.n) {
+        if (igs[i] == Adhes) { C.rx[i] = -C.sx[i] * C.dscl[i]; C.ry[i] = -C.sy[i] * C.dscl[i]; }
+        else if (igs[i] == Slip) {
+            const S tx = -C.ny[i], ty = C.nx[i];
+            const S st = tx * C.sx[i] + ty * C.sy[i];
+            C.rx[i] = -st * tx * C.dscl[i]; C.ry[i] = -st * ty * C.dscl[i];
+        } else { C.rx[i] = S(0); C.ry[i] = S(0); }
     }
     __syncthreads();
-    int itgd = 0, it_fb = -99;
-    double dif = 2.0, difid = 1.0, dif1 = 0.0, beta = 1.0, alpha = 0.0, alpha0 = 0.0;
-    bool lchanged = false;
-    lstagn = false;
-    set_nt(P);
-    slip();
-    // mixed-precision tiers (PatchDesc::precision): 1 FP32 products only, 2 also FP32
-    // scaling and local element solves, 3 also an FP32 line search
-    const bool f32_diag = o32 && d.precision >= 2, f32_ls = o32 && d.precision >= 3;
-    if (f32_diag) compute_diagscaling<float>(P, coefs);
-    else compute_diagscaling<double>(P, coefs);
-    set_residual(P);
-    {
-        double m = 0.0; FOR_I(i, n) m = fmax(m, fmax(fabs(rx[i]), fabs(ry[i])));
-        m = block_max1(red, m);
-        if (m < tiny) dif = 0.0;
+}
+
+// project_searchdir, gdsteady.f90:639-803 (variants E_trl, E_down(k), E_keep(f))
+template <typename S>
+__device__ __noinline__ void gd_project_searchdir(const PView &P, const GdCols<S> &C, int imeth, int kdown) {
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx, my = P.my;
+    const int *igs = P.igs();
+    S *dvx = C.dvx, *dvy = C.dvy, *vx = C.vx, *vy = C.vy;
+    const S *nx = C.nx, *ny = C.ny, *trc = C.trc;
+    S *dxi = C.zx, *dyi = C.zy;   // copies of the input search direction (E_down)
+    const S fac_v = S(1000), fdecay = (S)d.fdecay, zero = S(0);
+    auto clampv = [&](S vt, S tb) { return (vt >= zero ? S(1) : S(-1)) * fmin(fabs(vt), fac_v * tb); };
+    __syncthreads();
+    if (imeth == 2) { FOR_I(i, P.n) { dxi[i] = dvx[i]; dyi[i] = dvy[i]; } __syncthreads(); }
+    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+        const int i0 = iy * mx;
+        int ii = (mx - 1) + i0;
+        vx[ii] = zero; vy[ii] = zero;
+        for (int ix = mx - 2; ix >= 0; ix--) {
+            ii = ix + i0;
+            const S tx = -ny[ii], ty = nx[ii];
+            if (imeth == 1) {
+                if (igs[ii] == Adhes) { vx[ii] = vx[ii + 1] + dvx[ii]; vy[ii] = vy[ii + 1] + dvy[ii]; }
+                else if (igs[ii] == Slip) {
+                    const S vt = clampv(tx * dvx[ii] + ty * dvy[ii], trc[ii]);
+                    vx[ii] = tx * vt; vy[ii] = ty * vt;
+                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                } else {
+                    vx[ii] = zero; vy[ii] = zero;
+                    dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
+                }
+            } else if (imeth == 2) {
+                if (igs[ii] == Adhes) {
+                    if (ix + 1 + kdown <= mx) {
+                        vx[ii] = vx[ii + 1] + dxi[ii] - dxi[ii + kdown];
+                        vy[ii] = vy[ii + 1] + dyi[ii] - dyi[ii + kdown];
+                    } else { vx[ii] = vx[ii + 1] + dxi[ii]; vy[ii] = vy[ii + 1] + dyi[ii]; }
+                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                } else {
+                    if (igs[ii] == Slip) {
+                        const S vt = clampv(tx * dxi[ii] + ty * dyi[ii], trc[ii]);
+                        vx[ii] = tx * vt; vy[ii] = ty * vt;
+                        dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                    } else {
+                        vx[ii] = zero; vy[ii] = zero;
+                        dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
+                    }
+                    for (int kk = 1; kk <= kdown; kk++) if (ix + 1 + kk <= mx) { dxi[ii + kk] = zero; dyi[ii + kk] = zero; }
+                }
+            } else {
+                if (igs[ii] == Adhes) {
+                    vx[ii] = fdecay * vx[ii + 1] + dvx[ii]; vy[ii] = fdecay * vy[ii + 1] + dvy[ii];
+                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                } else if (igs[ii] == Slip) {
+                    const S vt = clampv(tx * dvx[ii] + ty * dvy[ii], trc[ii]);
+                    vx[ii] = tx * vt; vy[ii] = ty * vt;
+                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
+                } else {
+                    vx[ii] = zero; vy[ii] = zero;
+                    dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
+                }
+            }
+        }
     }
-    while ((lchanged || dif > difid) && itgd < maxgd) {
-        itgd++;
-        FOR_I(i, n) { dvx[i] = rx[i]; dvy[i] = ry[i]; }
-        int imeth, kdown;
-        if (beta > d.betath || itgd - it_fb <= 1) { imeth = d.gd_meth; kdown = d.kdown; }
-        else { imeth = 2; kdown = d.kdowfb; it_fb = itgd; }
-        project_searchdir(P, imeth, kdown, trc);
-        if (o32) { prod_t<float>(*o32, dvx, dvy, qx, qy, OUT_INT, igs); nconv32++; }
-        else { prod_t<T>(op, dvx, dvy, qx, qy, OUT_INT, igs); nconv++; }
-        if (itgd <= 1) {
-            double a[2] = {0, 0};
-            FOR_I(i, n) { a[0] += rx[i] * rx[i] + ry[i] * ry[i]; a[1] += (rx[i] * qx[i] + ry[i] * qy[i]) * dscl[i]; }
-            block_sum<2>(red, a);
-            alpha0 = a[0] / a[1];
+    __syncthreads();
+}
+
+// compute_diagscaling on state S with element arithmetic in R
+template <typename S, typename R>
+__device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, const double coefs_d[2][2]) {
+    const PatchDesc &d = *P.d;
+    __syncthreads();
+    PHASE_START(tdg);
+    const int mx = P.mx, n = P.n;
+    const int *igs = P.igs();
+    S *dscl = C.dscl;
+    R coefs[2][2] = {{(R)coefs_d[0][0], (R)coefs_d[0][1]}, {(R)coefs_d[1][0], (R)coefs_d[1][1]}};
+    const R d_slp = (R)d.d_slp, pow_s = (R)d.pow_s;
+    int ndeg = 0;
+    FOR_I(ii, n) {
+        const int el = igs[ii];
+        if (el == Slip) {
+            int elnew = Slip;
+            R fac_s = R(0);
+            if (!slip_element<R>(d, coefs, (R)C.px[ii], (R)C.py[ii], (R)C.pn[ii], (R)C.sx[ii], (R)C.sy[ii], elnew, fac_s)) ndeg++;
+            else if (elnew == Slip) dscl[ii] = (S)(d_slp * pow(fac_s, pow_s));
+            else dscl[ii] = (S)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
+        } else if (el == Adhes) {
+            dscl[ii] = (S)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
         } else {
-            alpha0 = 0.5 * (alpha0 + alpha);
+            dscl[ii] = S(0);
+        }
+    }
+    ndeg = block_sumi1(P.sm->red, ndeg);
+    if (ndeg > 0 && threadIdx.x == 0) {
+        // serial pass with the reference's carry-over of elnew and fac_s (elements in order)
+        int elnew = Exter;
+        R fac_s = R(0);
+        for (int ii = 0; ii < n; ii++) {
+            const int el = igs[ii];
+            if (el == Slip) {
+                int e2 = el;
+                R f2 = fac_s;
+                if (slip_element<R>(d, coefs, (R)C.px[ii], (R)C.py[ii], (R)C.pn[ii], (R)C.sx[ii], (R)C.sy[ii], e2, f2)) {
+                    elnew = e2; fac_s = f2;
+                }
+            }
+            if (el == Slip && elnew == Slip) dscl[ii] = (S)(d_slp * pow(fac_s, pow_s));
+            else if (el == Adhes || elnew == Adhes) dscl[ii] = (S)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
+            else dscl[ii] = S(0);
+        }
+    }
+    __syncthreads();
+    PHASE_END(P, O_T_DIAG - O_T_TOTAL, tdg);
+}
+
+// scalar state of the iteration, carried across the switch from FP32 to FP64 state
+struct GdScal {
+    int itgd, it_fb;
+    double dif, difid, dif1, beta, alpha, alpha0;
+    bool lchanged;
+};
+
+struct GdCtx {
+    const Ops<double> *op64;
+    const Ops<float> *o32;
+    double coefs[2][2];
+    double facnel;
+    int tier;              // 0 plain, 1..4 mixed-precision tiers
+    bool have_base;        // residual replacement base valid (FP64 state)
+    int nconv64, nconv32, nls;
+};
+
+// slip s = ws + A dp: FP64 product, FP64 base + FP32 change (mixed, FP64 state), or FP32
+template <typename S>
+__device__ __noinline__ void gd_slip(const PView &P, const GdCols<S> &C, GdCtx &X) {
+    if constexpr (sizeof(S) == 8) {
+        if (X.o32) compute_slip_rr(P, *X.op64, *X.o32, X.have_base, X.nconv64, X.nconv32);
+        else compute_slip<double>(P, *X.op64, X.nconv64);
+    } else {
+        const int n = P.n;
+        const int *igs = P.igs();
+        FOR_I(i, n) { C.sx[i] = 0.0f; C.sy[i] = 0.0f; }
+        prod_t<float, float>(*X.o32, C.dpx, C.dpy, C.sx, C.sy, OUT_INT, igs); X.nconv32++;
+        FOR_I(i, n) if (igs[i] >= Adhes) { C.sx[i] += C.wsx[i]; C.sy[i] += C.wsy[i]; }
+        __syncthreads();
+    }
+}
+
+// search-direction product q = A dv
+template <typename S>
+__device__ inline void gd_product_q(const PView &P, const GdCols<S> &C, GdCtx &X) {
+    const int *igs = P.igs();
+    if constexpr (sizeof(S) == 8) {
+        if (X.o32) { prod_t<float, double>(*X.o32, C.dvx, C.dvy, C.qx, C.qy, OUT_INT, igs); X.nconv32++; }
+        else { prod_t<double, double>(*X.op64, C.dvx, C.dvy, C.qx, C.qy, OUT_INT, igs); X.nconv64++; }
+    } else {
+        prod_t<float, float>(*X.o32, C.dvx, C.dvy, C.qx, C.qy, OUT_INT, igs); X.nconv32++;
+    }
+}
+
+template <typename S>
+__device__ inline bool gd_linesearch(const PView &P, const GdCols<S> &C, GdCtx &X, double alpha0, double &alpha, int &its) {
+    if constexpr (sizeof(S) == 8) {
+        if (X.o32 && X.tier == 3) {
+            LsArrays<float> A;
+            ls_arrays(P, A);
+            return perform_linesearch<float>(P, A, alpha0, alpha, its);
+        }
+    }
+    return perform_linesearch<S>(P, ls_from_cols<S>(C), alpha0, alpha, its);
+}
+
+template <typename S>
+__device__ inline void gd_scaling(const PView &P, const GdCols<S> &C, const GdCtx &X) {
+    if constexpr (sizeof(S) == 8) {
+        if (X.o32 && X.tier >= 2) gd_diagscaling<double, float>(P, C, X.coefs);
+        else gd_diagscaling<double, double>(P, C, X.coefs);
+    } else {
+        gd_diagscaling<float, float>(P, C, X.coefs);
+    }
+}
+
+// dif (change of p, scaled by facdif) and difid (tolerance eps_stop) after an iteration
+template <typename S>
+__device__ inline void gd_difs(const PView &P, const GdCols<S> &C, const GdCtx &X, GdScal &g, double eps_stop,
+                               bool with_change) {
+    const int n = P.n;
+    double facdif;
+    if (g.beta >= 0.1) facdif = 1.0;
+    else if (g.beta >= 0.001) facdif = 0.1 / g.beta;
+    else facdif = 100.0;
+    double a[2] = {0, 0};
+    FOR_I(i, n) {
+        if (with_change) {
+            const S ex = C.pox[i] - C.px[i], ey = C.poy[i] - C.py[i];
+            a[0] += (double)(ex * ex + ey * ey);
+        }
+        a[1] += (double)(C.px[i] * C.px[i] + C.py[i] * C.py[i]);
+    }
+    block_sum<2>(P.sm->red, a);
+    if (with_change) g.dif = X.facnel * sqrt(a[0] / (2 * n)) * facdif;
+    g.difid = eps_stop * fmax(1e-6, X.facnel * sqrt(a[1] / (2 * n)));
+}
+
+// the GDsteady iterations (gdsteady.f90:9-606) on state S until the stopping test with
+// tolerance eps_stop holds or maxgd is reached; false on a failed line search
+template <typename S>
+__device__ __noinline__ bool gd_iterate(const PView &P, const GdCols<S> &C, GdCtx &X, GdScal &g, double eps_stop,
+                                        int maxgd) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n;
+    RedSmem &red = P.sm->red;
+    int *igs = P.igs(), *igsold = P.ci(I_OLD);
+    const S tiny = S(1e-12);
+    const bool r32 = (sizeof(S) == 4) || (X.o32 && X.tier >= 2);
+    while ((g.lchanged || g.dif > g.difid) && g.itgd < maxgd) {
+        g.itgd++;
+        FOR_I(i, n) { C.dvx[i] = C.rx[i]; C.dvy[i] = C.ry[i]; }
+        int imeth, kdown;
+        if (g.beta > d.betath || g.itgd - g.it_fb <= 1) { imeth = d.gd_meth; kdown = d.kdown; }
+        else { imeth = 2; kdown = d.kdowfb; g.it_fb = g.itgd; }
+        gd_project_searchdir<S>(P, C, imeth, kdown);
+        gd_product_q<S>(P, C, X);
+        if (g.itgd <= 1) {
+            double a[2] = {0, 0};
+            FOR_I(i, n) {
+                a[0] += (double)(C.rx[i] * C.rx[i] + C.ry[i] * C.ry[i]);
+                a[1] += (double)((C.rx[i] * C.qx[i] + C.ry[i] * C.qy[i]) * C.dscl[i]);
+            }
+            block_sum<2>(red, a);
+            g.alpha0 = a[0] / a[1];
+        } else {
+            g.alpha0 = 0.5 * (g.alpha0 + g.alpha);
         }
         int its_j = 0;
-        const bool ls_ok = f32_ls ? perform_linesearch<float>(P, alpha0, alpha, its_j)
-                                  : perform_linesearch<double>(P, alpha0, alpha, its_j);
-        if (!ls_ok) { err = dif; return -100000; }
-        nls += its_j;
+        if (!gd_linesearch<S>(P, C, X, g.alpha0, g.alpha, its_j)) return false;
+        X.nls += its_j;
         {
             double a[2] = {0, 0};
             FOR_I(i, n) if (igs[i] >= Adhes) {
-                double a0 = dscl[i] * qx[i], a1 = dscl[i] * qy[i];
-                a[0] += a0 * a0 + a1 * a1;
-                a[1] += rx[i] * rx[i] + ry[i] * ry[i];
+                const S a0 = C.dscl[i] * C.qx[i], a1 = C.dscl[i] * C.qy[i];
+                a[0] += (double)(a0 * a0 + a1 * a1);
+                a[1] += (double)(C.rx[i] * C.rx[i] + C.ry[i] * C.ry[i]);
             }
             block_sum<2>(red, a);
-            beta = alpha * sqrt(a[0]) / sqrt(a[1]);
+            g.beta = g.alpha * sqrt(a[0]) / sqrt(a[1]);
         }
+        const S al = (S)g.alpha;
         FOR_I(i, n) {
             igsold[i] = igs[i];
-            pox[i] = px[i]; poy[i] = py[i];
-            if (igs[i] >= Adhes) { dpx[i] += alpha * dvx[i]; dpy[i] += alpha * dvy[i]; }
+            C.pox[i] = C.px[i]; C.poy[i] = C.py[i];
+            if (igs[i] >= Adhes) { C.dpx[i] += al * C.dvx[i]; C.dpy[i] += al * C.dvy[i]; }
         }
-        apply_trcbnd(P, trc, dpx, dpy, px, py);
-        set_nt(P);
-        slip();
+        apply_trcbnd<S>(P, C.trc, C.dpx, C.dpy, C.px, C.py);
+        gd_set_nt<S>(P, C);
+        gd_slip<S>(P, C, X);
         // local optimisation (solve_elmtrc) and active-set updates
         int chg = 0;
         FOR_I(ii, n) {
             if (igsold[ii] == Slip) {
                 int elnew = igs[ii];
                 double cosdth;
-                if (f32_diag) {
-                    // mixed precision: the local element solve only feeds the release test below
-                    float prf[3] = {(float)px[ii], (float)py[ii], (float)pn[ii]};
-                    float sif[2] = {(float)sx[ii], (float)sy[ii]};
-                    const float cf[2][2] = {{(float)coefs[0][0], (float)coefs[0][1]}, {(float)coefs[1][0], (float)coefs[1][1]}};
+                if (r32) {
+                    // single precision: the local element solve only feeds the release test below
+                    float prf[3] = {(float)C.px[ii], (float)C.py[ii], (float)C.pn[ii]};
+                    float sif[2] = {(float)C.sx[ii], (float)C.sy[ii]};
+                    const float cf[2][2] = {{(float)X.coefs[0][0], (float)X.coefs[0][1]},
+                                            {(float)X.coefs[1][0], (float)X.coefs[1][1]}};
                     elm_solve<float>(elnew, cf, 1e-6f, 1.0f, 1.0f, prf, (float)d.fstat, sif);
-                    cosdth = (double)(((float)nx[ii] * prf[0] + (float)ny[ii] * prf[1]) / (float)trc[ii]);
+                    cosdth = (double)(((float)C.nx[ii] * prf[0] + (float)C.ny[ii] * prf[1]) / (float)C.trc[ii]);
                 } else {
-                    double pr[3] = {px[ii], py[ii], pn[ii]};
-                    double si[2] = {sx[ii], sy[ii]};
-                    elm_solve<double>(elnew, coefs, 1e-6, 1.0, 1.0, pr, d.fstat, si);
-                    cosdth = (nx[ii] * pr[0] + ny[ii] * pr[1]) / trc[ii];
+                    double pr[3] = {(double)C.px[ii], (double)C.py[ii], (double)C.pn[ii]};
+                    double si[2] = {(double)C.sx[ii], (double)C.sy[ii]};
+                    elm_solve<double>(elnew, X.coefs, 1e-6, 1.0, 1.0, pr, d.fstat, si);
+                    cosdth = ((double)C.nx[ii] * pr[0] + (double)C.ny[ii] * pr[1]) / (double)C.trc[ii];
                 }
-                double snrm = nx[ii] * sx[ii] + ny[ii] * sy[ii];
+                const S snrm = C.nx[ii] * C.sx[ii] + C.ny[ii] * C.sy[ii];
                 // the A->S test below only sees elements that were in adhesion
-                if ((snrm > 0.0 && (dscl[ii] >= 0.001 || elnew == Adhes)) || cosdth <= -0.5) { igs[ii] = Adhes; chg = 1; }
+                if ((snrm > S(0) && (C.dscl[ii] >= S(0.001) || elnew == Adhes)) || cosdth <= -0.5) { igs[ii] = Adhes; chg = 1; }
             } else if (igs[ii] == Adhes) {
-                double ptabs = sqrt(px[ii] * px[ii] + py[ii] * py[ii]);
-                if (ptabs >= trc[ii] - tiny) { igs[ii] = Slip; chg = 1; }
+                const S ptabs = sqrt(C.px[ii] * C.px[ii] + C.py[ii] * C.py[ii]);
+                if (ptabs >= C.trc[ii] - tiny) { igs[ii] = Slip; chg = 1; }
             }
         }
         chg = block_sumi1(red, chg);
-        lchanged = chg > 0;
-        if (f32_diag) compute_diagscaling<float>(P, coefs);
-        else compute_diagscaling<double>(P, coefs);
-        set_residual(P);
-        double facdif;
-        if (beta >= 0.1) facdif = 1.0;
-        else if (beta >= 0.001) facdif = 0.1 / beta;
-        else facdif = 100.0;
-        {
-            double a[2] = {0, 0};
-            FOR_I(i, n) {
-                double ex = pox[i] - px[i], ey = poy[i] - py[i];
-                a[0] += ex * ex + ey * ey;
-                a[1] += px[i] * px[i] + py[i] * py[i];
-            }
-            block_sum<2>(red, a);
-            dif = facnel * sqrt(a[0] / (2 * n)) * facdif;
-            difid = eps * fmax(1e-6, facnel * sqrt(a[1] / (2 * n)));
-        }
-        if (itgd == 1) dif1 = dif;
+        g.lchanged = chg > 0;
+        gd_scaling<S>(P, C, X);
+        gd_set_residual<S>(P, C);
+        gd_difs<S>(P, C, X, g, eps_stop, true);
+        if (g.itgd == 1) g.dif1 = g.dif;
     }
+    return true;
+}
+
+// set-up of the iteration on state S: traction bound, dp, normals, slip, scaling, residual
+template <typename S>
+__device__ __noinline__ void gd_start(const PView &P, const GdCols<S> &C, GdCtx &X, GdScal &g, bool fresh) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n, mx = P.mx;
+    const S fstat = (S)d.fstat;
+    FOR_I(i, n) {
+        C.trc[i] = fstat * C.pn[i];
+        if (fresh) C.dscl[i] = S(1);
+    }
+    if (fresh) {
+        FOR_I(ii, n) {
+            const int ix = ii % mx;
+            if (ix == mx - 1) { C.dpx[ii] = C.px[ii]; C.dpy[ii] = C.py[ii]; }
+            else { C.dpx[ii] = C.px[ii] - C.px[ii + 1]; C.dpy[ii] = C.py[ii] - C.py[ii + 1]; }
+        }
+    }
+    __syncthreads();
+    gd_set_nt<S>(P, C);
+    gd_slip<S>(P, C, X);
+    gd_scaling<S>(P, C, X);
+    gd_set_residual<S>(P, C);
+    if (fresh) {
+        double m = 0.0;
+        FOR_I(i, n) m = fmax(m, fmax(fabs((double)C.rx[i]), fabs((double)C.ry[i])));
+        m = block_max1(P.sm->red, m);
+        if (m < 1e-12) g.dif = 0.0;
+    }
+}
+
+// switch tolerance of tier 4: the FP32 iteration stops where single precision stops
+// resolving the change of the tractions; the FP64 iteration continues from there
+constexpr double kGdSwitchEps = 1e-5;
+
+// gdsteady, gdsteady.f90:9-606 (elastic).  Returns itgd (negated on stagnation);
+// lstagn as in the reference; returns -100000 when the line search has no bracket.
+// Mixed precision (o32 != nullptr): tiers 1-3 run the FP64 iteration with FP32 products
+// (see compute_slip_rr) and, from tier 2, FP32 element arithmetic; tier 4 runs the same
+// iteration on an FP32 state until its change falls below kGdSwitchEps and then continues
+// it, without a restart, on the FP64 state with tier-2 arithmetic.
+template <typename T>
+__device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd, double eps, double &err, bool &lstagn,
+                        int &nconv, int &nls, const Ops<float> *o32, int &nconv32) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n, mx = P.mx, my = P.my;
+    RedSmem &red = P.sm->red;
+    const int *igs = P.igs();
+    GdCtx X;
+    X.op64 = &op; X.o32 = o32; X.tier = o32 ? d.precision : 0; X.have_base = false;
+    X.nconv64 = 0; X.nconv32 = 0; X.nls = 0;
+    const size_t bsz = (size_t)4 * mx * my;
+    const size_t o0 = (size_t)mx + (size_t)my * 2 * mx;
+    X.coefs[0][0] = d.cf[0 * bsz + o0] / d.ga;
+    X.coefs[0][1] = d.cf[1 * bsz + o0] / d.ga;
+    X.coefs[1][0] = X.coefs[0][1];
+    X.coefs[1][1] = d.cf[2 * bsz + o0] / d.ga;
+    int nadh, nslip, nplast, nexter;
+    count_eldiv(P, nadh, nslip, nplast, nexter);
+    X.facnel = sqrt((double)(float)n / (double)(float)(nadh + nslip + nplast));
+    GdScal g;
+    g.itgd = 0; g.it_fb = -99; g.dif = 2.0; g.difid = 1.0; g.dif1 = 0.0; g.beta = 1.0; g.alpha = 0.0; g.alpha0 = 0.0;
+    g.lchanged = false;
+    lstagn = false;
+    const GdCols<double> C64 = gd_cols64(P);
+    bool ok = true;
+    if (o32 && X.tier >= 4) {
+        const GdCols<float> C32 = gd_cols32(P);
+        FOR_I(i, n) {
+            C32.pn[i] = (float)C64.pn[i]; C32.px[i] = (float)C64.px[i]; C32.py[i] = (float)C64.py[i];
+            C32.wsx[i] = (float)C64.wsx[i]; C32.wsy[i] = (float)C64.wsy[i];
+        }
+        __syncthreads();
+        gd_start<float>(P, C32, X, g, true);
+        ok = gd_iterate<float>(P, C32, X, g, fmax(eps, kGdSwitchEps), maxgd);
+        // continue on the FP64 state: same iteration counters, step lengths and scaling
+        FOR_I(i, n) {
+            C64.px[i] = C32.px[i]; C64.py[i] = C32.py[i]; C64.dpx[i] = C32.dpx[i]; C64.dpy[i] = C32.dpy[i];
+            C64.dscl[i] = C32.dscl[i];
+        }
+        __syncthreads();
+        X.tier = 2;
+        if (ok) {
+            gd_start<double>(P, C64, X, g, false);
+            gd_difs<double>(P, C64, X, g, eps, false);
+        }
+    } else {
+        gd_start<double>(P, C64, X, g, true);
+    }
+    if (ok) ok = gd_iterate<double>(P, C64, X, g, eps, maxgd);
+    nconv += X.nconv64; nconv32 += X.nconv32; nls += X.nls;
+    if (!ok) { err = g.dif; return -100000; }
     double resrms;
     {
         double a = 0; int c = 0;
-        FOR_I(i, n) if (igs[i] >= Adhes) { a += rx[i] * rx[i] + ry[i] * ry[i]; c += 2; }
+        FOR_I(i, n) if (igs[i] >= Adhes) { a += C64.rx[i] * C64.rx[i] + C64.ry[i] * C64.ry[i]; c += 2; }
         a = block_sum1(red, a); c = block_sumi1(red, c);
         resrms = sqrt(a / max(1, c));
     }
-    double res_dp = resrms / fmax(coefs[0][0], coefs[1][1]);
-    err = dif;
+    const double tiny = 1e-12;
+    double res_dp = resrms / fmax(X.coefs[0][0], X.coefs[1][1]);
+    err = g.dif;
     double conv = 1.0;
-    if (dif * dif1 > 0.0 && itgd > 1) conv = exp(log(dif / dif1) / (itgd - 1));
-    if (lchanged && itgd >= maxgd) lstagn = true;
-    else if (dif > difid && conv > 1.0 && itgd >= maxgd) lstagn = true;
-    else if (conv < 1.0 - tiny && res_dp > 5.0 * difid / (1.0 - conv)) { itgd = -itgd; lstagn = true; }
+    if (g.dif * g.dif1 > 0.0 && g.itgd > 1) conv = exp(log(g.dif / g.dif1) / (g.itgd - 1));
+    int itgd = g.itgd;
+    if (g.lchanged && itgd >= maxgd) lstagn = true;
+    else if (g.dif > g.difid && conv > 1.0 && itgd >= maxgd) lstagn = true;
+    else if (conv < 1.0 - tiny && res_dp > 5.0 * g.difid / (1.0 - conv)) { itgd = -itgd; lstagn = true; }
     return itgd;
 }
 
@@ -1396,8 +1694,8 @@ __device__ __noinline__ int tangcg(const PView &P, const Ops<T> &op, const T *Mx
             if (!use_fftprec) lchanged = true;
         }
         if (use_fftprec) {
-            convolve<T>(op.cv, rx, nullptr, zx, nullptr, 1, Mxx, nullptr, nullptr, OUT_INT, igs);
-            convolve<T>(op.cv, ry, nullptr, zy, nullptr, 1, Myy, nullptr, nullptr, OUT_INT, igs);
+            convolve<T, double>(op.cv, rx, nullptr, zx, nullptr, 1, Mxx, nullptr, nullptr, OUT_INT, igs);
+            convolve<T, double>(op.cv, ry, nullptr, zy, nullptr, 1, Myy, nullptr, nullptr, OUT_INT, igs);
             nconv++;
         } else {
             FOR_I(i, n) { zx[i] = rx[i]; zy[i] = ry[i]; }

@@ -24,7 +24,9 @@ extern "C" {
 
 /* library extension flag for cntc_setflags: 0 = FP64 throughout (default); mixed precision,
  * the FP64 iteration path with FP64 residual replacement: 1 = FP32 convolution products,
- * 2 = also FP32 diagonal scaling and local element solves, 3 = also an FP32 line search */
+ * 2 = also FP32 diagonal scaling and local element solves, 3 = also an FP32 line search,
+ * 4 = GDsteady on an FP32 state until single precision stops resolving the change, then the
+ * same iteration continued on the FP64 state with tier-2 arithmetic */
 #define CNTC_if_mixedprec 2010
 
 /* initialisation: cntc_initializeFirst 235-442, cntc_initializeFirst_new 446-472,
@@ -79,6 +81,17 @@ void cntc_calculate_batch(int *n, int *ire, int *icp, int *ierror);
  * before it returns.  The first call of a process looks up the array's device address and
  * creates the library's streams: make it before any stream capture of the caller. */
 void cntc_calculate_noalloc(int *ire, int *icp, int *ierror);
+/* extension (serving): queue the solve of (ire, icp) and return at once (ierror 0 when
+ * queued).  Queued solves are batched by free worker lanes as they arrive, up to a device
+ * memory admission budget, and run concurrently with earlier batches.  The problem's
+ * settings must not change until cntc_wait has returned for it. */
+void cntc_calculate_async(int *ire, int *icp, int *ierror);
+/* extension (serving): wait for a queued solve; ierror as cntc_calculate */
+void cntc_wait(int *ire, int *icp, int *ierror);
+/* extension: cntc_wait that also returns the time from queueing to completion (seconds) */
+void cntc_gb300_wait_latency(int *ire, int *icp, int *ierror, double *latency);
+/* extension: device-memory admission budget of the serving queue in GB (default 40) */
+void cntc_gb300_setadmissionbudget(double *gbytes);
 
 /* results: cntc_getFlags 4001-4160, cntc_getReferenceVelocity 4987-5017,
  * cntc_getHertzContact 5021-5066, cntc_getNumElements 5070-5099,

@@ -1,0 +1,73 @@
+"""Serving path: cntc_calculate_async / cntc_wait with continuous batching.
+
+Each result must be the same when the patch is solved alone (cntc_calculate) and when it
+shares device passes with other requests that arrive while earlier ones are running."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import cases as C
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("pn", "px", "py", "igs")
+SCALARS = ("fn", "fx", "fy", "mz", "pen", "itcg", "itgs", "ierror")
+
+
+def _cases(n, seed):
+    cs = C.batch_patches(n, seed=seed, mixed=1, eps=1e-8)
+    for c in cs:
+        c["potprm"] = [min(c["potprm"][0], 72), min(c["potprm"][1], 72)] + c["potprm"][2:]
+    return cs
+
+
+def _same(a, b):
+    for k in SCALARS:
+        assert a[k] == b[k], k
+    for k in FIELDS:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_async_results_equal_alone_and_in_mix(cntc):
+    cs = _cases(10, seed=21)
+    alone = []
+    for i, c in enumerate(cs):
+        cntc.setup_case(300 + i, 1, c)
+        assert cntc.calculate(300 + i, 1) == 0
+        alone.append(cntc.results(300 + i, 1))
+    for i, c in enumerate(cs):
+        cntc.setup_case(300 + i, 2, c)
+
+    def submit(idx, delay):
+        for i in idx:
+            assert cntc.calculate_async(300 + i, 2) == 0
+            time.sleep(delay)
+
+    # two waves: the second arrives while the first is on the device
+    t1 = threading.Thread(target=submit, args=(range(0, 5), 0.0))
+    t1.start()
+    t1.join()
+    time.sleep(0.02)
+    submit(range(5, 10), 0.005)
+    for i in range(len(cs)):
+        ierr, lat = cntc.wait(300 + i, 2, with_latency=True)
+        assert ierr == 0 and lat > 0.0
+    for i in range(len(cs)):
+        _same(cntc.results(300 + i, 2), alone[i])
+
+
+def test_async_refuses_duplicate_and_small_budget_completes(cntc):
+    cs = _cases(3, seed=22)
+    for i, c in enumerate(cs):
+        cntc.setup_case(320 + i, 1, c)
+    cntc.setadmissionbudget(1e-6)          # every request then runs alone
+    try:
+        for i in range(3):
+            assert cntc.calculate_async(320 + i, 1) == 0
+        assert cntc.calculate_async(320, 1) in (0, cntc.CNTC_err_other)
+        errs = [cntc.wait(320 + i, 1) for i in range(3)]
+        assert errs == [0, 0, 0]
+    finally:
+        cntc.setadmissionbudget(40.0)
