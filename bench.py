@@ -52,6 +52,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--max-side", type=int, default=0,
                     help="profiling aid: keep only patches with both sides <= this (0: all)")
+    ap.add_argument("--serving", action="store_true",
+                    help="serving stream (wheels x 2 patches, random-walk loads, Poisson arrivals, warm start)")
+    ap.add_argument("--wheels", type=int, default=256)
+    ap.add_argument("--time-steps", type=int, default=3)
+    ap.add_argument("--rate", type=float, default=25.0, help="Poisson arrival rate, requests/s")
     return ap.parse_args()
 
 
@@ -408,11 +413,111 @@ def run_reference(args, dist):
     }
 
 
+# ------------------------------------------------------------------------------------------
+# serving stream: wheels x 2 patches, each patch a fixed grid (32..128 square), creepages and
+# Fn on seeded random walks, every time step warm-started from the patch's previous traction;
+# requests arrive as a Poisson stream and are served by cntc_calculate_async / cntc_wait
+# ------------------------------------------------------------------------------------------
+def serving_cases(wheels, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(2 * wheels):
+        m = int(rng.integers(32, 129))
+        a = float(np.exp(rng.uniform(math.log(2.0), math.log(10.0))))
+        b = float(np.exp(rng.uniform(math.log(2.0), math.log(10.0))))
+        out.append(dict(tang=3, norm=1, bound=0, gausei=5, maxgs=999, maxin=100, maxnr=30, maxout=1, eps=1e-8,
+                        poiss=C.NU_STEEL, gg=C.G_STEEL, fstat=float(rng.uniform(0.2, 0.4)), veloc=10000.0,
+                        fn=float(rng.uniform(20e3, 150e3)), cksi=float(rng.uniform(-0.005, 0.005)),
+                        ceta=float(rng.uniform(-0.005, 0.005)), cphi=float(rng.uniform(-0.5, 0.5)) * 1e-3,
+                        ipotcn=-3, potprm=[m, m, a, b, 1.1], mixed=MIXED_TIER, iestim=1))
+    return out, rng
+
+
+def run_serving(args, dist):
+    import torch
+    import contact_gb300 as cg
+    torch.cuda.set_device(dist.local)
+    cg.load()
+    cases, rng = serving_cases(args.wheels, 3)
+    npatch = len(cases)
+    for i, c in enumerate(cases):
+        cg.setup_case(i + 1, 1, c)
+    # first solve of every patch (cold start) through the batched path
+    cg.calculate_batch(list(range(1, npatch + 1)), [1] * npatch)
+    rate = args.rate
+    total = npatch * args.time_steps
+    steps_done = [0] * npatch
+    free = list(range(npatch))
+    lat, lock = [], threading.Lock()
+    cv = threading.Condition(lock)
+    inflight = [0]
+
+    def waiter(i):
+        ierr, l = cg.wait(i + 1, 1, with_latency=True)
+        with cv:
+            lat.append((l, ierr))
+            inflight[0] -= 1
+            free.append(i)
+            cv.notify_all()
+
+    t0 = time.perf_counter()
+    t_next = t0
+    submitted = 0
+    threads = []
+    while submitted < total:
+        t_next += rng.exponential(1.0 / rate)
+        now = time.perf_counter()
+        if t_next > now:
+            time.sleep(t_next - now)
+        with cv:
+            cv.wait_for(lambda: len(free) > 0)
+            cand = [i for i in free if steps_done[i] < args.time_steps]
+            if not cand:
+                cv.wait_for(lambda: any(steps_done[i] < args.time_steps for i in free))
+                cand = [i for i in free if steps_done[i] < args.time_steps]
+            i = cand[int(rng.integers(len(cand)))]
+            free.remove(i)
+            inflight[0] += 1
+        c = cases[i]
+        c["cksi"] = float(np.clip(c["cksi"] + rng.normal(0, 2e-4), -0.005, 0.005))
+        c["ceta"] = float(np.clip(c["ceta"] + rng.normal(0, 2e-4), -0.005, 0.005))
+        c["fn"] = float(np.clip(c["fn"] + rng.normal(0, 2e3), 20e3, 150e3))
+        cg.setcreepages(i + 1, 1, c["cksi"], c["ceta"], c["cphi"])
+        cg.setnormalforce(i + 1, 1, c["fn"])
+        steps_done[i] += 1
+        assert cg.calculate_async(i + 1, 1) == 0
+        th = threading.Thread(target=waiter, args=(i,), daemon=True)
+        th.start()
+        threads.append(th)
+        submitted += 1
+    for th in threads:
+        th.join()
+    wall = time.perf_counter() - t0
+    ls = np.array([l for l, _ in lat])
+    errs = sum(1 for _, e in lat if e < 0)
+    if dist.rank != 0:
+        return None
+    return {"metric": METRIC, "value": total / wall, "unit": UNIT, "n_gpus": dist.world, "steps": args.time_steps,
+            "warmup": 1, "ms_per_step": wall * 1e3 / args.time_steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "mode": "serving",
+            "config": {"workload": "serving stream: %d wheels x 2 patches, grids 32..128 square, random-walk "
+                                   "creepages (2e-4) and Fn (2 kN), warm start, Poisson arrivals at %.1f/s, "
+                                   "admission budget 40 GB, %d time steps per patch" % (args.wheels, rate,
+                                                                                        args.time_steps),
+                       "requests": total},
+            "latency_ms": {"p50": float(np.percentile(ls, 50) * 1e3), "p99": float(np.percentile(ls, 99) * 1e3),
+                           "definition": "queueing to completion of each request"},
+            "failed_requests": errs}
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        out = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
+        if args.serving and args.impl != "reference":
+            out = run_serving(args, dist)
+        else:
+            out = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
         if out is not None:
             print(json.dumps(out), flush=True)
     finally:

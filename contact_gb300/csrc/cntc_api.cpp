@@ -633,8 +633,12 @@ struct Server {
             }
             std::vector<int> ire(batch.size()), icp(batch.size()), err(batch.size(), 0);
             for (size_t k = 0; k < batch.size(); k++) { ire[k] = batch[k]->ire; icp[k] = batch[k]->icp; }
+            const auto t_start = std::chrono::steady_clock::now();
             calculate_many((int)batch.size(), ire.data(), icp.data(), err.data());
             const auto now = std::chrono::steady_clock::now();
+            if (g_debug >= 2)
+                std::fprintf(stderr, "contact_gb300: serving pass of %zu requests (%.1f MB) took %.3f s\n", batch.size(),
+                             bytes / 1e6, std::chrono::duration<double>(now - t_start).count());
             {
                 std::lock_guard<std::mutex> lk(mu);
                 in_flight -= bytes;

@@ -451,8 +451,9 @@ __device__ __noinline__ void elm_solve(int &el, const R coef[2][2], R eps, R ome
                 R det = gradf[0][0] * gradf[1][1] - gradf[0][1] * gradf[1][0];
                 if (det == zero) itnr = maxnr;
                 else {
-                    dp[0] = -(gradf[1][1] * fk[0] - gradf[0][1] * fk[1]) / det;
-                    dp[1] = -(-gradf[1][0] * fk[0] + gradf[0][0] * fk[1]) / det;
+                    const R rdet = R(1) / det;
+                    dp[0] = -(gradf[1][1] * fk[0] - gradf[0][1] * fk[1]) * rdet;
+                    dp[1] = -(-gradf[1][0] * fk[0] + gradf[0][0] * fk[1]) * rdet;
                     pr[0] += dp[0]; pr[1] += dp[1];
                 }
                 si[0] = si0[0] + coef[0][0] * pr[0] + coef[0][1] * pr[1];
@@ -610,22 +611,38 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
                     dpy[ii] += pr[1] - py[ii];
                     px[ii] = pr[0]; py[ii] = pr[1];
                     sx[ii] = s[0]; sy[ii] = s[1];
+                    // propagate the new traction of element ii towards the trailing edge: p of an
+                    // adhesion element is the sum of the p in front of it and its dp (clipped to
+                    // the bound), slip elements keep p and take a new dp.  The traction in front
+                    // (pxn, pyn) and its element type are carried in registers.
+                    double pxn = px[ii], pyn = py[ii];
+                    int eln = igs[ii];
                     for (int kx = ix - ixinc; kx >= ixsta; kx -= ixinc) {
-                        int kk = (kx - 1) + (iy - 1) * mx, kn = kk + ixinc;
-                        if (igs[kk] == Adhes) {
-                            px[kk] = px[kn] + dpx[kk];
-                            py[kk] = py[kn] + dpy[kk];
-                            double ptabs = sqrt(px[kk] * px[kk] + py[kk] * py[kk]);
-                            double ptbnd = mus * pn[kk];
-                            if (ptabs > ptbnd) {
-                                px[kk] = px[kk] * ptbnd / ptabs; py[kk] = py[kk] * ptbnd / ptabs;
-                                dpx[kk] = px[kk] - px[kn]; dpy[kk] = py[kk] - py[kn];
+                        const int kk = (kx - 1) + (iy - 1) * mx;
+                        const int el = igs[kk];
+                        if (el == Adhes) {
+                            const double qx = pxn + dpx[kk], qy = pyn + dpy[kk];
+                            const double pp = qx * qx + qy * qy, ptbnd = mus * pn[kk];
+                            if (pp > ptbnd * ptbnd) {
+                                // clipped to the traction bound (|p| > bound compared in squares)
+                                const double f = ptbnd * inv_sqrt(pp);
+                                const double cx = qx * f, cy = qy * f;
+                                px[kk] = cx; py[kk] = cy;
+                                dpx[kk] = cx - pxn; dpy[kk] = cy - pyn;
+                                pxn = cx; pyn = cy;
+                            } else {
+                                px[kk] = qx; py[kk] = qy;
+                                pxn = qx; pyn = qy;
                             }
-                        } else if (igs[kk] == Slip || igs[kk] == Plast) {
-                            dpx[kk] = px[kk] - px[kn]; dpy[kk] = py[kk] - py[kn];
-                        } else if (igs[kk] <= Exter && igs[kn] >= Adhes) {
-                            dpx[kk] = -px[kn]; dpy[kk] = -py[kn];
+                        } else if (el == Slip || el == Plast) {
+                            const double cx = px[kk], cy = py[kk];
+                            dpx[kk] = cx - pxn; dpy[kk] = cy - pyn;
+                            pxn = cx; pyn = cy;
+                        } else {
+                            if (eln >= Adhes) { dpx[kk] = -pxn; dpy[kk] = -pyn; }
+                            pxn = px[kk]; pyn = py[kk];
                         }
+                        eln = el;
                     }
                 }
                 __syncthreads();
