@@ -22,6 +22,7 @@ CNTC_ic_force, CNTC_ic_frclaw, CNTC_ic_inflcf, CNTC_ic_mater = 1974, 1976, 1978,
 CNTC_ic_exrhs, CNTC_ic_iestim, CNTC_ic_output, CNTC_ic_flow, CNTC_ic_matfil = 1980, 1983, 1984, 1985, 1987
 CNTC_if_idebug, CNTC_if_ncase = 2000, 2005
 CNTC_if_mixedprec = 2010
+CNTC_if_groupctas = 2011
 CNTC_fld_h, CNTC_fld_mu, CNTC_fld_px, CNTC_fld_py, CNTC_fld_pn = 1, 2, 3, 4, 5
 CNTC_fld_ux, CNTC_fld_uy, CNTC_fld_un, CNTC_fld_sx, CNTC_fld_sy = 7, 8, 9, 15, 16
 CNTC_err_norm, CNTC_err_tang, CNTC_err_icp, CNTC_err_other = -27, -28, -31, -99
@@ -344,7 +345,7 @@ def kernel_launches():
 
 
 STAT_NAMES = ("nconv32", "nconv64", "nls", "status", "t_total", "t_conv", "t_ls", "t_diag", "t_gs", "t_norm",
-              "t_tang", "t_scan", "t_conv32", "conv_bytes", "t_start_ns", "t_end_ns")
+              "t_tang", "t_scan", "t_conv32", "conv_bytes", "t_start_ns", "t_end_ns", "ctas")
 
 
 def lastcopybytes():
@@ -422,9 +423,11 @@ def setup_case(ire, icp, case):
 
     Keys: tang, norm, bound, gausei, maxgs, maxin, maxnr, maxout, eps, gd (8 floats + kdowfb
     for G=5), poiss, gg, fstat, veloc, cksi, ceta, cphi, fn | pen, ipotcn, potprm,
-    h (element-wise undeformed distance, optional), mixed (0/1), dq (optional)."""
-    flags = [CNTC_ic_tang, CNTC_ic_bound, CNTC_ic_iestim, CNTC_if_mixedprec]
-    values = [case.get("tang", 3), case.get("bound", 0), case.get("iestim", 0), case.get("mixed", 0)]
+    h (element-wise undeformed distance, optional), mixed (0-4), dq (optional), group (CTAs
+    per patch: 0 automatic, 1 one CTA, n >= 2 a cooperative group of at most n)."""
+    flags = [CNTC_ic_tang, CNTC_ic_bound, CNTC_ic_iestim, CNTC_if_mixedprec, CNTC_if_groupctas]
+    values = [case.get("tang", 3), case.get("bound", 0), case.get("iestim", 0), case.get("mixed", 0),
+              case.get("group", 0)]
     setflags(ire, icp, flags, values)
     setfrictionmethod(ire, icp, 0, [case.get("fstat", 0.3), case.get("fstat", 0.3)])
     nu = case.get("poiss", 0.28)

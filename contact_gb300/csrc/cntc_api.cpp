@@ -77,8 +77,9 @@ struct Problem {
     // undeformed distance
     int ibase = 1;
     std::vector<double> prmudf = std::vector<double>(6, 0.0);
-    // engine settings (library extension, CNTC_if_mixedprec)
+    // engine settings (library extensions CNTC_if_mixedprec, CNTC_if_groupctas)
     int mixed = 0;
+    int group = 0;
     double eps32 = 1e-5;
     // results of the last calculation
     bool have = false;
@@ -198,7 +199,11 @@ int prepare(Problem &p, Prep &out) {
     // well); single rows (my = 1) are solved
     if (mx < 2 || my < 1) { log_msg("grids with mx < 2 are not supported"); return CNTC_err_other; }
     const int fx = cgb::opt_fft_size(mx), fy = cgb::opt_fft_size(my);
-    if (solve_smem_bytes(fx, fy) > 227 * 1024) { log_msg("patch too large for the single-block engine"); return CNTC_err_other; }
+    // one CTA per patch while its FFT lines fit the per-warp buffers, a cooperative group of
+    // CTAs for larger grids (or when CNTC_if_groupctas asks for one)
+    const int nblk = cgb::group_size(mx, my, fx, fy, p.group);
+    if (nblk < 1) { log_msg("patch too large for the device (shared memory of one FFT line)"); return CNTC_err_other; }
+    d.nblk = nblk;
     d.mx = mx; d.my = my; d.npot = mx * my; d.fx = fx; d.fy = fy;
     d.dx = dx; d.dy = dy; d.dxdy = dx * dy; d.xc1 = xl + 0.5 * dx; d.yc1 = yl + 0.5 * dy;
     d.tang = p.tang; d.norm = p.norm; d.bound = p.bound; d.iestim = p.iestim; d.force3 = p.force3;
@@ -282,6 +287,7 @@ void collect(Problem &p, const PatchDesc &d, const double *io) {
     p.itcg = (int)o[O_ITCG]; p.itgs = (int)o[O_ITGS]; p.solver = (int)o[O_SOLVER];
     p.ncon = (int)o[O_NCON]; p.nadh = (int)o[O_NADH]; p.nslip = (int)o[O_NSLIP];
     p.stats.assign(o + O_NCONV32, o + O_NSCAL);
+    p.stats.push_back((double)d.nblk);
     p.have = true;
     // kinematic outputs follow the reference: fn from the solution when N = 0
     if (p.norm == 0) p.fn = p.f_n;
@@ -332,7 +338,7 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
     bool any_upload = false;
     for (int k = 0; k < n; k++) {
         const PatchDesc &d = b.preps[live[k]].d;
-        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy);
+        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk);
         off_io[k] = tot_io; tot_io += s.io;
         off_work[k] = tot_work; tot_work += s.work;
         any_upload |= b.preps[live[k]].upload;
@@ -341,7 +347,7 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
     if ((e = grow((void **)&A.d_io, A.cap_io, tot_io, false)) != cudaSuccess) return (int)e;
     if ((e = grow((void **)&A.d_work, A.cap_work, tot_work, false)) != cudaSuccess) return (int)e;
     if ((e = grow((void **)&A.d_desc, A.cap_desc, n * sizeof(PatchDesc), false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.d_list, A.cap_list, 2 * n * sizeof(int) + 64, false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_list, A.cap_list, 3 * n * sizeof(int) + 64, false)) != cudaSuccess) return (int)e;
     if ((e = grow((void **)&A.h_io, A.cap_hio, tot_io, true)) != cudaSuccess) return (int)e;
     std::vector<PatchDesc> hd(n);
     std::vector<unsigned char> need_ic(n, 1);
@@ -444,7 +450,7 @@ int resident_setup(int n, const int *ire, const int *icp, int *ierror) {
     size_t tot_work = 0;
     for (int k = 0; k < m; k++) {
         const PatchDesc &d = b.preps[R->live[k]].d;
-        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy);
+        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk);
         R->off_io[k] = R->tot_io; R->tot_io += s.io;
         off_work[k] = tot_work; tot_work += s.work;
     }
@@ -453,7 +459,7 @@ int resident_setup(int n, const int *ire, const int *icp, int *ierror) {
     if ((e = grow((void **)&A.d_io, A.cap_io, R->tot_io, false)) != cudaSuccess) return (int)e;
     if ((e = grow((void **)&A.d_work, A.cap_work, tot_work, false)) != cudaSuccess) return (int)e;
     if ((e = grow((void **)&A.d_desc, A.cap_desc, m * sizeof(PatchDesc), false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.d_list, A.cap_list, 2 * m * sizeof(int) + 64, false)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_list, A.cap_list, 3 * m * sizeof(int) + 64, false)) != cudaSuccess) return (int)e;
     if ((e = grow((void **)&A.h_io, A.cap_hio, R->tot_io, true)) != cudaSuccess) return (int)e;
     R->hd.resize(m);
     R->need_ic.assign(m, 1);
@@ -554,7 +560,7 @@ int calculate_noalloc(int ire, int icp) {
     int st = prepare(*p, prep);
     if (st != 0) { p->have = false; return st; }
     PatchDesc hd = prep.d;
-    const PatchSizes s = patch_sizes(hd.mx, hd.my, hd.fx, hd.fy);
+    const PatchSizes s = patch_sizes(hd.mx, hd.my, hd.fx, hd.fy, hd.nblk);
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t off_list = up(sizeof(PatchDesc)), off_io = off_list + 256, off_work = off_io + up(s.io);
     if (off_work + s.work > kNoAllocBytes || s.io > sizeof(g_noalloc_host)) {
@@ -774,6 +780,7 @@ void cntc_setflags(int *ire, int *icp, int *lenflg, int *params, int *values) {
             case CNTC_ic_return: p->ret = std::max(0, std::min(3, v)); break;
             case CNTC_if_ncase: p->ncase = std::max(0, v - 1); break;
             case CNTC_if_mixedprec: p->mixed = (v >= 0 && v <= 4) ? v : 1; break;
+            case CNTC_if_groupctas: p->group = std::max(0, v); break;
             default: break;   // output, debugging and module-1 flags have no effect here
         }
     }
@@ -1029,6 +1036,7 @@ void cntc_getflags(int *ire, int *icp, int *lenflg, int *params, int *values) {
                 case CNTC_ic_iestim: v = p->iestim; break;
                 case CNTC_if_ncase: v = p->ncase; break;
                 case CNTC_if_mixedprec: v = p->mixed; break;
+                case CNTC_if_groupctas: v = p->group; break;
                 default: v = 0;
             }
         }

@@ -1,7 +1,11 @@
 // Device-side building blocks of the GB300 contact engine: complex arithmetic,
-// element-division codes and block-level reductions.  One thread block (CTA)
-// owns one contact patch; every scalar decision of the solver is made from a
-// block reduction and is therefore uniform across the CTA.
+// element-division codes, the patch group context and the reductions.
+//
+// A patch is solved by a group of thread blocks (CTAs): one CTA for grids whose FFT lines
+// fit the per-warp shared-memory buffers (the batched workloads), or a cooperative grid of
+// CTAs for large grids.  Every scalar decision of the solver is made from a reduction over
+// the whole group and is therefore uniform across it: within one CTA a deterministic
+// block tree, across CTAs the per-CTA partials summed in rank order by every CTA.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -39,6 +43,87 @@ struct RedSmem {
     int bcast_i[4];
 };
 
+// ---------------------------------------------------------------------------------------------
+// patch group: the CTAs that solve one patch together.  nblk == 1 is the single-CTA solve;
+// for nblk > 1 the CTAs are co-resident (cooperative launch) and meet at grid barriers.
+// Group scratch in global memory: bar[0] arrivals, bar[1] generation, bar[2] error flag;
+// part: two slots of nblk x kRedSlot partials (doubles), parti: the same for ints.
+// ---------------------------------------------------------------------------------------------
+constexpr int kRedSlot = 8;
+constexpr long long kBarrierTimeoutNs = 20000000000LL;   // a barrier gives up after 20 s
+
+struct GroupCtx {
+    int nblk, rank, seq;
+    unsigned *bar;
+    double *part;
+    int *parti;
+};
+
+__shared__ GroupCtx g_grp;
+
+__host__ __device__ inline size_t group_scratch_bytes(int nblk) {
+    return 256 + (size_t)2 * nblk * kRedSlot * (sizeof(double) + sizeof(int));
+}
+
+// set by every CTA at kernel start (thread 0), before its first barrier
+__device__ inline void group_init(int nblk, int rank, void *scratch) {
+    if (threadIdx.x == 0) {
+        g_grp.nblk = nblk;
+        g_grp.rank = rank;
+        g_grp.seq = 0;
+        g_grp.bar = (unsigned *)scratch;
+        g_grp.part = (double *)((char *)scratch + 256);
+        g_grp.parti = (int *)(g_grp.part + (size_t)2 * nblk * kRedSlot);
+    }
+    __syncthreads();
+}
+
+// element index of this thread within the group and the group's stride
+__device__ __forceinline__ int gtid() { return g_grp.rank * kThreads + threadIdx.x; }
+__device__ __forceinline__ int gstride() { return g_grp.nblk * kThreads; }
+// one thread of the whole group (global writes that must happen once)
+__device__ __forceinline__ bool glead() { return threadIdx.x == 0 && g_grp.rank == 0; }
+__device__ __forceinline__ bool grouped() { return g_grp.nblk > 1; }
+
+__device__ __forceinline__ long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return (long long)t;
+}
+
+// barrier of the group: a block barrier for one CTA; across CTAs a generation barrier on
+// the group scratch with memory fences on both sides (writes before it are visible to all
+// CTAs after it).  The wait is bounded: after kBarrierTimeoutNs the CTA sets the error flag
+// and returns; once the flag is set no CTA waits any more, so the solve runs out within its
+// iteration limits and the host reports the failure.
+__device__ __noinline__ void gsync_grid() {
+    if (threadIdx.x == 0) {
+        volatile unsigned *vb = g_grp.bar;
+        const unsigned gen = vb[1];
+        __threadfence();
+        const unsigned a = atomicAdd(g_grp.bar, 1u);
+        if (a == (unsigned)g_grp.nblk - 1) {
+            atomicExch(g_grp.bar, 0u);
+            __threadfence();
+            atomicAdd(g_grp.bar + 1, 1u);
+        } else {
+            const long long t0 = global_ns();
+            while (vb[1] == gen && vb[2] == 0u) {
+                __nanosleep(64);
+                if (global_ns() - t0 > kBarrierTimeoutNs) { atomicExch(g_grp.bar + 2, 1u); break; }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    __threadfence();
+}
+
+__device__ __forceinline__ void gsync() {
+    __syncthreads();
+    if (g_grp.nblk > 1) gsync_grid();
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     return v;
@@ -54,6 +139,45 @@ __device__ __forceinline__ double warp_max(double v) {
 __device__ __forceinline__ double warp_min(double v) {
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffffu, v, o));
     return v;
+}
+
+// Combine the block results v[0..K) (held by every thread of each CTA) over the CTAs of the
+// group: thread 0 of each CTA publishes its partials in the current slot, a grid barrier,
+// then warp 0 of every CTA combines all CTAs' partials in rank order (fixed lane split and
+// shuffle tree), so that every CTA obtains the same value.  op: 0 sum, 1 max, 2 min.
+template <typename V, int K>
+__device__ __forceinline__ void group_combine(RedSmem &s, V (&v)[K], V *bcast, int op) {
+    if (g_grp.nblk <= 1) return;
+    const int nb = g_grp.nblk, slot = g_grp.seq & 1;
+    V *part = (sizeof(V) == 8) ? (V *)(void *)g_grp.part : (V *)(void *)g_grp.parti;
+    part += (size_t)slot * nb * kRedSlot;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) part[g_grp.rank * kRedSlot + k] = v[k];
+    }
+    __syncthreads();
+    gsync_grid();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (w == 0) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            V t = (op == 0) ? V(0) : __ldcg(part + k);
+            for (int r = lane; r < nb; r += 32) {
+                const V x = __ldcg(part + (size_t)r * kRedSlot + k);
+                t = (op == 0) ? t + x : (op == 1 ? (t > x ? t : x) : (t < x ? t : x));
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const V y = __shfl_down_sync(0xffffffffu, t, o);
+                t = (op == 0) ? t + y : (op == 1 ? (t > y ? t : y) : (t < y ? t : y));
+            }
+            if (lane == 0) bcast[k] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = bcast[k];
+    if (threadIdx.x == 0) g_grp.seq++;
+    __syncthreads();
 }
 
 // sum of up to 4 doubles over the block, result broadcast to all threads
@@ -79,6 +203,7 @@ __device__ __forceinline__ void block_sum(RedSmem &s, double (&v)[K]) {
 #pragma unroll
     for (int k = 0; k < K; k++) v[k] = s.bcast_d[k];
     __syncthreads();
+    group_combine<double, K>(s, v, s.bcast_d, 0);
 }
 
 __device__ __forceinline__ double block_sum1(RedSmem &s, double v) {
@@ -109,6 +234,7 @@ __device__ __forceinline__ void block_sumi(RedSmem &s, int (&v)[K]) {
 #pragma unroll
     for (int k = 0; k < K; k++) v[k] = s.bcast_i[k];
     __syncthreads();
+    group_combine<int, K>(s, v, s.bcast_i, 0);
 }
 
 __device__ __forceinline__ int block_sumi1(RedSmem &s, int v) {
@@ -128,9 +254,10 @@ __device__ __forceinline__ double block_max1(RedSmem &s, double v) {
         if (lane == 0) s.bcast_d[0] = t;
     }
     __syncthreads();
-    double r = s.bcast_d[0];
+    double r[1] = {s.bcast_d[0]};
     __syncthreads();
-    return r;
+    group_combine<double, 1>(s, r, s.bcast_d, 1);
+    return r[0];
 }
 
 __device__ __forceinline__ double block_min1(RedSmem &s, double v) {
@@ -144,9 +271,10 @@ __device__ __forceinline__ double block_min1(RedSmem &s, double v) {
         if (lane == 0) s.bcast_d[0] = t;
     }
     __syncthreads();
-    double r = s.bcast_d[0];
+    double r[1] = {s.bcast_d[0]};
     __syncthreads();
-    return r;
+    group_combine<double, 1>(s, r, s.bcast_d, 2);
+    return r[0];
 }
 
 } // namespace cgb

@@ -82,10 +82,19 @@ struct SmemPlan {
     size_t off_tw64x, off_tw64y, off_tw32x, off_tw32y, off_wbuf, total;
 };
 
-__host__ __device__ inline SmemPlan smem_plan(int fx, int fy) {
+// single CTA (blk false): twiddle tables and one buffer region of 4 * max(NX, NY) complex
+// per warp in shared memory.  Patch group (blk true): one buffer region per CTA, the twiddle
+// tables live in the group scratch in global memory.
+__host__ __device__ inline SmemPlan smem_plan(int fx, int fy, bool blk = false) {
     SmemPlan s;
     s.NX = 2 * fx; s.NY = 2 * fy; s.nmax = s.NX > s.NY ? s.NX : s.NY;
     size_t o = 0;
+    if (blk) {
+        s.off_tw64x = s.off_tw64y = s.off_tw32x = s.off_tw32y = 0;
+        s.off_wbuf = 0;
+        s.total = (size_t)4 * s.nmax * 16;
+        return s;
+    }
     s.off_tw64x = o; o += (size_t)s.NX * 16;
     s.off_tw64y = o; o += (size_t)s.NY * 16;
     s.off_tw32x = o; o += (size_t)s.NX * 8;
@@ -96,24 +105,48 @@ __host__ __device__ inline SmemPlan smem_plan(int fx, int fy) {
     return s;
 }
 
+// twiddle tables of a patch group inside its scratch (after the barrier and partials):
+// convolution size NX, NY in FP64 and FP32, and the preconditioner period 2mx, 2my in FP64
+struct GroupTw {
+    size_t off64x, off64y, off32x, off32y, offpx, offpy, total;
+};
+
+__host__ __device__ inline GroupTw group_tw(int nblk, int mx, int my, int fx, int fy) {
+    GroupTw g;
+    size_t o = (group_scratch_bytes(nblk) + 255) & ~(size_t)255;
+    g.off64x = o; o += (size_t)2 * fx * 16;
+    g.off64y = o; o += (size_t)2 * fy * 16;
+    g.off32x = o; o += (size_t)2 * fx * 8;
+    g.off32y = o; o += (size_t)2 * fy * 8;
+    g.offpx = o; o += (size_t)2 * mx * 16;
+    g.offpy = o; o += (size_t)2 * my * 16;
+    g.total = (o + 255) & ~(size_t)255;
+    return g;
+}
+
 template <typename T>
 __device__ inline Conv<T> make_conv(const PatchDesc &d, unsigned char *smraw, const SmemPlan &sp) {
     Conv<T> cv;
+    const bool blk = d.nblk > 1;
     cv.mx = d.mx; cv.my = d.my; cv.fx = d.fx; cv.fy = d.fy;
     cv.NX = sp.NX; cv.NY = sp.NY; cv.nkx = d.fx + 1;
     fft_factorize(cv.NX, cv.px);
     fft_factorize(cv.NY, cv.py);
-    if (sizeof(T) == 8) {
+    cv.L = line_workers(blk);
+    if (blk) {
+        const GroupTw g = group_tw(d.nblk, d.mx, d.my, d.fx, d.fy);
+        char *base = (char *)d.gscr;
+        cv.twx = (C<T> *)(base + (sizeof(T) == 8 ? g.off64x : g.off32x));
+        cv.twy = (C<T> *)(base + (sizeof(T) == 8 ? g.off64y : g.off32y));
+    } else if (sizeof(T) == 8) {
         cv.twx = (C<T> *)(smraw + sp.off_tw64x);
         cv.twy = (C<T> *)(smraw + sp.off_tw64y);
-        cv.wbuf = (C<T> *)(smraw + sp.off_wbuf);
-        cv.wstride = 4 * sp.nmax;
     } else {
         cv.twx = (C<T> *)(smraw + sp.off_tw32x);
         cv.twy = (C<T> *)(smraw + sp.off_tw32y);
-        cv.wbuf = (C<T> *)(smraw + sp.off_wbuf);
-        cv.wstride = 4 * sp.nmax;
     }
+    cv.wbuf = (C<T> *)(smraw + sp.off_wbuf);
+    cv.wstride = 4 * sp.nmax;
     C<T> *R = (C<T> *)d.rbuf;
     cv.R0 = R;
     cv.R1 = R + (size_t)cv.nkx * cv.my;
@@ -148,14 +181,15 @@ __device__ inline void make_ops(Ops<T> &op, const PatchDesc &d, unsigned char *s
 __device__ __noinline__ void block_spectrum(const Conv<double> &cv, const double *src, double2 *S, double *K64,
                                             float *K32, double2 *a, double2 *b) {
     const int mx = cv.mx, my = cv.my, NX = cv.NX, NY = cv.NY, nkx = cv.nkx, fy = cv.fy;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const Lines &L = cv.L;
+    const int lane = L.lane, nl = L.nl;
     const int NONE = 1 << 30;
-    __syncthreads();
-    for (int pr = w; pr < NY / 2; pr += kWarps) {
+    gsync();
+    for (int pr = L.w0; pr < NY / 2; pr += L.nw) {
         const int r0 = 2 * pr, r1 = 2 * pr + 1;
         const int dy0 = r0 < my ? r0 : (r0 > NY - my ? r0 - NY : NONE);
         const int dy1 = r1 < my ? r1 : (r1 > NY - my ? r1 - NY : NONE);
-        for (int ix = lane; ix < NX; ix += 32) {
+        for (int ix = lane; ix < NX; ix += nl) {
             const int dx = ix < mx ? ix : (ix > NX - mx ? ix - NX : NONE);
             double v0 = 0, v1 = 0;
             if (dx != NONE) {
@@ -164,96 +198,114 @@ __device__ __noinline__ void block_spectrum(const Conv<double> &cv, const double
             }
             a[ix] = mkc<double>(v0, v1);
         }
-        double2 *z = warp_fft<double>(a, b, cv.px, cv.twx, -1);
-        for (int k = lane; k < nkx; k += 32) {
+        double2 *z = line_fft<double>(a, b, cv.px, cv.twx, -1, lane, nl, L.blk);
+        for (int k = lane; k < nkx; k += nl) {
             double2 zk = z[k], zn = z[(NX - k) % NX];
             S[(size_t)k * NY + r0] = mkc<double>(0.5 * (zk.x + zn.x), 0.5 * (zk.y - zn.y));
             S[(size_t)k * NY + r1] = mkc<double>(0.5 * (zk.y + zn.y), 0.5 * (zn.x - zk.x));
         }
-        __syncwarp();
+        line_sync(L.blk);
     }
-    __syncthreads();
-    for (int kx = w; kx < nkx; kx += kWarps) {
-        for (int iy = lane; iy < NY; iy += 32) a[iy] = S[(size_t)kx * NY + iy];
-        double2 *z = warp_fft<double>(a, b, cv.py, cv.twy, -1);
-        for (int ky = lane; ky <= fy; ky += 32) {
+    gsync();
+    for (int kx = L.w0; kx < nkx; kx += L.nw) {
+        for (int iy = lane; iy < NY; iy += nl) a[iy] = S[(size_t)kx * NY + iy];
+        double2 *z = line_fft<double>(a, b, cv.py, cv.twy, -1, lane, nl, L.blk);
+        for (int ky = lane; ky <= fy; ky += nl) {
             const size_t o = (size_t)kx * (fy + 1) + ky;
             K64[o] = z[ky].x;
             K32[o] = (float)z[ky].x;
         }
-        __syncwarp();
+        line_sync(L.blk);
     }
-    __syncthreads();
+    gsync();
 }
 
 // preconditioner kernel m = ga^2 IFFT(1 ./ FFT(c)) / (P Q) over the period P = 2mx, Q = 2my
 // (fft_makePrec, src/m_aijpj.f90:457-708), written in the layout of cf.  S: P*Q complex.
-__device__ __noinline__ void prec_spatial(const double *src, int mx, int my, double ga, const FftPlan &pp,
-                                          const FftPlan &pq, const double2 *twp, const double2 *twq, double2 *S,
-                                          double *dst, double2 *a, double2 *b) {
+__device__ __noinline__ void prec_spatial(const Lines &L, const double *src, int mx, int my, double ga,
+                                          const FftPlan &pp, const FftPlan &pq, const double2 *twp,
+                                          const double2 *twq, double2 *S, double *dst, double2 *a, double2 *b) {
     const int P = 2 * mx, Q = 2 * my;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    __syncthreads();
-    for (int iy = w; iy < Q; iy += kWarps) {
+    const int lane = L.lane, nl = L.nl;
+    gsync();
+    for (int iy = L.w0; iy < Q; iy += L.nw) {
         const int dy = iy < my ? iy : iy - Q;
-        for (int ix = lane; ix < P; ix += 32) {
+        for (int ix = lane; ix < P; ix += nl) {
             const int dx = ix < mx ? ix : ix - P;
             a[ix] = mkc<double>(src[(size_t)(dx + mx) + (size_t)(dy + my) * 2 * mx], 0.0);
         }
-        double2 *z = warp_fft<double>(a, b, pp, twp, -1);
-        for (int k = lane; k < P; k += 32) S[(size_t)iy * P + k] = z[k];
-        __syncwarp();
+        double2 *z = line_fft<double>(a, b, pp, twp, -1, lane, nl, L.blk);
+        for (int k = lane; k < P; k += nl) S[(size_t)iy * P + k] = z[k];
+        line_sync(L.blk);
     }
-    __syncthreads();
+    gsync();
     const double g2 = ga * ga;
-    for (int kx = w; kx < P; kx += kWarps) {
-        for (int iy = lane; iy < Q; iy += 32) a[iy] = S[(size_t)iy * P + kx];
-        double2 *z = warp_fft<double>(a, b, pq, twq, -1);
-        for (int ky = lane; ky < Q; ky += 32) {
+    for (int kx = L.w0; kx < P; kx += L.nw) {
+        for (int iy = lane; iy < Q; iy += nl) a[iy] = S[(size_t)iy * P + kx];
+        double2 *z = line_fft<double>(a, b, pq, twq, -1, lane, nl, L.blk);
+        for (int ky = lane; ky < Q; ky += nl) {
             const double2 c = z[ky];
             const double den = c.x * c.x + c.y * c.y;
             z[ky] = mkc<double>(g2 * c.x / den, -g2 * c.y / den);
         }
+        line_sync(L.blk);
         double2 *o = (z == a) ? b : a;
-        double2 *r = warp_fft<double>(z, o, pq, twq, +1);
-        for (int iy = lane; iy < Q; iy += 32) S[(size_t)iy * P + kx] = r[iy];
-        __syncwarp();
+        double2 *r = line_fft<double>(z, o, pq, twq, +1, lane, nl, L.blk);
+        for (int iy = lane; iy < Q; iy += nl) S[(size_t)iy * P + kx] = r[iy];
+        line_sync(L.blk);
     }
-    __syncthreads();
+    gsync();
     const double sc = 1.0 / ((double)P * (double)Q);
-    for (int iy = w; iy < Q; iy += kWarps) {
+    for (int iy = L.w0; iy < Q; iy += L.nw) {
         const int dy = iy < my ? iy : iy - Q;
-        for (int ix = lane; ix < P; ix += 32) a[ix] = S[(size_t)iy * P + ix];
-        double2 *z = warp_fft<double>(a, b, pp, twp, +1);
-        for (int ix = lane; ix < P; ix += 32) {
+        for (int ix = lane; ix < P; ix += nl) a[ix] = S[(size_t)iy * P + ix];
+        double2 *z = line_fft<double>(a, b, pp, twp, +1, lane, nl, L.blk);
+        for (int ix = lane; ix < P; ix += nl) {
             const int dx = ix < mx ? ix : ix - P;
             dst[(size_t)(dx + mx) + (size_t)(dy + my) * 2 * mx] = z[ix].x * sc;
         }
-        __syncwarp();
+        line_sync(L.blk);
     }
-    __syncthreads();
+    gsync();
 }
 
-__global__ void __launch_bounds__(kThreads) k_spectra(const PatchDesc *descs, const int *list) {
+// grid: one CTA per listed patch (group == 0), or the nblk CTAs of one patch group (group
+// != 0, cooperative launch, list[0] is the patch)
+__global__ void __launch_bounds__(kThreads) k_spectra(const PatchDesc *descs, const int *list, int group) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    const PatchDesc &d = descs[list[blockIdx.x]];
-    const SmemPlan sp = smem_plan(d.fx, d.fy);
+    const PatchDesc &d = descs[list[group ? 0 : blockIdx.x]];
+    const bool blk = group != 0;
+    group_init(blk ? d.nblk : 1, blk ? (int)blockIdx.x : 0, d.gscr);
+    const SmemPlan sp = smem_plan(d.fx, d.fy, blk);
     Conv<double> cv = make_conv<double>(d, smraw, sp);
     const int mx = d.mx, my = d.my;
-    const int w = threadIdx.x >> 5;
     const size_t bsz = (size_t)4 * mx * my;
     const size_t ksz = (size_t)cv.nkx * (d.fy + 1);
     double *K64 = const_cast<double *>(d.spec64);
     float *K32 = const_cast<float *>(d.spec32);
-    double2 *a = cv.wbuf + w * cv.wstride, *b = a + 2 * sp.nmax;
+    double2 *a = cv.wbuf + cv.L.widx * cv.wstride, *b = a + 2 * sp.nmax;
     // scratch in the work columns: S (complex), then the spatial preconditioner kernel
     double2 *S = (double2 *)d.wk;
     const size_t s_dbl = spectra_scratch_doubles(mx, my, d.fx, d.fy);
     double *msp = d.wk + s_dbl;
-    for (int blk = 0; blk < 4; blk++) {
-        make_twiddles<double>(cv.twx, cv.NX);
-        make_twiddles<double>(cv.twy, cv.NY);
-        block_spectrum(cv, d.cf + blk * bsz, S, K64 + blk * ksz, K32 + blk * ksz, a, b);
+    // twiddles of the preconditioner period: shared memory (single CTA, reusing the
+    // convolution tables) or their own tables in the group scratch
+    double2 *twpx = cv.twx, *twpy = cv.twy;
+    if (blk) {
+        const GroupTw g = group_tw(d.nblk, mx, my, d.fx, d.fy);
+        twpx = (double2 *)((char *)d.gscr + g.offpx);
+        twpy = (double2 *)((char *)d.gscr + g.offpy);
+        make_twiddles<double>(cv.twx, cv.NX, true);
+        make_twiddles<double>(cv.twy, cv.NY, true);
+        make_twiddles<double>(twpx, 2 * mx, true);
+        make_twiddles<double>(twpy, 2 * my, true);
+    }
+    for (int blkc = 0; blkc < 4; blkc++) {
+        if (!blk) {
+            make_twiddles<double>(cv.twx, cv.NX);
+            make_twiddles<double>(cv.twy, cv.NY);
+        }
+        block_spectrum(cv, d.cf + blkc * bsz, S, K64 + blkc * ksz, K32 + blkc * ksz, a, b);
     }
     // preconditioners zz -> 4, xx -> 5, yy -> 6
     FftPlan pp, pq;
@@ -261,12 +313,16 @@ __global__ void __launch_bounds__(kThreads) k_spectra(const PatchDesc *descs, co
     fft_factorize(2 * my, pq);
     const int srcblk[3] = {3, 0, 2};
     for (int k = 0; k < 3; k++) {
-        __syncthreads();
-        make_twiddles<double>(cv.twx, 2 * mx);
-        make_twiddles<double>(cv.twy, 2 * my);
-        prec_spatial(d.cf + srcblk[k] * bsz, mx, my, d.ga, pp, pq, cv.twx, cv.twy, S, msp, a, b);
-        make_twiddles<double>(cv.twx, cv.NX);
-        make_twiddles<double>(cv.twy, cv.NY);
+        gsync();
+        if (!blk) {
+            make_twiddles<double>(twpx, 2 * mx);
+            make_twiddles<double>(twpy, 2 * my);
+        }
+        prec_spatial(cv.L, d.cf + srcblk[k] * bsz, mx, my, d.ga, pp, pq, twpx, twpy, S, msp, a, b);
+        if (!blk) {
+            make_twiddles<double>(cv.twx, cv.NX);
+            make_twiddles<double>(cv.twy, cv.NY);
+        }
         block_spectrum(cv, msp, S, K64 + (4 + k) * ksz, K32 + (4 + k) * ksz, a, b);
     }
 }
@@ -297,7 +353,7 @@ __device__ __noinline__ void setup_patch(const PView &P) {
         if (d.iestim == 0) { pn[ii] = 0.0; igs[ii] = Exter; }
         if (d.iestim == 0 || d.iestim == 2 || d.tang == 0) { px[ii] = 0.0; py[ii] = 0.0; }
     }
-    __syncthreads();
+    gsync();
     const bool use_hz = (d.iestim == 0 && d.bound == 0 && d.ihertz >= 1);
     const double pi = 3.14159265358979323846;
     if ((d.bound == 2 || use_hz) && d.ihertz <= 3) {
@@ -316,7 +372,7 @@ __device__ __noinline__ void setup_patch(const PView &P) {
             pn[ii] = pnmax * fmax(0.0, f);
         }
     }
-    __syncthreads();
+    gsync();
     if ((d.bound >= 2 && d.bound <= 4) || use_hz) {
         FOR_I(ii, n) igs[ii] = (pn[ii] > (double)1e-20f) ? Adhes : Exter;
     } else if (d.iestim == 0) {
@@ -346,9 +402,9 @@ __device__ __noinline__ void setup_patch(const PView &P) {
         }
         FOR_I(ii, n) igs[ii] = (h[ii] - hmin < facpen * pentru) ? Adhes : Exter;
     }
-    __syncthreads();
+    gsync();
     FOR_I(ii, n) if (h[ii] > (double)1e29f) igs[ii] = Exter;
-    __syncthreads();
+    gsync();
 }
 
 // leading-edge fraction facdt (sxbnd, m_leadedge.f90:92-332) for rolling direction chi = 0
@@ -358,8 +414,8 @@ __device__ __noinline__ void compute_facdt(const PView &P, int solver, double *f
     const int *igs = P.igs();
     const bool is_roll = d.tang == 2 || d.tang == 3;
     const double fxdfac = (solver == 4) ? 2.0 : 1.0;
-    __syncthreads();
-    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+    gsync();
+    FOR_I(iy, my) {
         const int i0 = iy * mx;
         int ixb = mx;
         for (int ix = mx; ix >= 1; ix--) {
@@ -375,8 +431,10 @@ __device__ __noinline__ void compute_facdt(const PView &P, int solver, double *f
             }
         }
     }
-    __syncthreads();
+    gsync();
 }
+
+constexpr int kMaxGroupGsElements = 40000;
 
 // TANG, m_stang.f90:28-746 for Coulomb friction and prescribed creepages.
 // Returns ittang; -1000 when the reference would pick ConvexGS, -2000 on a failed line search.
@@ -395,7 +453,7 @@ __device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const O
     count_eldiv(P, nadh, nslip, nplast, nexter);
     const int k = nadh + nslip + nplast;
     int icount = 0;
-    for (int iy = threadIdx.x; iy < my; iy += kThreads) if (igs[iy * mx] >= Adhes) icount++;
+    FOR_I(iy, my) if (igs[iy * mx] >= Adhes) icount++;
     icount = block_sumi1(red, icount);
     int solver;
     if (is_ssrol) solver = (d.gausei == 5) ? 7 : (d.gausei != 2 ? 4 : 3);
@@ -413,6 +471,11 @@ __device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const O
     }
     solver_out = solver;
     if (solver == 3) return -1000;
+    // SteadyGS visits the elements one after another, with two group barriers per element in a
+    // patch group: beyond kMaxGroupGsElements a sweep would take seconds, so large groups
+    // refuse it (as the primary solver, and as GDsteady's fallback below)
+    const bool gs_ok = !grouped() || n <= kMaxGroupGsElements;
+    if (solver == 4 && !gs_ok) return -1000;
     // fixed part of the shift: wsfix = -facdt * hs with hs = -dq w (stang_rhs, K = 0)
     double *facdt = P.c(W_DSCL);
     compute_facdt(P, solver, facdt);
@@ -421,7 +484,7 @@ __device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const O
         wsx[i] = iel[i] ? -facdt[i] * wx[i] : 0.0;
         wsy[i] = iel[i] ? -facdt[i] * wy[i] : 0.0;
     }
-    __syncthreads();
+    gsync();
     int ittang = 0, itgs = 0;
     bool zready = false;
     double *one = P.c(W_ONE);
@@ -436,6 +499,7 @@ __device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const O
             bool lstagn = false;
             it = gdsteady<double>(P, op, d.maxgs, eps, errpt, lstagn, nconv, nls, o32, nconv32);
             if (it == -100000) return -2000;
+            if (lstagn && !gs_ok) return -1000;
             if (lstagn) it = stdygs(P, eps, d.maxgs, omegah, omegas, info, errpt);
         } else {
             if (o32) {
@@ -463,7 +527,7 @@ __device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const O
             areas(P);
             int ii0 = (max(1, mx / 2) - 1) + (max(1, my / 2) - 1) * mx;
             FOR_I(i, n) one[i] = 1.0;
-            __syncthreads();
+            gsync();
             int blk[2] = {0, 2};
             const double *vv[2] = {nullptr, nullptr};
             int rid[2] = {0, 1};
@@ -480,7 +544,7 @@ __device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const O
             if (newadh != 0) zready = false;
             if (info > 0) zready = true;
         }
-        __syncthreads();
+        gsync();
     }
     if (!zready) ittang = -1;
     itgs_out = itgs;
@@ -525,7 +589,7 @@ __device__ __noinline__ void soutpt(const PView &P, const Ops<T> &op, double pen
     const double fyrel = dxdy * a[2] / (fn * muscal + tiny);
     double mz = -dxdy * a[3] + dxdy * b[0];
     if (fabs(mz) < 0.5 * d.eps * (muscal * fn + tiny)) mz = 0.0;
-    if (threadIdx.x == 0) {
+    if (glead()) {
         out[O_FN] = fn;
         out[O_FX] = fxrel * (fn * muscal + tiny);
         out[O_FY] = fyrel * (fn * muscal + tiny);
@@ -537,7 +601,7 @@ __device__ __noinline__ void soutpt(const PView &P, const Ops<T> &op, double pen
         out[O_NADH] = c[0];
         out[O_NSLIP] = c[1];
     }
-    __syncthreads();
+    gsync();
 }
 
 // interior elements at the boundary of the potential contact (eldiv_count_atbnd,
@@ -559,11 +623,15 @@ __device__ __noinline__ int count_atbnd(const PView &P) {
 // ------------------------------------------------------------------------------------------
 // the patch solve
 // ------------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, const int *list) {
+// grid: one CTA per listed patch (group == 0), or the nblk CTAs of one patch group (group
+// != 0, cooperative launch, list[0] is the patch)
+__global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, const int *list, int group) {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ SolverSmem sm;
-    const PatchDesc &d = descs[list[blockIdx.x]];
-    const SmemPlan sp = smem_plan(d.fx, d.fy);
+    const PatchDesc &d = descs[list[group ? 0 : blockIdx.x]];
+    const bool blk = group != 0;
+    group_init(blk ? d.nblk : 1, blk ? (int)blockIdx.x : 0, d.gscr);
+    const SmemPlan sp = smem_plan(d.fx, d.fy, blk);
     PView P;
     P.d = &d; P.mx = d.mx; P.my = d.my; P.n = d.npot; P.sm = &sm;
     double *out = P.out();
@@ -576,8 +644,8 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
     make_ops<double>(op64, d, smraw, sp);
     op64.cv.tacc = &sm.t[O_T_CONV - O_T_TOTAL];
     op64.cv.bacc = &sm.algb;
-    make_twiddles<double>(op64.cv.twx, sp.NX);
-    make_twiddles<double>(op64.cv.twy, sp.NY);
+    make_twiddles<double>(op64.cv.twx, sp.NX, blk);
+    make_twiddles<double>(op64.cv.twy, sp.NY, blk);
     Ops<float> op32;
     const bool mixed = d.precision >= 1;
     if (mixed) {
@@ -585,13 +653,13 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
         op32.cv.tacc = &sm.t[O_T_CONV - O_T_TOTAL];
         op32.cv.tacc2 = &sm.t[O_T_CONV32 - O_T_TOTAL];
         op32.cv.bacc = &sm.algb;
-        make_twiddles<float>(op32.cv.twx, sp.NX);
-        make_twiddles<float>(op32.cv.twy, sp.NY);
+        make_twiddles<float>(op32.cv.twx, sp.NX, blk);
+        make_twiddles<float>(op32.cv.twy, sp.NY, blk);
     }
-    __syncthreads();
+    gsync();
     int status = ST_OK;
     if (op64.cv.px.nst < 0 || op64.cv.py.nst < 0) {
-        if (threadIdx.x == 0) { out[O_STATUS] = ST_BADSIZE; out[O_IERR] = -99; }
+        if (glead()) { out[O_STATUS] = ST_BADSIZE; out[O_IERR] = -99; }
         return;
     }
     // clear the work columns that the solvers expect at zero
@@ -603,7 +671,7 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
         }
         FOR_I(i, n) { P.ci(I_OLD)[i] = 0; P.ci(I_IEL)[i] = 0; }
     }
-    __syncthreads();
+    gsync();
     setup_patch(P);
     double pen = d.pen, fntrue = d.fntrue;
     int itnorm = 0, ittang = 0, itcg = 0, itgs = 0, solver = 0, nconv32 = 0, nconv64 = 0, nls = 0;
@@ -646,7 +714,9 @@ __global__ void __launch_bounds__(kThreads) k_solve(const PatchDesc *descs, cons
     if (threadIdx.x == 0) sm.t[O_T_TANG - O_T_TOTAL] = clock64() - t_tang0;
     soutpt<double>(P, op64, pen, fntrue, out);
     int atb = count_atbnd(P);
-    if (threadIdx.x == 0) {
+    // a barrier of the group that gave up (error flag in the group scratch)
+    if (blk && ((volatile unsigned *)g_grp.bar)[2] != 0u) status |= ST_GROUPFAIL;
+    if (glead()) {
         int ierr;
         if (status != ST_OK) ierr = -99;
         else if (itnorm < 0) ierr = -27;
@@ -705,7 +775,7 @@ int opt_fft_size(int fft_size) {
     return (int)prod;
 }
 
-PatchSizes patch_sizes(int mx, int my, int fx, int fy) {
+PatchSizes patch_sizes(int mx, int my, int fx, int fy, int nblk) {
     PatchSizes s;
     const size_t n = (size_t)mx * my;
     const size_t ksz = (size_t)(fx + 1) * (fy + 1);
@@ -719,12 +789,13 @@ PatchSizes patch_sizes(int mx, int my, int fx, int fy) {
     s.wk = align256(wkn * sizeof(double));
     s.wki = align256((size_t)(I_NCOL - 1) * n * sizeof(int));
     s.rbuf = align256((size_t)2 * (fx + 1) * my * 16);
-    s.work = s.cf + s.spec64 + s.spec32 + s.wk + s.wki + s.rbuf;
+    s.gscr = nblk > 1 ? group_tw(nblk, mx, my, fx, fy).total : 0;
+    s.work = s.cf + s.spec64 + s.spec32 + s.wk + s.wki + s.rbuf + s.gscr;
     return s;
 }
 
 void carve_patch(PatchDesc &d, char *io, char *work) {
-    const PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy);
+    const PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk);
     d.io = (double *)io;
     char *p = work;
     d.cf = (const double *)p; p += s.cf;
@@ -733,9 +804,10 @@ void carve_patch(PatchDesc &d, char *io, char *work) {
     d.wk = (double *)p; p += s.wk;
     d.wki = (int *)p; p += s.wki;
     d.rbuf = (void *)p; p += s.rbuf;
+    d.gscr = s.gscr ? (void *)p : nullptr; p += s.gscr;
 }
 
-size_t solve_smem_bytes(int fx, int fy) { return smem_plan(fx, fy).total; }
+size_t solve_smem_bytes(int fx, int fy, bool group) { return smem_plan(fx, fy, group).total; }
 
 static std::mutex g_attr_mu;
 static size_t g_attr_solve = 0, g_attr_spec = 0;
@@ -754,6 +826,47 @@ static cudaError_t ensure_smem_attr(size_t need) {
         g_attr_spec = need;
     }
     return e;
+}
+
+// dynamic shared memory a CTA of the patch kernels may use on the current device: the
+// opt-in maximum per block less the kernels' static shared memory
+size_t max_dynamic_smem() {
+    static std::mutex mu;
+    static size_t cached = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (cached) return cached;
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa, fb;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, k_solve) != cudaSuccess || cudaFuncGetAttributes(&fb, k_spectra) != cudaSuccess) {
+        cudaGetLastError();
+        return 227 * 1024 - 16384;     // no device: a conservative bound
+    }
+    cached = (size_t)optin - std::max(fa.sharedSizeBytes, fb.sharedSizeBytes);
+    return cached;
+}
+
+int group_size(int mx, int my, int fx, int fy, int requested) {
+    const size_t lim = max_dynamic_smem();
+    const bool fits1 = smem_plan(fx, fy, false).total <= lim;
+    if (requested == 1) return fits1 ? 1 : -1;
+    if (requested <= 0 && fits1) return 1;
+    const size_t sm = smem_plan(fx, fy, true).total;
+    if (sm > lim) return -1;
+    if (ensure_smem_attr(sm) != cudaSuccess) { cudaGetLastError(); return -1; }
+    int dev = 0, nsm = 0, occ_a = 0, occ_b = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_a, k_solve, kThreads, sm) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_b, k_spectra, kThreads, sm) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    const int cap = nsm * std::min(occ_a, occ_b);
+    if (cap < 2) return -1;
+    int want = requested >= 2 ? requested : (mx * my + kThreads - 1) / kThreads;
+    return std::max(2, std::min(want, cap));
 }
 
 // side streams of the calling host thread (created once, never destroyed before exit)
@@ -788,69 +901,102 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
         cudaEventRecord(timer->ev[2 * timer->nlaunch + (after ? 1 : 0)], stream);
         if (after) { timer->kind[timer->nlaunch] = kind; timer->nlaunch++; }
     };
-    // order: influence list first, then patches grouped by shared-memory class, largest first
-    std::vector<int> ic_list, order(n);
-    for (int i = 0; i < n; i++) { order[i] = i; if (compute_ic[i]) ic_list.push_back(i); }
+    auto smem_of = [&](int i) { return solve_smem_bytes(hdesc[i].fx, hdesc[i].fy, hdesc[i].nblk > 1); };
+    // order: influence list first, then the single-CTA patches grouped by shared-memory class,
+    // largest first, then the patch groups
+    std::vector<int> ic_list, ic_single, order, groups;
+    for (int i = 0; i < n; i++) {
+        if (compute_ic[i]) { ic_list.push_back(i); if (hdesc[i].nblk <= 1) ic_single.push_back(i); }
+        if (hdesc[i].nblk > 1) groups.push_back(i); else order.push_back(i);
+    }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        size_t sa = solve_smem_bytes(hdesc[a].fx, hdesc[a].fy), sb = solve_smem_bytes(hdesc[b].fx, hdesc[b].fy);
+        size_t sa = smem_of(a), sb = smem_of(b);
         if (sa != sb) return sa > sb;
         return hdesc[a].npot > hdesc[b].npot;
     });
+    const int nsingle = (int)order.size();
+    order.insert(order.end(), groups.begin(), groups.end());
     std::vector<int> all(ic_list);
+    all.insert(all.end(), ic_single.begin(), ic_single.end());
     all.insert(all.end(), order.begin(), order.end());
     cudaError_t e = cudaMemcpyAsync(d_list, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return (int)e;
     // the host vector must outlive the asynchronous copy
     e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess) return (int)e;
-    const int *d_ic = d_list, *d_order = d_list + ic_list.size();
+    const int *d_ic = d_list;
+    const int *d_ics = d_list + ic_list.size();
+    const int *d_order = d_ics + ic_single.size();
     size_t maxsm = 0;
-    for (int i = 0; i < n; i++) maxsm = std::max(maxsm, solve_smem_bytes(hdesc[i].fx, hdesc[i].fy));
+    for (int i = 0; i < n; i++) maxsm = std::max(maxsm, smem_of(i));
     e = ensure_smem_attr(maxsm);
     if (e != cudaSuccess) return (int)e;
     if (!ic_list.empty()) {
         int maxn = 0;
         size_t smax = 0;
-        for (int i : ic_list) {
-            maxn = std::max(maxn, 4 * hdesc[i].mx * hdesc[i].my);
-            smax = std::max(smax, solve_smem_bytes(hdesc[i].fx, hdesc[i].fy));
-        }
+        for (int i : ic_list) maxn = std::max(maxn, 4 * hdesc[i].mx * hdesc[i].my);
         dim3 g((maxn + kThreads - 1) / kThreads, (unsigned)ic_list.size());
         if (g.x > 64) g.x = 64;
         mark(0, false);
         k_influence<<<g, kThreads, 0, stream>>>(ddesc, d_ic);
         mark(0, true);
-        mark(1, false);
-        k_spectra<<<(unsigned)ic_list.size(), kThreads, smax, stream>>>(ddesc, d_ic);
-        mark(1, true);
-        g_launches += 2;
+        g_launches += 1;
+        if (!ic_single.empty()) {
+            for (int i : ic_single) smax = std::max(smax, smem_of(i));
+            mark(1, false);
+            k_spectra<<<(unsigned)ic_single.size(), kThreads, smax, stream>>>(ddesc, d_ics, 0);
+            mark(1, true);
+            g_launches += 1;
+        }
     }
     // one launch per shared-memory class (requirement within 25% of the class's first, largest
     // member); the classes run concurrently on side streams so that the SMs freed by one class
     // take CTAs of the others instead of idling until the slowest patch of a class finishes
     std::vector<std::pair<int, int>> classes;
-    for (int start = 0; start < n;) {
-        const size_t sm0 = solve_smem_bytes(hdesc[order[start]].fx, hdesc[order[start]].fy);
+    for (int start = 0; start < nsingle;) {
+        const size_t sm0 = smem_of(order[start]);
         int end = start + 1;
-        while (end < n && solve_smem_bytes(hdesc[order[end]].fx, hdesc[order[end]].fy) * 5 >= sm0 * 4) end++;
+        while (end < nsingle && smem_of(order[end]) * 5 >= sm0 * 4) end++;
         classes.push_back({start, end});
         start = end;
     }
-    SideStreams &ss = side_streams();
-    if (!ss.ok) return (int)cudaErrorNotReady;
     mark(2, false);
-    if ((e = cudaEventRecord(ss.fork, stream)) != cudaSuccess) return (int)e;
-    for (size_t c = 0; c < classes.size(); c++) {
-        cudaStream_t sc = ss.s[c % SideStreams::kN];
-        if (c < (size_t)SideStreams::kN && (e = cudaStreamWaitEvent(sc, ss.fork, 0)) != cudaSuccess) return (int)e;
-        const int start = classes[c].first, cnt = classes[c].second - classes[c].first;
-        const size_t sm0 = solve_smem_bytes(hdesc[order[start]].fx, hdesc[order[start]].fy);
-        k_solve<<<cnt, kThreads, sm0, sc>>>(ddesc, d_order + start);
-        g_launches += 1;
+    if (!classes.empty()) {
+        SideStreams &ss = side_streams();
+        if (!ss.ok) return (int)cudaErrorNotReady;
+        if ((e = cudaEventRecord(ss.fork, stream)) != cudaSuccess) return (int)e;
+        for (size_t c = 0; c < classes.size(); c++) {
+            cudaStream_t sc = ss.s[c % SideStreams::kN];
+            if (c < (size_t)SideStreams::kN && (e = cudaStreamWaitEvent(sc, ss.fork, 0)) != cudaSuccess) return (int)e;
+            const int start = classes[c].first, cnt = classes[c].second - classes[c].first;
+            const size_t sm0 = smem_of(order[start]);
+            k_solve<<<cnt, kThreads, sm0, sc>>>(ddesc, d_order + start, 0);
+            g_launches += 1;
+        }
+        for (int k = 0; k < SideStreams::kN && k < (int)classes.size(); k++) {
+            if ((e = cudaEventRecord(ss.join[k], ss.s[k])) != cudaSuccess) return (int)e;
+            if ((e = cudaStreamWaitEvent(stream, ss.join[k], 0)) != cudaSuccess) return (int)e;
+        }
     }
-    for (int k = 0; k < SideStreams::kN && k < (int)classes.size(); k++) {
-        if ((e = cudaEventRecord(ss.join[k], ss.s[k])) != cudaSuccess) return (int)e;
-        if ((e = cudaStreamWaitEvent(stream, ss.join[k], 0)) != cudaSuccess) return (int)e;
+    // patch groups: cooperative launches, one patch at a time on the caller's stream after
+    // all single-CTA work, so that nothing else of this library shares the SMs with them
+    for (int k = nsingle; k < (int)order.size(); k++) {
+        const int i = order[k];
+        const PatchDesc &h = hdesc[i];
+        const size_t sm = smem_of(i);
+        if ((e = cudaMemsetAsync(h.gscr, 0, 256, stream)) != cudaSuccess) return (int)e;
+        const int *lp = d_order + k;
+        int grp = 1;
+        void *args[3] = {(void *)&ddesc, (void *)&lp, (void *)&grp};
+        if (compute_ic[i]) {
+            e = cudaLaunchCooperativeKernel((const void *)k_spectra, dim3(h.nblk), dim3(kThreads), args, sm, stream);
+            if (e != cudaSuccess) return (int)e;
+            if ((e = cudaMemsetAsync(h.gscr, 0, 256, stream)) != cudaSuccess) return (int)e;
+            g_launches += 1;
+        }
+        e = cudaLaunchCooperativeKernel((const void *)k_solve, dim3(h.nblk), dim3(kThreads), args, sm, stream);
+        if (e != cudaSuccess) return (int)e;
+        g_launches += 1;
     }
     mark(2, true);
     return (int)cudaGetLastError();

@@ -36,7 +36,7 @@ enum OutScalar {
 };
 
 // solver status bits (O_STATUS)
-constexpr int ST_OK = 0, ST_UNSUPPORTED = 1, ST_NOBRACKET = 2, ST_NORMCG_DIV = 4, ST_BADSIZE = 8;
+constexpr int ST_OK = 0, ST_UNSUPPORTED = 1, ST_NOBRACKET = 2, ST_NORMCG_DIV = 4, ST_BADSIZE = 8, ST_GROUPFAIL = 16;
 
 struct PatchDesc {
     int mx, my, npot;
@@ -69,6 +69,11 @@ struct PatchDesc {
     const double *spec64;             // spectra [7][fx+1][fy+1]: xx, xy, yy, zz, M_zz, M_xx, M_yy
     const float *spec32;
     void *rbuf;                       // 2 * (fx+1) * my complex doubles
+    // patch group: nblk CTAs solve the patch together (1: a single CTA); gscr holds their
+    // barrier, reduction partials and twiddle tables (nblk > 1 only)
+    int nblk;
+    int pad2_;
+    void *gscr;
 };
 
 constexpr int kNumPhaseTimers = 9;   // O_T_TOTAL .. O_T_CONV32

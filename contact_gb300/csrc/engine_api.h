@@ -11,22 +11,33 @@ namespace cgb {
 // byte sizes of the per-patch device buffers: the io block (inputs and results) and the
 // work area (influence coefficients, spectra, solver columns, FFT column buffers)
 struct PatchSizes {
-    size_t io, cf, spec64, spec32, wk, wki, rbuf, work;
+    size_t io, cf, spec64, spec32, wk, wki, rbuf, gscr, work;
 };
 
-PatchSizes patch_sizes(int mx, int my, int fx, int fy);
+// nblk: CTAs of the patch group (1: the patch is solved by one CTA)
+PatchSizes patch_sizes(int mx, int my, int fx, int fy, int nblk = 1);
 
 // Assign the device pointers of d: io block at 'io' (patch_sizes().io bytes) and the work
 // buffers inside [work, work + patch_sizes().work).
 void carve_patch(PatchDesc &d, char *io, char *work);
 
-// dynamic shared memory needed by the solve kernel for FFT half sizes fx, fy
-size_t solve_smem_bytes(int fx, int fy);
+// dynamic shared memory needed by the solve kernel for FFT half sizes fx, fy, for a patch
+// solved by one CTA or (group) by a cooperative group of CTAs
+size_t solve_smem_bytes(int fx, int fy, bool group = false);
+
+// dynamic shared memory available to one CTA of the patch kernels on the current device
+size_t max_dynamic_smem();
+
+// CTAs of the group that solves an mx x my patch: 1 (one CTA) when the single-CTA plan fits
+// and requested <= 1; otherwise a cooperative group of min(requested or one element per
+// thread, co-resident CTAs of the device) CTAs.  requested: 0 automatic, 1 single CTA only,
+// n >= 2 a group of (at most) n CTAs.  Returns -1 when neither form fits the device.
+int group_size(int mx, int my, int fx, int fy, int requested);
 
 // Launch the engine for n patches whose descriptors live in device memory (ddesc) and
 // host memory (hdesc, same order).  compute_ic[i] != 0 requests influence coefficients and
 // spectra for patch i.  Patches are grouped by shared-memory class internally.
-// d_list is caller-owned device scratch for 2*n ints and must stay untouched until the
+// d_list is caller-owned device scratch for 3*n ints and must stay untouched until the
 // launched work has finished.  Returns a cudaError_t value.
 // Optional per-launch timing: when given, engine_run records ev[2k] before and ev[2k+1]
 // after its k-th kernel launch on 'stream' and sets kind[k] (0 influence coefficients,

@@ -8,6 +8,9 @@
 // coefficients are placed at (dx mod NX, dy mod NY); their spectra are real and
 // quadrant-symmetric (even/odd kernels), stored as (fx+1) x (fy+1) values per block.
 //
+// Lines are transformed by line workers: the warps of the CTA for patches solved by one CTA,
+// or the CTAs of the group (one CTA per line) for large patches.
+//
 //   step A  rows:    pairs of real rows (iy, iy+1) packed as one complex row, FFT over NX,
 //                    split into two Hermitian half spectra, stored column-major R[kx][iy]
 //   step B  columns: per kx, FFT over NY (only my non-zero inputs), multiply by the kernel
@@ -122,10 +125,10 @@ __device__ __forceinline__ void dft_small(C<T> (&v)[8], int dir) {
 // one Stockham stage of radix R: src -> dst, Ns = product of previous radices
 template <typename T, int R>
 __device__ __forceinline__ void stockham_stage(const C<T> *src, C<T> *dst, int n, int Ns,
-                                               const C<T> *tw, int dir, int lane) {
+                                               const C<T> *tw, int dir, int lane, int nl) {
     const int nb = n / R;
     const int tstep = n / (Ns * R);
-    for (int j = lane; j < nb; j += 32) {
+    for (int j = lane; j < nb; j += nl) {
         C<T> v[8];
         const int jm = j % Ns;
 #pragma unroll
@@ -149,11 +152,11 @@ __device__ __forceinline__ void stockham_stage(const C<T> *src, C<T> *dst, int n
 // O(p) sum; roots of unity come from the length-n table (W_p^e = tw[e * n/p])
 template <typename T>
 __device__ __forceinline__ void stockham_stage_generic(const C<T> *src, C<T> *dst, int n, int Ns, int R,
-                                                       const C<T> *tw, int dir, int lane) {
+                                                       const C<T> *tw, int dir, int lane, int nl) {
     const int nb = n / R;
     const int tstep = n / (Ns * R);
     const int wstep = n / R;
-    for (int t = lane; t < n; t += 32) {
+    for (int t = lane; t < n; t += nl) {
         const int j = t % nb, k = t / nb;
         const int jm = j % Ns;
         C<T> acc = mkc<T>(0, 0);
@@ -172,36 +175,67 @@ __device__ __forceinline__ void stockham_stage_generic(const C<T> *src, C<T> *ds
     }
 }
 
-// 1-D FFT of length n by one warp: input in a, scratch b; returns the buffer holding the
-// result. tw[k] = exp(-2 pi i k / n).
+// synchronisation of the threads that share one FFT line: a warp, or the whole CTA
+__device__ __forceinline__ void line_sync(bool blk) {
+    if (blk) __syncthreads(); else __syncwarp();
+}
+
+// 1-D FFT of length n by one line worker: a warp (lane = lane id, nl = 32) or the whole CTA
+// (lane = thread id, nl = kThreads, blk).  Input in a, scratch b; returns the buffer holding
+// the result, after a synchronisation of the worker.  tw[k] = exp(-2 pi i k / n).
 template <typename T>
-__device__ __noinline__ C<T> *warp_fft(C<T> *a, C<T> *b, const FftPlan &p, const C<T> *tw, int dir) {
-    const int lane = threadIdx.x & 31;
+__device__ __noinline__ C<T> *line_fft(C<T> *a, C<T> *b, const FftPlan &p, const C<T> *tw, int dir, int lane, int nl,
+                                       bool blk) {
     int Ns = 1;
     C<T> *src = a, *dst = b;
     for (int s = 0; s < p.nst; s++) {
         const int R = p.rad[s];
-        __syncwarp();
+        line_sync(blk);
         switch (R) {
-            case 8: stockham_stage<T, 8>(src, dst, p.n, Ns, tw, dir, lane); break;
-            case 4: stockham_stage<T, 4>(src, dst, p.n, Ns, tw, dir, lane); break;
-            case 2: stockham_stage<T, 2>(src, dst, p.n, Ns, tw, dir, lane); break;
-            case 3: stockham_stage<T, 3>(src, dst, p.n, Ns, tw, dir, lane); break;
-            case 5: stockham_stage<T, 5>(src, dst, p.n, Ns, tw, dir, lane); break;
-            case 7: stockham_stage<T, 7>(src, dst, p.n, Ns, tw, dir, lane); break;
-            default: stockham_stage_generic<T>(src, dst, p.n, Ns, R, tw, dir, lane); break;
+            case 8: stockham_stage<T, 8>(src, dst, p.n, Ns, tw, dir, lane, nl); break;
+            case 4: stockham_stage<T, 4>(src, dst, p.n, Ns, tw, dir, lane, nl); break;
+            case 2: stockham_stage<T, 2>(src, dst, p.n, Ns, tw, dir, lane, nl); break;
+            case 3: stockham_stage<T, 3>(src, dst, p.n, Ns, tw, dir, lane, nl); break;
+            case 5: stockham_stage<T, 5>(src, dst, p.n, Ns, tw, dir, lane, nl); break;
+            case 7: stockham_stage<T, 7>(src, dst, p.n, Ns, tw, dir, lane, nl); break;
+            default: stockham_stage_generic<T>(src, dst, p.n, Ns, R, tw, dir, lane, nl); break;
         }
         Ns *= R;
         C<T> *t = src; src = dst; dst = t;
     }
-    __syncwarp();
+    line_sync(blk);
     return src;
 }
 
-// twiddle table tw[k] = exp(-2 pi i k / n), filled by the whole block
+// 1-D FFT of length n by one warp
 template <typename T>
-__device__ inline void make_twiddles(C<T> *tw, int n) {
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+__device__ __forceinline__ C<T> *warp_fft(C<T> *a, C<T> *b, const FftPlan &p, const C<T> *tw, int dir) {
+    return line_fft<T>(a, b, p, tw, dir, threadIdx.x & 31, 32, false);
+}
+
+// line workers of a patch: the warps of the CTA (single-CTA solve) or the CTAs of the group
+// (cooperative solve of a large patch), each transforming one line at a time
+struct Lines {
+    int w0, nw;         // first line of this worker, number of workers (line stride)
+    int lane, nl;       // thread index within the worker, threads per worker
+    bool blk;           // worker = whole CTA
+    int widx;           // index of the worker's buffer region in this CTA
+};
+
+__device__ inline Lines line_workers(bool blk) {
+    Lines L;
+    L.blk = blk;
+    if (blk) { L.w0 = g_grp.rank; L.nw = g_grp.nblk; L.lane = threadIdx.x; L.nl = kThreads; L.widx = 0; }
+    else { L.w0 = threadIdx.x >> 5; L.nw = kWarps; L.lane = threadIdx.x & 31; L.nl = 32; L.widx = threadIdx.x >> 5; }
+    return L;
+}
+
+// twiddle table tw[k] = exp(-2 pi i k / n), filled by the whole block (a table in shared
+// memory), or by the whole group (a table in global memory, blk)
+template <typename T>
+__device__ inline void make_twiddles(C<T> *tw, int n, bool blk = false) {
+    const int k0 = blk ? gtid() : (int)threadIdx.x, ks = blk ? gstride() : (int)blockDim.x;
+    for (int k = k0; k < n; k += ks) {
         double s, c;
         sincospi(-2.0 * (double)k / (double)n, &s, &c);
         tw[k] = mkc<T>((T)c, (T)s);
@@ -215,9 +249,10 @@ template <typename T>
 struct Conv {
     int mx, my, NX, NY, fx, fy, nkx;
     FftPlan px, py;
-    C<T> *twx, *twy;        // shared: NX, NY
-    C<T> *wbuf;             // shared: per warp 4 * max(NX,NY)
-    int wstride;            // complex elements per warp buffer region
+    C<T> *twx, *twy;        // NX, NY: shared memory (single CTA) or global memory (group)
+    C<T> *wbuf;             // shared: per line worker 4 * max(NX,NY)
+    int wstride;            // complex elements per worker buffer region
+    Lines L;                // line workers
     C<T> *R0, *R1;          // global: nkx * my each, column-major [kx][iy]
     double scale;           // ga_inv / (NX NY)
     long long *tacc;        // shared accumulator of cycles spent in convolutions (may be null)
@@ -229,18 +264,19 @@ struct Conv {
 // into R0 (and R1).  'sel' optionally zeroes inputs outside a mask (mask[i] >= sel_lo).
 template <typename T, typename IO>
 __device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, const IO *in1, int ncomp) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const Lines &L = cv.L;
+    const int lane = L.lane, nl = L.nl;
     const int NX = cv.NX, mx = cv.mx, my = cv.my, nkx = cv.nkx;
-    C<T> *a = cv.wbuf + w * cv.wstride;
+    C<T> *a = cv.wbuf + L.widx * cv.wstride;
     C<T> *b = a + NX;
     const int npair = (my + 1) / 2;
     for (int comp = 0; comp < ncomp; comp++) {
         const IO *in = comp == 0 ? in0 : in1;
         C<T> *R = comp == 0 ? cv.R0 : cv.R1;
-        for (int pr = w; pr < npair; pr += kWarps) {
+        for (int pr = L.w0; pr < npair; pr += L.nw) {
             const int iy0 = 2 * pr, iy1 = 2 * pr + 1;
             const bool has1 = iy1 < my;
-            for (int ix = lane; ix < NX; ix += 32) {
+            for (int ix = lane; ix < NX; ix += nl) {
                 T re = 0, im = 0;
                 if (ix < mx) {
                     re = (T)in[iy0 * mx + ix];
@@ -248,8 +284,8 @@ __device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, con
                 }
                 a[ix] = mkc<T>(re, im);
             }
-            C<T> *z = warp_fft<T>(a, b, cv.px, cv.twx, -1);
-            for (int k = lane; k < nkx; k += 32) {
+            C<T> *z = line_fft<T>(a, b, cv.px, cv.twx, -1, lane, nl, L.blk);
+            for (int k = lane; k < nkx; k += nl) {
                 C<T> zk = z[k], zn = z[(NX - k) % NX];
                 // A = (Z[k] + conj Z[n-k]) / 2 ; B = (Z[k] - conj Z[n-k]) / (2i)
                 C<T> A = mkc<T>((T)0.5 * (zk.x + zn.x), (T)0.5 * (zk.y - zn.y));
@@ -257,6 +293,7 @@ __device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, con
                 R[(size_t)k * my + iy0] = A;
                 if (has1) R[(size_t)k * my + iy1] = B;
             }
+            line_sync(L.blk);
         }
     }
 }
@@ -266,23 +303,24 @@ __device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, con
 // K = {Kxx, Kxy, Kyy}.  Kernel blocks are (fx+1) x (fy+1) real, [kx][ky].
 template <typename T>
 __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0, const T *K1, const T *K2) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const Lines &L = cv.L;
+    const int lane = L.lane, nl = L.nl;
     const int NY = cv.NY, my = cv.my, nkx = cv.nkx, fy = cv.fy;
-    C<T> *a0 = cv.wbuf + w * cv.wstride;
+    C<T> *a0 = cv.wbuf + L.widx * cv.wstride;
     C<T> *b0 = a0 + NY;
     C<T> *a1 = b0 + NY;
     C<T> *b1 = a1 + NY;
-    for (int kx = w; kx < nkx; kx += kWarps) {
+    for (int kx = L.w0; kx < nkx; kx += L.nw) {
         C<T> *col0 = cv.R0 + (size_t)kx * my;
         C<T> *col1 = cv.R1 + (size_t)kx * my;
-        for (int iy = lane; iy < NY; iy += 32) {
+        for (int iy = lane; iy < NY; iy += nl) {
             a0[iy] = iy < my ? col0[iy] : mkc<T>(0, 0);
             if (ncomp == 2) a1[iy] = iy < my ? col1[iy] : mkc<T>(0, 0);
         }
-        C<T> *z0 = warp_fft<T>(a0, b0, cv.py, cv.twy, -1);
-        C<T> *z1 = (ncomp == 2) ? warp_fft<T>(a1, b1, cv.py, cv.twy, -1) : nullptr;
+        C<T> *z0 = line_fft<T>(a0, b0, cv.py, cv.twy, -1, lane, nl, L.blk);
+        C<T> *z1 = (ncomp == 2) ? line_fft<T>(a1, b1, cv.py, cv.twy, -1, lane, nl, L.blk) : nullptr;
         const size_t kb = (size_t)kx * (fy + 1);
-        for (int ky = lane; ky < NY; ky += 32) {
+        for (int ky = lane; ky < NY; ky += nl) {
             const int kq = ky <= fy ? ky : NY - ky;
             if (ncomp == 1) {
                 T k0 = K0[kb + kq];
@@ -296,17 +334,17 @@ __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0
             }
         }
         C<T> *o0 = (z0 == a0) ? b0 : a0;
-        C<T> *r0 = warp_fft<T>(z0, o0, cv.py, cv.twy, +1);
+        C<T> *r0 = line_fft<T>(z0, o0, cv.py, cv.twy, +1, lane, nl, L.blk);
         C<T> *r1 = nullptr;
         if (ncomp == 2) {
             C<T> *o1 = (z1 == a1) ? b1 : a1;
-            r1 = warp_fft<T>(z1, o1, cv.py, cv.twy, +1);
+            r1 = line_fft<T>(z1, o1, cv.py, cv.twy, +1, lane, nl, L.blk);
         }
-        for (int iy = lane; iy < my; iy += 32) {
+        for (int iy = lane; iy < my; iy += nl) {
             col0[iy] = r0[iy];
             if (ncomp == 2) col1[iy] = r1[iy];
         }
-        __syncwarp();
+        line_sync(L.blk);
     }
 }
 
@@ -319,19 +357,20 @@ constexpr int OUT_ADDINT = 2;   // u[i] += val where igs >= Adhes
 template <typename T, typename IO>
 __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1, int ncomp, int mode,
                               const int *igs) {
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const Lines &L = cv.L;
+    const int lane = L.lane, nl = L.nl;
     const int NX = cv.NX, mx = cv.mx, my = cv.my, nkx = cv.nkx;
-    C<T> *a = cv.wbuf + w * cv.wstride;
+    C<T> *a = cv.wbuf + L.widx * cv.wstride;
     C<T> *b = a + NX;
     const int npair = (my + 1) / 2;
     const T sc = (T)cv.scale;
     for (int comp = 0; comp < ncomp; comp++) {
         IO *out = comp == 0 ? out0 : out1;
         const C<T> *R = comp == 0 ? cv.R0 : cv.R1;
-        for (int pr = w; pr < npair; pr += kWarps) {
+        for (int pr = L.w0; pr < npair; pr += L.nw) {
             const int iy0 = 2 * pr, iy1 = 2 * pr + 1;
             const bool has1 = iy1 < my;
-            for (int k = lane; k < NX; k += 32) {
+            for (int k = lane; k < NX; k += nl) {
                 C<T> A, B;
                 if (k < nkx) {
                     A = R[(size_t)k * my + iy0];
@@ -343,8 +382,8 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1
                 // Z = A + i B
                 a[k] = mkc<T>(A.x - B.y, A.y + B.x);
             }
-            C<T> *z = warp_fft<T>(a, b, cv.px, cv.twx, +1);
-            for (int ix = lane; ix < mx; ix += 32) {
+            C<T> *z = line_fft<T>(a, b, cv.px, cv.twx, +1, lane, nl, L.blk);
+            for (int ix = lane; ix < mx; ix += nl) {
                 const int i0 = iy0 * mx + ix;
                 const IO v0 = (IO)(z[ix].x * sc);
                 if (mode == OUT_ALL) out[i0] = v0;
@@ -356,22 +395,23 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1
                     else if (igs[i1] >= Adhes) out[i1] = (mode == OUT_INT) ? v1 : out[i1] + v1;
                 }
             }
+            line_sync(L.blk);
         }
     }
 }
 
-// full product u = A p.  Synchronises the block before and after.
+// full product u = A p.  Synchronises the patch group before and after.
 template <typename T, typename IO = double>
 __device__ void convolve(const Conv<T> &cv, const IO *in0, const IO *in1, IO *out0, IO *out1,
                          int ncomp, const T *K0, const T *K1, const T *K2, int mode, const int *igs) {
-    __syncthreads();
+    gsync();
     long long t0 = clock64();
     conv_rows_fwd<T, IO>(cv, in0, in1, ncomp);
-    __syncthreads();
+    gsync();
     conv_cols<T>(cv, ncomp, K0, K1, K2);
-    __syncthreads();
+    gsync();
     conv_rows_inv<T, IO>(cv, out0, out1, ncomp, mode, igs);
-    __syncthreads();
+    gsync();
     if (threadIdx.x == 0) {
         const long long dt = clock64() - t0;
         if (cv.tacc) *cv.tacc += dt;

@@ -52,7 +52,8 @@ struct PView {
     __device__ float *f(int k) const { return (float *)c(W_FLS) + (size_t)k * n; }
 };
 
-#define FOR_I(i, n) for (int i = threadIdx.x; i < (n); i += kThreads)
+// strided loop of the patch group over n items (elements or rows)
+#define FOR_I(i, n) for (int i = gtid(); i < (n); i += gstride())
 
 // ------------------------------------------------------------------------------------------
 // small helpers
@@ -88,8 +89,8 @@ __device__ __noinline__ void areas(const PView &P) {
     const int mx = P.mx, my = P.my;
     const int *igs = P.igs();
     int *ext = P.ci(I_EXT);
-    __syncthreads();
-    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+    gsync();
+    FOR_I(iy, my) {
         const int i0 = iy * mx;
         int first = 1;
         while (igs[(first - 1) + i0] <= Exter && first != mx) first++;
@@ -98,7 +99,7 @@ __device__ __noinline__ void areas(const PView &P) {
         ext[iy] = first;
         ext[my + iy] = last;
     }
-    __syncthreads();
+    gsync();
 }
 
 // one row of A times a vector restricted to the row extents (gf3_AijPj, m_aijpj.f90:99-254):
@@ -115,7 +116,7 @@ __device__ __noinline__ void direct_rowsum(const PView &P, int ii, int nterm, co
     // iterate over (jy, jx) pairs; each thread takes a strided subset of the flattened range
     for (int jy = 1; jy <= my; jy++) {
         const int j0 = max(1, ext[jy - 1] - 1), j1 = min(mx, ext[my + jy - 1] + 1);
-        for (int jx = j0 + threadIdx.x; jx <= j1; jx += kThreads) {
+        for (int jx = j0 + gtid(); jx <= j1; jx += gstride()) {
             const size_t off = (size_t)(ix - jx + mx) + (size_t)(iy - jy + my) * 2 * mx;
             const int jj = (jx - 1) + (jy - 1) * mx;
             for (int t = 0; t < nterm; t++) {
@@ -179,7 +180,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
         hmin = block_min1(red, hmin) - pen;
         if (hmin >= 0.0) {
             FOR_I(i, n) { pn[i] = 0.0; igs[i] = Exter; }
-            __syncthreads();
+            gsync();
             err = 0.0;
             return 0;
         }
@@ -213,7 +214,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
             FOR_I(i, n) if (igs[i] >= Adhes) res[i] -= avg;
         }
     }
-    __syncthreads();
+    gsync();
     double rz1 = 0, rz2 = 0, rms_upd1 = 0, alpha = 0;
     int itcg = 0, itinn = 0;
     double rms_xk = 1.0, rms_upd = 2.0 * eps * rms_xk;
@@ -227,7 +228,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
             s = block_sum1(red, s); c = block_sumi1(red, c);
             double avg = s / (double)(float)max(1, c);
             FOR_I(i, n) if (igs[i] >= Adhes) z[i] -= avg;
-            __syncthreads();
+            gsync();
         }
         rz1 = rz2;
         {
@@ -256,7 +257,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
             s = block_sum1(red, s); c = block_sumi1(red, c);
             double avg = s / (double)(float)max(1, c);
             FOR_I(i, n) if (igs[i] >= Adhes) q[i] -= avg;
-            __syncthreads();
+            gsync();
         }
         double rv, vav;
         {
@@ -283,7 +284,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
         FOR_I(i, n) rprv[i] = res[i];
         if (itinn < numinn && rms_upd >= eps * rms_xk) {
             FOR_I(i, n) if (igs[i] >= Adhes) res[i] -= alpha * q[i];
-            __syncthreads();
+            gsync();
         } else {
             int chg = 0, dn = 0;
             FOR_I(i, n) if (igs[i] >= Adhes && pn[i] < 0.0) { igs[i] = Exter; pn[i] = 0.0; chg = 1; dn++; }
@@ -320,7 +321,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
                 davg = s / (double)(float)ncon;
                 FOR_I(i, n) if (igs[i] >= Adhes) dd[i] -= davg;   // proj_avg over AllInt (count = ncon)
             }
-            __syncthreads();
+            gsync();
             int nin = 0;
             FOR_I(i, n) {
                 res[i] = (igs[i] >= Adhes) ? -dd[i] : 0.0;
@@ -360,7 +361,7 @@ __device__ __noinline__ int snorm(const PView &P, const Ops<T> &op, int maxgs, i
         itnorm++;
         zready = true;
         FOR_I(i, n) if (igs[i] < Adhes) pn[i] = 0.0;
-        __syncthreads();
+        gsync();
         double errpn;
         int it = normcg<T>(P, op, maxgs, eps, pen, errpn, nconv);
         if (it < 0) { itcg_out = itcg; return -2; }
@@ -391,7 +392,7 @@ __device__ __noinline__ int snorm(const PView &P, const Ops<T> &op, int maxgs, i
     } while (!zready && itnorm < maxin);
     if (!zready) itnorm = -1;
     FOR_I(i, n) if (pn[i] < 0.0 && igs[i] >= Adhes) { pn[i] = 0.0; igs[i] = Exter; }
-    __syncthreads();
+    gsync();
     itcg_out = itcg;
     return itnorm;
 }
@@ -522,7 +523,7 @@ __device__ inline void stdygs_rowsum(const PView &P, const GsBox &b, int ii, con
     const size_t bsz = (size_t)4 * mx * my;
     const double *cxx = d.cf, *cxy = d.cf + bsz, *cyy = d.cf + 2 * bsz;
     double a[2] = {0.0, 0.0};
-    for (int k = threadIdx.x; k < b.cnt; k += kThreads) {
+    for (int k = gtid(); k < b.cnt; k += gstride()) {
         const int jy = b.jy0 + k / b.w, jx = b.jx0 + k % b.w;
         const int j0 = max(1, ext[jy - 1] - 1), j1 = min(mx, ext[my + jy - 1] + 1);
         if (jx < j0 || jx > j1) continue;
@@ -574,22 +575,22 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
             P.sm->bi[2] = jx1 >= jx0 ? jx1 - jx0 + 1 : 1;
             P.sm->bi[3] = (jy1 >= jy0 && jx1 >= jx0) ? (jy1 - jy0 + 1) * (jx1 - jx0 + 1) : 0;
         }
-        __syncthreads();
+        gsync();
         box.jy0 = P.sm->bi[0]; box.jx0 = P.sm->bi[1]; box.w = P.sm->bi[2]; box.cnt = P.sm->bi[3];
-        __syncthreads();
+        gsync();
     }
     int itgs = 0;
     double dif = 2.0, difid = 1.0, dif1 = 0.0;
     while (dif >= difid && itgs < maxgs) {
         itgs++;
-        double difacc = 0.0;      // held by thread 0
+        double difacc = 0.0;      // held by the group's lead thread
         for (int iy = 1; iy <= my; iy++) {
             for (int ix = ixsta; ix <= ixend; ix++) {
                 int ii = (ix - 1) + (iy - 1) * mx;
                 if (igs[ii] < Adhes) continue;
                 double s[2];
                 stdygs_rowsum(P, box, ii, dpx, dpy, s);
-                if (threadIdx.x == 0 && ix > ixsta) {
+                if (glead() && ix > ixsta) {
                     // the solver choice keeps the trailing column ix = 1 outside the contact area
                     int jx = ix - ixinc;
                     int jj = (jx - 1) + (iy - 1) * mx;
@@ -645,12 +646,11 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
                         eln = el;
                     }
                 }
-                __syncthreads();
+                gsync();
             }
         }
-        if (threadIdx.x == 0) P.sm->bd[0] = difacc;
-        __syncthreads();
-        dif = sqrt(P.sm->bd[0] / (2.0 * k));
+        // the lead thread's sum, broadcast to the group (the other threads add zeros)
+        dif = sqrt(block_sum1(red, glead() ? difacc : 0.0) / (2.0 * k));
         double a = 0; FOR_I(i, n) a += px[i] * px[i] + py[i] * py[i];
         a = block_sum1(red, a);
         double rms = sqrt(a / (2 * n));
@@ -676,10 +676,10 @@ template <typename R>
 __device__ __noinline__ void apply_trcbnd(const PView &P, const R *trc, R *dpx, R *dpy, R *px, R *py) {
     const int mx = P.mx, my = P.my;
     const int *igs = P.igs();
-    __syncthreads();
+    gsync();
     PHASE_START(tsc);
     const R zero = R(0);
-    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+    FOR_I(iy, my) {
         int ii = (mx - 1) + iy * mx;
         px[ii] = zero; py[ii] = zero;
         R pxn = zero, pyn = zero;
@@ -697,7 +697,7 @@ __device__ __noinline__ void apply_trcbnd(const PView &P, const R *trc, R *dpx, 
             pxn = qx; pyn = qy;
         }
     }
-    __syncthreads();
+    gsync();
     PHASE_END(P, O_T_SCAN - O_T_TOTAL, tsc);
 }
 
@@ -710,9 +710,9 @@ __device__ __noinline__ void project_searchdir(const PView &P, int imeth, int kd
     const double *nx = P.c(W_NX), *ny = P.c(W_NY);
     double *dxi = P.c(W_ZX), *dyi = P.c(W_ZY);   // copies of the input search direction (E_down)
     const double fac_v = 1000.0;
-    __syncthreads();
-    if (imeth == 2) { FOR_I(i, P.n) { dxi[i] = dvx[i]; dyi[i] = dvy[i]; } __syncthreads(); }
-    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+    gsync();
+    if (imeth == 2) { FOR_I(i, P.n) { dxi[i] = dvx[i]; dyi[i] = dvy[i]; } gsync(); }
+    FOR_I(iy, my) {
         const int i0 = iy * mx;
         int ii = (mx - 1) + i0;
         vx[ii] = 0.0; vy[ii] = 0.0;
@@ -765,7 +765,7 @@ __device__ __noinline__ void project_searchdir(const PView &P, int imeth, int kd
             }
         }
     }
-    __syncthreads();
+    gsync();
 }
 
 // compute_diagscaling, gdsteady.f90:901-1042.  In the reference 'elnew' and 'fac_s' carry over
@@ -823,7 +823,7 @@ __device__ inline bool slip_element(const PatchDesc &d, const R coefs[2][2], R p
 template <typename R>
 __device__ __noinline__ void compute_diagscaling(const PView &P, const double coefs_d[2][2]) {
     const PatchDesc &d = *P.d;
-    __syncthreads();
+    gsync();
     PHASE_START(tdg);
     const int mx = P.mx, n = P.n;
     const int *igs = P.igs();
@@ -847,7 +847,7 @@ __device__ __noinline__ void compute_diagscaling(const PView &P, const double co
         }
     }
     ndeg = block_sumi1(P.sm->red, ndeg);
-    if (ndeg > 0 && threadIdx.x == 0) {
+    if (ndeg > 0 && glead()) {
         // serial pass with the reference's carry-over of elnew and fac_s (elements in order)
         int elnew = Exter;
         R fac_s = R(0);
@@ -865,7 +865,7 @@ __device__ __noinline__ void compute_diagscaling(const PView &P, const double co
             else dscl[ii] = 0.0;
         }
     }
-    __syncthreads();
+    gsync();
     PHASE_END(P, O_T_DIAG - O_T_TOTAL, tdg);
 }
 
@@ -890,7 +890,7 @@ __device__ inline void ls_arrays(const PView &P, LsArrays<float> &A) {
     A.dpx = f[0]; A.dpy = f[1]; A.dvx = f[2]; A.dvy = f[3]; A.vx = f[4]; A.vy = f[5]; A.qx = f[6]; A.qy = f[7];
     A.sx = f[8]; A.sy = f[9]; A.nox = f[10]; A.noy = f[11]; A.dscl = f[12]; A.trc = f[13];
     A.pdx = P.f(14); A.pdy = P.f(15); A.pnx = P.f(16); A.pny = P.f(17);
-    __syncthreads();
+    gsync();
 }
 
 // perform_linesearch, gdsteady.f90:1046-1462.  Evaluations of rho(alpha) are block-parallel;
@@ -914,7 +914,7 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, const LsArrays<R
     bool has_bracket = false;
     int j = 0;
     if (threadIdx.x == 0) { S.alpha_j = 0.0; S.stop_j = 0; S.nobracket = 0; }
-    __syncthreads();
+    gsync();
     // adhesion elements keep their status during the search and their terms do not depend on
     // the trial tractions: their part of rho is the quadratic qa0 + 2 alpha qa1 + alpha^2 qa2
     double qa[3] = {0.0, 0.0, 0.0};
@@ -934,7 +934,7 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, const LsArrays<R
         // trial tractions: the traction-bound scan of dp + alpha dv along each row (apply_trcbnd)
         {
             PHASE_START(tsc);
-            for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+            FOR_I(iy, my) {
                 int ii = (mx - 1) + iy * mx;
                 A.pnx[ii] = R(0); A.pny[ii] = R(0);
                 R pxn = R(0), pyn = R(0);
@@ -952,7 +952,7 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, const LsArrays<R
                     pxn = qx; pyn = qy;
                 }
             }
-            __syncthreads();
+            gsync();
             PHASE_END(P, O_T_SCAN - O_T_TOTAL, tsc);
         }
         double acc[4] = {0, 0, 0, 0};     // rho, c0, c1, c2 of the slip elements
@@ -1089,13 +1089,13 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, const LsArrays<R
             S.stop_j = stop ? 1 : 0;
             S.jcount = j;
         }
-        __syncthreads();
+        gsync();
         if (S.stop_j) break;
     }
     alpha_out = S.alpha_j;
     jout = S.jcount;
     bool ok = !S.nobracket;
-    __syncthreads();
+    gsync();
     PHASE_END(P, O_T_LS - O_T_TOTAL, tls);
     return ok;
 }
@@ -1110,7 +1110,7 @@ __device__ __noinline__ void compute_slip(const PView &P, const Ops<T> &op, int 
     FOR_I(i, n) { sx[i] = 0.0; sy[i] = 0.0; }
     prod_t<T>(op, P.c(W_DPX), P.c(W_DPY), sx, sy, OUT_INT, igs); nconv++;
     FOR_I(i, n) if (igs[i] >= Adhes) { sx[i] += wsx[i]; sy[i] += wsy[i]; }
-    __syncthreads();
+    gsync();
 }
 
 // Mixed precision slip s = ws + A dp, with A dp = A dp_b + A (dp - dp_b): the base product
@@ -1148,7 +1148,7 @@ __device__ __noinline__ void compute_slip_rr(const PView &P, const Ops<double> &
             else { sx[i] = 0.0; sy[i] = 0.0; }
         }
         have_base = true;
-        __syncthreads();
+        gsync();
         return;
     }
     FOR_I(i, n) {
@@ -1156,14 +1156,14 @@ __device__ __noinline__ void compute_slip_rr(const PView &P, const Ops<double> &
         else { sx[i] = 0.0; sy[i] = 0.0; }
     }
     prod_t<float>(o32, tx, ty, sx, sy, OUT_ADDINT, igs); nconv32++;
-    __syncthreads();
+    gsync();
 }
 
 __device__ __noinline__ void set_nt(const PView &P) {
     const double *px = P.c(W_PX), *py = P.c(W_PY);
     double *nx = P.c(W_NX), *ny = P.c(W_NY);
     FOR_I(i, P.n) unit_dir(px[i], py[i], nx[i], ny[i]);
-    __syncthreads();
+    gsync();
 }
 
 __device__ __noinline__ void set_residual(const PView &P) {
@@ -1178,7 +1178,7 @@ __device__ __noinline__ void set_residual(const PView &P) {
             rx[i] = -st * tx * dscl[i]; ry[i] = -st * ty * dscl[i];
         } else { rx[i] = 0.0; ry[i] = 0.0; }
     }
-    __syncthreads();
+    gsync();
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1235,7 +1235,7 @@ __device__ inline LsArrays<S> ls_from_cols(const GdCols<S> &C) {
 template <typename S>
 __device__ __noinline__ void gd_set_nt(const PView &P, const GdCols<S> &C) {
     FOR_I(i, P.n) unit_dir<S>(C.px[i], C.py[i], C.nx[i], C.ny[i]);
-    __syncthreads();
+    gsync();
 }
 
 // residual of the scaled gradient: -dscl s (adhesion), its tangential part (slip)
@@ -1250,7 +1250,7 @@ __device__ __noinline__ void gd_set_residual(const PView &P, const GdCols<S> &C)
             C.rx[i] = -st * tx * C.dscl[i]; C.ry[i] = -st * ty * C.dscl[i];
         } else { C.rx[i] = S(0); C.ry[i] = S(0); }
     }
-    __syncthreads();
+    gsync();
 }
 
 // project_searchdir, gdsteady.f90:639-803 (variants E_trl, E_down(k), E_keep(f))
@@ -1264,9 +1264,9 @@ __device__ __noinline__ void gd_project_searchdir(const PView &P, const GdCols<S
     S *dxi = C.zx, *dyi = C.zy;   // copies of the input search direction (E_down)
     const S fac_v = S(1000), fdecay = (S)d.fdecay, zero = S(0);
     auto clampv = [&](S vt, S tb) { return (vt >= zero ? S(1) : S(-1)) * fmin(fabs(vt), fac_v * tb); };
-    __syncthreads();
-    if (imeth == 2) { FOR_I(i, P.n) { dxi[i] = dvx[i]; dyi[i] = dvy[i]; } __syncthreads(); }
-    for (int iy = threadIdx.x; iy < my; iy += kThreads) {
+    gsync();
+    if (imeth == 2) { FOR_I(i, P.n) { dxi[i] = dvx[i]; dyi[i] = dvy[i]; } gsync(); }
+    FOR_I(iy, my) {
         const int i0 = iy * mx;
         int ii = (mx - 1) + i0;
         vx[ii] = zero; vy[ii] = zero;
@@ -1316,14 +1316,14 @@ __device__ __noinline__ void gd_project_searchdir(const PView &P, const GdCols<S
             }
         }
     }
-    __syncthreads();
+    gsync();
 }
 
 // compute_diagscaling on state S with element arithmetic in R
 template <typename S, typename R>
 __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, const double coefs_d[2][2]) {
     const PatchDesc &d = *P.d;
-    __syncthreads();
+    gsync();
     PHASE_START(tdg);
     const int mx = P.mx, n = P.n;
     const int *igs = P.igs();
@@ -1346,7 +1346,7 @@ __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, 
         }
     }
     ndeg = block_sumi1(P.sm->red, ndeg);
-    if (ndeg > 0 && threadIdx.x == 0) {
+    if (ndeg > 0 && glead()) {
         // serial pass with the reference's carry-over of elnew and fac_s (elements in order)
         int elnew = Exter;
         R fac_s = R(0);
@@ -1364,7 +1364,7 @@ __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, 
             else dscl[ii] = S(0);
         }
     }
-    __syncthreads();
+    gsync();
     PHASE_END(P, O_T_DIAG - O_T_TOTAL, tdg);
 }
 
@@ -1397,7 +1397,7 @@ __device__ __noinline__ void gd_slip(const PView &P, const GdCols<S> &C, GdCtx &
         FOR_I(i, n) { C.sx[i] = 0.0f; C.sy[i] = 0.0f; }
         prod_t<float, float>(*X.o32, C.dpx, C.dpy, C.sx, C.sy, OUT_INT, igs); X.nconv32++;
         FOR_I(i, n) if (igs[i] >= Adhes) { C.sx[i] += C.wsx[i]; C.sy[i] += C.wsy[i]; }
-        __syncthreads();
+        gsync();
     }
 }
 
@@ -1564,7 +1564,7 @@ __device__ __noinline__ void gd_start(const PView &P, const GdCols<S> &C, GdCtx 
             else { C.dpx[ii] = C.px[ii] - C.px[ii + 1]; C.dpy[ii] = C.py[ii] - C.py[ii + 1]; }
         }
     }
-    __syncthreads();
+    gsync();
     gd_set_nt<S>(P, C);
     gd_slip<S>(P, C, X);
     gd_scaling<S>(P, C, X);
@@ -1618,7 +1618,7 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
             C32.pn[i] = (float)C64.pn[i]; C32.px[i] = (float)C64.px[i]; C32.py[i] = (float)C64.py[i];
             C32.wsx[i] = (float)C64.wsx[i]; C32.wsy[i] = (float)C64.wsy[i];
         }
-        __syncthreads();
+        gsync();
         gd_start<float>(P, C32, X, g, true);
         ok = gd_iterate<float>(P, C32, X, g, fmax(eps, kGdSwitchEps), maxgd);
         // continue on the FP64 state: same iteration counters, step lengths and scaling
@@ -1626,7 +1626,7 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
             C64.px[i] = C32.px[i]; C64.py[i] = C32.py[i]; C64.dpx[i] = C32.dpx[i]; C64.dpy[i] = C32.dpy[i];
             C64.dscl[i] = C32.dscl[i];
         }
-        __syncthreads();
+        gsync();
         X.tier = 2;
         if (ok) {
             gd_start<double>(P, C64, X, g, false);
@@ -1698,10 +1698,10 @@ __device__ __noinline__ int tangcg(const PView &P, const Ops<T> &op, const T *Mx
             }
             rx[i] = r0; ry[i] = r1;
         }
-        __syncthreads();
+        gsync();
     };
     FOR_I(i, n) if (igs[i] >= Adhes) { sx[i] += wsx[i]; sy[i] += wsy[i]; }
-    __syncthreads();
+    gsync();
     set_r();
     while ((lchanged || dif > difid) && itcg < maxcg) {
         itcg++; it_inn++;
@@ -1730,7 +1730,7 @@ __device__ __noinline__ int tangcg(const PView &P, const Ops<T> &op, const T *Mx
             }
             zx[i] = z0; zy[i] = z1;
         }
-        __syncthreads();
+        gsync();
         if (itcg <= 1 || lchanged) {
             FOR_I(i, n) { vx[i] = zx[i]; vy[i] = zy[i]; }
         } else {
@@ -1742,7 +1742,7 @@ __device__ __noinline__ int tangcg(const PView &P, const Ops<T> &op, const T *Mx
             else beta = -zq / vq;
             FOR_I(i, n) { vx[i] = beta * vx[i] + zx[i]; vy[i] = beta * vy[i] + zy[i]; }
         }
-        __syncthreads();
+        gsync();
         prod_t<T>(op, vx, vy, qx, qy, OUT_INT, igs); nconv++;
         FOR_I(i, n) if (igs[i] == Slip) {
             const double tx = -ny[i], ty = nx[i];
@@ -1808,7 +1808,7 @@ __device__ __noinline__ int tangcg(const PView &P, const Ops<T> &op, const T *Mx
         }
         if ((lchanged || dif > difid) && itcg < maxcg) {
             if (it_inn <= 0) { set_nt(P); set_r(); }
-            else { FOR_I(i, n) if (igs[i] >= Adhes) { rx[i] -= alpha * qx[i]; ry[i] -= alpha * qy[i]; } __syncthreads(); }
+            else { FOR_I(i, n) if (igs[i] >= Adhes) { rx[i] -= alpha * qx[i]; ry[i] -= alpha * qy[i]; } gsync(); }
         }
     }
     err = dif;

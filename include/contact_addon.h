@@ -14,6 +14,7 @@
  *   cntc_gb300_getsolverstats   convolution counts and per-phase cycle counts of the last solve
  *   cntc_gb300_resident_*       solve a staged batch repeatedly on device-resident inputs
  *   flag CNTC_if_mixedprec      (cntc_setflags) 1: FP32 convolutions + FP64 refinement
+ *   flag CNTC_if_groupctas      (cntc_setflags) CTAs per patch: one, or a cooperative group
  */
 #ifndef CONTACT_GB300_ADDON_H
 #define CONTACT_GB300_ADDON_H
@@ -28,6 +29,13 @@ extern "C" {
  * 4 = GDsteady on an FP32 state until single precision stops resolving the change, then the
  * same iteration continued on the FP64 state with tier-2 arithmetic */
 #define CNTC_if_mixedprec 2010
+
+/* library extension flag for cntc_setflags: CTAs that solve one patch together.  0 (default):
+ * one CTA per patch when the grid's FFT lines fit the per-warp shared-memory buffers (grid
+ * sides up to about 210), else a cooperative group of up to one CTA per 256 elements, bounded
+ * by the CTAs the device holds at once; 1: one CTA only (larger grids return CNTC_err_other);
+ * n >= 2: a group of at most n CTAs for any grid */
+#define CNTC_if_groupctas 2011
 
 /* initialisation: cntc_initializeFirst 235-442, cntc_initializeFirst_new 446-472,
  * cntc_initialize 476-576 */
@@ -136,7 +144,8 @@ long long cntc_gb300_kernel_launches(void);
  * [1] FP64 convolutions, [2] line-search steps, [3] status bits, [4..12] SM clock cycles
  * spent in: whole solve, convolutions, line search, diagonal scaling, Gauss-Seidel sweeps,
  * normal problem, tangential problem, row scans, FP32 convolutions; [13] algorithmic bytes
- * of the convolutions; [14], [15] GPU global timer (ns) at the start and end of the solve */
+ * of the convolutions; [14], [15] GPU global timer (ns) at the start and end of the solve;
+ * [16] CTAs that solved the patch */
 void cntc_gb300_getsolverstats(int *ire, int *icp, int *lenarr, double *values);
 
 /* extension (no reference counterpart): resident batch for throughput measurement.
