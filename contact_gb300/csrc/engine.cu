@@ -415,7 +415,7 @@ __device__ __noinline__ void compute_facdt(const PView &P, int solver, double *f
     const bool is_roll = d.tang == 2 || d.tang == 3;
     const double fxdfac = (solver == 4) ? 2.0 : 1.0;
     gsync();
-    FOR_I(iy, my) {
+    FOR_ROW(iy, my) {
         const int i0 = iy * mx;
         int ixb = mx;
         for (int ix = mx; ix >= 1; ix--) {
@@ -453,7 +453,7 @@ __device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const O
     count_eldiv(P, nadh, nslip, nplast, nexter);
     const int k = nadh + nslip + nplast;
     int icount = 0;
-    FOR_I(iy, my) if (igs[iy * mx] >= Adhes) icount++;
+    FOR_ROW(iy, my) if (igs[iy * mx] >= Adhes) icount++;
     icount = block_sumi1(red, icount);
     int solver;
     if (is_ssrol) solver = (d.gausei == 5) ? 7 : (d.gausei != 2 ? 4 : 3);

@@ -21,7 +21,7 @@ enum WsCol {
     W_FST = W_FLS + 9,                                       // 14 columns: 28 float columns of the FP32 GD state
     W_NCOL = W_FST + 14
 };
-enum WsIntCol { I_IGS = 0, I_OLD, I_EXT, I_IEL, I_NCOL };
+enum WsIntCol { I_IGS = 0, I_OLD, I_EXT, I_IEL, I_JX, I_NCOL };
 
 // output scalars
 enum OutScalar {

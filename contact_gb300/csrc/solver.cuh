@@ -52,8 +52,12 @@ struct PView {
     __device__ float *f(int k) const { return (float *)c(W_FLS) + (size_t)k * n; }
 };
 
-// strided loop of the patch group over n items (elements or rows)
+// strided loop of the patch group over n elements
 #define FOR_I(i, n) for (int i = gtid(); i < (n); i += gstride())
+// loop of the patch group over the rows of the grid, one row per thread.  Rows go round the
+// CTAs first (row iy to CTA iy mod nblk), so that the sequential row scans of a patch group
+// spread over all its SMs; for one CTA this is the plain thread-strided loop.
+#define FOR_ROW(iy, my) for (int iy = g_grp.rank + (int)threadIdx.x * g_grp.nblk; iy < (my); iy += gstride())
 
 // ------------------------------------------------------------------------------------------
 // small helpers
@@ -90,7 +94,7 @@ __device__ __noinline__ void areas(const PView &P) {
     const int *igs = P.igs();
     int *ext = P.ci(I_EXT);
     gsync();
-    FOR_I(iy, my) {
+    FOR_ROW(iy, my) {
         const int i0 = iy * mx;
         int first = 1;
         while (igs[(first - 1) + i0] <= Exter && first != mx) first++;
@@ -672,100 +676,87 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
 // GDsteady helpers (gdsteady.f90:610-1462); rows are scanned from the leading edge (ix = mx)
 // towards the trailing edge, one thread per row.
 // ------------------------------------------------------------------------------------------
+// The row scans below are sequential along x; their loads do not depend on the scan, so
+// each thread loads the next kScanBatch elements of its row while it runs the recurrence over
+// the current ones (two register buffers): the memory latency overlaps the dependent
+// arithmetic instead of adding to it.  The arithmetic is the same, element by element, as a
+// plain loop.
 template <typename R>
-__device__ __noinline__ void apply_trcbnd(const PView &P, const R *trc, R *dpx, R *dpy, R *px, R *py) {
-    const int mx = P.mx, my = P.my;
-    const int *igs = P.igs();
-    gsync();
-    PHASE_START(tsc);
-    const R zero = R(0);
-    FOR_I(iy, my) {
-        int ii = (mx - 1) + iy * mx;
-        px[ii] = zero; py[ii] = zero;
-        R pxn = zero, pyn = zero;
-        for (int ix = mx - 2; ix >= 0; ix--) {
-            ii = ix + iy * mx;
-            R qx, qy;
-            if (igs[ii] <= Exter) { qx = zero; qy = zero; }
-            else {
-                qx = pxn + dpx[ii]; qy = pyn + dpy[ii];
-                const R qq = qx * qx + qy * qy, tb = trc[ii];
-                if (igs[ii] == Slip || qq >= tb * tb) { const R f = tb * inv_sqrt(qq); qx *= f; qy *= f; }
+struct ScanBatch { static constexpr int U = sizeof(R) == 8 ? 4 : 8; };
+
+// inputs of the traction-bound scan for elements ixb, ixb-1, ..., ixb-U+1 of row i0: element
+// type, increment (dp, or dp + alpha dv in the line search) and bound; zeros past the row start
+template <typename R, int U>
+struct ScanIn {
+    int el[U];
+    R ax[U], ay[U], tb[U];
+    __device__ __forceinline__ void load(int ixb, int i0, const int *igs, const R *dpx, const R *dpy, const R *dvx,
+                                         const R *dvy, R aj, const R *trc) {
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int ii = ixb - u + i0;
+            el[u] = Exter; ax[u] = ay[u] = tb[u] = R(0);
+            if (ixb - u >= 0) {
+                el[u] = igs[ii];
+                if (dvx) { ax[u] = dpx[ii] + aj * dvx[ii]; ay[u] = dpy[ii] + aj * dvy[ii]; }
+                else { ax[u] = dpx[ii]; ay[u] = dpy[ii]; }
+                tb[u] = trc[ii];
             }
-            px[ii] = qx; py[ii] = qy;
-            dpx[ii] = qx - pxn; dpy[ii] = qy - pyn;
-            pxn = qx; pyn = qy;
         }
     }
-    gsync();
-    PHASE_END(P, O_T_SCAN - O_T_TOTAL, tsc);
+};
+
+// one traction-bound step: q = p(ix+1) + increment, clipped to the bound in slip elements
+// and where |q| reaches it (apply_trcbnd, gdsteady.f90:807-847)
+template <typename R>
+__device__ __forceinline__ void trcbnd_step(int el, R ax, R ay, R tb, R pxn, R pyn, R &qx, R &qy) {
+    qx = R(0); qy = R(0);
+    if (el > Exter) {
+        qx = pxn + ax; qy = pyn + ay;
+        const R qq = qx * qx + qy * qy;
+        if (el == Slip || qq >= tb * tb) { const R f = tb * inv_sqrt(qq); qx *= f; qy *= f; }
+    }
 }
 
-// project_searchdir, gdsteady.f90:639-803 (variants E_trl, E_down(k), E_keep(f))
-__device__ __noinline__ void project_searchdir(const PView &P, int imeth, int kdown, const double *trc) {
-    const PatchDesc &d = *P.d;
+// traction-bound scan of every row of the group: p from the increments, written to (ox, oy);
+// with wdpx/wdpy the clipped increments dp = q - p(ix+1) are written there (they may be the
+// input increments: an element is read one batch before it is written)
+template <typename R>
+__device__ __forceinline__ void trcbnd_rows(const PView &P, const R *trc, const R *dpx, const R *dpy, const R *dvx,
+                                            const R *dvy, R aj, R *ox, R *oy, R *wdpx, R *wdpy) {
     const int mx = P.mx, my = P.my;
     const int *igs = P.igs();
-    double *dvx = P.c(W_DVX), *dvy = P.c(W_DVY), *vx = P.c(W_VX), *vy = P.c(W_VY);
-    const double *nx = P.c(W_NX), *ny = P.c(W_NY);
-    double *dxi = P.c(W_ZX), *dyi = P.c(W_ZY);   // copies of the input search direction (E_down)
-    const double fac_v = 1000.0;
-    gsync();
-    if (imeth == 2) { FOR_I(i, P.n) { dxi[i] = dvx[i]; dyi[i] = dvy[i]; } gsync(); }
-    FOR_I(iy, my) {
+    constexpr int U = ScanBatch<R>::U;
+    FOR_ROW(iy, my) {
         const int i0 = iy * mx;
-        int ii = (mx - 1) + i0;
-        vx[ii] = 0.0; vy[ii] = 0.0;
-        for (int ix = mx - 2; ix >= 0; ix--) {
-            ii = ix + i0;
-            const double tx = -ny[ii], ty = nx[ii];
-            if (imeth == 1) {
-                if (igs[ii] == Adhes) { vx[ii] = vx[ii + 1] + dvx[ii]; vy[ii] = vy[ii + 1] + dvy[ii]; }
-                else if (igs[ii] == Slip) {
-                    double vt = tx * dvx[ii] + ty * dvy[ii];
-                    vt = dsign(1.0, vt) * fmin(fabs(vt), fac_v * trc[ii]);
-                    vx[ii] = tx * vt; vy[ii] = ty * vt;
-                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
-                } else {
-                    vx[ii] = 0.0; vy[ii] = 0.0;
-                    dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
-                }
-            } else if (imeth == 2) {
-                if (igs[ii] == Adhes) {
-                    if (ix + 1 + kdown <= mx) {
-                        vx[ii] = vx[ii + 1] + dxi[ii] - dxi[ii + kdown];
-                        vy[ii] = vy[ii + 1] + dyi[ii] - dyi[ii + kdown];
-                    } else { vx[ii] = vx[ii + 1] + dxi[ii]; vy[ii] = vy[ii + 1] + dyi[ii]; }
-                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
-                } else {
-                    if (igs[ii] == Slip) {
-                        double vt = tx * dxi[ii] + ty * dyi[ii];
-                        vt = dsign(1.0, vt) * fmin(fabs(vt), fac_v * trc[ii]);
-                        vx[ii] = tx * vt; vy[ii] = ty * vt;
-                        dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
-                    } else {
-                        vx[ii] = 0.0; vy[ii] = 0.0;
-                        dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
-                    }
-                    for (int kk = 1; kk <= kdown; kk++) if (ix + 1 + kk <= mx) { dxi[ii + kk] = 0.0; dyi[ii + kk] = 0.0; }
-                }
-            } else {
-                if (igs[ii] == Adhes) {
-                    vx[ii] = d.fdecay * vx[ii + 1] + dvx[ii]; vy[ii] = d.fdecay * vy[ii + 1] + dvy[ii];
-                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
-                } else if (igs[ii] == Slip) {
-                    double vt = tx * dvx[ii] + ty * dvy[ii];
-                    vt = dsign(1.0, vt) * fmin(fabs(vt), fac_v * trc[ii]);
-                    vx[ii] = tx * vt; vy[ii] = ty * vt;
-                    dvx[ii] = vx[ii] - vx[ii + 1]; dvy[ii] = vy[ii] - vy[ii + 1];
-                } else {
-                    vx[ii] = 0.0; vy[ii] = 0.0;
-                    dvx[ii] = -vx[ii + 1]; dvy[ii] = -vy[ii + 1];
-                }
+        ox[(mx - 1) + i0] = R(0); oy[(mx - 1) + i0] = R(0);
+        R pxn = R(0), pyn = R(0);
+        ScanIn<R, U> cur, nxt;
+        cur.load(mx - 2, i0, igs, dpx, dpy, dvx, dvy, aj, trc);
+        for (int ixb = mx - 2; ixb >= 0; ixb -= U) {
+            nxt.load(ixb - U, i0, igs, dpx, dpy, dvx, dvy, aj, trc);
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (ixb - u < 0) break;
+                const int ii = ixb - u + i0;
+                R qx, qy;
+                trcbnd_step<R>(cur.el[u], cur.ax[u], cur.ay[u], cur.tb[u], pxn, pyn, qx, qy);
+                ox[ii] = qx; oy[ii] = qy;
+                if (wdpx) { wdpx[ii] = qx - pxn; wdpy[ii] = qy - pyn; }
+                pxn = qx; pyn = qy;
             }
+            cur = nxt;
         }
     }
+}
+
+template <typename R>
+__device__ __noinline__ void apply_trcbnd(const PView &P, const R *trc, R *dpx, R *dpy, R *px, R *py) {
     gsync();
+    PHASE_START(tsc);
+    trcbnd_rows<R>(P, trc, dpx, dpy, nullptr, nullptr, R(0), px, py, dpx, dpy);
+    gsync();
+    PHASE_END(P, O_T_SCAN - O_T_TOTAL, tsc);
 }
 
 // compute_diagscaling, gdsteady.f90:901-1042.  In the reference 'elnew' and 'fac_s' carry over
@@ -774,11 +765,10 @@ __device__ __noinline__ void project_searchdir(const PView &P, int imeth, int kd
 // elements whose angle error stays below tiny_err after the perturbation.  All other
 // elements are independent and are handled in parallel; when a case (b) element exists the
 // whole pass is repeated serially with the reference's carry-over.
+// jx: the last element at or behind ix (towards the trailing edge, 1-based) that is not in
+// adhesion, or 1 (the reference's backward search from ix); see trailing_nonadh
 template <typename R>
-__device__ inline R dscl_adhesion(const PatchDesc &d, const int *igs, int ii, int mx, R old) {
-    const int ix = ii % mx + 1;
-    int jx = ix;
-    while (jx > 1 && igs[ii - ix + jx] == Adhes) jx--;
+__device__ inline R dscl_adhesion(const PatchDesc &d, int ix, int jx, R old) {
     const R d_cns = (R)d.d_cns, d_ifc = (R)d.d_ifc, d_lin = (R)d.d_lin;
     R dn;
     if (d_cns < d_ifc) dn = fmax(d_cns, d_ifc + R(ix - jx - 1) * fmin(R(0), d_lin));
@@ -816,57 +806,6 @@ __device__ inline bool slip_element(const PatchDesc &d, const R coefs[2][2], R p
         fac_s = fabs(upd_s) / fabs(err_0);
     }
     return true;
-}
-
-// R = float (mixed precision): the scaling is a preconditioner of the search direction, so
-// single precision changes the iteration path only at rounding level of the direction
-template <typename R>
-__device__ __noinline__ void compute_diagscaling(const PView &P, const double coefs_d[2][2]) {
-    const PatchDesc &d = *P.d;
-    gsync();
-    PHASE_START(tdg);
-    const int mx = P.mx, n = P.n;
-    const int *igs = P.igs();
-    const double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN), *sx = P.c(W_SX), *sy = P.c(W_SY);
-    double *dscl = P.c(W_DSCL);
-    R coefs[2][2] = {{(R)coefs_d[0][0], (R)coefs_d[0][1]}, {(R)coefs_d[1][0], (R)coefs_d[1][1]}};
-    const R d_slp = (R)d.d_slp, pow_s = (R)d.pow_s;
-    int ndeg = 0;
-    FOR_I(ii, n) {
-        const int el = igs[ii];
-        if (el == Slip) {
-            int elnew = Slip;
-            R fac_s = R(0);
-            if (!slip_element<R>(d, coefs, (R)px[ii], (R)py[ii], (R)pn[ii], (R)sx[ii], (R)sy[ii], elnew, fac_s)) ndeg++;
-            else if (elnew == Slip) dscl[ii] = (double)(d_slp * pow(fac_s, pow_s));
-            else dscl[ii] = (double)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
-        } else if (el == Adhes) {
-            dscl[ii] = (double)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
-        } else {
-            dscl[ii] = 0.0;
-        }
-    }
-    ndeg = block_sumi1(P.sm->red, ndeg);
-    if (ndeg > 0 && glead()) {
-        // serial pass with the reference's carry-over of elnew and fac_s (elements in order)
-        int elnew = Exter;
-        R fac_s = R(0);
-        for (int ii = 0; ii < n; ii++) {
-            const int el = igs[ii];
-            if (el == Slip) {
-                int e2 = el;
-                R f2 = fac_s;
-                if (slip_element<R>(d, coefs, (R)px[ii], (R)py[ii], (R)pn[ii], (R)sx[ii], (R)sy[ii], e2, f2)) {
-                    elnew = e2; fac_s = f2;
-                }
-            }
-            if (el == Slip && elnew == Slip) dscl[ii] = (double)(d_slp * pow(fac_s, pow_s));
-            else if (el == Adhes || elnew == Adhes) dscl[ii] = (double)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
-            else dscl[ii] = 0.0;
-        }
-    }
-    gsync();
-    PHASE_END(P, O_T_DIAG - O_T_TOTAL, tdg);
 }
 
 // arrays read and written by the line search, in its working precision
@@ -927,31 +866,13 @@ __device__ __noinline__ bool perform_linesearch(const PView &P, const LsArrays<R
         }
         block_sum<3>(red, qa);
     }
-    const int mx = P.mx, my = P.my;
     for (int guard = 0; guard < kMaxLs + 1; guard++) {
         const double alpha_j = S.alpha_j;
         const R aj = (R)alpha_j;
         // trial tractions: the traction-bound scan of dp + alpha dv along each row (apply_trcbnd)
         {
             PHASE_START(tsc);
-            FOR_I(iy, my) {
-                int ii = (mx - 1) + iy * mx;
-                A.pnx[ii] = R(0); A.pny[ii] = R(0);
-                R pxn = R(0), pyn = R(0);
-                for (int ix = mx - 2; ix >= 0; ix--) {
-                    ii = ix + iy * mx;
-                    const int el = igs[ii];
-                    R qx = R(0), qy = R(0);
-                    if (el > Exter) {
-                        qx = pxn + (A.dpx[ii] + aj * A.dvx[ii]);
-                        qy = pyn + (A.dpy[ii] + aj * A.dvy[ii]);
-                        const R qq = qx * qx + qy * qy, tb = A.trc[ii];
-                        if (el == Slip || qq >= tb * tb) { const R f = tb * inv_sqrt(qq); qx *= f; qy *= f; }
-                    }
-                    A.pnx[ii] = qx; A.pny[ii] = qy;
-                    pxn = qx; pyn = qy;
-                }
-            }
+            trcbnd_rows<R>(P, A.trc, A.dpx, A.dpy, A.dvx, A.dvy, aj, A.pnx, A.pny, nullptr, nullptr);
             gsync();
             PHASE_END(P, O_T_SCAN - O_T_TOTAL, tsc);
         }
@@ -1166,21 +1087,6 @@ __device__ __noinline__ void set_nt(const PView &P) {
     gsync();
 }
 
-__device__ __noinline__ void set_residual(const PView &P) {
-    const int *igs = P.igs();
-    const double *sx = P.c(W_SX), *sy = P.c(W_SY), *nx = P.c(W_NX), *ny = P.c(W_NY), *dscl = P.c(W_DSCL);
-    double *rx = P.c(W_RX), *ry = P.c(W_RY);
-    FOR_I(i, P.n) {
-        if (igs[i] == Adhes) { rx[i] = -sx[i] * dscl[i]; ry[i] = -sy[i] * dscl[i]; }
-        else if (igs[i] == Slip) {
-            const double tx = -ny[i], ty = nx[i];
-            double st = tx * sx[i] + ty * sy[i];
-            rx[i] = -st * tx * dscl[i]; ry[i] = -st * ty * dscl[i];
-        } else { rx[i] = 0.0; ry[i] = 0.0; }
-    }
-    gsync();
-}
-
 // ------------------------------------------------------------------------------------------
 // GDsteady state in a storage precision S: the FP64 work columns, or FP32 columns for the
 // single-precision part of mixed tier 4
@@ -1266,10 +1172,51 @@ __device__ __noinline__ void gd_project_searchdir(const PView &P, const GdCols<S
     auto clampv = [&](S vt, S tb) { return (vt >= zero ? S(1) : S(-1)) * fmin(fabs(vt), fac_v * tb); };
     gsync();
     if (imeth == 2) { FOR_I(i, P.n) { dxi[i] = dvx[i]; dyi[i] = dvy[i]; } gsync(); }
-    FOR_I(iy, my) {
+    constexpr int U = ScanBatch<S>::U;
+    FOR_ROW(iy, my) {
         const int i0 = iy * mx;
         int ii = (mx - 1) + i0;
         vx[ii] = zero; vy[ii] = zero;
+        if (imeth != 2) {
+            // E_trl (1) and E_keep (3): batched loads, the previous v carried in registers
+            S vxn = zero, vyn = zero;
+            for (int ixb = mx - 2; ixb >= 0; ixb -= U) {
+                int el[U];
+                S ex[U], ey[U], tx[U], ty[U], tb[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    const int jj = ixb - u + i0;
+                    el[u] = Exter; ex[u] = ey[u] = tx[u] = ty[u] = tb[u] = zero;
+                    if (ixb - u >= 0) {
+                        el[u] = igs[jj]; ex[u] = dvx[jj]; ey[u] = dvy[jj];
+                        tx[u] = -ny[jj]; ty[u] = nx[jj]; tb[u] = trc[jj];
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; u++) {
+                    if (ixb - u < 0) break;
+                    const int jj = ixb - u + i0;
+                    S wx, wy;
+                    if (el[u] == Adhes) {
+                        if (imeth == 1) { wx = vxn + ex[u]; wy = vyn + ey[u]; }
+                        else {
+                            wx = fdecay * vxn + ex[u]; wy = fdecay * vyn + ey[u];
+                            dvx[jj] = wx - vxn; dvy[jj] = wy - vyn;
+                        }
+                    } else if (el[u] == Slip) {
+                        const S vt = clampv(tx[u] * ex[u] + ty[u] * ey[u], tb[u]);
+                        wx = tx[u] * vt; wy = ty[u] * vt;
+                        dvx[jj] = wx - vxn; dvy[jj] = wy - vyn;
+                    } else {
+                        wx = zero; wy = zero;
+                        dvx[jj] = -vxn; dvy[jj] = -vyn;
+                    }
+                    vx[jj] = wx; vy[jj] = wy;
+                    vxn = wx; vyn = wy;
+                }
+            }
+            continue;
+        }
         for (int ix = mx - 2; ix >= 0; ix--) {
             ii = ix + i0;
             const S tx = -ny[ii], ty = nx[ii];
@@ -1319,7 +1266,26 @@ __device__ __noinline__ void gd_project_searchdir(const PView &P, const GdCols<S
     gsync();
 }
 
-// compute_diagscaling on state S with element arithmetic in R
+// compute_diagscaling on state S with element arithmetic in R.  R = float (mixed precision):
+// the scaling is a preconditioner of the search direction, so single precision changes the
+// iteration path only at rounding level of the direction
+// for every element, the 1-based column of the last element at or behind it in its row that
+// is not in adhesion (1 when there is none): one pass per row in place of a backward search
+// per element
+__device__ inline void trailing_nonadh(const PView &P, int *jxc) {
+    const int mx = P.mx, my = P.my;
+    const int *igs = P.igs();
+    FOR_ROW(iy, my) {
+        const int i0 = iy * mx;
+        int last = 1;
+        for (int ix = 1; ix <= mx; ix++) {
+            if (igs[i0 + ix - 1] != Adhes) last = ix;
+            jxc[i0 + ix - 1] = last;
+        }
+    }
+    gsync();
+}
+
 template <typename S, typename R>
 __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, const double coefs_d[2][2]) {
     const PatchDesc &d = *P.d;
@@ -1328,6 +1294,8 @@ __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, 
     const int mx = P.mx, n = P.n;
     const int *igs = P.igs();
     S *dscl = C.dscl;
+    int *jxc = P.ci(I_JX);
+    trailing_nonadh(P, jxc);
     R coefs[2][2] = {{(R)coefs_d[0][0], (R)coefs_d[0][1]}, {(R)coefs_d[1][0], (R)coefs_d[1][1]}};
     const R d_slp = (R)d.d_slp, pow_s = (R)d.pow_s;
     int ndeg = 0;
@@ -1338,9 +1306,9 @@ __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, 
             R fac_s = R(0);
             if (!slip_element<R>(d, coefs, (R)C.px[ii], (R)C.py[ii], (R)C.pn[ii], (R)C.sx[ii], (R)C.sy[ii], elnew, fac_s)) ndeg++;
             else if (elnew == Slip) dscl[ii] = (S)(d_slp * pow(fac_s, pow_s));
-            else dscl[ii] = (S)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
+            else dscl[ii] = (S)dscl_adhesion<R>(d, ii % mx + 1, jxc[ii], (R)dscl[ii]);
         } else if (el == Adhes) {
-            dscl[ii] = (S)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
+            dscl[ii] = (S)dscl_adhesion<R>(d, ii % mx + 1, jxc[ii], (R)dscl[ii]);
         } else {
             dscl[ii] = S(0);
         }
@@ -1360,7 +1328,7 @@ __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, 
                 }
             }
             if (el == Slip && elnew == Slip) dscl[ii] = (S)(d_slp * pow(fac_s, pow_s));
-            else if (el == Adhes || elnew == Adhes) dscl[ii] = (S)dscl_adhesion<R>(d, igs, ii, mx, (R)dscl[ii]);
+            else if (el == Adhes || elnew == Adhes) dscl[ii] = (S)dscl_adhesion<R>(d, ii % mx + 1, jxc[ii], (R)dscl[ii]);
             else dscl[ii] = S(0);
         }
     }

@@ -91,17 +91,25 @@ def rough_surface(mx, my, xl, yl, dx, dy, pen_hz, seed, rx=460.0, ry=300.0, nsin
     return h
 
 
-def config1(m, seed=1, gausei=5, eps=1e-8, mixed=0, fn=1e5, cksi=0.002, ceta=0.001, cphi=2e-4, mu=0.3):
+def config1(m, seed=1, gausei=5, eps=1e-8, mixed=0, fn=1e5, cksi=0.002, ceta=0.001, cphi=2e-4, mu=0.3, maxgs=999):
     """Non-Hertzian grid case: square m x m grid over [-1.25a, 1.25a]^2 of the Hertz solution
-    for Rx=460, Ry=300 mm; element-wise h with seeded roughness."""
+    for Rx=460, Ry=300 mm; element-wise h with seeded roughness.  GDsteady needs more
+    iterations as the grid grows (about 300 at 128^2): large grids raise maxgs."""
     a_est = 7.2 * (fn / 1e5) ** (1.0 / 3.0)
     half = 1.25 * a_est
     dx = 2 * half / m
     pen_hz = 0.16 * (fn / 1e5) ** (2.0 / 3.0)
     h = rough_surface(m, m, -half, -half, dx, dx, pen_hz, seed)
-    return dict(tang=3, norm=1, bound=0, gausei=gausei, maxgs=999, maxin=100, maxnr=30, maxout=1, eps=eps,
+    return dict(tang=3, norm=1, bound=0, gausei=gausei, maxgs=maxgs, maxin=100, maxnr=30, maxout=1, eps=eps,
                 poiss=NU_STEEL, gg=G_STEEL, fstat=mu, veloc=10000.0, fn=fn, cksi=cksi, ceta=ceta, cphi=cphi,
                 ipotcn=1, potprm=[m, m, -half, -half, dx, dx], h=h, mixed=mixed)
+
+
+def config4(seed=4, mixed=0, maxgs=5000, eps=1e-8):
+    """Large single patch: 1024^2 rough-surface grid as config1, Fn=150 kN, creepages
+    (0.003, 0, 0.3 rad/m), mu=0.25."""
+    return config1(1024, seed=seed, fn=150e3, cksi=0.003, ceta=0.0, cphi=3e-4, mu=0.25, mixed=mixed, maxgs=maxgs,
+                   eps=eps)
 
 
 def batch_patches(n, seed=2, mixed=1, eps=1e-8):

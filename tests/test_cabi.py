@@ -66,10 +66,11 @@ def test_python_bindings_match_header():
 
 def test_flags_roundtrip(lib):
     ire, icp = 901, 1
-    cg.setflags(ire, icp, [cg.CNTC_ic_tang, cg.CNTC_ic_bound, cg.CNTC_ic_iestim, cg.CNTC_if_mixedprec],
-                [1, 2, 3, 1])
-    assert getflags(ire, icp, [cg.CNTC_ic_tang, cg.CNTC_ic_bound, cg.CNTC_ic_iestim, cg.CNTC_if_mixedprec]) == \
-        [1, 2, 3, 1]
+    flags = [cg.CNTC_ic_tang, cg.CNTC_ic_bound, cg.CNTC_ic_iestim, cg.CNTC_if_mixedprec, cg.CNTC_if_groupctas]
+    cg.setflags(ire, icp, flags, [1, 2, 3, 1, 12])
+    assert getflags(ire, icp, flags) == [1, 2, 3, 1, 12]
+    cg.setflags(ire, icp, [cg.CNTC_if_groupctas], [-4])          # negative: automatic
+    assert getflags(ire, icp, [cg.CNTC_if_groupctas]) == [0]
     cg.finalize(ire)
 
 
