@@ -91,14 +91,21 @@ struct Problem {
     std::vector<int> igs;
     std::vector<double> stats;           // engine statistics: convolution counts, status, phase cycles
     double tcpu = 0, twall = 0;
-    // device resources
-    char *d_io = nullptr, *d_work = nullptr;
-    size_t cap_io = 0, cap_work = 0;
-    PatchDesc *d_desc = nullptr;
-    int *d_list = nullptr;
+    // device cache of the influence coefficients and spectra (cntc_calculate, _batch, _async):
+    // they depend only on the grid, dx, dy and the material, and are reused while that key
+    // stays the same
     char key[128] = {0};          // geometry key of the cached influence coefficients
     bool ic_valid = false;
+    void *d_ic = nullptr;
+    size_t cap_ic = 0;
+    int ic_dev = -1;
     std::mutex busy;
+    // frees the device cache (cntc_finalize, cntc_finalizelast; not at process exit, when
+    // the CUDA runtime may already be gone and the driver reclaims the memory)
+    void release_device() {
+        if (d_ic) cudaFree(d_ic);
+        d_ic = nullptr; cap_ic = 0; ic_valid = false;
+    }
 };
 
 std::mutex g_mu;
@@ -236,7 +243,8 @@ int prepare(Problem &p, Prep &out) {
     // geometry key for reuse of influence coefficients and spectra
     char key[128];
     std::snprintf(key, sizeof(key), "%d %d %.17g %.17g %.17g %.17g", mx, my, dx, dy, ga, nu);
-    out.ic_needed = !(p.ic_valid && std::strcmp(key, p.key) == 0);
+    if (std::strcmp(key, p.key) != 0) p.ic_valid = false;    // the cache holds another geometry
+    out.ic_needed = !p.ic_valid;
     std::strcpy(p.key, key);
     // warm start needs a previous solution on the same grid
     out.upload = (d.ibase == 9);
@@ -351,10 +359,38 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
     if ((e = grow((void **)&A.h_io, A.cap_hio, tot_io, true)) != cudaSuccess) return (int)e;
     std::vector<PatchDesc> hd(n);
     std::vector<unsigned char> need_ic(n, 1);
+    std::vector<int> ic_fill;     // patches whose coefficient cache this pass fills
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
     for (int k = 0; k < n; k++) {
         hd[k] = b.preps[live[k]].d;
         carve_patch(hd[k], A.d_io + off_io[k], A.d_work + off_work[k]);
-        (void)reuse_ic_allowed;
+        if (reuse_ic_allowed) {
+            // coefficients and spectra live in the problem's own device buffer: reused when
+            // the geometry is unchanged, computed into it otherwise (without a buffer, when
+            // the allocation fails, they are computed in the pass's work area as before)
+            Problem &p = *b.probs[live[k]];
+            const PatchSizes ps = patch_sizes(hd[k].mx, hd[k].my, hd[k].fx, hd[k].fy, hd[k].nblk);
+            const size_t icb = ps.cf + ps.spec64 + ps.spec32;
+            const bool hit = p.ic_valid && !b.preps[live[k]].ic_needed && p.d_ic && p.ic_dev == dev && p.cap_ic >= icb;
+            if (!hit) {
+                p.ic_valid = false;
+                if (p.d_ic && (p.cap_ic < icb || p.ic_dev != dev)) { cudaFree(p.d_ic); p.d_ic = nullptr; p.cap_ic = 0; }
+                if (!p.d_ic) {
+                    if (cudaMalloc(&p.d_ic, icb) == cudaSuccess) { p.cap_ic = icb; p.ic_dev = dev; }
+                    else { cudaGetLastError(); p.d_ic = nullptr; }
+                }
+                if (p.d_ic) ic_fill.push_back(k);
+            } else {
+                need_ic[k] = 0;
+            }
+            if (p.d_ic) {
+                char *c = (char *)p.d_ic;
+                hd[k].cf = (const double *)c;
+                hd[k].spec64 = (const double *)(c + ps.cf);
+                hd[k].spec32 = (const float *)(c + ps.cf + ps.spec64);
+            }
+        }
         if (b.preps[live[k]].upload)
             stage_inputs(*b.probs[live[k]], hd[k], (double *)((char *)A.h_io + off_io[k]));
     }
@@ -371,6 +407,7 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
     if ((e = cudaMemcpyAsync(A.h_io, A.d_io, tot_io, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return (int)e;
     t_d2h_bytes = (long long)tot_io;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return (int)e;
+    for (int k : ic_fill) b.probs[live[k]]->ic_valid = true;
     for (int k = 0; k < n; k++) collect(*b.probs[live[k]], hd[k], (const double *)((const char *)A.h_io + off_io[k]));
     return 0;
 }
@@ -1210,13 +1247,14 @@ void cntc_getiterationcounts(int *ire, int *icp, int *lenarr, int *values) {
 void cntc_finalize(int *ire) {
     std::lock_guard<std::mutex> lk(g_mu);
     for (auto it = g_problems.begin(); it != g_problems.end();) {
-        if (it->second->ire == *ire) it = g_problems.erase(it);
+        if (it->second->ire == *ire) { it->second->release_device(); it = g_problems.erase(it); }
         else ++it;
     }
 }
 
 void cntc_finalizelast() {
     std::lock_guard<std::mutex> lk(g_mu);
+    for (auto &kv : g_problems) kv.second->release_device();
     g_problems.clear();
     g_initialized = -1;
 }

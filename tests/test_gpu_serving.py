@@ -71,3 +71,32 @@ def test_async_refuses_duplicate_and_small_budget_completes(cntc):
         assert errs == [0, 0, 0]
     finally:
         cntc.setadmissionbudget(40.0)
+
+
+def test_coefficient_cache_reused_and_exact(cntc):
+    """Influence coefficients and spectra stay on the device per problem: a new time step
+    with other creepages and Fn on the same grid launches only the solve kernel, and its
+    result equals a fresh problem's; a new grid recomputes them."""
+    c = C.config0(gausei=5, eps=1e-8, mx=40, my=36, mixed=1)
+    cntc.setup_case(320, 1, c)
+    assert cntc.calculate(320, 1) == 0
+    step = dict(c, cksi=0.0012, ceta=-0.0004, fn=9.1e4)
+    cntc.setcreepages(320, 1, step["cksi"], step["ceta"], step["cphi"])
+    cntc.setnormalforce(320, 1, step["fn"])
+    k0 = cntc.kernel_launches()
+    assert cntc.calculate(320, 1) == 0
+    assert cntc.kernel_launches() - k0 == 1          # solve only: coefficients reused
+    cntc.setup_case(321, 1, step)
+    k0 = cntc.kernel_launches()
+    assert cntc.calculate(321, 1) == 0
+    assert cntc.kernel_launches() - k0 == 3          # influence, spectra, solve
+    _same(cntc.results(320, 1), cntc.results(321, 1))
+    # another grid on the same problem: recomputed, equal to a fresh problem
+    other = dict(step, potprm=[44, 30] + step["potprm"][2:])
+    cntc.setup_case(320, 1, other)
+    k0 = cntc.kernel_launches()
+    assert cntc.calculate(320, 1) == 0
+    assert cntc.kernel_launches() - k0 == 3
+    cntc.setup_case(322, 1, other)
+    assert cntc.calculate(322, 1) == 0
+    _same(cntc.results(320, 1), cntc.results(322, 1))
