@@ -84,6 +84,29 @@ _PROTOS = {
     "cntc_getcalculationtime": [_IP, _IP, _DP, _DP],
     "cntc_resetcalculationtime": [_IP, _IP],
     "cntc_getiterationcounts": [_IP, _IP, _IP, _IP],
+    "cntc_getparameters": [_IP, _IP, _IP, _IP, _DP],
+    "cntc_setmetadata": [_IP, _IP, _IP, _IP, _DP],
+    "cntc_getmaximumtemperature": [_IP, _IP, _DP, _DP],
+    "cntc_readinpfile": [_IP, _IP, _CP, _IP, _IP],
+    "cntc_setverticalforce": [_IP, _DP],
+    "cntc_setprofileinputfname": [_IP, _CP, _IP, _IP, _IP, _IP, _DP],
+    "cntc_setprofileinputvalues": [_IP, _IP, _DP, _IP, _IP, _IP, _DP],
+    "cntc_settrackdimensions": [_IP, _IP, _IP, _DP],
+    "cntc_setwheelsetdimensions": [_IP, _IP, _IP, _DP],
+    "cntc_setwheelsetposition": [_IP, _IP, _IP, _DP],
+    "cntc_setwheelsetvelocity": [_IP, _IP, _IP, _DP],
+    "cntc_setwheelsetflexibility": [_IP, _IP, _IP, _DP],
+    "cntc_getprofilevalues": [_IP, _IP, _IP, _IP, _IP, _DP, _IP, _DP],
+    "cntc_getprofilevalues_new": [_IP, _IP, _IP, _IP, _IP, _DP, _IP, _DP],
+    "cntc_getwheelsetposition": [_IP, _IP, _DP],
+    "cntc_getwheelsetvelocity": [_IP, _IP, _DP],
+    "cntc_getnumcontactpatches": [_IP, _IP],
+    "cntc_getcontactlocation": [_IP, _IP, _IP, _DP],
+    "cntc_getglobalforces": [_IP, _IP, _IP, _DP],
+    "subs_addblock": [_IP, _IP, _IP, _IP, _IP, _IP, _IP, _DP, _DP, _DP],
+    "subs_calculate": [_IP, _IP, _IP],
+    "subs_getblocksize": [_IP, _IP, _IP, _IP, _IP, _IP],
+    "subs_getresults": [_IP, _IP, _IP, _IP, _IP, _IP, _DP],
     "cntc_finalize": [_IP],
     "cntc_finalizelast": [],
     "cntc_gb300_kernel_launches": [],

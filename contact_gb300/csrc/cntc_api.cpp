@@ -1244,6 +1244,110 @@ void cntc_getiterationcounts(int *ire, int *icp, int *lenarr, int *values) {
     for (int i = 0; i < *lenarr && i < 6; i++) values[i] = v[i];
 }
 
+void cntc_getparameters(int *ire, int *icp, int *itask, int *lenarr, double *values) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    const int n = *lenarr;
+    auto put = [&](int k, double v) { if (k <= n) values[k - 1] = v; };
+    if (*itask == 1) {
+        put(1, p->veloc / p->s_veloc);
+        put(2, p->chi / p->s_angle);
+        put(3, (p->have ? p->r_dq : p->dq) / p->s_len);
+        put(4, 0.0); put(5, 0.0);            // spin centre offsets: not supported, zero
+        put(6, 0.0);                         // tau_c0: elastic material
+    } else if (*itask == 2) {
+        // combin_mater (m_hierarch_data.f90:1543-1553)
+        const double ga = 2.0 / (1.0 / p->gg[0] + 1.0 / p->gg[1]);
+        const double nu = ga * (p->poiss[0] / p->gg[0] + p->poiss[1] / p->gg[1]) / 2.0;
+        const double ak = (ga / 4.0) * ((1.0 - 2.0 * p->poiss[0]) / p->gg[0] - (1.0 - 2.0 * p->poiss[1]) / p->gg[1]);
+        put(1, p->gg[0] * p->s_area); put(2, p->gg[1] * p->s_area); put(3, ga * p->s_area);
+        put(4, p->poiss[0]); put(5, p->poiss[1]); put(6, nu); put(7, ak);
+        for (int k = 8; k <= 22; k++) put(k, 0.0);   // no flexibility, layer, damping or plasticity data
+    } else if (*itask == 3) {
+        put(1, 0.0);                         // Coulomb friction (L = 0)
+        put(2, 1.0); put(3, 0.0); put(4, 0.0);
+        put(5, 0.0); put(6, p->fstat); put(7, p->fkin);
+    }
+}
+
+void cntc_setmetadata(int *ire, int *icp, int *lenmta, int *params, double *values) {
+    (void)ire; (void)icp; (void)lenmta; (void)params; (void)values;   // output metadata only
+}
+
+void cntc_getmaximumtemperature(int *ire, int *icp, double *t1max, double *t2max) {
+    if (!lookup(*ire, *icp, false)) return;
+    *t1max = 0.0;
+    *t2max = 0.0;
+}
+
+// outside the solve path: wheel-rail module, input-file reader, subsurface stresses
+static void not_supported(const char *name) {
+    char msg[160];
+    std::snprintf(msg, sizeof msg, "%s: not supported by this library (module-3 solve path only)", name);
+    log_msg(msg);
+}
+static void zero(int *lenarr, double *values) { for (int i = 0; i < *lenarr; i++) values[i] = 0.0; }
+
+void cntc_readinpfile(int *, int *, const char *, int *, int *ierror) {
+    not_supported("cntc_readinpfile");
+    *ierror = CNTC_err_other;
+}
+void cntc_setverticalforce(int *, double *) { not_supported("cntc_setverticalforce"); }
+void cntc_setprofileinputfname(int *, const char *, int *, int *, int *, int *, double *) {
+    not_supported("cntc_setprofileinputfname");
+}
+void cntc_setprofileinputvalues(int *, int *, double *, int *, int *, int *, double *) {
+    not_supported("cntc_setprofileinputvalues");
+}
+void cntc_settrackdimensions(int *, int *, int *, double *) { not_supported("cntc_settrackdimensions"); }
+void cntc_setwheelsetdimensions(int *, int *, int *, double *) { not_supported("cntc_setwheelsetdimensions"); }
+void cntc_setwheelsetposition(int *, int *, int *, double *) { not_supported("cntc_setwheelsetposition"); }
+void cntc_setwheelsetvelocity(int *, int *, int *, double *) { not_supported("cntc_setwheelsetvelocity"); }
+void cntc_setwheelsetflexibility(int *, int *, int *, double *) { not_supported("cntc_setwheelsetflexibility"); }
+void cntc_getprofilevalues(int *, int *, int *, int *, int *, double *, int *lenarr, double *values) {
+    not_supported("cntc_getprofilevalues");
+    zero(lenarr, values);
+}
+void cntc_getprofilevalues_new(int *, int *, int *, int *, int *, double *, int *lenarr, double *values) {
+    not_supported("cntc_getprofilevalues_new");
+    zero(lenarr, values);
+}
+void cntc_getwheelsetposition(int *, int *lenarr, double *values) {
+    not_supported("cntc_getwheelsetposition");
+    zero(lenarr, values);
+}
+void cntc_getwheelsetvelocity(int *, int *lenarr, double *values) {
+    not_supported("cntc_getwheelsetvelocity");
+    zero(lenarr, values);
+}
+void cntc_getnumcontactpatches(int *, int *npatch) {
+    not_supported("cntc_getnumcontactpatches");
+    *npatch = 0;
+}
+void cntc_getcontactlocation(int *, int *, int *lenarr, double *values) {
+    not_supported("cntc_getcontactlocation");
+    zero(lenarr, values);
+}
+void cntc_getglobalforces(int *, int *, int *lenarr, double *values) {
+    not_supported("cntc_getglobalforces");
+    zero(lenarr, values);
+}
+void subs_addblock(int *, int *, int *, int *, int *, int *, int *, double *, double *, double *) {
+    not_supported("subs_addblock");
+}
+void subs_calculate(int *, int *, int *ierror) {
+    not_supported("subs_calculate");
+    *ierror = CNTC_err_other;
+}
+void subs_getblocksize(int *, int *, int *, int *nx, int *ny, int *nz) {
+    not_supported("subs_getblocksize");
+    *nx = 0; *ny = 0; *nz = 0;
+}
+void subs_getresults(int *, int *, int *, int *lenarr, int *ncol, int *, double *values) {
+    not_supported("subs_getresults");
+    for (int i = 0; i < *lenarr * std::max(0, *ncol); i++) values[i] = 0.0;
+}
+
 void cntc_finalize(int *ire) {
     std::lock_guard<std::mutex> lk(g_mu);
     for (auto it = g_problems.begin(); it != g_problems.end();) {

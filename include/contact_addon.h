@@ -134,6 +134,55 @@ void cntc_resetcalculationtime(int *ire, int *icp);
 /* extension: [itnorm, ittang, itcg, itgs, solver id, ierror] of the last solve */
 void cntc_getiterationcounts(int *ire, int *icp, int *lenarr, int *values);
 
+/* module 3 parameters: cntc_getParameters 4164-4258 (itask 1 kinematics, 2 material,
+ * 3 friction; values in the selected units) */
+void cntc_getparameters(int *ire, int *icp, int *itask, int *lenarr, double *values);
+/* metadata for output files only: cntc_setMetadata 1055-1124 (accepted, no effect on a solve) */
+void cntc_setmetadata(int *ire, int *icp, int *lenmta, int *params, double *values);
+/* temperature (not computed here, heat digit 0): cntc_getMaximumTemperature 5630-5668;
+ * returns 0, 0 as the reference does without a temperature solution */
+void cntc_getmaximumtemperature(int *ire, int *icp, double *t1max, double *t2max);
+
+/* Entry points of the wheel-rail module (module 1), the input-file reader and subsurface
+ * stresses.  They lie outside this library's solve path; they are exported so that hosts
+ * binding the reference's full interface load this library unchanged.  Each logs that it is
+ * not supported and returns: setters without effect, getters with zero outputs, and
+ * ierror = CNTC_err_other where the call has one.  Fortran implementations:
+ * cntc_readInpFile 729-776, cntc_setVerticalForce 2261-2290, cntc_setProfileInputFname
+ * 2654-2749, cntc_setProfileInputValues 2753-2829, cntc_setTrackDimensions 2833-2985,
+ * cntc_setWheelsetDimensions 2989-3063, cntc_setWheelsetPosition 3067-3132,
+ * cntc_setWheelsetVelocity 3136-3214, cntc_setWheelsetFlexibility 3218-3326,
+ * cntc_getProfileValues 4262-4693, cntc_getProfileValues_new 4697-4718,
+ * cntc_getWheelsetPosition 4722-4752, cntc_getWheelsetVelocity 4756-4786,
+ * cntc_getNumContactPatches 4790-4812, cntc_getContactLocation 4816-4983,
+ * cntc_getGlobalForces 5322-5456, subs_addBlock 3330-3515, subs_calculate 3904-3997,
+ * subs_getBlocksize 6071-6109, subs_getResults 6113-6187 */
+void cntc_readinpfile(int *ire, int *inp_type, const char *c_fname, int *len_fname, int *ierror);
+void cntc_setverticalforce(int *ire, double *fz);
+void cntc_setprofileinputfname(int *ire, const char *c_fname, int *len_fname, int *nints, int *iparam,
+                               int *nreals, double *rparam);
+void cntc_setprofileinputvalues(int *ire, int *npoint, double *values, int *nints, int *iparam, int *nreals,
+                                double *rparam);
+void cntc_settrackdimensions(int *ire, int *ztrack, int *nparam, double *rparam);
+void cntc_setwheelsetdimensions(int *ire, int *ewheel, int *nparam, double *rparam);
+void cntc_setwheelsetposition(int *ire, int *ewheel, int *nparam, double *rparam);
+void cntc_setwheelsetvelocity(int *ire, int *ewheel, int *nparam, double *rparam);
+void cntc_setwheelsetflexibility(int *ire, int *ewheel, int *nparam, double *rparam);
+void cntc_getprofilevalues(int *ire, int *itask, int *nints, int *iparam, int *nreals, double *rparam, int *lenarr,
+                           double *values);
+void cntc_getprofilevalues_new(int *ire, int *itask, int *nints, int *iparam, int *nreals, double *rparam,
+                               int *lenarr, double *values);
+void cntc_getwheelsetposition(int *ire, int *lenarr, double *values);
+void cntc_getwheelsetvelocity(int *ire, int *lenarr, double *values);
+void cntc_getnumcontactpatches(int *ire, int *npatch);
+void cntc_getcontactlocation(int *ire, int *icp, int *lenarr, double *values);
+void cntc_getglobalforces(int *ire, int *icp, int *lenarr, double *values);
+void subs_addblock(int *ire, int *icp, int *iblk, int *isubs, int *nx, int *ny, int *nz, double *xparam,
+                   double *yparam, double *zparam);
+void subs_calculate(int *ire, int *icp, int *ierror);
+void subs_getblocksize(int *ire, int *icp, int *iblk, int *nx, int *ny, int *nz);
+void subs_getresults(int *ire, int *icp, int *iblk, int *lenarr, int *ncol, int *icol, double *values);
+
 /* clean-up: cntc_finalize 6243-6290, cntc_finalizeLast 6294-6375 */
 void cntc_finalize(int *ire);
 void cntc_finalizelast(void);

@@ -23,7 +23,7 @@ def header_prototypes():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
     protos = {}
-    for m in re.finditer(r"\b(?:void|int|long long|double)\s+(cntc_\w+)\s*\(([^)]*)\)\s*;", text):
+    for m in re.finditer(r"\b(?:void|int|long long|double)\s+((?:cntc|subs)_\w+)\s*\(([^)]*)\)\s*;", text):
         args = m.group(2).strip()
         protos[m.group(1)] = 0 if args in ("", "void") else len(args.split(","))
     return protos
