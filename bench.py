@@ -557,12 +557,15 @@ def run_large(args, dist):
             raise RuntimeError("large patch could not be prepared")
         if args.warmup > 0:
             rb.solve(args.warmup)
+        k0 = cg.kernel_launches()
         t = rb.solve(max(1, args.steps))
+        launches = cg.kernel_launches() - k0
         err = rb.collect()
         rb.release()
         st = cg.getsolverstats(1, icp)
         it = cg.getiterationcounts(1, icp)
-        forms[mixed] = dict(ms=float(t[:, 0].mean()), ierror=int(err[0]), stats=st, it=it, res=cg.results(1, icp))
+        forms[mixed] = dict(ms=float(t[:, 0].mean()), ierror=int(err[0]), stats=st, it=it, res=cg.results(1, icp),
+                            launches=launches)
     clk = clocks.stop()
     # end to end through cntc_calculate (host buffers; copies and set-up inside)
     torch.cuda.synchronize()
@@ -610,7 +613,7 @@ def run_large(args, dist):
                          "note": "algorithmic bytes of the convolutions / SM cycles in them at the sampled clock"},
             "e2e": {"value": 1.0 / te, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ierror": int(e_err)},
-            "clocks": clk, "gpu_launches": 3}
+            "clocks": clk, "gpu_launches": int(a["launches"])}
 
 
 def main():
