@@ -124,3 +124,69 @@ def test_unknown_problem_getters_leave_output(lib):
     z = ctypes.c_double(-7.0)
     lib.cntc_getcontactforces(_i(999), _i(9), ctypes.byref(fn), ctypes.byref(z), ctypes.byref(z), ctypes.byref(z))
     assert fn.value == -7.0
+
+
+def _getparameters(lib, ire, icp, itask, n=30):
+    v = np.full(n, -1.0)
+    lib.cntc_getparameters(_i(ire), _i(icp), _i(itask), _i(n), v.ctypes.data_as(cg._DP))
+    return v
+
+
+def test_getparameters_material_friction_kinematics(lib):
+    """cntc_getParameters (contact_addon.f90:4164-4258): itask 2 material with combin_mater's
+    ga, nu and ak, itask 3 the Coulomb friction, itask 1 the kinematics; values in the
+    selected units (SI: moduli in N/m^2, velocity in m/s)."""
+    ire, icp = 906, 1
+    cg.setmaterialparameters(ire, icp, 0, [0.3, 0.25, 80000.0, 90000.0])
+    cg.setfrictionmethod(ire, icp, 0, [0.35, 0.3])
+    cg.setreferencevelocity(ire, icp, 20000.0)
+    m = _getparameters(lib, ire, icp, 2)
+    ga = 2.0 / (1 / 80000.0 + 1 / 90000.0)
+    assert m[:3] == pytest.approx([80000.0, 90000.0, ga])
+    assert m[3:6] == pytest.approx([0.3, 0.25, ga * (0.3 / 80000.0 + 0.25 / 90000.0) / 2])
+    assert m[6] == pytest.approx((ga / 4) * ((1 - 0.6) / 80000.0 - (1 - 0.5) / 90000.0))
+    assert np.all(m[7:22] == 0.0) and np.all(m[22:] == -1.0)     # only 22 values are written
+    f = _getparameters(lib, ire, icp, 3)
+    # L = 0 keeps one coefficient, the smaller of fstat and fkin (contact_addon.f90:1817-1822)
+    assert f[:7] == pytest.approx([0, 1, 0, 0, 0, 0.3, 0.3])
+    k = _getparameters(lib, ire, icp, 1)
+    assert k[0] == 20000.0 and np.all(k[6:] == -1.0)
+    cg.setflags(ire, icp, [cg.CNTC_if_units], [cg.CNTC_un_si])
+    assert _getparameters(lib, ire, icp, 2)[0] == pytest.approx(80000.0 * 1e6)
+    assert _getparameters(lib, ire, icp, 1)[0] == pytest.approx(20.0)
+    short = _getparameters(lib, ire, icp, 2, n=2)                 # lenarr bounds the output
+    assert short.size == 2
+    cg.finalize(ire)
+
+
+def test_entry_points_outside_the_solve_path(lib):
+    """Wheel-rail, input-file and subsurface entry points exist and report 'not supported':
+    outputs zeroed, ierror CNTC_err_other; metadata is accepted; temperatures are zero."""
+    ire, icp = 907, 1
+    cg.setnormalforce(ire, icp, 1e4)
+    ierr = ctypes.c_int(0)
+    name = b"track.inp"
+    lib.cntc_readinpfile(_i(ire), _i(1), name, _i(len(name)), ctypes.byref(ierr))
+    assert ierr.value == cg.CNTC_err_other
+    lib.subs_calculate(_i(ire), _i(icp), ctypes.byref(ierr))
+    assert ierr.value == -99
+    npatch = ctypes.c_int(5)
+    lib.cntc_getnumcontactpatches(_i(ire), ctypes.byref(npatch))
+    assert npatch.value == 0
+    v = np.full(6, 3.0)
+    lib.cntc_getcontactlocation(_i(ire), _i(icp), _i(6), v.ctypes.data_as(cg._DP))
+    assert np.all(v == 0.0)
+    nx, ny, nz = ctypes.c_int(1), ctypes.c_int(1), ctypes.c_int(1)
+    lib.subs_getblocksize(_i(ire), _i(icp), _i(1), ctypes.byref(nx), ctypes.byref(ny), ctypes.byref(nz))
+    assert (nx.value, ny.value, nz.value) == (0, 0, 0)
+    w = np.full((2, 3), 4.0)
+    icol = np.zeros(2, dtype=np.int32)
+    lib.subs_getresults(_i(ire), _i(icp), _i(1), _i(3), _i(2), icol.ctypes.data_as(cg._IP), w.ctypes.data_as(cg._DP))
+    assert np.all(w == 0.0)
+    params = np.array([1], dtype=np.int32)
+    vals = np.array([0.5])
+    lib.cntc_setmetadata(_i(ire), _i(icp), _i(1), params.ctypes.data_as(cg._IP), vals.ctypes.data_as(cg._DP))
+    t1, t2 = ctypes.c_double(-1), ctypes.c_double(-1)
+    lib.cntc_getmaximumtemperature(_i(ire), _i(icp), ctypes.byref(t1), ctypes.byref(t2))
+    assert (t1.value, t2.value) == (0.0, 0.0)
+    cg.finalize(ire)
