@@ -446,7 +446,8 @@ def setup_case(ire, icp, case):
 
     Keys: tang, norm, bound, gausei, maxgs, maxin, maxnr, maxout, eps, gd (8 floats + kdowfb
     for G=5), poiss, gg, fstat, veloc, cksi, ceta, cphi, fn | pen, ipotcn, potprm,
-    h (element-wise undeformed distance, optional), mixed (0-4), dq (optional), group (CTAs
+    h (element-wise undeformed distance, optional), prmudf (6 coefficients of a quadratic
+    undeformed distance, ibase 1, optional), mixed (0-4), dq (optional), group (CTAs
     per patch: 0 automatic, 1 one CTA, n >= 2 a cooperative group of at most n)."""
     flags = [CNTC_ic_tang, CNTC_ic_bound, CNTC_ic_iestim, CNTC_if_mixedprec, CNTC_if_groupctas]
     values = [case.get("tang", 3), case.get("bound", 0), case.get("iestim", 0), case.get("mixed", 0),
@@ -476,6 +477,8 @@ def setup_case(ire, icp, case):
         setpotcontact(ire, icp, ipot, case["potprm"][:6])
     if "h" in case:
         setundeformeddistc(ire, icp, 9, np.asarray(case["h"], dtype=np.float64).ravel())
+    elif "prmudf" in case:
+        setundeformeddistc(ire, icp, 1, np.asarray(case["prmudf"], dtype=np.float64))
     if case.get("norm", 1) == 1:
         setnormalforce(ire, icp, case["fn"])
     else:

@@ -4,6 +4,7 @@ A case is a plain dict (see contact_gb300.setup_case for the keys).  The same di
 drives the GB300 library through its C-ABI and the CPU oracle, so both solve exactly
 the same problem.
 """
+import ctypes
 import math
 import os
 import sys
@@ -71,6 +72,22 @@ def tractcurv_case(cksi):
     return dict(tang=3, norm=1, bound=0, gausei=0, maxgs=80, maxin=200, maxnr=5, maxout=1, eps=1e-6,
                 poiss=0.28, gg=82000.0, fstat=0.33, veloc=10000.0, fn=106700.0, cksi=cksi, ceta=0.0, cphi=0.0,
                 ipotcn=-2, potprm=[48, 44, 0.0008, 0.5, 1.1], dq=0.5)
+
+
+def cattaneo_case(icase, cksi=0.0):
+    """examples/cattaneo.inp, a polyethylene ball (G 200 N/mm^2, nu 0.42, mu 0.4) on a plane,
+    19x19 grid, Fn 9.1954 N, eps 1e-4.  Case 1: Hertzian semi-axes 1 mm, normal problem only.
+    Case 2: the same geometry as quadratic undeformed distance 0.01 x^2 + 0.01 y^2 on the grid
+    from -1.26667 mm with spacing 0.13333 mm, and the shift problem (T=1, TangCG) with rigid
+    shift cksi (the reference prescribes the force and finds the shift by Newton-Raphson)."""
+    c = dict(tang=0, norm=1, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=1, eps=1e-4,
+             poiss=0.42, gg=200.0, fstat=0.4, veloc=1.0, fn=9.1954, cksi=0.0, ceta=0.0, cphi=0.0)
+    if icase == 1:
+        c.update(ipotcn=-3, potprm=[19, 19, 1.0, 1.0, 1.26667])
+    else:
+        c.update(tang=1, cksi=cksi, ipotcn=1, potprm=[19, 19, -1.26667, -1.26667, 0.13333, 0.13333],
+                 prmudf=[0.01, 0.0, 0.01, 0.0, 0.0, 0.0])
+    return c
 
 
 def rough_surface(mx, my, xl, yl, dx, dy, pen_hz, seed, rx=460.0, ry=300.0, nsin=8):
@@ -166,6 +183,12 @@ def to_oracle(case):
                                  pow_s=0.9))
         pb.fdecay, pb.betath, pb.kdowfb = gd["fdecay"], gd["betath"], gd["kdowfb"]
         pb.d_ifc, pb.d_lin, pb.d_cns, pb.d_slp, pb.pow_s = gd["d_ifc"], gd["d_lin"], gd["d_cns"], gd["d_slp"], gd["pow_s"]
+    if "prmudf" in case:
+        arr = np.ascontiguousarray(case["prmudf"], dtype=np.float64)
+        pb.ibase = 1
+        pb.nprmudf = arr.size
+        pb.prmudf = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        pb._keep = arr                       # alive until the solve returns
     return pb, case.get("h")
 
 

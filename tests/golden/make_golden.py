@@ -1,6 +1,6 @@
 """Extract golden vectors from the reference's own regression outputs.
 
-Reads, as text, two files of the CONTACT repository and writes compact JSON
+Reads, as text, three output files of the CONTACT repository and writes compact JSON
 fixtures next to this script:
 
 * testbank/test_table_mx11.ref_fx -> test_table_mx11.json
@@ -12,6 +12,12 @@ fixtures next to this script:
   first series (cases 1-30) of examples/tractcurv.inp (Hertz a1/aob input, 48x44 grid,
   Coulomb friction, SteadyGS): forces, energy, approach, pmax to 4 digits,
   element counts, iteration counts and the element-division picture.
+* examples/cattaneo.ref_out -> cattaneo.json
+  examples/cattaneo.inp, 19x19 grid, polyethylene ball on a plane (G 200, nu 0.42, mu 0.4):
+  case 1 the Hertzian normal problem (NormCG), case 2 the non-Hertzian quadratic geometry
+  with the shift problem (T=1, TangCG) whose tangential force the reference prescribes by
+  Newton-Raphson on the shift; kept: the converged shift Cksi printed by that iteration,
+  forces, approach, pmax, element counts and the element-division picture.
 
 Usage: python tests/golden/make_golden.py [reference_root]
 """
@@ -78,6 +84,51 @@ def parse_tractcurv(path, inp_path, ncase_max=30):
     return {"source": "examples/tractcurv.ref_out", "series": 1, "cases": out}
 
 
+def _results_block(body):
+    """Printed results of one case: forces, approach, pmax, counts, picture."""
+    rec = {}
+    ln = body.splitlines()
+    for i, s in enumerate(ln):
+        if s.strip().startswith("FN") and "ELAST.EN." in s:
+            v = ln[i + 1].split()
+            rec.update(fn=float(v[0]), fx=float(v[1]), fy=float(v[2]), mz=float(v[3]), elen=float(v[4]))
+        if s.strip().startswith("FN/G"):
+            v = ln[i + 1].split()
+            rec.update(approach=float(v[3]), pmax=float(v[4]))
+        if s.strip().startswith("NPOT") and "NCON" in s:
+            v = ln[i + 1].split()
+            rec.update(npot=int(v[0]), ncon=int(v[1]), nadh=int(v[2]), nslip=int(v[3]))
+        if "FORM OF THE CONTACT" in s:
+            rows = []
+            j = i + 1
+            while re.match(r"^\s+\d+\s+\S", ln[j]) and not ln[j].strip().startswith("1 2"):
+                parts = ln[j].split()
+                if not parts[0].isdigit() or len(parts) < 2:
+                    break
+                rows.append("".join(parts[1:]))
+                j += 1
+            rec["picture"] = rows[::-1]     # row iy=1 first
+    return rec
+
+
+def parse_cattaneo(path):
+    text = open(path).read()
+    blocks = re.split(r"\n Case\s+(\d+)\n", text)
+    out = []
+    for k in range(1, len(blocks), 2):
+        icase = int(blocks[k])
+        body = blocks[k + 1]
+        rec = {"case": icase}
+        m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+        rec["norm_ncon"], rec["norm_itcg"] = int(m.group(1)), int(m.group(3))
+        nr = re.findall(r"NR_Fy,\s+Cksi, Fxk:\s+(\S+)\s+(\S+)", body)
+        if nr:
+            rec["cksi"], rec["fx_rel_nr"] = float(nr[-1][0]), float(nr[-1][1])
+        rec.update(_results_block(body))
+        out.append(rec)
+    return {"source": "examples/cattaneo.ref_out", "cases": out}
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     tt = parse_test_table(os.path.join(root, "testbank", "test_table_mx11.ref_fx"))
@@ -87,7 +138,11 @@ def main():
                          os.path.join(root, "examples", "tractcurv.inp"))
     with open(os.path.join(HERE, "tractcurv_series1.json"), "w") as f:
         json.dump(tc, f, indent=0)
-    print("test_table cases:", len(tt["cases"]), " tractcurv cases:", len(tc["cases"]))
+    ca = parse_cattaneo(os.path.join(root, "examples", "cattaneo.ref_out"))
+    with open(os.path.join(HERE, "cattaneo.json"), "w") as f:
+        json.dump(ca, f, indent=0)
+    print("test_table cases:", len(tt["cases"]), " tractcurv cases:", len(tc["cases"]),
+          " cattaneo cases:", len(ca["cases"]))
 
 
 if __name__ == "__main__":

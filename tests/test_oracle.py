@@ -2,8 +2,9 @@
 
 test_table_mx11.json holds the 3220 printed lines of src/test_table.f90 (testbank/
 test_table_mx11.ref_fx); tractcurv_series1.json the first series of examples/tractcurv.inp
-(examples/tractcurv.ref_out).  The oracle has to reproduce both at their printed precision
-before any GPU result is compared with it.
+(examples/tractcurv.ref_out); cattaneo.json the two cases of examples/cattaneo.inp
+(examples/cattaneo.ref_out: NormCG, and TangCG on the shift problem).  The oracle has to
+reproduce them at their printed precision before any GPU result is compared with it.
 """
 import json
 import math
@@ -183,3 +184,35 @@ def test_gdsteady_matches_steadygs(oracle):
     assert np.array_equal(g0["igs"], g5["igs"])
     assert abs(g5["fx"] - g0["fx"]) <= 1e-9 * abs(g0["fx"])
     assert np.abs(g5["px"] - g0["px"]).max() <= 1e-8 * np.abs(g0["pn"]).max()
+
+
+def _printed4(x, gold):
+    """x agrees with a value printed to 4 significant digits (half a unit of the last one)."""
+    if gold == 0.0:
+        return abs(x) < 5e-4
+    unit = 10.0 ** (math.floor(math.log10(abs(gold))) - 3)
+    return abs(x - gold) <= 0.5 * unit * (1 + 1e-9)
+
+
+def _picture(igs, mx, my):
+    sym = {0: ".", 1: "*", 2: "S", 3: "P"}
+    return ["".join(sym[int(igs[iy * mx + ix])] for ix in range(mx)) for iy in range(my)]
+
+
+def test_cattaneo_against_golden(oracle):
+    """examples/cattaneo.inp: the Hertzian normal problem (NormCG) and the shift problem on the
+    quadratic geometry (TangCG, T=1) at the shift the reference's Newton-Raphson converged to.
+    Forces, approach, pmax and elastic energy to the printed 4 digits; element counts, the
+    element-division picture and the NormCG iteration count exact."""
+    gold = _load("cattaneo.json")
+    for g in gold["cases"]:
+        o = C.oracle_solve(C.cattaneo_case(g["case"], g.get("cksi", 0.0)))
+        assert o["ierror"] == 0
+        for key, gk in (("fn", "fn"), ("fx", "fx"), ("pen", "approach"), ("pmax", "pmax"), ("elen", "elen")):
+            assert _printed4(o[key], g[gk]), (g["case"], key, o[key], g[gk])
+        assert (o["ncon"], o["nadh"], o["nslip"]) == (g["ncon"], g["nadh"], g["nslip"])
+        assert o["itcg"] == g["norm_itcg"]
+        assert _picture(o["igs"], 19, 19) == [r.replace("o", ".") for r in g["picture"]]
+        if g["case"] == 2:
+            assert o["solver"] == 2                     # TangCG
+            assert _printed4(o["fx"] / (0.4 * o["fn"]), g["fx_rel_nr"])
