@@ -90,6 +90,16 @@ def cattaneo_case(icase, cksi=0.0):
     return c
 
 
+def test_caddon_element1():
+    """Result element 1 of src/test_caddon.f90 in CONTACT units (mm, N, rad/mm): steel
+    (G 82000 N/mm^2, nu 0.28, mu 0.3), Hertzian semi-axes 4.25 x 7 mm on a 21x33 grid (scale
+    21/17), penetration 0.05 mm prescribed, creepage 0.001, spin 0.4 rad/m, rolling speed
+    24 m/s, SteadyGS with maxgs 999, maxin 30, eps 1e-4."""
+    return dict(tang=3, norm=0, bound=0, gausei=0, maxgs=999, maxin=30, maxnr=30, maxout=1, eps=1e-4,
+                poiss=0.28, gg=82000.0, fstat=0.3, veloc=24000.0, pen=0.05, cksi=0.001, ceta=0.0, cphi=0.4e-3,
+                ipotcn=-3, potprm=[21, 33, 4.25, 7.0, 21.0 / 17.0], dq=0.5)
+
+
 def rough_surface(mx, my, xl, yl, dx, dy, pen_hz, seed, rx=460.0, ry=300.0, nsin=8):
     """Non-Hertzian undeformed distance: x^2/(2Rx) + y^2/(2Ry) + a seeded sum of 8 sinusoids
     (wavelength 1-5 mm, total amplitude 5% of the Hertzian approach)."""

@@ -1,6 +1,6 @@
 """Extract golden vectors from the reference's own regression outputs.
 
-Reads, as text, three output files of the CONTACT repository and writes compact JSON
+Reads, as text, four output files of the CONTACT repository and writes compact JSON
 fixtures next to this script:
 
 * testbank/test_table_mx11.ref_fx -> test_table_mx11.json
@@ -18,6 +18,13 @@ fixtures next to this script:
   with the shift problem (T=1, TangCG) whose tangential force the reference prescribes by
   Newton-Raphson on the shift; kept: the converged shift Cksi printed by that iteration,
   forces, approach, pmax, element counts and the element-division picture.
+
+* testbank/test_caddon.ref_out -> test_caddon_re1.json
+  output of src/test_caddon.f90 for result element 1 (module 3 through the library
+  interface in SPCK units: Hertzian 21x33 grid, penetration prescribed, creepage 0.001,
+  spin 0.4 rad/m, SteadyGS, eps 1e-4): grid spacing, forces, moment, patch areas, maximum
+  pressure and traction, positions and values of the largest tractions.  (Result element 2
+  uses a falling friction law and an interfacial layer, outside this build.)
 
 Usage: python tests/golden/make_golden.py [reference_root]
 """
@@ -129,6 +136,29 @@ def parse_cattaneo(path):
     return {"source": "examples/cattaneo.ref_out", "cases": out}
 
 
+def parse_test_caddon(path):
+    text = open(path).read()
+    block = text.split("...start processing of Result Element")[1]     # element 1, first solve
+    num = r"([-+]?[\d.]+(?:[EeDd][-+]?\d+)?)"
+    rec = {}
+    m = re.search(r"Dx=\s*" + num + r", Dy=\s*" + num, block)
+    rec["dx_m"], rec["dy_m"] = float(m.group(1)), float(m.group(2))
+    rec["pen_m"] = float(re.search(r"Pen=\s*" + num, block).group(1))
+    m = re.search(r"Tn=\s*" + num + r", Fx=\s*" + num + r", Fy=\s*" + num + r" \[N\], Mz=\s*" + num, block)
+    rec["tn"], rec["fx"], rec["fy"], rec["mz_nm"] = (float(m.group(k)) for k in range(1, 5))
+    m = re.search(r"Mx=\s*(\d+), My=\s*(\d+)", block)
+    rec["mx"], rec["my"] = int(m.group(1)), int(m.group(2))
+    m = re.search(r"C=\s*" + num + r" \[m2\], H=\s*" + num + r" \[m2\], S=\s*" + num, block)
+    rec["carea_m2"], rec["harea_m2"], rec["sarea_m2"] = (float(m.group(k)) for k in range(1, 4))
+    m = re.search(r"Pnmax=\s*" + num + r", Ptmax=\s*" + num, block)
+    rec["pnmax_mpa"], rec["ptmax_mpa"] = float(m.group(1)), float(m.group(2))
+    for key in ("Pn", "Px", "Py"):
+        m = re.search(key + r"\(\s*(\d+),\s*(\d+)\)=\s*" + num, block)
+        rec[key.lower() + "_max"] = [int(m.group(1)), int(m.group(2)), float(m.group(3))]
+    return {"source": "testbank/test_caddon.ref_out", "element": 1, "units": "SPCK (m, N, forces on body 2)",
+            "result": rec}
+
+
 def main():
     root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     tt = parse_test_table(os.path.join(root, "testbank", "test_table_mx11.ref_fx"))
@@ -141,8 +171,11 @@ def main():
     ca = parse_cattaneo(os.path.join(root, "examples", "cattaneo.ref_out"))
     with open(os.path.join(HERE, "cattaneo.json"), "w") as f:
         json.dump(ca, f, indent=0)
+    tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
+    with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
+        json.dump(tcd, f, indent=0)
     print("test_table cases:", len(tt["cases"]), " tractcurv cases:", len(tc["cases"]),
-          " cattaneo cases:", len(ca["cases"]))
+          " cattaneo cases:", len(ca["cases"]), " test_caddon element 1:", tcd["result"]["tn"])
 
 
 if __name__ == "__main__":

@@ -3,8 +3,10 @@
 test_table_mx11.json holds the 3220 printed lines of src/test_table.f90 (testbank/
 test_table_mx11.ref_fx); tractcurv_series1.json the first series of examples/tractcurv.inp
 (examples/tractcurv.ref_out); cattaneo.json the two cases of examples/cattaneo.inp
-(examples/cattaneo.ref_out: NormCG, and TangCG on the shift problem).  The oracle has to
-reproduce them at their printed precision before any GPU result is compared with it.
+(examples/cattaneo.ref_out: NormCG, and TangCG on the shift problem); test_caddon_re1.json
+result element 1 of src/test_caddon.f90 (testbank/test_caddon.ref_out: penetration
+prescribed, spin, SteadyGS, printed in SPCK units).  The oracle has to reproduce them at
+their printed precision before any GPU result is compared with it.
 """
 import json
 import math
@@ -216,3 +218,33 @@ def test_cattaneo_against_golden(oracle):
         if g["case"] == 2:
             assert o["solver"] == 2                     # TangCG
             assert _printed4(o["fx"] / (0.4 * o["fn"]), g["fx_rel_nr"])
+
+
+def test_caddon_element1_against_golden(oracle):
+    """src/test_caddon.f90, result element 1 (testbank/test_caddon.ref_out).  The reference
+    printed in SPCK units: lengths in m, forces in N acting on body 2 (the sign of CONTACT's
+    forces and tangential tractions flips, src/m_global_data.f90:478-486).  Compared at the
+    printed decimals: grid spacing, forces, moment, patch areas, maximum pressure and traction,
+    and the positions and values of the largest pn, px, py."""
+    g = _load("test_caddon_re1.json")["result"]
+    o = C.oracle_solve(C.test_caddon_element1())
+    assert o["ierror"] == 0 and o["solver"] == 4          # SteadyGS
+
+    def near(x, gold, decimals):
+        return abs(x - gold) <= 0.5 * 10.0 ** (-decimals) * (1 + 1e-9)
+
+    assert near(o["dx"] * 1e-3, g["dx_m"], 5) and near(o["dy"] * 1e-3, g["dy_m"], 5)
+    assert (o["mx"], o["my"]) == (g["mx"], g["my"])
+    assert near(o["fn"], g["tn"], 1)
+    assert near(-o["fx"], g["fx"], 1) and near(-o["fy"], g["fy"], 1)
+    assert near(-o["mz"] * 1e-3, g["mz_nm"], 1)
+    dxdy = o["dx"] * o["dy"] * 1e-6
+    assert near(o["ncon"] * dxdy, g["carea_m2"], 6)
+    assert near(o["nadh"] * dxdy, g["harea_m2"], 6) and near(o["nslip"] * dxdy, g["sarea_m2"], 6)
+    pt = np.hypot(o["px"], o["py"])
+    assert near(o["pmax"], g["pnmax_mpa"], 1) and near(pt.max(), g["ptmax_mpa"], 1)
+    mx = o["mx"]
+    for key, arr, sign in (("pn_max", o["pn"], 1.0), ("px_max", o["px"], -1.0), ("py_max", o["py"], -1.0)):
+        i = int(np.argmax(np.abs(arr)))
+        assert [i % mx + 1, i // mx + 1] == g[key][:2], key
+        assert near(sign * arr[i], g[key][2], 1), key
