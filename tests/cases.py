@@ -100,6 +100,24 @@ def test_caddon_element1():
                 ipotcn=-3, potprm=[21, 33, 4.25, 7.0, 21.0 / 17.0], dq=0.5)
 
 
+def testbank_case(icase):
+    """Cases of testbank/testbank.inp.  1: shift problem (T=1) with prescribed approach
+    0.01131 mm and shift 0.00304 mm, steel, mu 0.3, quadratic geometry 0.0056566 (x^2 + y^2)
+    on a 17x17 grid from -1.13333 mm with spacing 0.13333 mm, TangCG, eps 1e-8.
+    7: steady rolling, Fn 0.4705, creepage -0.00304, mu 0.4013, G 1, nu 0.28, dq 0.2 mm,
+    quadratic geometry 0.002963 (x^2 + y^2) on a 41x41 grid from -4.1 mm with spacing 0.2 mm,
+    SteadyGS with maxgs 80, maxin 30, eps 1e-6."""
+    if icase == 1:
+        return dict(tang=1, norm=0, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=1, eps=1e-8,
+                    poiss=0.28, gg=82000.0, fstat=0.3, veloc=1.0, pen=0.01131, cksi=0.00304, ceta=0.0, cphi=0.0,
+                    ipotcn=1, potprm=[17, 17, -1.13333, -1.13333, 0.13333, 0.13333],
+                    prmudf=[0.0056566, 0.0, 0.0056566, 0.0, 0.0, 0.0])
+    return dict(tang=3, norm=1, bound=0, gausei=0, maxgs=80, maxin=30, maxnr=5, maxout=1, eps=1e-6,
+                poiss=0.28, gg=1.0, fstat=0.4013, veloc=1000.0, fn=0.4705, cksi=-0.00304, ceta=0.0, cphi=0.0,
+                dq=0.2, ipotcn=1, potprm=[41, 41, -4.1, -4.1, 0.2, 0.2],
+                prmudf=[0.002963, 0.0, 0.002963, 0.0, 0.0, 0.0])
+
+
 def rough_surface(mx, my, xl, yl, dx, dy, pen_hz, seed, rx=460.0, ry=300.0, nsin=8):
     """Non-Hertzian undeformed distance: x^2/(2Rx) + y^2/(2Ry) + a seeded sum of 8 sinusoids
     (wavelength 1-5 mm, total amplitude 5% of the Hertzian approach)."""

@@ -1,6 +1,6 @@
 """Extract golden vectors from the reference's own regression outputs.
 
-Reads, as text, four output files of the CONTACT repository and writes compact JSON
+Reads, as text, five output files of the CONTACT repository and writes compact JSON
 fixtures next to this script:
 
 * testbank/test_table_mx11.ref_fx -> test_table_mx11.json
@@ -25,6 +25,13 @@ fixtures next to this script:
   spin 0.4 rad/m, SteadyGS, eps 1e-4): grid spacing, forces, moment, patch areas, maximum
   pressure and traction, positions and values of the largest tractions.  (Result element 2
   uses a falling friction law and an interfacial layer, outside this build.)
+
+* testbank/testbank.ref_out -> testbank_cases.json
+  cases 1 and 7 of testbank/testbank.inp, the stand-alone program's regression set: case 1
+  the shift problem with prescribed approach (17x17 quadratic geometry, TangCG, eps 1e-8),
+  case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6).  The other
+  cases use features outside this build (ConvexGS, bilinear loading, falling or variable
+  friction, other materials, transient sequences).
 
 Usage: python tests/golden/make_golden.py [reference_root]
 """
@@ -110,7 +117,9 @@ def _results_block(body):
             j = i + 1
             while re.match(r"^\s+\d+\s+\S", ln[j]) and not ln[j].strip().startswith("1 2"):
                 parts = ln[j].split()
-                if not parts[0].isdigit() or len(parts) < 2:
+                # a picture row: its row number, then one symbol per element (the column
+                # numbers below the picture are digits)
+                if not parts[0].isdigit() or len(parts) < 2 or any(t.isdigit() for t in parts[1:]):
                     break
                 rows.append("".join(parts[1:]))
                 j += 1
@@ -134,6 +143,25 @@ def parse_cattaneo(path):
         rec.update(_results_block(body))
         out.append(rec)
     return {"source": "examples/cattaneo.ref_out", "cases": out}
+
+
+def parse_testbank(path, wanted=(1, 7)):
+    text = open(path).read()
+    blocks = re.split(r"\n Case\s+(\d+)\n", text)
+    out = []
+    for k in range(1, len(blocks), 2):
+        icase = int(blocks[k])
+        if icase not in wanted:
+            continue
+        body = blocks[k + 1]
+        rec = {"case": icase}
+        m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+        rec["norm_itcg"] = int(m.group(3))
+        m = re.search(r"Tang: final element division: A, S=\s*(\d+)\s+(\d+)\s+It(CG|GS)=\s*(\d+)", body)
+        rec["tang_solver"], rec["tang_it"] = m.group(3), int(m.group(4))
+        rec.update(_results_block(body))
+        out.append(rec)
+    return {"source": "testbank/testbank.ref_out", "cases": out}
 
 
 def parse_test_caddon(path):
@@ -174,6 +202,9 @@ def main():
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)
+    tb = parse_testbank(os.path.join(root, "testbank", "testbank.ref_out"))
+    with open(os.path.join(HERE, "testbank_cases.json"), "w") as f:
+        json.dump(tb, f, indent=0)
     print("test_table cases:", len(tt["cases"]), " tractcurv cases:", len(tc["cases"]),
           " cattaneo cases:", len(ca["cases"]), " test_caddon element 1:", tcd["result"]["tn"])
 

@@ -5,7 +5,8 @@ test_table_mx11.ref_fx); tractcurv_series1.json the first series of examples/tra
 (examples/tractcurv.ref_out); cattaneo.json the two cases of examples/cattaneo.inp
 (examples/cattaneo.ref_out: NormCG, and TangCG on the shift problem); test_caddon_re1.json
 result element 1 of src/test_caddon.f90 (testbank/test_caddon.ref_out: penetration
-prescribed, spin, SteadyGS, printed in SPCK units).  The oracle has to reproduce them at
+prescribed, spin, SteadyGS, printed in SPCK units); testbank_cases.json cases 1 and 7 of
+testbank/testbank.inp (TangCG shift with prescribed approach, SteadyGS on a 41x41 grid).  The oracle has to reproduce them at
 their printed precision before any GPU result is compared with it.
 """
 import json
@@ -248,3 +249,21 @@ def test_caddon_element1_against_golden(oracle):
         i = int(np.argmax(np.abs(arr)))
         assert [i % mx + 1, i // mx + 1] == g[key][:2], key
         assert near(sign * arr[i], g[key][2], 1), key
+
+
+def test_testbank_cases_against_golden(oracle):
+    """testbank/testbank.inp cases 1 (shift, approach prescribed, TangCG) and 7 (steady rolling,
+    SteadyGS, 41x41): forces, moment, approach, pmax and elastic energy to the printed 4
+    digits; element counts, pictures and the NormCG and TangCG/SteadyGS iteration counts
+    exact."""
+    gold = _load("testbank_cases.json")
+    for g in gold["cases"]:
+        o = C.oracle_solve(C.testbank_case(g["case"]))
+        assert o["ierror"] == 0
+        for key, gk in (("fn", "fn"), ("fx", "fx"), ("mz", "mz"), ("pen", "approach"), ("pmax", "pmax"),
+                        ("elen", "elen")):
+            assert _printed4(o[key], g[gk]), (g["case"], key, o[key], g[gk])
+        assert (o["ncon"], o["nadh"], o["nslip"]) == (g["ncon"], g["nadh"], g["nslip"])
+        assert o["itcg"] == g["norm_itcg"] and o["itgs"] == g["tang_it"]
+        assert o["solver"] == (2 if g["tang_solver"] == "CG" else 4)
+        assert _picture(o["igs"], o["mx"], o["my"]) == [r.replace("o", ".") for r in g["picture"]]
