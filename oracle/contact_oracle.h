@@ -2,17 +2,20 @@
  * CPU ORACLE -- test infrastructure only.
  *
  * A serial C++ restatement of CONTACT's module-3 rolling-contact solve path
- * (eve70a/CONTACT, Fortran 90), used as the checker for the GB300 library and
+ * (eve70a/CONTACT, Fortran 90), used as the parity reference of the GB300 library and
  * as the timed CPU baseline.  Nothing in the product library links or calls
  * this code; only tests/, __graft_entry__.smoke() and bench.py's CPU legs do.
  *
  * Parity pinning: the oracle reproduces the reference's golden outputs
  * testbank/test_table_mx11.ref_fx (3220 Hertzian steady-rolling cases, NormCG
- * + SteadyGS, printed to 6 decimals) and the first series of
- * examples/tractcurv.ref_out (48x44 grid, 4 significant digits); see
- * tests/test_oracle_golden.py.  GDsteady (G=5) and TangCG (T=1,2) have no
- * golden output in the reference: those paths are restated line by line but
- * their parity is anchored only on the shared algorithms they call.
+ * + SteadyGS, printed to 6 decimals), the first series of
+ * examples/tractcurv.ref_out (48x44 grid, 4 significant digits), both cases of
+ * examples/cattaneo.ref_out (NormCG, TangCG on the shift problem), result
+ * element 1 of testbank/test_caddon.ref_out (approach prescribed, spin) and
+ * cases 1 and 7 of testbank/testbank.ref_out (TangCG shift, SteadyGS 41x41);
+ * see tests/test_oracle.py.  GDsteady (G=5) and transient rolling (T=2) have no
+ * golden output in the reference: those paths are restated line by line and
+ * their parity is anchored on the shared algorithms they call.
  *
  * One function solves one contact patch, the way cntc_calculate() does for one
  * (ire,icp) pair in src/contact_addon.f90:3754-3900.

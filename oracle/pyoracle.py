@@ -1,7 +1,7 @@
 """CPU ORACLE -- test infrastructure only.
 
 ctypes front end of oracle/_build/libcontact_oracle.so, the serial C++ restatement
-of CONTACT's module-3 solve path.  Used by tests/ (as the checker), by
+of CONTACT's module-3 solve path.  Used by tests/ (the reference results), by
 __graft_entry__.smoke() and by bench.py's CPU-baseline legs; never by the
 product library.
 """

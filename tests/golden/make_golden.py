@@ -24,13 +24,13 @@ fixtures next to this script:
   interface in SPCK units: Hertzian 21x33 grid, penetration prescribed, creepage 0.001,
   spin 0.4 rad/m, SteadyGS, eps 1e-4): grid spacing, forces, moment, patch areas, maximum
   pressure and traction, positions and values of the largest tractions.  (Result element 2
-  uses a falling friction law and an interfacial layer, outside this build.)
+  uses a falling friction law and an interfacial layer, outside this library.)
 
 * testbank/testbank.ref_out -> testbank_cases.json
   cases 1 and 7 of testbank/testbank.inp, the stand-alone program's regression set: case 1
   the shift problem with prescribed approach (17x17 quadratic geometry, TangCG, eps 1e-8),
   case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6).  The other
-  cases use features outside this build (ConvexGS, bilinear loading, falling or variable
+  cases use features outside this library (ConvexGS, bilinear loading, falling or variable
   friction, other materials, transient sequences).
 
 Usage: python tests/golden/make_golden.py [reference_root]
