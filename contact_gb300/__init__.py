@@ -447,7 +447,7 @@ def setup_case(ire, icp, case):
     Keys: tang, norm, bound, gausei, maxgs, maxin, maxnr, maxout, eps, gd (8 floats + kdowfb
     for G=5), poiss, gg, fstat, veloc, cksi, ceta, cphi, fn | pen, ipotcn, potprm,
     h (element-wise undeformed distance, optional), prmudf (6 coefficients of a quadratic
-    undeformed distance, ibase 1, optional), mixed (0-4), dq (optional), group (CTAs
+    undeformed distance, ibase 1, optional), mixed (0-4), dq and chi (optional), group (CTAs
     per patch: 0 automatic, 1 one CTA, n >= 2 a cooperative group of at most n)."""
     flags = [CNTC_ic_tang, CNTC_ic_bound, CNTC_ic_iestim, CNTC_if_mixedprec, CNTC_if_groupctas]
     values = [case.get("tang", 3), case.get("bound", 0), case.get("iestim", 0), case.get("mixed", 0),
@@ -469,7 +469,7 @@ def setup_case(ire, icp, case):
     else:
         setsolverflags(ire, icp, gdig, ip, [case.get("eps", 1e-6)])
     if "dq" in case:
-        setrollingstepsize(ire, icp, 0.0, case["dq"])
+        setrollingstepsize(ire, icp, case.get("chi", 0.0), case["dq"])
     ipot = case.get("ipotcn", -3)
     if ipot < 0:
         sethertzcontact(ire, icp, ipot, case["potprm"][:5])

@@ -162,6 +162,11 @@ int prepare(Problem &p, Prep &out) {
         log_msg("only M=0, L=0, F=0, E=0 are supported");
         return CNTC_err_other;
     }
+    if (p.heat == 3) { log_msg("temperatures (H=3) are not computed by this library"); return CNTC_err_other; }
+    if (p.gencr >= 3) {
+        log_msg("influence coefficients: only piecewise-constant loading (C=2) is supported");
+        return CNTC_err_other;
+    }
     if (!(p.bound == 0 || p.bound == 2 || p.bound == 3)) { log_msg("B digit not supported"); return CNTC_err_other; }
     if (p.tang != 0 && p.tang != 3 && p.pvtime != 2) {
         log_msg("transient sequences (P != 2 with T = 1, 2) are not supported");
@@ -880,8 +885,17 @@ void cntc_setmaterialparameters(int *ire, int *icp, int *imeth, int *nparam, dou
     p->gg[1] = rparam[3] * p->s_forc / p->s_area;
 }
 
+// H digit (cntc_setTemperatureData, src/contact_addon.f90:1477-1550): the method is recorded
+// so that a solve with temperatures (H = 3) is refused; the temperature data are not used
 void cntc_settemperaturedata(int *ire, int *icp, int *imeth, int *nparam, double *rparam) {
-    (void)ire; (void)icp; (void)imeth; (void)nparam; (void)rparam;
+    (void)rparam;
+    static const int nparam_loc[4] = {0, 0, 0, 9};
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    const int h = *imeth;
+    if (h < 0 || h == 2 || h > 3) return;
+    if ((nparam_loc[h] == 0 && *nparam >= 2) || (nparam_loc[h] != 0 && *nparam != nparam_loc[h])) return;
+    p->heat = h;
 }
 
 void cntc_settimestep(int *ire, int *icp, double *dt) {

@@ -198,6 +198,8 @@ def to_oracle(case):
     pb.veloc = case.get("veloc", 10000.0)
     if "dq" in case:
         pb.dq = case["dq"]
+    if "chi" in case:
+        pb.chi = case["chi"]
     pb.cksi, pb.ceta, pb.cphi = case.get("cksi", 0.0), case.get("ceta", 0.0), case.get("cphi", 0.0)
     if pb.norm == 1:
         pb.fn = case["fn"]

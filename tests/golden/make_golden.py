@@ -1,6 +1,6 @@
 """Extract golden vectors from the reference's own regression outputs.
 
-Reads, as text, five output files of the CONTACT repository and writes compact JSON
+Reads, as text, output and input files of the CONTACT repository and writes compact JSON
 fixtures next to this script:
 
 * testbank/test_table_mx11.ref_fx -> test_table_mx11.json
@@ -32,6 +32,12 @@ fixtures next to this script:
   case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6).  The other
   cases use features outside this library (ConvexGS, bilinear loading, falling or variable
   friction, other materials, transient sequences).
+
+* perfc_test/*.inp + perfc_test/get_times.ref_out -> perfc_cases.json
+  the reference's performance inputs that this library solves (normal problems 1p-8p,
+  1f-4f on 71x81 to 575x647 grids; shift problems 1s-8s), read with contact_gb300.inp
+  (the geometry kept as its IBASE-2 table), with the published contact/slip counts,
+  iteration counts and wall-clock seconds of the reference's 2016 performance run.
 
 Usage: python tests/golden/make_golden.py [reference_root]
 """
@@ -164,6 +170,28 @@ def parse_testbank(path, wanted=(1, 7)):
     return {"source": "testbank/testbank.ref_out", "cases": out}
 
 
+PERFC = ["norm_problm_1p", "norm_problm_2p", "norm_problm_4p", "norm_problm_8p", "norm_problm_1f",
+         "norm_problm_2f", "norm_problm_4f", "tang_problm_1s", "tang_problm_2s", "tang_problm_4s",
+         "tang_problm_8s"]
+
+
+def parse_perfc(root):
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from contact_gb300 import inp
+    times = {}
+    for ln in open(os.path.join(root, "perfc_test", "get_times.ref_out")):
+        m = re.match(r"(\w+): (ncon|nslp)=\s*(\d+), (ItCG|ItGS)=\s*(\d+), (?:tot|wall)\.(?:wall|tang)=\s*([\d.]+)", ln)
+        if m:
+            times[m.group(1)] = {m.group(2): int(m.group(3)), m.group(4).lower(): int(m.group(5)),
+                                 "wall_s": float(m.group(6))}
+    out = []
+    for name in PERFC:
+        cases = inp.read_inp(open(os.path.join(root, "perfc_test", name + ".inp")).read())
+        c = {k: v for k, v in cases[0].items() if k != "h"}
+        out.append({"name": name, "case": c, "reference": times[name]})
+    return {"source": "perfc_test/*.inp, perfc_test/get_times.ref_out (2016-07-29, 1 thread)", "cases": out}
+
+
 def parse_test_caddon(path):
     text = open(path).read()
     block = text.split("...start processing of Result Element")[1]     # element 1, first solve
@@ -205,6 +233,9 @@ def main():
     tb = parse_testbank(os.path.join(root, "testbank", "testbank.ref_out"))
     with open(os.path.join(HERE, "testbank_cases.json"), "w") as f:
         json.dump(tb, f, indent=0)
+    pf = parse_perfc(root)
+    with open(os.path.join(HERE, "perfc_cases.json"), "w") as f:
+        json.dump(pf, f, separators=(",", ":"))
     print("test_table cases:", len(tt["cases"]), " tractcurv cases:", len(tc["cases"]),
           " cattaneo cases:", len(ca["cases"]), " test_caddon element 1:", tcd["result"]["tn"])
 

@@ -13,6 +13,7 @@ import re
 import numpy as np
 import pytest
 
+import cases as C
 import contact_gb300 as cg
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -189,4 +190,31 @@ def test_entry_points_outside_the_solve_path(lib):
     t1, t2 = ctypes.c_double(-1), ctypes.c_double(-1)
     lib.cntc_getmaximumtemperature(_i(ire), _i(icp), ctypes.byref(t1), ctypes.byref(t2))
     assert (t1.value, t2.value) == (0.0, 0.0)
+    cg.finalize(ire)
+
+
+def _calc(lib, ire, icp):
+    ierr = ctypes.c_int(12345)
+    lib.cntc_calculate(_i(ire), _i(icp), ctypes.byref(ierr))
+    return ierr.value
+
+
+def test_unsupported_options_refused_before_any_device_work(lib):
+    """Options outside the engine return CNTC_err_other from cntc_calculate (never a silent
+    fallback); the refusal comes from the set-up, so it needs no device: bilinear loading
+    (C=3), temperatures (H=3), viscoelastic material (M=1), prescribed total force (F=1)."""
+    base = C.config0(gausei=5, eps=1e-8, mx=21, my=21)
+    ire = 908
+    cg.setup_case(ire, 1, base)
+    cg.setflags(ire, 1, [cg.CNTC_ic_inflcf], [3])
+    assert _calc(lib, ire, 1) == cg.CNTC_err_other
+    cg.setup_case(ire, 2, base)
+    lib.cntc_settemperaturedata(_i(ire), _i(2), _i(3), _i(9), np.zeros(9).ctypes.data_as(cg._DP))
+    assert _calc(lib, ire, 2) == cg.CNTC_err_other
+    cg.setup_case(ire, 3, base)
+    cg.setmaterialparameters(ire, 3, 1, [0.28, 0.28, 82000.0, 82000.0, 0.0, 0.0, 0.0, 0.0])
+    assert _calc(lib, ire, 3) == cg.CNTC_err_other
+    cg.setup_case(ire, 4, base)
+    cg.setflags(ire, 4, [cg.CNTC_ic_force], [1])
+    assert _calc(lib, ire, 4) == cg.CNTC_err_other
     cg.finalize(ire)

@@ -267,3 +267,20 @@ def test_testbank_cases_against_golden(oracle):
         assert o["itcg"] == g["norm_itcg"] and o["itgs"] == g["tang_it"]
         assert o["solver"] == (2 if g["tang_solver"] == "CG" else 4)
         assert _picture(o["igs"], o["mx"], o["my"]) == [r.replace("o", ".") for r in g["picture"]]
+
+
+@pytest.mark.parametrize("name", ["norm_problm_1p", "norm_problm_1f", "norm_problm_2p", "norm_problm_2f",
+                                  "tang_problm_1s"])
+def test_perfc_against_published_run(oracle, name):
+    """The reference's performance inputs (perfc_test/*.inp, read by contact_gb300.inp; the
+    geometry an IBASE-2 table): contact or slip counts and NormCG / TangCG iteration counts of
+    the reference's published performance run (perfc_test/get_times.ref_out)."""
+    from contact_gb300 import inp
+    g = [c for c in _load("perfc_cases.json")["cases"] if c["name"] == name][0]
+    o = C.oracle_solve(inp.materialize(g["case"]))
+    ref = g["reference"]
+    assert o["ierror"] == 0
+    if "ncon" in ref:
+        assert (o["ncon"], o["itcg"]) == (ref["ncon"], ref["itcg"])
+    else:
+        assert o["solver"] == 2 and (o["nslip"], o["itgs"]) == (ref["nslp"], ref["itgs"])
