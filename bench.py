@@ -205,8 +205,9 @@ def measured_peaks():
 # CPU baseline: the oracle on all host cores, bounded sample, scaled by the FFT cost proxy
 # ------------------------------------------------------------------------------------------
 def cpu_sample_rate(cases, budget_s, seed, threads=None):
-    """Solve a seeded sample of the workload's patches with the CPU oracle on a thread pool
-    (ctypes releases the GIL).  Patches are drawn from those no larger than 64x64 so that a
+    """Solve a seeded sample of the workload's patches with the CPU oracle (its baseline
+    build, with a Stockham FFT in place of the parity build's simple recursive FFT) on a
+    thread pool (ctypes releases the GIL).  Patches are drawn from those no larger than 64x64 so that a
     sample ends within the budget; the measured time per unit of the FFT cost proxy is then
     applied to the whole workload's proxy.  Returns (solves/s, threads, description)."""
     from concurrent.futures import ThreadPoolExecutor
@@ -222,7 +223,7 @@ def cpu_sample_rate(cases, budget_s, seed, threads=None):
     def one(i):
         c = dict(cases[i], mixed=0)
         ts = time.perf_counter()
-        C.oracle_solve(c)
+        C.oracle_solve(c, fast=True)
         return time.perf_counter() - ts, fft_proxy(c)
 
     with ThreadPoolExecutor(max_workers=threads) as ex:
@@ -250,9 +251,9 @@ def cpu_sample_rate(cases, budget_s, seed, threads=None):
     mean_proxy = float(np.mean([fft_proxy(c) for c in cases]))
     sec_per_patch = t_sum / p_sum * mean_proxy          # one core, average patch of the workload
     rate = threads / sec_per_patch
-    desc = ("%d patches (sides <= 64) of the workload solved by the oracle in %.1f s wall on %d threads; "
-            "core-seconds per unit of F log2 F (F = doubled FFT grid) applied to the full workload's mix"
-            % (done, wall, threads))
+    desc = ("%d patches (sides <= 64) of the workload solved by the oracle (its baseline build: Stockham FFT) "
+            "in %.1f s wall on %d threads; core-seconds per unit of F log2 F (F = doubled FFT grid) applied to "
+            "the full workload's mix" % (done, wall, threads))
     return rate, threads, desc
 
 

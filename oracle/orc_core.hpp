@@ -280,6 +280,7 @@ inline void fft1d(cplx *a, int n, bool inv) {
     fft_rec(in.data(), 1, a, n, pl.fac.data(), pl, 1, inv, tmp.data());
 }
 
+#ifndef ORC_FAST_FFT
 // 2-D transform of a (nx fastest, ny rows)
 inline void fft2d(std::vector<cplx> &a, int nx, int ny, bool inv) {
     for (int iy = 0; iy < ny; iy++) fft1d(a.data() + (size_t)iy * nx, nx, inv);
@@ -290,6 +291,140 @@ inline void fft2d(std::vector<cplx> &a, int nx, int ny, bool inv) {
         for (int iy = 0; iy < ny; iy++) a[ix + (size_t)iy * nx] = col[iy];
     }
 }
+#else
+// ---------------------------------------------------------------------------------------------
+// Baseline build (-DORC_FAST_FFT): the same transforms by an iterative Stockham autosort FFT
+// (Stockham's self-sorting formulation, as in Van Loan, "Computational Frameworks for the
+// Fast Fourier Transform", 1992, sec. 1.7) with radix-4/2/3/5 butterflies, per-stage
+// twiddle tables and columns transformed in blocks.  It stands in for the optimised FFT
+// library the reference links, so that the timed CPU baseline is not slowed by the simple
+// recursive FFT above; results agree with it to rounding.
+// ---------------------------------------------------------------------------------------------
+struct StockhamPlan {
+    int n = 0;
+    std::vector<int> rad;
+    std::vector<std::vector<cplx>> tw;     // per stage: w^(r k), k < Ns, r < p, w = exp(-2 pi i / (Ns p))
+    std::vector<std::vector<cplx>> roots;  // per stage of a radix above 5: exp(-2 pi i q / p), q < p
+};
+
+inline const StockhamPlan &stockham_plan(int n) {
+    static thread_local std::map<int, StockhamPlan> cache;
+    auto it = cache.find(n);
+    if (it != cache.end()) return it->second;
+    StockhamPlan p; p.n = n;
+    int m = n;
+    for (int f : {4, 2, 3, 5}) while (m % f == 0) { p.rad.push_back(f); m /= f; }
+    for (int f = 7; m > 1; f += 2) while (m % f == 0) { p.rad.push_back(f); m /= f; }
+    int ns = 1;
+    for (int r : p.rad) {
+        std::vector<cplx> t((size_t)ns * r);
+        for (int k = 0; k < ns; k++)
+            for (int q = 0; q < r; q++) {
+                const double a = -2.0 * pi * (double)((long)q * k) / (double)((long)ns * r);
+                t[(size_t)k * r + q] = cplx(std::cos(a), std::sin(a));
+            }
+        p.tw.push_back(std::move(t));
+        std::vector<cplx> ro;
+        if (r > 5)
+            for (int q = 0; q < r; q++) {
+                const double a = -2.0 * pi * (double)q / (double)r;
+                ro.push_back(cplx(std::cos(a), std::sin(a)));
+            }
+        p.roots.push_back(std::move(ro));
+        ns *= r;
+    }
+    return cache.emplace(n, std::move(p)).first->second;
+}
+
+// one Stockham stage of radix p over 'cnt' interleaved transforms (element e of transform t
+// at x[e * cnt + t]); inv: conjugate twiddles and roots
+inline void stockham_stage(const cplx *x, cplx *y, int n, int ns, int p, const cplx *tw, const cplx *roots,
+                           bool inv, int cnt) {
+    const int nb = n / p;
+    const double sg = inv ? 1.0 : -1.0;
+    thread_local std::vector<cplx> vbig, obig;
+    if (p > 16) { vbig.resize(p); obig.resize(p); }
+    for (int j = 0; j < nb; j++) {
+        const int k = j % ns;
+        const int o = (j / ns) * ns * p + k;
+        const cplx *twk = tw + (size_t)k * p;
+        for (int t = 0; t < cnt; t++) {
+            cplx v[16];
+            cplx *vb = (p <= 16) ? v : vbig.data();
+            for (int r = 0; r < p; r++) {
+                cplx a = x[(size_t)(j + r * nb) * cnt + t];
+                if (r > 0 && k > 0) a *= inv ? std::conj(twk[r]) : twk[r];
+                vb[r] = a;
+            }
+            if (p == 2) {
+                const cplx a = vb[0], b = vb[1];
+                vb[0] = a + b; vb[1] = a - b;
+            } else if (p == 4) {
+                const cplx a0 = vb[0] + vb[2], a1 = vb[0] - vb[2], a2 = vb[1] + vb[3], a3 = vb[1] - vb[3];
+                const cplx a3r(-sg * a3.imag(), sg * a3.real());     // a3 * (sg i)
+                vb[0] = a0 + a2; vb[2] = a0 - a2; vb[1] = a1 + a3r; vb[3] = a1 - a3r;
+            } else if (p == 3) {
+                const double c1 = -0.5, s1 = sg * 0.86602540378443864676;
+                const cplx a = vb[0], b = vb[1], c = vb[2];
+                const cplx t1 = b + c, t2 = a + c1 * t1;
+                const cplx t3(-s1 * (b - c).imag(), s1 * (b - c).real());
+                vb[0] = a + t1; vb[1] = t2 + t3; vb[2] = t2 - t3;
+            } else if (p == 5) {
+                const double c1 = 0.30901699437494742410, c2 = -0.80901699437494742410;
+                const double s1 = sg * 0.95105651629515357212, s2 = sg * 0.58778525229247312917;
+                const cplx a = vb[0], b1 = vb[1] + vb[4], b2 = vb[2] + vb[3], d1 = vb[1] - vb[4], d2 = vb[2] - vb[3];
+                const cplx t1 = a + c1 * b1 + c2 * b2, t2 = a + c2 * b1 + c1 * b2;
+                const cplx u1 = s1 * d1 + s2 * d2, u2 = s2 * d1 - s1 * d2;
+                const cplx i1(-u1.imag(), u1.real()), i2(-u2.imag(), u2.real());
+                vb[0] = a + b1 + b2; vb[1] = t1 + i1; vb[4] = t1 - i1; vb[2] = t2 + i2; vb[3] = t2 - i2;
+            } else {
+                cplx out[16];
+                cplx *ob = (p <= 16) ? out : obig.data();
+                for (int q = 0; q < p; q++) {
+                    cplx acc = vb[0];
+                    for (int r = 1; r < p; r++) {
+                        const cplx w = roots[(size_t)((long)r * q % p)];
+                        acc += vb[r] * (inv ? std::conj(w) : w);
+                    }
+                    ob[q] = acc;
+                }
+                for (int q = 0; q < p; q++) vb[q] = ob[q];
+            }
+            for (int r = 0; r < p; r++) y[(size_t)(o + r * ns) * cnt + t] = vb[r];
+        }
+    }
+}
+
+// cnt interleaved transforms of length n in a (element e of transform t at a[e * cnt + t])
+inline void stockham_many(cplx *a, int n, int cnt, bool inv, std::vector<cplx> &scratch) {
+    const StockhamPlan &pl = stockham_plan(n);
+    scratch.resize((size_t)n * cnt);
+    cplx *src = a, *dst = scratch.data();
+    int ns = 1;
+    for (size_t s = 0; s < pl.rad.size(); s++) {
+        stockham_stage(src, dst, n, ns, pl.rad[s], pl.tw[s].data(), pl.roots[s].data(), inv, cnt);
+        ns *= pl.rad[s];
+        std::swap(src, dst);
+    }
+    if (src != a) std::copy(src, src + (size_t)n * cnt, a);
+}
+
+// 2-D transform of a (nx fastest, ny rows): rows one by one, columns in blocks of 16
+inline void fft2d(std::vector<cplx> &a, int nx, int ny, bool inv) {
+    thread_local std::vector<cplx> scratch, blk;
+    for (int iy = 0; iy < ny; iy++) stockham_many(a.data() + (size_t)iy * nx, nx, 1, inv, scratch);
+    const int B = 16;
+    for (int ix0 = 0; ix0 < nx; ix0 += B) {
+        const int w = std::min(B, nx - ix0);
+        blk.resize((size_t)ny * w);
+        for (int iy = 0; iy < ny; iy++)
+            for (int t = 0; t < w; t++) blk[(size_t)iy * w + t] = a[(size_t)iy * nx + ix0 + t];
+        stockham_many(blk.data(), ny, w, inv, scratch);
+        for (int iy = 0; iy < ny; iy++)
+            for (int t = 0; t < w; t++) a[(size_t)iy * nx + ix0 + t] = blk[(size_t)iy * w + t];
+    }
+}
+#endif
 
 // opt_fft_size, m_aijpj.f90:1022-1119: a 2^a 3^b 5^c 7^d >= n found greedily, starting from the next
 // power of two and trading factors while the product stays >= n (not always the smallest such number)

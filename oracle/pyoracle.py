@@ -13,6 +13,7 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libcontact_oracle.so")
+_LIB_FAST_PATH = os.path.join(_HERE, "_build", "libcontact_oracle_fast.so")
 _lib = None
 
 
@@ -83,12 +84,29 @@ def build(quiet=True):
         print(out.stdout)
 
 
-def lib():
+_libs = {}
+
+
+def lib(fast=False):
+    """The oracle library; fast=True the build with the Stockham FFT (the timed CPU
+    baseline), otherwise the parity build."""
     global _lib
-    if _lib is None:
-        if not os.path.exists(_LIB_PATH):
+    key = bool(fast)
+    if key not in _libs:
+        path = _LIB_FAST_PATH if key else _LIB_PATH
+        if not os.path.exists(path):
             build()
-        _lib = ctypes.CDLL(_LIB_PATH)
+        _l = ctypes.CDLL(path)
+        _setup(_l)
+        _libs[key] = _l
+        if not key:
+            _lib = _l
+    return _libs[key]
+
+
+def _setup(_lib):
+    """ctypes prototypes of the oracle's entry points."""
+    if True:
         _lib.orc_calculate.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(Result)]
         _lib.orc_calculate.restype = ctypes.c_int
         _lib.orc_default_problem.argtypes = [ctypes.POINTER(Problem)]
@@ -116,11 +134,11 @@ def default_problem():
     return pb
 
 
-def solve(pb, h=None, warm=None, fields=True):
+def solve(pb, h=None, warm=None, fields=True, fast=False):
     """Solve one case; returns a dict of scalars and (optionally) fields.
 
     h: element-wise undeformed distance (ibase 9); warm: dict(igs, pn, px, py)
-    used as initial estimate when pb.iestim > 0."""
+    used as initial estimate when pb.iestim > 0; fast: the baseline build (Stockham FFT)."""
     keep = []
     if h is not None:
         hh = np.ascontiguousarray(h, dtype=np.float64).ravel()
@@ -147,7 +165,7 @@ def solve(pb, h=None, warm=None, fields=True):
             setattr(res, k, _dptr(arrs[k]))
         arrs["igs"] = np.zeros(n, dtype=np.int32)
         res.igs = arrs["igs"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
-    lib().orc_calculate(ctypes.byref(pb), ctypes.byref(res))
+    lib(fast).orc_calculate(ctypes.byref(pb), ctypes.byref(res))
     out = {k: getattr(res, k) for k, _ in Result._fields_ if k not in
            ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h", "igs")}
     out.update(arrs)

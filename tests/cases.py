@@ -222,7 +222,8 @@ def to_oracle(case):
     return pb, case.get("h")
 
 
-def oracle_solve(case):
+def oracle_solve(case, fast=False):
+    """The oracle's solve of a case; fast: its baseline build (Stockham FFT)."""
     import pyoracle as po
     pb, h = to_oracle(case)
-    return po.solve(pb, h=h)
+    return po.solve(pb, h=h, fast=fast)

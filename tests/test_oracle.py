@@ -284,3 +284,23 @@ def test_perfc_against_published_run(oracle, name):
         assert (o["ncon"], o["itcg"]) == (ref["ncon"], ref["itcg"])
     else:
         assert o["solver"] == 2 and (o["nslip"], o["itgs"]) == (ref["nslp"], ref["itgs"])
+
+
+def test_baseline_build_equals_parity_build(oracle):
+    """The oracle's baseline build (Stockham FFT, timed as the CPU baseline) solves like the
+    parity build: same iterations and element division, forces within 1e-12, tractions
+    within 1e-12 of pmax, on steady rolling (GDsteady, SteadyGS), shift and a rail geometry."""
+    from contact_gb300 import inp
+    perfc = [c for c in _load("perfc_cases.json")["cases"] if c["name"] == "norm_problm_1p"][0]
+    for case in (C.config0(gausei=5, eps=1e-10, mx=31, my=27), C.config0(gausei=0, eps=1e-8, mx=25, my=25),
+                 C.cattaneo_case(2, 0.008155), inp.materialize(perfc["case"])):
+        a = C.oracle_solve(case)
+        b = C.oracle_solve(case, fast=True)
+        assert (a["ierror"], a["itcg"], a["itgs"]) == (b["ierror"], b["itcg"], b["itgs"])
+        assert np.array_equal(a["igs"], b["igs"])
+        scale = max(abs(a["fn"]), 1e-30)
+        for k in ("fn", "fx", "fy"):
+            assert abs(a[k] - b[k]) <= 1e-12 * scale, k
+        pmax = np.abs(a["pn"]).max()
+        for k in ("pn", "px", "py"):
+            assert np.abs(a[k] - b[k]).max() <= 1e-12 * pmax, k
