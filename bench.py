@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--large", action="store_true",
                     help="large single patch: 1024^2 rough surface (Fn 150 kN, creepages 0.003/0/0.3 rad/m, "
                          "mu 0.25), FP64 against FP32 convolutions + FP64 refinement, solved by a CTA group")
+    ap.add_argument("--perfc", action="store_true",
+                    help="the reference's own performance inputs (perfc_test: normal problems 71x81 to 575x647, "
+                         "shift problems), FP64, each through cntc_calculate, against the published 2016 timings")
     ap.add_argument("--large-side", type=int, default=1024)
     ap.add_argument("--large-maxgs", type=int, default=3000)
     ap.add_argument("--large-eps", type=float, default=1e-6,
@@ -617,6 +620,55 @@ def run_large(args, dist):
             "clocks": clk, "gpu_launches": int(a["launches"])}
 
 
+# ------------------------------------------------------------------------------------------
+# the reference's performance inputs (perfc_test/*.inp, committed in parsed form): each case
+# solved in FP64 through cntc_calculate (host buffers, set-up and copies included), against
+# the counts and wall-clock seconds of the reference's published run (1 thread, 2016)
+# ------------------------------------------------------------------------------------------
+def run_perfc(args, dist):
+    import torch
+    import contact_gb300 as cg
+    from contact_gb300 import inp
+    torch.cuda.set_device(dist.local)
+    cg.load()
+    with open(os.path.join(ROOT, "tests", "golden", "perfc_cases.json")) as f:
+        gold = json.load(f)["cases"]
+    rows = []
+    # one warm-up solve (kernel attributes, streams); every timed problem is new, so it
+    # computes its influence coefficients like the reference's single run
+    cg.setup_case(199, 1, inp.materialize(gold[0]["case"]))
+    cg.calculate(199, 1)
+    cg.finalize(199)
+    for k, g in enumerate(gold):
+        case = inp.materialize(g["case"])
+        ire = 200 + k
+        cg.setup_case(ire, 2, case)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ierr = cg.calculate(ire, 2)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        r = cg.results(ire, 2)
+        ref = g["reference"]
+        row = {"name": g["name"], "grid": case["potprm"][:2], "ierror": ierr, "s": dt, "ref_s": ref["wall_s"],
+               "speedup": ref["wall_s"] / dt if dt > 0 else None, "ctas": int(cg.getsolverstats(ire, 2)["ctas"])}
+        if "ncon" in ref:
+            row.update(ncon=r["ncon"], itcg=r["itcg"], ref_ncon=ref["ncon"], ref_itcg=ref["itcg"])
+        else:
+            row.update(nslip=r["nslip"], itcg=r["itgs"], ref_nslip=ref["nslp"], ref_itcg=ref["itgs"])
+        rows.append(row)
+        cg.finalize(ire)
+    if dist.rank != 0:
+        return None
+    tot, tot_ref = sum(r["s"] for r in rows), sum(r["ref_s"] for r in rows)
+    return {"metric": METRIC, "value": len(rows) / tot, "unit": UNIT, "n_gpus": dist.world, "steps": 1,
+            "warmup": 1, "ms_per_step": tot * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "the reference's performance inputs (perfc_test)", "mode": "perfc",
+            "config": {"workload": "perfc_test normal problems 1p-8p, 1f-4f and shift problems 1s-8s, FP64, "
+                                   "one cntc_calculate each"},
+            "total_s": tot, "reference_total_s": tot_ref, "cases": rows}
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -625,6 +677,8 @@ def main():
             out = run_serving(args, dist)
         elif args.large and args.impl != "reference":
             out = run_large(args, dist)
+        elif args.perfc and args.impl != "reference":
+            out = run_perfc(args, dist)
         else:
             out = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
         if out is not None:
