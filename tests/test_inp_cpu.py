@@ -78,3 +78,79 @@ def test_perfc_fixture_matches_the_inputs():
     fresh = _read("perfc_test/%s.inp" % g["name"])[0]
     _same_case(fresh, g["case"])
     assert np.array_equal(fresh["h"], c["h"])
+
+
+DECK = """
+ 3  MODULE
+  {pbtnfs}      P-B-T-N-F-S
+  022020        L-D-C-M-Z-E
+  0000341     H-G-I-A-O-W-R
+   200  100  30  1  1.0E-08           MAXGS, MAXIN, MAXNR, MAXOUT, EPS
+   9.1954   {cksi}   0.0   0.0         FN, CKSI, CETA, CPHI
+   0.4  0.4                            FSTAT, FKIN
+{veloc}   0.42  0.42  200.  200.       POISS 1,2,  GG 1,2
+   {ipotcn}                            IPOTCN
+   {potline}
+{geom}
+ 0  MODULE
+"""
+
+
+def _deck(ipotcn, potline, geom, tang=1, cksi=0.008155):
+    veloc = "   0.0  0.13333  1000.       CHI, DQ, VELOC\n" if tang == 3 else ""
+    return DECK.format(pbtnfs="20%d100" % tang, cksi=cksi, veloc=veloc, ipotcn=ipotcn, potline=potline, geom=geom)
+
+
+QUAD = "   1   1                IBASE, IPLAN\n   0.01 0.0 0.01 0.0 0.0 0.0    B1..B6"
+
+
+def test_potential_contact_forms_agree(oracle):
+    """IPOTCN 1 (lower-left corner and spacing), 2 (corners), 3 (first centre and spacing)
+    and 4 (first and last centres) describing the same 19x19 grid read into the same
+    element centres, and the oracle gives the same solution for each."""
+    forms = [(1, "19 19 -1.26667 -1.26667 0.13333 0.13333"),
+             (2, "19 19 -1.26667 -1.26667 1.26660 1.26660"),
+             (3, "19 19 -1.200005 -1.200005 0.13333 0.13333"),
+             (4, "19 19 -1.200005 -1.200005 1.199935 1.199935")]
+    res = []
+    for ip, line in forms:
+        c = inp.read_inp(_deck(ip, line, QUAD))[0]
+        assert c["ipotcn"] == ip and c["tang"] == 1 and c["prmudf"] == pytest.approx([0.01, 0, 0.01, 0, 0, 0])
+        res.append(C.oracle_solve(c))
+    for r in res[1:]:
+        assert np.array_equal(r["igs"], res[0]["igs"])
+        assert r["fx"] == pytest.approx(res[0]["fx"], rel=1e-9) and r["fn"] == pytest.approx(res[0]["fn"], rel=1e-12)
+
+
+def test_geometry_forms_agree(oracle):
+    """IBASE 1 (quadratic), 3 (no sines, x^2/p7 + y^2/p8) and 9 (element-wise) describing
+    the same undeformed distance give the same solution."""
+    pot = "19 19 -1.26667 -1.26667 0.13333 0.13333"
+    a = inp.read_inp(_deck(1, pot, QUAD))[0]
+    b = inp.read_inp(_deck(1, pot, "   3   1     IBASE, IPLAN\n   0 0 0 0 0 0 100.0 100.0"))[0]
+    x = -1.26667 + (np.arange(19) + 0.5) * 0.13333
+    X, Y = np.meshgrid(x, x)
+    h = 0.01 * X ** 2 + 0.01 * Y ** 2
+    body = "\n".join(" ".join("%.17g" % v for v in h.ravel()[k:k + 5]) for k in range(0, 361, 5))
+    c = inp.read_inp(_deck(1, pot, "   9   1     IBASE, IPLAN\n" + body))[0]
+    assert np.allclose(b["h"], h.ravel(), rtol=0, atol=1e-15) and np.allclose(c["h"], h.ravel(), rtol=0, atol=0)
+    ra, rb, rc = (C.oracle_solve(z) for z in (a, b, c))
+    for r in (rb, rc):
+        assert np.array_equal(r["igs"], ra["igs"]) and r["fx"] == pytest.approx(ra["fx"], rel=1e-9)
+
+
+def test_rolling_case_reads_the_step_line():
+    """T=3 reads CHI, DQ, VELOC; values a later case omits keep their previous value."""
+    text = _deck(1, "19 19 -1.26667 -1.26667 0.13333 0.13333", QUAD, tang=3, cksi=-0.001)
+    c = inp.read_inp(text)[0]
+    assert c["tang"] == 3 and c["dq"] == pytest.approx(0.13333) and c["veloc"] == 1000.0 and "chi" not in c
+    two = text.replace(" 0  MODULE", """ 3  MODULE
+  203100      P-B-T-N-F-S
+  000000      L-D-C-M-Z-E
+  0100341     H-G-I-A-O-W-R
+   9.1954  -0.002  0.0  0.0      FN, CKSI, CETA, CPHI
+   0.3  0.3                      FSTAT, FKIN
+ 0  MODULE""")
+    cs = inp.read_inp(two)
+    assert len(cs) == 2 and cs[1]["cksi"] == -0.002 and cs[1]["fstat"] == 0.3
+    assert cs[1]["maxgs"] == 200 and cs[1]["potprm"] == cs[0]["potprm"] and cs[1]["prmudf"] == cs[0]["prmudf"]
