@@ -12,7 +12,8 @@ non-numeric word, required values may continue on the next lines, Fortran number
 Values that a case does not repeat keep their previous value, as in the program: a case
 with G=1 keeps the solver settings, D=0 the potential contact, Z<2 the geometry.
 
-Supported: control digits of module 3 with Coulomb friction (L=0, V=0), elastic materials
+Supported: control digits of module 3, creepages or total forces prescribed (F=0, 1, 2),
+with Coulomb friction (L=0, V=0), elastic materials
 (M=0), no thin-sheet, heat, extra-rigid-slip or subsurface inputs; potential contact
 IPOTCN -3..-1 and 1..4; geometry IBASE 1 (quadratic), 2 (circular in x, tabulated in y),
 3 (sines in x) and 9 (element-wise), planform IPLAN 1.  IBASE 2 and 3 are evaluated here
@@ -179,8 +180,6 @@ def read_inp(text):
         if xh["X"] >= 1:
             L.read("iI")
         bad = []
-        if pb["F"] != 0:
-            bad.append("total forces prescribed (F=%d)" % pb["F"])
         if vd["V"] != 0 or vd["L"] not in (0, 1):
             bad.append("friction law V=%d L=%d" % (vd["V"], vd["L"]))
         if vd["M"] != 0 or pb["B"] == 1:
@@ -211,7 +210,16 @@ def read_inp(text):
             c["pen"] = kin[0]
         else:
             c["fn"] = kin[0]
-        c["cksi"], c["ceta"], c["cphi"] = kin[1], kin[2], kin[3]
+        # m_sinput.f90:720-733: F=0 creepages, F=1 Fx/(mu Fn) and ceta, F=2 Fx/(mu Fn) and Fy/(mu Fn)
+        if pb["F"] == 0:
+            c["cksi"], c["ceta"] = kin[1], kin[2]
+        elif pb["F"] == 1:
+            c["fxrel"], c["ceta"] = kin[1], kin[2]
+        else:
+            c["fxrel"], c["fyrel"] = kin[1], kin[2]
+        c["cphi"] = kin[3]
+        if pb["F"] != 0:
+            c["force3"] = pb["F"]
         if vd["L"] != 1:
             st["fstat"] = L.read("dd")[0]
         if vd["C"] in (2, 3, 4, 9):

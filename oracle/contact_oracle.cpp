@@ -37,7 +37,16 @@ struct Case {
     Inflcf cs, cv, ms;
     int itnorm = 0, ittang = 0, itcg = 0, itgs = 0, solver_eff = 0;
     bool unsupported = false, aborted = false;
+    // sensitivities sens(iout, iin) (t_output%sens, m_hierarch_data.f90:122-128, 814):
+    // iout 0..3 = Fn, Fx, Fy, Mz; iin 0..3 = pen, cksi, ceta, cphi
+    double sens[4][4] = {};
+    // Newton-Raphson history on the creepages: per iteration ittang, itnr, cksi, Fx/(mu Fn),
+    // ceta, Fy/(mu Fn), solver iterations
+    std::vector<double> nr_hist;
 };
+
+constexpr int iout_fn = 0, iout_fx1 = 1, iout_fy1 = 2, iout_mz1 = 3;
+constexpr int iin_dpen = 0, iin_dksi1 = 1, iin_deta1 = 2, iin_dphi1 = 3;
 
 // set_tang_rhs, m_sdis.f90:498-583 (M=0, no extra rhs)
 void set_tang_rhs(Case &c) {
@@ -137,6 +146,15 @@ void init_curr_data(Case &c, int ihertz) {
         for (int ii = 0; ii < c.npot; ii++) if (c.igs.el[ii] >= Adhes) c.igs.el[ii] = Adhes;
     for (int ii = 0; ii < c.npot; ii++) if (c.hs.vn(ii) > (double)1e29f) c.igs.el[ii] = Exter;
     areas(c.igs);
+    // initial sensitivities and creepages, m_sdis.f90:754-766
+    if (pb->iestim == 0) for (int io = iout_fx1; io <= iout_mz1; io++) c.sens[io][iin_dpen] = 0.0;
+    if (pb->iestim == 0 && (pb->norm != 1 || ihertz != 0)) c.sens[iout_fn][iin_dpen] = 0.0;
+    if (pb->iestim == 0 || pb->iestim == 2) {
+        if (pb->force3 >= 1) c.cksi = 1e-6;
+        if (pb->force3 == 2) c.ceta = 0.0;
+        for (int io = iout_fn; io <= iout_mz1; io++)
+            for (int ji = iin_dksi1; ji <= iin_dphi1; ji++) c.sens[io][ji] = 0.0;
+    }
 }
 
 // stang_rhs, m_stang.f90:749-951 (steady rolling / first step, pv = 0)
@@ -155,20 +173,24 @@ void stang_rhs(Case &c, const std::vector<int> &iel, const std::vector<double> &
             wsfix.c[ik - 1][ii] = wsrig.c[ik - 1][ii] + usn.c[ik - 1][ii] - uvn.c[ik - 1][ii];
 }
 
-// tang_solver, m_solvpt.f90:382-493
-int tang_solver(Case &c, const GF3 &wstot, int &info1, double &err) {
+// tang_solver, m_solvpt.f90:382-493; is_sens: the sensitivity solve (mxsens, epsens)
+int tang_solver(Case &c, const GF3 &wstot, int &info1, double &err, bool is_sens = false) {
     TangCtx &tc = c.tc;
     int it = 0;
     bool bad = false;
+    int maxit = is_sens ? c.pb->mxsens : tc.maxgs;
+    double eps = is_sens ? c.pb->epsens : tc.eps;
     if (c.solver_eff == isolv_stdygs) {
-        it = stdygs(tc, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, tc.eps, tc.maxgs, tc.omegah, tc.omegas, info1, err, bad);
+        it = stdygs(tc, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, eps, maxit, tc.omegah, tc.omegas, info1, err, bad,
+                    is_sens);
     } else if (c.solver_eff == isolv_gdstdy) {
         bool lstagn = false;
-        it = gdsteady(tc, tc.maxgs, tc.eps, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, err, lstagn, bad);
+        it = gdsteady(tc, maxit, eps, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, err, lstagn, bad);
         if (!bad && lstagn)
-            it = stdygs(tc, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, tc.eps, tc.maxgs, tc.omegah, tc.omegas, info1, err, bad);
+            it = stdygs(tc, wstot, c.cs, c.igs, c.mus, c.ps, c.ss, eps, maxit, tc.omegah, tc.omegas, info1, err, bad,
+                        is_sens);
     } else if (c.solver_eff == isolv_tangcg) {
-        it = tangcg(tc, tc.maxgs, tc.eps, wstot, c.cs, c.ms, c.igs, c.mus, c.ps, c.ss, err, bad);
+        it = tangcg(tc, maxit, eps, wstot, c.cs, c.ms, c.igs, c.mus, c.ps, c.ss, err, bad, is_sens);
     } else {
         c.unsupported = true;
         return 0;
@@ -177,7 +199,234 @@ int tang_solver(Case &c, const GF3 &wstot, int &info1, double &err) {
     return it;
 }
 
-// stang, m_stang.f90:28-746 (Coulomb friction, creepages prescribed F=0)
+// relative total forces Fx/(mu Fn), Fy/(mu Fn) of the current tractions
+void rel_forces(const Case &c, double &fx, double &fy) {
+    fx = c.dxdy * gf_sum(AllElm, c.ps, ikX, c.igs) / (c.muscal * c.fntrue);
+    fy = c.dxdy * gf_sum(AllElm, c.ps, ikY, c.igs) / (c.muscal * c.fntrue);
+}
+
+// solvpt, m_solvpt.f90:51-378: one tangential solve for the current element division; when
+// total forces are prescribed (F=1: Fx, F=2: Fx and Fy) a Newton-Raphson iteration on cksi
+// (and ceta) around it, with the derivatives taken as secants of its own steps.
+int solvpt(Case &c, int ittang, const std::vector<int> &iel, const std::vector<double> &facdt, const GF3 &wsfix,
+           int &info1, double &err) {
+    const orc_problem *pb = c.pb;
+    const int npot = c.npot, f3 = pb->force3;
+    const double dq = c.dq;
+    int nadh, nslip, nplast, nexter;
+    areas(c.igs);
+    eldiv_count(c.igs, nadh, nslip, nplast, nexter);
+    GF3 wstot; wstot.init(npot);
+    gf_copy(AllElm, wsfix, wstot, ikTANG, c.igs);
+    if (f3 >= 1) for (int ii : iel) wstot.vx(ii) += facdt[ii] * c.cksi * dq;
+    if (f3 >= 2) for (int ii : iel) wstot.vy(ii) += facdt[ii] * c.ceta * dq;
+    info1 = 0;
+    int it = tang_solver(c, wstot, info1, err);
+    if (c.unsupported || c.aborted) return it;
+    double fxkp1, fykp1;
+    rel_forces(c, fxkp1, fykp1);
+    int itgs = it;
+    eldiv_count(c.igs, nadh, nslip, nplast, nexter);
+    auto record = [&](int itnr, int its) {
+        double row[7] = {(double)ittang, (double)itnr, c.cksi, fxkp1, c.ceta, fykp1, (double)its};
+        c.nr_hist.insert(c.nr_hist.end(), row, row + 7);
+    };
+    double (&sens)[4][4] = c.sens;
+    if (f3 >= 1 && info1 <= 1) {
+        int itnr = 0;
+        record(itnr, it);
+        double df = std::fabs(pb->fxrel - fxkp1);
+        if (f3 >= 2) df += std::fabs(pb->fyrel - fykp1);
+        while (df > c.tc.eps && itnr < pb->maxnr && info1 <= 1) {
+            itnr++;
+            double dfx = pb->fxrel - fxkp1, dfy = pb->fyrel - fykp1;
+            double dcksi = 0.0, dceta = 0.0;
+            if (f3 == 1) {
+                dceta = 0.0;
+                if (std::fabs(sens[iout_fx1][iin_dksi1]) > (double)1e-6f) dcksi = dfx / sens[iout_fx1][iin_dksi1];
+                else dcksi = (double)0.00003f;
+            } else {
+                double det = sens[iout_fx1][iin_dksi1] * sens[iout_fy1][iin_deta1] -
+                             sens[iout_fy1][iin_dksi1] * sens[iout_fx1][iin_deta1];
+                if (det > c.tc.eps) {
+                    dcksi = (sens[iout_fy1][iin_deta1] * dfx - sens[iout_fy1][iin_dksi1] * dfy) / det;
+                    dceta = (-sens[iout_fx1][iin_deta1] * dfx + sens[iout_fx1][iin_dksi1] * dfy) / det;
+                } else {
+                    dcksi = 0.000003;
+                    dceta = 0.000003;
+                }
+            }
+            int ithalf[2] = {0, 0};
+            for (int ifxy = 1; ifxy <= f3; ifxy++) {
+                double fxk = fxkp1, fyk = fykp1;
+                if (ifxy == 1) {
+                    c.cksi += dcksi;
+                    for (int ii : iel) wstot.vx(ii) += facdt[ii] * dcksi * dq;
+                } else {
+                    c.ceta += dceta;
+                    for (int ii : iel) wstot.vy(ii) += facdt[ii] * dceta * dq;
+                }
+                it = tang_solver(c, wstot, info1, err);
+                if (c.unsupported || c.aborted) return itgs + it;
+                rel_forces(c, fxkp1, fykp1);
+                itgs += it;
+                ithalf[ifxy - 1] = it;
+                eldiv_count(c.igs, nadh, nslip, nplast, nexter);
+                double dfxk = fxkp1 - fxk, dfyk = fykp1 - fyk;
+                double scl = c.muscal * c.fntrue / ((nadh + nslip + nplast) * c.dxdy);
+                if (ifxy == 1) {
+                    if (nadh > 0) {
+                        double dpxavg = dfxk * scl;
+                        if (sens[iout_fx1][iin_dksi1] == 0.0 || std::fabs(dpxavg) > 10.0 * err)
+                            sens[iout_fx1][iin_dksi1] = dfxk / dcksi;
+                        double dpyavg = dfyk * scl;
+                        if (std::fabs(dpyavg) > 10.0 * err) sens[iout_fy1][iin_dksi1] = dfyk / dcksi;
+                    } else if (std::fabs(sens[iout_fx1][iin_dksi1]) < (double)1e-6f) {
+                        sens[iout_fx1][iin_dksi1] = fxkp1 / c.cksi;
+                    }
+                } else {
+                    if (nadh > 0) {
+                        double dpxavg = dfxk * scl;
+                        if (std::fabs(dpxavg) > 10.0 * err) sens[iout_fx1][iin_deta1] = dfxk / dceta;
+                        double dpyavg = dfyk * scl;
+                        if (sens[iout_fy1][iin_deta1] == 0.0 || std::fabs(dpyavg) > 10.0 * err)
+                            sens[iout_fy1][iin_deta1] = dfyk / dceta;
+                    } else if (std::fabs(sens[iout_fy1][iin_deta1]) < (double)1e-6f) {
+                        sens[iout_fy1][iin_deta1] = fykp1 / c.ceta;
+                    }
+                }
+                df = std::fabs(pb->fxrel - fxkp1);
+                if (f3 >= 2) df += std::fabs(pb->fyrel - fykp1);
+            }
+            record(itnr, ithalf[0] + ithalf[1]);
+        }
+        // the reference adds the Newton-Raphson residual to the error estimate with the element
+        // code Slip (= 2) in the place of the number of slip elements (m_solvpt.f90:361)
+        err += 2.0 * df * c.muscal * c.fntrue / ((nadh + Slip + nplast) * c.dxdy);
+    } else {
+        sens[iout_fx1][iin_dksi1] = 0.0; sens[iout_fy1][iin_dksi1] = 0.0;
+        sens[iout_fx1][iin_deta1] = 0.0; sens[iout_fy1][iin_deta1] = 0.0;
+    }
+    return itgs;
+}
+
+// linrol, m_hertz.f90:1147-1247: Kalker's creepage coefficients C11, C22, C23 of the linear
+// theory for an elliptic contact with semi-axes ratio a/b, from his table of Cij at
+// nu = 0, 1/4, 1/2 (Kalker 1990, table E.3) with the asymptotes for g = min(a/b, b/a) < 0.1.
+// The table holds single-precision constants, as the reference's data statement does.
+void linrol(double nu, double aob, double &cxx, double &cyy, double &cyz) {
+    static const float cij[2][10][3][3] = {      // [a<b | a>b][g row][C11, C22, C23][nu 0, 1/4, 1/2]
+        {{{2.51f, 3.31f, 4.85f}, {2.51f, 2.52f, 2.53f}, {.334f, .473f, .731f}},
+         {{2.59f, 3.37f, 4.81f}, {2.59f, 2.63f, 2.66f}, {.483f, .603f, .809f}},
+         {{2.68f, 3.44f, 4.80f}, {2.68f, 2.75f, 2.81f}, {.607f, .715f, .889f}},
+         {{2.78f, 3.53f, 4.82f}, {2.78f, 2.88f, 2.98f}, {.720f, .823f, .977f}},
+         {{2.88f, 3.62f, 4.83f}, {2.88f, 3.01f, 3.14f}, {.827f, .929f, 1.07f}},
+         {{2.98f, 3.72f, 4.91f}, {2.98f, 3.14f, 3.31f}, {.930f, 1.03f, 1.18f}},
+         {{3.09f, 3.81f, 4.97f}, {3.09f, 3.28f, 3.48f}, {1.03f, 1.14f, 1.29f}},
+         {{3.19f, 3.91f, 5.05f}, {3.19f, 3.41f, 3.65f}, {1.13f, 1.25f, 1.40f}},
+         {{3.29f, 4.01f, 5.12f}, {3.29f, 3.54f, 3.82f}, {1.23f, 1.36f, 1.51f}},
+         {{3.40f, 4.12f, 5.20f}, {3.40f, 3.67f, 3.98f}, {1.33f, 1.47f, 1.63f}}},
+        {{{10.7f, 11.7f, 12.9f}, {10.7f, 12.8f, 16.0f}, {12.2f, 14.6f, 18.0f}},
+         {{6.96f, 7.78f, 8.82f}, {6.96f, 8.14f, 9.79f}, {5.72f, 6.63f, 7.89f}},
+         {{5.57f, 6.34f, 7.34f}, {5.57f, 6.40f, 7.51f}, {3.79f, 4.32f, 5.01f}},
+         {{4.84f, 5.57f, 6.57f}, {4.84f, 5.48f, 6.31f}, {2.88f, 3.24f, 3.70f}},
+         {{4.37f, 5.10f, 6.11f}, {4.37f, 4.90f, 5.56f}, {2.35f, 2.62f, 2.96f}},
+         {{4.06f, 4.78f, 5.80f}, {4.06f, 4.50f, 5.04f}, {2.01f, 2.23f, 2.50f}},
+         {{3.82f, 4.54f, 5.58f}, {3.82f, 4.21f, 4.67f}, {1.76f, 1.95f, 2.18f}},
+         {{3.65f, 4.36f, 5.42f}, {3.65f, 3.99f, 4.39f}, {1.58f, 1.75f, 1.94f}},
+         {{3.51f, 4.22f, 5.30f}, {3.51f, 3.81f, 4.16f}, {1.44f, 1.59f, 1.77f}},
+         {{3.40f, 4.12f, 5.20f}, {3.40f, 3.67f, 3.98f}, {1.33f, 1.47f, 1.63f}}}};
+    int icase;
+    double g;
+    if (aob <= 1.0) { g = aob; icase = 0; } else { g = 1.0 / aob; icase = 1; }
+    if (icase == 0 && g < 0.101) {
+        cxx = pi * pi / 4.0 / (1.0 - nu);
+        cyy = pi * pi / 4.0;
+        cyz = pi * std::sqrt(g) / 3.0 / (1.0 - nu) * (1.0 + nu * (std::log(16.0 / g) - 5.0));
+    } else if (icase == 1 && g < 0.101) {
+        double al = std::log(16.0 / (g * g));
+        cxx = 2.0 * pi / (al - 2.0 * nu) / g * (1.0 + (3.0 - std::log(4.0)) / (al - 2.0 * nu));
+        cyy = 2.0 * pi / g * (1.0 + (1.0 - nu) * (3.0 - std::log(4.0)) / ((1.0 - nu) * al + 2.0 * nu)) /
+              ((1.0 - nu) * al + 2.0 * nu);
+        cyz = 2.0 * pi / 3.0 / std::pow(g, 1.5) / ((1.0 - nu) * al - 2.0 + 4.0 * nu);
+    } else {
+        int irow = (int)(10.0 * g - 0.005);            // 1-based row, truncated as an integer assignment
+        double fac = 10.0 * g - (double)(float)irow;
+        double cc[3];
+        for (int ic = 0; ic < 3; ic++) {
+            double cn[3];
+            for (int in = 0; in < 3; in++)
+                cn[in] = fac * (double)cij[icase][irow][ic][in] + (1.0 - fac) * (double)cij[icase][irow - 1][ic][in];
+            cc[ic] = (nu - 0.25) * (nu - 0.50) * 8.0 / cn[0] - (nu - 0.50) * nu * 16.0 / cn[1] +
+                     nu * (nu - 0.25) * 8.0 / cn[2];
+        }
+        cxx = 1.0 / cc[0]; cyy = 1.0 / cc[1]; cyz = 1.0 / cc[2];
+    }
+}
+
+// char_creep, m_solvpt.f90:497-540: characteristic creepages from the linear theory, with the
+// contact's effective radius from its area and its semi-axes from the element bounding box
+void char_creep(Case &c, double &ch_ksi, double &ch_eta, double &ch_phi) {
+    int nadh, nslip, nplast, nexter;
+    eldiv_count(c.igs, nadh, nslip, nplast, nexter);
+    int ncon = nadh + nslip + nplast;
+    double rc = std::sqrt((double)(float)ncon * c.dx * c.dy / pi);
+    areas(c.igs);
+    double a = (double)(float)std::max(1, c.igs.ixmax - c.igs.ixmin + 1) * c.dx * 0.5;
+    double b = (double)(float)std::max(1, c.igs.iymax - c.igs.iymin + 1) * c.dy * 0.5;
+    double c11, c22, c23;
+    linrol(c.nu, a / b, c11, c22, c23);
+    ch_ksi = c.pb->fstat * c.fntrue / (rc * rc * c.ga * c11);
+    ch_eta = c.pb->fstat * c.fntrue / (rc * rc * c.ga * c22);
+    ch_phi = c.pb->fstat * c.fntrue / (rc * rc * rc * c.ga * c23);
+}
+
+// sens_tang, m_solvpt.f90:544-796: d(Fx, Fy, Mz) / d(cksi, ceta, cphi) by one extra solve per
+// creepage, perturbed by 1e-4 of its characteristic size and started from the solution,
+// which is restored afterwards
+void sens_tang(Case &c, const std::vector<int> &iel, const std::vector<double> &facdt, const GF3 &wsfix) {
+    const int npot = c.npot, f3 = c.pb->force3;
+    double fxrel, fyrel;
+    rel_forces(c, fxrel, fyrel);
+    auto moment = [&]() {
+        double dx_y = 0, dy_x = 0;
+        for (int ii = 0; ii < npot; ii++) { dx_y += c.ps.vx(ii) * c.g.y[ii]; dy_x += c.ps.vy(ii) * c.g.x[ii]; }
+        return c.dxdy * (-dx_y + dy_x);
+    };
+    double mztrue = moment();
+    double ch[3];
+    char_creep(c, ch[0], ch[1], ch[2]);
+    GF3 wstot; wstot.init(npot);
+    gf_copy(AllElm, wsfix, wstot, ikTANG, c.igs);
+    if (f3 >= 1) for (int ii : iel) wstot.vx(ii) += facdt[ii] * c.cksi * c.dq;
+    if (f3 >= 2) for (int ii : iel) wstot.vy(ii) += facdt[ii] * c.ceta * c.dq;
+    for (int icrp = iin_dksi1; icrp <= iin_dphi1; icrp++) {
+        GF3 wsloc = wstot;
+        double dcrp = 0.0001 * ch[icrp - iin_dksi1];
+        for (int ii : iel) {
+            if (icrp == iin_dksi1) wsloc.vx(ii) += facdt[ii] * dcrp * c.dq;
+            else if (icrp == iin_deta1) wsloc.vy(ii) += facdt[ii] * dcrp * c.dq;
+            else {
+                wsloc.vx(ii) -= facdt[ii] * dcrp * c.g.y[ii] * c.dq;
+                wsloc.vy(ii) += facdt[ii] * dcrp * c.g.x[ii] * c.dq;
+            }
+        }
+        Eldiv igs0 = c.igs;
+        GF3 ps0 = c.ps, us0 = c.us, ss0 = c.ss;
+        int info1 = 0; double err = 0.0;
+        tang_solver(c, wsloc, info1, err, true);
+        if (c.unsupported || c.aborted) return;
+        double fxloc, fyloc;
+        rel_forces(c, fxloc, fyloc);
+        double mzloc = moment();
+        c.sens[iout_fx1][icrp] = (fxloc - fxrel) / dcrp;
+        c.sens[iout_fy1][icrp] = (fyloc - fyrel) / dcrp;
+        c.sens[iout_mz1][icrp] = (mzloc - mztrue) / dcrp;
+        c.igs = igs0; c.ps = ps0; c.us = us0; c.ss = ss0;
+    }
+}
+
+// stang, m_stang.f90:28-746 (Coulomb friction)
 int stang(Case &c) {
     const orc_problem *pb = c.pb;
     TangCtx &tc = c.tc;
@@ -218,12 +467,8 @@ int stang(Case &c) {
     while (!zready && ittang < tc.maxin) {
         ittang++;
         zready = true;
-        // solvpt, m_solvpt.f90:51-378 (F=0)
-        areas(c.igs);
-        GF3 wstot; wstot.init(npot);
-        gf_copy(AllElm, wsfix, wstot, ikTANG, c.igs);
         int info = 0; double errpt = 0.0;
-        int it = tang_solver(c, wstot, info, errpt);
+        int it = solvpt(c, ittang, iel, facdt, wsfix, info, errpt);
         if (c.unsupported || c.aborted) return -1;
         itgs += it;
         if (info >= 3) { zready = true; ittang = -1; }
@@ -262,6 +507,10 @@ int stang(Case &c) {
     }
     if (!zready) ittang = -1;
     c.itgs = itgs;
+    if (pb->sens >= 3) {
+        sens_tang(c, iel, facdt, wsfix);
+        if (c.unsupported || c.aborted) return -1;
+    }
     return ittang;
 }
 
@@ -308,6 +557,7 @@ void orc_default_problem(orc_problem *pb) {
     pb->fstat = 0.3; pb->fkin = 0.3;
     pb->veloc = 1e3; pb->chi = 0.0; pb->dq = -1.0;
     pb->ipotcn = -3; pb->ibase = 1;
+    pb->sens = 1; pb->mxsens = 30; pb->epsens = 1e-4;                                   // solv_init
 }
 
 int orc_opt_fft_size(int n) { return opt_fft_size(n); }
@@ -491,7 +741,8 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
         } else {
             int itcg = 0;
             nc.fntrue = c.fntrue;
-            it = snorm(nc, pb->maxgs, pb->maxin, pb->eps, c.cs, c.ms, c.hs, c.pen, c.igs, c.ps, itcg);
+            it = snorm(nc, pb->maxgs, pb->maxin, pb->eps, c.cs, c.ms, c.hs, c.pen, c.igs, c.ps, itcg,
+                       pb->sens, pb->mxsens, pb->epsens, &c.sens[iout_fn][iin_dpen]);
             c.itcg = itcg;
             if (it == -2) { c.aborted = true; break; }
             if (pb->norm == 0) c.fntrue = c.dxdy * gf_sum(AllElm, c.ps, ikZ, c.igs);
@@ -520,6 +771,11 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     r->a1 = c.a1; r->b1 = c.b1; r->aa = c.aa; r->bb = c.bb; r->rho = c.rho; r->cp = c.cp; r->aob = c.aob;
     r->cksi = c.cksi; r->ceta = c.ceta; r->cphi = c.cphi;
     r->itnorm = c.itnorm; r->ittang = c.ittang; r->itcg = c.itcg; r->itgs = c.itgs; r->solver = c.solver_eff;
+    for (int io = 0; io < 4; io++)
+        for (int ji = 0; ji < 4; ji++) r->sens[io + 4 * ji] = c.sens[io][ji];
+    r->nnr = (int)(c.nr_hist.size() / 7);
+    if (r->nr_hist)
+        for (int q = 0; q < std::min(r->nnr, r->nr_cap) * 7; q++) r->nr_hist[q] = c.nr_hist[q];
     if (c.unsupported || c.aborted) { r->ierror = CNTC_err_other; return r->ierror; }
     soutpt(c, r);
     r->pen = c.pen;

@@ -12,8 +12,10 @@
  * examples/tractcurv.ref_out (48x44 grid, 4 significant digits), both cases of
  * examples/cattaneo.ref_out (NormCG, TangCG on the shift problem), result
  * element 1 of testbank/test_caddon.ref_out (approach prescribed, spin) and
- * cases 1 and 7 of testbank/testbank.ref_out (TangCG shift, SteadyGS 41x41);
- * see tests/test_oracle.py.  GDsteady (G=5) and transient rolling (T=2) have no
+ * cases 1 and 7 of testbank/testbank.ref_out (TangCG shift, SteadyGS 41x41),
+ * and the Newton-Raphson iterations on prescribed total forces of case 2 of
+ * examples/cattaneo.ref_out (F=2) and case 1 of examples/catt_to_cart.ref_out
+ * (F=1); see tests/test_oracle.py.  GDsteady (G=5) and transient rolling (T=2) have no
  * golden output in the reference: those paths are restated line by line and
  * their parity is anchored on the shared algorithms they call.
  *
@@ -59,6 +61,10 @@ typedef struct {
     /* previous solution used when iestim>0 (may be NULL) */
     const int    *igs_init;
     const double *pn_init, *px_init, *py_init;
+    /* sensitivities (CNTC_ic_sens, contact_addon.f90:846): 1 none, 2 d Fn/d pen,
+     * 3 also d (Fx,Fy,Mz)/d (cksi,ceta,cphi); solver limits of those solves (G=6 flags) */
+    int    sens, mxsens;
+    double epsens;
 } orc_problem;
 
 /* Outputs of one case.  Array pointers are caller-allocated with mx*my
@@ -77,6 +83,14 @@ typedef struct {
     double *sx, *sy;
     double *h;
     int    *igs;
+    /* sens(iout, iin) column-major as t_output%sens: iout Fn, Fx/(mu Fn), Fy/(mu Fn), Mz;
+     * iin pen, cksi, ceta, cphi (zero where not computed) */
+    double sens[16];
+    /* Newton-Raphson history when total forces are prescribed (F=1,2): per iteration
+     * 7 values ittang, itnr, cksi, Fx/(mu Fn), ceta, Fy/(mu Fn), solver iterations; nr_hist
+     * caller-allocated with room for nr_cap iterations (may be NULL), nnr = iterations made */
+    int     nr_cap, nnr;
+    double *nr_hist;
 } orc_result;
 
 void orc_default_problem(orc_problem *pb);

@@ -16,10 +16,15 @@ struct NormCtx {
 // normcg, m_solvpn.f90:24-461.  Returns itcg; err out.  Sets 'abort' when the reference
 // would stop the program (divergence past maxcg, m_solvpn.f90:423-429).
 inline int normcg(const NormCtx &cx, bool use_fftprec, int maxcg, double eps, Inflcf &cs, Inflcf &ms,
-                  const GF3 &hstot, double &pen, Eldiv &igs, GF3 &ps, double &err, bool &abort) {
+                  const GF3 &hstot, double &pen, Eldiv &igs, GF3 &ps, double &err, bool &abort,
+                  bool is_sens = false) {
     const int mx = cx.mx, my = cx.my, npot = cx.npot;
     const double dxdy = cx.dxdy, fntrue = cx.fntrue;
     abort = false;
+    // is_sens: the stopping tolerance is relative to the change from the initial estimate
+    // (m_solvpn.f90:92-97, 281-290)
+    GF3 ps0, tmp1;
+    if (is_sens) { ps0 = ps; tmp1.init(npot); }
     int numinn = (npot <= 150) ? 3 : (npot <= 400) ? 2 : 1;
     GF3 rhs, res, r_prv, dd, z, v, q;
     for (GF3 *g : {&rhs, &res, &r_prv, &dd, &z, &v, &q}) g->init(npot);
@@ -91,7 +96,15 @@ inline int normcg(const NormCtx &cx, bool use_fftprec, int maxcg, double eps, In
         gf_axpy(AllInt, alpha, v, ps, ikZ, igs);
         rms_upd = std::fabs(alpha) * gf_rms(AllInt, v, ikZ, igs);
         if (itcg == 1) rms_upd1 = rms_upd;
-        if (itcg <= 3 || itcg % 10 == 0) rms_xk = gf_rms(AllInt, ps, ikZ, igs);
+        if (itcg <= 3 || itcg % 10 == 0) {
+            if (!is_sens) {
+                rms_xk = gf_rms(AllInt, ps, ikZ, igs);
+            } else {
+                gf_copy(AllElm, ps, tmp1, ikZ, igs);
+                gf_axpy(AllElm, -1.0, ps0, tmp1, ikZ, igs);
+                rms_xk = gf_rms(AllInt, tmp1, ikZ, igs);
+            }
+        }
         gf_copy(AllElm, res, r_prv, ikZ, igs);
         if (itinn < numinn && rms_upd >= eps * rms_xk) {
             gf_axpy(AllInt, -alpha, q, res, ikZ, igs);
@@ -145,10 +158,33 @@ inline int normcg(const NormCtx &cx, bool use_fftprec, int maxcg, double eps, In
     return itcg;
 }
 
-// snorm, m_snorm.f90:31-378 (sensitivities not computed).  Returns itnorm (-1: maxin reached,
-// -2: normcg divergence).
+// sens_norm, m_solvpn.f90:531-650: d Fn / d pen from one NormCG solve with the approach
+// perturbed by 0.67 % of the largest normal displacement, started from the solution.
+// Returns false when that solve diverges (the reference stops there).
+inline bool sens_norm(const NormCtx &cx, int mxsens, double epsens, Inflcf &cs, Inflcf &ms,
+                      const GF3 &hstot, double pen, double fntrue, const Eldiv &igs, const GF3 &ps,
+                      const GF3 &unn, double &sens_fn_pen) {
+    NormCtx loc = cx;
+    loc.ic_norm = 0;
+    double pentru = gf_max(AllInt, unn, ikZ, igs);
+    double dpen = 0.0067 * pentru;
+    double penloc = pen + dpen;
+    Eldiv igsloc = igs;
+    GF3 psloc; psloc.init(cx.npot);
+    gf_copy(AllElm, ps, psloc, ikZ, igsloc);
+    double err; bool abort;
+    normcg(loc, true, mxsens, epsens, cs, ms, hstot, penloc, igsloc, psloc, err, abort, true);
+    if (abort) return false;
+    double fnloc = cx.dxdy * gf_sum(AllElm, psloc, ikZ, igsloc);
+    sens_fn_pen = (fnloc - fntrue) / dpen;
+    return true;
+}
+
+// snorm, m_snorm.f90:31-378.  Returns itnorm (-1: maxin reached, -2: normcg divergence).
+// sens >= 2 adds d Fn / d pen (m_snorm.f90:357-368) into sens_fn_pen, else sets it to zero.
 inline int snorm(const NormCtx &cx, int maxgs, int maxin, double eps, Inflcf &cs, Inflcf &ms,
-                 const GF3 &hs, double &pen, Eldiv &igs1, GF3 &ps1, int &itcg_out) {
+                 const GF3 &hs, double &pen, Eldiv &igs1, GF3 &ps1, int &itcg_out,
+                 int sens = 1, int mxsens = 30, double epsens = 1e-4, double *sens_fn_pen = nullptr) {
     const int mx = cx.mx, my = cx.my, npot = cx.npot;
     areas(igs1);
     bool use_vecfft = (npot >= 700);
@@ -209,6 +245,17 @@ inline int snorm(const NormCtx &cx, int maxgs, int maxin, double eps, Inflcf &cs
         if (ps1.c[2][i] < 0.0 && igs1.el[i] >= Adhes) { ps1.c[2][i] = 0.0; igs1.el[i] = Exter; }
     areas(igs1);
     itcg_out = itcg;
+    if (sens_fn_pen) {
+        if (sens >= 2) {
+            double fntrue = cx.fntrue;
+            if (cx.ic_norm == 0) fntrue = cx.dxdy * gf_sum(AllElm, ps1, ikZ, igs1);
+            if (!use_vecfft) vecaijpj(igs1, AllElm, unn, ikZ, ps1, igs1, ikZ, cs, mx, my);
+            if (!sens_norm(cx, mxsens, epsens, cs, ms, hstot, pen, fntrue, igs1, ps1, unn, *sens_fn_pen))
+                return -2;
+        } else {
+            *sens_fn_pen = 0.0;
+        }
+    }
     return itnorm;
 }
 

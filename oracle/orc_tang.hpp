@@ -85,10 +85,14 @@ inline void sxbnd(const TangCtx &cx, int solver_eff, const Eldiv &igs, const Gri
 // ------------------------------------------------------------------------------------------
 inline int stdygs(const TangCtx &cx, const GF3 &ws, Inflcf &cs, Eldiv &igs, const std::vector<double> &mus,
                   GF3 &ps, GF3 &ss, double eps, int maxgs, double omegah, double omegas,
-                  int &info, double &err, bool &bad) {
+                  int &info, double &err, bool &bad, bool is_sens = false) {
     const int mx = cx.mx, my = cx.my, npot = cx.npot;
     bad = false;
     int ixsta, ixinc, ixend;
+    // is_sens: the stopping tolerance is relative to the change from the initial estimate
+    // (m_solvpt.f90:2893-2899, 3138-3145)
+    GF3 ps0, tmp;
+    if (is_sens) { ps0 = ps; tmp.init(npot); }
     if (std::fabs(cx.chi) < 0.01) { ixsta = 1; ixinc = 1; ixend = mx; }
     else if (std::fabs(cx.chi - pi) < 0.01) { ixsta = mx; ixinc = -1; ixend = 1; }
     else { bad = true; return 0; }
@@ -166,7 +170,13 @@ inline int stdygs(const TangCtx &cx, const GF3 &ws, Inflcf &cs, Eldiv &igs, cons
             }
         }
         dif = std::sqrt(dif / (2.0 * k));
-        difid = eps * std::max(1e-6, facnel * gf_rms(AllElm, ps, ikTANG, igs));
+        if (!is_sens) {
+            difid = eps * std::max(1e-6, facnel * gf_rms(AllElm, ps, ikTANG, igs));
+        } else {
+            gf_copy(AllElm, ps, tmp, ikTANG, igs);
+            gf_axpy(AllElm, -1.0, ps0, tmp, ikTANG, igs);
+            difid = eps * std::max(1e-6, facnel * gf_rms(AllElm, tmp, ikTANG, igs));
+        }
         if (itgs == 1) dif1 = dif;
     }
     double conv = 1.0;
@@ -671,13 +681,17 @@ inline int gdsteady(const TangCtx &cx, int maxgd, double eps, const GF3 &ws, Inf
 // TangCG, m_solvpt.f90:1841-2442 (elastic, no plasticity)
 // ------------------------------------------------------------------------------------------
 inline int tangcg(const TangCtx &cx, int maxcg, double eps, const GF3 &ws, Inflcf &cs, Inflcf &ms, Eldiv &igs,
-                  const std::vector<double> &mu, GF3 &ps, GF3 &ss, double &err, bool &bad) {
+                  const std::vector<double> &mu, GF3 &ps, GF3 &ss, double &err, bool &bad,
+                  bool is_sens = false) {
     const int num_inn = 4;
     const double small = 1e-6;
     const int mx = cx.mx, my = cx.my, npot = cx.npot;
     bad = false;
     double ga = cs.ga;
     bool use_fftprec = true;
+    // is_sens: tolerance relative to the change from the initial estimate (m_solvpt.f90:1908-1914)
+    GF3 ps0, tmp;
+    if (is_sens) { ps0 = ps; tmp.init(npot); }
     if (std::max(std::fabs(cs.at(0, 0, 1, 2)), std::fabs(cs.at(0, 0, 2, 1))) >
         (double)1e-8f * std::min(cs.at(0, 0, 1, 1), cs.at(0, 0, 2, 2))) { bad = true; return 0; }
     fft_makeprec(1, cs, 1, ms);
@@ -779,7 +793,14 @@ inline int tangcg(const TangCtx &cx, int maxcg, double eps, const GF3 &ws, Inflc
         dif = alpha * facnel * gf_rms(AllElm, v, ikTANG, igs);
         difinn += dif;
         if (itcg <= 5 || itcg % 5 == 1) {
-            double ptang = facnel * gf_rms(AllElm, ps, ikTANG, igs);
+            double ptang;
+            if (!is_sens) {
+                ptang = facnel * gf_rms(AllElm, ps, ikTANG, igs);
+            } else {
+                gf_copy(AllElm, ps, tmp, ikTANG, igs);
+                gf_axpy(AllElm, -1.0, ps0, tmp, ikTANG, igs);
+                ptang = facnel * gf_rms(AllElm, tmp, ikTANG, igs);
+            }
             difid = eps * std::max(1e-6, ptang);
             trsinn = (double)0.01f * ptang;
         }

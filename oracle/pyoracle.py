@@ -47,6 +47,7 @@ class Problem(ctypes.Structure):
         ("pn_init", ctypes.POINTER(ctypes.c_double)),
         ("px_init", ctypes.POINTER(ctypes.c_double)),
         ("py_init", ctypes.POINTER(ctypes.c_double)),
+        ("sens", ctypes.c_int), ("mxsens", ctypes.c_int), ("epsens", ctypes.c_double),
     ]
 
 
@@ -72,7 +73,12 @@ class Result(ctypes.Structure):
         ("sx", ctypes.POINTER(ctypes.c_double)), ("sy", ctypes.POINTER(ctypes.c_double)),
         ("h", ctypes.POINTER(ctypes.c_double)),
         ("igs", ctypes.POINTER(ctypes.c_int)),
+        ("sens", ctypes.c_double * 16),
+        ("nr_cap", ctypes.c_int), ("nnr", ctypes.c_int), ("nr_hist", ctypes.POINTER(ctypes.c_double)),
     ]
+
+
+NR_CAP = 256
 
 
 def build(quiet=True):
@@ -165,9 +171,15 @@ def solve(pb, h=None, warm=None, fields=True, fast=False):
             setattr(res, k, _dptr(arrs[k]))
         arrs["igs"] = np.zeros(n, dtype=np.int32)
         res.igs = arrs["igs"].ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    hist = np.zeros(NR_CAP * 7, dtype=np.float64)
+    res.nr_cap = NR_CAP
+    res.nr_hist = _dptr(hist)
     lib(fast).orc_calculate(ctypes.byref(pb), ctypes.byref(res))
     out = {k: getattr(res, k) for k, _ in Result._fields_ if k not in
-           ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h", "igs")}
+           ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h", "igs", "sens", "nr_cap", "nr_hist")}
+    # sens[iout][iin]: iout Fn, Fx, Fy, Mz; iin pen, cksi, ceta, cphi
+    out["sens"] = np.array(res.sens[:], dtype=np.float64).reshape(4, 4).T.copy()
+    out["nr"] = hist[:7 * min(res.nnr, NR_CAP)].reshape(-1, 7).copy()
     out.update(arrs)
     return out
 

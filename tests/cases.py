@@ -90,6 +90,25 @@ def cattaneo_case(icase, cksi=0.0):
     return c
 
 
+def cattaneo_forces_case():
+    """Case 2 of examples/cattaneo.inp as the reference states it: the tangential forces
+    prescribed (F=2), Fx = -0.875 mu Fn and Fy = 0, met by Newton-Raphson on the shifts."""
+    c = cattaneo_case(2)
+    del c["cksi"], c["ceta"]
+    c.update(force3=2, fxrel=-0.875, fyrel=0.0)
+    return c
+
+
+def catt_to_cart_case1():
+    """Case 1 of examples/catt_to_cart.inp: Cattaneo shift of a ball (G 1, nu 0.28, mu 0.4013,
+    Fn 0.4705) on a 34x33 grid from -4.125 mm with spacing 0.25 mm, quadratic geometry
+    0.002963 (x^2 + y^2), Fx = -0.657 mu Fn prescribed (F=1), ceta 0, TangCG, eps 1e-7."""
+    return dict(tang=1, norm=1, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=1, eps=1e-7,
+                poiss=0.28, gg=1.0, fstat=0.4013, veloc=1.0, fn=0.4705, ceta=0.0, cphi=0.0, force3=1,
+                fxrel=-0.657, ipotcn=1, potprm=[34, 33, -4.125, -4.125, 0.25, 0.25],
+                prmudf=[0.002963, 0.0, 0.002963, 0.0, 0.0, 0.0])
+
+
 def test_caddon_element1():
     """Result element 1 of src/test_caddon.f90 in CONTACT units (mm, N, rad/mm): steel
     (G 82000 N/mm^2, nu 0.28, mu 0.3), Hertzian semi-axes 4.25 x 7 mm on a 21x33 grid (scale
@@ -201,6 +220,9 @@ def to_oracle(case):
     if "chi" in case:
         pb.chi = case["chi"]
     pb.cksi, pb.ceta, pb.cphi = case.get("cksi", 0.0), case.get("ceta", 0.0), case.get("cphi", 0.0)
+    pb.force3 = case.get("force3", 0)
+    pb.fxrel, pb.fyrel = case.get("fxrel", 0.0), case.get("fyrel", 0.0)
+    pb.sens = case.get("sens", 1)
     if pb.norm == 1:
         pb.fn = case["fn"]
     else:

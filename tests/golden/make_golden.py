@@ -15,9 +15,14 @@ fixtures next to this script:
 * examples/cattaneo.ref_out -> cattaneo.json
   examples/cattaneo.inp, 19x19 grid, polyethylene ball on a plane (G 200, nu 0.42, mu 0.4):
   case 1 the Hertzian normal problem (NormCG), case 2 the non-Hertzian quadratic geometry
-  with the shift problem (T=1, TangCG) whose tangential force the reference prescribes by
-  Newton-Raphson on the shift; kept: the converged shift Cksi printed by that iteration,
-  forces, approach, pmax, element counts and the element-division picture.
+  with the shift problem (T=1, TangCG) whose tangential forces the reference prescribes
+  (F=2) and meets by Newton-Raphson on the shifts; kept: the iterations of that process
+  (shifts, relative forces, TangCG iterations), the sensitivities it leaves, forces,
+  approach, pmax, element counts and the element-division picture.
+* examples/catt_to_cart.ref_out -> catt_to_cart_case1.json
+  case 1 of examples/catt_to_cart.inp, the Cattaneo shift problem on a 34x33 grid with Fx
+  prescribed (F=1, TangCG, eps 1e-7): the Newton-Raphson iterations, the sensitivity
+  dFx/dcksi, forces, shift, element counts and the element-division picture.
 
 * testbank/test_caddon.ref_out -> test_caddon_re1.json
   output of src/test_caddon.f90 for result element 1 (module 3 through the library
@@ -133,6 +138,40 @@ def _results_block(body):
     return rec
 
 
+def _nr_history(body):
+    """The Newton-Raphson iterations on prescribed total forces (m_solvpt.f90:152-160, 336-347):
+    per iteration [itnr, cksi, Fx/(mu Fn), ceta, Fy/(mu Fn), solver iterations]; ceta and Fy are
+    None where only Fx is prescribed (F=1)."""
+    num = r"(\S+)"
+    rows = []
+    for m in re.finditer(r"\n\s+(\d+), NR_F(x|y),\s+Cksi, Fxk:\s+" + num + r"\s+" + num +
+                         r"(?:\s+It(?:CG|GS|GD):\s+(\d+))?(?:\n\s+Ceta, Fyk:\s+" + num + r"\s+" + num +
+                         r"\s+It(?:CG|GS|GD):\s+(\d+))?", body):
+        if m.group(2) == "x":
+            rows.append([int(m.group(1)), float(m.group(3)), float(m.group(4)), None, None, int(m.group(5))])
+        else:
+            rows.append([int(m.group(1)), float(m.group(3)), float(m.group(4)), float(m.group(6)),
+                         float(m.group(7)), int(m.group(8))])
+    return rows
+
+
+def _sensitivities(body):
+    """The printed table of sensitivities: rows FN, FX, FY; columns d/dpen, d/dksi, d/deta,
+    d/dphi (zero where not computed)."""
+    ln = body.splitlines()
+    for i, s in enumerate(ln):
+        if s.strip().startswith("DF/DPEN"):
+            return [[float(v) for v in ln[i + j].split()[1:5]] for j in (1, 2, 3)]
+    return None
+
+
+def _tang_final(rec, body):
+    m = re.search(r"Tang: final element division: A, S=\s*(\d+)\s+(\d+)\s+It(CG|GS)=\s*(\d+)", body)
+    if m:
+        rec["tang_nadh"], rec["tang_nslip"] = int(m.group(1)), int(m.group(2))
+        rec["tang_solver"], rec["tang_it"] = m.group(3), int(m.group(4))
+
+
 def parse_cattaneo(path):
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
@@ -143,12 +182,33 @@ def parse_cattaneo(path):
         rec = {"case": icase}
         m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
         rec["norm_ncon"], rec["norm_itcg"] = int(m.group(1)), int(m.group(3))
-        nr = re.findall(r"NR_Fy,\s+Cksi, Fxk:\s+(\S+)\s+(\S+)", body)
+        nr = _nr_history(body)
         if nr:
-            rec["cksi"], rec["fx_rel_nr"] = float(nr[-1][0]), float(nr[-1][1])
+            rec["nr"] = nr
+            rec["cksi"], rec["fx_rel_nr"] = nr[-1][1], nr[-1][2]
+            rec["sens"] = _sensitivities(body)
+        _tang_final(rec, body)
         rec.update(_results_block(body))
         out.append(rec)
     return {"source": "examples/cattaneo.ref_out", "cases": out}
+
+
+def parse_catt_to_cart(path):
+    """Case 1 of examples/catt_to_cart.inp: the Cattaneo shift with Fx prescribed (F=1)."""
+    text = open(path).read()
+    blocks = re.split(r"\n Case\s+(\d+)\n", text)
+    body = blocks[2]
+    assert int(blocks[1]) == 1
+    rec = {"case": 1}
+    m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+    rec["norm_ncon"], rec["norm_itcg"] = int(m.group(1)), int(m.group(3))
+    rec["nr"] = _nr_history(body)
+    rec["sens"] = _sensitivities(body)
+    _tang_final(rec, body)
+    rec.update(_results_block(body))
+    m = re.search(r"FN/G\s+SHIFT X.*\n\s*(\S+)\s+(\S+)", body)
+    rec["shift_x"] = float(m.group(2))
+    return {"source": "examples/catt_to_cart.ref_out", "cases": [rec]}
 
 
 def parse_testbank(path, wanted=(1, 7)):
@@ -227,6 +287,9 @@ def main():
     ca = parse_cattaneo(os.path.join(root, "examples", "cattaneo.ref_out"))
     with open(os.path.join(HERE, "cattaneo.json"), "w") as f:
         json.dump(ca, f, indent=0)
+    cc = parse_catt_to_cart(os.path.join(root, "examples", "catt_to_cart.ref_out"))
+    with open(os.path.join(HERE, "catt_to_cart_case1.json"), "w") as f:
+        json.dump(cc, f, indent=0)
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)

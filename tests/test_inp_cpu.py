@@ -38,7 +38,7 @@ def test_number_forms():
 
 
 KEYS = ("tang", "norm", "bound", "gausei", "maxgs", "maxin", "maxnr", "maxout", "eps", "poiss", "gg", "fstat",
-        "fn", "pen", "cksi", "ceta", "cphi", "ipotcn", "dq")
+        "fn", "pen", "cksi", "ceta", "cphi", "ipotcn", "dq", "force3", "fxrel", "fyrel")
 
 
 def _same_case(a, b):
@@ -61,7 +61,8 @@ def test_tractcurv_first_series():
 def test_cattaneo_and_testbank():
     cs = _read("examples/cattaneo.inp")
     _same_case(cs[0], C.cattaneo_case(1))
-    assert "total forces prescribed" in cs[1]["unsupported"]
+    _same_case(cs[1], C.cattaneo_forces_case())
+    _same_case(_read("examples/catt_to_cart.inp")[0], C.catt_to_cart_case1())
     tb = _read("testbank/testbank.inp")
     _same_case(tb[0], C.testbank_case(1))
     assert "C=3" in tb[1]["unsupported"]                 # bilinear loading

@@ -6,8 +6,10 @@ test_table_mx11.ref_fx); tractcurv_series1.json the first series of examples/tra
 (examples/cattaneo.ref_out: NormCG, and TangCG on the shift problem); test_caddon_re1.json
 result element 1 of src/test_caddon.f90 (testbank/test_caddon.ref_out: penetration
 prescribed, spin, SteadyGS, printed in SPCK units); testbank_cases.json cases 1 and 7 of
-testbank/testbank.inp (TangCG shift with prescribed approach, SteadyGS on a 41x41 grid).  The oracle has to reproduce them at
-their printed precision before any GPU result is compared with it.
+testbank/testbank.inp (TangCG shift with prescribed approach, SteadyGS on a 41x41 grid);
+catt_to_cart_case1.json case 1 of examples/catt_to_cart.inp (Fx prescribed, Newton-Raphson
+on the shift).  The oracle has to reproduce them at their printed precision before any GPU
+result is compared with it.
 """
 import json
 import math
@@ -221,6 +223,113 @@ def test_cattaneo_against_golden(oracle):
             assert _printed4(o["fx"] / (0.4 * o["fn"]), g["fx_rel_nr"])
 
 
+def _printed3(x, gold):
+    """x agrees with a value printed to 3 significant digits."""
+    unit = 10.0 ** (math.floor(math.log10(abs(gold))) - 2)
+    return abs(x - gold) <= 0.5 * unit * (1 + 1e-9)
+
+
+@pytest.mark.parametrize("name", ["cattaneo", "catt_to_cart"])
+def test_newton_raphson_on_prescribed_forces(oracle, name):
+    """Total tangential forces prescribed: case 2 of examples/cattaneo.inp (F=2, Fx and Fy)
+    and case 1 of examples/catt_to_cart.inp (F=1, Fx).  Every Newton-Raphson iteration the
+    reference printed (m_solvpt.f90:152-347): its shifts and relative forces to the printed 4
+    digits (values below 1e-15 are rounding noise and are skipped) and its TangCG iteration
+    count exact; then the final element division, the sensitivities the iteration leaves
+    (3 printed digits), forces, approach, pmax, elastic energy and the picture."""
+    if name == "cattaneo":
+        g = [c for c in _load("cattaneo.json")["cases"] if c["case"] == 2][0]
+        case, mx, my = C.cattaneo_forces_case(), 19, 19
+    else:
+        g = _load("catt_to_cart_case1.json")["cases"][0]
+        case, mx, my = C.catt_to_cart_case1(), 34, 33
+    o = C.oracle_solve(case)
+    assert o["ierror"] == 0 and o["solver"] == 2
+    nr = o["nr"]
+    assert len(nr) == len(g["nr"])
+    for row, gr in zip(nr, g["nr"]):
+        assert int(row[1]) == gr[0] and int(row[6]) == gr[5], (row, gr)
+        for k, gk in ((2, 1), (3, 2), (4, 3), (5, 4)):
+            if gr[gk] is None or (gr[gk] != 0.0 and abs(gr[gk]) < 1e-15):
+                continue
+            assert _printed4(row[k], gr[gk]), (row, gr)
+    assert (o["nadh"], o["nslip"], o["itgs"]) == (g["tang_nadh"], g["tang_nslip"], g["tang_it"])
+    assert o["itcg"] == g["norm_itcg"]
+    for io in range(3):
+        for ji in range(4):
+            gold = g["sens"][io][ji]
+            if gold == 0.0:
+                assert o["sens"][io][ji] == 0.0
+            else:
+                assert _printed3(o["sens"][io][ji], gold), (io, ji, o["sens"][io][ji], gold)
+    for key, gk in (("fn", "fn"), ("fx", "fx"), ("pen", "approach"), ("pmax", "pmax"), ("elen", "elen")):
+        assert _printed4(o[key], g[gk]), (key, o[key], g[gk])
+    assert _printed4(o["cksi"], g["nr"][-1][1])
+    assert (o["ncon"], o["nadh"], o["nslip"]) == (g["ncon"], g["nadh"], g["nslip"])
+    assert _picture(o["igs"], mx, my) == [r.replace("o", ".") for r in g["picture"]]
+
+
+@pytest.mark.parametrize("gausei", [0, 5])
+def test_prescribed_forces_steady_rolling(oracle, gausei):
+    """Steady rolling (T=3, SteadyGS or GDsteady) with Fx (F=1) or Fx and Fy (F=2) prescribed:
+    the Newton-Raphson meets the forces to the solver tolerance, the creepage it finds gives
+    the same solution when prescribed (F=0), and both solvers find the same creepage."""
+    base = C.config0(gausei=gausei, eps=1e-8, mx=25, my=25)
+    mufn = base["fstat"] * base["fn"]
+    f1 = dict(base, force3=1, fxrel=-0.6)
+    del f1["cksi"]
+    o = C.oracle_solve(f1)
+    assert o["ierror"] == 0 and len(o["nr"]) >= 3
+    assert abs(o["fx"] / mufn + 0.6) <= 1e-8
+    p = C.oracle_solve(dict(base, cksi=o["cksi"]))
+    assert np.array_equal(p["igs"], o["igs"])
+    assert np.abs(p["px"] - o["px"]).max() <= 1e-7 * np.abs(o["pn"]).max()
+    assert o["cksi"] == pytest.approx(0.00239699817, rel=1e-8)
+    f2 = dict(f1, force3=2, fyrel=0.3)
+    del f2["ceta"]
+    o2 = C.oracle_solve(f2)
+    assert o2["ierror"] == 0
+    assert abs(o2["fx"] / mufn + 0.6) <= 1e-8 and abs(o2["fy"] / mufn - 0.3) <= 1e-8
+    assert (o2["cksi"], o2["ceta"]) == (pytest.approx(0.00251180622, rel=1e-8), pytest.approx(-0.00135477422, rel=1e-8))
+
+
+def test_sensitivities_against_differences(oracle):
+    """sens_tang (sens 3) and sens_norm (sens 2), which the reference's printed outputs never
+    exercise: one warm-started solve per perturbed input, against central differences of
+    full solves.  dF/dcksi and dF/dceta within 0.1 %, the spin column within 5 % (the
+    reference's quick estimate), d Fn/d pen within 1 % on a fixed quadratic geometry (a
+    Hertzian input recomputes the curvatures from the approach), N=0 and N=1 alike."""
+    c = C.config0(gausei=0, eps=1e-8, mx=25, my=25)
+    r = C.oracle_solve(dict(c, sens=3))
+    assert r["ierror"] == 0
+    mufn = c["fstat"] * r["fn"]
+    fd = np.zeros((4, 4))
+    tol = {1: 1e-3, 2: 1e-3, 3: 5e-2}
+    for ji, key, h in ((1, "cksi", 1e-6), (2, "ceta", 1e-6), (3, "cphi", 1e-7)):
+        a = C.oracle_solve(dict(c, **{key: c[key] + h}))
+        b = C.oracle_solve(dict(c, **{key: c[key] - h}))
+        fd[1, ji] = (a["fx"] - b["fx"]) / (2 * h) / mufn
+        fd[2, ji] = (a["fy"] - b["fy"]) / (2 * h) / mufn
+        fd[3, ji] = (a["mz"] - b["mz"]) / (2 * h)
+    for io in (1, 2, 3):
+        # entries that vanish by symmetry are compared against the scale of their row
+        scale = np.abs(fd[io, 1:]).max()
+        for ji in (1, 2, 3):
+            err = abs(r["sens"][io][ji] - fd[io, ji])
+            assert err <= tol[ji] * abs(fd[io, ji]) + 1e-4 * scale, (io, ji, r["sens"][io][ji], fd[io, ji])
+    q = C.catt_to_cart_case1()
+    q.update(force3=0, cksi=0.0, tang=0, eps=1e-8)
+    n1 = C.oracle_solve(dict(q, sens=2))
+    pen = n1["pen"]
+    d = dict(q, norm=0, pen=pen, sens=2)
+    del d["fn"]
+    n0 = C.oracle_solve(d)
+    hp = 1e-4 * pen
+    fd = (C.oracle_solve(dict(d, pen=pen + hp, sens=1))["fn"] - C.oracle_solve(dict(d, pen=pen - hp, sens=1))["fn"]) / (2 * hp)
+    assert abs(n0["sens"][0][0] - fd) <= 1e-2 * fd and abs(n1["sens"][0][0] - fd) <= 1e-2 * fd
+    assert np.count_nonzero(C.oracle_solve(q)["sens"]) == 0            # sens 1: nothing computed
+
+
 def test_caddon_element1_against_golden(oracle):
     """src/test_caddon.f90, result element 1 (testbank/test_caddon.ref_out).  The reference
     printed in SPCK units: lengths in m, forces in N acting on body 2 (the sign of CONTACT's
@@ -293,7 +402,7 @@ def test_baseline_build_equals_parity_build(oracle):
     from contact_gb300 import inp
     perfc = [c for c in _load("perfc_cases.json")["cases"] if c["name"] == "norm_problm_1p"][0]
     for case in (C.config0(gausei=5, eps=1e-10, mx=31, my=27), C.config0(gausei=0, eps=1e-8, mx=25, my=25),
-                 C.cattaneo_case(2, 0.008155), inp.materialize(perfc["case"])):
+                 C.cattaneo_case(2, 0.008155), C.cattaneo_forces_case(), inp.materialize(perfc["case"])):
         a = C.oracle_solve(case)
         b = C.oracle_solve(case, fast=True)
         assert (a["ierror"], a["itcg"], a["itgs"]) == (b["ierror"], b["itcg"], b["itgs"])
