@@ -15,7 +15,8 @@
  * cases 1 and 7 of testbank/testbank.ref_out (TangCG shift, SteadyGS 41x41),
  * and the Newton-Raphson iterations on prescribed total forces of case 2 of
  * examples/cattaneo.ref_out (F=2) and case 1 of examples/catt_to_cart.ref_out
- * (F=1); see tests/test_oracle.py.  GDsteady (G=5) and transient rolling (T=2) have no
+ * (F=1), and the element tables of examples/carter2d.ref_out (55x1 strip,
+ * SteadyGS); see tests/test_oracle.py.  GDsteady (G=5) and transient rolling (T=2) have no
  * golden output in the reference: those paths are restated line by line and
  * their parity is anchored on the shared algorithms they call.
  *

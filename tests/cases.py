@@ -109,6 +109,16 @@ def catt_to_cart_case1():
                 prmudf=[0.002963, 0.0, 0.002963, 0.0, 0.0, 0.0])
 
 
+def carter2d_case():
+    """examples/carter2d.inp: Carter's two-dimensional steady rolling (T=3, SteadyGS, eps 1e-5)
+    on a 55x1 strip from x = -1.05 mm with dx 0.04 mm and dy 200 mm, steel (G 82000, nu
+    0.28, mu 0.3), Fn 35780 N, creepage -0.00024, undeformed distance 0.001 x^2."""
+    return dict(tang=3, norm=1, bound=0, gausei=0, maxgs=999, maxin=100, maxnr=30, maxout=1, eps=1e-5,
+                poiss=0.28, gg=82000.0, fstat=0.3, veloc=30000.0, fn=35780.0, cksi=-0.00024, ceta=0.0, cphi=0.0,
+                ipotcn=3, potprm=[55, 1, -1.05, 0.0, 0.04, 200.0], dq=0.0401,
+                prmudf=[0.001, 0.0, 0.0, 0.0, 0.0, 0.0])
+
+
 def test_caddon_element1():
     """Result element 1 of src/test_caddon.f90 in CONTACT units (mm, N, rad/mm): steel
     (G 82000 N/mm^2, nu 0.28, mu 0.3), Hertzian semi-axes 4.25 x 7 mm on a 21x33 grid (scale

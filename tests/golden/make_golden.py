@@ -24,6 +24,11 @@ fixtures next to this script:
   prescribed (F=1, TangCG, eps 1e-7): the Newton-Raphson iterations, the sensitivity
   dFx/dcksi, forces, shift, element counts and the element-division picture.
 
+* examples/carter2d.ref_out -> carter2d.json
+  examples/carter2d.inp, Carter's two-dimensional steady rolling problem on a 55x1 strip
+  (dy 200 mm, SteadyGS, eps 1e-5), printed with its element tables: the approach to 8 digits,
+  pn per element after NORM, element codes, px and shift sx after TANG, totals and counts.
+
 * testbank/test_caddon.ref_out -> test_caddon_re1.json
   output of src/test_caddon.f90 for result element 1 (module 3 through the library
   interface in SPCK units: Hertzian 21x33 grid, penetration prescribed, creepage 0.001,
@@ -211,6 +216,44 @@ def parse_catt_to_cart(path):
     return {"source": "examples/catt_to_cart.ref_out", "cases": [rec]}
 
 
+def _table_after(ln, title, ncol):
+    """Rows of the element table that follows a debug title (ix, iy, ii, then numbers)."""
+    i = next(k for k, t in enumerate(ln) if t.strip() == title)
+    rows = []
+    for t in ln[i + 1:]:
+        parts = [p for p in t.replace(",", " ").split()]
+        if len(parts) == ncol and parts[0].isdigit():
+            rows.append([float(p) for p in parts])
+        elif rows:
+            break
+    return rows
+
+
+def parse_carter2d(path):
+    """examples/carter2d.inp: Carter's two-dimensional rolling problem (55x1 strip, SteadyGS),
+    printed with element tables: the normal solution (approach to 8 digits, pn per element to
+    4 decimals) and the tangential one after the slip-area update (element code, px to 4
+    decimals, shift sx to 7 decimals)."""
+    text = open(path).read()
+    body = re.split(r"\n Case\s+(\d+)\n", text)[2]
+    ln = body.splitlines()
+    rec = {"case": 1}
+    m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+    rec["norm_ncon"], rec["norm_itcg"] = int(m.group(1)), int(m.group(3))
+    _tang_final(rec, body)
+    rec["pen8"] = float(re.search(r"Nmdbg: solution of NORM:\n pen =\s*(\S+)", body).group(1))
+    norm = _table_after(ln, "Nmdbg: solution of NORM:", 9)
+    rec["pn"] = [r[8] for r in norm]
+    rec["norm_code"] = [int(r[7]) for r in norm]
+    tang = _table_after(ln, "Nmdbg: after expanding slip-area:", 9)
+    rec["tang_code"] = [int(r[3]) for r in tang]
+    rec["tang_ii"] = [int(r[2]) for r in tang]
+    rec["px"] = [r[4] for r in tang]
+    rec["sx"] = [r[6] for r in tang]
+    rec.update(_results_block(body))
+    return {"source": "examples/carter2d.ref_out", "cases": [rec]}
+
+
 def parse_testbank(path, wanted=(1, 7)):
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
@@ -290,6 +333,9 @@ def main():
     cc = parse_catt_to_cart(os.path.join(root, "examples", "catt_to_cart.ref_out"))
     with open(os.path.join(HERE, "catt_to_cart_case1.json"), "w") as f:
         json.dump(cc, f, indent=0)
+    c2 = parse_carter2d(os.path.join(root, "examples", "carter2d.ref_out"))
+    with open(os.path.join(HERE, "carter2d.json"), "w") as f:
+        json.dump(c2, f, indent=0)
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)

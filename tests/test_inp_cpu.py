@@ -63,6 +63,7 @@ def test_cattaneo_and_testbank():
     _same_case(cs[0], C.cattaneo_case(1))
     _same_case(cs[1], C.cattaneo_forces_case())
     _same_case(_read("examples/catt_to_cart.inp")[0], C.catt_to_cart_case1())
+    _same_case(_read("examples/carter2d.inp")[0], C.carter2d_case())        # with an XFLOW line
     tb = _read("testbank/testbank.inp")
     _same_case(tb[0], C.testbank_case(1))
     assert "C=3" in tb[1]["unsupported"]                 # bilinear loading

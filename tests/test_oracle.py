@@ -8,7 +8,7 @@ result element 1 of src/test_caddon.f90 (testbank/test_caddon.ref_out: penetrati
 prescribed, spin, SteadyGS, printed in SPCK units); testbank_cases.json cases 1 and 7 of
 testbank/testbank.inp (TangCG shift with prescribed approach, SteadyGS on a 41x41 grid);
 catt_to_cart_case1.json case 1 of examples/catt_to_cart.inp (Fx prescribed, Newton-Raphson
-on the shift).  The oracle has to reproduce them at their printed precision before any GPU
+on the shift); carter2d.json the element tables of examples/carter2d.inp (a 55x1 strip).  The oracle has to reproduce them at their printed precision before any GPU
 result is compared with it.
 """
 import json
@@ -328,6 +328,29 @@ def test_sensitivities_against_differences(oracle):
     fd = (C.oracle_solve(dict(d, pen=pen + hp, sens=1))["fn"] - C.oracle_solve(dict(d, pen=pen - hp, sens=1))["fn"]) / (2 * hp)
     assert abs(n0["sens"][0][0] - fd) <= 1e-2 * fd and abs(n1["sens"][0][0] - fd) <= 1e-2 * fd
     assert np.count_nonzero(C.oracle_solve(q)["sens"]) == 0            # sens 1: nothing computed
+
+
+def test_carter2d_element_tables(oracle):
+    """examples/carter2d.inp (a 55x1 strip, SteadyGS): the approach to the printed 8 digits,
+    pn of every element after NORM and px of every contact element after TANG to the printed
+    4 decimals, the shift sx to 7 decimals, element codes, totals to 4 digits and the NormCG and
+    SteadyGS iteration counts exact."""
+    g = _load("carter2d.json")["cases"][0]
+    o = C.oracle_solve(C.carter2d_case())
+    assert o["ierror"] == 0 and o["solver"] == 4
+    assert abs(o["pen"] - g["pen8"]) <= 0.5e-8
+    assert np.abs(o["pn"] - np.array(g["pn"])).max() <= 0.5e-4 * (1 + 1e-9)
+    assert [int(v >= 1) for v in o["igs"]] == g["norm_code"]          # contact set of NORM, kept by TANG
+    idx = np.array(g["tang_ii"]) - 1
+    assert [int(o["igs"][i]) for i in idx] == g["tang_code"]
+    assert np.abs(o["px"][idx] - np.array(g["px"])).max() <= 0.5e-4 * (1 + 1e-9)
+    dq = 0.04                                            # T=3 with SteadyGS: dq = dx
+    assert np.abs(o["sx"][idx] * dq - np.array(g["sx"])).max() <= 0.5e-7 * (1 + 1e-6)
+    for key, gk in (("fn", "fn"), ("fx", "fx"), ("pen", "approach"), ("pmax", "pmax"), ("elen", "elen")):
+        assert _printed4(o[key], g[gk]), (key, o[key], g[gk])
+    assert (o["ncon"], o["nadh"], o["nslip"]) == (g["ncon"], g["nadh"], g["nslip"])
+    assert (o["itcg"], o["itgs"]) == (g["norm_itcg"], g["tang_it"])
+    assert _picture(o["igs"], 55, 1) == [r.replace("o", ".") for r in g["picture"]]
 
 
 def test_caddon_element1_against_golden(oracle):
