@@ -11,7 +11,8 @@
  * + SteadyGS, printed to 6 decimals), the first series of
  * examples/tractcurv.ref_out (48x44 grid, 4 significant digits), both cases of
  * examples/cattaneo.ref_out (NormCG, TangCG on the shift problem), result
- * element 1 of testbank/test_caddon.ref_out (approach prescribed, spin) and
+ * element 1 of testbank/test_caddon.ref_out and testbank/contact_nonhz.ref_out
+ * (approach prescribed, spin) and
  * cases 1 and 7 of testbank/testbank.ref_out (TangCG shift, SteadyGS 41x41),
  * and the Newton-Raphson iterations on prescribed total forces of case 2 of
  * examples/cattaneo.ref_out (F=2) and case 1 of examples/catt_to_cart.ref_out

@@ -36,6 +36,11 @@ fixtures next to this script:
   pressure and traction, positions and values of the largest tractions.  (Result element 2
   uses a falling friction law and an interfacial layer, outside this library.)
 
+* testbank/contact_nonhz.ref_out -> contact_nonhz_re1.json
+  the same call sequence as test_caddon's element 1, printed by the library in CONTACT units
+  (mm, N): forces, moment, energy, approach, pmax to 4 digits, element counts, NormCG and
+  SteadyGS iterations and the element-division picture.
+
 * testbank/testbank.ref_out -> testbank_cases.json
   cases 1 and 7 of testbank/testbank.inp, the stand-alone program's regression set: case 1
   the shift problem with prescribed approach (17x17 quadratic geometry, TangCG, eps 1e-8),
@@ -295,6 +300,21 @@ def parse_perfc(root):
     return {"source": "perfc_test/*.inp, perfc_test/get_times.ref_out (2016-07-29, 1 thread)", "cases": out}
 
 
+def parse_contact_nonhz(path):
+    """testbank/contact_nonhz.ref_out, result element 1, first case: the call sequence of
+    src/test_caddon.f90's element 1 printed by the library in CONTACT units."""
+    text = open(path).read()
+    body = re.split(r"\n Case\s+1 for contact problem\s+\d+ on result element\s+1\n", text)[1]
+    body = re.split(r"\n Case\s+\d+ for contact problem", body)[0]
+    rec = {"element": 1, "case": 1}
+    m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+    rec["norm_ncon"], rec["norm_itcg"] = int(m.group(1)), int(m.group(3))
+    _tang_final(rec, body)
+    rec.update(_results_block(body))
+    return {"source": "testbank/contact_nonhz.ref_out", "units": "CONTACT (mm, N, forces on body 1)",
+            "cases": [rec]}
+
+
 def parse_test_caddon(path):
     text = open(path).read()
     block = text.split("...start processing of Result Element")[1]     # element 1, first solve
@@ -336,6 +356,9 @@ def main():
     c2 = parse_carter2d(os.path.join(root, "examples", "carter2d.ref_out"))
     with open(os.path.join(HERE, "carter2d.json"), "w") as f:
         json.dump(c2, f, indent=0)
+    cn = parse_contact_nonhz(os.path.join(root, "testbank", "contact_nonhz.ref_out"))
+    with open(os.path.join(HERE, "contact_nonhz_re1.json"), "w") as f:
+        json.dump(cn, f, indent=0)
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)

@@ -8,7 +8,9 @@ result element 1 of src/test_caddon.f90 (testbank/test_caddon.ref_out: penetrati
 prescribed, spin, SteadyGS, printed in SPCK units); testbank_cases.json cases 1 and 7 of
 testbank/testbank.inp (TangCG shift with prescribed approach, SteadyGS on a 41x41 grid);
 catt_to_cart_case1.json case 1 of examples/catt_to_cart.inp (Fx prescribed, Newton-Raphson
-on the shift); carter2d.json the element tables of examples/carter2d.inp (a 55x1 strip).  The oracle has to reproduce them at their printed precision before any GPU
+on the shift); carter2d.json the element tables of examples/carter2d.inp (a 55x1 strip);
+contact_nonhz_re1.json result element 1 of testbank/contact_nonhz.ref_out (test_caddon's
+element 1 in CONTACT units, with exact counts).  The oracle has to reproduce them at their printed precision before any GPU
 result is compared with it.
 """
 import json
@@ -381,6 +383,21 @@ def test_caddon_element1_against_golden(oracle):
         i = int(np.argmax(np.abs(arr)))
         assert [i % mx + 1, i // mx + 1] == g[key][:2], key
         assert near(sign * arr[i], g[key][2], 1), key
+
+
+def test_contact_nonhz_element1(oracle):
+    """testbank/contact_nonhz.ref_out, result element 1: test_caddon's element-1 call sequence
+    printed in CONTACT units.  Forces, moment, elastic energy, approach and pmax to 4 digits;
+    element counts, NormCG and SteadyGS iterations and the picture exact."""
+    g = _load("contact_nonhz_re1.json")["cases"][0]
+    o = C.oracle_solve(C.test_caddon_element1())
+    assert o["ierror"] == 0 and o["solver"] == 4
+    for key, gk in (("fn", "fn"), ("fx", "fx"), ("fy", "fy"), ("mz", "mz"), ("elen", "elen"), ("pen", "approach"),
+                    ("pmax", "pmax")):
+        assert _printed4(o[key], g[gk]), (key, o[key], g[gk])
+    assert (o["ncon"], o["nadh"], o["nslip"]) == (g["ncon"], g["nadh"], g["nslip"])
+    assert (o["itcg"], o["itgs"]) == (g["norm_itcg"], g["tang_it"])
+    assert _picture(o["igs"], o["mx"], o["my"]) == [r.replace("o", ".") for r in g["picture"]]
 
 
 def test_testbank_cases_against_golden(oracle):
