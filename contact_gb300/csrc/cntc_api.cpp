@@ -295,7 +295,10 @@ void collect(Problem &p, const PatchDesc &d, const double *io) {
     const int *igs = (const int *)(o + O_NSCAL);
     p.igs.assign(igs, igs + n);
     p.f_n = o[O_FN]; p.f_x = o[O_FX]; p.f_y = o[O_FY]; p.m_z = o[O_MZ];
-    p.r_pen = o[O_PEN]; p.elen = o[O_ELEN]; p.pmax = o[O_PMAX];
+    p.r_pen = o[O_PEN]; p.pmax = o[O_PMAX];
+    // the normal problem is skipped for B = 2..4 and its elastic energy is reported as zero
+    // (m_soutpt.f90:453-458)
+    p.elen = (d.bound >= 2 && d.bound <= 4) ? 0.0 : o[O_ELEN];
     p.ierror = (int)o[O_IERR]; p.itnorm = (int)o[O_ITNORM]; p.ittang = (int)o[O_ITTANG];
     p.itcg = (int)o[O_ITCG]; p.itgs = (int)o[O_ITGS]; p.solver = (int)o[O_SOLVER];
     p.ncon = (int)o[O_NCON]; p.nadh = (int)o[O_NADH]; p.nslip = (int)o[O_NSLIP];

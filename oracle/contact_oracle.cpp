@@ -531,13 +531,15 @@ void soutpt(Case &c, orc_result *r) {
     for (int ii = 0; ii < npot; ii++) { dx_y += c.ps.vx(ii) * c.g.y[ii]; dy_x += c.ps.vy(ii) * c.g.x[ii]; }
     double mztrue = -c.dxdy * dx_y + c.dxdy * dy_x;
     if (std::fabs(mztrue) < 0.5 * c.tc.eps * (c.muscal * c.fntrue + tiny_)) mztrue = 0.0;
-    double elen = 0.5 * 1e-3 * c.dxdy * gf_dot(AllInt, c.us, c.ps, ikALL, c.igs);
+    // B=2..4 (normal problem skipped): no elastic energy, deformed distance zero (m_soutpt.f90:453-470)
+    bool skipped = c.pb->bound >= 2 && c.pb->bound <= 4;
+    double elen = skipped ? 0.0 : 0.5 * 1e-3 * c.dxdy * gf_dot(AllInt, c.us, c.ps, ikALL, c.igs);
     double pmax = gf_max(AllElm, c.ps, ikZ, c.igs);
     r->fn = c.fntrue; r->fx = fxtrue; r->fy = fytrue; r->mz = mztrue;
     r->elen = elen; r->pmax = pmax;
     r->ncon = nadh + nslip + nplast; r->nadh = nadh; r->nslip = nslip;
     for (int ii = 0; ii < npot; ii++) {
-        c.ss.vn(ii) = -c.pen + c.hs.vn(ii) + c.us.vn(ii);
+        c.ss.vn(ii) = skipped ? 0.0 : -c.pen + c.hs.vn(ii) + c.us.vn(ii);
         if (c.igs.el[ii] != Slip) { c.ss.vx(ii) = 0.0; c.ss.vy(ii) = 0.0; }
     }
 }

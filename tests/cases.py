@@ -135,7 +135,20 @@ def testbank_case(icase):
     on a 17x17 grid from -1.13333 mm with spacing 0.13333 mm, TangCG, eps 1e-8.
     7: steady rolling, Fn 0.4705, creepage -0.00304, mu 0.4013, G 1, nu 0.28, dq 0.2 mm,
     quadratic geometry 0.002963 (x^2 + y^2) on a 41x41 grid from -4.1 mm with spacing 0.2 mm,
-    SteadyGS with maxgs 80, maxin 30, eps 1e-6."""
+    SteadyGS with maxgs 80, maxin 30, eps 1e-6.
+    10: case 1 with Fn 1722 N, Fx = -0.875 mu Fn and Fy = 0 prescribed (F=2), the grid given by
+    its corners.  13: a Cattaneo shift on a 41x41 Hertzian grid (semi-axes 4.1 mm, scale
+    1.17143) with the normal problem skipped for the elliptical traction bound (B=2), Fn
+    0.7563, Fx = 0.657 mu Fn prescribed (F=1), G 1, nu 0.28, mu 0.4013, TangCG, eps 1e-6."""
+    if icase == 10:
+        return dict(tang=1, norm=1, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=1, eps=1e-8,
+                    poiss=0.28, gg=82000.0, fstat=0.3, veloc=1.0, fn=1722.0, cphi=0.0, force3=2, fxrel=-0.875,
+                    fyrel=0.0, ipotcn=2, potprm=[17, 17, -1.13333, -1.13333, 1.13333, 1.13333],
+                    prmudf=[0.0056566, 0.0, 0.0056566, 0.0, 0.0, 0.0])
+    if icase == 13:
+        return dict(tang=1, norm=1, bound=2, gausei=0, maxgs=80, maxin=100, maxnr=30, maxout=1, eps=1e-6,
+                    poiss=0.28, gg=1.0, fstat=0.4013, veloc=1.0, fn=0.7563, ceta=0.0, cphi=0.0, force3=1,
+                    fxrel=0.657, ipotcn=-3, potprm=[41, 41, 4.1, 4.1, 1.17143])
     if icase == 1:
         return dict(tang=1, norm=0, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=1, eps=1e-8,
                     poiss=0.28, gg=82000.0, fstat=0.3, veloc=1.0, pen=0.01131, cksi=0.00304, ceta=0.0, cphi=0.0,

@@ -42,11 +42,13 @@ fixtures next to this script:
   SteadyGS iterations and the element-division picture.
 
 * testbank/testbank.ref_out -> testbank_cases.json
-  cases 1 and 7 of testbank/testbank.inp, the stand-alone program's regression set: case 1
-  the shift problem with prescribed approach (17x17 quadratic geometry, TangCG, eps 1e-8),
-  case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6).  The other
-  cases use features outside this library (ConvexGS, bilinear loading, falling or variable
-  friction, other materials, transient sequences).
+  cases 1, 7, 10 and 13 of testbank/testbank.inp, the stand-alone program's regression set:
+  case 1 the shift problem with prescribed approach (17x17 quadratic geometry, TangCG, eps
+  1e-8), case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6), case 10
+  the same shift with Fn, Fx and Fy prescribed (F=2, Newton-Raphson on both shifts), case 13
+  a shift on a 41x41 Hertzian grid with the normal problem skipped (B=2) and Fx prescribed
+  (F=1).  The other cases use features outside this library (ConvexGS, bilinear loading,
+  falling or variable friction, other materials, transient sequences, Fastsim).
 
 * perfc_test/*.inp + perfc_test/get_times.ref_out -> perfc_cases.json
   the reference's performance inputs that this library solves (normal problems 1p-8p,
@@ -259,7 +261,7 @@ def parse_carter2d(path):
     return {"source": "examples/carter2d.ref_out", "cases": [rec]}
 
 
-def parse_testbank(path, wanted=(1, 7)):
+def parse_testbank(path, wanted=(1, 7, 10, 13)):
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
     out = []
@@ -270,9 +272,12 @@ def parse_testbank(path, wanted=(1, 7)):
         body = blocks[k + 1]
         rec = {"case": icase}
         m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
-        rec["norm_itcg"] = int(m.group(3))
-        m = re.search(r"Tang: final element division: A, S=\s*(\d+)\s+(\d+)\s+It(CG|GS)=\s*(\d+)", body)
-        rec["tang_solver"], rec["tang_it"] = m.group(3), int(m.group(4))
+        rec["norm_itcg"] = int(m.group(3)) if m else 0          # 0: normal problem skipped (B=2)
+        _tang_final(rec, body)
+        nr = _nr_history(body)
+        if nr:
+            rec["nr"] = nr
+            rec["sens"] = _sensitivities(body)
         rec.update(_results_block(body))
         out.append(rec)
     return {"source": "testbank/testbank.ref_out", "cases": out}

@@ -231,6 +231,27 @@ def _printed3(x, gold):
     return abs(x - gold) <= 0.5 * unit * (1 + 1e-9)
 
 
+def _check_nr(o, g):
+    """The printed Newton-Raphson iterations (shifts and relative forces to 4 digits, values
+    below 1e-15 being rounding noise; solver iterations exact) and the sensitivities they
+    leave (3 digits, zero where the reference prints zero)."""
+    nr = o["nr"]
+    assert len(nr) == len(g["nr"])
+    for row, gr in zip(nr, g["nr"]):
+        assert int(row[1]) == gr[0] and int(row[6]) == gr[5], (row, gr)
+        for k, gk in ((2, 1), (3, 2), (4, 3), (5, 4)):
+            if gr[gk] is None or (gr[gk] != 0.0 and abs(gr[gk]) < 1e-15):
+                continue
+            assert _printed4(row[k], gr[gk]), (row, gr)
+    for io in range(3):
+        for ji in range(4):
+            gold = g["sens"][io][ji]
+            if gold == 0.0:
+                assert o["sens"][io][ji] == 0.0
+            else:
+                assert _printed3(o["sens"][io][ji], gold), (io, ji, o["sens"][io][ji], gold)
+
+
 @pytest.mark.parametrize("name", ["cattaneo", "catt_to_cart"])
 def test_newton_raphson_on_prescribed_forces(oracle, name):
     """Total tangential forces prescribed: case 2 of examples/cattaneo.inp (F=2, Fx and Fy)
@@ -247,23 +268,9 @@ def test_newton_raphson_on_prescribed_forces(oracle, name):
         case, mx, my = C.catt_to_cart_case1(), 34, 33
     o = C.oracle_solve(case)
     assert o["ierror"] == 0 and o["solver"] == 2
-    nr = o["nr"]
-    assert len(nr) == len(g["nr"])
-    for row, gr in zip(nr, g["nr"]):
-        assert int(row[1]) == gr[0] and int(row[6]) == gr[5], (row, gr)
-        for k, gk in ((2, 1), (3, 2), (4, 3), (5, 4)):
-            if gr[gk] is None or (gr[gk] != 0.0 and abs(gr[gk]) < 1e-15):
-                continue
-            assert _printed4(row[k], gr[gk]), (row, gr)
+    _check_nr(o, g)
     assert (o["nadh"], o["nslip"], o["itgs"]) == (g["tang_nadh"], g["tang_nslip"], g["tang_it"])
     assert o["itcg"] == g["norm_itcg"]
-    for io in range(3):
-        for ji in range(4):
-            gold = g["sens"][io][ji]
-            if gold == 0.0:
-                assert o["sens"][io][ji] == 0.0
-            else:
-                assert _printed3(o["sens"][io][ji], gold), (io, ji, o["sens"][io][ji], gold)
     for key, gk in (("fn", "fn"), ("fx", "fx"), ("pen", "approach"), ("pmax", "pmax"), ("elen", "elen")):
         assert _printed4(o[key], g[gk]), (key, o[key], g[gk])
     assert _printed4(o["cksi"], g["nr"][-1][1])
@@ -401,10 +408,11 @@ def test_contact_nonhz_element1(oracle):
 
 
 def test_testbank_cases_against_golden(oracle):
-    """testbank/testbank.inp cases 1 (shift, approach prescribed, TangCG) and 7 (steady rolling,
-    SteadyGS, 41x41): forces, moment, approach, pmax and elastic energy to the printed 4
-    digits; element counts, pictures and the NormCG and TangCG/SteadyGS iteration counts
-    exact."""
+    """testbank/testbank.inp cases 1 (shift, approach prescribed, TangCG), 7 (steady rolling,
+    SteadyGS, 41x41), 10 (shift with Fn, Fx, Fy prescribed) and 13 (Hertzian shift, normal
+    problem skipped, Fx prescribed): forces, moment, approach, pmax and elastic energy to the
+    printed 4 digits; element counts, pictures and the NormCG and TangCG/SteadyGS iteration
+    counts exact; the Newton-Raphson iterations of cases 10 and 13 as printed."""
     gold = _load("testbank_cases.json")
     for g in gold["cases"]:
         o = C.oracle_solve(C.testbank_case(g["case"]))
@@ -416,6 +424,8 @@ def test_testbank_cases_against_golden(oracle):
         assert o["itcg"] == g["norm_itcg"] and o["itgs"] == g["tang_it"]
         assert o["solver"] == (2 if g["tang_solver"] == "CG" else 4)
         assert _picture(o["igs"], o["mx"], o["my"]) == [r.replace("o", ".") for r in g["picture"]]
+        if "nr" in g:
+            _check_nr(o, g)
 
 
 @pytest.mark.parametrize("name", ["norm_problm_1p", "norm_problm_1f", "norm_problm_2p", "norm_problm_2f",
