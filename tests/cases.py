@@ -268,7 +268,7 @@ def to_oracle(case):
 
 
 def oracle_solve(case, fast=False):
-    """The oracle's solve of a case; fast: its baseline build (Stockham FFT)."""
+    """The oracle's solve of a case; fast: its baseline build (Stockham FFT, real-input convolutions)."""
     import pyoracle as po
     pb, h = to_oracle(case)
     return po.solve(pb, h=h, fast=fast)

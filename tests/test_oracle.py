@@ -448,11 +448,14 @@ def test_perfc_against_published_run(oracle, name):
 def test_baseline_build_equals_parity_build(oracle):
     """The oracle's baseline build (Stockham FFT, timed as the CPU baseline) solves like the
     parity build: same iterations and element division, forces within 1e-12, tractions
-    within 1e-12 of pmax, on steady rolling (GDsteady, SteadyGS), shift and a rail geometry."""
+    within 1e-12 of pmax, on steady rolling (GDsteady, SteadyGS), shifts (with forces
+    prescribed), a two-dimensional strip and a rail geometry; FFT lengths with factors 2, 3,
+    5 and 7 and a length-2 column transform."""
     from contact_gb300 import inp
     perfc = [c for c in _load("perfc_cases.json")["cases"] if c["name"] == "norm_problm_1p"][0]
     for case in (C.config0(gausei=5, eps=1e-10, mx=31, my=27), C.config0(gausei=0, eps=1e-8, mx=25, my=25),
-                 C.cattaneo_case(2, 0.008155), C.cattaneo_forces_case(), inp.materialize(perfc["case"])):
+                 C.cattaneo_case(2, 0.008155), C.cattaneo_forces_case(), C.testbank_case(13), C.carter2d_case(),
+                 inp.materialize(perfc["case"])):
         a = C.oracle_solve(case)
         b = C.oracle_solve(case, fast=True)
         assert (a["ierror"], a["itcg"], a["itgs"]) == (b["ierror"], b["itcg"], b["itgs"])
