@@ -8,6 +8,7 @@
 #include "orc_hertz.hpp"
 #include "orc_norm.hpp"
 #include "orc_tang.hpp"
+#include "orc_subsurf.hpp"
 
 using namespace orc;
 
@@ -565,6 +566,32 @@ void orc_default_problem(orc_problem *pb) {
 int orc_opt_fft_size(int n) { return opt_fft_size(n); }
 
 double orc_eli(double elmodk, double *ellk, double *elle) { return eli(elmodk, *ellk, *elle); }
+
+static void subs_store(const SubsPoint &r, double *o) {
+    for (int i = 0; i < 3; i++) o[i] = r.u[i];
+    o[3] = r.sighyd; o[4] = r.sigvm; o[5] = r.sigtr;
+    for (int i = 0; i < 3; i++) o[6 + i] = r.sigmaj[i];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) o[9 + 3 * i + j] = r.sig[i][j];
+}
+
+void orc_subsurf_points(int mx, int my, double dx, double dy, double xc1, double yc1, const double *pn,
+                        const double *px, const double *py, const double *gg, const double *poiss, int npts,
+                        const double *xyz, double *out) {
+    SubsLoad L{mx, my, dx, dy, xc1, yc1, pn, px, py, {gg[0], gg[1]}, {poiss[0], poiss[1]}};
+    for (int q = 0; q < npts; q++) subs_store(sstres_point(L, xyz + 3 * q), out + (size_t)q * ORC_SUBS_NCOL);
+}
+
+void orc_subsurf_depths(int mx, int my, double dx, double dy, double xc1, double yc1, const double *pn,
+                        const double *px, const double *py, const double *gg, const double *poiss, int nz,
+                        const double *z, double *out) {
+    SubsLoad L{mx, my, dx, dy, xc1, yc1, pn, px, py, {gg[0], gg[1]}, {poiss[0], poiss[1]}};
+    std::vector<SubsPoint> r((size_t)mx * my);
+    for (int iz = 0; iz < nz; iz++) {
+        sstres_fft_depth(L, z[iz], r.data());
+        for (size_t ii = 0; ii < r.size(); ii++) subs_store(r[ii], out + ((size_t)iz * r.size() + ii) * ORC_SUBS_NCOL);
+    }
+}
 
 void orc_influence_coefficients(int mx, int my, double dx, double dy, double nu, double ak, double xshft,
                                 double yshft, double *out) {

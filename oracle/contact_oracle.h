@@ -18,7 +18,9 @@
  * and the Newton-Raphson iterations on prescribed total forces of case 2 of
  * examples/cattaneo.ref_out (F=2) and case 1 of examples/catt_to_cart.ref_out
  * (F=1), and the element tables of examples/carter2d.ref_out (55x1 strip,
- * SteadyGS); see tests/test_oracle.py.  GDsteady (G=5) and transient rolling (T=2) have no
+ * SteadyGS); see tests/test_oracle.py.  Its subsurface stresses (orc_subsurf.hpp)
+ * reproduce examples/subsurf.ref_subs and the maxima of subsurf.ref_out
+ * (tests/test_subsurf_cpu.py).  GDsteady (G=5) and transient rolling (T=2) have no
  * golden output in the reference: those paths are restated line by line and
  * their parity is anchored on the shared algorithms they call.
  *
@@ -112,6 +114,21 @@ void orc_convolve(int mx, int my, const double *cf_block, double ga, const doubl
 void orc_convolve_direct(int mx, int my, const double *cf_block, double ga, const double *p, double *u);
 /* complete elliptic integrals used by the Hertz solution */
 double orc_eli(double elmodk, double *ellk, double *elle);
+
+/* Subsurface elastic field of surface tractions pn, px, py (body 1) on an mx x my grid with
+ * element centres from (xc1, yc1) and spacing dx, dy; gg, poiss [2] the two bodies (z >= 0 in
+ * body 1, z < 0 in body 2).  Per point ORC_SUBS_NCOL values: ux, uy, uz, sighyd, sigvm, sigtr,
+ * sigma1..3 (largest first), then the stress tensor row by row. */
+#define ORC_SUBS_NCOL 18
+/* at npts arbitrary points xyz[3*q..] by direct summation (m_subsurf.f90 sstres) */
+void orc_subsurf_points(int mx, int my, double dx, double dy, double xc1, double yc1, const double *pn,
+                        const double *px, const double *py, const double *gg, const double *poiss, int npts,
+                        const double *xyz, double *out);
+/* at all element centres at each of nz depths by influence coefficients and FFT convolution
+ * (m_subsurf.f90 sstres_inflcf + sstres_fft); out[(iz*mx*my + ii)*ORC_SUBS_NCOL ...] */
+void orc_subsurf_depths(int mx, int my, double dx, double dy, double xc1, double yc1, const double *pn,
+                        const double *px, const double *py, const double *gg, const double *poiss, int nz,
+                        const double *z, double *out);
 
 #ifdef __cplusplus
 }

@@ -127,6 +127,10 @@ def _setup(_lib):
                                                     ctypes.c_double, ctypes.c_double, _dp]
         _lib.orc_convolve.argtypes = [ctypes.c_int, ctypes.c_int, _dp, ctypes.c_double, _dp, _dp]
         _lib.orc_convolve_direct.argtypes = [ctypes.c_int, ctypes.c_int, _dp, ctypes.c_double, _dp, _dp]
+        _subs = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                 _dp, _dp, _dp, _dp, _dp, ctypes.c_int, _dp, _dp]
+        _lib.orc_subsurf_points.argtypes = _subs
+        _lib.orc_subsurf_depths.argtypes = _subs
     return _lib
 
 
@@ -210,3 +214,36 @@ def convolve(cf_block, ga, p, direct=False):
     fn = lib().orc_convolve_direct if direct else lib().orc_convolve
     fn(mx, my, _dptr(cb), float(ga), _dptr(pp), _dptr(u))
     return u
+
+
+SUBS_COLS = ("ux", "uy", "uz", "sighyd", "sigvm", "sigtr", "sigma1", "sigma2", "sigma3",
+             "sxx", "sxy", "sxz", "syx", "syy", "syz", "szx", "szy", "szz")
+
+
+def _subs_args(grid, pn, px, py, gg, poiss):
+    mx, my, dx, dy, xc1, yc1 = grid
+    arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (pn, px, py)]
+    g = np.ascontiguousarray(gg if np.ndim(gg) else (gg, gg), dtype=np.float64)
+    nu = np.ascontiguousarray(poiss if np.ndim(poiss) else (poiss, poiss), dtype=np.float64)
+    return [int(mx), int(my), float(dx), float(dy), float(xc1), float(yc1)] + [_dptr(a) for a in arrs] + \
+        [_dptr(g), _dptr(nu)], arrs + [g, nu]
+
+
+def subsurf_points(grid, pn, px, py, gg, poiss, xyz, fast=False):
+    """Subsurface field at arbitrary points (direct sum); grid = (mx, my, dx, dy, xc1, yc1).
+    Returns an (npts, 18) array with the columns SUBS_COLS."""
+    args, keep = _subs_args(grid, pn, px, py, gg, poiss)
+    pts = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((pts.shape[0], len(SUBS_COLS)))
+    lib(fast).orc_subsurf_points(*args, pts.shape[0], _dptr(pts), _dptr(out))
+    return out
+
+
+def subsurf_depths(grid, pn, px, py, gg, poiss, z, fast=False):
+    """Subsurface field at every element centre at each depth z (influence coefficients and
+    FFT convolution).  Returns an (nz, my*mx, 18) array."""
+    args, keep = _subs_args(grid, pn, px, py, gg, poiss)
+    zz = np.ascontiguousarray(z, dtype=np.float64).ravel()
+    out = np.zeros((zz.size, int(grid[0]) * int(grid[1]), len(SUBS_COLS)))
+    lib(fast).orc_subsurf_depths(*args, zz.size, _dptr(zz), _dptr(out))
+    return out

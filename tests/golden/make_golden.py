@@ -29,6 +29,12 @@ fixtures next to this script:
   (dy 200 mm, SteadyGS, eps 1e-5), printed with its element tables: the approach to 8 digits,
   pn per element after NORM, element codes, px and shift sx after TANG, totals and counts.
 
+* examples/subsurf.ref_subs + subsurf.ref_out -> subsurf.json
+  the subsurface elastic field of one loaded 1x1 mm element (pressure 1, traction 0.999):
+  displacements, hydrostatic and von Mises stresses and the six stress components at 15
+  depths below one point and below a 7x7 subgrid of a 21x21 block, as printed, and the
+  printed maxima of both cases (pressure alone and with traction).
+
 * testbank/test_caddon.ref_out -> test_caddon_re1.json
   output of src/test_caddon.f90 for result element 1 (module 3 through the library
   interface in SPCK units: Hertzian 21x33 grid, penetration prescribed, creepage 0.001,
@@ -320,6 +326,43 @@ def parse_contact_nonhz(path):
             "cases": [rec]}
 
 
+SUBS_PICK = (0, 4, 8, 10, 12, 16, 20)      # x and y indices of the 21 x 21 block kept in the fixture
+
+
+def parse_subsurf(root):
+    """examples/subsurf.inp: one 1x1 mm element, G 1, nu 0.28, pn = 1; case 1 the pressure
+    alone, case 2 with the traction px = 0.999 (Fx prescribed, the element in adhesion).
+    From subsurf.ref_subs (written by case 2): the field at all 15 depths of block 1 and of a
+    7x7 subgrid of block 2, as printed (the strings keep their printed precision); from
+    subsurf.ref_out: the printed block summaries (maxima and their positions) of both
+    cases."""
+    rows = [ln.split() for ln in open(os.path.join(root, "examples", "subsurf.ref_subs"))
+            if not ln.startswith("%")]
+    heads = [i for i, r in enumerate(rows) if len(r) == 14 and r[3] == "0.000"]
+    b1 = rows[heads[0] + 1:heads[1]]
+    b2 = rows[heads[1] + 1:]
+    n2 = 21
+    keep2 = [r for k, r in enumerate(b2) if (k % n2) in SUBS_PICK and ((k // n2) % n2) in SUBS_PICK]
+    text = open(os.path.join(root, "examples", "subsurf.ref_out")).read()
+    summaries = []
+    for case_no, body in enumerate(re.split(r"\n Case\s+\d+\n", text)[1:], start=1):
+        for nb, blk in re.findall(r"SUBSURFACE STRESSES BLOCK\s+(\d):\s*\n(.*?)\n\n", body + "\n\n", re.S):
+            for ln in blk.strip().splitlines():
+                m = re.match(r"\s*(ABSMAX|MAX|MIN)\s+(\w+)\s*=\s*(\S+)\s+AT \(X,Y,Z\) = \(\s*(\S+),\s*(\S+),\s*(\S+)\)",
+                             ln)
+                if m:
+                    summaries.append({"case": case_no, "block": int(nb), "kind": m.group(1), "quantity": m.group(2),
+                                      "value": float(m.group(3)), "at": [float(m.group(k)) for k in (4, 5, 6)]})
+    return {"source": "examples/subsurf.ref_subs, examples/subsurf.ref_out",
+            "columns": ["X", "Y", "Z", "UX", "UY", "UZ", "SIGHYD", "SIGVM", "SIGXX", "SIGXY", "SIGXZ", "SIGYY",
+                        "SIGYZ", "SIGZZ"],
+            "grid": {"mx": 1, "my": 1, "dx": 1.0, "dy": 1.0, "xc1": 0.0001, "yc1": 0.0002}, "gg": 1.0, "poiss": 0.28,
+            "tractions": {"1": [1.0, 0.0, 0.0], "2": [1.0, 0.999, 0.0]},
+            "block1": b1, "block2_subgrid": keep2, "block2_pick": list(SUBS_PICK),
+            "block2_x": [float(r[0]) for r in b2[:n2]], "block2_y": [float(b2[k * n2][1]) for k in range(n2)],
+            "block2_z": [float(b2[k * n2 * n2][2]) for k in range(len(b2) // (n2 * n2))], "summaries": summaries}
+
+
 def parse_test_caddon(path):
     text = open(path).read()
     block = text.split("...start processing of Result Element")[1]     # element 1, first solve
@@ -364,6 +407,9 @@ def main():
     cn = parse_contact_nonhz(os.path.join(root, "testbank", "contact_nonhz.ref_out"))
     with open(os.path.join(HERE, "contact_nonhz_re1.json"), "w") as f:
         json.dump(cn, f, indent=0)
+    ss = parse_subsurf(root)
+    with open(os.path.join(HERE, "subsurf.json"), "w") as f:
+        json.dump(ss, f, separators=(",", ":"))
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)
