@@ -44,6 +44,11 @@ struct Case {
     // Newton-Raphson history on the creepages: per iteration ittang, itnr, cksi, Fx/(mu Fn),
     // ceta, Fy/(mu Fn), solver iterations
     std::vector<double> nr_hist;
+    // ConvexGS: contact elements, leading edge, and for steady rolling csv = cs - cv
+    std::vector<int> iel, ii2j;
+    Ledg ledg;
+    Inflcf csv;
+    bool have_csv = false;
 };
 
 constexpr int iout_fn = 0, iout_fx1 = 1, iout_fy1 = 2, iout_mz1 = 3;
@@ -192,6 +197,9 @@ int tang_solver(Case &c, const GF3 &wstot, int &info1, double &err, bool is_sens
                         is_sens);
     } else if (c.solver_eff == isolv_tangcg) {
         it = tangcg(tc, maxit, eps, wstot, c.cs, c.ms, c.igs, c.mus, c.ps, c.ss, err, bad, is_sens);
+    } else if (c.solver_eff == isolv_cnvxgs) {
+        it = cnvxgs(tc, wstot, c.cs, c.have_csv ? &c.csv : nullptr, c.ledg, c.ii2j, c.iel, c.igs, c.mus, c.ps, c.ss,
+                    eps, maxit, tc.omegah, tc.omegas, info1, err, is_sens);
     } else {
         c.unsupported = true;
         return 0;
@@ -456,9 +464,24 @@ int stang(Case &c) {
             else { tc.omegah = 0.8; tc.omegas = 0.6; }
         } else { tc.omegah = 0.5; tc.omegas = 0.5; }
     }
-    if (c.solver_eff == isolv_cnvxgs) { c.unsupported = true; return -1; }
-    std::vector<double> facdt; std::vector<int> ii2j;
-    sxbnd(tc, c.solver_eff, c.igs, c.g, facdt, ii2j);
+    std::vector<double> facdt;
+    sxbnd(tc, c.solver_eff, c.igs, c.g, facdt, c.ii2j, &c.ledg);
+    c.iel = iel;
+    if (c.solver_eff == isolv_cnvxgs && is_ssrol && !c.have_csv) {
+        // csv, m_visc.f90:289-354 (no dq scaling): the tangential rows of cs minus those of the
+        // coefficients shifted by one rolling step; the normal row of cs
+        Inflcf sh; sh.alloc(mx, my, c.dx, c.dy);
+        elascf_pcwcns(c.ak, c.nu, mx, my, c.dx, c.dy, std::cos(c.chi) * c.dq, std::sin(c.chi) * c.dq, sh);
+        c.csv.alloc(mx, my, c.dx, c.dy);
+        c.csv.ga = c.ga; c.csv.ga_inv = 1.0 / c.ga; c.csv.nt_cpl = c.cs.nt_cpl;
+        for (int jk = 0; jk < 3; jk++)
+            for (size_t q = 0; q < c.cs.cf[0][0].size(); q++) {
+                c.csv.cf[0][jk][q] = c.cs.cf[0][jk][q] - sh.cf[0][jk][q];
+                c.csv.cf[1][jk][q] = c.cs.cf[1][jk][q] - sh.cf[1][jk][q];
+                c.csv.cf[2][jk][q] = c.cs.cf[2][jk][q];
+            }
+        c.have_csv = true;
+    }
     c.mus.assign(npot, pb->fstat);
     GF3 wsfix; wsfix.init(npot);
     stang_rhs(c, iel, facdt, wsfix);

@@ -1,8 +1,9 @@
 // CPU ORACLE -- test infrastructure only (see contact_oracle.h).
 //
 // Tangential problem: stang (m_stang.f90:28-746), stang_rhs (:749-951), leading edge
-// sxbnd (m_leadedge.f90:92-332), the solvers SteadyGS (m_solvpt.f90:2825-3254),
-// GDsteady (gdsteady.f90:9-1462) and TangCG (m_solvpt.f90:1841-2442).
+// sxbnd and subnd (m_leadedge.f90:92-394), the solvers SteadyGS (m_solvpt.f90:2825-3254),
+// ConvexGS (m_solvpt.f90:2446-2821), GDsteady (gdsteady.f90:9-1462) and TangCG
+// (m_solvpt.f90:1841-2442).
 #pragma once
 #include "orc_conv.hpp"
 #include "orc_elm.hpp"
@@ -22,9 +23,18 @@ struct TangCtx {
     double fdecay, betath, d_ifc, d_lin, d_cns, d_slp, pow_s;
 };
 
+// Leading edge of the contact area (t_leadedge, m_leadedge.f90:20-70): per row iy the
+// positions jbnd[iy-1] .. jbnd[iy]-1 (1-based), their last interior column ixbnd, their
+// relative offset facdx to the edge and the rolling direction ixinc
+struct Ledg {
+    std::vector<int> jbnd, ixbnd;
+    std::vector<double> facdx;
+    int ixinc = 1;
+};
+
 // sxbnd, m_leadedge.f90:92-332: facdt per element, leading edge index map ii2j (0 = none)
 inline void sxbnd(const TangCtx &cx, int solver_eff, const Eldiv &igs, const Grid &g,
-                  std::vector<double> &facdt, std::vector<int> &ii2j) {
+                  std::vector<double> &facdt, std::vector<int> &ii2j, Ledg *ledg = nullptr) {
     const int mx = cx.mx, my = cx.my;
     bool is_roll = cx.tang == 2 || cx.tang == 3;
     int ixsta, ixinc, ixend;
@@ -78,6 +88,33 @@ inline void sxbnd(const TangCtx &cx, int solver_eff, const Eldiv &igs, const Gri
             if (ix == ixend) break;
         }
     }
+    if (ledg) {
+        ledg->jbnd = jbnd;
+        ledg->ixbnd = ixbnd;
+        ledg->facdx.assign(npos + 1, fxdfac);
+        ledg->ixinc = ixinc;
+    }
+}
+
+// subnd, m_leadedge.f90:336-394: the tangential displacement difference at each leading edge
+// position, interpolated between its last interior element and the next one; zero where the
+// edge is within two elements of the grid's end
+inline void subnd(const TangCtx &cx, const Ledg &L, const GF3 &p, const Eldiv &pe, const Inflcf &c,
+                  std::vector<double> &ubnd) {
+    const int mx = cx.mx, my = cx.my, ixinc = L.ixinc;
+    const int npos = L.jbnd[my];
+    ubnd.assign((size_t)2 * (npos + 1), 0.0);
+    for (int iy = 1; iy <= my; iy++)
+        for (int j = L.jbnd[iy - 1]; j <= L.jbnd[iy] - 1; j++) {
+            const int ix0 = L.ixbnd[j];
+            if ((ixinc > 0 && ix0 + 2 > mx) || (ixinc < 0 && ix0 - 2 <= 0)) continue;
+            const int ii = (ix0 - 1) + (iy - 1) * mx;
+            for (int ik = 1; ik <= 2; ik++) {
+                const double u0 = aijpj(ii, ik, p, pe, -3, c, mx, my);
+                const double u1 = aijpj(ii + ixinc, ik, p, pe, -3, c, mx, my);
+                ubnd[(size_t)2 * j + ik - 1] = (1.0 - L.facdx[j]) * u0 + L.facdx[j] * u1;
+            }
+        }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -168,6 +205,89 @@ inline int stdygs(const TangCtx &cx, const GF3 &ws, Inflcf &cs, Eldiv &igs, cons
                     }
                 }
             }
+        }
+        dif = std::sqrt(dif / (2.0 * k));
+        if (!is_sens) {
+            difid = eps * std::max(1e-6, facnel * gf_rms(AllElm, ps, ikTANG, igs));
+        } else {
+            gf_copy(AllElm, ps, tmp, ikTANG, igs);
+            gf_axpy(AllElm, -1.0, ps0, tmp, ikTANG, igs);
+            difid = eps * std::max(1e-6, facnel * gf_rms(AllElm, tmp, ikTANG, igs));
+        }
+        if (itgs == 1) dif1 = dif;
+    }
+    double conv = 1.0;
+    if (dif * dif1 != 0.0 && itgs > 1) conv = std::exp(std::log(dif / dif1) / (itgs - 1));
+    err = dif;
+    info = 0;
+    if (itgs >= maxgs) info = 1;
+    if (itgs >= maxgs && conv > 0.997) info = 2;
+    if (itgs >= maxgs && conv > 1.0) info = 3;
+    return itgs;
+}
+
+// ------------------------------------------------------------------------------------------
+// ConvexGS, m_solvpt.f90:2446-2821 (elastic, no third-body layer): block Gauss-Seidel over the
+// contact elements in the order of iel (reversed for chi = pi) with the element solver plstrc.
+// Shifts per element from the current tractions: cs for shifts and transient rolling (T=1, 2);
+// for steady rolling (T=3) csv = cs - cv (the displacement difference of one rolling step), or
+// near the leading edge cs minus the edge estimate ubnd (subnd, refreshed every sweep).
+// ------------------------------------------------------------------------------------------
+inline int cnvxgs(const TangCtx &cx, const GF3 &ws, Inflcf &cs, const Inflcf *csv, const Ledg &L,
+                  const std::vector<int> &ii2j, const std::vector<int> &iel, Eldiv &igs,
+                  const std::vector<double> &mus, GF3 &ps, GF3 &ss, double eps, int maxgs, double omegah,
+                  double omegas, int &info, double &err, bool is_sens = false) {
+    const int mx = cx.mx, my = cx.my, npot = cx.npot, k = (int)iel.size();
+    const bool is_ssrol = cx.tang == 3;
+    if (k == 0) { info = 0; err = 0.0; return 0; }
+    GF3 ps0, tmp;
+    if (is_sens) { ps0 = ps; tmp.init(npot); }
+    int ista, iinc, iend;
+    if (std::fabs(cx.chi - pi) < 0.01) { ista = k - 1; iinc = -1; iend = 0; }
+    else { ista = 0; iinc = 1; iend = k - 1; }
+    double coefs[2][2], coefsv[2][2];
+    coefs[0][0] = cs.ga_inv * cs.at(0, 0, 1, 1); coefs[0][1] = cs.ga_inv * cs.at(0, 0, 1, 2);
+    coefs[1][0] = cs.ga_inv * cs.at(0, 0, 2, 1); coefs[1][1] = cs.ga_inv * cs.at(0, 0, 2, 2);
+    const Inflcf &cv = csv ? *csv : cs;
+    coefsv[0][0] = cv.ga_inv * cv.at(0, 0, 1, 1); coefsv[0][1] = cv.ga_inv * cv.at(0, 0, 1, 2);
+    coefsv[1][0] = cv.ga_inv * cv.at(0, 0, 2, 1); coefsv[1][1] = cv.ga_inv * cv.at(0, 0, 2, 2);
+    int nadh, nslip, nplst, nexter;
+    eldiv_count(igs, nadh, nslip, nplst, nexter);
+    const double facnel = std::sqrt((double)(float)npot / (double)(float)(nadh + nslip + nplst));
+    int itgs = 0;
+    double dif = 2.0, difid = 1.0, dif1 = 0.0;
+    std::vector<double> ubnd;
+    while (dif >= difid && itgs < maxgs) {
+        itgs++;
+        dif = 0.0;
+        if (is_ssrol) subnd(cx, L, ps, igs, cs, ubnd);
+        for (int i = ista; ; i += iinc) {
+            const int ii = iel[i];
+            if (itgs <= 1000 || itgs % 2 == 0 || igs.el[ii] == Adhes) {
+                double pr[3] = {ps.c[0][ii], ps.c[1][ii], ps.c[2][ii]};
+                double dupl[2] = {0.0, 0.0}, taucs = 0.0;
+                const bool zledge = is_ssrol && ii2j[ii] > 0;
+                double s[2];
+                if (!is_ssrol) {
+                    s[0] = ws.c[0][ii] + aijpj(ii, ikX, ps, igs, ikTANG, cs, mx, my);
+                    s[1] = ws.c[1][ii] + aijpj(ii, ikY, ps, igs, ikTANG, cs, mx, my);
+                } else if (!zledge) {
+                    s[0] = ws.c[0][ii] + aijpj(ii, ikX, ps, igs, ikTANG, cv, mx, my);
+                    s[1] = ws.c[1][ii] + aijpj(ii, ikY, ps, igs, ikTANG, cv, mx, my);
+                } else {
+                    const int j = ii2j[ii];
+                    s[0] = ws.c[0][ii] + aijpj(ii, ikX, ps, igs, ikTANG, cs, mx, my) - ubnd[(size_t)2 * j];
+                    s[1] = ws.c[1][ii] + aijpj(ii, ikY, ps, igs, ikTANG, cs, mx, my) - ubnd[(size_t)2 * j + 1];
+                }
+                int el = igs.el[ii];
+                plstrc(el, (!is_ssrol || zledge) ? coefs : coefsv, eps, omegah, omegas, pr, mus[ii], false, 0.0, 0.0,
+                       0.0, taucs, s, dupl);
+                igs.el[ii] = el;
+                dif += (ps.c[0][ii] - pr[0]) * (ps.c[0][ii] - pr[0]) + (ps.c[1][ii] - pr[1]) * (ps.c[1][ii] - pr[1]);
+                ps.c[0][ii] = pr[0]; ps.c[1][ii] = pr[1];
+                ss.c[0][ii] = s[0]; ss.c[1][ii] = s[1];
+            }
+            if (i == iend) break;
         }
         dif = std::sqrt(dif / (2.0 * k));
         if (!is_sens) {

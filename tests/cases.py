@@ -109,6 +109,20 @@ def catt_to_cart_case1():
                 prmudf=[0.002963, 0.0, 0.002963, 0.0, 0.0, 0.0])
 
 
+def subsurf_case(icase):
+    """examples/subsurf.inp: one 1x1 mm element (first corner at -0.4999, -0.4998), G 1, nu
+    0.28, mu 1, Fn 1, geometry 2.16 (x^2 + y^2), eps 1e-6.  Case 1: the normal problem alone.
+    Case 2: steady rolling with Fx = 0.999 mu Fn prescribed (F=1); contact reaches the
+    trailing column, so the reference solves it by ConvexGS."""
+    c = dict(tang=0, norm=1, bound=0, gausei=0, maxgs=80, maxin=100, maxnr=30, maxout=1, eps=1e-6, poiss=0.28,
+             gg=1.0, fstat=1.0, veloc=30000.0, fn=1.0, cksi=0.0, ceta=0.0, cphi=0.0,
+             ipotcn=1, potprm=[1, 1, -0.4999, -0.4998, 1.0, 1.0], prmudf=[2.16, 0.0, 2.16, 0.0, 0.0, 0.0])
+    if icase == 2:
+        del c["cksi"]
+        c.update(tang=3, force3=1, fxrel=0.999)
+    return c
+
+
 def carter2d_case():
     """examples/carter2d.inp: Carter's two-dimensional steady rolling (T=3, SteadyGS, eps 1e-5)
     on a 55x1 strip from x = -1.05 mm with dx 0.04 mm and dy 200 mm, steel (G 82000, nu
@@ -133,6 +147,8 @@ def testbank_case(icase):
     """Cases of testbank/testbank.inp.  1: shift problem (T=1) with prescribed approach
     0.01131 mm and shift 0.00304 mm, steel, mu 0.3, quadratic geometry 0.0056566 (x^2 + y^2)
     on a 17x17 grid from -1.13333 mm with spacing 0.13333 mm, TangCG, eps 1e-8.
+    6: Carter's strip (as examples/carter2d.inp, first centre at -1.045 mm) by ConvexGS (G=2,
+    omegah = omegas = 0.8) with a rolling step dq of 0.2 mm = 5 dx.
     7: steady rolling, Fn 0.4705, creepage -0.00304, mu 0.4013, G 1, nu 0.28, dq 0.2 mm,
     quadratic geometry 0.002963 (x^2 + y^2) on a 41x41 grid from -4.1 mm with spacing 0.2 mm,
     SteadyGS with maxgs 80, maxin 30, eps 1e-6.
@@ -140,6 +156,11 @@ def testbank_case(icase):
     its corners.  13: a Cattaneo shift on a 41x41 Hertzian grid (semi-axes 4.1 mm, scale
     1.17143) with the normal problem skipped for the elliptical traction bound (B=2), Fn
     0.7563, Fx = 0.657 mu Fn prescribed (F=1), G 1, nu 0.28, mu 0.4013, TangCG, eps 1e-6."""
+    if icase == 6:
+        return dict(tang=3, norm=1, bound=0, gausei=2, maxgs=999, maxin=100, maxnr=30, maxout=1, eps=1e-5,
+                    omegah=0.8, omegas=0.8, poiss=0.28, gg=82000.0, fstat=0.3, veloc=30000.0, fn=35780.0,
+                    cksi=-0.00024, ceta=0.0, cphi=0.0, dq=0.2, ipotcn=3, potprm=[55, 1, -1.045, 0.0, 0.04, 200.0],
+                    prmudf=[0.001, 0.0, 0.0, 0.0, 0.0, 0.0])
     if icase == 10:
         return dict(tang=1, norm=1, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=1, eps=1e-8,
                     poiss=0.28, gg=82000.0, fstat=0.3, veloc=1.0, fn=1722.0, cphi=0.0, force3=2, fxrel=-0.875,
@@ -244,6 +265,8 @@ def to_oracle(case):
         pb.chi = case["chi"]
     pb.cksi, pb.ceta, pb.cphi = case.get("cksi", 0.0), case.get("ceta", 0.0), case.get("cphi", 0.0)
     pb.force3 = case.get("force3", 0)
+    if "omegah" in case:
+        pb.omegah, pb.omegas = case["omegah"], case["omegas"]
     pb.fxrel, pb.fyrel = case.get("fxrel", 0.0), case.get("fyrel", 0.0)
     pb.sens = case.get("sens", 1)
     if pb.norm == 1:

@@ -30,7 +30,10 @@ fixtures next to this script:
   pn per element after NORM, element codes, px and shift sx after TANG, totals and counts.
 
 * examples/subsurf.ref_subs + subsurf.ref_out -> subsurf.json
-  the subsurface elastic field of one loaded 1x1 mm element (pressure 1, traction 0.999):
+  the two solves of examples/subsurf.inp (one 1x1 mm element: the normal problem, then
+  steady rolling with Fx prescribed, which the reference solves by ConvexGS and
+  Newton-Raphson) with their printed results, and the subsurface elastic field of the second
+  one's tractions (pressure 1, traction 0.999):
   displacements, hydrostatic and von Mises stresses and the six stress components at 15
   depths below one point and below a 7x7 subgrid of a 21x21 block, as printed, and the
   printed maxima of both cases (pressure alone and with traction).
@@ -50,7 +53,7 @@ fixtures next to this script:
 * testbank/testbank.ref_out -> testbank_cases.json
   cases 1, 7, 10 and 13 of testbank/testbank.inp, the stand-alone program's regression set:
   case 1 the shift problem with prescribed approach (17x17 quadratic geometry, TangCG, eps
-  1e-8), case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6), case 10
+  1e-8), case 6 Carter's strip by ConvexGS (G=2) with a rolling step of 5 dx, case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6), case 10
   the same shift with Fn, Fx and Fy prescribed (F=2, Newton-Raphson on both shifts), case 13
   a shift on a 41x41 Hertzian grid with the normal problem skipped (B=2) and Fx prescribed
   (F=1).  The other cases use features outside this library (ConvexGS, bilinear loading,
@@ -267,7 +270,7 @@ def parse_carter2d(path):
     return {"source": "examples/carter2d.ref_out", "cases": [rec]}
 
 
-def parse_testbank(path, wanted=(1, 7, 10, 13)):
+def parse_testbank(path, wanted=(1, 6, 7, 10, 13)):
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
     out = []
@@ -344,6 +347,19 @@ def parse_subsurf(root):
     n2 = 21
     keep2 = [r for k, r in enumerate(b2) if (k % n2) in SUBS_PICK and ((k // n2) % n2) in SUBS_PICK]
     text = open(os.path.join(root, "examples", "subsurf.ref_out")).read()
+    solves = []
+    for case_no, body in enumerate(re.split(r"\n Case\s+\d+\n", text)[1:], start=1):
+        rec = {"case": case_no}
+        m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+        rec["norm_itcg"] = int(m.group(3))
+        _tang_final(rec, body)
+        nr = _nr_history(body)
+        if nr:
+            rec["nr"] = nr
+            rec["sens"] = _sensitivities(body)
+        rec.update(_results_block(body))
+        rec.pop("picture", None)
+        solves.append(rec)
     summaries = []
     for case_no, body in enumerate(re.split(r"\n Case\s+\d+\n", text)[1:], start=1):
         for nb, blk in re.findall(r"SUBSURFACE STRESSES BLOCK\s+(\d):\s*\n(.*?)\n\n", body + "\n\n", re.S):
@@ -356,11 +372,11 @@ def parse_subsurf(root):
     return {"source": "examples/subsurf.ref_subs, examples/subsurf.ref_out",
             "columns": ["X", "Y", "Z", "UX", "UY", "UZ", "SIGHYD", "SIGVM", "SIGXX", "SIGXY", "SIGXZ", "SIGYY",
                         "SIGYZ", "SIGZZ"],
-            "grid": {"mx": 1, "my": 1, "dx": 1.0, "dy": 1.0, "xc1": 0.0001, "yc1": 0.0002}, "gg": 1.0, "poiss": 0.28,
-            "tractions": {"1": [1.0, 0.0, 0.0], "2": [1.0, 0.999, 0.0]},
+            "gg": 1.0, "poiss": 0.28,
             "block1": b1, "block2_subgrid": keep2, "block2_pick": list(SUBS_PICK),
             "block2_x": [float(r[0]) for r in b2[:n2]], "block2_y": [float(b2[k * n2][1]) for k in range(n2)],
-            "block2_z": [float(b2[k * n2 * n2][2]) for k in range(len(b2) // (n2 * n2))], "summaries": summaries}
+            "block2_z": [float(b2[k * n2 * n2][2]) for k in range(len(b2) // (n2 * n2))], "summaries": summaries,
+            "solves": solves}
 
 
 def parse_test_caddon(path):

@@ -1,7 +1,8 @@
 """Subsurface stresses in the CPU oracle (oracle/orc_subsurf.hpp) against the reference's printed
-field (examples/subsurf.ref_subs, .ref_out; fixture tests/golden/subsurf.json), against Love's
-closed form for the stress below a uniformly loaded rectangle, and its FFT path (element
-centres, per-depth influence coefficients) against its direct path.
+field (examples/subsurf.ref_subs, .ref_out; fixture tests/golden/subsurf.json) of the oracle's
+own solves of examples/subsurf.inp, against Love's closed form for the stress below a uniformly
+loaded rectangle, and its FFT path (element centres, per-depth influence coefficients) against
+its direct path.
 """
 import json
 import math
@@ -33,16 +34,50 @@ def _half_unit(tok):
     return 0.5 * 10.0 ** (-(len(t.split(".")[1]) if "." in t else 0))
 
 
+_SOLVES = {}
+
+
+def _solve(case):
+    if case not in _SOLVES:
+        _SOLVES[case] = C.oracle_solve(C.subsurf_case(case))
+    return _SOLVES[case]
+
+
 def _field(po, g, case, pts):
-    pn, px, py = g["tractions"][str(case)]
-    gr = g["grid"]
-    return po.subsurf_points((gr["mx"], gr["my"], gr["dx"], gr["dy"], gr["xc1"], gr["yc1"]), [pn], [px], [py],
-                             g["gg"], g["poiss"], pts)
+    """The field of the oracle's own solution of the example's case (1: pressure alone,
+    2: pressure and the traction found by ConvexGS and Newton-Raphson)."""
+    r = _solve(case)
+    grid = (r["mx"], r["my"], r["dx"], r["dy"], r["xc1"], r["yc1"])
+    return po.subsurf_points(grid, r["pn"], r["px"], r["py"], g["gg"], g["poiss"], pts)
+
+
+def test_solves_of_the_example(oracle, gold):
+    """The two solves of examples/subsurf.inp as printed: the normal problem, and steady rolling
+    with Fx prescribed on the single element (ConvexGS inside a Newton-Raphson on cksi, three
+    iterations of two sweeps): forces, moment, elastic energy, approach, pmax to 4 digits,
+    counts and iterations exact, the Newton-Raphson rows and dFx/dcksi as printed."""
+    for g in gold["solves"]:
+        o = _solve(g["case"])
+        assert o["ierror"] >= 0 and o["itcg"] == g["norm_itcg"]
+        for key, gk in (("fn", "fn"), ("fx", "fx"), ("mz", "mz"), ("elen", "elen"), ("pen", "approach"),
+                        ("pmax", "pmax")):
+            gold_v = g[gk]
+            unit = 0.5e-4 if gold_v == 0.0 else 0.5 * 10.0 ** (math.floor(math.log10(abs(gold_v))) - 3)
+            assert abs(o[key] - gold_v) <= unit * (1 + 1e-9), (g["case"], key, o[key], gold_v)
+        assert (o["ncon"], o["nadh"], o["nslip"]) == (g["ncon"], g["nadh"], g["nslip"])
+        if "nr" in g:
+            assert o["solver"] == 3 and o["itgs"] == g["tang_it"]
+            assert [int(r[6]) for r in o["nr"]] == [r[5] for r in g["nr"]]
+            for row, gr in zip(o["nr"], g["nr"]):
+                for k, gk in ((2, 1), (3, 2)):
+                    unit = 0.5 * 10.0 ** (math.floor(math.log10(abs(gr[gk]))) - 3)
+                    assert abs(row[k] - gr[gk]) <= unit * (1 + 1e-9), (row, gr)
+            assert abs(o["sens"][1][1] - g["sens"][1][1]) <= 0.005
 
 
 def test_field_against_printed_table(oracle, gold):
-    """All printed values of block 1 and of the 7x7 subgrid of block 2 (case 2: pressure 1 and
-    traction 0.999 on one element): displacements, hydrostatic and von Mises stress and the six
+    """All printed values of block 1 and of the 7x7 subgrid of block 2 (case 2: the pressure and
+    traction of the oracle's solve, 1 and 0.999): displacements, hydrostatic and von Mises stress and the six
     stress components within half a unit of their last printed digit.  Components that vanish
     (the shear stresses on the free surface) print as rounding residues of order 1e-14; those
     are held to 1e-12 of their column's largest value instead."""
