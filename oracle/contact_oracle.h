@@ -13,8 +13,8 @@
  * examples/cattaneo.ref_out (NormCG, TangCG on the shift problem), result
  * element 1 of testbank/test_caddon.ref_out and testbank/contact_nonhz.ref_out
  * (approach prescribed, spin) and
- * cases 1, 6, 7, 10 and 13 of testbank/testbank.ref_out (TangCG shift, ConvexGS
- * strip, SteadyGS 41x41, shifts with prescribed forces),
+ * cases 1, 6, 7, 9, 10 and 13 of testbank/testbank.ref_out (TangCG shift, ConvexGS
+ * strip, SteadyGS 41x41, two coupled materials, shifts with prescribed forces),
  * and the Newton-Raphson iterations on prescribed total forces of case 2 of
  * examples/cattaneo.ref_out (F=2) and case 1 of examples/catt_to_cart.ref_out
  * (F=1), and the element tables of examples/carter2d.ref_out (55x1 strip,

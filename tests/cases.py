@@ -152,6 +152,9 @@ def testbank_case(icase):
     7: steady rolling, Fn 0.4705, creepage -0.00304, mu 0.4013, G 1, nu 0.28, dq 0.2 mm,
     quadratic geometry 0.002963 (x^2 + y^2) on a 41x41 grid from -4.1 mm with spacing 0.2 mm,
     SteadyGS with maxgs 80, maxin 30, eps 1e-6.
+    9: steady rolling with different materials (nu 0.1 and 0.28, G 1 and 81000: K = 0.4, the
+    normal and tangential problems coupled and solved alternately, maxout 10), Fn 2.468, Fx =
+    -0.4718 mu Fn prescribed, spin 1e-4, mu 0.6, 25x25 grid, SteadyGS.
     10: case 1 with Fn 1722 N, Fx = -0.875 mu Fn and Fy = 0 prescribed (F=2), the grid given by
     its corners.  13: a Cattaneo shift on a 41x41 Hertzian grid (semi-axes 4.1 mm, scale
     1.17143) with the normal problem skipped for the elliptical traction bound (B=2), Fn
@@ -161,6 +164,11 @@ def testbank_case(icase):
                     omegah=0.8, omegas=0.8, poiss=0.28, gg=82000.0, fstat=0.3, veloc=30000.0, fn=35780.0,
                     cksi=-0.00024, ceta=0.0, cphi=0.0, dq=0.2, ipotcn=3, potprm=[55, 1, -1.045, 0.0, 0.04, 200.0],
                     prmudf=[0.001, 0.0, 0.0, 0.0, 0.0, 0.0])
+    if icase == 9:
+        return dict(tang=3, norm=1, bound=0, gausei=0, maxgs=80, maxin=100, maxnr=30, maxout=10, eps=1e-6,
+                    poiss=0.1, poiss2=0.28, gg=1.0, gg2=0.81e5, fstat=0.6, veloc=1000.0, fn=2.468, ceta=0.0,
+                    cphi=1e-4, force3=1, fxrel=-0.4718, dq=1.1, ipotcn=1,
+                    potprm=[25, 25, -13.75, -13.75, 1.1, 1.1], prmudf=[0.3332e-3, 0.0, 0.3332e-3, 0.0, 0.0, 0.0])
     if icase == 10:
         return dict(tang=1, norm=1, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=1, eps=1e-8,
                     poiss=0.28, gg=82000.0, fstat=0.3, veloc=1.0, fn=1722.0, cphi=0.0, force3=2, fxrel=-0.875,
@@ -255,8 +263,8 @@ def to_oracle(case):
     pb.eps = case.get("eps", 1e-6)
     nu = case.get("poiss", 0.28)
     g = case.get("gg", 82000.0)
-    pb.poiss1 = pb.poiss2 = nu
-    pb.gg1 = pb.gg2 = g
+    pb.poiss1, pb.poiss2 = nu, case.get("poiss2", nu)
+    pb.gg1, pb.gg2 = g, case.get("gg2", g)
     pb.fstat = pb.fkin = case.get("fstat", 0.3)
     pb.veloc = case.get("veloc", 10000.0)
     if "dq" in case:

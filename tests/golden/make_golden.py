@@ -53,7 +53,8 @@ fixtures next to this script:
 * testbank/testbank.ref_out -> testbank_cases.json
   cases 1, 7, 10 and 13 of testbank/testbank.inp, the stand-alone program's regression set:
   case 1 the shift problem with prescribed approach (17x17 quadratic geometry, TangCG, eps
-  1e-8), case 6 Carter's strip by ConvexGS (G=2) with a rolling step of 5 dx, case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6), case 10
+  1e-8), case 6 Carter's strip by ConvexGS (G=2) with a rolling step of 5 dx, case 9 steady
+  rolling of two different materials (coupled normal and tangential problems), case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6), case 10
   the same shift with Fn, Fx and Fy prescribed (F=2, Newton-Raphson on both shifts), case 13
   a shift on a 41x41 Hertzian grid with the normal problem skipped (B=2) and Fx prescribed
   (F=1).  The other cases use features outside this library (ConvexGS, bilinear loading,
@@ -187,7 +188,10 @@ def _sensitivities(body):
 
 
 def _tang_final(rec, body):
-    m = re.search(r"Tang: final element division: A, S=\s*(\d+)\s+(\d+)\s+It(CG|GS)=\s*(\d+)", body)
+    """Element counts and iterations of the case's last TANG solve (the last outer iteration
+    where the normal and tangential problems are solved alternately)."""
+    ms = list(re.finditer(r"Tang: final element division: A, S=\s*(\d+)\s+(\d+)\s+It(CG|GS)=\s*(\d+)", body))
+    m = ms[-1] if ms else None
     if m:
         rec["tang_nadh"], rec["tang_nslip"] = int(m.group(1)), int(m.group(2))
         rec["tang_solver"], rec["tang_it"] = m.group(3), int(m.group(4))
@@ -270,7 +274,7 @@ def parse_carter2d(path):
     return {"source": "examples/carter2d.ref_out", "cases": [rec]}
 
 
-def parse_testbank(path, wanted=(1, 6, 7, 10, 13)):
+def parse_testbank(path, wanted=(1, 6, 7, 9, 10, 13)):
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
     out = []
@@ -280,8 +284,8 @@ def parse_testbank(path, wanted=(1, 6, 7, 10, 13)):
             continue
         body = blocks[k + 1]
         rec = {"case": icase}
-        m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
-        rec["norm_itcg"] = int(m.group(3)) if m else 0          # 0: normal problem skipped (B=2)
+        ms = re.findall(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+        rec["norm_itcg"] = int(ms[-1][2]) if ms else 0          # last NORM; 0: skipped (B=2)
         _tang_final(rec, body)
         nr = _nr_history(body)
         if nr:

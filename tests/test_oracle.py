@@ -409,7 +409,8 @@ def test_contact_nonhz_element1(oracle):
 
 def test_testbank_cases_against_golden(oracle):
     """testbank/testbank.inp cases 1 (shift, approach prescribed, TangCG), 6 (Carter's strip by
-    ConvexGS with a rolling step of 5 dx), 7 (steady rolling, SteadyGS, 41x41), 10 (shift with
+    ConvexGS with a rolling step of 5 dx), 7 (steady rolling, SteadyGS, 41x41), 9 (two
+    materials: coupled normal and tangential problems, ten outer iterations), 10 (shift with
     Fn, Fx, Fy prescribed) and 13 (Hertzian shift, normal problem skipped, Fx prescribed):
     forces, moment, approach, pmax and elastic energy to the printed 4 digits; element counts,
     pictures and the NormCG and TangCG/SteadyGS/ConvexGS iteration counts exact; the
