@@ -238,6 +238,11 @@ def setcreepages(ire, icp, vx, vy, phi):
     load().cntc_setcreepages(_i(ire), _i(icp), _d(vx), _d(vy), _d(phi))
 
 
+def settangentialforces(ire, icp, fx, fy):
+    """Total tangential forces relative to fstat Fn (used with the F digit 1 or 2)."""
+    load().cntc_settangentialforces(_i(ire), _i(icp), _d(fx), _d(fy))
+
+
 def calculate(ire, icp):
     _require_gpu()
     ierr = ctypes.c_int(0)
@@ -445,7 +450,8 @@ def setup_case(ire, icp, case):
     """Apply a case description (the same dict the tests hand to the oracle) to (ire, icp).
 
     Keys: tang, norm, bound, gausei, maxgs, maxin, maxnr, maxout, eps, gd (8 floats + kdowfb
-    for G=5), poiss, gg, fstat, veloc, cksi, ceta, cphi, fn | pen, ipotcn, potprm,
+    for G=5), poiss, gg (poiss2, gg2 for a different body 2), fstat, veloc, cksi, ceta, cphi,
+    force3 with fxrel, fyrel (total forces prescribed), fn | pen, ipotcn, potprm,
     h (element-wise undeformed distance, optional), prmudf (6 coefficients of a quadratic
     undeformed distance, ibase 1, optional), mixed (0-4), dq and chi (optional), group (CTAs
     per patch: 0 automatic, 1 one CTA, n >= 2 a cooperative group of at most n)."""
@@ -456,7 +462,10 @@ def setup_case(ire, icp, case):
     setfrictionmethod(ire, icp, 0, [case.get("fstat", 0.3), case.get("fstat", 0.3)])
     nu = case.get("poiss", 0.28)
     g = case.get("gg", 82000.0)
-    setmaterialparameters(ire, icp, 0, [nu, nu, g, g])
+    setmaterialparameters(ire, icp, 0, [nu, case.get("poiss2", nu), g, case.get("gg2", g)])
+    if case.get("force3", 0) >= 1:
+        setflags(ire, icp, [CNTC_ic_force], [case["force3"]])
+        settangentialforces(ire, icp, case.get("fxrel", 0.0), case.get("fyrel", 0.0))
     setreferencevelocity(ire, icp, case.get("veloc", 10000.0))
     gdig = case.get("gausei", 0)
     ip = [case.get("maxgs", 999), case.get("maxin", 100), case.get("maxnr", 30), case.get("maxout", 1)]

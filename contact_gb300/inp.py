@@ -13,7 +13,7 @@ Values that a case does not repeat keep their previous value, as in the program:
 with G=1 keeps the solver settings, D=0 the potential contact, Z<2 the geometry.
 
 Supported: control digits of module 3, creepages or total forces prescribed (F=0, 1, 2),
-with Coulomb friction (L=0, V=0), elastic materials
+with Coulomb friction (L=0, V=0), elastic materials (two different bodies: keys poiss2, gg2)
 (M=0), no thin-sheet, heat, extra-rigid-slip or subsurface inputs; potential contact
 IPOTCN -3..-1 and 1..4; geometry IBASE 1 (quadratic), 2 (circular in x, tabulated in y),
 3 (sines in x) and 9 (element-wise), planform IPLAN 1.  IBASE 2 and 3 are evaluated here
@@ -263,13 +263,13 @@ def read_inp(text):
                 else:
                     cases.append({"unsupported": "geometry IBASE=%d" % ib})
                     break
-        if st["poiss"][0] != st["poiss"][1] or st["gg"][0] != st["gg"][1]:
-            cases.append({"unsupported": "different materials of the two bodies"})
-            break
         c.update(tang=pb["T"], norm=pb["N"], bound=pb["B"], pvtime=pb["P"], iestim=xh["I"],
                  gausei=st.get("gausei", 0), maxgs=st["maxgs"], maxin=st["maxin"], maxnr=st["maxnr"],
                  maxout=st["maxout"], eps=st["eps"], poiss=st["poiss"][0], gg=st["gg"][0], fstat=st["fstat"],
+                 standalone=True,
                  veloc=st["veloc"], ipotcn=pot["ipotcn"], potprm=[pot["mx"], pot["my"]] + list(pot["prm"]))
+        if st["poiss"][0] != st["poiss"][1] or st["gg"][0] != st["gg"][1]:
+            c["poiss2"], c["gg2"] = st["poiss"][1], st["gg"][1]
         if st["gd"] is not None:
             c["gd"] = dict(st["gd"])
         if pb["T"] in (2, 3):

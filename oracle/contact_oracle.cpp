@@ -547,8 +547,11 @@ void soutpt(Case &c, orc_result *r) {
     int nadh, nslip, nplast, nexter;
     eldiv_count(c.igs, nadh, nslip, nplast, nexter);
     if (c.pb->norm == 0) c.fntrue = c.dxdy * gf_sum(AllElm, c.ps, ikZ, c.igs);
-    double fxrel = c.dxdy * gf_sum(AllElm, c.ps, ikX, c.igs) / (c.fntrue * c.muscal + tiny_);
-    double fyrel = c.dxdy * gf_sum(AllElm, c.ps, ikY, c.igs) / (c.fntrue * c.muscal + tiny_);
+    // prescribed total forces are reported as prescribed (m_soutpt.f90:427-434)
+    double fxrel = (c.pb->force3 >= 1) ? c.pb->fxrel
+                                       : c.dxdy * gf_sum(AllElm, c.ps, ikX, c.igs) / (c.fntrue * c.muscal + tiny_);
+    double fyrel = (c.pb->force3 >= 2) ? c.pb->fyrel
+                                       : c.dxdy * gf_sum(AllElm, c.ps, ikY, c.igs) / (c.fntrue * c.muscal + tiny_);
     double fxtrue = fxrel * (c.fntrue * c.muscal + tiny_);
     double fytrue = fyrel * (c.fntrue * c.muscal + tiny_);
     double dx_y = 0, dy_x = 0;
@@ -660,7 +663,7 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     c.ak = (c.ga / 4.0) * ((1.0 - 2.0 * p1) / gg1 - (1.0 - 2.0 * p2) / gg2);
     c.maxout = pb->maxout;
     if (c.maxout >= 2 && std::fabs(c.ak) < 1e-4) c.maxout = 1;
-    if (c.maxout <= 1 && std::fabs(c.ak) >= 1e-4) c.maxout = 10;
+    if (c.maxout <= 1 && std::fabs(c.ak) >= 1e-4 && !pb->standalone) c.maxout = 10;
     c.fntrue = pb->fn; c.pen = pb->pen;
     c.cksi = pb->cksi; c.ceta = pb->ceta; c.cphi = pb->cphi;
     c.chi = pb->chi; c.veloc = pb->veloc;
@@ -760,6 +763,9 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
             c.ps.vy(ii) = pb->py_init ? pb->py_init[ii] : 0.0;
         }
     }
+    if (pb->sens_init)
+        for (int io = 0; io < 4; io++)
+            for (int ji = 0; ji < 4; ji++) c.sens[io][ji] = pb->sens_init[io + 4 * ji];
     init_curr_data(c, ihertz);
     // solver context
     TangCtx &tc = c.tc;

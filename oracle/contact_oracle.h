@@ -17,8 +17,9 @@
  * strip, SteadyGS 41x41, two coupled materials, shifts with prescribed forces),
  * and the Newton-Raphson iterations on prescribed total forces of case 2 of
  * examples/cattaneo.ref_out (F=2) and case 1 of examples/catt_to_cart.ref_out
- * (F=1), and the element tables of examples/carter2d.ref_out (55x1 strip,
- * SteadyGS); see tests/test_oracle.py.  Its subsurface stresses (orc_subsurf.hpp)
+ * (F=1), the element tables of examples/carter2d.ref_out (55x1 strip,
+ * SteadyGS) and the five printed cases of examples/bentall.ref_out (two coupled
+ * materials, chi = 180 deg, a warm-started sequence); see tests/test_oracle.py.  Its subsurface stresses (orc_subsurf.hpp)
  * reproduce examples/subsurf.ref_subs and the maxima of subsurf.ref_out
  * (tests/test_subsurf_cpu.py).  GDsteady (G=5) and transient rolling (T=2) have no
  * golden output in the reference: those paths are restated line by line and
@@ -70,6 +71,12 @@ typedef struct {
      * 3 also d (Fx,Fy,Mz)/d (cksi,ceta,cphi); solver limits of those solves (G=6 flags) */
     int    sens, mxsens;
     double epsens;
+    /* 1: the stand-alone program's input rules (m_sinput.f90:1000-1030): MAXOUT as given for
+     * dissimilar materials, where the library raises it to 10 (contact_addon.f90:1461-1462) */
+    int    standalone;
+    /* sensitivities of the previous case (16 values as orc_result.sens, may be NULL); kept
+     * where the initial estimate keeps them (iestim 1, 3), as the creepages are */
+    const double *sens_init;
 } orc_problem;
 
 /* Outputs of one case.  Array pointers are caller-allocated with mx*my

@@ -48,6 +48,8 @@ class Problem(ctypes.Structure):
         ("px_init", ctypes.POINTER(ctypes.c_double)),
         ("py_init", ctypes.POINTER(ctypes.c_double)),
         ("sens", ctypes.c_int), ("mxsens", ctypes.c_int), ("epsens", ctypes.c_double),
+        ("standalone", ctypes.c_int),
+        ("sens_init", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -147,9 +149,14 @@ def default_problem():
 def solve(pb, h=None, warm=None, fields=True, fast=False):
     """Solve one case; returns a dict of scalars and (optionally) fields.
 
-    h: element-wise undeformed distance (ibase 9); warm: dict(igs, pn, px, py)
-    used as initial estimate when pb.iestim > 0; fast: the baseline build (Stockham FFT, real-input convolutions)."""
+    h: element-wise undeformed distance (ibase 9); warm: dict(igs, pn, px, py[, sens])
+    used as initial estimate when pb.iestim > 0; fast: the baseline build (Stockham FFT,
+    real-input convolutions)."""
     keep = []
+    if warm is not None and "sens" in warm:
+        sv = np.ascontiguousarray(np.asarray(warm["sens"], dtype=np.float64).T.ravel())
+        keep.append(sv)
+        pb.sens_init = _dptr(sv)
     if h is not None:
         hh = np.ascontiguousarray(h, dtype=np.float64).ravel()
         keep.append(hh)

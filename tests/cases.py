@@ -277,6 +277,9 @@ def to_oracle(case):
         pb.omegah, pb.omegas = case["omegah"], case["omegas"]
     pb.fxrel, pb.fyrel = case.get("fxrel", 0.0), case.get("fyrel", 0.0)
     pb.sens = case.get("sens", 1)
+    pb.standalone = int(case.get("standalone", False))
+    if "iestim" in case:
+        pb.iestim = case["iestim"]
     if pb.norm == 1:
         pb.fn = case["fn"]
     else:
@@ -296,6 +299,32 @@ def to_oracle(case):
         pb.prmudf = arr.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
         pb._keep = arr                       # alive until the solve returns
     return pb, case.get("h")
+
+
+def replay_oracle(case_list, fast=False):
+    """Solve the cases of an input file (contact_gb300.inp.read_inp) in order through the
+    oracle, carrying the state from case to case as the stand-alone program does: a case with
+    an initial estimate (IESTIM 1) starts from the previous solution and its sensitivities;
+    creepages that a case does not prescribe (total forces given) keep their previous value.
+    Transient sequences (P = 0, 1) are not replayed."""
+    import pyoracle as po
+    out, prev = [], None
+    for case in case_list:
+        c = dict(case)
+        if c.get("pvtime", 2) != 2:
+            raise ValueError("transient sequences are not replayed")
+        if prev is not None:
+            if c.get("force3", 0) >= 1:
+                c.setdefault("cksi", prev["cksi"])
+            if c.get("force3", 0) >= 2:
+                c.setdefault("ceta", prev["ceta"])
+        pb, h = to_oracle(c)
+        warm = None
+        if c.get("iestim", 0) >= 1 and prev is not None:
+            warm = dict(igs=prev["igs"], pn=prev["pn"], px=prev["px"], py=prev["py"], sens=prev["sens"])
+        prev = po.solve(pb, h=h, warm=warm, fast=fast)
+        out.append(prev)
+    return out
 
 
 def oracle_solve(case, fast=False):

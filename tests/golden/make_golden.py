@@ -38,6 +38,11 @@ fixtures next to this script:
   depths below one point and below a 7x7 subgrid of a 21x21 block, as printed, and the
   printed maxima of both cases (pressure alone and with traction).
 
+* examples/bentall.inp + bentall.ref_out -> bentall.json
+  steady rolling of two different materials (coupled normal and tangential problems,
+  several outer iterations) on a 216x1 strip at chi = 180 deg with Fx prescribed: the
+  reader's six cases, to be replayed in order, and the printed results of cases 2-6.
+
 * testbank/test_caddon.ref_out -> test_caddon_re1.json
   output of src/test_caddon.f90 for result element 1 (module 3 through the library
   interface in SPCK units: Hertzian 21x33 grid, penetration prescribed, creepage 0.001,
@@ -145,6 +150,8 @@ def _results_block(body):
         if s.strip().startswith("NPOT") and "NCON" in s:
             v = ln[i + 1].split()
             rec.update(npot=int(v[0]), ncon=int(v[1]), nadh=int(v[2]), nslip=int(v[3]))
+            if len(v) >= 6 and "INORM" in s:
+                rec.update(inorm=int(v[4]), itang=int(v[5]))
         if "FORM OF THE CONTACT" in s:
             rows = []
             j = i + 1
@@ -383,6 +390,36 @@ def parse_subsurf(root):
             "solves": solves}
 
 
+def parse_bentall(root):
+    """examples/bentall.inp: steady rolling of two different materials on a 216x1 strip at chi =
+    180 deg, Fx prescribed, the normal and tangential problems coupled: the reader's six cases
+    (replayed in order, case 2 starting from case 1's solution) and the printed results of
+    cases 2-6 (case 1 prints none): every Newton-Raphson row over all outer iterations, the
+    last solve's counts and iterations, the number of outer iterations, forces, energy,
+    approach, pmax, creepage, sensitivities and the picture."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from contact_gb300 import inp
+    cases = inp.read_inp(open(os.path.join(root, "examples", "bentall.inp")).read())
+    text = open(os.path.join(root, "examples", "bentall.ref_out")).read()
+    blocks = re.split(r"\n Case\s+(\d+)\n", text)
+    out = []
+    for k in range(1, len(blocks), 2):
+        body = blocks[k + 1]
+        if "TOTAL FORCES" not in body:
+            continue
+        rec = {"case": int(blocks[k])}
+        ms = re.findall(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+        rec["norm_itcg"] = int(ms[-1][2])
+        _tang_final(rec, body)
+        rec["nr"] = _nr_history(body)
+        rec["sens"] = _sensitivities(body)
+        m = re.search(r"FN/G\s+CREEP X.*\n\s*(\S+)\s+(\S+)", body)
+        rec["cksi"] = float(m.group(2))
+        rec.update(_results_block(body))
+        out.append(rec)
+    return {"source": "examples/bentall.inp, examples/bentall.ref_out", "inputs": cases, "cases": out}
+
+
 def parse_test_caddon(path):
     text = open(path).read()
     block = text.split("...start processing of Result Element")[1]     # element 1, first solve
@@ -430,6 +467,9 @@ def main():
     ss = parse_subsurf(root)
     with open(os.path.join(HERE, "subsurf.json"), "w") as f:
         json.dump(ss, f, separators=(",", ":"))
+    bt = parse_bentall(root)
+    with open(os.path.join(HERE, "bentall.json"), "w") as f:
+        json.dump(bt, f, indent=0)
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)

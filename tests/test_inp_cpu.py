@@ -67,7 +67,10 @@ def test_cattaneo_and_testbank():
     tb = _read("testbank/testbank.inp")
     _same_case(tb[0], C.testbank_case(1))
     assert "C=3" in tb[1]["unsupported"]                 # bilinear loading
-    assert "different materials" in _read("examples/bentall.inp")[0]["unsupported"]
+    b = _read("examples/bentall.inp")
+    assert len(b) == 6 and all("unsupported" not in c for c in b)          # two materials: poiss2, gg2
+    assert (b[0]["poiss"], b[0]["poiss2"], b[0]["gg"], b[0]["gg2"]) == (0.31, 0.28, 23000.0, 82000.0)
+    assert b[0]["chi"] == pytest.approx(math.pi) and b[1]["iestim"] == 1 and b[1]["force3"] == 1
 
 
 def test_perfc_fixture_matches_the_inputs():
