@@ -656,6 +656,7 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     Case c;
     c.pb = pb;
     r->ierror = 0;
+    r->nout = 0;
     // combin_mater, m_hierarch_data.f90:1543-1553
     double gg1 = pb->gg1, gg2 = pb->gg2, p1 = pb->poiss1, p2 = pb->poiss2;
     c.ga = 2.0 / (1.0 / gg1 + 1.0 / gg2);
@@ -822,6 +823,8 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
             gf_axpy(AllElm, -1.0, c.ps, po1, ikALL, c.igs);
             dif = gf_rms(AllInt, po1, ikALL, c.igs);
             difid = 5.0 * pb->eps * gf_rms(AllInt, c.ps, ikALL, c.igs);
+            if (r->nout < 64) { r->outer[2 * r->nout] = dif; r->outer[2 * r->nout + 1] = difid; }
+            r->nout++;
             gf_copy(AllElm, c.ps, po1, ikALL, c.igs);
         }
     }

@@ -13,8 +13,9 @@
  * examples/cattaneo.ref_out (NormCG, TangCG on the shift problem), result
  * element 1 of testbank/test_caddon.ref_out and testbank/contact_nonhz.ref_out
  * (approach prescribed, spin) and
- * cases 1, 6, 7, 9, 10 and 13 of testbank/testbank.ref_out (TangCG shift, ConvexGS
- * strip, SteadyGS 41x41, two coupled materials, shifts with prescribed forces),
+ * cases 1, 6, 7, 9, 10, 13, 17 and 25 of testbank/testbank.ref_out (TangCG shift,
+ * ConvexGS strip, SteadyGS 41x41, coupled materials, prescribed forces, transient
+ * rolling from rest),
  * and the Newton-Raphson iterations on prescribed total forces of case 2 of
  * examples/cattaneo.ref_out (F=2) and case 1 of examples/catt_to_cart.ref_out
  * (F=1), the element tables of examples/carter2d.ref_out (55x1 strip,
@@ -103,6 +104,10 @@ typedef struct {
      * caller-allocated with room for nr_cap iterations (may be NULL), nnr = iterations made */
     int     nr_cap, nnr;
     double *nr_hist;
+    /* outer iterations of the coupled normal and tangential problems (panprc): per iteration
+     * the change of the tractions and its tolerance 5 eps |p| (the first 64) */
+    int     nout;
+    double  outer[128];
 } orc_result;
 
 void orc_default_problem(orc_problem *pb);

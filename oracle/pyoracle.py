@@ -77,6 +77,7 @@ class Result(ctypes.Structure):
         ("igs", ctypes.POINTER(ctypes.c_int)),
         ("sens", ctypes.c_double * 16),
         ("nr_cap", ctypes.c_int), ("nnr", ctypes.c_int), ("nr_hist", ctypes.POINTER(ctypes.c_double)),
+        ("nout", ctypes.c_int), ("outer", ctypes.c_double * 128),
     ]
 
 
@@ -187,7 +188,8 @@ def solve(pb, h=None, warm=None, fields=True, fast=False):
     res.nr_hist = _dptr(hist)
     lib(fast).orc_calculate(ctypes.byref(pb), ctypes.byref(res))
     out = {k: getattr(res, k) for k, _ in Result._fields_ if k not in
-           ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h", "igs", "sens", "nr_cap", "nr_hist")}
+           ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h", "igs", "sens", "nr_cap", "nr_hist", "outer")}
+    out["outer"] = np.array(res.outer[:2 * min(res.nout, 64)], dtype=np.float64).reshape(-1, 2)
     # sens[iout][iin]: iout Fn, Fx, Fy, Mz; iin pen, cksi, ceta, cphi
     out["sens"] = np.array(res.sens[:], dtype=np.float64).reshape(4, 4).T.copy()
     out["nr"] = hist[:7 * min(res.nnr, NR_CAP)].reshape(-1, 7).copy()

@@ -155,6 +155,11 @@ def testbank_case(icase):
     9: steady rolling with different materials (nu 0.1 and 0.28, G 1 and 81000: K = 0.4, the
     normal and tangential problems coupled and solved alternately, maxout 10), Fn 2.468, Fx =
     -0.4718 mu Fn prescribed, spin 1e-4, mu 0.6, 25x25 grid, SteadyGS.
+    17: transient rolling from rest (T=2, dq 0.4 mm) of case 7's geometry, Fx = 0.657 mu Fn
+    prescribed, TangCG, maxin 30, maxnr 5.
+    25: a shift (T=1) of two very different bodies (nu 0.5, G 2e7 against nu 0, G 200) pressed
+    by Fn 400 kN on a flat 251x1 strip from x = -20 mm, dx 0.16 mm, mu 0.4, eps 1e-8, up to
+    30 outer iterations of the coupled problems.
     10: case 1 with Fn 1722 N, Fx = -0.875 mu Fn and Fy = 0 prescribed (F=2), the grid given by
     its corners.  13: a Cattaneo shift on a 41x41 Hertzian grid (semi-axes 4.1 mm, scale
     1.17143) with the normal problem skipped for the elliptical traction bound (B=2), Fn
@@ -169,6 +174,16 @@ def testbank_case(icase):
                     poiss=0.1, poiss2=0.28, gg=1.0, gg2=0.81e5, fstat=0.6, veloc=1000.0, fn=2.468, ceta=0.0,
                     cphi=1e-4, force3=1, fxrel=-0.4718, dq=1.1, ipotcn=1,
                     potprm=[25, 25, -13.75, -13.75, 1.1, 1.1], prmudf=[0.3332e-3, 0.0, 0.3332e-3, 0.0, 0.0, 0.0])
+    if icase == 17:
+        return dict(tang=2, norm=1, bound=0, gausei=0, maxgs=80, maxin=30, maxnr=5, maxout=1, eps=1e-6, poiss=0.28,
+                    gg=1.0, fstat=0.4013, veloc=1000.0, fn=0.4705, ceta=0.0, cphi=0.0, force3=1, fxrel=0.657, dq=0.4,
+                    ipotcn=1, potprm=[41, 41, -4.1, -4.1, 0.2, 0.2], prmudf=[0.002963, 0.0, 0.002963, 0.0, 0.0, 0.0],
+                    standalone=True)
+    if icase == 25:
+        return dict(tang=1, norm=1, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=30, eps=1e-8,
+                    poiss=0.5, poiss2=0.0, gg=2e7, gg2=200.0, fstat=0.4, veloc=1.0, fn=400000.0, cksi=0.0, ceta=0.0,
+                    cphi=0.0, ipotcn=3, potprm=[251, 1, -20.0, 0.0, 0.16, 1000.0],
+                    prmudf=[0.0, 0.0, 0.0, 0.0, 0.0, 0.0], standalone=True)
     if icase == 10:
         return dict(tang=1, norm=1, bound=0, gausei=0, maxgs=100, maxin=100, maxnr=30, maxout=1, eps=1e-8,
                     poiss=0.28, gg=82000.0, fstat=0.3, veloc=1.0, fn=1722.0, cphi=0.0, force3=2, fxrel=-0.875,

@@ -62,7 +62,9 @@ fixtures next to this script:
   rolling of two different materials (coupled normal and tangential problems), case 7 steady rolling on a 41x41 quadratic geometry (SteadyGS, eps 1e-6), case 10
   the same shift with Fn, Fx and Fy prescribed (F=2, Newton-Raphson on both shifts), case 13
   a shift on a 41x41 Hertzian grid with the normal problem skipped (B=2) and Fx prescribed
-  (F=1).  The other cases use features outside this library (ConvexGS, bilinear loading,
+  (F=1), case 17 transient rolling from rest with Fx prescribed (T=2, TangCG), case 25 a shift
+  of two very different materials (G 2e7 and 200) on a 251x1 strip with up to 30 outer
+  iterations.  The other cases use features outside this library (ConvexGS, bilinear loading,
   falling or variable friction, other materials, transient sequences, Fastsim).
 
 * perfc_test/*.inp + perfc_test/get_times.ref_out -> perfc_cases.json
@@ -281,7 +283,7 @@ def parse_carter2d(path):
     return {"source": "examples/carter2d.ref_out", "cases": [rec]}
 
 
-def parse_testbank(path, wanted=(1, 6, 7, 9, 10, 13)):
+def parse_testbank(path, wanted=(1, 6, 7, 9, 10, 13, 17, 25)):
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
     out = []
@@ -298,6 +300,9 @@ def parse_testbank(path, wanted=(1, 6, 7, 9, 10, 13)):
         if nr:
             rec["nr"] = nr
             rec["sens"] = _sensitivities(body)
+        outer = re.findall(r"\d+, Panag/Out: \|Pk - Pk-1\|,  5 Eps \|Pk\| :\s*(\S+)\s+(\S+)", body)
+        if outer:
+            rec["outer"] = [[float(a), float(b)] for a, b in outer]
         rec.update(_results_block(body))
         out.append(rec)
     return {"source": "testbank/testbank.ref_out", "cases": out}
