@@ -188,8 +188,8 @@ def read_inp(text):
             bad.append("heat, extra rigid slip or subsurface inputs")
         if len(vl) >= 2 and vl[1] % 10 >= 2:
             bad.append("damping inputs")
-        if pb["T"] in (1, 2) and pb["P"] != 2:
-            bad.append("transient sequence (P=%d with T=%d)" % (pb["P"], pb["T"]))
+        if pb["P"] == 3:
+            bad.append("previous time instance kept as is (P=3)")
         if bad:
             cases.append({"unsupported": "; ".join(bad)})
             break

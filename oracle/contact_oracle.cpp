@@ -32,8 +32,8 @@ struct Case {
     TangCtx tc;
     int maxout;
     // state
-    Eldiv igs;
-    GF3 ps, hs, us, ss;
+    Eldiv igs, igv;                 // current and previous element division
+    GF3 ps, hs, us, ss, pv;         // pv: tractions of the previous time instance
     std::vector<double> mus;
     Inflcf cs, cv, ms;
     int itnorm = 0, ittang = 0, itcg = 0, itgs = 0, solver_eff = 0;
@@ -163,20 +163,37 @@ void init_curr_data(Case &c, int ihertz) {
     }
 }
 
-// stang_rhs, m_stang.f90:749-951 (steady rolling / first step, pv = 0)
+// stang_rhs, m_stang.f90:749-951: the fixed part of the shift, wsfix = -facdt h + u(ps_n)
+// - u'(pv): for steady rolling u' of the current pressure through cv; for shifts and transient
+// rolling u' of the previous tractions (normal and tangential), and at the leading edge of
+// transient rolling the edge estimate ubnd of the previous tractions
 void stang_rhs(Case &c, const std::vector<int> &iel, const std::vector<double> &facdt, GF3 &wsfix) {
     const int mx = c.mx, my = c.my, n = c.npot;
+    const bool is_ssrol = c.pb->tang == 3;
     areas(c.igs);
-    GF3 usn, uvn; usn.init(n); uvn.init(n);
+    areas(c.igv);
+    GF3 usn, uvn, uvt; usn.init(n); uvn.init(n); uvt.init(n);
     GF3 wsrig; wsrig.init(n);
     for (int ik = 1; ik <= 2; ik++)
         for (int ii : iel) wsrig.c[ik - 1][ii] = -facdt[ii] * c.hs.c[ik - 1][ii];
     vecaijpj(c.igs, AllInt, usn, ikTANG, c.ps, c.igs, ikZ, c.cs, mx, my);
-    if (c.pb->tang == 3) vecaijpj(c.igs, AllInt, uvn, ikTANG, c.ps, c.igs, ikZ, c.cv, mx, my);
-    // T=1,2 with a fresh sequence: previous tractions pv are zero, so uvn = uvt = ubnd = 0
+    if (!is_ssrol) {
+        vecaijpj(c.igs, AllInt, uvn, ikTANG, c.pv, c.igv, ikZ, c.cv, mx, my);
+        vecaijpj(c.igs, AllInt, uvt, ikTANG, c.pv, c.igv, ikTANG, c.cv, mx, my);
+    } else {
+        vecaijpj(c.igs, AllInt, uvn, ikTANG, c.ps, c.igs, ikZ, c.cv, mx, my);
+    }
+    std::vector<double> ubnd;
+    subnd(c.tc, c.ledg, c.pv, c.igv, c.cs, ubnd);
     for (int ik = 1; ik <= 2; ik++)
-        for (int ii : iel)
-            wsfix.c[ik - 1][ii] = wsrig.c[ik - 1][ii] + usn.c[ik - 1][ii] - uvn.c[ik - 1][ii];
+        for (int ii : iel) {
+            const int j = c.ii2j[ii];
+            double w;
+            if (is_ssrol) w = wsrig.c[ik - 1][ii] + usn.c[ik - 1][ii] - uvn.c[ik - 1][ii];
+            else if (j <= 0) w = wsrig.c[ik - 1][ii] + usn.c[ik - 1][ii] - uvn.c[ik - 1][ii] - uvt.c[ik - 1][ii];
+            else w = wsrig.c[ik - 1][ii] + usn.c[ik - 1][ii] - ubnd[(size_t)2 * j + ik - 1];
+            wsfix.c[ik - 1][ii] = w;
+        }
 }
 
 // tang_solver, m_solvpt.f90:382-493; is_sens: the sensitivity solve (mxsens, epsens)
@@ -767,6 +784,23 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     if (pb->sens_init)
         for (int io = 0; io < 4; io++)
             for (int ji = 0; ji < 4; ji++) c.sens[io][ji] = pb->sens_init[io + 4 * ji];
+    // set_prev_data, m_sdis.f90:208-312: the previous time instance (P=0 all of it, P=1 the
+    // normal part, P=2 none)
+    c.pv.init(c.npot);
+    c.igv.init(c.mx, c.my);
+    if (pb->pvtime <= 1 && pb->igv_init) {
+        for (int ii = 0; ii < c.npot; ii++) {
+            c.igv.el[ii] = pb->igv_init[ii];
+            c.pv.vn(ii) = pb->pvn_init ? pb->pvn_init[ii] : 0.0;
+            if (pb->pvtime == 0) {
+                c.pv.vx(ii) = pb->pvx_init ? pb->pvx_init[ii] : 0.0;
+                c.pv.vy(ii) = pb->pvy_init ? pb->pvy_init[ii] : 0.0;
+            } else if (c.igv.el[ii] >= Adhes) {
+                c.igv.el[ii] = Adhes;                    // P=1: the normal part of the division
+            }
+        }
+    }
+    areas(c.igv);
     init_curr_data(c, ihertz);
     // solver context
     TangCtx &tc = c.tc;

@@ -19,8 +19,10 @@
  * and the Newton-Raphson iterations on prescribed total forces of case 2 of
  * examples/cattaneo.ref_out (F=2) and case 1 of examples/catt_to_cart.ref_out
  * (F=1), the element tables of examples/carter2d.ref_out (55x1 strip,
- * SteadyGS) and the five printed cases of examples/bentall.ref_out (two coupled
- * materials, chi = 180 deg, a warm-started sequence); see tests/test_oracle.py.  Its subsurface stresses (orc_subsurf.hpp)
+ * SteadyGS), the five printed cases of examples/bentall.ref_out (two coupled
+ * materials, chi = 180 deg, a warm-started sequence) and all 171 cases of
+ * examples/catt_to_cart.ref_out (transient sequences from the previous time
+ * instance); see tests/test_oracle.py.  Its subsurface stresses (orc_subsurf.hpp)
  * reproduce examples/subsurf.ref_subs and the maxima of subsurf.ref_out
  * (tests/test_subsurf_cpu.py).  GDsteady (G=5) and transient rolling (T=2) have no
  * golden output in the reference: those paths are restated line by line and
@@ -78,6 +80,10 @@ typedef struct {
     /* sensitivities of the previous case (16 values as orc_result.sens, may be NULL); kept
      * where the initial estimate keeps them (iestim 1, 3), as the creepages are */
     const double *sens_init;
+    /* tractions and element division of the previous time instance for transient sequences
+     * (pvtime 0: all components, 1: the normal one; may be NULL: zero, as for pvtime 2) */
+    const int    *igv_init;
+    const double *pvn_init, *pvx_init, *pvy_init;
 } orc_problem;
 
 /* Outputs of one case.  Array pointers are caller-allocated with mx*my

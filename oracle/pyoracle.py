@@ -50,6 +50,9 @@ class Problem(ctypes.Structure):
         ("sens", ctypes.c_int), ("mxsens", ctypes.c_int), ("epsens", ctypes.c_double),
         ("standalone", ctypes.c_int),
         ("sens_init", ctypes.POINTER(ctypes.c_double)),
+        ("igv_init", ctypes.POINTER(ctypes.c_int)),
+        ("pvn_init", ctypes.POINTER(ctypes.c_double)), ("pvx_init", ctypes.POINTER(ctypes.c_double)),
+        ("pvy_init", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -147,13 +150,20 @@ def default_problem():
     return pb
 
 
-def solve(pb, h=None, warm=None, fields=True, fast=False):
+def solve(pb, h=None, warm=None, fields=True, fast=False, prev=None):
     """Solve one case; returns a dict of scalars and (optionally) fields.
 
     h: element-wise undeformed distance (ibase 9); warm: dict(igs, pn, px, py[, sens])
-    used as initial estimate when pb.iestim > 0; fast: the baseline build (Stockham FFT,
-    real-input convolutions)."""
+    used as initial estimate when pb.iestim > 0; prev: dict(igs, pn, px, py), the previous
+    time instance of a transient sequence (pb.pvtime 0 or 1); fast: the baseline build
+    (Stockham FFT, real-input convolutions)."""
     keep = []
+    if prev is not None:
+        igv = np.ascontiguousarray(prev["igs"], dtype=np.int32)
+        pvs = [np.ascontiguousarray(prev[k], dtype=np.float64) for k in ("pn", "px", "py")]
+        keep += [igv] + pvs
+        pb.igv_init = igv.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        pb.pvn_init, pb.pvx_init, pb.pvy_init = (_dptr(a) for a in pvs)
     if warm is not None and "sens" in warm:
         sv = np.ascontiguousarray(np.asarray(warm["sens"], dtype=np.float64).T.ravel())
         keep.append(sv)

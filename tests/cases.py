@@ -293,6 +293,7 @@ def to_oracle(case):
     pb.fxrel, pb.fyrel = case.get("fxrel", 0.0), case.get("fyrel", 0.0)
     pb.sens = case.get("sens", 1)
     pb.standalone = int(case.get("standalone", False))
+    pb.pvtime = case.get("pvtime", 2)
     if "iestim" in case:
         pb.iestim = case["iestim"]
     if pb.norm == 1:
@@ -316,28 +317,71 @@ def to_oracle(case):
     return pb, case.get("h")
 
 
+def _grid_of(case, prev):
+    """(mx, my, dx, dy, xc1, yc1) of an explicit potential contact (IPOTCN 1..4, potcon_fill),
+    or the previous solution's grid for a Hertzian one."""
+    ip, pr = case.get("ipotcn", -3), case["potprm"]
+    mx, my = int(pr[0]), int(pr[1])
+    if ip == 1:
+        return mx, my, pr[4], pr[5], pr[2] + 0.5 * pr[4], pr[3] + 0.5 * pr[5]
+    if ip == 2:
+        dx, dy = (pr[4] - pr[2]) / mx, (pr[5] - pr[3]) / my
+        return mx, my, dx, dy, pr[2] + 0.5 * dx, pr[3] + 0.5 * dy
+    if ip == 3:
+        return mx, my, pr[4], pr[5], pr[2], pr[3]
+    if ip == 4:
+        return mx, my, (pr[4] - pr[2]) / max(1, mx - 1), (pr[5] - pr[3]) / max(1, my - 1), pr[2], pr[3]
+    return prev["mx"], prev["my"], prev["dx"], prev["dy"], prev["xc1"], prev["yc1"]
+
+
+def _on_grid(prev, grid):
+    """The previous solution's element division and tractions carried to a grid of the same
+    spacing shifted by whole elements (eldiv_resize, gf3_resize: m_gridfunc_sub.f90:21-159):
+    exterior and zero where the old grid does not reach."""
+    mx, my, dx, dy, xc1, yc1 = grid
+    kx = int(round((xc1 - prev["xc1"]) / dx))
+    ky = int(round((yc1 - prev["yc1"]) / dy))
+    out = {"igs": np.zeros(mx * my, dtype=np.int32)}
+    for k in ("pn", "px", "py"):
+        out[k] = np.zeros(mx * my)
+    for iy in range(my):
+        jy = iy + ky
+        if not 0 <= jy < prev["my"]:
+            continue
+        for ix in range(mx):
+            jx = ix + kx
+            if 0 <= jx < prev["mx"]:
+                out["igs"][ix + iy * mx] = prev["igs"][jx + jy * prev["mx"]]
+                for k in ("pn", "px", "py"):
+                    out[k][ix + iy * mx] = prev[k][jx + jy * prev["mx"]]
+    return out
+
+
 def replay_oracle(case_list, fast=False):
     """Solve the cases of an input file (contact_gb300.inp.read_inp) in order through the
     oracle, carrying the state from case to case as the stand-alone program does: a case with
     an initial estimate (IESTIM 1) starts from the previous solution and its sensitivities;
     creepages that a case does not prescribe (total forces given) keep their previous value.
-    Transient sequences (P = 0, 1) are not replayed."""
+    In a transient sequence (P = 0, 1) the previous solution is the previous time instance.
+    Where the potential contact moves by whole elements, the previous solution moves with it."""
     import pyoracle as po
     out, prev = [], None
     for case in case_list:
         c = dict(case)
-        if c.get("pvtime", 2) != 2:
-            raise ValueError("transient sequences are not replayed")
         if prev is not None:
             if c.get("force3", 0) >= 1:
                 c.setdefault("cksi", prev["cksi"])
             if c.get("force3", 0) >= 2:
                 c.setdefault("ceta", prev["ceta"])
         pb, h = to_oracle(c)
-        warm = None
-        if c.get("iestim", 0) >= 1 and prev is not None:
-            warm = dict(igs=prev["igs"], pn=prev["pn"], px=prev["px"], py=prev["py"], sens=prev["sens"])
-        prev = po.solve(pb, h=h, warm=warm, fast=fast)
+        warm = pv = None
+        if prev is not None and (c.get("iestim", 0) >= 1 or c.get("pvtime", 2) <= 1):
+            moved = _on_grid(prev, _grid_of(c, prev))
+            if c.get("iestim", 0) >= 1:
+                warm = dict(moved, sens=prev["sens"])
+            if c.get("pvtime", 2) <= 1:
+                pv = moved
+        prev = po.solve(pb, h=h, warm=warm, fast=fast, prev=pv)
         out.append(prev)
     return out
 

@@ -19,6 +19,10 @@ fixtures next to this script:
   (F=2) and meets by Newton-Raphson on the shifts; kept: the iterations of that process
   (shifts, relative forces, TangCG iterations), the sensitivities it leaves, forces,
   approach, pmax, element counts and the element-division picture.
+* examples/catt_to_cart.inp + catt_to_cart.ref_out -> catt_to_cart_sequence.json
+  all 171 cases: three transient sequences (rolling on a fixed grid, shifts on a fixed and
+  on a moving grid) continuing from case to case with Fx prescribed: the reader's cases and
+  the printed Newton-Raphson rows and counts.
 * examples/catt_to_cart.ref_out -> catt_to_cart_case1.json
   case 1 of examples/catt_to_cart.inp, the Cattaneo shift problem on a 34x33 grid with Fx
   prescribed (F=1, TangCG, eps 1e-7): the Newton-Raphson iterations, the sensitivity
@@ -227,7 +231,7 @@ def parse_cattaneo(path):
     return {"source": "examples/cattaneo.ref_out", "cases": out}
 
 
-def parse_catt_to_cart(path):
+def parse_catt_to_cart_case1(path):
     """Case 1 of examples/catt_to_cart.inp: the Cattaneo shift with Fx prescribed (F=1)."""
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
@@ -425,6 +429,33 @@ def parse_bentall(root):
     return {"source": "examples/bentall.inp, examples/bentall.ref_out", "inputs": cases, "cases": out}
 
 
+def parse_catt_to_cart(root):
+    """examples/catt_to_cart.inp, all 171 cases: three sequences from a Cattaneo shift into
+    rolling (transient rolling, T=2, on a fixed 34x33 grid; shifts on a world-fixed 90x33 grid;
+    shifts on a 34x33 grid that moves one element per step), each case continuing from the
+    previous time instance (P=0) with Fx prescribed: the reader's cases, to be replayed in
+    order, and per case the printed Newton-Raphson rows, and the counts where printed."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from contact_gb300 import inp
+    cases = inp.read_inp(open(os.path.join(root, "examples", "catt_to_cart.inp")).read())
+    for c in cases:
+        for k, v in list(c.items()):
+            if hasattr(v, "tolist"):
+                c[k] = v.tolist()
+    text = open(os.path.join(root, "examples", "catt_to_cart.ref_out")).read()
+    blocks = re.split(r"\n Case\s+(\d+)\n", text)
+    out = []
+    for k in range(1, len(blocks), 2):
+        body = blocks[k + 1]
+        rec = {"case": int(blocks[k]), "nr": _nr_history(body)}
+        res = _results_block(body)
+        for key in ("ncon", "nadh", "nslip", "fn", "fx", "approach", "pmax"):
+            if key in res:
+                rec[key] = res[key]
+        out.append(rec)
+    return {"source": "examples/catt_to_cart.inp, examples/catt_to_cart.ref_out", "inputs": cases, "cases": out}
+
+
 def parse_test_caddon(path):
     text = open(path).read()
     block = text.split("...start processing of Result Element")[1]     # element 1, first solve
@@ -460,7 +491,10 @@ def main():
     ca = parse_cattaneo(os.path.join(root, "examples", "cattaneo.ref_out"))
     with open(os.path.join(HERE, "cattaneo.json"), "w") as f:
         json.dump(ca, f, indent=0)
-    cc = parse_catt_to_cart(os.path.join(root, "examples", "catt_to_cart.ref_out"))
+    cs = parse_catt_to_cart(root)
+    with open(os.path.join(HERE, "catt_to_cart_sequence.json"), "w") as f:
+        json.dump(cs, f, separators=(",", ":"))
+    cc = parse_catt_to_cart_case1(os.path.join(root, "examples", "catt_to_cart.ref_out"))
     with open(os.path.join(HERE, "catt_to_cart_case1.json"), "w") as f:
         json.dump(cc, f, indent=0)
     c2 = parse_carter2d(os.path.join(root, "examples", "carter2d.ref_out"))

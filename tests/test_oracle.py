@@ -386,6 +386,31 @@ def test_two_body_shift_outer_iterations(oracle):
     assert abs(o["fx"]) < 5e-4 and abs(o["pen"] - g["approach"]) <= 0.5e-5
 
 
+def test_catt_to_cart_sequences(oracle):
+    """examples/catt_to_cart.inp replayed in order, all 171 cases: from a Cattaneo shift into
+    transient rolling (T=2) on a fixed grid, then shifts (T=1, approach prescribed) on a
+    world-fixed grid and on a grid that moves one element per step, each case continuing
+    from the previous time instance (P=0) with Fx prescribed.  Every printed Newton-Raphson
+    row (creepage and relative force to 4 digits, TangCG iterations exact) and the counts,
+    forces and approach where printed."""
+    g = _load("catt_to_cart_sequence.json")
+    res = C.replay_oracle(g["inputs"])
+    assert len(res) == len(g["cases"]) == 171
+    rows = 0
+    for gc, o in zip(g["cases"], res):
+        assert o["ierror"] >= 0, gc["case"]
+        assert len(o["nr"]) == len(gc["nr"]), gc["case"]
+        for row, gr in zip(o["nr"], gc["nr"]):
+            assert int(row[1]) == gr[0] and int(row[6]) == gr[5], (gc["case"], row, gr)
+            assert _printed4(row[2], gr[1]) and _printed4(row[3], gr[2]), (gc["case"], row, gr)
+            rows += 1
+        if "ncon" in gc:
+            assert (o["ncon"], o["nadh"], o["nslip"]) == (gc["ncon"], gc["nadh"], gc["nslip"]), gc["case"]
+            for key, gk in (("fn", "fn"), ("fx", "fx"), ("pen", "approach"), ("pmax", "pmax")):
+                assert _printed4(o[key], gc[gk]), (gc["case"], key, o[key], gc[gk])
+    assert rows == 430
+
+
 def test_bentall_sequence(oracle):
     """examples/bentall.inp replayed in order (two different materials, chi = 180 deg, Fx
     prescribed, the normal and tangential problems coupled; case 2 starts from case 1's
