@@ -16,7 +16,8 @@ Supported: control digits of module 3, creepages or total forces prescribed (F=0
 with Coulomb friction (L=0, V=0), elastic materials (two different bodies: keys poiss2, gg2)
 (M=0), no thin-sheet, heat, extra-rigid-slip or subsurface inputs; potential contact
 IPOTCN -3..-1 and 1..4; geometry IBASE 1 (quadratic), 2 (circular in x, tabulated in y),
-3 (sines in x) and 9 (element-wise), planform IPLAN 1.  IBASE 2 and 3 are evaluated here
+3 (sines in x) and 9 (element-wise), planform IPLAN 1; subsurface points (S digit, key
+'subs'), previous time instances (P digit, key 'pvtime').  IBASE 2 and 3 are evaluated here
 (set_norm_rhs, src/m_sdis.f90:321-494) and handed on element-wise.  A case that uses
 anything else is returned with an 'unsupported' entry and ends the reading.
 """
@@ -184,8 +185,8 @@ def read_inp(text):
             bad.append("friction law V=%d L=%d" % (vd["V"], vd["L"]))
         if vd["M"] != 0 or pb["B"] == 1:
             bad.append("material M=%d B=%d" % (vd["M"], pb["B"]))
-        if xh["H"] != 0 or vd["E"] != 0 or pb["S"] >= 2:
-            bad.append("heat, extra rigid slip or subsurface inputs")
+        if xh["H"] != 0 or vd["E"] != 0:
+            bad.append("heat or extra rigid slip inputs")
         if len(vl) >= 2 and vl[1] % 10 >= 2:
             bad.append("damping inputs")
         if pb["P"] == 3:
@@ -268,6 +269,10 @@ def read_inp(text):
                  maxout=st["maxout"], eps=st["eps"], poiss=st["poiss"][0], gg=st["gg"][0], fstat=st["fstat"],
                  standalone=True,
                  veloc=st["veloc"], ipotcn=pot["ipotcn"], potprm=[pot["mx"], pot["my"]] + list(pot["prm"]))
+        if pb["S"] >= 2:
+            st["subs"] = _read_subsurface(L, pb["S"], st.get("subs"))
+        if pb["S"] >= 1 and st.get("subs"):
+            c["subs"] = st["subs"]
         if st["poiss"][0] != st["poiss"][1] or st["gg"][0] != st["gg"][1]:
             c["poiss2"], c["gg2"] = st["poiss"][1], st["gg"][1]
         if st["gd"] is not None:
@@ -281,6 +286,48 @@ def read_inp(text):
             c[key] = np.asarray(val, dtype=np.float64) if key == "h" else list(val)
         cases.append(materialize(c))
     return cases
+
+
+def _read_subsurface(L, sdigit, prev):
+    """Subsurface points of a case (subsurf_input, src/m_subsurf.f90:65-298): the A, O digits
+    for the results and, for S=3, blocks until ISUBS = 0.  Each block a dict: isubs and
+    either the element selection ('ix', 'iy': 1-based column and row numbers, isubs 1-3 and
+    5-7; None for all) with depths 'z', or coordinate lists 'x', 'y', 'z' (isubs 9).  S=2 keeps
+    the previous blocks."""
+    L.read("ii")
+    if sdigit < 3:
+        return prev
+    blocks = []
+    isubs = L.read("i")[0]
+    while isubs >= 1:
+        b = {"isubs": isubs}
+        if isubs in (1, 5):
+            b["ix"] = b["iy"] = None
+        elif isubs in (2, 6):
+            xl, xinc, xh = L.read("iii")
+            yl, yinc, yh = L.read("iii")
+            b["ix"] = list(range(xl, xh + 1, max(1, xinc)))
+            b["iy"] = list(range(yl, yh + 1, max(1, yinc)))
+        elif isubs in (3, 7):
+            nx, ny = L.read("ii")
+            b["ix"] = sorted(set(int(v) for v in L.read_array(nx)))
+            b["iy"] = sorted(set(int(v) for v in L.read_array(ny)))
+        if isubs in (1, 2, 3):
+            nz, zl, dz = L.read("idd")
+            b["z"] = [zl + k * dz for k in range(max(1, nz))]
+        elif isubs in (5, 6, 7):
+            nz = L.read("i")[0]
+            b["z"] = sorted(L.read_array(max(1, nz)))
+        elif isubs == 9:
+            nx, ny, nz = L.read("iii")
+            b["x"] = sorted(L.read_array(max(1, nx)))
+            b["y"] = sorted(L.read_array(max(1, ny)))
+            b["z"] = sorted(L.read_array(max(1, nz)))
+        else:
+            raise ValueError("subsurface input option ISUBS=%d" % isubs)
+        blocks.append(b)
+        isubs = L.read("i")[0]
+    return blocks
 
 
 def materialize(case):

@@ -22,7 +22,8 @@
  * SteadyGS), the five printed cases of examples/bentall.ref_out (two coupled
  * materials, chi = 180 deg, a warm-started sequence) and all 171 cases of
  * examples/catt_to_cart.ref_out (transient sequences from the previous time
- * instance); see tests/test_oracle.py.  Its subsurface stresses (orc_subsurf.hpp)
+ * instance); see tests/test_oracle.py.  With the subsurface stresses it reproduces
+ * all 35 load steps of examples/spence35.ref_out (tests/test_subsurf_cpu.py).  Its subsurface stresses (orc_subsurf.hpp)
  * reproduce examples/subsurf.ref_subs and the maxima of subsurf.ref_out
  * (tests/test_subsurf_cpu.py).  GDsteady (G=5) and transient rolling (T=2) have no
  * golden output in the reference: those paths are restated line by line and

@@ -47,6 +47,11 @@ fixtures next to this script:
   several outer iterations) on a 216x1 strip at chi = 180 deg with Fx prescribed: the
   reader's six cases, to be replayed in order, and the printed results of cases 2-6.
 
+* examples/spence35.inp + spence35.ref_out -> spence35.json
+  Spence's problem in 35 load steps (two materials, coupled problems, each step continuing
+  from the previous one, subsurface stresses along one row): the reader's cases, the printed
+  outer iterations, totals and counts, and the printed subsurface maxima.
+
 * testbank/test_caddon.ref_out -> test_caddon_re1.json
   output of src/test_caddon.f90 for result element 1 (module 3 through the library
   interface in SPCK units: Hertzian 21x33 grid, penetration prescribed, creepage 0.001,
@@ -456,6 +461,40 @@ def parse_catt_to_cart(root):
     return {"source": "examples/catt_to_cart.inp, examples/catt_to_cart.ref_out", "inputs": cases, "cases": out}
 
 
+def parse_spence35(root):
+    """examples/spence35.inp, all 35 cases: Spence's problem, a sphere of one material pressed
+    into and lifted off a half-space of another (the normal and tangential problems coupled)
+    in 35 load steps, each continuing from the previous one (P=0), with subsurface stresses
+    along one grid row: the reader's cases and per case the printed outer iterations, totals
+    and counts where printed, and the printed subsurface maxima of cases 6, 18 and 35."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from contact_gb300 import inp
+    cases = inp.read_inp(open(os.path.join(root, "examples", "spence35.inp")).read())
+    text = open(os.path.join(root, "examples", "spence35.ref_out")).read()
+    blocks = re.split(r"\n Case\s+(\d+)\n", text)
+    out = []
+    for k in range(1, len(blocks), 2):
+        body = blocks[k + 1]
+        rec = {"case": int(blocks[k])}
+        rec["outer"] = [[float(a), float(b)] for a, b in
+                        re.findall(r"Panag/Out: \|Pk - Pk-1\|,  5 Eps \|Pk\| :\s*(\S+)\s+(\S+)", body)]
+        res = _results_block(body)
+        res.pop("picture", None)
+        rec.update(res)
+        subs = []
+        for nb, blk in re.findall(r"SUBSURFACE STRESSES BLOCK\s+(\d):\s*\n(.*?)\n\n", body + "\n\n", re.S):
+            for ln in blk.strip().splitlines():
+                m = re.match(r"\s*(ABSMAX|MAX|MIN)\s+(\w+)\s*=\s*(\S+)\s+AT \(X,Y,Z\) = \(\s*(\S+),\s*(\S+),\s*(\S+)\)",
+                             ln)
+                if m:
+                    subs.append({"block": int(nb), "kind": m.group(1), "quantity": m.group(2),
+                                 "value": float(m.group(3)), "at": [float(m.group(j)) for j in (4, 5, 6)]})
+        if subs:
+            rec["subs"] = subs
+        out.append(rec)
+    return {"source": "examples/spence35.inp, examples/spence35.ref_out", "inputs": cases, "cases": out}
+
+
 def parse_test_caddon(path):
     text = open(path).read()
     block = text.split("...start processing of Result Element")[1]     # element 1, first solve
@@ -509,6 +548,9 @@ def main():
     bt = parse_bentall(root)
     with open(os.path.join(HERE, "bentall.json"), "w") as f:
         json.dump(bt, f, indent=0)
+    sp = parse_spence35(root)
+    with open(os.path.join(HERE, "spence35.json"), "w") as f:
+        json.dump(sp, f, separators=(",", ":"))
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)

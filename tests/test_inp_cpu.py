@@ -67,6 +67,11 @@ def test_cattaneo_and_testbank():
     tb = _read("testbank/testbank.inp")
     _same_case(tb[0], C.testbank_case(1))
     assert "C=3" in tb[1]["unsupported"]                 # bilinear loading
+    sp = _read("examples/spence35.inp")
+    assert len(sp) == 35 and sp[1]["pvtime"] == 0 and sp[0]["subs"][0]["isubs"] == 2
+    assert sp[0]["subs"][0]["iy"] == [23] and len(sp[0]["subs"][0]["ix"]) == 45 and sp[5]["subs"] == sp[0]["subs"]
+    ss = _read("examples/subsurf.inp")
+    assert [b["isubs"] for b in ss[0]["subs"]] == [9, 9] and len(ss[0]["subs"][1]["x"]) == 21
     b = _read("examples/bentall.inp")
     assert len(b) == 6 and all("unsupported" not in c for c in b)          # two materials: poiss2, gg2
     assert (b[0]["poiss"], b[0]["poiss2"], b[0]["gg"], b[0]["gg2"]) == (0.31, 0.28, 23000.0, 82000.0)

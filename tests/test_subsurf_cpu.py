@@ -151,3 +151,50 @@ def test_fft_path_equals_direct_path(oracle):
     scale = np.abs(d).max(axis=(0, 1)) + 1e-300
     err = (np.abs(f - d) / scale).max(axis=(1, 2))
     assert err[0] <= 1e-5 and (err[1:] <= 1e-12).all(), err
+
+
+def test_spence35_sequence(oracle):
+    """examples/spence35.inp replayed in order, all 35 load steps of Spence's problem: a body of
+    one material (G 0.5) pressed into and lifted off one of another (G 1e5), the normal and
+    tangential problems coupled (K != 0), each step continuing from the previous one (P=0).
+    Every printed outer iteration (the change of the tractions and its tolerance, 4 digits)
+    and their number, totals to 4 digits and counts where printed; and the printed maxima of
+    the subsurface stresses along one grid row at z = 1e-6 (the element-centre FFT path) in
+    steps 6, 18 and 35, to 3 decimals and at the printed position."""
+    import pyoracle as po
+
+    def p4(x, gold):
+        if gold == 0.0:
+            return abs(x) < 5e-4
+        return abs(x - gold) <= 0.5 * 10.0 ** (math.floor(math.log10(abs(gold))) - 3) * (1 + 1e-9)
+
+    with open(os.path.join(GOLD, "spence35.json")) as f:
+        g = json.load(f)
+    res = C.replay_oracle(g["inputs"])
+    assert len(res) == len(g["cases"]) == 35
+    nsum = 0
+    for c, gc, o in zip(g["inputs"], g["cases"], res):
+        assert o["ierror"] >= 0
+        assert len(o["outer"]) == len(gc["outer"]), gc["case"]
+        for k, (a, b) in enumerate(gc["outer"]):
+            assert p4(o["outer"][k][0], a) and p4(o["outer"][k][1], b), (gc["case"], k)
+        for key, gk in (("fn", "fn"), ("fx", "fx"), ("fy", "fy"), ("elen", "elen"), ("pen", "approach"),
+                        ("pmax", "pmax")):
+            assert p4(o[key], gc[gk]), (gc["case"], key, o[key], gc[gk])
+        if "ncon" in gc:
+            assert (o["ncon"], o["nadh"], o["nslip"]) == (gc["ncon"], gc["nadh"], gc["nslip"])
+        if "subs" in gc:
+            b = c["subs"][0]
+            grid = (o["mx"], o["my"], o["dx"], o["dy"], o["xc1"], o["yc1"])
+            f = po.subsurf_depths(grid, o["pn"], o["px"], o["py"], (c["gg"], c.get("gg2", c["gg"])),
+                                  (c["poiss"], c.get("poiss2", c["poiss"])), b["z"])
+            sel = [(ix - 1) + (iy - 1) * o["mx"] for iy in b["iy"] for ix in b["ix"]]
+            pts = [(o["xc1"] + (ix - 1) * o["dx"], o["yc1"] + (iy - 1) * o["dy"]) for iy in b["iy"] for ix in b["ix"]]
+            for s in gc["subs"]:
+                col = f[0][sel, ORC[s["quantity"]]]
+                i = int(np.argmax(np.abs(col)) if s["kind"] == "ABSMAX" else np.argmax(col) if s["kind"] == "MAX"
+                        else np.argmin(col))
+                assert abs(col[i] - s["value"]) <= 0.5e-3 * (1 + 1e-9), (gc["case"], s)
+                assert np.allclose(np.round(pts[i], 3), s["at"][:2]), (gc["case"], s, pts[i])
+                nsum += 1
+    assert nsum == 24
