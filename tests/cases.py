@@ -109,6 +109,31 @@ def catt_to_cart_case1():
                 prmudf=[0.002963, 0.0, 0.002963, 0.0, 0.0, 0.0])
 
 
+def testbank_chain(name):
+    """Sequences of testbank/testbank.inp whose later cases continue from the previous time
+    instance (P=0), to be replayed in order (replay_oracle).  'mindlin': case 10 then case 11,
+    a shift with the approach 0.01131 mm prescribed and Fx = -0.875 mu Fn, Fy = 0 from case
+    10's tractions.  'rolling': case 13 (Hertzian shift) then cases 14-16, transient rolling
+    (dq 0.2 mm) with Fx prescribed and the previous solution as initial estimate, the last
+    step with creepage -0.002124, dq 0.8 mm and the grid from curvature 0.2963e-2 and a/b 1.
+    'tilted': case 25 then case 26, the same bodies with the surface tilted by -0.031816."""
+    if name == "mindlin":
+        c10 = testbank_case(10)
+        c11 = dict(c10, pvtime=0, norm=0, pen=0.01131, force3=2, fxrel=-0.875, fyrel=0.0, standalone=True)
+        del c11["fn"]
+        return [dict(c10, standalone=True), c11]
+    if name == "rolling":
+        c13 = dict(testbank_case(13), standalone=True)
+        c14 = dict(c13, pvtime=0, bound=0, tang=2, iestim=1, maxin=100, maxnr=30, dq=0.2, veloc=1000.0)
+        c16 = dict(c14, force3=0, cksi=-0.002124, dq=0.8, ipotcn=-2, potprm=[41, 41, 0.2963e-2, 1.0, 1.17143])
+        return [c13, c14, dict(c14), c16]
+    if name == "tilted":
+        c25 = testbank_case(25)
+        c26 = dict(c25, pvtime=0, prmudf=[0.0, 0.0, 0.0, -0.031816, 0.0, 0.0])
+        return [c25, c26]
+    raise ValueError(name)
+
+
 def subsurf_case(icase):
     """examples/subsurf.inp: one 1x1 mm element (first corner at -0.4999, -0.4998), G 1, nu
     0.28, mu 1, Fn 1, geometry 2.16 (x^2 + y^2), eps 1e-6.  Case 1: the normal problem alone.

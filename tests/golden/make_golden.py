@@ -73,7 +73,9 @@ fixtures next to this script:
   a shift on a 41x41 Hertzian grid with the normal problem skipped (B=2) and Fx prescribed
   (F=1), case 17 transient rolling from rest with Fx prescribed (T=2, TangCG), case 25 a shift
   of two very different materials (G 2e7 and 200) on a 251x1 strip with up to 30 outer
-  iterations.  The other cases use features outside this library (ConvexGS, bilinear loading,
+  iterations, and the cases that continue from the previous time instance: 11 (after 10),
+  14-16 (transient rolling after 13) and 26 (after 25, the surface tilted).  The other cases
+  use features outside this library (ConvexGS, bilinear loading,
   falling or variable friction, other materials, transient sequences, Fastsim).
 
 * perfc_test/*.inp + perfc_test/get_times.ref_out -> perfc_cases.json
@@ -292,7 +294,7 @@ def parse_carter2d(path):
     return {"source": "examples/carter2d.ref_out", "cases": [rec]}
 
 
-def parse_testbank(path, wanted=(1, 6, 7, 9, 10, 13, 17, 25)):
+def parse_testbank(path, wanted=(1, 6, 7, 9, 10, 11, 13, 14, 15, 16, 17, 25, 26)):
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
     out = []

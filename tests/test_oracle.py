@@ -367,6 +367,41 @@ def test_carter2d_element_tables(oracle):
     assert _picture(o["igs"], 55, 1) == [r.replace("o", ".") for r in g["picture"]]
 
 
+@pytest.mark.parametrize("chain,cases", [("mindlin", [10, 11]), ("rolling", [13, 14, 15, 16]),
+                                         ("tilted", [25, 26])])
+def test_testbank_sequences(oracle, chain, cases):
+    """The testbank cases that continue from the previous time instance (P=0), replayed after
+    their predecessors: a Mindlin multi-step shift (11 after 10: approach and both forces
+    prescribed), transient rolling after a Hertzian shift (14-16 after 13: Fx prescribed, the
+    previous solution as initial estimate, then a creepage and a longer step), and a tilted
+    surface after a two-body shift (26 after 25).  The Newton-Raphson rows, counts, forces,
+    approach and pmax as printed; for 26 its 14 outer iterations (the first nine changes as
+    printed, the later ones within 0.1 %)."""
+    gold = {g["case"]: g for g in _load("testbank_cases.json")["cases"]}
+    res = C.replay_oracle(C.testbank_chain(chain))
+    for icase, o in zip(cases, res):
+        g = gold[icase]
+        assert o["ierror"] >= 0, icase
+        if "nr" in g:
+            _check_nr(o, g)
+        if "ncon" in g:
+            assert (o["ncon"], o["nadh"], o["nslip"]) == (g["ncon"], g["nadh"], g["nslip"]), icase
+        if "outer" in g and icase == 26:
+            # as for case 25: the first nine outer changes as printed, the later ones (down
+            # at 1e-6 of the first) within 0.1 %
+            assert len(o["outer"]) == len(g["outer"])
+            for k, (a, b) in enumerate(g["outer"]):
+                assert _printed4(o["outer"][k][1], b), (icase, k)
+                if k < 9:
+                    assert _printed4(o["outer"][k][0], a), (icase, k)
+                else:
+                    assert abs(o["outer"][k][0] - a) <= 1e-3 * a, (icase, k)
+        for key, gk in (("fn", "fn"), ("fx", "fx"), ("pmax", "pmax"), ("elen", "elen")):
+            assert _printed4(o[key], g[gk]), (icase, key, o[key], g[gk])
+        assert abs(o["pen"] - g["approach"]) <= 0.5 * 10.0 ** (math.floor(math.log10(abs(g["approach"]))) - 3) + 1e-9 \
+            or _printed4(o["pen"], g["approach"]), icase
+
+
 def test_two_body_shift_outer_iterations(oracle):
     """testbank case 25: a shift of two very different bodies (G 2e7 and 200), whose coupled
     normal and tangential problems converge over 16 outer iterations at eps 1e-8.  The printed
@@ -489,8 +524,8 @@ def test_testbank_cases_against_golden(oracle):
     Newton-Raphson iterations of cases 10 and 13 as printed."""
     gold = _load("testbank_cases.json")
     for g in gold["cases"]:
-        if "ncon" not in g:
-            continue                                   # printed without counts (case 25, below)
+        if "ncon" not in g or g["case"] in (11, 14, 15, 16, 26):
+            continue                   # printed without counts (25), or part of a sequence (below)
         o = C.oracle_solve(C.testbank_case(g["case"]))
         assert o["ierror"] == 0
         for key, gk in (("fn", "fn"), ("fx", "fx"), ("mz", "mz"), ("pen", "approach"), ("pmax", "pmax"),
