@@ -13,7 +13,7 @@ Values that a case does not repeat keep their previous value, as in the program:
 with G=1 keeps the solver settings, D=0 the potential contact, Z<2 the geometry.
 
 Supported: control digits of module 3, creepages or total forces prescribed (F=0, 1, 2),
-with Coulomb friction (L=0, V=0), elastic materials (two different bodies: keys poiss2, gg2)
+with Coulomb or falling friction (L=0, 2, 3, 4; V=0), elastic materials (two different bodies: keys poiss2, gg2)
 (M=0), no thin-sheet, heat, extra-rigid-slip or subsurface inputs; potential contact
 IPOTCN -3..-1 and 1..4; geometry IBASE 1 (quadratic), 2 (circular in x, tabulated in y),
 3 (sines in x) and 9 (element-wise), planform IPLAN 1; subsurface points (S digit, key
@@ -181,7 +181,7 @@ def read_inp(text):
         if xh["X"] >= 1:
             L.read("iI")
         bad = []
-        if vd["V"] != 0 or vd["L"] not in (0, 1):
+        if vd["V"] != 0 or vd["L"] not in (0, 1, 2, 3, 4):
             bad.append("friction law V=%d L=%d" % (vd["V"], vd["L"]))
         if vd["M"] != 0 or pb["B"] == 1:
             bad.append("material M=%d B=%d" % (vd["M"], pb["B"]))
@@ -199,9 +199,11 @@ def read_inp(text):
             v = L.read("iiiidI")
             st.update(maxgs=v[0], maxin=v[1], maxnr=v[2], maxout=v[3], eps=v[4], gausei=g)
             if g in (2, 3):
-                L.read("ddid")
+                v = L.read("ddid")
+                st.update(relax=dict(omegah=v[0], omegas=v[1], inislp=v[2], omgslp=v[3]))
             if g == 4:
-                L.read("id")
+                v = L.read("id")
+                st.update(relax=dict(st.get("relax") or {}, inislp=v[0], omgslp=v[1]))
             if g == 5:
                 v = L.read("ddiddddd")
                 st["gd"] = dict(fdecay=v[0], betath=v[1], kdowfb=v[2], d_ifc=v[3], d_lin=v[4], d_cns=v[5],
@@ -221,8 +223,13 @@ def read_inp(text):
         c["cphi"] = kin[3]
         if pb["F"] != 0:
             c["force3"] = pb["F"]
-        if vd["L"] != 1:
+        if vd["L"] == 0:
             st["fstat"] = L.read("dd")[0]
+            st["flaw"] = None
+        elif vd["L"] in (2, 3, 4):
+            # falling friction (fric_input, src/m_friclaw.f90:622-868): fkin, f1, sabsh1, f2,
+            # sabsh2, then the friction memory memdst, mem_s0
+            st["flaw"] = dict(frclaw=vd["L"], flaw=L.read("ddddd"), mem=L.read("dd"))
         if vd["C"] in (2, 3, 4, 9):
             if pb["T"] in (2, 3):
                 v = L.read("addD")
@@ -277,6 +284,12 @@ def read_inp(text):
             c["poiss2"], c["gg2"] = st["poiss"][1], st["gg"][1]
         if st["gd"] is not None:
             c["gd"] = dict(st["gd"])
+        if st.get("relax") is not None and c["gausei"] in (2, 3, 4):
+            c.update(st["relax"])
+        if st.get("flaw"):
+            f = st["flaw"]
+            c.update(frclaw=f["frclaw"], flaw=list(f["flaw"]), memdst=f["mem"][0], mem_s0=f["mem"][1])
+            c["fstat"] = f["flaw"][0] + f["flaw"][1] + f["flaw"][3]
         if pb["T"] in (2, 3):
             c["dq"] = st["dq"]
             if abs(st["chi"]) > 1e-12:

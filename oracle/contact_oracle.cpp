@@ -44,6 +44,10 @@ struct Case {
     // Newton-Raphson history on the creepages: per iteration ittang, itnr, cksi, Fx/(mu Fn),
     // ceta, Fy/(mu Fn), solver iterations
     std::vector<double> nr_hist;
+    // falling friction: the static coefficient of the law, the history of the slip loop
+    double fstat_eff = 0.0;
+    std::vector<double> slp_hist;
+    std::vector<double> muv, svx, svy;   // previous coefficient of friction and shift (set_prev_data)
     // ConvexGS: contact elements, leading edge, and for steady rolling csv = cs - cv
     std::vector<int> iel, ii2j;
     Ledg ledg;
@@ -402,9 +406,9 @@ void char_creep(Case &c, double &ch_ksi, double &ch_eta, double &ch_phi) {
     double b = (double)(float)std::max(1, c.igs.iymax - c.igs.iymin + 1) * c.dy * 0.5;
     double c11, c22, c23;
     linrol(c.nu, a / b, c11, c22, c23);
-    ch_ksi = c.pb->fstat * c.fntrue / (rc * rc * c.ga * c11);
-    ch_eta = c.pb->fstat * c.fntrue / (rc * rc * c.ga * c22);
-    ch_phi = c.pb->fstat * c.fntrue / (rc * rc * rc * c.ga * c23);
+    ch_ksi = c.fstat_eff * c.fntrue / (rc * rc * c.ga * c11);
+    ch_eta = c.fstat_eff * c.fntrue / (rc * rc * c.ga * c22);
+    ch_phi = c.fstat_eff * c.fntrue / (rc * rc * rc * c.ga * c23);
 }
 
 // sens_tang, m_solvpt.f90:544-796: d(Fx, Fy, Mz) / d(cksi, ceta, cphi) by one extra solve per
@@ -452,7 +456,21 @@ void sens_tang(Case &c, const std::vector<int> &iel, const std::vector<double> &
     }
 }
 
-// stang, m_stang.f90:28-746 (Coulomb friction)
+// fric_veldep_mu_steady, m_friclaw.f90:397-449: the coefficient of friction at steady sliding
+// with velocity v for the falling laws L = 2 (linear), 3 (rational), 4 (exponential)
+double mu_steady(const orc_problem *pb, double v) {
+    const double fkin = pb->flaw[0], f1 = pb->flaw[1], f2 = pb->flaw[3];
+    // a term that is absent gets a velocity scale of at least 1e-4 (m_friclaw.f90:826-846)
+    const double s1 = (f1 < 1e-8) ? std::max(1e-4, pb->flaw[2]) : pb->flaw[2];
+    const double s2 = (f2 < 1e-8) ? std::max(1e-4, pb->flaw[4]) : pb->flaw[4];
+    if (pb->frclaw == 2)
+        return fkin + f1 * std::max(0.0, 1.0 - 0.5 * v / s1) + f2 * std::max(0.0, 1.0 - 0.5 * v / s2);
+    if (pb->frclaw == 3) return fkin + f1 / (1.0 + v / s1) + f2 / (1.0 + (v / s2) * (v / s2));
+    if (pb->frclaw == 4) return fkin + f1 * std::exp(-std::log(2.0) * v / s1) + f2 * std::exp(-std::log(2.0) * v / s2);
+    return pb->fstat;
+}
+
+// stang, m_stang.f90:28-746 (Coulomb and falling friction)
 int stang(Case &c) {
     const orc_problem *pb = c.pb;
     TangCtx &tc = c.tc;
@@ -499,12 +517,49 @@ int stang(Case &c) {
             }
         c.have_csv = true;
     }
-    c.mus.assign(npot, pb->fstat);
-    GF3 wsfix; wsfix.init(npot);
-    stang_rhs(c, iel, facdt, wsfix);
+    // falling friction: an outer iteration on the slip velocity, m_stang.f90:250-690; the
+    // coefficient per element from the steady law at the last slip velocity, for steady
+    // rolling carried from the leading edge with the friction memory
+    const bool use_out_it = pb->frclaw >= 2 && pb->frclaw <= 4;
+    const int ixinc = (is_roll && std::fabs(c.chi - pi) < 0.01) ? -1 : 1;
+    const int ixend = (ixinc < 0) ? 1 : mx;
+    const double dt = c.dq / std::max(1e-10, c.veloc);
+    std::vector<double> slpvel(npot, 0.0), slpprv(npot, 0.0), musted(npot, 0.0), muv = c.muv;
+    // initial slip velocity, m_stang.f90:250-264: the previous shift (INISLP 0), zero (> 0),
+    // the rolling velocity (< 0)
+    for (int ii = 0; ii < npot; ii++)
+        slpvel[ii] = (pb->inislp == 0) ? std::sqrt(c.svx[ii] * c.svx[ii] + c.svy[ii] * c.svy[ii]) / dt
+                   : (pb->inislp > 0) ? 0.0 : c.veloc;
+    if (!use_out_it) c.mus.assign(npot, pb->fstat);
+    double omgslp = pb->omgslp;
+    int itslp = 0;
+    bool zreasl = false;
     int ittang = 0, itgs = 0;
     bool zready = false;
+    GF3 wsfix; wsfix.init(npot);
     GF3 tmp; tmp.init(npot);
+    Eldiv igsprv;
+    while (itslp <= std::max(1, tc.maxin - 10) && !zreasl) {
+    itslp++;
+    zreasl = true;
+    slpprv = slpvel;
+    igsprv = c.igs;
+    if (use_out_it) {
+        for (int ii = 0; ii < npot; ii++) musted[ii] = mu_steady(pb, slpvel[ii]);
+        for (int iy = 1; iy <= my; iy++) {
+            if (is_ssrol) muv[(ixend - 1) + (iy - 1) * mx] = c.fstat_eff;
+            for (int ix = ixend; ; ix -= ixinc) {
+                const int ii = (ix - 1) + (iy - 1) * mx;
+                const double theta = (pb->memdst <= 1e-9) ? 0.0
+                    : pb->memdst / (pb->memdst + dt * std::max(slpvel[ii], pb->mem_s0));
+                c.mus[ii] = theta * muv[ii] + (1.0 - theta) * musted[ii];
+                if (is_ssrol && ix != ixsta) muv[ii - ixinc] = c.mus[ii];
+                if (ix == ixsta) break;
+            }
+        }
+    }
+    stang_rhs(c, iel, facdt, wsfix);
+    zready = false;
     while (!zready && ittang < tc.maxin) {
         ittang++;
         zready = true;
@@ -547,6 +602,28 @@ int stang(Case &c) {
         }
     }
     if (!zready) ittang = -1;
+    if (use_out_it) {
+        int nadh, nslip, nplast, nexter;
+        eldiv_count(c.igs, nadh, nslip, nplast, nexter);
+        int nchanged = 0;
+        for (int ii = 0; ii < npot; ii++) if (c.igs.el[ii] != igsprv.el[ii]) nchanged++;
+        for (int ii = 0; ii < npot; ii++)
+            slpvel[ii] = (c.igs.el[ii] == Exter) ? 0.0
+                : std::sqrt(c.ss.vx(ii) * c.ss.vx(ii) + c.ss.vy(ii) * c.ss.vy(ii)) / dt;
+        GF3 d, v; d.init(npot); v.init(npot);
+        for (int ii = 0; ii < npot; ii++) { slpprv[ii] -= slpvel[ii]; d.vx(ii) = slpprv[ii]; v.vx(ii) = slpvel[ii]; }
+        const double dif = gf_rms(AllInt, d, ikX, c.igs);
+        const double difid = 0.001 * gf_rms(AllInt, v, ikX, c.igs);
+        if (itslp > 1)
+            for (int ii = 0; ii < npot; ii++)
+                if (c.igs.el[ii] == Slip && c.mus[ii] > muv[ii])
+                    slpvel[ii] = std::max(0.0, slpvel[ii] - (omgslp - 1.0) * slpprv[ii]);
+        double row[4] = {(double)nadh, (double)nslip, dif, difid};
+        c.slp_hist.insert(c.slp_hist.end(), row, row + 4);
+        if (dif > difid && nslip > 0) zreasl = false;
+        if (!zreasl && nchanged > 0 && itslp % 20 == 0) omgslp = 0.8 * omgslp;
+    }
+    }
     c.itgs = itgs;
     if (pb->sens >= 3) {
         sens_tang(c, iel, facdt, wsfix);
@@ -685,7 +762,9 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     c.fntrue = pb->fn; c.pen = pb->pen;
     c.cksi = pb->cksi; c.ceta = pb->ceta; c.cphi = pb->cphi;
     c.chi = pb->chi; c.veloc = pb->veloc;
-    c.muscal = pb->fstat;
+    // the static coefficient of a falling law, fric_update (m_friclaw.f90:296-310)
+    c.fstat_eff = (pb->frclaw >= 2 && pb->frclaw <= 4) ? pb->flaw[0] + pb->flaw[1] + pb->flaw[3] : pb->fstat;
+    c.muscal = c.fstat_eff;
     // Hertzian solution & potential contact (hzsol m_hertz.f90:29-93, potcon_hertz)
     int ihertz = 0;
     c.mx = std::max(1, (int)std::nearbyint(pb->potprm[0]));
@@ -772,7 +851,7 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     c.ps.init(c.npot);
     c.ss.init(c.npot);
     c.igs.init(c.mx, c.my);
-    c.mus.assign(c.npot, pb->fstat);
+    c.mus.assign(c.npot, c.fstat_eff);
     if (pb->iestim != 0 && pb->igs_init) {
         for (int ii = 0; ii < c.npot; ii++) {
             c.igs.el[ii] = pb->igs_init[ii];
@@ -801,6 +880,31 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
         }
     }
     areas(c.igv);
+    // coefficient of friction and shift of the previous time instance (P=0): copied for shifts,
+    // carried one rolling step for rolling (gf3_dq_shift, m_gridfunc.f90:1864-1987) with the
+    // static coefficient and zero shift beyond the grid; otherwise the static coefficient
+    c.muv.assign(c.npot, c.fstat_eff);
+    c.svx.assign(c.npot, 0.0); c.svy.assign(c.npot, 0.0);
+    if (pb->pvtime == 0 && pb->mus_init) {
+        const bool rolling = pb->tang == 2 || pb->tang == 3;
+        int kx = 0; double facx = 0.0;
+        if (rolling) {
+            kx = (int)(c.dq * std::cos(c.chi) / dx);
+            facx = c.dq * std::cos(c.chi) / dx - (double)(float)kx;
+        }
+        for (int iy = 0; iy < c.my; iy++)
+            for (int ix = 0; ix < c.mx; ix++) {
+                auto at = [&](const double *f, int jx, double ext) {
+                    return (jx < 0 || jx >= c.mx) ? ext : f[jx + iy * c.mx];
+                };
+                const int ii = ix + iy * c.mx;
+                c.muv[ii] = (1.0 - facx) * at(pb->mus_init, ix + kx, c.fstat_eff) + facx * at(pb->mus_init, ix + kx + 1, c.fstat_eff);
+                if (pb->svx_init) {
+                    c.svx[ii] = (1.0 - facx) * at(pb->svx_init, ix + kx, 0.0) + facx * at(pb->svx_init, ix + kx + 1, 0.0);
+                    c.svy[ii] = (1.0 - facx) * at(pb->svy_init, ix + kx, 0.0) + facx * at(pb->svy_init, ix + kx + 1, 0.0);
+                }
+            }
+    }
     init_curr_data(c, ihertz);
     // solver context
     TangCtx &tc = c.tc;
@@ -868,6 +972,8 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     r->itnorm = c.itnorm; r->ittang = c.ittang; r->itcg = c.itcg; r->itgs = c.itgs; r->solver = c.solver_eff;
     for (int io = 0; io < 4; io++)
         for (int ji = 0; ji < 4; ji++) r->sens[io + 4 * ji] = c.sens[io][ji];
+    r->nslp = (int)(c.slp_hist.size() / 4);
+    for (int q = 0; q < std::min(r->nslp, 64) * 4; q++) r->slp[q] = c.slp_hist[q];
     r->nnr = (int)(c.nr_hist.size() / 7);
     if (r->nr_hist)
         for (int q = 0; q < std::min(r->nnr, r->nr_cap) * 7; q++) r->nr_hist[q] = c.nr_hist[q];
@@ -885,6 +991,7 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
         if (r->sy) r->sy[ii] = c.ss.vy(ii) / c.dq;
         if (r->h) r->h[ii] = c.hs.vn(ii);
         if (r->igs) r->igs[ii] = c.igs.el[ii];
+        if (r->mus) r->mus[ii] = c.mus[ii];
     }
     if (c.itnorm < 0) r->ierror = CNTC_err_norm;
     else if (c.ittang < 0) r->ierror = CNTC_err_tang;

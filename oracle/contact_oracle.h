@@ -85,6 +85,15 @@ typedef struct {
      * (pvtime 0: all components, 1: the normal one; may be NULL: zero, as for pvtime 2) */
     const int    *igv_init;
     const double *pvn_init, *pvx_init, *pvy_init;
+    /* friction law (L digit, m_friclaw.f90): 0 Coulomb (fstat, fkin above); 2, 3, 4 falling
+     * with the slip velocity, linear, rational, exponential: flaw = [fkin, f1, sabsh1, f2,
+     * sabsh2] (flin / frat / fexp), with the memory distance memdst and velocity mem_s0 */
+    int    frclaw;
+    double flaw[5];
+    double memdst, mem_s0;
+    /* previous time instance of a transient sequence with falling friction: the coefficient of
+     * friction and the shift per element (may be NULL) */
+    const double *mus_init, *svx_init, *svy_init;
 } orc_problem;
 
 /* Outputs of one case.  Array pointers are caller-allocated with mx*my
@@ -103,6 +112,7 @@ typedef struct {
     double *sx, *sy;
     double *h;
     int    *igs;
+    double *mus;                   /* coefficient of friction per element (may be NULL) */
     /* sens(iout, iin) column-major as t_output%sens: iout Fn, Fx/(mu Fn), Fy/(mu Fn), Mz;
      * iin pen, cksi, ceta, cphi (zero where not computed) */
     double sens[16];
@@ -115,6 +125,11 @@ typedef struct {
      * the change of the tractions and its tolerance 5 eps |p| (the first 64) */
     int     nout;
     double  outer[128];
+    /* iterations on the slip velocity for falling friction (L = 2..4): per iteration the
+     * adhesion and slip counts, the change of the slip velocities and its tolerance
+     * 0.001 |s| (the first 64) */
+    int     nslp;
+    double  slp[256];
 } orc_result;
 
 void orc_default_problem(orc_problem *pb);

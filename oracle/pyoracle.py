@@ -53,6 +53,10 @@ class Problem(ctypes.Structure):
         ("igv_init", ctypes.POINTER(ctypes.c_int)),
         ("pvn_init", ctypes.POINTER(ctypes.c_double)), ("pvx_init", ctypes.POINTER(ctypes.c_double)),
         ("pvy_init", ctypes.POINTER(ctypes.c_double)),
+        ("frclaw", ctypes.c_int), ("flaw", ctypes.c_double * 5), ("memdst", ctypes.c_double),
+        ("mem_s0", ctypes.c_double),
+        ("mus_init", ctypes.POINTER(ctypes.c_double)), ("svx_init", ctypes.POINTER(ctypes.c_double)),
+        ("svy_init", ctypes.POINTER(ctypes.c_double)),
     ]
 
 
@@ -78,9 +82,11 @@ class Result(ctypes.Structure):
         ("sx", ctypes.POINTER(ctypes.c_double)), ("sy", ctypes.POINTER(ctypes.c_double)),
         ("h", ctypes.POINTER(ctypes.c_double)),
         ("igs", ctypes.POINTER(ctypes.c_int)),
+        ("mus", ctypes.POINTER(ctypes.c_double)),
         ("sens", ctypes.c_double * 16),
         ("nr_cap", ctypes.c_int), ("nnr", ctypes.c_int), ("nr_hist", ctypes.POINTER(ctypes.c_double)),
         ("nout", ctypes.c_int), ("outer", ctypes.c_double * 128),
+        ("nslp", ctypes.c_int), ("slp", ctypes.c_double * 256),
     ]
 
 
@@ -164,6 +170,10 @@ def solve(pb, h=None, warm=None, fields=True, fast=False, prev=None):
         keep += [igv] + pvs
         pb.igv_init = igv.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
         pb.pvn_init, pb.pvx_init, pb.pvy_init = (_dptr(a) for a in pvs)
+        if "mus" in prev:
+            extra = [np.ascontiguousarray(prev[k], dtype=np.float64) for k in ("mus", "svx", "svy")]
+            keep += extra
+            pb.mus_init, pb.svx_init, pb.svy_init = (_dptr(a) for a in extra)
     if warm is not None and "sens" in warm:
         sv = np.ascontiguousarray(np.asarray(warm["sens"], dtype=np.float64).T.ravel())
         keep.append(sv)
@@ -188,7 +198,7 @@ def solve(pb, h=None, warm=None, fields=True, fast=False, prev=None):
     res = Result()
     arrs = {}
     if fields:
-        for k in ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h"):
+        for k in ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h", "mus"):
             arrs[k] = np.zeros(n, dtype=np.float64)
             setattr(res, k, _dptr(arrs[k]))
         arrs["igs"] = np.zeros(n, dtype=np.int32)
@@ -198,7 +208,9 @@ def solve(pb, h=None, warm=None, fields=True, fast=False, prev=None):
     res.nr_hist = _dptr(hist)
     lib(fast).orc_calculate(ctypes.byref(pb), ctypes.byref(res))
     out = {k: getattr(res, k) for k, _ in Result._fields_ if k not in
-           ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h", "igs", "sens", "nr_cap", "nr_hist", "outer")}
+           ("pn", "px", "py", "un", "ux", "uy", "sx", "sy", "h", "igs", "mus", "sens", "nr_cap", "nr_hist", "outer",
+            "slp")}
+    out["slp"] = np.array(res.slp[:4 * min(res.nslp, 64)], dtype=np.float64).reshape(-1, 4)
     out["outer"] = np.array(res.outer[:2 * min(res.nout, 64)], dtype=np.float64).reshape(-1, 2)
     # sens[iout][iin]: iout Fn, Fx, Fy, Mz; iin pen, cksi, ceta, cphi
     out["sens"] = np.array(res.sens[:], dtype=np.float64).reshape(4, 4).T.copy()

@@ -315,6 +315,13 @@ def to_oracle(case):
     pb.force3 = case.get("force3", 0)
     if "omegah" in case:
         pb.omegah, pb.omegas = case["omegah"], case["omegas"]
+    if "inislp" in case:
+        pb.inislp, pb.omgslp = case["inislp"], case["omgslp"]
+    if case.get("frclaw", 0) >= 2:
+        pb.frclaw = case["frclaw"]
+        for k, v in enumerate(case["flaw"]):
+            pb.flaw[k] = v
+        pb.memdst, pb.mem_s0 = case.get("memdst", 0.0), case.get("mem_s0", 0.0)
     pb.fxrel, pb.fyrel = case.get("fxrel", 0.0), case.get("fyrel", 0.0)
     pb.sens = case.get("sens", 1)
     pb.standalone = int(case.get("standalone", False))
@@ -366,8 +373,10 @@ def _on_grid(prev, grid):
     mx, my, dx, dy, xc1, yc1 = grid
     kx = int(round((xc1 - prev["xc1"]) / dx))
     ky = int(round((yc1 - prev["yc1"]) / dy))
+    keys = ("pn", "px", "py", "mus", "svx", "svy")
+    prev = dict(prev, svx=prev["sx"] * prev.get("dq_used", 1.0), svy=prev["sy"] * prev.get("dq_used", 1.0))
     out = {"igs": np.zeros(mx * my, dtype=np.int32)}
-    for k in ("pn", "px", "py"):
+    for k in keys:
         out[k] = np.zeros(mx * my)
     for iy in range(my):
         jy = iy + ky
@@ -377,9 +386,20 @@ def _on_grid(prev, grid):
             jx = ix + kx
             if 0 <= jx < prev["mx"]:
                 out["igs"][ix + iy * mx] = prev["igs"][jx + jy * prev["mx"]]
-                for k in ("pn", "px", "py"):
+                for k in keys:
                     out[k][ix + iy * mx] = prev[k][jx + jy * prev["mx"]]
     return out
+
+
+def _step(case):
+    """The rolling step dq a case is solved with (check_roll_stepsize, m_sdis.f90:125-206):
+    dx for steady rolling other than by ConvexGS, 1 for shifts."""
+    grid = _grid_of(case, None) if case.get("ipotcn", -3) >= 1 else None
+    if case.get("tang", 3) not in (2, 3):
+        return 1.0
+    if case.get("tang") == 3 and case.get("gausei", 0) != 2 and grid is not None:
+        return grid[2]
+    return case.get("dq", grid[2] if grid else 1.0)
 
 
 def replay_oracle(case_list, fast=False):
@@ -407,6 +427,7 @@ def replay_oracle(case_list, fast=False):
             if c.get("pvtime", 2) <= 1:
                 pv = moved
         prev = po.solve(pb, h=h, warm=warm, fast=fast, prev=pv)
+        prev["dq_used"] = _step(c)
         out.append(prev)
     return out
 

@@ -52,6 +52,10 @@ fixtures next to this script:
   from the previous one, subsurface stresses along one row): the reader's cases, the printed
   outer iterations, totals and counts, and the printed subsurface maxima.
 
+* examples/veldep_fric.inp + veldep_fric.ref_out -> veldep_fric_case1.json
+  case 1, steady rolling with an exponential falling friction law (L=4) on a 92x1 strip by
+  ConvexGS: the printed iterations on the slip velocity, sweeps, counts and totals.
+
 * testbank/test_caddon.ref_out -> test_caddon_re1.json
   output of src/test_caddon.f90 for result element 1 (module 3 through the library
   interface in SPCK units: Hertzian 21x33 grid, penetration prescribed, creepage 0.001,
@@ -497,6 +501,28 @@ def parse_spence35(root):
     return {"source": "examples/spence35.inp, examples/spence35.ref_out", "inputs": cases, "cases": out}
 
 
+def parse_veldep_fric(root):
+    """Case 1 of examples/veldep_fric.inp: steady rolling on a 92x1 strip (ConvexGS) with an
+    exponential falling friction law (L=4): the reader's case and the printed iterations on
+    the slip velocity (adhesion and slip counts, the change of the slip velocities and its
+    tolerance), the ConvexGS sweeps, counts and totals."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from contact_gb300 import inp
+    case = inp.read_inp(open(os.path.join(root, "examples", "veldep_fric.inp")).read())[0]
+    case = {k: (v.tolist() if hasattr(v, "tolist") else v) for k, v in case.items()}
+    body = re.split(r"\n Case\s+\d+\n", open(os.path.join(root, "examples", "veldep_fric.ref_out")).read())[1]
+    rec = {"slp": [[int(a), int(b), float(c), float(d)] for a, b, c, d in
+                   re.findall(r"Vel-dep: A, S=\s*(\d+)\s+(\d+), \|Sk-Sk-1\|, \.001 \|Sk\| :\s*(\S+)\s+(\S+)", body)]}
+    m = re.search(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+    rec["norm_ncon"], rec["norm_itcg"] = int(m.group(1)), int(m.group(3))
+    _tang_final(rec, body)
+    res = _results_block(body)
+    res.pop("picture", None)
+    rec.update(res)
+    return {"source": "examples/veldep_fric.inp, examples/veldep_fric.ref_out (case 1)", "input": case,
+            "result": rec}
+
+
 def parse_test_caddon(path):
     text = open(path).read()
     block = text.split("...start processing of Result Element")[1]     # element 1, first solve
@@ -553,6 +579,9 @@ def main():
     sp = parse_spence35(root)
     with open(os.path.join(HERE, "spence35.json"), "w") as f:
         json.dump(sp, f, separators=(",", ":"))
+    vf = parse_veldep_fric(root)
+    with open(os.path.join(HERE, "veldep_fric_case1.json"), "w") as f:
+        json.dump(vf, f, indent=0)
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)

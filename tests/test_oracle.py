@@ -468,6 +468,26 @@ def test_bentall_sequence(oracle):
             assert _printed4(o[key], gc[gk]), (gc["case"], key, o[key], gc[gk])
 
 
+def test_falling_friction_steady_rolling(oracle):
+    """examples/veldep_fric.inp case 1: steady rolling with an exponential falling friction law
+    (L=4: mu = fkin + fexp1 2^(-v/sabsh1)) on a 92x1 strip by ConvexGS, the coefficient of
+    friction per element following the slip velocity of the previous solve (m_stang.f90:
+    250-690).  Every printed iteration on the slip velocity (adhesion and slip counts, the
+    change of the slip velocities and its tolerance, 4 digits), the 687 ConvexGS sweeps, the
+    NormCG iterations, counts and totals."""
+    g = _load("veldep_fric_case1.json")
+    gr = g["result"]
+    o = C.oracle_solve(g["input"])
+    assert o["ierror"] >= 0 and o["solver"] == 3
+    assert len(o["slp"]) == len(gr["slp"])
+    for row, gs in zip(o["slp"], gr["slp"]):
+        assert (int(row[0]), int(row[1])) == (gs[0], gs[1]) and _printed4(row[2], gs[2]) and _printed4(row[3], gs[3])
+    assert (o["itcg"], o["itgs"]) == (gr["norm_itcg"], gr["tang_it"])
+    assert (o["ncon"], o["nadh"], o["nslip"]) == (gr["ncon"], gr["nadh"], gr["nslip"])
+    for key, gk in (("fn", "fn"), ("fx", "fx"), ("elen", "elen"), ("pen", "approach"), ("pmax", "pmax")):
+        assert _printed4(o[key], gr[gk]), (key, o[key], gr[gk])
+
+
 def test_caddon_element1_against_golden(oracle):
     """src/test_caddon.f90, result element 1 (testbank/test_caddon.ref_out).  The reference
     printed in SPCK units: lengths in m, forces in N acting on body 2 (the sign of CONTACT's
