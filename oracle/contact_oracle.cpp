@@ -540,89 +540,89 @@ int stang(Case &c) {
     GF3 tmp; tmp.init(npot);
     Eldiv igsprv;
     while (itslp <= std::max(1, tc.maxin - 10) && !zreasl) {
-    itslp++;
-    zreasl = true;
-    slpprv = slpvel;
-    igsprv = c.igs;
-    if (use_out_it) {
-        for (int ii = 0; ii < npot; ii++) musted[ii] = mu_steady(pb, slpvel[ii]);
-        for (int iy = 1; iy <= my; iy++) {
-            if (is_ssrol) muv[(ixend - 1) + (iy - 1) * mx] = c.fstat_eff;
-            for (int ix = ixend; ; ix -= ixinc) {
-                const int ii = (ix - 1) + (iy - 1) * mx;
-                const double theta = (pb->memdst <= 1e-9) ? 0.0
-                    : pb->memdst / (pb->memdst + dt * std::max(slpvel[ii], pb->mem_s0));
-                c.mus[ii] = theta * muv[ii] + (1.0 - theta) * musted[ii];
-                if (is_ssrol && ix != ixsta) muv[ii - ixinc] = c.mus[ii];
-                if (ix == ixsta) break;
-            }
-        }
-    }
-    stang_rhs(c, iel, facdt, wsfix);
-    zready = false;
-    while (!zready && ittang < tc.maxin) {
-        ittang++;
-        zready = true;
-        int info = 0; double errpt = 0.0;
-        int it = solvpt(c, ittang, iel, facdt, wsfix, info, errpt);
-        if (c.unsupported || c.aborted) return -1;
-        itgs += it;
-        if (info >= 3) { zready = true; ittang = -1; }
-        int newins = 0;
-        double tol = std::sqrt(2.0) * errpt;
-        for (int ii : iel) {
-            if (c.igs.el[ii] == Adhes) {
-                double pabs = std::sqrt(c.ps.vx(ii) * c.ps.vx(ii) + c.ps.vy(ii) * c.ps.vy(ii));
-                if (pabs >= c.mus[ii] * c.ps.vn(ii) + tol) {
-                    newins++;
-                    c.igs.el[ii] = Slip;
-                    c.ps.vx(ii) = c.ps.vx(ii) * c.mus[ii] * c.ps.vn(ii) / pabs;
-                    c.ps.vy(ii) = c.ps.vy(ii) * c.mus[ii] * c.ps.vn(ii) / pabs;
+        itslp++;
+        zreasl = true;
+        slpprv = slpvel;
+        igsprv = c.igs;
+        if (use_out_it) {
+            for (int ii = 0; ii < npot; ii++) musted[ii] = mu_steady(pb, slpvel[ii]);
+            for (int iy = 1; iy <= my; iy++) {
+                if (is_ssrol) muv[(ixend - 1) + (iy - 1) * mx] = c.fstat_eff;
+                for (int ix = ixend; ; ix -= ixinc) {
+                    const int ii = (ix - 1) + (iy - 1) * mx;
+                    const double theta = (pb->memdst <= 1e-9) ? 0.0
+                        : pb->memdst / (pb->memdst + dt * std::max(slpvel[ii], pb->mem_s0));
+                    c.mus[ii] = theta * muv[ii] + (1.0 - theta) * musted[ii];
+                    if (is_ssrol && ix != ixsta) muv[ii - ixinc] = c.mus[ii];
+                    if (ix == ixsta) break;
                 }
             }
         }
-        if (newins != 0) zready = false;
-        if (zready) {
-            areas(c.igs);
-            int ii0 = (std::max(1, mx / 2) - 1) + (std::max(1, my / 2) - 1) * mx;
-            gf_set(AllElm, 1.0, tmp, ikTANG, c.igs);
-            double tol1 = errpt * 2.0 * std::fabs(aijpj(ii0, ikX, tmp, c.igs, ikX, c.cs, mx, my));
-            double tol2 = errpt * 2.0 * std::fabs(aijpj(ii0, ikY, tmp, c.igs, ikY, c.cs, mx, my));
-            int newadh = 0;
+        stang_rhs(c, iel, facdt, wsfix);
+        zready = false;
+        while (!zready && ittang < tc.maxin) {
+            ittang++;
+            zready = true;
+            int info = 0; double errpt = 0.0;
+            int it = solvpt(c, ittang, iel, facdt, wsfix, info, errpt);
+            if (c.unsupported || c.aborted) return -1;
+            itgs += it;
+            if (info >= 3) { zready = true; ittang = -1; }
+            int newins = 0;
+            double tol = std::sqrt(2.0) * errpt;
             for (int ii : iel) {
-                if (c.igs.el[ii] == Slip) {
-                    double ww = c.ss.vx(ii) * c.ps.vx(ii) + c.ss.vy(ii) * c.ps.vy(ii);
-                    double tl = tol1 * std::fabs(c.ps.vx(ii)) + tol2 * std::fabs(c.ps.vy(ii)) +
-                                errpt * (std::fabs(c.ss.vx(ii)) + std::fabs(c.ss.vy(ii)));
-                    if (ww > tl) { c.igs.el[ii] = Adhes; newadh++; }
+                if (c.igs.el[ii] == Adhes) {
+                    double pabs = std::sqrt(c.ps.vx(ii) * c.ps.vx(ii) + c.ps.vy(ii) * c.ps.vy(ii));
+                    if (pabs >= c.mus[ii] * c.ps.vn(ii) + tol) {
+                        newins++;
+                        c.igs.el[ii] = Slip;
+                        c.ps.vx(ii) = c.ps.vx(ii) * c.mus[ii] * c.ps.vn(ii) / pabs;
+                        c.ps.vy(ii) = c.ps.vy(ii) * c.mus[ii] * c.ps.vn(ii) / pabs;
+                    }
                 }
             }
-            if (newadh != 0) zready = false;
-            if (info > 0) zready = true;
+            if (newins != 0) zready = false;
+            if (zready) {
+                areas(c.igs);
+                int ii0 = (std::max(1, mx / 2) - 1) + (std::max(1, my / 2) - 1) * mx;
+                gf_set(AllElm, 1.0, tmp, ikTANG, c.igs);
+                double tol1 = errpt * 2.0 * std::fabs(aijpj(ii0, ikX, tmp, c.igs, ikX, c.cs, mx, my));
+                double tol2 = errpt * 2.0 * std::fabs(aijpj(ii0, ikY, tmp, c.igs, ikY, c.cs, mx, my));
+                int newadh = 0;
+                for (int ii : iel) {
+                    if (c.igs.el[ii] == Slip) {
+                        double ww = c.ss.vx(ii) * c.ps.vx(ii) + c.ss.vy(ii) * c.ps.vy(ii);
+                        double tl = tol1 * std::fabs(c.ps.vx(ii)) + tol2 * std::fabs(c.ps.vy(ii)) +
+                                    errpt * (std::fabs(c.ss.vx(ii)) + std::fabs(c.ss.vy(ii)));
+                        if (ww > tl) { c.igs.el[ii] = Adhes; newadh++; }
+                    }
+                }
+                if (newadh != 0) zready = false;
+                if (info > 0) zready = true;
+            }
         }
-    }
-    if (!zready) ittang = -1;
-    if (use_out_it) {
-        int nadh, nslip, nplast, nexter;
-        eldiv_count(c.igs, nadh, nslip, nplast, nexter);
-        int nchanged = 0;
-        for (int ii = 0; ii < npot; ii++) if (c.igs.el[ii] != igsprv.el[ii]) nchanged++;
-        for (int ii = 0; ii < npot; ii++)
-            slpvel[ii] = (c.igs.el[ii] == Exter) ? 0.0
-                : std::sqrt(c.ss.vx(ii) * c.ss.vx(ii) + c.ss.vy(ii) * c.ss.vy(ii)) / dt;
-        GF3 d, v; d.init(npot); v.init(npot);
-        for (int ii = 0; ii < npot; ii++) { slpprv[ii] -= slpvel[ii]; d.vx(ii) = slpprv[ii]; v.vx(ii) = slpvel[ii]; }
-        const double dif = gf_rms(AllInt, d, ikX, c.igs);
-        const double difid = 0.001 * gf_rms(AllInt, v, ikX, c.igs);
-        if (itslp > 1)
+        if (!zready) ittang = -1;
+        if (use_out_it) {
+            int nadh, nslip, nplast, nexter;
+            eldiv_count(c.igs, nadh, nslip, nplast, nexter);
+            int nchanged = 0;
+            for (int ii = 0; ii < npot; ii++) if (c.igs.el[ii] != igsprv.el[ii]) nchanged++;
             for (int ii = 0; ii < npot; ii++)
-                if (c.igs.el[ii] == Slip && c.mus[ii] > muv[ii])
-                    slpvel[ii] = std::max(0.0, slpvel[ii] - (omgslp - 1.0) * slpprv[ii]);
-        double row[4] = {(double)nadh, (double)nslip, dif, difid};
-        c.slp_hist.insert(c.slp_hist.end(), row, row + 4);
-        if (dif > difid && nslip > 0) zreasl = false;
-        if (!zreasl && nchanged > 0 && itslp % 20 == 0) omgslp = 0.8 * omgslp;
-    }
+                slpvel[ii] = (c.igs.el[ii] == Exter) ? 0.0
+                    : std::sqrt(c.ss.vx(ii) * c.ss.vx(ii) + c.ss.vy(ii) * c.ss.vy(ii)) / dt;
+            GF3 d, v; d.init(npot); v.init(npot);
+            for (int ii = 0; ii < npot; ii++) { slpprv[ii] -= slpvel[ii]; d.vx(ii) = slpprv[ii]; v.vx(ii) = slpvel[ii]; }
+            const double dif = gf_rms(AllInt, d, ikX, c.igs);
+            const double difid = 0.001 * gf_rms(AllInt, v, ikX, c.igs);
+            if (itslp > 1)
+                for (int ii = 0; ii < npot; ii++)
+                    if (c.igs.el[ii] == Slip && c.mus[ii] > muv[ii])
+                        slpvel[ii] = std::max(0.0, slpvel[ii] - (omgslp - 1.0) * slpprv[ii]);
+            double row[4] = {(double)nadh, (double)nslip, dif, difid};
+            c.slp_hist.insert(c.slp_hist.end(), row, row + 4);
+            if (dif > difid && nslip > 0) zreasl = false;
+            if (!zreasl && nchanged > 0 && itslp % 20 == 0) omgslp = 0.8 * omgslp;
+        }
     }
     c.itgs = itgs;
     if (pb->sens >= 3) {
