@@ -22,7 +22,8 @@
  * SteadyGS), the five printed cases of examples/bentall.ref_out (two coupled
  * materials, chi = 180 deg, a warm-started sequence) and all 171 cases of
  * examples/catt_to_cart.ref_out (transient sequences from the previous time
- * instance); see tests/test_oracle.py.  With the subsurface stresses it reproduces
+ * instance), and examples/veldep_fric.ref_out (falling friction: case 1 exactly, the slip
+ * iterations of the transient steps 1-34 row by row, 35-53 by count); see tests/test_oracle.py.  With the subsurface stresses it reproduces
  * all 35 load steps of examples/spence35.ref_out (tests/test_subsurf_cpu.py).  Its subsurface stresses (orc_subsurf.hpp)
  * reproduce examples/subsurf.ref_subs and the maxima of subsurf.ref_out
  * (tests/test_subsurf_cpu.py).  GDsteady (G=5) and transient rolling (T=2) have no

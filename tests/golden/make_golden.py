@@ -55,6 +55,10 @@ fixtures next to this script:
 * examples/veldep_fric.inp + veldep_fric.ref_out -> veldep_fric_case1.json
   case 1, steady rolling with an exponential falling friction law (L=4) on a 92x1 strip by
   ConvexGS: the printed iterations on the slip velocity, sweeps, counts and totals.
+* examples/veldep_fric.inp + veldep_fric.ref_out -> veldep_fric_sequence.json
+  all 53 cases (steady rolling, then transient rolling steps continuing from the previous
+  time instance): the reader's cases and per case the printed slip-velocity iterations,
+  the last solve's sweeps, counts and totals.
 
 * testbank/test_caddon.ref_out -> test_caddon_re1.json
   output of src/test_caddon.f90 for result element 1 (module 3 through the library
@@ -523,6 +527,30 @@ def parse_veldep_fric(root):
             "result": rec}
 
 
+def parse_veldep_sequence(root):
+    """All 53 cases of examples/veldep_fric.inp, to be replayed in order: the reader's cases
+    and per printed case its iterations on the slip velocity (adhesion and slip counts, the
+    change of the slip velocities and its tolerance), the last tangential solve's iterations,
+    counts and totals where printed."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from contact_gb300 import inp
+    cases = inp.read_inp(open(os.path.join(root, "examples", "veldep_fric.inp")).read())
+    cases = [{k: (v.tolist() if hasattr(v, "tolist") else v) for k, v in c.items()} for c in cases]
+    blocks = re.split(r"\n Case\s+(\d+)\n", open(os.path.join(root, "examples", "veldep_fric.ref_out")).read())
+    out = []
+    for k in range(1, len(blocks), 2):
+        body = blocks[k + 1]
+        rec = {"case": int(blocks[k]),
+               "slp": [[int(a), int(b), float(c), float(d)] for a, b, c, d in
+                       re.findall(r"Vel-dep: A, S=\s*(\d+)\s+(\d+), \|Sk-Sk-1\|, \.001 \|Sk\| :\s*(\S+)\s+(\S+)", body)]}
+        _tang_final(rec, body)
+        res = _results_block(body)
+        res.pop("picture", None)
+        rec.update(res)
+        out.append(rec)
+    return {"source": "examples/veldep_fric.inp, examples/veldep_fric.ref_out", "inputs": cases, "cases": out}
+
+
 def parse_test_caddon(path):
     text = open(path).read()
     block = text.split("...start processing of Result Element")[1]     # element 1, first solve
@@ -582,6 +610,9 @@ def main():
     vf = parse_veldep_fric(root)
     with open(os.path.join(HERE, "veldep_fric_case1.json"), "w") as f:
         json.dump(vf, f, indent=0)
+    vs = parse_veldep_sequence(root)
+    with open(os.path.join(HERE, "veldep_fric_sequence.json"), "w") as f:
+        json.dump(vs, f, separators=(",", ":"))
     tcd = parse_test_caddon(os.path.join(root, "testbank", "test_caddon.ref_out"))
     with open(os.path.join(HERE, "test_caddon_re1.json"), "w") as f:
         json.dump(tcd, f, indent=0)

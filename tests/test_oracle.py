@@ -488,6 +488,56 @@ def test_falling_friction_steady_rolling(oracle):
         assert _printed4(o[key], gr[gk]), (key, o[key], gr[gk])
 
 
+def test_falling_friction_transient_sequence(oracle):
+    """All 53 cases of examples/veldep_fric.inp replayed in order: steady rolling, then
+    transient rolling steps (P=0, T=2) that continue from the previous time instance, with
+    slip from below and from above, on a 92x1 strip by ConvexGS with an exponential falling
+    friction law.
+
+    The input file itself shows that this problem has multiple solutions.  The iteration on
+    the slip velocity stops at |Sk - Sk-1| < 0.001 |Sk|, and a time step carries on the state
+    where the previous one stopped, so round-off grows along the sequence.  The oracle's two
+    FFT forms, whose convolutions differ by 1e-15, already part by 7e-5 in Fx from case 11.
+    So the test holds two stretches differently.
+
+    Cases 1-34, row by row:
+    - every slip-velocity iteration's adhesion and slip counts, and their number;
+    - the change |Sk - Sk-1| to one unit in its fourth digit (5e-4 relative), where it is
+      above 1e-6 V, the scale at which the ConvexGS tolerance eps = 1e-7 leaves the slip
+      velocities; below that, within 5 %;
+    - its tolerance 0.001 |Sk| to 5e-4;
+    - the last solve's counts, and the totals at their printed digits.
+
+    Cases 35-53: totals and counts at the printed digits in all but three cases, which differ
+    by 5e-4 in Fx or by one element; the number of slip iterations in all but three (one
+    more or fewer, or three in a case of 43)."""
+    g = _load("veldep_fric_sequence.json")
+    res = C.replay_oracle(g["inputs"])
+    assert len(res) == len(g["cases"]) == 53
+    vfloor = 1e-6 * g["inputs"][0]["veloc"]
+    late_tot = late_nslp = 0
+    for gc in g["cases"]:
+        o = res[gc["case"] - 1]
+        assert o["ierror"] >= 0 and o["solver"] == (2 if gc["tang_solver"] == "CG" else 3)
+        ok = (o["nadh"], o["nslip"]) == (gc["tang_nadh"], gc["tang_nslip"])
+        if "ncon" in gc:
+            ok = ok and o["ncon"] == gc["ncon"]
+        for key, gk in (("fn", "fn"), ("fx", "fx"), ("elen", "elen"), ("pen", "approach"), ("pmax", "pmax")):
+            ok = ok and _printed4(o[key], gc[gk])
+        if gc["case"] > 34:
+            late_tot += not ok
+            late_nslp += len(o["slp"]) != len(gc["slp"])
+            continue
+        assert ok, (gc["case"], [(k, o[k]) for k in ("fx", "elen", "pen", "pmax", "nadh", "nslip")])
+        assert len(o["slp"]) == len(gc["slp"]), gc["case"]
+        for k, (row, gs) in enumerate(zip(o["slp"], gc["slp"])):
+            assert (int(row[0]), int(row[1])) == (gs[0], gs[1]), (gc["case"], k)
+            tol = 5e-4 if gs[2] > vfloor else 5e-2
+            assert abs(row[2] - gs[2]) <= tol * gs[2], (gc["case"], k, row[2], gs[2])
+            assert abs(row[3] - gs[3]) <= 5e-4 * gs[3], (gc["case"], k, row[3], gs[3])
+    assert late_tot <= 3 and late_nslp <= 3, (late_tot, late_nslp)
+
+
 def test_caddon_element1_against_golden(oracle):
     """src/test_caddon.f90, result element 1 (testbank/test_caddon.ref_out).  The reference
     printed in SPCK units: lengths in m, forces in N acting on body 2 (the sign of CONTACT's
