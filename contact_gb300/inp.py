@@ -14,7 +14,8 @@ with G=1 keeps the solver settings, D=0 the potential contact, Z<2 the geometry.
 
 Supported: control digits of module 3, creepages or total forces prescribed (F=0, 1, 2),
 with Coulomb or falling friction (L=0, 2, 3, 4; V=0), elastic materials (two different bodies: keys poiss2, gg2)
-(M=0), no thin-sheet, heat, extra-rigid-slip or subsurface inputs; potential contact
+(M=0) or elastic bodies with an elastic interfacial layer (M=4 with TAU_C0 = 0: keys mater, gg3,
+laythk, tau_c0, k_tau), no thin-sheet, heat or extra-rigid-slip inputs; potential contact
 IPOTCN -3..-1 and 1..4; geometry IBASE 1 (quadratic), 2 (circular in x, tabulated in y),
 3 (sines in x) and 9 (element-wise), planform IPLAN 1; subsurface points (S digit, key
 'subs'), previous time instances (P digit, key 'pvtime').  IBASE 2 and 3 are evaluated here
@@ -183,7 +184,7 @@ def read_inp(text):
         bad = []
         if vd["V"] != 0 or vd["L"] not in (0, 1, 2, 3, 4):
             bad.append("friction law V=%d L=%d" % (vd["V"], vd["L"]))
-        if vd["M"] != 0 or pb["B"] == 1:
+        if vd["M"] not in (0, 4) or pb["B"] == 1:
             bad.append("material M=%d B=%d" % (vd["M"], pb["B"]))
         if xh["H"] != 0 or vd["E"] != 0:
             bad.append("heat or extra rigid slip inputs")
@@ -239,6 +240,14 @@ def read_inp(text):
                 break
             v = L.read("dddd")
             st.update(poiss=(v[0], v[1]), gg=(v[2], v[3]))
+            if vd["M"] == 4:
+                # the interfacial layer (m_sinput.f90:942-955): GG3, LAYTHK, TAU_C0, K_TAU;
+                # TAU_C0 >= 1e10 means no yield limit
+                v = L.read("dddd")
+                st["layer"] = dict(gg3=v[0], laythk=v[1], tau_c0=0.0 if v[2] >= 1e10 else v[2], k_tau=v[3])
+        if vd["M"] == 4 and (st.get("layer") is None or st["layer"]["tau_c0"] > 1e-10):
+            cases.append({"unsupported": "plastic interfacial layer (M=4, TAU_C0 > 0)"})
+            break
         if vd["D"] == 2:
             ip = L.read("i")[0]
             if -3 <= ip <= -1:
@@ -282,6 +291,8 @@ def read_inp(text):
             c["subs"] = st["subs"]
         if st["poiss"][0] != st["poiss"][1] or st["gg"][0] != st["gg"][1]:
             c["poiss2"], c["gg2"] = st["poiss"][1], st["gg"][1]
+        if vd["M"] == 4:
+            c.update(mater=4, **st["layer"])
         if st["gd"] is not None:
             c["gd"] = dict(st["gd"])
         if st.get("relax") is not None and c["gausei"] in (2, 3, 4):

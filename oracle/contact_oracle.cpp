@@ -509,6 +509,7 @@ int stang(Case &c) {
         elascf_pcwcns(c.ak, c.nu, mx, my, c.dx, c.dy, std::cos(c.chi) * c.dq, std::sin(c.chi) * c.dq, sh);
         c.csv.alloc(mx, my, c.dx, c.dy);
         c.csv.ga = c.ga; c.csv.ga_inv = 1.0 / c.ga; c.csv.nt_cpl = c.cs.nt_cpl;
+        c.csv.use_3bl = c.cs.use_3bl; c.csv.flx_3bl = c.cs.flx_3bl;
         for (int jk = 0; jk < 3; jk++)
             for (size_t q = 0; q < c.cs.cf[0][0].size(); q++) {
                 c.csv.cf[0][jk][q] = c.cs.cf[0][jk][q] - sh.cf[0][jk][q];
@@ -756,6 +757,14 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     c.ga = 2.0 / (1.0 / gg1 + 1.0 / gg2);
     c.nu = c.ga * (p1 / gg1 + p2 / gg2) / 2.0;
     c.ak = (c.ga / 4.0) * ((1.0 - 2.0 * p1) / gg1 - (1.0 - 2.0 * p2) / gg2);
+    // M=0 elastic, M=4 with an elastic interfacial layer; a plastic layer (use_plast,
+    // m_stang.f90:68) is not restated
+    if ((pb->mater != 0 && pb->mater != 4) ||
+        (pb->mater == 4 && (pb->tau_c0 > 1e-10 && pb->tau_c0 <= 1e10))) {
+        r->ierror = CNTC_err_other; return r->ierror;
+    }
+    const bool use_3bl = pb->mater == 4 && pb->laythk >= 1e-10;           // inflcf_mater
+    const double flx_3bl = pb->mater == 4 ? pb->laythk / pb->gg3 : 0.0;  // m_sinput.f90:955
     c.maxout = pb->maxout;
     if (c.maxout >= 2 && std::fabs(c.ak) < 1e-4) c.maxout = 1;
     if (c.maxout <= 1 && std::fabs(c.ak) >= 1e-4 && !pb->standalone) c.maxout = 10;
@@ -804,19 +813,22 @@ int orc_calculate(const orc_problem *pb, orc_result *r) {
     // check_roll_stepsize, m_sdis.f90:125-206
     bool is_roll = pb->tang == 2 || pb->tang == 3, is_ssrol = pb->tang == 3;
     c.dq = (pb->dq > 0.0) ? pb->dq : dx;
-    if (is_ssrol && pb->gausei != 2) {
+    if ((is_ssrol && pb->gausei != 2) || pb->mater == 4) {
         if (pb->tang >= 1 && std::fabs(c.chi) > 0.01 && std::fabs(c.chi - pi) > 0.01) c.chi = 0.0;
         c.dq = dx;
     }
     if (!is_roll) { c.chi = 0.0; c.dq = 1.0; c.veloc = 1.0; }
     // influence coefficients, sgencr m_visc.f90:127-376
     c.cs.alloc(c.mx, c.my, dx, dy); c.ms.alloc(c.mx, c.my, dx, dy);
-    for (Inflcf *f : {&c.cs, &c.ms}) { f->ga = c.ga; f->ga_inv = 1.0 / c.ga; }
+    for (Inflcf *f : {&c.cs, &c.ms}) {
+        f->ga = c.ga; f->ga_inv = 1.0 / c.ga; f->use_3bl = use_3bl; f->flx_3bl = flx_3bl;
+    }
     elascf_pcwcns(c.ak, c.nu, c.mx, c.my, dx, dy, 0.0, 0.0, c.cs);
     bool nt_cpl = std::fabs(c.ak) >= 1e-6;
     c.cs.nt_cpl = nt_cpl; c.ms.nt_cpl = nt_cpl;
     if (is_roll && (nt_cpl || pb->tang == 2)) {
         c.cv.alloc(c.mx, c.my, dx, dy); c.cv.ga = c.ga; c.cv.ga_inv = 1.0 / c.ga; c.cv.nt_cpl = nt_cpl;
+        c.cv.use_3bl = use_3bl; c.cv.flx_3bl = flx_3bl;
         elascf_pcwcns(c.ak, c.nu, c.mx, c.my, dx, dy, std::cos(c.chi) * c.dq, std::sin(c.chi) * c.dq, c.cv);
         for (int jk = 1; jk <= 3; jk++)
             for (size_t q = 0; q < c.cv.cf[0][0].size(); q++) {

@@ -9,7 +9,8 @@
  * Parity pinning: the oracle reproduces the reference's golden outputs
  * testbank/test_table_mx11.ref_fx (3220 Hertzian steady-rolling cases, NormCG
  * + SteadyGS, printed to 6 decimals), the first series of
- * examples/tractcurv.ref_out (48x44 grid, 4 significant digits), both cases of
+ * examples/tractcurv.ref_out (48x44 grid, 4 significant digits) and its second series (cases
+ * 31-60: an elastic interfacial layer, M=4, with falling friction and a friction memory), both cases of
  * examples/cattaneo.ref_out (NormCG, TangCG on the shift problem), result
  * element 1 of testbank/test_caddon.ref_out and testbank/contact_nonhz.ref_out
  * (approach prescribed, spin) and
@@ -95,6 +96,11 @@ typedef struct {
     /* previous time instance of a transient sequence with falling friction: the coefficient of
      * friction and the shift per element (may be NULL) */
     const double *mus_init, *svx_init, *svy_init;
+    /* material model (M digit): 0 elastic; 4 elastic bodies with an interfacial layer of modulus
+     * gg3 and thickness laythk (m_sinput.f90:942-955), its flexibility laythk / gg3 added to the
+     * tangential displacements; a plastic layer (tau_c0 > 0) is not restated */
+    int    mater;
+    double gg3, laythk, tau_c0, k_tau;
 } orc_problem;
 
 /* Outputs of one case.  Array pointers are caller-allocated with mx*my

@@ -121,7 +121,10 @@ inline double aijpj(int ii, int ik, const GF3 &p, const Eldiv &pe, int jkarg, co
                 rowsum += c.at(ix - jx, iy - jy, ik, jk) * pv[(jx - 1) + jh2];
             partsum += rowsum;
         }
-    return partsum * c.ga_inv;
+    partsum *= c.ga_inv;
+    // the layer's own term (m_aijpj.f90:246-252); jkarg -2 and -3 both contain direction ik
+    if (c.use_3bl && ik <= ikY && (jkarg == ik || jkarg <= ikTANG)) partsum += c.flx_3bl * p.col(ik)[ii];
+    return partsum;
 }
 
 // fft_VecAijPj, m_aijpj.f90:712-1015: u_ik (+)= C_ik,jk * p_jk on the elements of igs in iigs.
@@ -191,7 +194,7 @@ inline void fft_vecaijpj(const Eldiv &igs, bool ladd, int iigs, GF3 &u, int ik, 
         }
 }
 
-// gf3_VecAijPj, m_aijpj.f90:258-451 (FFT branch; M=4 and B=1 layer terms not used here)
+// gf3_VecAijPj, m_aijpj.f90:258-451 (FFT branch, with the M=4 layer term; B=1 is not restated)
 inline void vecaijpj(const Eldiv &igs, int iigs, GF3 &u, int ikarg, const GF3 &p, const Eldiv &pe,
                      int jkarg, Inflcf &c, int mx, int my) {
     int ik0, ik1, jk0, jk1;
@@ -212,6 +215,17 @@ inline void vecaijpj(const Eldiv &igs, int iigs, GF3 &u, int ikarg, const GF3 &p
         }
     }
     gf_scal(iigs, c.ga_inv, u, ikarg, igs);
+    if (c.use_3bl) {                              // m_aijpj.f90:409-421
+        int g0, g1;
+        igsrange(iigs, g0, g1);
+        for (int ik = ik0; ik <= std::min(ik1, (int)ikY); ik++) {
+            if (!(jkarg == ik || jkarg <= ikTANG)) continue;
+            double *uv = u.col(ik);
+            const double *pv = p.col(ik);
+            for (int ii = 0; ii < (int)igs.el.size(); ii++)
+                if (igs.el[ii] >= g0 && igs.el[ii] <= g1) uv[ii] += c.flx_3bl * pv[ii];
+        }
+    }
 }
 
 // fft_makePrec, m_aijpj.f90:457-708: m = ga^2 * IFFT(1 ./ FFT(c)) on the cf window

@@ -578,6 +578,10 @@ struct Inflcf {
     double dx = 0, dy = 0, dq = 0;
     bool nt_cpl = true;
     double ga = 1, ga_inv = 1;
+    // interfacial layer of M=4 (inflcf_mater, m_hierarch_data.f90:1557-1570): flexibility
+    // laythk / gg3 of px on ux and py on uy
+    bool use_3bl = false;
+    double flx_3bl = 0;
     std::vector<double> cf[3][3];                 // (2cf_mx)*(2cf_my), ix fastest
     int fft_mx = -1, fft_my = -1;
     bool fft_ok[3][3] = {};

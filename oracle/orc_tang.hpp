@@ -125,6 +125,7 @@ inline int stdygs(const TangCtx &cx, const GF3 &ws, Inflcf &cs, Eldiv &igs, cons
                   int &info, double &err, bool &bad, bool is_sens = false) {
     const int mx = cx.mx, my = cx.my, npot = cx.npot;
     bad = false;
+    const double flx = cs.use_3bl ? cs.flx_3bl : 0.0;     // m_solvpt.f90:2922-2929
     int ixsta, ixinc, ixend;
     // is_sens: the stopping tolerance is relative to the change from the initial estimate
     // (m_solvpt.f90:2893-2899, 3138-3145)
@@ -163,10 +164,10 @@ inline int stdygs(const TangCtx &cx, const GF3 &ws, Inflcf &cs, Eldiv &igs, cons
                 int jj = (jx - 1) + (iy - 1) * mx;
                 while (igs.el[jj] == Adhes && jx != ixsta) { jx -= ixinc; jj = (jx - 1) + (iy - 1) * mx; }
                 double coef[2][2];
-                coef[0][0] = cs.ga_inv * (cs.at(0, 0, 1, 1) - cs.at(jx - ix, 0, 1, 1));
+                coef[0][0] = cs.ga_inv * (cs.at(0, 0, 1, 1) - cs.at(jx - ix, 0, 1, 1)) + flx;
                 coef[0][1] = cs.ga_inv * (cs.at(0, 0, 1, 2) - cs.at(jx - ix, 0, 1, 2));
                 coef[1][0] = cs.ga_inv * (cs.at(0, 0, 2, 1) - cs.at(jx - ix, 0, 2, 1));
-                coef[1][1] = cs.ga_inv * (cs.at(0, 0, 2, 2) - cs.at(jx - ix, 0, 2, 2));
+                coef[1][1] = cs.ga_inv * (cs.at(0, 0, 2, 2) - cs.at(jx - ix, 0, 2, 2)) + flx;
                 double s[2];
                 s[0] = ws.c[0][ii] + aijpj(ii, ikX, dp, igs, ikTANG, cs, mx, my);
                 s[1] = ws.c[1][ii] + aijpj(ii, ikY, dp, igs, ikTANG, cs, mx, my);
@@ -246,11 +247,12 @@ inline int cnvxgs(const TangCtx &cx, const GF3 &ws, Inflcf &cs, const Inflcf *cs
     if (std::fabs(cx.chi - pi) < 0.01) { ista = k - 1; iinc = -1; iend = 0; }
     else { ista = 0; iinc = 1; iend = k - 1; }
     double coefs[2][2], coefsv[2][2];
-    coefs[0][0] = cs.ga_inv * cs.at(0, 0, 1, 1); coefs[0][1] = cs.ga_inv * cs.at(0, 0, 1, 2);
-    coefs[1][0] = cs.ga_inv * cs.at(0, 0, 2, 1); coefs[1][1] = cs.ga_inv * cs.at(0, 0, 2, 2);
+    const double flx = cs.use_3bl ? cs.flx_3bl : 0.0;     // m_solvpt.f90:2523-2552
+    coefs[0][0] = cs.ga_inv * cs.at(0, 0, 1, 1) + flx; coefs[0][1] = cs.ga_inv * cs.at(0, 0, 1, 2);
+    coefs[1][0] = cs.ga_inv * cs.at(0, 0, 2, 1); coefs[1][1] = cs.ga_inv * cs.at(0, 0, 2, 2) + flx;
     const Inflcf &cv = csv ? *csv : cs;
-    coefsv[0][0] = cv.ga_inv * cv.at(0, 0, 1, 1); coefsv[0][1] = cv.ga_inv * cv.at(0, 0, 1, 2);
-    coefsv[1][0] = cv.ga_inv * cv.at(0, 0, 2, 1); coefsv[1][1] = cv.ga_inv * cv.at(0, 0, 2, 2);
+    coefsv[0][0] = cv.ga_inv * cv.at(0, 0, 1, 1) + flx; coefsv[0][1] = cv.ga_inv * cv.at(0, 0, 1, 2);
+    coefsv[1][0] = cv.ga_inv * cv.at(0, 0, 2, 1); coefsv[1][1] = cv.ga_inv * cv.at(0, 0, 2, 2) + flx;
     int nadh, nslip, nplst, nexter;
     eldiv_count(igs, nadh, nslip, nplst, nexter);
     const double facnel = std::sqrt((double)(float)npot / (double)(float)(nadh + nslip + nplst));
@@ -668,10 +670,11 @@ inline int gdsteady(const TangCtx &cx, int maxgd, double eps, const GF3 &ws, Inf
     const int mx = cx.mx, my = cx.my, npot = cx.npot;
     bad = false;
     double coefs[2][2];
-    coefs[0][0] = cs.ga_inv * cs.at(0, 0, 1, 1);
+    const double flx = cs.use_3bl ? cs.flx_3bl : 0.0;     // gdsteady.f90:54-74
+    coefs[0][0] = cs.ga_inv * cs.at(0, 0, 1, 1) + flx;
     coefs[0][1] = cs.ga_inv * cs.at(0, 0, 1, 2);
     coefs[1][0] = cs.ga_inv * cs.at(0, 0, 2, 1);
-    coefs[1][1] = cs.ga_inv * cs.at(0, 0, 2, 2);
+    coefs[1][1] = cs.ga_inv * cs.at(0, 0, 2, 2) + flx;
     Eldiv igsold = igs, igsopt = igs;
     GF3 dp, n, t, r, dv, v, q, psopt, ssopt, pold;
     for (GF3 *g : {&dp, &n, &t, &r, &dv, &v, &q, &psopt, &ssopt, &pold}) g->init(npot);

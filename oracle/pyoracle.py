@@ -57,6 +57,8 @@ class Problem(ctypes.Structure):
         ("mem_s0", ctypes.c_double),
         ("mus_init", ctypes.POINTER(ctypes.c_double)), ("svx_init", ctypes.POINTER(ctypes.c_double)),
         ("svy_init", ctypes.POINTER(ctypes.c_double)),
+        ("mater", ctypes.c_int), ("gg3", ctypes.c_double), ("laythk", ctypes.c_double),
+        ("tau_c0", ctypes.c_double), ("k_tau", ctypes.c_double),
     ]
 
 

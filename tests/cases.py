@@ -322,6 +322,9 @@ def to_oracle(case):
         for k, v in enumerate(case["flaw"]):
             pb.flaw[k] = v
         pb.memdst, pb.mem_s0 = case.get("memdst", 0.0), case.get("mem_s0", 0.0)
+    if case.get("mater", 0) == 4:
+        pb.mater = 4
+        pb.gg3, pb.laythk, pb.tau_c0, pb.k_tau = case["gg3"], case["laythk"], case["tau_c0"], case["k_tau"]
     pb.fxrel, pb.fyrel = case.get("fxrel", 0.0), case.get("fyrel", 0.0)
     pb.sens = case.get("sens", 1)
     pb.standalone = int(case.get("standalone", False))

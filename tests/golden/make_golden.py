@@ -55,6 +55,10 @@ fixtures next to this script:
 * examples/veldep_fric.inp + veldep_fric.ref_out -> veldep_fric_case1.json
   case 1, steady rolling with an exponential falling friction law (L=4) on a 92x1 strip by
   ConvexGS: the printed iterations on the slip velocity, sweeps, counts and totals.
+* examples/tractcurv.inp + tractcurv.ref_out -> tractcurv_series2.json
+  the second series (cases 31-60): elastic bodies with an elastic interfacial layer (M=4),
+  exponential falling friction with a friction memory, SteadyGS on a 48x44 grid: the reader's
+  cases and per case the slip-velocity iterations, counts, iterations, totals and picture.
 * examples/veldep_fric.inp + veldep_fric.ref_out -> veldep_fric_sequence.json
   all 53 cases (steady rolling, then transient rolling steps continuing from the previous
   time instance): the reader's cases and per case the printed slip-velocity iterations,
@@ -527,6 +531,34 @@ def parse_veldep_fric(root):
             "result": rec}
 
 
+def parse_tractcurv_series2(root):
+    """Cases 31-60 of examples/tractcurv.inp, the series with an interfacial layer (M=4, TAU_C0 0)
+    and exponential falling friction with a friction memory: the reader's cases and per case
+    the printed slip-velocity iterations (the change of the slip velocities and its tolerance),
+    the NormCG and SteadyGS iterations, counts, totals and the element-division picture."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from contact_gb300 import inp
+    cases = inp.read_inp(open(os.path.join(root, "examples", "tractcurv.inp")).read())[30:60]
+    cases = [{k: (v.tolist() if hasattr(v, "tolist") else v) for k, v in c.items()} for c in cases]
+    blocks = re.split(r"\n Case\s+(\d+)\n", open(os.path.join(root, "examples", "tractcurv.ref_out")).read())
+    out = []
+    for k in range(1, len(blocks), 2):
+        icase = int(blocks[k])
+        if not 31 <= icase <= 60:
+            continue
+        body = blocks[k + 1]
+        rec = {"case": icase,
+               "slp": [[float(c), float(d)] for c, d in
+                       re.findall(r"Vel-dep: \|Sk-Sk-1\|, \.001 \|Sk\| :\s*(\S+)\s+(\S+)", body)]}
+        ms = re.findall(r"Norm: final element division: C, E=\s*(\d+)\s+(\d+)\s+ItCG=\s*(\d+)", body)
+        rec["norm_itcg"] = int(ms[-1][2])
+        _tang_final(rec, body)
+        rec.update(_results_block(body))
+        out.append(rec)
+    return {"source": "examples/tractcurv.inp, examples/tractcurv.ref_out (cases 31-60)", "inputs": cases,
+            "cases": out}
+
+
 def parse_veldep_sequence(root):
     """All 53 cases of examples/veldep_fric.inp, to be replayed in order: the reader's cases
     and per printed case its iterations on the slip velocity (adhesion and slip counts, the
@@ -610,6 +642,9 @@ def main():
     vf = parse_veldep_fric(root)
     with open(os.path.join(HERE, "veldep_fric_case1.json"), "w") as f:
         json.dump(vf, f, indent=0)
+    t2 = parse_tractcurv_series2(root)
+    with open(os.path.join(HERE, "tractcurv_series2.json"), "w") as f:
+        json.dump(t2, f, separators=(",", ":"))
     vs = parse_veldep_sequence(root)
     with open(os.path.join(HERE, "veldep_fric_sequence.json"), "w") as f:
         json.dump(vs, f, separators=(",", ":"))

@@ -52,10 +52,16 @@ def _same_case(a, b):
 
 def test_tractcurv_first_series():
     cs = _read("examples/tractcurv.inp")
-    assert len([c for c in cs if "unsupported" not in c]) == 30
-    assert "unsupported" in cs[30]                       # series 2: falling friction, interface layer
+    assert len([c for c in cs if "unsupported" not in c]) == 60
     for c in cs[:30]:
         _same_case(c, C.tractcurv_case(c["cksi"]))
+    # series 2: an elastic interfacial layer (M=4), kept by the cases that repeat only the M digit,
+    # and exponential falling friction with a friction memory
+    for c in cs[30:60]:
+        assert (c["mater"], c["gg3"], c["laythk"], c["tau_c0"]) == (4, 8200.0, 1.25, 0.0)
+        assert (c["frclaw"], c["memdst"], c["mem_s0"]) == (4, 0.003, 1.0)
+    assert "M=3" in cs[60]["unsupported"]                # series 3: FASTSIM
+    assert "plastic" in _read("examples/plastic_3bl.inp")[1]["unsupported"]
 
 
 def test_cattaneo_and_testbank():

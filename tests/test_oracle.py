@@ -109,6 +109,45 @@ def test_tractcurv_series(oracle, tc_gold):
         assert pic == [row.replace("o", ".") for row in c["picture"]], c["case"]
 
 
+def test_tractcurv_interfacial_layer(oracle):
+    """The second series of examples/tractcurv.inp (cases 31-60), replayed in order: elastic
+    bodies with an elastic interfacial layer (M=4, GG3 8200, LAYTHK 1.25, no yield limit), whose
+    flexibility LAYTHK/GG3 adds to the tangential displacements (m_aijpj.f90:246-252, 409-421)
+    and to the diagonals of the tangential solvers; exponential falling friction with a friction
+    memory (MEMDST 0.003), by SteadyGS on a 48x44 grid.  Every printed slip-velocity iteration
+    and its tolerance to 4 digits, the NormCG and SteadyGS iterations, counts and the
+    element-division picture exactly, forces, energy, approach and pmax to 4 digits."""
+    g = _load("tractcurv_series2.json")
+    res = C.replay_oracle(g["inputs"])
+    assert len(res) == len(g["cases"]) == 30
+    for o, gc in zip(res, g["cases"]):
+        assert o["ierror"] >= 0 and o["solver"] == 4, gc["case"]
+        assert len(o["slp"]) == len(gc["slp"]), gc["case"]
+        for row, gs in zip(o["slp"], gc["slp"]):
+            assert _close4(row[2], gs[0]) and _close4(row[3], gs[1]), (gc["case"], row, gs)
+        assert (o["itcg"], o["itgs"]) == (gc["norm_itcg"], gc["tang_it"]), gc["case"]
+        assert (o["ncon"], o["nadh"], o["nslip"]) == (gc["ncon"], gc["nadh"], gc["nslip"]), gc["case"]
+        for key, gk in (("fn", "fn"), ("fx", "fx"), ("elen", "elen"), ("pen", "approach"), ("pmax", "pmax")):
+            assert _close4(o[key], gc[gk]), (gc["case"], key, o[key], gc[gk])
+        sym = np.array([".", "*", "S", "P"])[o["igs"]].reshape(44, 48)
+        assert ["".join(row) for row in sym] == [row.replace("o", ".") for row in gc["picture"]], gc["case"]
+
+
+def test_interfacial_layer_flexibility(oracle):
+    """The layer's term on its own: with M=4 the tangential row products gain LAYTHK/GG3 times
+    the element's own traction, in the FFT product and the direct row sum alike, and a layer of
+    zero thickness is the elastic case (inflcf_mater, m_hierarch_data.f90:1557-1570)."""
+    base = C.tractcurv_case(0.001)
+    layer = dict(base, mater=4, gg3=8200.0, laythk=1.25, tau_c0=0.0, k_tau=0.0)
+    thin = dict(layer, laythk=0.0)
+    o0, o1, o2 = (C.oracle_solve(c) for c in (base, layer, thin))
+    assert o2["fx"] == o0["fx"] and o2["nslip"] == o0["nslip"]
+    # the flexible layer lowers the tangential stiffness: less |Fx| at the same creepage
+    assert abs(o1["fx"]) < abs(o0["fx"])
+    # a plastic layer is refused, not approximated
+    assert C.oracle_solve(dict(layer, tau_c0=560.0))["ierror"] < 0
+
+
 def _opt_fft_size_py(n):
     """Independent restatement of m_aijpj.f90:1022-1119: start at the next power of two and apply
     the factor trades (e.g. 4 -> 3, 6 -> 5, 8 -> 7) while the product stays >= n."""
