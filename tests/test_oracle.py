@@ -1,17 +1,14 @@
 """The CPU oracle against the reference's own regression outputs (CPU only).
 
-test_table_mx11.json holds the 3220 printed lines of src/test_table.f90 (testbank/
-test_table_mx11.ref_fx); tractcurv_series1.json the first series of examples/tractcurv.inp
-(examples/tractcurv.ref_out); cattaneo.json the two cases of examples/cattaneo.inp
-(examples/cattaneo.ref_out: NormCG, and TangCG on the shift problem); test_caddon_re1.json
-result element 1 of src/test_caddon.f90 (testbank/test_caddon.ref_out: penetration
-prescribed, spin, SteadyGS, printed in SPCK units); testbank_cases.json cases 1 and 7 of
-testbank/testbank.inp (TangCG shift with prescribed approach, SteadyGS on a 41x41 grid);
-catt_to_cart_case1.json case 1 of examples/catt_to_cart.inp (Fx prescribed, Newton-Raphson
-on the shift); carter2d.json the element tables of examples/carter2d.inp (a 55x1 strip);
-contact_nonhz_re1.json result element 1 of testbank/contact_nonhz.ref_out (test_caddon's
-element 1 in CONTACT units, with exact counts).  The oracle has to reproduce them at their printed precision before any GPU
-result is compared with it.
+The fixtures under tests/golden are the reference's printed outputs, read as text by
+tests/golden/make_golden.py; each test names the output it reproduces:
+- testbank/test_table_mx11.ref_fx: 3220 lines of src/test_table.f90;
+- examples/tractcurv.ref_out: series 1 (elastic) and series 2 (interfacial layer, falling friction);
+- examples/cattaneo, catt_to_cart, carter2d, bentall, spence35, veldep_fric (.ref_out);
+- testbank/testbank.ref_out cases, test_caddon.ref_out and contact_nonhz.ref_out.
+Sequences are replayed in order through the input reader (tests/cases.py replay_oracle).  The
+oracle has to reproduce them at their printed precision before any GPU result is compared
+with it.
 """
 import json
 import math
@@ -671,13 +668,18 @@ def test_baseline_build_equals_parity_build(oracle):
     """The oracle's baseline build (Stockham FFT, timed as the CPU baseline) solves like the
     parity build: same iterations and element division, forces within 1e-12, tractions
     within 1e-12 of pmax, on steady rolling (GDsteady, SteadyGS), shifts (with forces
-    prescribed), a two-dimensional strip and a rail geometry; FFT lengths with factors 2, 3,
-    5 and 7 and a length-2 column transform."""
+    prescribed), a two-dimensional strip and a rail geometry, and with an interfacial layer
+    (M=4) under GDsteady and TangCG; FFT lengths with factors 2, 3, 5 and 7 and a length-2
+    column transform."""
     from contact_gb300 import inp
     perfc = [c for c in _load("perfc_cases.json")["cases"] if c["name"] == "norm_problm_1p"][0]
+
+    def layer(c):
+        return dict(c, mater=4, gg3=0.1 * c["gg"], laythk=0.05, tau_c0=0.0, k_tau=0.0)
     for case in (C.config0(gausei=5, eps=1e-10, mx=31, my=27), C.config0(gausei=0, eps=1e-8, mx=25, my=25),
                  C.cattaneo_case(2, 0.008155), C.cattaneo_forces_case(), C.testbank_case(13), C.carter2d_case(),
-                 inp.materialize(perfc["case"])):
+                 inp.materialize(perfc["case"]), layer(C.config0(gausei=5, eps=1e-10, mx=31, my=27)),
+                 layer(C.cattaneo_case(2, 0.008155))):
         a = C.oracle_solve(case)
         b = C.oracle_solve(case, fast=True)
         assert (a["ierror"], a["itcg"], a["itgs"]) == (b["ierror"], b["itcg"], b["itgs"])
