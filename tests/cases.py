@@ -188,7 +188,15 @@ def testbank_case(icase):
     10: case 1 with Fn 1722 N, Fx = -0.875 mu Fn and Fy = 0 prescribed (F=2), the grid given by
     its corners.  13: a Cattaneo shift on a 41x41 Hertzian grid (semi-axes 4.1 mm, scale
     1.17143) with the normal problem skipped for the elliptical traction bound (B=2), Fn
-    0.7563, Fx = 0.657 mu Fn prescribed (F=1), G 1, nu 0.28, mu 0.4013, TangCG, eps 1e-6."""
+    0.7563, Fx = 0.657 mu Fn prescribed (F=1), G 1, nu 0.28, mu 0.4013, TangCG, eps 1e-6.
+    4: steady rolling on a 3x3 Hertzian grid (semi-axes 0.5 mm, scale 3) with one element in
+    contact, two materials (G 200 and 1, nu 0.28), Fn 1, Fx = 0.999 mu Fn prescribed (F=1), mu 1,
+    SteadyGS, eps 1e-4, up to 10 outer iterations of the coupled problems."""
+    if icase == 4:
+        return dict(tang=3, norm=1, bound=0, gausei=0, maxgs=80, maxin=100, maxnr=30, maxout=10, eps=1e-4,
+                    poiss=0.28, poiss2=0.28, gg=200.0, gg2=1.0, fstat=1.0, veloc=1000.0, fn=1.0, ceta=0.0,
+                    cphi=0.0, force3=1, fxrel=0.999, dq=1.0, ipotcn=-3, potprm=[3, 3, 0.5, 0.5, 3.0],
+                    standalone=True)
     if icase == 6:
         return dict(tang=3, norm=1, bound=0, gausei=2, maxgs=999, maxin=100, maxnr=30, maxout=1, eps=1e-5,
                     omegah=0.8, omegas=0.8, poiss=0.28, gg=82000.0, fstat=0.3, veloc=30000.0, fn=35780.0,

@@ -306,7 +306,7 @@ def parse_carter2d(path):
     return {"source": "examples/carter2d.ref_out", "cases": [rec]}
 
 
-def parse_testbank(path, wanted=(1, 6, 7, 9, 10, 11, 13, 14, 15, 16, 17, 25, 26)):
+def parse_testbank(path, wanted=(1, 4, 6, 7, 9, 10, 11, 13, 14, 15, 16, 17, 25, 26)):
     text = open(path).read()
     blocks = re.split(r"\n Case\s+(\d+)\n", text)
     out = []

@@ -620,14 +620,15 @@ def test_contact_nonhz_element1(oracle):
 
 
 def test_testbank_cases_against_golden(oracle):
-    """testbank/testbank.inp cases 1 (shift, approach prescribed, TangCG), 6 (Carter's strip by
+    """testbank/testbank.inp cases 1 (shift, approach prescribed, TangCG), 4 (steady rolling of
+    two materials with Fx prescribed: Newton-Raphson over two outer iterations), 6 (Carter's strip by
     ConvexGS with a rolling step of 5 dx), 7 (steady rolling, SteadyGS, 41x41), 9 (two
     materials: coupled normal and tangential problems, ten outer iterations), 17 (transient
     rolling from rest, Fx prescribed), 10 (shift with
     Fn, Fx, Fy prescribed) and 13 (Hertzian shift, normal problem skipped, Fx prescribed):
     forces, moment, approach, pmax and elastic energy to the printed 4 digits; element counts,
     pictures and the NormCG and TangCG/SteadyGS/ConvexGS iteration counts exact; the
-    Newton-Raphson iterations of cases 10 and 13 as printed."""
+    Newton-Raphson iterations of cases 4, 10 and 13 as printed."""
     gold = _load("testbank_cases.json")
     for g in gold["cases"]:
         if "ncon" not in g or g["case"] in (11, 14, 15, 16, 26):
@@ -645,6 +646,11 @@ def test_testbank_cases_against_golden(oracle):
             assert _picture(o["igs"], o["mx"], o["my"]) == [r.replace("o", ".") for r in g["picture"]]
         if "nr" in g:
             _check_nr(o, g)
+        if "outer" in g:              # the change of the tractions per outer iteration, its tolerance
+            assert o["nout"] == len(g["outer"]), g["case"]
+            for (d, t), (gd, gt) in zip(o["outer"], g["outer"]):
+                assert (gd < 1e-12 and d < 1e-12) or _printed4(d, gd), (g["case"], d, gd)
+                assert _printed4(t, gt), (g["case"], t, gt)
 
 
 @pytest.mark.parametrize("name", ["norm_problm_1p", "norm_problm_1f", "norm_problm_2p", "norm_problm_2f",
