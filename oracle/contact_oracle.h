@@ -14,7 +14,7 @@
  * examples/cattaneo.ref_out (NormCG, TangCG on the shift problem), result
  * element 1 of testbank/test_caddon.ref_out and testbank/contact_nonhz.ref_out
  * (approach prescribed, spin) and
- * cases 1, 4, 6, 7, 9-11, 13-17, 25 and 26 of testbank/testbank.ref_out (TangCG shift,
+ * cases 1, 3, 4, 6, 7, 9-11, 13-17, 25 and 26 of testbank/testbank.ref_out (TangCG shift,
  * ConvexGS strip, SteadyGS 41x41, coupled materials, prescribed forces, transient
  * rolling from rest),
  * and the Newton-Raphson iterations on prescribed total forces of case 2 of

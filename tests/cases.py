@@ -192,6 +192,10 @@ def testbank_case(icase):
     4: steady rolling on a 3x3 Hertzian grid (semi-axes 0.5 mm, scale 3) with one element in
     contact, two materials (G 200 and 1, nu 0.28), Fn 1, Fx = 0.999 mu Fn prescribed (F=1), mu 1,
     SteadyGS, eps 1e-4, up to 10 outer iterations of the coupled problems."""
+    if icase == 3:                # case 4's bodies and grid, normal problem only
+        return dict(tang=0, norm=1, bound=0, gausei=0, maxgs=80, maxin=100, maxnr=30, maxout=1, eps=1e-4,
+                    poiss=0.28, poiss2=0.28, gg=200.0, gg2=1.0, fstat=1.0, veloc=1.0, fn=1.0, cksi=0.0,
+                    ceta=0.0, cphi=0.0, ipotcn=-3, potprm=[3, 3, 0.5, 0.5, 3.0], standalone=True)
     if icase == 4:
         return dict(tang=3, norm=1, bound=0, gausei=0, maxgs=80, maxin=100, maxnr=30, maxout=10, eps=1e-4,
                     poiss=0.28, poiss2=0.28, gg=200.0, gg2=1.0, fstat=1.0, veloc=1000.0, fn=1.0, ceta=0.0,

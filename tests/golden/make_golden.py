@@ -59,6 +59,8 @@ fixtures next to this script:
   the second series (cases 31-60): elastic bodies with an elastic interfacial layer (M=4),
   exponential falling friction with a friction memory, SteadyGS on a 48x44 grid: the reader's
   cases and per case the slip-velocity iterations, counts, iterations, totals and picture.
+* testbank/testbank.ref_out -> testbank_case3_subs.json
+  case 3: the normal problem of two bodies and the subsurface field at six points in both.
 * examples/veldep_fric.inp + veldep_fric.ref_out -> veldep_fric_sequence.json
   all 53 cases (steady rolling, then transient rolling steps continuing from the previous
   time instance): the reader's cases and per case the printed slip-velocity iterations,
@@ -559,6 +561,32 @@ def parse_tractcurv_series2(root):
             "cases": out}
 
 
+def parse_testbank_case3(path):
+    """Case 3 of testbank/testbank.inp: the normal problem of two bodies (G 200 and 1) on a 3x3
+    Hertzian grid with one element in contact, and the subsurface field at six points in both
+    bodies: per point x, y, z, the three displacements, the stress tensor row by row, SigHyd and
+    SigVM as printed (strings), and the block's printed maxima."""
+    body = re.split(r"\n Case\s+(\d+)\n", open(path).read())
+    body = body[body.index("3") + 1]
+    s = r"\s*(\S+?)\s*"
+    pts = []
+    for m in re.finditer(r"Position \(X,Y,Z\):" + s * 3 + r"\n.*\n" +
+                         "".join(r"\s*%d%s;%s%s%s\n" % (i, s, s, s, s) for i in (1, 2, 3)) +
+                         r"\s*SigHyd =" + s + r", SigVM =" + s + r"\n", body):
+        g = m.groups()
+        pts.append(list(g[0:3]) + [g[3], g[7], g[11]] + list(g[4:7]) + list(g[8:11]) + list(g[12:15]) + list(g[15:17]))
+    summ = []
+    for ln in body.splitlines():
+        m = re.match(r"\s*(ABSMAX|MAX|MIN)\s+(\w+)\s*=\s*(\S+)\s+AT \(X,Y,Z\) = \(\s*(\S+),\s*(\S+),\s*(\S+)\)", ln)
+        if m:
+            summ.append({"kind": m.group(1), "quantity": m.group(2).lower(), "value": float(m.group(3)),
+                         "at": [float(m.group(k)) for k in (4, 5, 6)]})
+    res = _results_block(body)
+    return {"source": "testbank/testbank.ref_out (case 3)", "points": pts, "summaries": summ,
+            "approach": res["approach"], "pmax": res["pmax"], "fn": res["fn"],
+            "norm_itcg": int(re.search(r"ItCG=\s*(\d+)", body).group(1))}
+
+
 def parse_veldep_sequence(root):
     """All 53 cases of examples/veldep_fric.inp, to be replayed in order: the reader's cases
     and per printed case its iterations on the slip velocity (adhesion and slip counts, the
@@ -642,6 +670,8 @@ def main():
     vf = parse_veldep_fric(root)
     with open(os.path.join(HERE, "veldep_fric_case1.json"), "w") as f:
         json.dump(vf, f, indent=0)
+    with open(os.path.join(HERE, "testbank_case3_subs.json"), "w") as f:
+        json.dump(parse_testbank_case3(os.path.join(root, "testbank", "testbank.ref_out")), f, indent=0)
     t2 = parse_tractcurv_series2(root)
     with open(os.path.join(HERE, "tractcurv_series2.json"), "w") as f:
         json.dump(t2, f, separators=(",", ":"))

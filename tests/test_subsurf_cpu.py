@@ -198,3 +198,30 @@ def test_spence35_sequence(oracle):
                 assert np.allclose(np.round(pts[i], 3), s["at"][:2]), (gc["case"], s, pts[i])
                 nsum += 1
     assert nsum == 24
+
+
+def test_two_bodies_at_points(oracle):
+    """testbank/testbank.inp case 3: the normal problem of two bodies (G 200 above, 1 below) with
+    one element in contact, and the field at six points on both sides of the surface (z = -1 in
+    the soft body, 0.2 and 1 in the stiff one): the approach and pmax as printed, every printed
+    displacement, stress component, SigHyd and SigVM within half a unit of its last digit, and
+    the block's maxima at their printed positions."""
+    import pyoracle as po
+    g = json.load(open(os.path.join(GOLD, "testbank_case3_subs.json")))
+    o = C.oracle_solve(C.testbank_case(3))
+    assert o["ierror"] == 0 and o["itcg"] == g["norm_itcg"] and o["ncon"] == 1
+    assert abs(o["pen"] - g["approach"]) <= 0.5e-6 and abs(o["pmax"] - g["pmax"]) <= 0.5e-3
+    pts = np.array([[float(v) for v in r[:3]] for r in g["points"]])
+    f = po.subsurf_points((o["mx"], o["my"], o["dx"], o["dy"], o["xc1"], o["yc1"]), o["pn"], o["px"], o["py"],
+                          [200.0, 1.0], [0.28, 0.28], pts)
+    at = {n: k for k, n in enumerate(po.SUBS_COLS)}
+    at.update(sigxx=at["sxx"], sigyy=at["syy"], sigzz=at["szz"])
+    cols = ["ux", "uy", "uz", "sxx", "sxy", "sxz", "syx", "syy", "syz", "szx", "szy", "szz", "sighyd", "sigvm"]
+    for q, r in enumerate(g["points"]):
+        for c, name in enumerate(cols):
+            assert abs(f[q, at[name]] - float(r[3 + c])) <= _half_unit(r[3 + c]) * (1 + 1e-9), (r[:3], name)
+    for sm in g["summaries"]:
+        col = f[:, at[sm["quantity"]]]
+        i = int(np.argmax(np.abs(col)) if sm["kind"] == "ABSMAX" else np.argmax(col) if sm["kind"] == "MAX"
+                else np.argmin(col))
+        assert abs(col[i] - sm["value"]) <= 0.5e-3 * (1 + 1e-9) and np.allclose(pts[i], sm["at"]), sm
