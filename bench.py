@@ -34,6 +34,7 @@ for _p in (ROOT, os.path.join(ROOT, "tests")):
 
 import cases as C  # noqa: E402
 
+T_START = time.perf_counter()
 METRIC = "solves/s & p99 latency, mixed+batched vs plain FP64 on GB300 at 1e-8 rel err"
 UNIT = "solves/s"
 
@@ -48,8 +49,16 @@ def parse():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--plain-sample", type=int, default=608,
                     help="patches of the same workload solved in plain FP64 for the mixed/plain ratio")
-    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="wall-clock budget of the CPU baseline sample")
+    ap.add_argument("--depth", type=int, default=3,
+                    help="buffer sets of the resident batch: consecutive passes overlap over this many sets "
+                         "(continuous batching across steps); 1 runs the passes one after another")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-threads", type=int, default=0, help="host threads of the CPU legs (0: all)")
+    ap.add_argument("--cpu-max-side", type=int, default=0,
+                    help="test aid: draw the CPU sample from patches with both sides <= this (0: all sizes)")
+    ap.add_argument("--time-budget", type=float, default=1500.0,
+                    help="wall-clock seconds the default run must end within; timed passes that would not fit "
+                         "are not run (the line reports steps run and steps requested)")
     ap.add_argument("--max-side", type=int, default=0,
                     help="profiling aid: keep only patches with both sides <= this (0: all)")
     ap.add_argument("--serving", action="store_true",
@@ -79,18 +88,6 @@ def workload(n, seed, mixed=MIXED_TIER, max_side=0):
         return C.batch_patches(n, seed=seed, mixed=mixed, eps=1e-8)
     allc = C.batch_patches(4096, seed=seed, mixed=mixed, eps=1e-8)
     return [c for c in allc if c["potprm"][0] <= max_side and c["potprm"][1] <= max_side][:n]
-
-
-def fft_proxy(case):
-    """Cost proxy of one patch for scaling CPU samples: F log2 F with F the doubled FFT grid
-    (the cost of one convolution) times sqrt(mx my), for the growth of GDsteady's iteration
-    count with the grid's side.  Calibrated on patches with sides <= 64, it predicts the
-    oracle's mean time on the workload's first 64 patches within 10 % (F log2 F alone: a
-    factor 2.2 low)."""
-    from contact_gb300 import opt_fft_size as opt
-    mx, my = int(case["potprm"][0]), int(case["potprm"][1])
-    f = 4 * opt(mx) * opt(my)
-    return f * math.log2(f) * math.sqrt(mx * my)
 
 
 # ------------------------------------------------------------------------------------------
@@ -209,59 +206,49 @@ def measured_peaks():
 
 
 # ------------------------------------------------------------------------------------------
-# CPU baseline: the oracle on all host cores, bounded sample, scaled by the FFT cost proxy
+# CPU baseline: the oracle on all host cores, on a sample stratified over the workload's sizes
 # ------------------------------------------------------------------------------------------
-def cpu_sample_rate(cases, budget_s, seed, threads=None):
-    """Solve a seeded sample of the workload's patches with the CPU oracle (its baseline
-    build, with a Stockham FFT and real-input convolutions in place of the parity build's
-    simple recursive FFT) on a thread pool (ctypes releases the GIL).  Patches are drawn from those no larger than 64x64 so that a
-    sample ends within the budget; the measured time per unit of the FFT cost proxy is then
-    applied to the whole workload's proxy.  Returns (solves/s, threads, description)."""
+def stratified_sample(cases, nstrata, seed):
+    """One patch from each of nstrata equal-count strata of the workload ordered by element
+    count, drawn with the given seed: every stratum weighs 1/nstrata of the workload, so the
+    mean time over the sample estimates the workload's mean time per patch."""
+    rng = np.random.default_rng(seed)
+    order = sorted(range(len(cases)), key=lambda i: (cases[i]["potprm"][0] * cases[i]["potprm"][1], i))
+    edges = np.linspace(0, len(order), nstrata + 1).astype(int)
+    return [order[int(rng.integers(edges[k], edges[k + 1]))] for k in range(nstrata) if edges[k + 1] > edges[k]]
+
+
+def cpu_sample_rate(cases, seed, threads=None, nstrata=None):
+    """Solve a stratified sample of the workload (one patch per size stratum, sides 24-160
+    alike) with the CPU oracle's baseline build (Stockham FFT, real-input convolutions) on a
+    thread pool, one patch per thread at a time as the reference's OpenMP patch loop does
+    (ctypes releases the GIL).  Throughput = threads x patches / (sum of per-patch seconds):
+    the rate of a pool that stays busy on the whole workload, measured on patches of every
+    size with no extrapolation.  Returns (solves/s, threads, description, wall seconds)."""
     from concurrent.futures import ThreadPoolExecutor
     import pyoracle as po
     po.build()
     threads = threads or os.cpu_count() or 1
-    rng = np.random.default_rng(seed)
-    small = [i for i, c in enumerate(cases) if c["potprm"][0] <= 64 and c["potprm"][1] <= 64]
-    order = list(rng.permutation(small))
-    t_sum, p_sum, done = 0.0, 0.0, 0
-    t0 = time.perf_counter()
+    nstrata = nstrata or threads
+    idx = stratified_sample(cases, nstrata, seed)
 
     def one(i):
         c = dict(cases[i], mixed=0)
         ts = time.perf_counter()
         C.oracle_solve(c, fast=True)
-        return time.perf_counter() - ts, fft_proxy(c)
+        return time.perf_counter() - ts
 
+    t0 = time.perf_counter()
     with ThreadPoolExecutor(max_workers=threads) as ex:
-        pending = set()
-        it = iter(order)
-        while True:
-            while len(pending) < threads and time.perf_counter() - t0 < budget_s:
-                try:
-                    pending.add(ex.submit(one, next(it)))
-                except StopIteration:
-                    break
-            if not pending:
-                break
-            fin = [f for f in pending if f.done()]
-            if not fin:
-                time.sleep(0.01)
-                continue
-            for f in fin:
-                pending.discard(f)
-                dt, px = f.result()
-                t_sum += dt
-                p_sum += px
-                done += 1
+        times = list(ex.map(one, idx))
     wall = time.perf_counter() - t0
-    mean_proxy = float(np.mean([fft_proxy(c) for c in cases]))
-    sec_per_patch = t_sum / p_sum * mean_proxy          # one core, average patch of the workload
-    rate = threads / sec_per_patch
-    desc = ("%d patches (sides <= 64) of the workload solved by the oracle (its baseline build: Stockham FFT, real-input convolutions) "
-            "in %.1f s wall on %d threads; core-seconds per unit of F log2 F sqrt(mx my) (F = doubled FFT grid) "
-            "applied to the full workload's mix" % (done, wall, threads))
-    return rate, threads, desc
+    rate = threads * len(idx) / sum(times)
+    sides = sorted(int(cases[i]["potprm"][0]) * int(cases[i]["potprm"][1]) for i in idx)
+    desc = ("%d patches of the workload, one per equal-count stratum of element count (%d to %d elements, "
+            "sides 24-160: stratified over the full range, no extrapolation), solved by the oracle's baseline "
+            "build on %d threads in %.1f s wall; rate = threads x patches / sum of per-patch seconds"
+            % (len(idx), sides[0], sides[-1], threads, wall))
+    return rate, threads, desc, wall
 
 
 # ------------------------------------------------------------------------------------------
@@ -282,26 +269,39 @@ def run_gb300(args, dist):
     cases = workload(args.patches, args.seed, mixed=MIXED_TIER, max_side=args.max_side)
     n = len(cases)
     ire, icp = setup_problems(cg, cases)
-    rb = cg.ResidentBatch(ire, icp)
+    rb = cg.ResidentBatch(ire, icp, depth=args.depth)
     bad = int((rb.setup_errors != 0).sum())
     if bad:
         raise RuntimeError("%d patches could not be prepared" % bad)
-    launches0 = cg.kernel_launches()
-    rb.solve(args.warmup)
+    # warm-up passes, one at a time; the wall time of the last one sizes the rest of the run
+    t_pass = 0.0
+    for _ in range(args.warmup):
+        tw = time.perf_counter()
+        rb.solve(1)
+        t_pass = time.perf_counter() - tw
+    # wall-clock guard: the timed passes, the plain-FP64 sample (about 0.4 of a pass with its
+    # mixed twin), the end-to-end pass and the CPU leg must end within --time-budget seconds
+    # of the start; fewer timed passes are run (and reported) only if they would not
+    reserve = 1.6 * t_pass + 90.0
+    avail = args.time_budget - (time.perf_counter() - T_START) - reserve
+    steps = args.steps
+    if t_pass > 0 and avail < steps * t_pass:
+        steps = max(1, int(avail // t_pass))
+    steps = int(-dist.max(-steps))          # the smallest count over the ranks
     dist.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(dist.local)
     clocks.start()
     launches1 = cg.kernel_launches()
-    times = rb.solve(args.steps)
+    times = rb.solve(steps)
     gpu_launches = cg.kernel_launches() - launches1
     torch.cuda.synchronize()
     dist.barrier()
     clk = clocks.stop()
     t_total_ms = float(times[:, 0].sum())
     t_total_ms = dist.max(t_total_ms)
-    ms_per_step = t_total_ms / args.steps
-    value = dist.sum(n * args.steps) / (t_total_ms / 1e3)
+    ms_per_step = t_total_ms / steps
+    value = dist.sum(n * steps) / (t_total_ms / 1e3)
 
     # results and per-patch statistics of the last step
     err = rb.collect()
@@ -319,7 +319,7 @@ def run_gb300(args, dist):
         npot = int(c["potprm"][0]) * int(c["potprm"][1])
         itgd = r["itgs"] if r["solver"] == 7 else 0
         alg += s["conv_bytes"] + 8.0 * npot * (12 * r["itcg"] + 20 * itgd + 16 * s["nls"])
-    solve_ms = float(times[-1, 1])
+    solve_ms = ms_per_step
     sm_cycles = float(sum(s["t_total"] for s in stats))
     # where the patch-solve kernel's time goes: SM cycles per phase summed over the patches
     # (phases nest: convolutions inside NORM and TANG, FP32 convolutions inside convolutions,
@@ -378,14 +378,15 @@ def run_gb300(args, dist):
                          "max(|F_t|, 1e-3 mu Fn) of the mixed form against this FP64 form" % len(pc)}
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
-        rate, thr, desc = cpu_sample_rate(cases, args.cpu_seconds, args.seed)
+        rate, thr, desc, _ = cpu_sample_rate(cases, args.seed, threads=args.cpu_threads or None)
         cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port", "sample": desc}
     if dist.rank != 0:
         return None
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "steps_requested": args.steps,
         "config": {"workload": "batched mixed-size Hertzian steady rolling, %d patches, sides 24-160, "
                                "GDsteady, FP32 convolutions + FP64 refinement, eps 1e-8" % n,
                    "patches": n, "seed": args.seed, "parallelism": "replicas x%d" % dist.world,
@@ -418,26 +419,42 @@ def run_gb300(args, dist):
 # reference arm: the CPU oracle on the host cores
 # ------------------------------------------------------------------------------------------
 def run_reference(args, dist):
+    """The reference arm: the oracle (the CPU restatement of the reference's solve path; the
+    reference itself does not build here) on all host threads.  A warm-up step solves one small
+    patch per thread; each timed step solves one stratified sample of the workload (one patch
+    per size stratum, as many strata as threads)."""
     if dist.rank != 0:
         return None
+    import pyoracle as po
+    po.build()
     cases = workload(args.patches, args.seed, mixed=0)
-    budget = max(5.0, min(args.cpu_seconds, 30.0))
-    for w in range(args.warmup):
-        cpu_sample_rate(cases, 1.0, args.seed + 1000 + w)
-    rates = []
-    t0 = time.perf_counter()
+    if args.cpu_max_side > 0:
+        cases = [c for c in cases if max(c["potprm"][0], c["potprm"][1]) <= args.cpu_max_side]
+    threads = args.cpu_threads or os.cpu_count() or 1
+    small = [c for c in cases if c["potprm"][0] * c["potprm"][1] <= 48 * 48][:threads]
+    from concurrent.futures import ThreadPoolExecutor
+    for _ in range(args.warmup):
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(lambda c: C.oracle_solve(dict(c, mixed=0), fast=True), small))
+    tot_patch_s, tot_n, walls = 0.0, 0, []
+    desc = ""
     for s in range(args.steps):
-        r, thr, desc = cpu_sample_rate(cases, budget, args.seed + s)
-        rates.append(r)
-    wall = time.perf_counter() - t0
-    value = float(np.mean(rates))
+        r, thr, desc, wall = cpu_sample_rate(cases, args.seed + 7919 * s, threads=threads)
+        n = len(stratified_sample(cases, threads, args.seed + 7919 * s))
+        tot_patch_s += thr * n / r
+        tot_n += n
+        walls.append(wall)
+    value = threads * tot_n / tot_patch_s
+    desc = ("%d steps x %d patches, each step one stratified sample (one patch per equal-count stratum of element "
+            "count over the full 24-160 side range, no extrapolation) solved by the oracle's baseline build on %d "
+            "threads; rate = threads x patches / sum of per-patch seconds" % (args.steps, threads, threads))
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": wall * 1e3 / max(1, args.steps), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": float(np.mean(walls)) * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
         "config": {"workload": "batched mixed-size Hertzian steady rolling, %d patches, sides 24-160, "
                                "GDsteady, FP64, eps 1e-8" % len(cases), "patches": len(cases), "seed": args.seed},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": thr, "kind": "port", "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

@@ -115,7 +115,9 @@ _PROTOS = {
     "cntc_gb300_resident_solve": [_IP, _DP, _IP],
     "cntc_gb300_resident_collect": [_IP, _IP],
     "cntc_gb300_resident_release": [],
+    "cntc_gb300_resident_depth": [_IP],
     "cntc_gb300_lastcopybytes": [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
+    "cntc_gb300_fmapeaks": [_DP],
 }
 
 
@@ -132,7 +134,7 @@ def load(path=None):
     for name, args in _PROTOS.items():
         f = getattr(lib, name)
         f.argtypes = args
-        f.restype = ctypes.c_longlong if name == "cntc_gb300_kernel_launches" else None
+        f.restype = {"cntc_gb300_kernel_launches": ctypes.c_longlong, "cntc_gb300_fmapeaks": ctypes.c_int}.get(name)
     _lib = lib
     return lib
 
@@ -320,6 +322,21 @@ def getpenetration(ire, icp):
     return v.value
 
 
+def getcreepages(ire, icp):
+    """(cksi, ceta, cphi) of the problem; after a solve with prescribed total forces the
+    creepages that the Newton-Raphson found."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    load().cntc_getcreepages(_i(ire), _i(icp), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    return a.value, b.value, c.value
+
+
+def getsensitivities(ire, icp, lenout=4, lenin=4):
+    """sens[iout, iin]: outputs fn, fx, fy, mz; inputs pen, cksi, ceta, cphi (caller's units)."""
+    out = np.zeros(lenout * lenin)
+    load().cntc_getsensitivities(_i(ire), _i(icp), _i(lenout), _i(lenin), out.ctypes.data_as(_DP))
+    return out.reshape(lenin, lenout).T.copy()
+
+
 def getcontactpatchareas(ire, icp):
     v = [ctypes.c_double() for _ in range(3)]
     load().cntc_getcontactpatchareas(_i(ire), _i(icp), *[ctypes.byref(x) for x in v])
@@ -383,6 +400,16 @@ def lastcopybytes():
     return a.value, b.value
 
 
+def fma_peaks():
+    """Measured FMA peaks of the current device: {"fp64_tflops": .., "fp32_tflops": ..}."""
+    _require_gpu()
+    out = (ctypes.c_double * 2)()
+    rc = load().cntc_gb300_fmapeaks(out)
+    if rc != 0:
+        raise RuntimeError("FMA peak measurement failed")
+    return {"fp64_tflops": out[0], "fp32_tflops": out[1]}
+
+
 def opt_fft_size(n):
     """FFT length used for a grid side n (m_aijpj.f90:1022-1119): start from the next power of two
     and trade factors (4 -> 3, 32 -> 27, 6 -> 5, 16 -> 15, 27 -> 25, 8 -> 7, 15 -> 14, 10 -> 9)
@@ -406,10 +433,12 @@ def opt_fft_size(n):
 
 
 class ResidentBatch:
-    """Problems staged in device memory once and solved repeatedly (inputs resident in HBM)."""
+    """Problems staged in device memory once and solved repeatedly (inputs resident in HBM).
+    depth > 1 stages them in that many buffer sets so that consecutive passes overlap."""
 
-    def __init__(self, ire_list, icp_list):
+    def __init__(self, ire_list, icp_list, depth=1):
         _require_gpu()
+        load().cntc_gb300_resident_depth(_i(depth))
         self.n = len(ire_list)
         a, ap = _iarr(ire_list)
         b, bp = _iarr(icp_list)
@@ -455,16 +484,16 @@ def setup_case(ire, icp, case):
     h (element-wise undeformed distance, optional), prmudf (6 coefficients of a quadratic
     undeformed distance, ibase 1, optional), mixed (0-4), dq and chi (optional), group (CTAs
     per patch: 0 automatic, 1 one CTA, n >= 2 a cooperative group of at most n)."""
-    flags = [CNTC_ic_tang, CNTC_ic_bound, CNTC_ic_iestim, CNTC_if_mixedprec, CNTC_if_groupctas]
+    flags = [CNTC_ic_tang, CNTC_ic_bound, CNTC_ic_iestim, CNTC_if_mixedprec, CNTC_if_groupctas, CNTC_ic_pvtime,
+             CNTC_ic_force]
     values = [case.get("tang", 3), case.get("bound", 0), case.get("iestim", 0), case.get("mixed", 0),
-              case.get("group", 0)]
+              case.get("group", 0), case.get("pvtime", 2), case.get("force3", 0)]
     setflags(ire, icp, flags, values)
     setfrictionmethod(ire, icp, 0, [case.get("fstat", 0.3), case.get("fstat", 0.3)])
     nu = case.get("poiss", 0.28)
     g = case.get("gg", 82000.0)
     setmaterialparameters(ire, icp, 0, [nu, case.get("poiss2", nu), g, case.get("gg2", g)])
     if case.get("force3", 0) >= 1:
-        setflags(ire, icp, [CNTC_ic_force], [case["force3"]])
         settangentialforces(ire, icp, case.get("fxrel", 0.0), case.get("fyrel", 0.0))
     setreferencevelocity(ire, icp, case.get("veloc", 10000.0))
     gdig = case.get("gausei", 0)
@@ -475,6 +504,14 @@ def setup_case(ire, icp, case):
         setsolverflags(ire, icp, 5, ip + [gd["kdowfb"]],
                        [case.get("eps", 1e-6), gd["fdecay"], gd["betath"], gd["d_ifc"], gd["d_lin"], gd["d_cns"],
                         gd["d_slp"], gd["pow_s"]])
+    elif gdig in (2, 3):
+        # ConvexGS / SteadyGS with their relaxation: [maxgs, maxin, maxnr, maxout, inislp],
+        # [eps, omegah, omegas, omgslp]
+        setsolverflags(ire, icp, gdig, ip + [case.get("inislp", 0)],
+                       [case.get("eps", 1e-6), case.get("omegah", 0.9), case.get("omegas", 1.0),
+                        case.get("omgslp", 0.5)])
+    elif gdig == 4:
+        setsolverflags(ire, icp, gdig, ip + [case.get("inislp", 0)], [case.get("eps", 1e-6), case.get("omgslp", 0.5)])
     else:
         setsolverflags(ire, icp, gdig, ip, [case.get("eps", 1e-6)])
     if "dq" in case:

@@ -87,6 +87,7 @@ struct Problem {
     double r_dx = 0, r_dy = 0, r_xc1 = 0, r_yc1 = 0, r_dq = 1;
     double f_n = 0, f_x = 0, f_y = 0, m_z = 0, r_pen = 0, elen = 0, pmax = 0;
     int ncon = 0, nadh = 0, nslip = 0;
+    double sens_nr[4] = {0, 0, 0, 0};   // dFx/dcksi, dFy/dcksi, dFx/deta, dFy/deta (relative forces)
     std::vector<double> fields;   // W_H .. W_SN columns, npot each
     std::vector<int> igs;
     std::vector<double> stats;           // engine statistics: convolution counts, status, phase cycles
@@ -99,14 +100,30 @@ struct Problem {
     void *d_ic = nullptr;
     size_t cap_ic = 0;
     int ic_dev = -1;
+    // device copy of the last solution (px, py, pn, element division; prev_bytes layout): the
+    // initial estimate of the next solve (IESTIM) and its previous time instance (P = 0, 1)
+    // without a trip through host memory.  prev_key: grid of that solution.
+    double *d_prev = nullptr;
+    size_t cap_prev = 0;
+    int prev_dev = -1;
+    bool prev_valid = false;
+    char prev_key[160] = {0};
     std::mutex busy;
-    // frees the device cache (cntc_finalize, cntc_finalizelast; not at process exit, when
+    // frees the device caches (cntc_finalize, cntc_finalizelast; not at process exit, when
     // the CUDA runtime may already be gone and the driver reclaims the memory)
-    void release_device() {
-        if (d_ic) cudaFree(d_ic);
-        d_ic = nullptr; cap_ic = 0; ic_valid = false;
-    }
+    void release_device();
 };
+
+// bytes of device memory held by the problems' caches (coefficients and previous solutions),
+// counted against the serving admission budget
+std::atomic<long long> g_cache_bytes(0);
+
+void Problem::release_device() {
+    if (d_ic) { cudaFree(d_ic); g_cache_bytes -= (long long)cap_ic; }
+    d_ic = nullptr; cap_ic = 0; ic_valid = false;
+    if (d_prev) { cudaFree(d_prev); g_cache_bytes -= (long long)cap_prev; }
+    d_prev = nullptr; cap_prev = 0; prev_valid = false;
+}
 
 std::mutex g_mu;
 std::map<long, std::unique_ptr<Problem>> g_problems;
@@ -158,8 +175,8 @@ int prepare(Problem &p, Prep &out) {
     const double nu = ga * (p.poiss[0] / p.gg[0] + p.poiss[1] / p.gg[1]) / 2.0;
     const double ak = (ga / 4.0) * ((1.0 - 2.0 * p.poiss[0]) / p.gg[0] - (1.0 - 2.0 * p.poiss[1]) / p.gg[1]);
     if (std::fabs(ak) >= 1e-6) { log_msg("non-identical materials (K != 0) are not supported"); return CNTC_err_other; }
-    if (p.mater != 0 || p.frclaw != 0 || p.force3 != 0 || p.rztang != 0 || p.varfrc != 0) {
-        log_msg("only M=0, L=0, F=0, E=0 are supported");
+    if (p.mater != 0 || p.frclaw != 0 || p.rztang != 0 || p.varfrc != 0) {
+        log_msg("only M=0, L=0, E=0 are supported");
         return CNTC_err_other;
     }
     if (p.heat == 3) { log_msg("temperatures (H=3) are not computed by this library"); return CNTC_err_other; }
@@ -168,10 +185,6 @@ int prepare(Problem &p, Prep &out) {
         return CNTC_err_other;
     }
     if (!(p.bound == 0 || p.bound == 2 || p.bound == 3)) { log_msg("B digit not supported"); return CNTC_err_other; }
-    if (p.tang != 0 && p.tang != 3 && p.pvtime != 2) {
-        log_msg("transient sequences (P != 2 with T = 1, 2) are not supported");
-        return CNTC_err_other;
-    }
     // potential contact and Hertz (hzsol m_hertz.f90:29-93, potcon_hertz, potcon_fill)
     int ihertz = 0;
     double xl, yl, dx, dy;
@@ -245,12 +258,25 @@ int prepare(Problem &p, Prep &out) {
     }
     d.precision = p.mixed;
     d.eps32 = std::max(p.eps, p.eps32);
+    d.maxnr = p.maxnr;
+    d.pvtime = p.pvtime;
+    d.fxrel = p.fxrel; d.fyrel = p.fyrel;
+    for (int k = 0; k < 4; k++) d.sens0[k] = p.sens_nr[k];
     // geometry key for reuse of influence coefficients and spectra
     char key[128];
     std::snprintf(key, sizeof(key), "%d %d %.17g %.17g %.17g %.17g", mx, my, dx, dy, ga, nu);
     if (std::strcmp(key, p.key) != 0) p.ic_valid = false;    // the cache holds another geometry
     out.ic_needed = !p.ic_valid;
     std::strcpy(p.key, key);
+    // continuation from the previous time instance (P = 0) of shifts and transient rolling
+    // reads the previous tractions element by element: the grid must be the one of that solve
+    // (the reference also moves them with a potential contact that moves by whole elements;
+    // that form is not provided here)
+    if (p.pvtime == 0 && (p.tang == 1 || p.tang == 2) && p.have &&
+        !(p.r_mx == mx && p.r_my == my && p.r_dx == dx && p.r_dy == dy && p.r_xc1 == d.xc1 && p.r_yc1 == d.yc1)) {
+        log_msg("continuation from the previous time instance on a moved or changed grid is not supported");
+        return CNTC_err_other;
+    }
     // warm start needs a previous solution on the same grid
     out.upload = (d.ibase == 9);
     if (p.iestim != 0) {
@@ -262,10 +288,12 @@ int prepare(Problem &p, Prep &out) {
 }
 
 // fill the io staging block of one patch with its inputs
-void stage_inputs(Problem &p, const PatchDesc &d, double *io) {
+// warm: stage the initial estimate from the host copy of the last result (false when the
+// solve reads the problem's device copy instead)
+void stage_inputs(Problem &p, const PatchDesc &d, double *io, bool warm = true) {
     const int n = d.npot;
     if (d.ibase == 9) for (int i = 0; i < n; i++) io[(size_t)W_H * n + i] = p.prmudf[i] * 1.0;
-    if (d.iestim != 0 && p.have) {
+    if (warm && d.iestim != 0 && p.have) {
         int *igs = (int *)(io + (size_t)kIoCols * n + O_NSCAL);
         double *px = io + (size_t)W_PX * n, *py = io + (size_t)W_PY * n, *pn = io + (size_t)W_PN * n;
         for (int i = 0; i < n; i++) {
@@ -302,8 +330,15 @@ void collect(Problem &p, const PatchDesc &d, const double *io) {
     p.ierror = (int)o[O_IERR]; p.itnorm = (int)o[O_ITNORM]; p.ittang = (int)o[O_ITTANG];
     p.itcg = (int)o[O_ITCG]; p.itgs = (int)o[O_ITGS]; p.solver = (int)o[O_SOLVER];
     p.ncon = (int)o[O_NCON]; p.nadh = (int)o[O_NADH]; p.nslip = (int)o[O_NSLIP];
-    p.stats.assign(o + O_NCONV32, o + O_NSCAL);
+    p.stats.assign(o + O_NCONV32, o + O_TEND + 1);
     p.stats.push_back((double)d.nblk);
+    // total forces prescribed: the creepages found by the Newton-Raphson and its sensitivities
+    // (the reference keeps them in the problem's kinematics and output, m_solvpt.f90:51-378)
+    if (d.tang != 0 && d.force3 >= 1) {
+        p.cksi = o[O_CKSI];
+        if (d.force3 >= 2) p.ceta = o[O_CETA];
+    }
+    for (int k = 0; k < 4; k++) p.sens_nr[k] = o[O_SENS + k];
     p.have = true;
     // kinematic outputs follow the reference: fn from the solution when N = 0
     if (p.norm == 0) p.fn = p.f_n;
@@ -368,6 +403,7 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
     std::vector<PatchDesc> hd(n);
     std::vector<unsigned char> need_ic(n, 1);
     std::vector<int> ic_fill;     // patches whose coefficient cache this pass fills
+    std::vector<unsigned char> dev_prev(n, 0);   // patches that start from their device copy
     int dev = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
     for (int k = 0; k < n; k++) {
@@ -383,9 +419,11 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
             const bool hit = p.ic_valid && !b.preps[live[k]].ic_needed && p.d_ic && p.ic_dev == dev && p.cap_ic >= icb;
             if (!hit) {
                 p.ic_valid = false;
-                if (p.d_ic && (p.cap_ic < icb || p.ic_dev != dev)) { cudaFree(p.d_ic); p.d_ic = nullptr; p.cap_ic = 0; }
+                if (p.d_ic && (p.cap_ic < icb || p.ic_dev != dev)) {
+                    cudaFree(p.d_ic); g_cache_bytes -= (long long)p.cap_ic; p.d_ic = nullptr; p.cap_ic = 0;
+                }
                 if (!p.d_ic) {
-                    if (cudaMalloc(&p.d_ic, icb) == cudaSuccess) { p.cap_ic = icb; p.ic_dev = dev; }
+                    if (cudaMalloc(&p.d_ic, icb) == cudaSuccess) { p.cap_ic = icb; p.ic_dev = dev; g_cache_bytes += (long long)icb; }
                     else { cudaGetLastError(); p.d_ic = nullptr; }
                 }
                 if (p.d_ic) ic_fill.push_back(k);
@@ -398,9 +436,33 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
                 hd[k].spec64 = (const double *)(c + ps.cf);
                 hd[k].spec32 = (const float *)(c + ps.cf + ps.spec64);
             }
+            // the previous solution in device memory: read when the grid is unchanged and the
+            // solve asks for it (initial estimate or previous time instance), then overwritten
+            // by this solve's own solution
+            const size_t pb = prev_bytes(hd[k].npot);
+            char pkey[160];
+            std::snprintf(pkey, sizeof(pkey), "%d %d %.17g %.17g %.17g %.17g", hd[k].mx, hd[k].my, hd[k].dx, hd[k].dy,
+                          hd[k].xc1, hd[k].yc1);
+            const bool want = hd[k].iestim != 0 || (hd[k].pvtime <= 1 && (hd[k].tang == 1 || hd[k].tang == 2));
+            const bool prev_ok = p.prev_valid && p.d_prev && p.prev_dev == dev && std::strcmp(pkey, p.prev_key) == 0;
+            if (p.d_prev && (p.cap_prev < pb || p.prev_dev != dev)) {
+                cudaFree(p.d_prev); g_cache_bytes -= (long long)p.cap_prev;
+                p.d_prev = nullptr; p.cap_prev = 0; p.prev_valid = false;
+            }
+            if (!p.d_prev) {
+                if (cudaMalloc((void **)&p.d_prev, pb) == cudaSuccess) {
+                    p.cap_prev = pb; p.prev_dev = dev; g_cache_bytes += (long long)pb;
+                } else { cudaGetLastError(); p.d_prev = nullptr; }
+            }
+            if (want && prev_ok) {
+                hd[k].prev = p.d_prev;
+                dev_prev[k] = 1;
+            }
+            hd[k].save = p.d_prev;
+            if (p.d_prev) { std::strcpy(p.prev_key, pkey); p.prev_valid = false; }
         }
         if (b.preps[live[k]].upload)
-            stage_inputs(*b.probs[live[k]], hd[k], (double *)((char *)A.h_io + off_io[k]));
+            stage_inputs(*b.probs[live[k]], hd[k], (double *)((char *)A.h_io + off_io[k]), !dev_prev[k]);
     }
     cudaStream_t st = cudaStreamPerThread;
     t_h2d_bytes = (long long)(n * sizeof(PatchDesc));
@@ -416,6 +478,7 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
     t_d2h_bytes = (long long)tot_io;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return (int)e;
     for (int k : ic_fill) b.probs[live[k]]->ic_valid = true;
+    for (int k = 0; k < n; k++) if (hd[k].save) b.probs[live[k]]->prev_valid = true;
     for (int k = 0; k < n; k++) collect(*b.probs[live[k]], hd[k], (const double *)((const char *)A.h_io + off_io[k]));
     return 0;
 }
@@ -454,32 +517,56 @@ int calculate_many(int n, const int *ire, const int *icp, int *ierror) {
 // resident batch: a set of prepared problems staged in device memory once and solved again
 // and again on the same inputs (throughput with inputs already in HBM).  Each solve runs the
 // whole engine, influence coefficients included.
+//
+// Consecutive passes overlap (continuous batching across passes): the batch is staged in
+// `depth` buffer sets, each with its own caller stream and side-stream set, and pass r runs
+// in set r mod depth.  The SMs that the last patches of pass r leave idle take the CTAs of
+// passes r+1 .. r+depth-1; pass r+depth waits (stream order) until pass r has finished with
+// its buffers.  depth 1 is the plain sequence of passes.
 // ------------------------------------------------------------------------------------------
+struct ResSet {
+    char *d_io = nullptr, *d_work = nullptr;
+    PatchDesc *d_desc = nullptr;
+    int *d_list = nullptr;
+    std::vector<PatchDesc> hd;
+    cudaStream_t st = nullptr;
+    EngineTimer tm;
+    bool have_events = false;
+};
+
 struct Resident {
     Batch b;
     std::vector<int> live;
-    std::vector<PatchDesc> hd;
     std::vector<unsigned char> need_ic;
     std::vector<size_t> off_io;
     size_t tot_io = 0;
-    Arena A;
-    EngineTimer tm;
-    bool have_events = false;
+    double *h_io = nullptr;       // pinned staging
+    ResSet set[kMaxPassSets];
+    int depth = 1;
+    int last = 0;                 // set of the last pass
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     ~Resident() {
-        if (have_events) for (auto &e : tm.ev) cudaEventDestroy(e);
-        if (A.d_io) cudaFree(A.d_io);
-        if (A.d_work) cudaFree(A.d_work);
-        if (A.d_desc) cudaFree(A.d_desc);
-        if (A.d_list) cudaFree(A.d_list);
-        if (A.h_io) cudaFreeHost(A.h_io);
+        for (ResSet &r : set) {
+            if (r.have_events) for (auto &e : r.tm.ev) cudaEventDestroy(e);
+            if (r.d_io) cudaFree(r.d_io);
+            if (r.d_work) cudaFree(r.d_work);
+            if (r.d_desc) cudaFree(r.d_desc);
+            if (r.d_list) cudaFree(r.d_list);
+            if (r.st) cudaStreamDestroy(r.st);
+        }
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (h_io) cudaFreeHost(h_io);
     }
 };
 std::mutex g_res_mu;
 std::unique_ptr<Resident> g_res;
+int g_res_depth = 1;
 
 int resident_setup(int n, const int *ire, const int *icp, int *ierror) {
     g_res.reset();
     auto R = std::make_unique<Resident>();
+    R->depth = std::max(1, std::min(g_res_depth, kMaxPassSets));
     Batch &b = R->b;
     b.probs.resize(n); b.preps.resize(n); b.status.assign(n, 0);
     for (int i = 0; i < n; i++) {
@@ -499,67 +586,111 @@ int resident_setup(int n, const int *ire, const int *icp, int *ierror) {
         R->off_io[k] = R->tot_io; R->tot_io += s.io;
         off_work[k] = tot_work; tot_work += s.work;
     }
-    Arena &A = R->A;
     cudaError_t e;
-    if ((e = grow((void **)&A.d_io, A.cap_io, R->tot_io, false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.d_work, A.cap_work, tot_work, false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.d_desc, A.cap_desc, m * sizeof(PatchDesc), false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.d_list, A.cap_list, 3 * m * sizeof(int) + 64, false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.h_io, A.cap_hio, R->tot_io, true)) != cudaSuccess) return (int)e;
-    R->hd.resize(m);
+    if ((e = cudaMallocHost((void **)&R->h_io, std::max<size_t>(R->tot_io, 256))) != cudaSuccess) return (int)e;
     R->need_ic.assign(m, 1);
+    std::vector<PatchDesc> hd0(m);
     for (int k = 0; k < m; k++) {
-        R->hd[k] = b.preps[R->live[k]].d;
-        carve_patch(R->hd[k], A.d_io + R->off_io[k], A.d_work + off_work[k]);
-        stage_inputs(*b.probs[R->live[k]], R->hd[k], (double *)((char *)A.h_io + R->off_io[k]));
+        hd0[k] = b.preps[R->live[k]].d;
+        stage_inputs(*b.probs[R->live[k]], hd0[k], (double *)((char *)R->h_io + R->off_io[k]));
     }
-    cudaStream_t st = cudaStreamPerThread;
-    if ((e = cudaMemcpyAsync(A.d_io, A.h_io, R->tot_io, cudaMemcpyHostToDevice, st)) != cudaSuccess) return (int)e;
-    if ((e = cudaMemcpyAsync(A.d_desc, R->hd.data(), m * sizeof(PatchDesc), cudaMemcpyHostToDevice, st)) != cudaSuccess)
-        return (int)e;
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return (int)e;
-    for (auto &ev : R->tm.ev) if ((e = cudaEventCreate(&ev)) != cudaSuccess) return (int)e;
-    R->have_events = true;
+    for (int si = 0; si < R->depth; si++) {
+        ResSet &S = R->set[si];
+        if ((e = cudaMalloc((void **)&S.d_io, std::max<size_t>(R->tot_io, 256))) != cudaSuccess) return (int)e;
+        if ((e = cudaMalloc((void **)&S.d_work, std::max<size_t>(tot_work, 256))) != cudaSuccess) return (int)e;
+        if ((e = cudaMalloc((void **)&S.d_desc, std::max<size_t>(m * sizeof(PatchDesc), 256))) != cudaSuccess)
+            return (int)e;
+        if ((e = cudaMalloc((void **)&S.d_list, 3 * m * sizeof(int) + 64)) != cudaSuccess) return (int)e;
+        if ((e = cudaStreamCreateWithFlags(&S.st, cudaStreamNonBlocking)) != cudaSuccess) return (int)e;
+        S.hd = hd0;
+        for (int k = 0; k < m; k++) carve_patch(S.hd[k], S.d_io + R->off_io[k], S.d_work + off_work[k]);
+        if ((e = cudaMemcpyAsync(S.d_io, R->h_io, R->tot_io, cudaMemcpyHostToDevice, S.st)) != cudaSuccess)
+            return (int)e;
+        if ((e = cudaMemcpyAsync(S.d_desc, S.hd.data(), m * sizeof(PatchDesc), cudaMemcpyHostToDevice, S.st)) !=
+            cudaSuccess)
+            return (int)e;
+        if ((e = cudaStreamSynchronize(S.st)) != cudaSuccess) return (int)e;
+        for (auto &ev : S.tm.ev) if ((e = cudaEventCreate(&ev)) != cudaSuccess) return (int)e;
+        S.have_events = true;
+    }
+    if ((e = cudaEventCreate(&R->ev0)) != cudaSuccess) return (int)e;
+    if ((e = cudaEventCreate(&R->ev1)) != cudaSuccess) return (int)e;
     g_res = std::move(R);
     return 0;
 }
 
-// one solve of the resident batch; times[0] = device time of the whole pass (first to last
-// launch), times[1] = patch-solve kernels, times[2] = influence-coefficient and spectrum
-// kernels (ms, CUDA events on the launching stream), times[3] = number of launches
-int resident_solve(double *times) {
+// nrep solves of the resident batch, overlapped over the buffer sets.  Per solve r:
+// times[4r] = device time of the whole sequence / nrep (CUDA events on the first set's stream,
+// around all passes), times[4r+1] = span of pass r's patch-solve launches, times[4r+2] = span of
+// its influence-coefficient and spectrum kernels (ms, events on the pass's stream),
+// times[4r+3] = its number of launches
+int resident_solve(int nrep, double *times) {
     Resident *R = g_res.get();
-    if (!R || R->hd.empty()) return -1;
-    cudaStream_t st = cudaStreamPerThread;
-    int rc = engine_run(R->hd.data(), R->A.d_desc, (int)R->hd.size(), R->need_ic.data(), R->A.d_list, st, &R->tm);
-    if (rc != 0) return rc;
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return (int)e;
-    const EngineTimer &tm = R->tm;
-    float ms = 0.f;
-    times[0] = times[1] = times[2] = 0.0;
-    if (tm.nlaunch > 0) {
-        cudaEventElapsedTime(&ms, tm.ev[0], tm.ev[2 * tm.nlaunch - 1]);
-        times[0] = ms;
+    if (!R || R->live.empty()) return -1;
+    const int m = (int)R->live.size(), D = R->depth;
+    cudaError_t e;
+    cudaStream_t s0 = R->set[0].st;
+    if ((e = cudaEventRecord(R->ev0, s0)) != cudaSuccess) return (int)e;
+    for (int si = 1; si < D; si++)
+        if ((e = cudaStreamWaitEvent(R->set[si].st, R->ev0, 0)) != cudaSuccess) return (int)e;
+    std::vector<std::vector<double>> spans(nrep, std::vector<double>(3, 0.0));
+    auto read_spans = [&](int r, ResSet &S) {
+        const EngineTimer &tm = S.tm;
+        float ms = 0.f;
+        for (int k = 0; k < tm.nlaunch; k++) {
+            cudaEventElapsedTime(&ms, tm.ev[2 * k], tm.ev[2 * k + 1]);
+            spans[r][tm.kind[k] == 2 ? 0 : 1] += ms;
+        }
+        spans[r][2] = tm.nlaunch;
+    };
+    std::vector<int> pending(D, -1);     // the pass whose timing events a set still holds
+    for (int r = 0; r < nrep; r++) {
+        const int si = r % D;
+        ResSet &S = R->set[si];
+        if (pending[si] >= 0) {
+            // the set's previous pass must be done before its events are reused (engine_run also
+            // waits on the stream before it launches)
+            if ((e = cudaStreamSynchronize(S.st)) != cudaSuccess) return (int)e;
+            read_spans(pending[si], S);
+        }
+        int rc = engine_run(S.hd.data(), S.d_desc, m, R->need_ic.data(), S.d_list, S.st, &S.tm, si);
+        if (rc != 0) return rc;
+        pending[si] = r;
+        R->last = si;
     }
-    for (int k = 0; k < tm.nlaunch; k++) {
-        cudaEventElapsedTime(&ms, tm.ev[2 * k], tm.ev[2 * k + 1]);
-        times[tm.kind[k] == 2 ? 1 : 2] += ms;
+    for (int si = 1; si < D; si++) {
+        // each wait takes the record made just before it
+        if ((e = cudaEventRecord(R->ev1, R->set[si].st)) != cudaSuccess) return (int)e;
+        if ((e = cudaStreamWaitEvent(s0, R->ev1, 0)) != cudaSuccess) return (int)e;
     }
-    times[3] = tm.nlaunch;
+    if ((e = cudaEventRecord(R->ev1, s0)) != cudaSuccess) return (int)e;
+    if ((e = cudaEventSynchronize(R->ev1)) != cudaSuccess) return (int)e;
+    for (int si = 0; si < D; si++) {
+        if ((e = cudaStreamSynchronize(R->set[si].st)) != cudaSuccess) return (int)e;
+        if (pending[si] >= 0) read_spans(pending[si], R->set[si]);
+    }
+    float total = 0.f;
+    cudaEventElapsedTime(&total, R->ev0, R->ev1);
+    for (int r = 0; r < nrep; r++) {
+        times[4 * r] = total / nrep;
+        times[4 * r + 1] = spans[r][0];
+        times[4 * r + 2] = spans[r][1];
+        times[4 * r + 3] = spans[r][2];
+    }
     return 0;
 }
 
+// results of the last pass back to the problems
 int resident_collect(int *ierror) {
     Resident *R = g_res.get();
     if (!R) return -1;
-    cudaStream_t st = cudaStreamPerThread;
-    cudaError_t e = cudaMemcpyAsync(R->A.h_io, R->A.d_io, R->tot_io, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    ResSet &S = R->set[R->last];
+    cudaError_t e = cudaMemcpyAsync(R->h_io, S.d_io, R->tot_io, cudaMemcpyDeviceToHost, S.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S.st);
     if (e != cudaSuccess) return (int)e;
     for (size_t k = 0; k < R->live.size(); k++) {
         const int i = R->live[k];
-        collect(*R->b.probs[i], R->hd[k], (const double *)((const char *)R->A.h_io + R->off_io[k]));
+        collect(*R->b.probs[i], S.hd[k], (const double *)((const char *)R->h_io + R->off_io[k]));
         ierror[i] = R->b.probs[i]->ierror;
     }
     return 0;
@@ -605,6 +736,13 @@ int calculate_noalloc(int ire, int icp) {
     int st = prepare(*p, prep);
     if (st != 0) { p->have = false; return st; }
     PatchDesc hd = prep.d;
+    if (hd.pvtime == 0 && (hd.tang == 1 || hd.tang == 2) && p->have) {
+        // the previous time instance lives in the problem's device copy, which this entry
+        // point does not keep
+        log_msg("cntc_calculate_noalloc: continuation from the previous time instance (P = 0) is not supported");
+        p->have = false;
+        return CNTC_err_other;
+    }
     const PatchSizes s = patch_sizes(hd.mx, hd.my, hd.fx, hd.fy, hd.nblk);
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t off_list = up(sizeof(PatchDesc)), off_io = off_list + 256, off_work = off_io + up(s.io);
@@ -622,7 +760,7 @@ int calculate_noalloc(int ire, int icp) {
     cudaStream_t stream = cudaStreamPerThread;
     cudaError_t e = cudaMemcpyAsync(base + off_io, g_noalloc_host, s.io, cudaMemcpyHostToDevice, stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(base, &hd, sizeof(PatchDesc), cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) return CNTC_err_other;
+    if (e != cudaSuccess) { p->have = false; return CNTC_err_other; }
     const unsigned char need_ic = 1;
     int rc = engine_run(&hd, (PatchDesc *)base, 1, &need_ic, (int *)(base + off_list), stream);
     if (rc == 0) e = cudaMemcpyAsync(g_noalloc_host, base + off_io, s.io, cudaMemcpyDeviceToHost, stream);
@@ -669,13 +807,16 @@ struct Server {
             size_t bytes = 0;
             {
                 std::unique_lock<std::mutex> lk(mu);
-                cv_work.wait(lk, [&] { return stop || (!queue.empty() && in_flight + queue.front()->bytes <= budget) ||
+                // the problems' device caches (coefficients, previous solutions) count against
+                // the budget beside the passes in flight
+                auto held = [&] { return in_flight + (size_t)std::max(0LL, g_cache_bytes.load()); };
+                cv_work.wait(lk, [&] { return stop || (!queue.empty() && held() + queue.front()->bytes <= budget) ||
                                              (!queue.empty() && in_flight == 0); });
                 if (stop && queue.empty()) return;
                 while (!queue.empty()) {
                     const size_t b = queue.front()->bytes;
                     // a single request larger than the budget runs alone
-                    if (in_flight + bytes + b > budget && !(batch.empty() && in_flight == 0)) break;
+                    if (held() + bytes + b > budget && !(batch.empty() && in_flight == 0)) break;
                     bytes += b;
                     batch.push_back(queue.front());
                     queue.pop_front();
@@ -1238,9 +1379,23 @@ void cntc_getdisplacements(int *ire, int *icp, int *lenarr, double *un, double *
     f = CNTC_fld_un; cntc_getfielddata(ire, icp, &f, lenarr, un);
 }
 
+// sens(iout + (iin-1) lenout) for outputs fn, fx, fy, mz and inputs pen, cksi, ceta, cphi, in the
+// caller's units (cntc_getSensitivities 5919-6007).  The Newton-Raphson on prescribed total
+// forces leaves d(Fx, Fy)/d(cksi, ceta); the other entries are zero ("not computed").
 void cntc_getsensitivities(int *ire, int *icp, int *lenout, int *lenin, double *sens) {
-    (void)ire; (void)icp;
     for (int i = 0; i < (*lenout) * (*lenin); i++) sens[i] = 0.0;
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p) return;
+    // internal -> external: dFx/dcksi * fac_in(cksi) / fac_out(fx); fac_out = 1 for the relative
+    // forces; fac_in = s_len for shifts (T = 1), 1 for rolling
+    const double fin = (p->tang == 1) ? p->s_len : 1.0;
+    auto put = [&](int iout, int iin, double v) {
+        if (iout <= *lenout && iin <= *lenin) sens[(iout - 1) + (iin - 1) * (*lenout)] = v * fin;
+    };
+    put(2, 2, p->sens_nr[0]);
+    put(3, 2, p->sens_nr[1]);
+    put(2, 3, p->sens_nr[2]);
+    put(3, 3, p->sens_nr[3]);
 }
 
 void cntc_getcalculationtime(int *ire, int *icp, double *tcpu, double *twall) {
@@ -1399,10 +1554,17 @@ void cntc_gb300_resident_setup(int *n, int *ire, int *icp, int *ierror) {
 void cntc_gb300_resident_solve(int *nrep, double *times, int *ierror) {
     std::lock_guard<std::mutex> lk(g_res_mu);
     *ierror = 0;
-    for (int r = 0; r < *nrep; r++) {
-        int rc = resident_solve(times + 4 * r);
-        if (rc != 0) { *ierror = CNTC_err_other; return; }
+    if (*nrep <= 0) return;
+    int rc = resident_solve(*nrep, times);
+    if (rc != 0) {
+        *ierror = CNTC_err_other;
+        if (g_debug >= 1) std::fprintf(stderr, "contact_gb300: resident solve error %d\n", rc);
     }
+}
+
+void cntc_gb300_resident_depth(int *depth) {
+    std::lock_guard<std::mutex> lk(g_res_mu);
+    g_res_depth = std::max(1, std::min(*depth, kMaxPassSets));
 }
 
 void cntc_gb300_resident_collect(int *n, int *ierror) {

@@ -25,10 +25,48 @@ long long kernel_launch_count() { return g_launches.load(); }
 // ------------------------------------------------------------------------------------------
 // influence coefficients
 // ------------------------------------------------------------------------------------------
-__device__ inline void corner(int ix, int iy, double dx, double dy, double &x, double &y, double &r) {
-    x = (double)(float)ix * dx - 0.5 * dx;
-    y = (double)(float)iy * dy - 0.5 * dy;
+// corner (ix, iy) of the element grid, shifted by (xsh, ysh): the coordinates in the order of
+// operations of elascf_pcwcns (m_visc.f90:470-489), so that the coefficients are bitwise
+// those of a serial evaluation
+__device__ inline void corner(int ix, int iy, double dx, double dy, double xsh, double ysh, double &x, double &y,
+                              double &r) {
+    x = ((double)(float)ix * dx + xsh) - 0.5 * dx;
+    y = ((double)(float)iy * dy + ysh) - 0.5 * dy;
     r = sqrt(x * x + y * y);
+}
+
+// influence coefficients xx, xy (= yx), yy, zz of offset (ix, iy) for piecewise-constant
+// loading (elascf_pcwcns, m_visc.f90:431-604) on grids shifted by (xsh, ysh); zero for rows
+// below iy0 (single-row grids)
+__device__ inline void influence_at(int ix, int iy, int iy0, double dx, double dy, double nu, double xsh, double ysh,
+                                    double c[4]) {
+    const double pi = 3.14159265358979323846;
+    const double e1 = (1.0 - nu) / pi, e2 = 1.0 / pi, e3 = nu / pi;
+    const double tolx = dx * 1e-10;
+    double c11 = 0, c12 = 0, c22 = 0, c33 = 0;
+    if (iy >= iy0) {
+        double x00, y00, r00, x01, y01, r01, x10, y10, r10, x11, y11, r11;
+        corner(ix, iy, dx, dy, xsh, ysh, x00, y00, r00);
+        corner(ix, iy + 1, dx, dy, xsh, ysh, x01, y01, r01);
+        corner(ix + 1, iy, dx, dy, xsh, ysh, x10, y10, r10);
+        corner(ix + 1, iy + 1, dx, dy, xsh, ysh, x11, y11, r11);
+        c12 = 0.0 - e3 * r00;
+        c12 = c12 + e3 * r01;
+        c12 = c12 + e3 * r10;
+        c12 = c12 - e3 * r11;
+        double X0, X1, Y0, Y1;     // xly2y1(ix,iy), xly2y1(ix+1,iy), ylx2x1(ix,iy), ylx2x1(ix,iy+1)
+        X0 = (fmin(fabs(y00 + r00), fabs(y01 + r01)) < tolx) ? 0.0 : x00 * log((y01 + r01) / (y00 + r00));
+        X1 = (fmin(fabs(y10 + r10), fabs(y11 + r11)) < tolx) ? 0.0 : x10 * log((y11 + r11) / (y10 + r10));
+        Y0 = (fmin(fabs(x00 + r00), fabs(x10 + r10)) < tolx) ? 0.0 : y00 * log((x10 + r10) / (x00 + r00));
+        Y1 = (fmin(fabs(x01 + r01), fabs(x11 + r11)) < tolx) ? 0.0 : y01 * log((x11 + r11) / (x01 + r01));
+        c33 = 0.0 - e1 * (X0 + Y0);
+        c33 = c33 + e1 * (X1 + Y1);
+        c11 = 0.0 - (e1 * X0 + e2 * Y0);
+        c11 = c11 + (e1 * X1 + e2 * Y1);
+        c22 = 0.0 - (e1 * Y0 + e2 * X0);
+        c22 = c22 + (e1 * Y1 + e2 * X1);
+    }
+    c[0] = c11; c[1] = c12; c[2] = c22; c[3] = c33;
 }
 
 // grid: (blocks per patch, number of listed patches); list[] gives the patch indices
@@ -36,42 +74,57 @@ __global__ void __launch_bounds__(kThreads) k_influence(const PatchDesc *descs, 
     const PatchDesc &d = descs[list[blockIdx.y]];
     const int mx = d.mx, my = d.my;
     const int total = 4 * mx * my;
-    const double pi = 3.14159265358979323846;
-    const double e1 = (1.0 - d.nu) / pi, e2 = 1.0 / pi, e3 = d.nu / pi;
-    const double dx = d.dx, dy = d.dy, tolx = dx * 1e-10;
     const int iy0 = (my == 1) ? 0 : -my;
     double *cf = const_cast<double *>(d.cf);
     const size_t bsz = (size_t)total;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         const int ix = t % (2 * mx) - mx, iy = t / (2 * mx) - my;
-        double c11 = 0, c12 = 0, c22 = 0, c33 = 0;
-        if (iy >= iy0) {
-            double x00, y00, r00, x01, y01, r01, x10, y10, r10, x11, y11, r11;
-            corner(ix, iy, dx, dy, x00, y00, r00);
-            corner(ix, iy + 1, dx, dy, x01, y01, r01);
-            corner(ix + 1, iy, dx, dy, x10, y10, r10);
-            corner(ix + 1, iy + 1, dx, dy, x11, y11, r11);
-            c12 = 0.0 - e3 * r00;
-            c12 = c12 + e3 * r01;
-            c12 = c12 + e3 * r10;
-            c12 = c12 - e3 * r11;
-            double X0, X1, Y0, Y1;     // xly2y1(ix,iy), xly2y1(ix+1,iy), ylx2x1(ix,iy), ylx2x1(ix,iy+1)
-            X0 = (fmin(fabs(y00 + r00), fabs(y01 + r01)) < tolx) ? 0.0 : x00 * log((y01 + r01) / (y00 + r00));
-            X1 = (fmin(fabs(y10 + r10), fabs(y11 + r11)) < tolx) ? 0.0 : x10 * log((y11 + r11) / (y10 + r10));
-            Y0 = (fmin(fabs(x00 + r00), fabs(x10 + r10)) < tolx) ? 0.0 : y00 * log((x10 + r10) / (x00 + r00));
-            Y1 = (fmin(fabs(x01 + r01), fabs(x11 + r11)) < tolx) ? 0.0 : y01 * log((x11 + r11) / (x01 + r01));
-            c33 = 0.0 - e1 * (X0 + Y0);
-            c33 = c33 + e1 * (X1 + Y1);
-            c11 = 0.0 - (e1 * X0 + e2 * Y0);
-            c11 = c11 + (e1 * X1 + e2 * Y1);
-            c22 = 0.0 - (e1 * Y0 + e2 * X0);
-            c22 = c22 + (e1 * Y1 + e2 * X1);
-        }
-        cf[0 * bsz + t] = c11;
-        cf[1 * bsz + t] = c12;
-        cf[2 * bsz + t] = c22;
-        cf[3 * bsz + t] = c33;
+        double c[4];
+        influence_at(ix, iy, iy0, d.dx, d.dy, d.nu, 0.0, 0.0, c);
+        cf[0 * bsz + t] = c[0];
+        cf[1 * bsz + t] = c[1];
+        cf[2 * bsz + t] = c[2];
+        cf[3 * bsz + t] = c[3];
     }
+}
+
+// steady-rolling coefficients of ConvexGS: csv = cs - cv for blocks xx, xy, yy, where cv are
+// the coefficients of the grid shifted by one rolling step (dq cos chi, dq sin chi)
+// (m_visc.f90:289-354); written in the layout of cf to csv[3][2my][2mx]
+__device__ __noinline__ void steady_coefs(const PatchDesc &d, double *csv) {
+    const int mx = d.mx, my = d.my;
+    const int total = 4 * mx * my;
+    const int iy0 = (my == 1) ? 0 : -my;
+    const double xsh = cos(d.chi) * d.dq, ysh = sin(d.chi) * d.dq;
+    for (int t = gtid(); t < total; t += gstride()) {
+        const int ix = t % (2 * mx) - mx, iy = t / (2 * mx) - my;
+        double c[4];
+        influence_at(ix, iy, iy0, d.dx, d.dy, d.nu, xsh, ysh, c);
+        csv[0 * (size_t)total + t] = d.cf[0 * (size_t)total + t] - c[0];
+        csv[1 * (size_t)total + t] = d.cf[1 * (size_t)total + t] - c[1];
+        csv[2 * (size_t)total + t] = d.cf[2 * (size_t)total + t] - c[2];
+    }
+    gsync();
+}
+
+// coefficients of transient rolling cv: the grid shifted by one rolling step, formed as
+// cs - (cs - shifted) like the reference's cv (m_visc.f90:289-354), blocks xx, xy, yy in the
+// layout of cf
+__device__ __noinline__ void transient_coefs(const PatchDesc &d, double *cv) {
+    const int mx = d.mx, my = d.my;
+    const int total = 4 * mx * my;
+    const int iy0 = (my == 1) ? 0 : -my;
+    const double xsh = cos(d.chi) * d.dq, ysh = sin(d.chi) * d.dq;
+    for (int t = gtid(); t < total; t += gstride()) {
+        const int ix = t % (2 * mx) - mx, iy = t / (2 * mx) - my;
+        double c[4];
+        influence_at(ix, iy, iy0, d.dx, d.dy, d.nu, xsh, ysh, c);
+        for (int k = 0; k < 3; k++) {
+            const double cs = d.cf[k * (size_t)total + t];
+            cv[k * (size_t)total + t] = cs - (cs - c[k]);
+        }
+    }
+    gsync();
 }
 
 // ------------------------------------------------------------------------------------------
@@ -82,9 +135,19 @@ struct SmemPlan {
     size_t off_tw64x, off_tw64y, off_tw32x, off_tw32y, off_wbuf, total;
 };
 
-// single CTA (blk false): twiddle tables and one buffer region of 4 * max(NX, NY) complex
-// per warp in shared memory.  Patch group (blk true): one buffer region per CTA, the twiddle
-// tables live in the group scratch in global memory.
+// Shared memory of a patch CTA: the convolution's batch buffer (cbuf) and, for a single CTA,
+// the twiddle tables of the convolution size in FP64 and FP32 (a patch group keeps them in its
+// scratch in global memory).  The batch buffer holds at least one ping-pong pair of the
+// longest line for both components of a tangential product (64 (nmax + 1) bytes in FP64), and
+// kConvBufBytes otherwise, so that two CTAs of the largest single-CTA grids share an SM.  The
+// kernel-spectra set-up uses the same buffer for one CTA-wide line (4 nmax complex FP64).
+constexpr size_t kConvBufBytes = 80 * 1024;
+
+__host__ __device__ inline size_t conv_buf_bytes(int nmax) {
+    const size_t need = (size_t)64 * (nmax + 1);
+    return need > kConvBufBytes ? need : kConvBufBytes;
+}
+
 __host__ __device__ inline SmemPlan smem_plan(int fx, int fy, bool blk = false) {
     SmemPlan s;
     s.NX = 2 * fx; s.NY = 2 * fy; s.nmax = s.NX > s.NY ? s.NX : s.NY;
@@ -92,7 +155,7 @@ __host__ __device__ inline SmemPlan smem_plan(int fx, int fy, bool blk = false) 
     if (blk) {
         s.off_tw64x = s.off_tw64y = s.off_tw32x = s.off_tw32y = 0;
         s.off_wbuf = 0;
-        s.total = (size_t)4 * s.nmax * 16;
+        s.total = conv_buf_bytes(s.nmax);
         return s;
     }
     s.off_tw64x = o; o += (size_t)s.NX * 16;
@@ -100,7 +163,7 @@ __host__ __device__ inline SmemPlan smem_plan(int fx, int fy, bool blk = false) 
     s.off_tw32x = o; o += (size_t)s.NX * 8;
     s.off_tw32y = o; o += (size_t)s.NY * 8;
     o = (o + 15) & ~(size_t)15;
-    s.off_wbuf = o; o += (size_t)kWarps * 4 * s.nmax * 16;
+    s.off_wbuf = o; o += conv_buf_bytes(s.nmax);
     s.total = o;
     return s;
 }
@@ -147,6 +210,8 @@ __device__ inline Conv<T> make_conv(const PatchDesc &d, unsigned char *smraw, co
     }
     cv.wbuf = (C<T> *)(smraw + sp.off_wbuf);
     cv.wstride = 4 * sp.nmax;
+    cv.cbuf = (C<T> *)(smraw + sp.off_wbuf);
+    cv.ccap = (int)(conv_buf_bytes(sp.nmax) / sizeof(C<T>));
     C<T> *R = (C<T> *)d.rbuf;
     cv.R0 = R;
     cv.R1 = R + (size_t)cv.nkx * cv.my;
@@ -278,6 +343,9 @@ __global__ void __launch_bounds__(kThreads) k_spectra(const PatchDesc *descs, co
     group_init(blk ? d.nblk : 1, blk ? (int)blockIdx.x : 0, d.gscr);
     const SmemPlan sp = smem_plan(d.fx, d.fy, blk);
     Conv<double> cv = make_conv<double>(d, smraw, sp);
+    // one line at a time per CTA (all its threads on the line): the batch buffer holds one
+    // CTA-wide line region of 4 nmax complex
+    cv.L = line_workers(true);
     const int mx = d.mx, my = d.my;
     const size_t bsz = (size_t)4 * mx * my;
     const size_t ksz = (size_t)cv.nkx * (d.fy + 1);
@@ -342,6 +410,28 @@ __device__ __noinline__ void setup_patch(const PView &P) {
     const double facphi = 1.0 / 6.0;
     const double xofs = is_roll ? cos(d.chi) * d.dq * facphi : 0.0;
     const double yofs = is_roll ? sin(d.chi) * d.dq * facphi : 0.0;
+    // initial estimate from the problem's previous solution kept in device memory, regularised
+    // as init_curr_data does (m_sdis.f90:716-729): I = 1 zeroes exterior tractions and puts slip
+    // tractions on the bound, I = 2 keeps the contact area only
+    if (d.prev && d.iestim != 0) {
+        const double *qx = d.prev, *qy = d.prev + n, *qn = d.prev + 2 * (size_t)n;
+        const int *qg = (const int *)(d.prev + 3 * (size_t)n);
+        FOR_I(ii, n) {
+            int g = qg[ii];
+            double ax = qx[ii], ay = qy[ii], an = qn[ii];
+            if (d.iestim == 1) {
+                if (g <= Exter) { an = ax = ay = 0.0; }
+                else if (g == Slip) {
+                    const double pabs = fmax(1e-10, sqrt(ax * ax + ay * ay));
+                    ax = d.fstat * an * ax / pabs;
+                    ay = d.fstat * an * ay / pabs;
+                }
+            }
+            if (d.iestim == 2) { if (g >= Adhes) g = Adhes; ax = ay = 0.0; }
+            igs[ii] = g; px[ii] = ax; py[ii] = ay; pn[ii] = an;
+        }
+        gsync();
+    }
     FOR_I(ii, n) {
         const double x = d.xc1 + (ii % mx) * d.dx, y = d.yc1 + (ii / mx) * d.dy;
         if (d.ibase != 9) h[ii] = d.prm[0] * x * x + d.prm[1] * x * y + d.prm[2] * y * y + d.prm[3] * x + d.prm[4] * y + d.prm[5];
@@ -407,8 +497,11 @@ __device__ __noinline__ void setup_patch(const PView &P) {
     gsync();
 }
 
-// leading-edge fraction facdt (sxbnd, m_leadedge.f90:92-332) for rolling direction chi = 0
-__device__ __noinline__ void compute_facdt(const PView &P, int solver, double *facdt) {
+// leading-edge fraction facdt (sxbnd, m_leadedge.f90:92-332) for rolling direction chi = 0.
+// edge (optional, ConvexGS in steady rolling): per element the 1-based column of its leading
+// edge where the element lies within one rolling step of it (facdt < 0.9999, the reference's
+// ii2j > 0), else 0
+__device__ __noinline__ void compute_facdt(const PView &P, int solver, double *facdt, int *edge = nullptr) {
     const PatchDesc &d = *P.d;
     const int mx = P.mx, my = P.my;
     const int *igs = P.igs();
@@ -421,6 +514,7 @@ __device__ __noinline__ void compute_facdt(const PView &P, int solver, double *f
         for (int ix = mx; ix >= 1; ix--) {
             const int ii = (ix - 1) + i0;
             if ((igs[ii] >= Adhes) && (ix == mx || igs[ii + 1] <= Exter)) ixb = ix;
+            int je = 0;
             if (!is_roll) facdt[ii] = 1.0;
             else if (igs[ii] <= Exter) facdt[ii] = 0.0;
             else if (ix + 2 > mx) facdt[ii] = 1.0;
@@ -428,7 +522,9 @@ __device__ __noinline__ void compute_facdt(const PView &P, int solver, double *f
                 const double xbnd = d.xc1 + (ixb - 1) * d.dx + fxdfac * d.dx;
                 const double x = d.xc1 + (ix - 1) * d.dx;
                 facdt[ii] = fmin(1.0, (xbnd - x) / d.dq);
+                if (facdt[ii] < 0.9999) je = ixb;
             }
+            if (edge) edge[ii] = je;
         }
     }
     gsync();
@@ -436,19 +532,164 @@ __device__ __noinline__ void compute_facdt(const PView &P, int solver, double *f
 
 constexpr int kMaxGroupGsElements = 40000;
 
-// TANG, m_stang.f90:28-746 for Coulomb friction and prescribed creepages.
-// Returns ittang; -1000 when the reference would pick ConvexGS, -2000 on a failed line search.
-// With o32 (mixed precision): GDsteady runs once with FP32 direction products and FP64
-// residual replacement; TangCG runs an FP32 pass to eps32 followed by an FP64 pass.
-__device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const Ops<float> *o32, double eps,
-                                  double eps32, int &itgs_out, int &solver_out, int &nconv, int &nconv32, int &nls) {
+// state of TANG shared by the solver dispatch and the Newton-Raphson on total forces
+struct TangRun {
+    int solver;
+    double omegah, omegas, eps, eps32;
+    const Ops<double> *op;
+    const Ops<float> *o32;
+    const double *csv;            // ConvexGS in steady rolling: csv = cs - cv
+    const int *edge;              // ConvexGS: leading-edge column per element
+    bool any_edge, gs_ok;
+    int nconv, nconv32, nls;
+    double fntrue;                // total normal force of the solution
+    double cksi, ceta;            // creepages (updated when total forces are prescribed)
+    double sens[4];               // dFx/dcksi, dFy/dcksi, dFx/deta, dFy/deta (relative forces)
+};
+
+// tang_solver, m_solvpt.f90:382-493: one solve of the tangential problem for the current element
+// division and shift ws (W_WSX, W_WSY).  Returns the iterations; -1000 for a Gauss-Seidel solver
+// on a patch group too large for it, -2000 on a failed line search.
+__device__ __noinline__ int tang_solver(const PView &P, TangRun &T, int &info, double &errpt) {
+    const PatchDesc &d = *P.d;
+    int it = 0;
+    info = 0;
+    errpt = 0.0;
+    if (T.solver == 4) {
+        it = stdygs(P, T.eps, d.maxgs, T.omegah, T.omegas, info, errpt, T.o32 ? T.op : nullptr);
+    } else if (T.solver == 3) {
+        it = cnvxgs(P, *T.op, T.csv, T.edge, T.any_edge, T.eps, d.maxgs, T.omegah, T.omegas, info, errpt);
+    } else if (T.solver == 7) {
+        bool lstagn = false;
+        it = gdsteady<double>(P, *T.op, d.maxgs, T.eps, errpt, lstagn, T.nconv, T.nls, T.o32, T.nconv32);
+        if (it == -100000) return -2000;
+        if (lstagn && !T.gs_ok) return -1000;
+        if (lstagn) it = stdygs(P, T.eps, d.maxgs, T.omegah, T.omegas, info, errpt, T.o32 ? T.op : nullptr);
+    } else {
+        int it32 = 0;
+        if (T.o32) {
+            it32 = tangcg<float>(P, *T.o32, T.o32->K[5], T.o32->K[6], d.maxgs, T.eps32, errpt, T.nconv32);
+            it32 = it32 > 0 ? it32 : 0;
+        }
+        it = tangcg<double>(P, *T.op, T.op->K[5], T.op->K[6], d.maxgs, T.eps, errpt, T.nconv) + it32;
+    }
+    return it;
+}
+
+// total tangential forces relative to mu Fn
+__device__ inline void rel_forces(const PView &P, const TangRun &T, double &fx, double &fy) {
+    const PatchDesc &d = *P.d;
+    const double *px = P.c(W_PX), *py = P.c(W_PY);
+    double a[2] = {0.0, 0.0};
+    FOR_I(i, P.n) { a[0] += px[i]; a[1] += py[i]; }
+    block_sum<2>(P.sm->red, a);
+    fx = d.dxdy * a[0] / (d.fstat * T.fntrue);
+    fy = d.dxdy * a[1] / (d.fstat * T.fntrue);
+}
+
+// solvpt, m_solvpt.f90:51-378: the tangential solve with shift wstot = wsfix + facdt dq (cksi,
+// ceta) for the prescribed components; with total forces prescribed (F=1: Fx, F=2: Fx and Fy) a
+// Newton-Raphson iteration on cksi (and ceta) around it, its derivatives the secants of its own
+// steps.  Returns the solver iterations summed over the Newton-Raphson steps (negative codes as
+// tang_solver); errpt includes the Newton-Raphson residual as the reference adds it.
+__device__ __noinline__ int solvpt(const PView &P, TangRun &T, int &info, double &errpt) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n, f3 = d.force3;
+    const int *iel = P.ci(I_IEL);
+    const double *facdt = P.c(W_FACDT), *wfx = P.c(W_WFX), *wfy = P.c(W_WFY);
+    double *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+    const double dq = d.dq;
+    FOR_I(i, n) {
+        wsx[i] = wfx[i];
+        wsy[i] = wfy[i];
+        if (iel[i] && f3 >= 1) wsx[i] += facdt[i] * T.cksi * dq;
+        if (iel[i] && f3 >= 2) wsy[i] += facdt[i] * T.ceta * dq;
+    }
+    gsync();
+    int it = tang_solver(P, T, info, errpt);
+    if (it < 0 || f3 == 0) return it;
+    int itgs = it;
+    double fxkp1, fykp1;
+    rel_forces(P, T, fxkp1, fykp1);
+    double *sens = T.sens;     // [0] dFx/dcksi, [1] dFy/dcksi, [2] dFx/deta, [3] dFy/deta
+    if (info <= 1) {
+        int itnr = 0;
+        double df = fabs(d.fxrel - fxkp1);
+        if (f3 >= 2) df += fabs(d.fyrel - fykp1);
+        int nadh = 0, nslip = 0, nplast = 0, nexter = 0;
+        count_eldiv(P, nadh, nslip, nplast, nexter);
+        while (df > T.eps && itnr < d.maxnr && info <= 1) {
+            itnr++;
+            const double dfx = d.fxrel - fxkp1, dfy = d.fyrel - fykp1;
+            double dcksi = 0.0, dceta = 0.0;
+            if (f3 == 1) {
+                if (fabs(sens[0]) > (double)1e-6f) dcksi = dfx / sens[0];
+                else dcksi = (double)0.00003f;
+            } else {
+                const double det = sens[0] * sens[3] - sens[1] * sens[2];
+                if (det > T.eps) {
+                    dcksi = (sens[3] * dfx - sens[1] * dfy) / det;
+                    dceta = (-sens[2] * dfx + sens[0] * dfy) / det;
+                } else {
+                    dcksi = 0.000003;
+                    dceta = 0.000003;
+                }
+            }
+            for (int ifxy = 1; ifxy <= f3; ifxy++) {
+                const double fxk = fxkp1, fyk = fykp1;
+                const double dc = ifxy == 1 ? dcksi : dceta;
+                if (ifxy == 1) T.cksi += dcksi; else T.ceta += dceta;
+                double *w = ifxy == 1 ? wsx : wsy;
+                FOR_I(i, n) if (iel[i]) w[i] += facdt[i] * dc * dq;
+                gsync();
+                it = tang_solver(P, T, info, errpt);
+                if (it < 0) return it;
+                itgs += it;
+                rel_forces(P, T, fxkp1, fykp1);
+                count_eldiv(P, nadh, nslip, nplast, nexter);
+                const double dfxk = fxkp1 - fxk, dfyk = fykp1 - fyk;
+                const double scl = d.fstat * T.fntrue / ((nadh + nslip + nplast) * d.dxdy);
+                if (ifxy == 1) {
+                    if (nadh > 0) {
+                        if (sens[0] == 0.0 || fabs(dfxk * scl) > 10.0 * errpt) sens[0] = dfxk / dcksi;
+                        if (fabs(dfyk * scl) > 10.0 * errpt) sens[1] = dfyk / dcksi;
+                    } else if (fabs(sens[0]) < (double)1e-6f) {
+                        sens[0] = fxkp1 / T.cksi;
+                    }
+                } else {
+                    if (nadh > 0) {
+                        if (fabs(dfxk * scl) > 10.0 * errpt) sens[2] = dfxk / dceta;
+                        if (sens[3] == 0.0 || fabs(dfyk * scl) > 10.0 * errpt) sens[3] = dfyk / dceta;
+                    } else if (fabs(sens[3]) < (double)1e-6f) {
+                        sens[3] = fykp1 / T.ceta;
+                    }
+                }
+                df = fabs(d.fxrel - fxkp1);
+                if (f3 >= 2) df += fabs(d.fyrel - fykp1);
+            }
+        }
+        // the Newton-Raphson residual joins the error estimate, with the element code Slip (= 2)
+        // in the place of the number of slip elements as in the reference (m_solvpt.f90:361)
+        errpt += 2.0 * df * d.fstat * T.fntrue / ((nadh + Slip + nplast) * d.dxdy);
+    } else {
+        sens[0] = sens[1] = sens[2] = sens[3] = 0.0;
+    }
+    return itgs;
+}
+
+// TANG, m_stang.f90:28-746 for Coulomb friction, creepages or total forces prescribed.
+// Returns ittang; -1000 for a Gauss-Seidel solver on a patch group too large for it, -2000 on
+// a failed line search.  With T.o32 (mixed precision): GDsteady runs once with FP32 direction
+// products and FP64 residual replacement; SteadyGS takes FP32 sums of its in-sweep changes on
+// an FP64 base; TangCG runs an FP32 pass to eps32 followed by an FP64 pass.
+__device__ __noinline__ int stang(const PView &P, TangRun &T, int &itgs_out) {
     const PatchDesc &d = *P.d;
     const int mx = P.mx, my = P.my, n = P.n;
     RedSmem &red = P.sm->red;
     int *igs = P.igs(), *iel = P.ci(I_IEL);
     const bool is_ssrol = d.tang == 3;
     double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN), *sx = P.c(W_SX), *sy = P.c(W_SY);
-    double *wsx = P.c(W_WSX), *wsy = P.c(W_WSY), *wx = P.c(W_WX), *wy = P.c(W_WY);
+    double *wfx = P.c(W_WFX), *wfy = P.c(W_WFY), *wx = P.c(W_WX), *wy = P.c(W_WY);
     int nadh, nslip, nplast, nexter;
     count_eldiv(P, nadh, nslip, nplast, nexter);
     const int k = nadh + nslip + nplast;
@@ -469,45 +710,95 @@ __device__ __noinline__ int stang(const PView &P, const Ops<double> &op, const O
             else { omegah = 0.8; omegas = 0.6; }
         } else { omegah = 0.5; omegas = 0.5; }
     }
-    solver_out = solver;
-    if (solver == 3) return -1000;
-    // SteadyGS visits the elements one after another, with two group barriers per element in a
-    // patch group: beyond kMaxGroupGsElements a sweep would take seconds, so large groups
-    // refuse it (as the primary solver, and as GDsteady's fallback below)
-    const bool gs_ok = !grouped() || n <= kMaxGroupGsElements;
-    if (solver == 4 && !gs_ok) return -1000;
+    T.solver = solver;
+    T.omegah = omegah;
+    T.omegas = omegas;
+    // SteadyGS and ConvexGS visit the elements one after another, with two group barriers per
+    // element in a patch group: beyond kMaxGroupGsElements a sweep would take seconds, so large
+    // groups refuse them (as the primary solver, and as GDsteady's fallback)
+    T.gs_ok = !grouped() || n <= kMaxGroupGsElements;
+    if ((solver == 4 || solver == 3) && !T.gs_ok) return -1000;
     // fixed part of the shift: wsfix = -facdt * hs with hs = -dq w (stang_rhs, K = 0)
-    double *facdt = P.c(W_DSCL);
-    compute_facdt(P, solver, facdt);
+    double *facdt = P.c(W_FACDT);
+    int *edge = P.ci(I_JX);
+    const bool cnvx_ss = solver == 3 && is_ssrol;
+    const bool trans_prev = d.pvtime == 0 && d.prev && d.tang == 2;
+    compute_facdt(P, solver, facdt, (cnvx_ss || trans_prev) ? edge : nullptr);
+    // ConvexGS in steady rolling: csv in the columns of the FP32 work arrays W_FLS .. W_FLS + 11
+    // (three blocks of 4 mx my doubles; ConvexGS uses none of those arrays), and whether any
+    // element takes a leading-edge estimate
+    T.csv = nullptr;
+    T.edge = edge;
+    T.any_edge = false;
+    if (cnvx_ss) {
+        double *csv = P.c(W_FLS);
+        steady_coefs(d, csv);
+        T.csv = csv;
+        int c = 0;
+        FOR_I(i, n) if (edge[i] > 0) c++;
+        T.any_edge = block_sumi1(red, c) > 0;
+    }
     FOR_I(i, n) {
         iel[i] = igs[i] >= Adhes ? 1 : 0;
-        wsx[i] = iel[i] ? -facdt[i] * wx[i] : 0.0;
-        wsy[i] = iel[i] ? -facdt[i] * wy[i] : 0.0;
+        wfx[i] = iel[i] ? -facdt[i] * wx[i] : 0.0;
+        wfy[i] = iel[i] ? -facdt[i] * wy[i] : 0.0;
     }
     gsync();
+    // shifts and transient rolling continuing from the previous time instance (P = 0):
+    // wsfix -= u' of the previous tangential tractions, through cs for shifts and through cv
+    // (one rolling step) for transient rolling, where elements within one rolling step of
+    // their leading edge take the edge estimate of subnd instead (stang_rhs, m_stang.f90:749-951;
+    // with identical materials the normal terms vanish, and P = 1 keeps only them)
+    if (d.pvtime == 0 && d.prev && (d.tang == 1 || d.tang == 2)) {
+        const double *pvx = d.prev, *pvy = d.prev + n;
+        const int *igv = (const int *)(d.prev + 3 * (size_t)n);
+        double *ux = P.c(W_UX), *uy = P.c(W_UY);
+        // cs pv on all elements: u' of the shift, or the edge estimate at ix0 + 1 (facdx = 1)
+        prod_t<double>(*T.op, pvx, pvy, ux, uy, OUT_ALL, igs);
+        if (d.tang == 1) {
+            FOR_I(i, n) if (iel[i]) { wfx[i] -= ux[i]; wfy[i] -= uy[i]; }
+        } else {
+            double *cvc = P.c(W_FLS);          // 12 columns, overwritten by the solver later
+            transient_coefs(d, cvc);
+            const size_t bsz = (size_t)4 * mx * my;
+            const double *cxx = cvc, *cxy = cvc + bsz, *cyy = cvc + 2 * bsz;
+            FOR_I(i, n) {
+                if (!iel[i]) continue;
+                const int ix0 = edge[i];
+                if (ix0 > 0) {
+                    if (ix0 + 2 <= mx) {
+                        const int je = ix0 + (i / mx) * mx;
+                        wfx[i] -= ux[je]; wfy[i] -= uy[je];
+                    }
+                    continue;
+                }
+                const int ix = i % mx, iy = i / mx;
+                double a0 = 0.0, a1 = 0.0;
+                for (int j = 0; j < n; j++) {
+                    if (igv[j] < Adhes) continue;
+                    const int jx = j % mx, jy = j / mx;
+                    const size_t off = (size_t)(ix - jx + mx) + (size_t)(iy - jy + my) * 2 * mx;
+                    a0 += cxx[off] * pvx[j] + cxy[off] * pvy[j];
+                    a1 += cxy[off] * pvx[j] + cyy[off] * pvy[j];
+                }
+                wfx[i] -= a0 / d.ga; wfy[i] -= a1 / d.ga;
+            }
+        }
+        gsync();
+    }
+    // row extents of the contact area for the row sums (solvpt, m_solvpt.f90:51-378, sets them
+    // before the solver; the contact area does not change within TANG)
+    areas(P);
     int ittang = 0, itgs = 0;
     bool zready = false;
     double *one = P.c(W_ONE);
     while (!zready && ittang < d.maxin) {
         ittang++;
         zready = true;
-        int info = 0, it = 0;
+        int info = 0;
         double errpt = 0.0;
-        if (solver == 4) {
-            it = stdygs(P, eps, d.maxgs, omegah, omegas, info, errpt);
-        } else if (solver == 7) {
-            bool lstagn = false;
-            it = gdsteady<double>(P, op, d.maxgs, eps, errpt, lstagn, nconv, nls, o32, nconv32);
-            if (it == -100000) return -2000;
-            if (lstagn && !gs_ok) return -1000;
-            if (lstagn) it = stdygs(P, eps, d.maxgs, omegah, omegas, info, errpt);
-        } else {
-            if (o32) {
-                it = tangcg<float>(P, *o32, o32->K[5], o32->K[6], d.maxgs, eps32, errpt, nconv32);
-                itgs += it > 0 ? it : 0;
-            }
-            it = tangcg<double>(P, op, op.K[5], op.K[6], d.maxgs, eps, errpt, nconv);
-        }
+        const int it = solvpt(P, T, info, errpt);
+        if (it < 0) return it;
         itgs += it;
         if (info >= 3) { zready = true; ittang = -1; }
         const double tol = sqrt(2.0) * errpt;
@@ -585,8 +876,9 @@ __device__ __noinline__ void soutpt(const PView &P, const Ops<T> &op, double pen
     pmax = block_max1(red, pmax);
     const double dxdy = d.dxdy, muscal = d.fstat, tiny = 1e-20;
     const double fn = (d.norm == 0) ? dxdy * a[0] : fntrue;
-    const double fxrel = dxdy * a[1] / (fn * muscal + tiny);
-    const double fyrel = dxdy * a[2] / (fn * muscal + tiny);
+    // prescribed total forces are reported as prescribed (m_soutpt.f90:427-434)
+    const double fxrel = (d.force3 >= 1) ? d.fxrel : dxdy * a[1] / (fn * muscal + tiny);
+    const double fyrel = (d.force3 >= 2) ? d.fyrel : dxdy * a[2] / (fn * muscal + tiny);
     double mz = -dxdy * a[3] + dxdy * b[0];
     if (fabs(mz) < 0.5 * d.eps * (muscal * fn + tiny)) mz = 0.0;
     if (glead()) {
@@ -703,9 +995,24 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, c
         ncon = block_sumi1(sm.red, ncon);
     }
     long long t_tang0 = clock64();
+    // creepages and Newton-Raphson sensitivities: a fresh start takes cksi = 1e-6 (and ceta = 0
+    // for F = 2) and zero sensitivities when total forces are prescribed (m_sdis.f90:754-766)
+    TangRun T;
+    T.op = &op64; T.o32 = mixed ? &op32 : nullptr; T.eps = d.eps; T.eps32 = d.eps32;
+    T.nconv = 0; T.nconv32 = 0; T.nls = 0;
+    T.solver = 0; T.fntrue = fntrue;
+    T.cksi = d.cksi; T.ceta = d.ceta;
+    for (int k = 0; k < 4; k++) T.sens[k] = d.sens0[k];
+    if (d.iestim == 0 || d.iestim == 2) {
+        if (d.force3 >= 1) T.cksi = 1e-6;
+        if (d.force3 == 2) T.ceta = 0.0;
+        for (int k = 0; k < 4; k++) T.sens[k] = 0.0;
+    }
     if (d.tang != 0 && ncon > 0 && itnorm >= 0) {
-        int it = 0, itg = 0;
-        it = stang(P, op64, mixed ? &op32 : nullptr, d.eps, d.eps32, itg, solver, nconv64, nconv32, nls);
+        int itg = 0;
+        const int it = stang(P, T, itg);
+        solver = T.solver;
+        nconv64 += T.nconv; nconv32 += T.nconv32; nls += T.nls;
         itgs += itg;
         if (it == -1000) status |= ST_UNSUPPORTED;
         if (it == -2000) status |= ST_NOBRACKET;
@@ -714,6 +1021,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, c
     if (threadIdx.x == 0) sm.t[O_T_TANG - O_T_TOTAL] = clock64() - t_tang0;
     soutpt<double>(P, op64, pen, fntrue, out);
     int atb = count_atbnd(P);
+    // the solution, kept in device memory for the problem's next warm start or time instance
+    if (d.save) {
+        const int n = d.npot;
+        const int *igs = P.igs();
+        const double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN);
+        int *sg = (int *)(d.save + 3 * (size_t)n);
+        FOR_I(i, n) { d.save[i] = px[i]; d.save[n + i] = py[i]; d.save[2 * (size_t)n + i] = pn[i]; sg[i] = igs[i]; }
+        gsync();
+    }
     // a barrier of the group that gave up (error flag in the group scratch)
     if (blk && ((volatile unsigned *)g_grp.bar)[2] != 0u) status |= ST_GROUPFAIL;
     if (glead()) {
@@ -739,6 +1055,9 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, c
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(g_end));
         out[O_TSTART] = (double)g_start;
         out[O_TEND] = (double)g_end;
+        out[O_CKSI] = T.cksi;
+        out[O_CETA] = T.ceta;
+        for (int k = 0; k < 4; k++) out[O_SENS + k] = T.sens[k];
     }
 }
 
@@ -847,11 +1166,15 @@ size_t max_dynamic_smem() {
     return cached;
 }
 
+// grids above this many elements are solved by a patch group when the choice is automatic:
+// one CTA would spend seconds per solve where a group spreads the work over many SMs
+constexpr int kMaxSingleCtaElements = 44100;     // 210 x 210
+
 int group_size(int mx, int my, int fx, int fy, int requested) {
     const size_t lim = max_dynamic_smem();
     const bool fits1 = smem_plan(fx, fy, false).total <= lim;
     if (requested == 1) return fits1 ? 1 : -1;
-    if (requested <= 0 && fits1) return 1;
+    if (requested <= 0 && fits1 && mx * my <= kMaxSingleCtaElements) return 1;
     const size_t sm = smem_plan(fx, fy, true).total;
     if (sm > lim) return -1;
     if (ensure_smem_attr(sm) != cudaSuccess) { cudaGetLastError(); return -1; }
@@ -869,19 +1192,20 @@ int group_size(int mx, int my, int fx, int fy, int requested) {
     return std::max(2, std::min(want, cap));
 }
 
-// side streams of the calling host thread (created once, never destroyed before exit)
+// side streams of the calling host thread, one set per concurrent pass (created on first use,
+// never destroyed before exit)
 struct SideStreams {
     static constexpr int kN = 16;
     cudaStream_t s[kN];
     cudaEvent_t fork, join[kN];
-    bool ok = false;
+    bool init = false, ok = false;
 };
 
-static SideStreams &side_streams() {
-    thread_local SideStreams ss;
-    thread_local bool init = false;
-    if (!init) {
-        init = true;
+static SideStreams &side_streams(int set) {
+    thread_local SideStreams sets[kMaxPassSets];
+    SideStreams &ss = sets[set];
+    if (!ss.init) {
+        ss.init = true;
         bool ok = cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) == cudaSuccess;
         for (int k = 0; k < SideStreams::kN && ok; k++) {
             ok = cudaStreamCreateWithFlags(&ss.s[k], cudaStreamNonBlocking) == cudaSuccess &&
@@ -893,7 +1217,8 @@ static SideStreams &side_streams() {
 }
 
 int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
-               int *d_list, cudaStream_t stream, EngineTimer *timer) {
+               int *d_list, cudaStream_t stream, EngineTimer *timer, int pass_set) {
+    if (pass_set < 0 || pass_set >= kMaxPassSets) return (int)cudaErrorInvalidValue;
     if (timer) timer->nlaunch = 0;
     if (n <= 0) return 0;
     auto mark = [&](int kind, bool after) {
@@ -962,7 +1287,7 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
     }
     mark(2, false);
     if (!classes.empty()) {
-        SideStreams &ss = side_streams();
+        SideStreams &ss = side_streams(pass_set);
         if (!ss.ok) return (int)cudaErrorNotReady;
         if ((e = cudaEventRecord(ss.fork, stream)) != cudaSuccess) return (int)e;
         for (size_t c = 0; c < classes.size(); c++) {

@@ -15,8 +15,9 @@ enum WsCol {
     W_HSTOT, W_RHS, W_RES, W_RPRV, W_DD, W_Z, W_V, W_Q,      // NormCG
     W_WSX, W_WSY, W_DPX, W_DPY, W_DSCL, W_NX, W_NY,          // TANG
     W_RX, W_RY, W_DVX, W_DVY, W_VX, W_VY, W_QX, W_QY,
-    W_POX, W_POY, W_PDX, W_PDY, W_PNX, W_PNY, W_TRC, W_ZX, W_ZY, W_ONE,
+    W_POX, W_POY, W_WFX, W_WFY, W_PNX, W_PNY, W_TRC, W_ZX, W_ZY, W_ONE,   // W_WF*: fixed shift wsfix
     W_DBX, W_DBY, W_SBX, W_SBY, W_TX, W_TY,                  // mixed precision: base dp, A dp_base, change
+    W_FACDT,                                                 // leading-edge fraction of the rolling step
     W_FLS,                                                   // 9 columns: 18 float columns of the line search
     W_FST = W_FLS + 9,                                       // 14 columns: 28 float columns of the FP32 GD state
     W_NCOL = W_FST + 14
@@ -32,7 +33,9 @@ enum OutScalar {
     O_T_CONV32,                            // SM cycles in FP32 convolutions (part of O_T_CONV)
     O_ALGB,                                // algorithmic bytes of the convolutions (inputs, spectra, outputs)
     O_TSTART, O_TEND,                      // global timer (ns) at the start and end of the solve
-    O_NSCAL
+    O_CKSI, O_CETA,                        // creepages (solved for when total forces are prescribed)
+    O_SENS,                                // 4: dFx/dcksi, dFy/dcksi, dFx/deta, dFy/deta of the Newton-Raphson
+    O_NSCAL = O_SENS + 4
 };
 
 // solver status bits (O_STATUS)
@@ -58,7 +61,16 @@ struct PatchDesc {
     double prm[6];
     int precision;                    // 0: FP64 throughout; 1-3: mixed-precision tiers (see gdsteady)
     double eps32;                     // tolerance of the FP32 phase
-    int pad_;
+    int maxnr;                        // Newton-Raphson iterations on prescribed total forces
+    double fxrel, fyrel;              // prescribed Fx / (mu Fn), Fy / (mu Fn) (force3 >= 1, >= 2)
+    double sens0[4];                  // Newton-Raphson sensitivities of the previous solve (warm start)
+    int pvtime;                       // P digit: 0 previous time instance, 1 its normal part, 2 none
+    int pad3_;
+    // previous solution of the problem in device memory (prev_block layout), or nullptr: the
+    // initial estimate when iestim != 0 and the previous time instance when pvtime <= 1.
+    // save: where the solve leaves its own solution in the same layout (may equal prev), or nullptr.
+    const double *prev;
+    double *save;
     // io block: columns W_H .. W_SN (kIoCols * npot doubles), then O_NSCAL output scalars,
     // then the element division (npot ints).  Inputs (element-wise h, warm-start tractions
     // and element division) arrive and all results leave through this block.
@@ -81,6 +93,12 @@ constexpr int kIoCols = W_HSTOT;      // W_H .. W_SN live in the io block
 
 __host__ __device__ inline size_t io_doubles(int npot) {
     return (size_t)kIoCols * npot + O_NSCAL + (size_t)(npot + 1) / 2;
+}
+
+// block of a problem's previous solution: px, py, pn (npot doubles each), then the element
+// division (npot ints)
+__host__ __device__ inline size_t prev_bytes(int npot) {
+    return ((size_t)3 * npot * sizeof(double) + (size_t)npot * sizeof(int) + 255) & ~(size_t)255;
 }
 
 } // namespace cgb

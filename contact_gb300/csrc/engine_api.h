@@ -49,8 +49,12 @@ struct EngineTimer {
     int nlaunch = 0;
 };
 
+// pass_set: which of the calling thread's kMaxPassSets side-stream sets the pass launches its
+// shared-memory classes on; passes that run concurrently (on different caller streams) use
+// different sets so that no class of one waits for a class of the other.
+constexpr int kMaxPassSets = 4;
 int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
-               int *d_list, cudaStream_t stream, EngineTimer *timer = nullptr);
+               int *d_list, cudaStream_t stream, EngineTimer *timer = nullptr, int pass_set = 0);
 
 // smallest 2^a 3^b 5^c 7^d >= n, following opt_fft_size (src/m_aijpj.f90:1022-1119)
 int opt_fft_size(int n);

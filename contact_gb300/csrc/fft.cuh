@@ -8,17 +8,21 @@
 // coefficients are placed at (dx mod NX, dy mod NY); their spectra are real and
 // quadrant-symmetric (even/odd kernels), stored as (fx+1) x (fy+1) values per block.
 //
-// Lines are transformed by line workers: the warps of the CTA for patches solved by one CTA,
-// or the CTAs of the group (one CTA per line) for large patches.
+// The convolution transforms its lines in batches: a CTA loads as many lines as its shared-
+// memory buffer holds and runs each Stockham stage over all butterflies of the batch at once
+// (batch_fft), so that every thread has work in every stage whatever the line length, and one
+// block barrier per stage serves the whole batch.  Batches go round the CTAs of a patch group.
 //
 //   step A  rows:    pairs of real rows (iy, iy+1) packed as one complex row, FFT over NX,
 //                    split into two Hermitian half spectra, stored column-major R[kx][iy]
+//                    (written with the rows of a batch fastest, so that stores are coalesced)
 //   step B  columns: per kx, FFT over NY (only my non-zero inputs), multiply by the kernel
 //                    spectrum (2x2 block for tangential products), inverse FFT, keep the my
 //                    output rows, write back in place
 //   step C  rows:    inverse of step A, real outputs ix < mx scaled by ga_inv / (NX NY)
 //
-// The full NX x NY spectrum is never stored: step B keeps one column in shared memory.
+// The full NX x NY spectrum is never stored: step B keeps a batch of columns in shared memory.
+// Single transforms by a warp or a CTA (line_fft) serve the set-up of the kernel spectra.
 #pragma once
 #include "common.cuh"
 
@@ -175,6 +179,94 @@ __device__ __forceinline__ void stockham_stage_generic(const C<T> *src, C<T> *ds
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// batched transforms: nl lines of length n at buf + l * ld, all butterflies of a stage spread
+// over the threads of the CTA
+// ---------------------------------------------------------------------------------------------
+template <typename T, int R>
+__device__ __forceinline__ void batch_stage(const C<T> *src, C<T> *dst, int ld, int n, int Ns, int nl,
+                                            const C<T> *tw, int dir) {
+    const int nb = n / R;
+    const int tstep = n / (Ns * R);
+    const int total = nl * nb;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int l = t / nb, j = t - l * nb;
+        const C<T> *sl = src + (size_t)l * ld;
+        C<T> *dl = dst + (size_t)l * ld;
+        C<T> v[8];
+        const int jm = j % Ns;
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+            C<T> a = sl[j + r * nb];
+            if (r > 0 && jm > 0) {
+                C<T> w = tw[r * jm * tstep];          // r * jm * tstep < n
+                if (dir > 0) w = cconj<T>(w);
+                a = cmul<T>(a, w);
+            }
+            v[r] = a;
+        }
+        dft_small<T, R>(v, dir);
+        const int idx = (j - jm) * R + jm;           // (j / Ns) Ns R + jm
+#pragma unroll
+        for (int r = 0; r < R; r++) dl[idx + r * Ns] = v[r];
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ void batch_stage_generic(const C<T> *src, C<T> *dst, int ld, int n, int Ns, int R, int nl,
+                                                    const C<T> *tw, int dir) {
+    const int nb = n / R;
+    const int tstep = n / (Ns * R);
+    const int wstep = n / R;
+    const int total = nl * n;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int l = t / n, tt = t - l * n;
+        const int j = tt % nb, k = tt / nb;
+        const int jm = j % Ns;
+        const C<T> *sl = src + (size_t)l * ld;
+        C<T> acc = mkc<T>(0, 0);
+        for (int r = 0; r < R; r++) {
+            C<T> a = sl[j + r * nb];
+            if (r > 0 && jm > 0) {
+                C<T> w = tw[(r * jm * tstep) % n];
+                if (dir > 0) w = cconj<T>(w);
+                a = cmul<T>(a, w);
+            }
+            C<T> wr = tw[(size_t)((r * k) % R) * wstep];
+            if (dir > 0) wr = cconj<T>(wr);
+            acc = cadd<T>(acc, cmul<T>(a, wr));
+        }
+        dst[(size_t)l * ld + (j - jm) * R + jm + k * Ns] = acc;
+    }
+}
+
+// batched 1-D FFT by the whole CTA: nl lines (uniform over the CTA) of length p.n, line l at
+// a + l * ld, scratch b of the same layout.  Returns the buffer holding the result, after a
+// block barrier.  tw[k] = exp(-2 pi i k / n).
+template <typename T>
+__device__ __noinline__ C<T> *batch_fft(C<T> *a, C<T> *b, int ld, int nl, const FftPlan &p, const C<T> *tw,
+                                        int dir) {
+    int Ns = 1;
+    C<T> *src = a, *dst = b;
+    for (int s = 0; s < p.nst; s++) {
+        const int R = p.rad[s];
+        __syncthreads();
+        switch (R) {
+            case 8: batch_stage<T, 8>(src, dst, ld, p.n, Ns, nl, tw, dir); break;
+            case 4: batch_stage<T, 4>(src, dst, ld, p.n, Ns, nl, tw, dir); break;
+            case 2: batch_stage<T, 2>(src, dst, ld, p.n, Ns, nl, tw, dir); break;
+            case 3: batch_stage<T, 3>(src, dst, ld, p.n, Ns, nl, tw, dir); break;
+            case 5: batch_stage<T, 5>(src, dst, ld, p.n, Ns, nl, tw, dir); break;
+            case 7: batch_stage<T, 7>(src, dst, ld, p.n, Ns, nl, tw, dir); break;
+            default: batch_stage_generic<T>(src, dst, ld, p.n, Ns, R, nl, tw, dir); break;
+        }
+        Ns *= R;
+        C<T> *t = src; src = dst; dst = t;
+    }
+    __syncthreads();
+    return src;
+}
+
 // synchronisation of the threads that share one FFT line: a warp, or the whole CTA
 __device__ __forceinline__ void line_sync(bool blk) {
     if (blk) __syncthreads(); else __syncwarp();
@@ -250,9 +342,11 @@ struct Conv {
     int mx, my, NX, NY, fx, fy, nkx;
     FftPlan px, py;
     C<T> *twx, *twy;        // NX, NY: shared memory (single CTA) or global memory (group)
-    C<T> *wbuf;             // shared: per line worker 4 * max(NX,NY)
+    C<T> *wbuf;             // shared: per line worker 4 * max(NX,NY) (kernel spectra set-up)
     int wstride;            // complex elements per worker buffer region
-    Lines L;                // line workers
+    Lines L;                // line workers (kernel spectra set-up)
+    C<T> *cbuf;             // shared: the batch buffer of the convolution (both ping-pong halves)
+    int ccap;               // complex elements of type T in cbuf
     C<T> *R0, *R1;          // global: nkx * my each, column-major [kx][iy]
     double scale;           // ga_inv / (NX NY)
     long long *tacc;        // shared accumulator of cycles spent in convolutions (may be null)
@@ -260,91 +354,120 @@ struct Conv {
     double *bacc;           // shared accumulator of algorithmic bytes (may be null)
 };
 
-// step A: forward row transforms of ncomp real inputs (element-major, mx*my doubles each)
-// into R0 (and R1).  'sel' optionally zeroes inputs outside a mask (mask[i] >= sel_lo).
+// loads each thread keeps in flight when it moves data from global to shared memory
+constexpr int kLoadUnroll = 4;
+
+// batches of the convolution go round the CTAs of the patch group (one CTA: all batches)
+#define FOR_BATCH(bt, nbat) for (int bt = g_grp.rank; bt < (nbat); bt += g_grp.nblk)
+
+// step A: forward row transforms of ncomp real inputs (element-major, mx*my each) into R0
+// (and R1).  Lines are row pairs; a batch holds cap of them (stride NX + 1 complex).
 template <typename T, typename IO>
 __device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, const IO *in1, int ncomp) {
-    const Lines &L = cv.L;
-    const int lane = L.lane, nl = L.nl;
     const int NX = cv.NX, mx = cv.mx, my = cv.my, nkx = cv.nkx;
-    C<T> *a = cv.wbuf + L.widx * cv.wstride;
-    C<T> *b = a + NX;
+    const int ld = NX + 1;
+    const int cap = cv.ccap / (2 * ld);
+    C<T> *a = cv.cbuf, *b = cv.cbuf + (size_t)cap * ld;
     const int npair = (my + 1) / 2;
+    const int nbat = (npair + cap - 1) / cap;
     for (int comp = 0; comp < ncomp; comp++) {
         const IO *in = comp == 0 ? in0 : in1;
         C<T> *R = comp == 0 ? cv.R0 : cv.R1;
-        for (int pr = L.w0; pr < npair; pr += L.nw) {
-            const int iy0 = 2 * pr, iy1 = 2 * pr + 1;
-            const bool has1 = iy1 < my;
-            for (int ix = lane; ix < NX; ix += nl) {
-                T re = 0, im = 0;
-                if (ix < mx) {
-                    re = (T)in[iy0 * mx + ix];
-                    if (has1) im = (T)in[iy1 * mx + ix];
+        FOR_BATCH(bt, nbat) {
+            const int p0 = bt * cap, nl = min(cap, npair - p0);
+            // kLoadUnroll loads in flight per thread before their shared-memory stores
+            for (int t0 = threadIdx.x; t0 < nl * NX; t0 += kLoadUnroll * blockDim.x) {
+                C<T> v[kLoadUnroll];
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int t = t0 + u * blockDim.x;
+                    T re = 0, im = 0;
+                    if (t < nl * NX) {
+                        const int l = t / NX, ix = t - l * NX;
+                        const int iy0 = 2 * (p0 + l);
+                        if (ix < mx) {
+                            re = (T)in[iy0 * mx + ix];
+                            if (iy0 + 1 < my) im = (T)in[(iy0 + 1) * mx + ix];
+                        }
+                    }
+                    v[u] = mkc<T>(re, im);
                 }
-                a[ix] = mkc<T>(re, im);
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int t = t0 + u * blockDim.x;
+                    if (t < nl * NX) { const int l = t / NX; a[(size_t)l * ld + (t - l * NX)] = v[u]; }
+                }
             }
-            C<T> *z = line_fft<T>(a, b, cv.px, cv.twx, -1, lane, nl, L.blk);
-            for (int k = lane; k < nkx; k += nl) {
-                C<T> zk = z[k], zn = z[(NX - k) % NX];
-                // A = (Z[k] + conj Z[n-k]) / 2 ; B = (Z[k] - conj Z[n-k]) / (2i)
-                C<T> A = mkc<T>((T)0.5 * (zk.x + zn.x), (T)0.5 * (zk.y - zn.y));
-                C<T> B = mkc<T>((T)0.5 * (zk.y + zn.y), (T)0.5 * (zn.x - zk.x));
-                R[(size_t)k * my + iy0] = A;
-                if (has1) R[(size_t)k * my + iy1] = B;
+            C<T> *z = batch_fft<T>(a, b, ld, nl, cv.px, cv.twx, -1);
+            // A = (Z[k] + conj Z[n-k]) / 2 ; B = (Z[k] - conj Z[n-k]) / (2i); rows of the batch fastest
+            for (int t = threadIdx.x; t < nkx * nl; t += blockDim.x) {
+                const int k = t / nl, l = t - k * nl;
+                const int iy0 = 2 * (p0 + l);
+                const C<T> zk = z[(size_t)l * ld + k], zn = z[(size_t)l * ld + (k ? NX - k : 0)];
+                R[(size_t)k * my + iy0] = mkc<T>((T)0.5 * (zk.x + zn.x), (T)0.5 * (zk.y - zn.y));
+                if (iy0 + 1 < my) R[(size_t)k * my + iy0 + 1] = mkc<T>((T)0.5 * (zk.y + zn.y), (T)0.5 * (zn.x - zk.x));
             }
-            line_sync(L.blk);
+            __syncthreads();
         }
     }
 }
 
 // step B: per column kx, forward FFT over NY, multiply by the kernel spectrum, inverse FFT.
 // ncomp == 1: u = K0 p ; ncomp == 2: (ux,uy) = [[Kxx, Kxy],[Kxy, Kyy]] (px,py) with
-// K = {Kxx, Kxy, Kyy}.  Kernel blocks are (fx+1) x (fy+1) real, [kx][ky].
+// K = {Kxx, Kxy, Kyy}.  Kernel blocks are (fx+1) x (fy+1) real, [kx][ky].  A batch holds cap
+// columns, each as ncomp lines (stride NY + 1 complex).
 template <typename T>
 __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0, const T *K1, const T *K2) {
-    const Lines &L = cv.L;
-    const int lane = L.lane, nl = L.nl;
     const int NY = cv.NY, my = cv.my, nkx = cv.nkx, fy = cv.fy;
-    C<T> *a0 = cv.wbuf + L.widx * cv.wstride;
-    C<T> *b0 = a0 + NY;
-    C<T> *a1 = b0 + NY;
-    C<T> *b1 = a1 + NY;
-    for (int kx = L.w0; kx < nkx; kx += L.nw) {
-        C<T> *col0 = cv.R0 + (size_t)kx * my;
-        C<T> *col1 = cv.R1 + (size_t)kx * my;
-        for (int iy = lane; iy < NY; iy += nl) {
-            a0[iy] = iy < my ? col0[iy] : mkc<T>(0, 0);
-            if (ncomp == 2) a1[iy] = iy < my ? col1[iy] : mkc<T>(0, 0);
+    const int ld = NY + 1;
+    const int cap = cv.ccap / (2 * ld * ncomp);
+    C<T> *a = cv.cbuf, *b = cv.cbuf + (size_t)cap * ncomp * ld;
+    const int nbat = (nkx + cap - 1) / cap;
+    FOR_BATCH(bt, nbat) {
+        const int k0 = bt * cap, nc = min(cap, nkx - k0), nl = nc * ncomp;
+        for (int t0 = threadIdx.x; t0 < nl * NY; t0 += kLoadUnroll * blockDim.x) {
+            C<T> v[kLoadUnroll];
+#pragma unroll
+            for (int u = 0; u < kLoadUnroll; u++) {
+                const int t = t0 + u * blockDim.x;
+                v[u] = mkc<T>(0, 0);
+                if (t < nl * NY) {
+                    const int line = t / NY, iy = t - line * NY;
+                    const int c = line / ncomp, comp = line - c * ncomp;
+                    if (iy < my) v[u] = ((comp == 0 ? cv.R0 : cv.R1) + (size_t)(k0 + c) * my)[iy];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kLoadUnroll; u++) {
+                const int t = t0 + u * blockDim.x;
+                if (t < nl * NY) { const int line = t / NY; a[(size_t)line * ld + (t - line * NY)] = v[u]; }
+            }
         }
-        C<T> *z0 = line_fft<T>(a0, b0, cv.py, cv.twy, -1, lane, nl, L.blk);
-        C<T> *z1 = (ncomp == 2) ? line_fft<T>(a1, b1, cv.py, cv.twy, -1, lane, nl, L.blk) : nullptr;
-        const size_t kb = (size_t)kx * (fy + 1);
-        for (int ky = lane; ky < NY; ky += nl) {
+        C<T> *z = batch_fft<T>(a, b, ld, nl, cv.py, cv.twy, -1);
+        for (int t = threadIdx.x; t < nc * NY; t += blockDim.x) {
+            const int c = t / NY, ky = t - c * NY;
+            const size_t kb = (size_t)(k0 + c) * (fy + 1);
             const int kq = ky <= fy ? ky : NY - ky;
             if (ncomp == 1) {
-                T k0 = K0[kb + kq];
-                z0[ky] = cscale<T>(z0[ky], k0);
+                z[(size_t)c * ld + ky] = cscale<T>(z[(size_t)c * ld + ky], K0[kb + kq]);
             } else {
                 // the xy kernel is odd in y: its real spectrum is odd in ky
-                T kxx = K0[kb + kq], kxy = (ky <= fy) ? K1[kb + kq] : -K1[kb + kq], kyy = K2[kb + kq];
-                C<T> p0 = z0[ky], p1 = z1[ky];
+                const T kxx = K0[kb + kq], kxy = (ky <= fy) ? K1[kb + kq] : -K1[kb + kq], kyy = K2[kb + kq];
+                C<T> *z0 = z + (size_t)(2 * c) * ld, *z1 = z0 + ld;
+                const C<T> p0 = z0[ky], p1 = z1[ky];
                 z0[ky] = cadd<T>(cscale<T>(p0, kxx), cscale<T>(p1, kxy));
                 z1[ky] = cadd<T>(cscale<T>(p0, kxy), cscale<T>(p1, kyy));
             }
         }
-        C<T> *o0 = (z0 == a0) ? b0 : a0;
-        C<T> *r0 = line_fft<T>(z0, o0, cv.py, cv.twy, +1, lane, nl, L.blk);
-        C<T> *r1 = nullptr;
-        if (ncomp == 2) {
-            C<T> *o1 = (z1 == a1) ? b1 : a1;
-            r1 = line_fft<T>(z1, o1, cv.py, cv.twy, +1, lane, nl, L.blk);
+        C<T> *o = (z == a) ? b : a;
+        C<T> *r = batch_fft<T>(z, o, ld, nl, cv.py, cv.twy, +1);
+        for (int t = threadIdx.x; t < nl * my; t += blockDim.x) {
+            const int line = t / my, iy = t - line * my;
+            const int c = line / ncomp, comp = line - c * ncomp;
+            C<T> *col = (comp == 0 ? cv.R0 : cv.R1) + (size_t)(k0 + c) * my;
+            col[iy] = r[(size_t)line * ld + iy];
         }
-        for (int iy = lane; iy < my; iy += nl) {
-            col0[iy] = r0[iy];
-            if (ncomp == 2) col1[iy] = r1[iy];
-        }
-        line_sync(L.blk);
+        __syncthreads();
     }
 }
 
@@ -353,49 +476,71 @@ constexpr int OUT_ALL = 0;      // u[i] = val for all elements
 constexpr int OUT_INT = 1;      // u[i] = val where igs >= Adhes (AllInt), others untouched
 constexpr int OUT_ADDINT = 2;   // u[i] += val where igs >= Adhes
 
-// step C: inverse row transforms, writes u (element-major doubles)
+// step C: inverse row transforms, writes u (element-major)
 template <typename T, typename IO>
 __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1, int ncomp, int mode,
                               const int *igs) {
-    const Lines &L = cv.L;
-    const int lane = L.lane, nl = L.nl;
     const int NX = cv.NX, mx = cv.mx, my = cv.my, nkx = cv.nkx;
-    C<T> *a = cv.wbuf + L.widx * cv.wstride;
-    C<T> *b = a + NX;
+    const int ld = NX + 1;
+    const int cap = cv.ccap / (2 * ld);
+    C<T> *a = cv.cbuf, *b = cv.cbuf + (size_t)cap * ld;
     const int npair = (my + 1) / 2;
+    const int nbat = (npair + cap - 1) / cap;
     const T sc = (T)cv.scale;
     for (int comp = 0; comp < ncomp; comp++) {
         IO *out = comp == 0 ? out0 : out1;
         const C<T> *R = comp == 0 ? cv.R0 : cv.R1;
-        for (int pr = L.w0; pr < npair; pr += L.nw) {
-            const int iy0 = 2 * pr, iy1 = 2 * pr + 1;
-            const bool has1 = iy1 < my;
-            for (int k = lane; k < NX; k += nl) {
-                C<T> A, B;
-                if (k < nkx) {
-                    A = R[(size_t)k * my + iy0];
-                    B = has1 ? R[(size_t)k * my + iy1] : mkc<T>(0, 0);
-                } else {
-                    A = cconj<T>(R[(size_t)(NX - k) * my + iy0]);
-                    B = has1 ? cconj<T>(R[(size_t)(NX - k) * my + iy1]) : mkc<T>(0, 0);
+        FOR_BATCH(bt, nbat) {
+            const int p0 = bt * cap, nl = min(cap, npair - p0);
+            // Z = A + i B from the half spectra of rows iy0, iy0 + 1 (rows of the batch fastest)
+            for (int t0 = threadIdx.x; t0 < NX * nl; t0 += kLoadUnroll * blockDim.x) {
+                C<T> v[kLoadUnroll];
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int t = t0 + u * blockDim.x;
+                    v[u] = mkc<T>(0, 0);
+                    if (t < NX * nl) {
+                        const int k = t / nl, l = t - k * nl;
+                        const int iy0 = 2 * (p0 + l);
+                        const bool has1 = iy0 + 1 < my;
+                        C<T> A, B;
+                        if (k < nkx) {
+                            A = R[(size_t)k * my + iy0];
+                            B = has1 ? R[(size_t)k * my + iy0 + 1] : mkc<T>(0, 0);
+                        } else {
+                            A = cconj<T>(R[(size_t)(NX - k) * my + iy0]);
+                            B = has1 ? cconj<T>(R[(size_t)(NX - k) * my + iy0 + 1]) : mkc<T>(0, 0);
+                        }
+                        v[u] = mkc<T>(A.x - B.y, A.y + B.x);
+                    }
                 }
-                // Z = A + i B
-                a[k] = mkc<T>(A.x - B.y, A.y + B.x);
+#pragma unroll
+                for (int u = 0; u < kLoadUnroll; u++) {
+                    const int t = t0 + u * blockDim.x;
+                    if (t < NX * nl) { const int k = t / nl; a[(size_t)(t - k * nl) * ld + k] = v[u]; }
+                }
             }
-            C<T> *z = line_fft<T>(a, b, cv.px, cv.twx, +1, lane, nl, L.blk);
-            for (int ix = lane; ix < mx; ix += nl) {
+            C<T> *z = batch_fft<T>(a, b, ld, nl, cv.px, cv.twx, +1);
+#pragma unroll 4
+            for (int t = threadIdx.x; t < nl * mx; t += blockDim.x) {
+                const int l = t / mx, ix = t - l * mx;
+                const int iy0 = 2 * (p0 + l);
+                const C<T> zz = z[(size_t)l * ld + ix];
                 const int i0 = iy0 * mx + ix;
-                const IO v0 = (IO)(z[ix].x * sc);
-                if (mode == OUT_ALL) out[i0] = v0;
-                else if (igs[i0] >= Adhes) out[i0] = (mode == OUT_INT) ? v0 : out[i0] + v0;
-                if (has1) {
-                    const int i1 = iy1 * mx + ix;
-                    const IO v1 = (IO)(z[ix].y * sc);
-                    if (mode == OUT_ALL) out[i1] = v1;
-                    else if (igs[i1] >= Adhes) out[i1] = (mode == OUT_INT) ? v1 : out[i1] + v1;
+                const bool has1 = iy0 + 1 < my;
+                const IO v0 = (IO)(zz.x * sc), v1 = (IO)(zz.y * sc);
+                if (mode == OUT_ALL) {
+                    out[i0] = v0;
+                    if (has1) out[i0 + mx] = v1;
+                } else {
+                    const int g0 = igs[i0], g1 = has1 ? igs[i0 + mx] : Exter;
+                    const IO o0 = (mode == OUT_ADDINT && g0 >= Adhes) ? out[i0] : IO(0);
+                    const IO o1 = (mode == OUT_ADDINT && g1 >= Adhes) ? out[i0 + mx] : IO(0);
+                    if (g0 >= Adhes) out[i0] = (mode == OUT_INT) ? v0 : o0 + v0;
+                    if (g1 >= Adhes) out[i0 + mx] = (mode == OUT_INT) ? v1 : o1 + v1;
                 }
             }
-            line_sync(L.blk);
+            __syncthreads();
         }
     }
 }

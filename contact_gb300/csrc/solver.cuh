@@ -518,14 +518,16 @@ struct TangState {
 // coefficients and vectors independently.
 struct GsBox { int jy0, jx0, w, cnt; };
 
+// cf3: blocks xx, xy (= yx), yy of the coefficients in the layout of cf (block stride 4 mx my)
 __device__ inline void stdygs_rowsum(const PView &P, const GsBox &b, int ii, const double *dpx, const double *dpy,
-                                     double s[2]) {
+                                     double s[2], const double *cf3 = nullptr) {
     const PatchDesc &d = *P.d;
     const int mx = P.mx, my = P.my;
     const int ix = ii % mx + 1, iy = ii / mx + 1;
     const int *ext = P.ci(I_EXT);
     const size_t bsz = (size_t)4 * mx * my;
-    const double *cxx = d.cf, *cxy = d.cf + bsz, *cyy = d.cf + 2 * bsz;
+    if (!cf3) cf3 = d.cf;
+    const double *cxx = cf3, *cxy = cf3 + bsz, *cyy = cf3 + 2 * bsz;
     double a[2] = {0.0, 0.0};
     for (int k = gtid(); k < b.cnt; k += gstride()) {
         const int jy = b.jy0 + k / b.w, jx = b.jx0 + k % b.w;
@@ -542,7 +544,67 @@ __device__ inline void stdygs_rowsum(const PView &P, const GsBox &b, int ii, con
     s[1] = a[1] / d.ga;
 }
 
-__device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double omegah, double omegas, int &info, double &err) {
+// bounding box of the row extents of the contact area (row1st - 1 .. rowlst + 1 per row)
+__device__ inline GsBox gs_box(const PView &P) {
+    const int mx = P.mx, my = P.my;
+    const int *ext = P.ci(I_EXT);
+    GsBox box;
+    if (threadIdx.x == 0) {
+        int jy0 = my + 1, jy1 = 0, jx0 = mx + 1, jx1 = 0;
+        for (int jy = 1; jy <= my; jy++) {
+            const int j0 = max(1, ext[jy - 1] - 1), j1 = min(mx, ext[my + jy - 1] + 1);
+            if (j0 > j1) continue;
+            jy0 = min(jy0, jy); jy1 = max(jy1, jy);
+            jx0 = min(jx0, j0); jx1 = max(jx1, j1);
+        }
+        P.sm->bi[0] = jy0; P.sm->bi[1] = jx0;
+        P.sm->bi[2] = jx1 >= jx0 ? jx1 - jx0 + 1 : 1;
+        P.sm->bi[3] = (jy1 >= jy0 && jx1 >= jx0) ? (jy1 - jy0 + 1) * (jx1 - jx0 + 1) : 0;
+    }
+    gsync();
+    box.jy0 = P.sm->bi[0]; box.jx0 = P.sm->bi[1]; box.w = P.sm->bi[2]; box.cnt = P.sm->bi[3];
+    gsync();
+    return box;
+}
+
+// FP32 row sum of the change of dp within the current sweep (mixed-precision SteadyGS):
+// ga_inv * sum_j A(ii, j) delta(j) over the row extents, coefficients and changes in FP32
+// (per-thread sums), combined across the group in FP64
+__device__ inline void stdygs_rowsum32(const PView &P, const GsBox &b, int ii, const float *cf32, const float *ddx,
+                                       const float *ddy, double s[2]) {
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx, my = P.my;
+    const int ix = ii % mx + 1, iy = ii / mx + 1;
+    const int *ext = P.ci(I_EXT);
+    const size_t bsz = (size_t)4 * mx * my;
+    const float *cxx = cf32, *cxy = cf32 + bsz, *cyy = cf32 + 2 * bsz;
+    float a0 = 0.f, a1 = 0.f;
+    for (int k = gtid(); k < b.cnt; k += gstride()) {
+        const int jy = b.jy0 + k / b.w, jx = b.jx0 + k % b.w;
+        const int j0 = max(1, ext[jy - 1] - 1), j1 = min(mx, ext[my + jy - 1] + 1);
+        if (jx < j0 || jx > j1) continue;
+        const size_t off = (size_t)(ix - jx + mx) + (size_t)(iy - jy + my) * 2 * mx;
+        const int jj = (jx - 1) + (jy - 1) * mx;
+        const float vx = ddx[jj], vy = ddy[jj], c01 = cxy[off];
+        a0 = fmaf(cxx[off], vx, fmaf(c01, vy, a0));
+        a1 = fmaf(c01, vx, fmaf(cyy[off], vy, a1));
+    }
+    double a[2] = {(double)a0, (double)a1};
+    block_sum<2>(P.sm->red, a);
+    s[0] = a[0] / d.ga;
+    s[1] = a[1] / d.ga;
+}
+
+// SteadyGS, m_solvpt.f90:2825-3254.  o64 (mixed precision): each sweep starts from an FP64
+// product s_b = A dp_b of the current dp (one FFT convolution); an element's shift within the
+// sweep is s_b plus the FP32 row sum of the change dp - dp_b made so far in the sweep, so that
+// the shift keeps FP64 accuracy up to the FP32 rounding of that change.
+// After an element is solved its new traction is carried towards the trailing edge through
+// the adhesion elements behind it, up to and including the first element that is not in
+// adhesion: that element keeps its traction and absorbs the change in its dp, so the elements
+// behind it keep the values that the last carry through it gave them.
+__device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double omegah, double omegas, int &info,
+                                   double &err, const Ops<double> *o64 = nullptr) {
     PHASE_START(tgs);
     const PatchDesc &d = *P.d;
     const int mx = P.mx, my = P.my, n = P.n;
@@ -554,6 +616,15 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
     const size_t bsz = (size_t)4 * mx * my;
     const double mus = d.fstat;
     const int ixsta = 1, ixinc = 1, ixend = mx;
+    const bool mix = o64 != nullptr;
+    // mixed: FP32 coefficients xx, xy, yy (6 double columns from W_FST), the FP32 change (one
+    // double column after them), the FP64 base dp_b and its product s_b
+    float *cf32 = (float *)P.c(W_FST);
+    float *ddx = (float *)P.c(W_FST + 6), *ddy = ddx + n;
+    double *dbx = P.c(W_DBX), *dby = P.c(W_DBY), *sbx = P.c(W_SBX), *sby = P.c(W_SBY);
+    if (mix) {
+        for (int t = gtid(); t < (int)(3 * bsz); t += gstride()) cf32[t] = (float)d.cf[t];
+    }
     FOR_I(ii, n) {
         int ix = ii % mx + 1;
         if (ix != ixend) { dpx[ii] = px[ii] - px[ii + ixinc]; dpy[ii] = py[ii] - py[ii + ixinc]; }
@@ -564,37 +635,25 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
     int k = nadh + nslip + nplst;
     double facnel = sqrt((double)(float)n / (double)(float)k);
     // bounding box of the row extents (constant: the contact area does not change in TANG)
-    GsBox box;
-    {
-        const int *ext = P.ci(I_EXT);
-        if (threadIdx.x == 0) {
-            int jy0 = my + 1, jy1 = 0, jx0 = mx + 1, jx1 = 0;
-            for (int jy = 1; jy <= my; jy++) {
-                const int j0 = max(1, ext[jy - 1] - 1), j1 = min(mx, ext[my + jy - 1] + 1);
-                if (j0 > j1) continue;
-                jy0 = min(jy0, jy); jy1 = max(jy1, jy);
-                jx0 = min(jx0, j0); jx1 = max(jx1, j1);
-            }
-            P.sm->bi[0] = jy0; P.sm->bi[1] = jx0;
-            P.sm->bi[2] = jx1 >= jx0 ? jx1 - jx0 + 1 : 1;
-            P.sm->bi[3] = (jy1 >= jy0 && jx1 >= jx0) ? (jy1 - jy0 + 1) * (jx1 - jx0 + 1) : 0;
-        }
-        gsync();
-        box.jy0 = P.sm->bi[0]; box.jx0 = P.sm->bi[1]; box.w = P.sm->bi[2]; box.cnt = P.sm->bi[3];
-        gsync();
-    }
+    const GsBox box = gs_box(P);
     int itgs = 0;
     double dif = 2.0, difid = 1.0, dif1 = 0.0;
     while (dif >= difid && itgs < maxgs) {
         itgs++;
+        if (mix) {
+            FOR_I(i, n) { dbx[i] = dpx[i]; dby[i] = dpy[i]; ddx[i] = 0.f; ddy[i] = 0.f; }
+            prod_t<double>(*o64, dbx, dby, sbx, sby, OUT_ALL, igs);
+        }
         double difacc = 0.0;      // held by the group's lead thread
         for (int iy = 1; iy <= my; iy++) {
             for (int ix = ixsta; ix <= ixend; ix++) {
                 int ii = (ix - 1) + (iy - 1) * mx;
                 if (igs[ii] < Adhes) continue;
                 double s[2];
-                stdygs_rowsum(P, box, ii, dpx, dpy, s);
+                if (mix) stdygs_rowsum32(P, box, ii, cf32, ddx, ddy, s);
+                else stdygs_rowsum(P, box, ii, dpx, dpy, s);
                 if (glead() && ix > ixsta) {
+                    if (mix) { s[0] += sbx[ii]; s[1] += sby[ii]; }
                     // the solver choice keeps the trailing column ix = 1 outside the contact area
                     int jx = ix - ixinc;
                     int jj = (jx - 1) + (iy - 1) * mx;
@@ -616,10 +675,12 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
                     dpy[ii] += pr[1] - py[ii];
                     px[ii] = pr[0]; py[ii] = pr[1];
                     sx[ii] = s[0]; sy[ii] = s[1];
-                    // propagate the new traction of element ii towards the trailing edge: p of an
+                    if (mix) { ddx[ii] = (float)(dpx[ii] - dbx[ii]); ddy[ii] = (float)(dpy[ii] - dby[ii]); }
+                    // carry the new traction of element ii towards the trailing edge: p of an
                     // adhesion element is the sum of the p in front of it and its dp (clipped to
-                    // the bound), slip elements keep p and take a new dp.  The traction in front
-                    // (pxn, pyn) and its element type are carried in registers.
+                    // the bound); the first element that is not in adhesion takes a new dp and
+                    // ends the carry.  The traction in front (pxn, pyn) and its element type are
+                    // carried in registers.
                     double pxn = px[ii], pyn = py[ii];
                     int eln = igs[ii];
                     for (int kx = ix - ixinc; kx >= ixsta; kx -= ixinc) {
@@ -642,11 +703,11 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
                         } else if (el == Slip || el == Plast) {
                             const double cx = px[kk], cy = py[kk];
                             dpx[kk] = cx - pxn; dpy[kk] = cy - pyn;
-                            pxn = cx; pyn = cy;
-                        } else {
-                            if (eln >= Adhes) { dpx[kk] = -pxn; dpy[kk] = -pyn; }
-                            pxn = px[kk]; pyn = py[kk];
+                        } else if (eln >= Adhes) {
+                            dpx[kk] = -pxn; dpy[kk] = -pyn;
                         }
+                        if (mix) { ddx[kk] = (float)(dpx[kk] - dbx[kk]); ddy[kk] = (float)(dpy[kk] - dby[kk]); }
+                        if (el != Adhes) break;
                         eln = el;
                     }
                 }
@@ -658,6 +719,97 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
         double a = 0; FOR_I(i, n) a += px[i] * px[i] + py[i] * py[i];
         a = block_sum1(red, a);
         double rms = sqrt(a / (2 * n));
+        difid = eps * fmax(1e-6, facnel * rms);
+        if (itgs == 1) dif1 = dif;
+    }
+    double conv = 1.0;
+    if (dif * dif1 != 0.0 && itgs > 1) conv = exp(log(dif / dif1) / (itgs - 1));
+    err = dif;
+    info = 0;
+    if (itgs >= maxgs) info = 1;
+    if (itgs >= maxgs && conv > 0.997) info = 2;
+    if (itgs >= maxgs && conv > 1.0) info = 3;
+    PHASE_END(P, O_T_GS - O_T_TOTAL, tgs);
+    return itgs;
+}
+
+// ------------------------------------------------------------------------------------------
+// ConvexGS, m_solvpt.f90:2446-2821 (elastic): block Gauss-Seidel over the contact elements in
+// index order with the element solver plstrc.  The shift of an element comes from the current
+// tractions: through cs for shifts and transient rolling; for steady rolling through
+// csv = cs - cv (one rolling step apart, steady_coefs) or, for elements within one rolling
+// step of their leading edge (edge[ii] > 0), through cs minus the displacement difference just
+// past that edge (subnd, m_leadedge.f90:336-394), refreshed at the start of every sweep.
+// Each element's row sum is a group reduction; the group's lead thread solves the element.
+// edge: per element the 1-based column of its leading edge, 0 when the element takes no edge
+// estimate; csv: blocks xx, xy, yy (steady rolling), else nullptr.
+// ------------------------------------------------------------------------------------------
+__device__ __noinline__ int cnvxgs(const PView &P, const Ops<double> &op, const double *csv, const int *edge,
+                                   bool any_edge, double eps, int maxgs, double omegah, double omegas, int &info,
+                                   double &err) {
+    PHASE_START(tgs);
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx, my = P.my, n = P.n;
+    RedSmem &red = P.sm->red;
+    int *igs = P.igs();
+    double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN);
+    const double *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+    double *sx = P.c(W_SX), *sy = P.c(W_SY);
+    double *ux = P.c(W_UX), *uy = P.c(W_UY);       // cs p, for the leading-edge estimate
+    const size_t bsz = (size_t)4 * mx * my;
+    const size_t o0 = (size_t)mx + (size_t)my * 2 * mx;
+    const double mus = d.fstat;
+    const bool ssrol = csv != nullptr;
+    double coefs[2][2], coefsv[2][2];
+    coefs[0][0] = d.cf[0 * bsz + o0] / d.ga; coefs[0][1] = d.cf[1 * bsz + o0] / d.ga;
+    coefs[1][0] = coefs[0][1];               coefs[1][1] = d.cf[2 * bsz + o0] / d.ga;
+    const double *cv = ssrol ? csv : d.cf;
+    coefsv[0][0] = cv[0 * bsz + o0] / d.ga; coefsv[0][1] = cv[1 * bsz + o0] / d.ga;
+    coefsv[1][0] = coefsv[0][1];            coefsv[1][1] = cv[2 * bsz + o0] / d.ga;
+    int nadh, nslip, nplst, nexter;
+    count_eldiv(P, nadh, nslip, nplst, nexter);
+    const int k = nadh + nslip + nplst;
+    if (k == 0) { info = 0; err = 0.0; PHASE_END(P, O_T_GS - O_T_TOTAL, tgs); return 0; }
+    const double facnel = sqrt((double)(float)n / (double)(float)k);
+    const GsBox box = gs_box(P);
+    int itgs = 0;
+    double dif = 2.0, difid = 1.0, dif1 = 0.0;
+    while (dif >= difid && itgs < maxgs) {
+        itgs++;
+        if (ssrol && any_edge) {
+            // u = cs p on all elements: the edge estimate of position ix0 is u at ix0 + 1
+            // (facdx = 1 for ConvexGS), zero when the edge is within two elements of the end
+            prod_t<double>(op, px, py, ux, uy, OUT_ALL, igs);
+        }
+        double difacc = 0.0;      // held by the group's lead thread
+        for (int ii = 0; ii < n; ii++) {
+            const int el0 = igs[ii];
+            if (el0 < Adhes) continue;
+            if (!(itgs <= 1000 || itgs % 2 == 0 || el0 == Adhes)) continue;
+            const int ix0 = ssrol ? edge[ii] : 0;
+            const bool zledge = ix0 > 0;
+            double s[2];
+            stdygs_rowsum(P, box, ii, px, py, s, zledge ? d.cf : cv);
+            if (glead()) {
+                s[0] += wsx[ii]; s[1] += wsy[ii];
+                if (zledge && ix0 + 2 <= mx) {
+                    const int je = ix0 + (ii / mx) * mx;     // 0-based index of column ix0 + 1
+                    s[0] -= ux[je]; s[1] -= uy[je];
+                }
+                double pr[3] = {px[ii], py[ii], pn[ii]};
+                int el = el0;
+                elm_solve(el, zledge ? coefs : coefsv, eps, omegah, omegas, pr, mus, s);
+                igs[ii] = el;
+                difacc += (px[ii] - pr[0]) * (px[ii] - pr[0]) + (py[ii] - pr[1]) * (py[ii] - pr[1]);
+                px[ii] = pr[0]; py[ii] = pr[1];
+                sx[ii] = s[0]; sy[ii] = s[1];
+            }
+            gsync();
+        }
+        dif = sqrt(block_sum1(red, glead() ? difacc : 0.0) / (2.0 * k));
+        double a = 0; FOR_I(i, n) a += px[i] * px[i] + py[i] * py[i];
+        a = block_sum1(red, a);
+        const double rms = sqrt(a / (2 * n));
         difid = eps * fmax(1e-6, facnel * rms);
         if (itgs == 1) dif1 = dif;
     }

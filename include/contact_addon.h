@@ -13,6 +13,7 @@
  *   cntc_gb300_kernel_launches  number of GPU kernels this library has launched
  *   cntc_gb300_getsolverstats   convolution counts and per-phase cycle counts of the last solve
  *   cntc_gb300_resident_*       solve a staged batch repeatedly on device-resident inputs
+ *   cntc_gb300_fmapeaks         measured FP64 / FP32 FMA peaks of the device
  *   flag CNTC_if_mixedprec      (cntc_setflags) 1: FP32 convolutions + FP64 refinement
  *   flag CNTC_if_groupctas      (cntc_setflags) CTAs per patch: one, or a cooperative group
  */
@@ -212,6 +213,16 @@ void cntc_gb300_lastcopybytes(long long *h2d, long long *d2h);
 void cntc_gb300_resident_solve(int *nrep, double *times, int *ierror);
 void cntc_gb300_resident_collect(int *n, int *ierror);
 void cntc_gb300_resident_release(void);
+/* extension (no reference counterpart): number of buffer sets (1..4, default 1) of the next
+ * cntc_gb300_resident_setup.  With depth d > 1 consecutive passes of cntc_gb300_resident_solve
+ * overlap: pass r runs in set r mod d on its own streams, so the SMs that the last patches of a
+ * pass leave idle take the next passes' patches (continuous batching).  times[4r] is then the
+ * device time of all nrep passes divided by nrep. */
+void cntc_gb300_resident_depth(int *depth);
+/* extension (no reference counterpart): FMA peaks of the current device, measured with CUDA
+ * events: out[0] FP64, out[1] FP32, in TFLOP/s.  The denominators of the patch-solve kernel's
+ * arithmetic roofline.  Returns 0, or -1 when a measurement failed. */
+int cntc_gb300_fmapeaks(double *out);
 
 #ifdef __cplusplus
 }

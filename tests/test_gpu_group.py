@@ -48,6 +48,18 @@ def test_group_tangcg_shift(cntc, oracle):
     assert_parity(g, o, case)
 
 
+def test_group_convexgs(cntc, oracle):
+    """ConvexGS (contact in the trailing column and a rolling step of 2.5 elements) solved by 4
+    CTAs: the steady-rolling coefficients and the leading-edge estimate in a patch group."""
+    case = C.config0(gausei=2, eps=1e-8, mx=31, my=21)
+    case["dq"] = 2.5 * 2 * 1.1 * 6.0 / 31
+    g = run_gpu(cntc, dict(case, group=4), ire=75)
+    assert ctas(cntc, 75) == 4
+    o = C.oracle_solve(case)
+    assert o["solver"] == 3 and g["solver"] == 3
+    assert_parity(g, o, case)
+
+
 def test_group_rough_96_matches_oracle(cntc, oracle):
     """Non-Hertzian rough surface, 96x96, element-wise h, 36 CTAs."""
     case = C.config1(96)

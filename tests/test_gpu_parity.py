@@ -239,17 +239,41 @@ def test_contact_touching_boundary(cntc, oracle):
     assert_parity(g, o, case, iterations=False)
 
 
-def test_contact_in_trailing_column_refused(cntc, oracle):
+def test_contact_in_trailing_column_convexgs(cntc, oracle):
     """Contact in the trailing column selects ConvexGS in the reference (m_stang.f90 solver
-    choice).  The oracle restates ConvexGS and solves the case (with contact on the boundary
-    of the potential contact: a positive ierror); this engine does not provide it yet and
-    returns CNTC_err_other, never a silent fallback."""
+    choice, src/m_solvpt.f90:2446-2821), with contact on the boundary of the potential contact
+    (a positive ierror).  Same element division, forces, tractions and sweeps as the oracle."""
     case = C.config0(gausei=5, eps=1e-8, mx=21, my=21)
     case["potprm"] = [21, 21, 6.0, 4.0, 0.9]
     o = C.oracle_solve(case)
     g = run_gpu(cntc, case, ire=8)
-    assert o["ierror"] > 0 and o["solver"] == 3
-    assert g["ierror_call"] == cntc.CNTC_err_other
+    assert o["ierror"] > 0 and o["solver"] == 3 and g["solver"] == 3
+    assert_parity(g, o, case)
+
+
+@pytest.mark.parametrize("dq_dx", [1.0, 2.5, 5.0])
+def test_convexgs_rolling_step(cntc, oracle, dq_dx):
+    """ConvexGS chosen by its G digit (G=2) in steady rolling with a rolling step of dq_dx
+    elements: the steady-rolling coefficients csv = cs - cv of one step, and for dq > dx the
+    leading-edge estimate (subnd) on the elements within one step of the edge."""
+    mx, my = 31, 21
+    case = C.config0(gausei=2, eps=1e-8, mx=mx, my=my)
+    case["dq"] = dq_dx * 2 * 1.1 * 6.0 / mx
+    case["chi"] = 0.0
+    o = C.oracle_solve(case)
+    g = run_gpu(cntc, case, ire=11)
+    assert o["ierror"] == 0 and o["solver"] == 3 and g["solver"] == 3
+    assert_parity(g, o, case)
+
+
+def test_convexgs_shift(cntc, oracle):
+    """ConvexGS (G=2) for the shift problem (T=1): shifts through cs from the tractions."""
+    case = C.config0(gausei=2, eps=1e-8, mx=21, my=21)
+    case["tang"] = 1
+    o = C.oracle_solve(case)
+    g = run_gpu(cntc, case, ire=12)
+    assert o["ierror"] == 0 and o["solver"] == 3 and g["solver"] == 3
+    assert_parity(g, o, case)
 
 
 def test_pure_spin_and_zero_creepage(cntc, oracle):

@@ -62,7 +62,7 @@ def test_reference_arm_under_torchrun_rank0_prints_once():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()),
            os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1",
-           "--warmup", "0", "--cpu-seconds", "2", "--patches", "64"]
+           "--warmup", "0", "--cpu-threads", "2", "--cpu-max-side", "40", "--patches", "256"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]

@@ -29,6 +29,22 @@ def test_noalloc_matches_calculate_twice(cntc, mixed):
         _same(cntc.results(61, 1), ref)
 
 
+@pytest.mark.parametrize("mx,my,group", [(128, 128, 0), (41, 37, 4)])
+def test_noalloc_near_limit_and_grouped(cntc, mx, my, group):
+    """A grid near the 16 MiB limit, and a patch group of 4 CTAs (its group scratch carved from
+    the same array), each against cntc_calculate on two calls in a row."""
+    case = dict(C.config0(gausei=5, eps=1e-8, mx=mx, my=my), group=group)
+    cntc.setup_case(63, 1, case)
+    assert cntc.calculate(63, 1) == 0
+    ref = cntc.results(63, 1)
+    for _ in range(2):
+        cntc.setup_case(64, 1, case)
+        assert cntc.calculate_noalloc(64, 1) == 0
+        if group:
+            assert int(cntc.getsolverstats(64, 1)["ctas"]) == group
+        _same(cntc.results(64, 1), ref)
+
+
 def test_noalloc_rejects_oversize(cntc):
     case = C.config0(gausei=5, eps=1e-8, mx=160, my=160)      # ~19 MB of device data > 16 MiB
     cntc.setup_case(62, 1, case)
