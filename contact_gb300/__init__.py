@@ -20,6 +20,7 @@ CNTC_if_units, CNTC_un_cntc, CNTC_un_spck, CNTC_un_si = 1933, 1934, 1935, 1936
 CNTC_ic_config, CNTC_ic_pvtime, CNTC_ic_bound, CNTC_ic_tang, CNTC_ic_norm = 1967, 1970, 1971, 1972, 1973
 CNTC_ic_force, CNTC_ic_frclaw, CNTC_ic_inflcf, CNTC_ic_mater = 1974, 1976, 1978, 1979
 CNTC_ic_exrhs, CNTC_ic_iestim, CNTC_ic_output, CNTC_ic_flow, CNTC_ic_matfil = 1980, 1983, 1984, 1985, 1987
+CNTC_ic_sens = 1988
 CNTC_if_idebug, CNTC_if_ncase = 2000, 2005
 CNTC_if_mixedprec = 2010
 CNTC_if_groupctas = 2011
@@ -485,9 +486,9 @@ def setup_case(ire, icp, case):
     undeformed distance, ibase 1, optional), mixed (0-4), dq and chi (optional), group (CTAs
     per patch: 0 automatic, 1 one CTA, n >= 2 a cooperative group of at most n)."""
     flags = [CNTC_ic_tang, CNTC_ic_bound, CNTC_ic_iestim, CNTC_if_mixedprec, CNTC_if_groupctas, CNTC_ic_pvtime,
-             CNTC_ic_force]
+             CNTC_ic_force, CNTC_ic_sens]
     values = [case.get("tang", 3), case.get("bound", 0), case.get("iestim", 0), case.get("mixed", 0),
-              case.get("group", 0), case.get("pvtime", 2), case.get("force3", 0)]
+              case.get("group", 0), case.get("pvtime", 2), case.get("force3", 0), case.get("sens", 1)]
     setflags(ire, icp, flags, values)
     setfrictionmethod(ire, icp, 0, [case.get("fstat", 0.3), case.get("fstat", 0.3)])
     nu = case.get("poiss", 0.28)
@@ -514,6 +515,8 @@ def setup_case(ire, icp, case):
         setsolverflags(ire, icp, gdig, ip + [case.get("inislp", 0)], [case.get("eps", 1e-6), case.get("omgslp", 0.5)])
     else:
         setsolverflags(ire, icp, gdig, ip, [case.get("eps", 1e-6)])
+    if "mxsens" in case or "epsens" in case:
+        setsolverflags(ire, icp, 6, [case.get("mxsens", 30)], [case.get("epsens", 1e-4)])
     if "dq" in case:
         setrollingstepsize(ire, icp, case.get("chi", 0.0), case["dq"])
     ipot = case.get("ipotcn", -3)

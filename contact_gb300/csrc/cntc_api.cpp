@@ -87,7 +87,9 @@ struct Problem {
     double r_dx = 0, r_dy = 0, r_xc1 = 0, r_yc1 = 0, r_dq = 1;
     double f_n = 0, f_x = 0, f_y = 0, m_z = 0, r_pen = 0, elen = 0, pmax = 0;
     int ncon = 0, nadh = 0, nslip = 0;
-    double sens_nr[4] = {0, 0, 0, 0};   // dFx/dcksi, dFy/dcksi, dFx/deta, dFy/deta (relative forces)
+    // sensitivities of the last solve [out * 4 + in]: out Fn, Fx/(mu Fn), Fy/(mu Fn), Mz; in pen, cksi,
+    // ceta, cphi (internal units)
+    double sens_all[16] = {0};
     std::vector<double> fields;   // W_H .. W_SN columns, npot each
     std::vector<int> igs;
     std::vector<double> stats;           // engine statistics: convolution counts, status, phase cycles
@@ -261,7 +263,8 @@ int prepare(Problem &p, Prep &out) {
     d.maxnr = p.maxnr;
     d.pvtime = p.pvtime;
     d.fxrel = p.fxrel; d.fyrel = p.fyrel;
-    for (int k = 0; k < 4; k++) d.sens0[k] = p.sens_nr[k];
+    for (int k = 0; k < 16; k++) d.sens0[k] = p.sens_all[k];
+    d.sens = p.sens; d.mxsens = p.mxsens; d.epsens = p.epsens;
     // geometry key for reuse of influence coefficients and spectra
     char key[128];
     std::snprintf(key, sizeof(key), "%d %d %.17g %.17g %.17g %.17g", mx, my, dx, dy, ga, nu);
@@ -338,7 +341,7 @@ void collect(Problem &p, const PatchDesc &d, const double *io) {
         p.cksi = o[O_CKSI];
         if (d.force3 >= 2) p.ceta = o[O_CETA];
     }
-    for (int k = 0; k < 4; k++) p.sens_nr[k] = o[O_SENS + k];
+    for (int k = 0; k < 16; k++) p.sens_all[k] = o[O_SENS + k];
     p.have = true;
     // kinematic outputs follow the reference: fn from the solution when N = 0
     if (p.norm == 0) p.fn = p.f_n;
@@ -524,6 +527,8 @@ int calculate_many(int n, const int *ire, const int *icp, int *ierror) {
 // passes r+1 .. r+depth-1; pass r+depth waits (stream order) until pass r has finished with
 // its buffers.  depth 1 is the plain sequence of passes.
 // ------------------------------------------------------------------------------------------
+constexpr int kMaxResidentSets = 4;
+
 struct ResSet {
     char *d_io = nullptr, *d_work = nullptr;
     PatchDesc *d_desc = nullptr;
@@ -541,7 +546,7 @@ struct Resident {
     std::vector<size_t> off_io;
     size_t tot_io = 0;
     double *h_io = nullptr;       // pinned staging
-    ResSet set[kMaxPassSets];
+    ResSet set[kMaxResidentSets];
     int depth = 1;
     int last = 0;                 // set of the last pass
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -566,7 +571,7 @@ int g_res_depth = 1;
 int resident_setup(int n, const int *ire, const int *icp, int *ierror) {
     g_res.reset();
     auto R = std::make_unique<Resident>();
-    R->depth = std::max(1, std::min(g_res_depth, kMaxPassSets));
+    R->depth = std::max(1, std::min(g_res_depth, kMaxResidentSets));
     Batch &b = R->b;
     b.probs.resize(n); b.preps.resize(n); b.status.assign(n, 0);
     for (int i = 0; i < n; i++) {
@@ -653,7 +658,7 @@ int resident_solve(int nrep, double *times) {
             if ((e = cudaStreamSynchronize(S.st)) != cudaSuccess) return (int)e;
             read_spans(pending[si], S);
         }
-        int rc = engine_run(S.hd.data(), S.d_desc, m, R->need_ic.data(), S.d_list, S.st, &S.tm, si);
+        int rc = engine_run(S.hd.data(), S.d_desc, m, R->need_ic.data(), S.d_list, S.st, &S.tm);
         if (rc != 0) return rc;
         pending[si] = r;
         R->last = si;
@@ -1380,22 +1385,22 @@ void cntc_getdisplacements(int *ire, int *icp, int *lenarr, double *un, double *
 }
 
 // sens(iout + (iin-1) lenout) for outputs fn, fx, fy, mz and inputs pen, cksi, ceta, cphi, in the
-// caller's units (cntc_getSensitivities 5919-6007).  The Newton-Raphson on prescribed total
-// forces leaves d(Fx, Fy)/d(cksi, ceta); the other entries are zero ("not computed").
+// caller's units (cntc_getSensitivities 5919-6007): zero where not computed.  The Newton-Raphson on
+// prescribed total forces leaves d(Fx, Fy)/d(cksi, ceta); S >= 2 adds dFn/dpen, S >= 3 the
+// derivatives of Fx, Fy and Mz with respect to all three creepages.
 void cntc_getsensitivities(int *ire, int *icp, int *lenout, int *lenin, double *sens) {
     for (int i = 0; i < (*lenout) * (*lenin); i++) sens[i] = 0.0;
     Problem *p = lookup(*ire, *icp, false);
     if (!p) return;
-    // internal -> external: dFx/dcksi * fac_in(cksi) / fac_out(fx); fac_out = 1 for the relative
-    // forces; fac_in = s_len for shifts (T = 1), 1 for rolling
-    const double fin = (p->tang == 1) ? p->s_len : 1.0;
-    auto put = [&](int iout, int iin, double v) {
-        if (iout <= *lenout && iin <= *lenin) sens[(iout - 1) + (iin - 1) * (*lenout)] = v * fin;
-    };
-    put(2, 2, p->sens_nr[0]);
-    put(3, 2, p->sens_nr[1]);
-    put(2, 3, p->sens_nr[2]);
-    put(3, 3, p->sens_nr[3]);
+    // internal -> external: d out / d in * fac_in / fac_out (module 3: no mirroring)
+    double fac_in[4] = {p->s_len, 1.0, 1.0, 1.0 / p->s_len};
+    if (p->tang == 1) { fac_in[1] = p->s_len; fac_in[2] = p->s_len; fac_in[3] = 1.0; }
+    const double fac_out[4] = {p->s_forc, 1.0, 1.0, p->s_forc * p->s_len};
+    for (int iin = 1; iin <= *lenin; iin++)
+        for (int iout = 1; iout <= *lenout; iout++)
+            if (iout <= 4 && iin <= 4)
+                sens[(iout - 1) + (iin - 1) * (*lenout)] =
+                    p->sens_all[(iout - 1) * 4 + (iin - 1)] * fac_in[iin - 1] / fac_out[iout - 1];
 }
 
 void cntc_getcalculationtime(int *ire, int *icp, double *tcpu, double *twall) {
@@ -1564,7 +1569,7 @@ void cntc_gb300_resident_solve(int *nrep, double *times, int *ierror) {
 
 void cntc_gb300_resident_depth(int *depth) {
     std::lock_guard<std::mutex> lk(g_res_mu);
-    g_res_depth = std::max(1, std::min(*depth, kMaxPassSets));
+    g_res_depth = std::max(1, std::min(*depth, kMaxResidentSets));
 }
 
 void cntc_gb300_resident_collect(int *n, int *ierror) {

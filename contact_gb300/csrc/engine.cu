@@ -544,7 +544,9 @@ struct TangRun {
     int nconv, nconv32, nls;
     double fntrue;                // total normal force of the solution
     double cksi, ceta;            // creepages (updated when total forces are prescribed)
-    double sens[4];               // dFx/dcksi, dFy/dcksi, dFx/deta, dFy/deta (relative forces)
+    double *sens;                 // sensitivities [out * 4 + in]: out Fn, Fx, Fy, Mz; in pen, cksi, ceta, cphi
+    int maxgs;                    // iterations and tolerance of the current solve (the sensitivity
+    const double *p0x, *p0y;      // solves change them); p0: base of their stopping rule
 };
 
 // tang_solver, m_solvpt.f90:382-493: one solve of the tangential problem for the current element
@@ -555,23 +557,26 @@ __device__ __noinline__ int tang_solver(const PView &P, TangRun &T, int &info, d
     int it = 0;
     info = 0;
     errpt = 0.0;
+    const int maxgs = T.maxgs;
     if (T.solver == 4) {
-        it = stdygs(P, T.eps, d.maxgs, T.omegah, T.omegas, info, errpt, T.o32 ? T.op : nullptr);
+        it = stdygs(P, T.eps, maxgs, T.omegah, T.omegas, info, errpt, T.o32 ? T.op : nullptr, T.p0x, T.p0y);
     } else if (T.solver == 3) {
-        it = cnvxgs(P, *T.op, T.csv, T.edge, T.any_edge, T.eps, d.maxgs, T.omegah, T.omegas, info, errpt);
+        it = cnvxgs(P, *T.op, T.csv, T.edge, T.any_edge, T.eps, maxgs, T.omegah, T.omegas, info, errpt, T.p0x, T.p0y);
     } else if (T.solver == 7) {
         bool lstagn = false;
-        it = gdsteady<double>(P, *T.op, d.maxgs, T.eps, errpt, lstagn, T.nconv, T.nls, T.o32, T.nconv32);
+        it = gdsteady<double>(P, *T.op, maxgs, T.eps, errpt, lstagn, T.nconv, T.nls, T.o32, T.nconv32);
         if (it == -100000) return -2000;
         if (lstagn && !T.gs_ok) return -1000;
-        if (lstagn) it = stdygs(P, T.eps, d.maxgs, T.omegah, T.omegas, info, errpt, T.o32 ? T.op : nullptr);
+        if (lstagn)
+            it = stdygs(P, T.eps, maxgs, T.omegah, T.omegas, info, errpt, T.o32 ? T.op : nullptr, T.p0x, T.p0y);
     } else {
         int it32 = 0;
         if (T.o32) {
-            it32 = tangcg<float>(P, *T.o32, T.o32->K[5], T.o32->K[6], d.maxgs, T.eps32, errpt, T.nconv32);
+            it32 = tangcg<float>(P, *T.o32, T.o32->K[5], T.o32->K[6], maxgs, fmax(T.eps32, T.eps), errpt, T.nconv32,
+                                 T.p0x, T.p0y);
             it32 = it32 > 0 ? it32 : 0;
         }
-        it = tangcg<double>(P, *T.op, T.op->K[5], T.op->K[6], d.maxgs, T.eps, errpt, T.nconv) + it32;
+        it = tangcg<double>(P, *T.op, T.op->K[5], T.op->K[6], maxgs, T.eps, errpt, T.nconv, T.p0x, T.p0y) + it32;
     }
     return it;
 }
@@ -611,7 +616,9 @@ __device__ __noinline__ int solvpt(const PView &P, TangRun &T, int &info, double
     int itgs = it;
     double fxkp1, fykp1;
     rel_forces(P, T, fxkp1, fykp1);
-    double *sens = T.sens;     // [0] dFx/dcksi, [1] dFy/dcksi, [2] dFx/deta, [3] dFy/deta
+    // the Newton-Raphson's secants dFx/dcksi, dFy/dcksi, dFx/deta, dFy/deta
+    double &s_xk = T.sens[1 * 4 + 1], &s_yk = T.sens[2 * 4 + 1], &s_xe = T.sens[1 * 4 + 2], &s_ye = T.sens[2 * 4 + 2];
+    double sens[4] = {s_xk, s_yk, s_xe, s_ye};
     if (info <= 1) {
         int itnr = 0;
         double df = fabs(d.fxrel - fxkp1);
@@ -674,7 +681,193 @@ __device__ __noinline__ int solvpt(const PView &P, TangRun &T, int &info, double
     } else {
         sens[0] = sens[1] = sens[2] = sens[3] = 0.0;
     }
+    s_xk = sens[0]; s_yk = sens[1]; s_xe = sens[2]; s_ye = sens[3];
     return itgs;
+}
+
+// Kalker's coefficients of the linear theory for an elliptic contact: C11, C22, C23 at nu = 0,
+// 1/4, 1/2 for g = min(a/b, b/a) = 0.1 .. 1 (Kalker 1990, table E.3), as single-precision values
+// like the reference's data statement (linrol, m_hertz.f90:1147-1247).  [a < b | a > b][g row]
+// [C11, C22, C23][nu].  Published theory: the values are the table's.
+__constant__ float c_kalker[2][10][3][3] = {
+    {{{2.51f, 3.31f, 4.85f}, {2.51f, 2.52f, 2.53f}, {.334f, .473f, .731f}},
+     {{2.59f, 3.37f, 4.81f}, {2.59f, 2.63f, 2.66f}, {.483f, .603f, .809f}},
+     {{2.68f, 3.44f, 4.80f}, {2.68f, 2.75f, 2.81f}, {.607f, .715f, .889f}},
+     {{2.78f, 3.53f, 4.82f}, {2.78f, 2.88f, 2.98f}, {.720f, .823f, .977f}},
+     {{2.88f, 3.62f, 4.83f}, {2.88f, 3.01f, 3.14f}, {.827f, .929f, 1.07f}},
+     {{2.98f, 3.72f, 4.91f}, {2.98f, 3.14f, 3.31f}, {.930f, 1.03f, 1.18f}},
+     {{3.09f, 3.81f, 4.97f}, {3.09f, 3.28f, 3.48f}, {1.03f, 1.14f, 1.29f}},
+     {{3.19f, 3.91f, 5.05f}, {3.19f, 3.41f, 3.65f}, {1.13f, 1.25f, 1.40f}},
+     {{3.29f, 4.01f, 5.12f}, {3.29f, 3.54f, 3.82f}, {1.23f, 1.36f, 1.51f}},
+     {{3.40f, 4.12f, 5.20f}, {3.40f, 3.67f, 3.98f}, {1.33f, 1.47f, 1.63f}}},
+    {{{10.7f, 11.7f, 12.9f}, {10.7f, 12.8f, 16.0f}, {12.2f, 14.6f, 18.0f}},
+     {{6.96f, 7.78f, 8.82f}, {6.96f, 8.14f, 9.79f}, {5.72f, 6.63f, 7.89f}},
+     {{5.57f, 6.34f, 7.34f}, {5.57f, 6.40f, 7.51f}, {3.79f, 4.32f, 5.01f}},
+     {{4.84f, 5.57f, 6.57f}, {4.84f, 5.48f, 6.31f}, {2.88f, 3.24f, 3.70f}},
+     {{4.37f, 5.10f, 6.11f}, {4.37f, 4.90f, 5.56f}, {2.35f, 2.62f, 2.96f}},
+     {{4.06f, 4.78f, 5.80f}, {4.06f, 4.50f, 5.04f}, {2.01f, 2.23f, 2.50f}},
+     {{3.82f, 4.54f, 5.58f}, {3.82f, 4.21f, 4.67f}, {1.76f, 1.95f, 2.18f}},
+     {{3.65f, 4.36f, 5.42f}, {3.65f, 3.99f, 4.39f}, {1.58f, 1.75f, 1.94f}},
+     {{3.51f, 4.22f, 5.30f}, {3.51f, 3.81f, 4.16f}, {1.44f, 1.59f, 1.77f}},
+     {{3.40f, 4.12f, 5.20f}, {3.40f, 3.67f, 3.98f}, {1.33f, 1.47f, 1.63f}}}};
+
+// creepage coefficients C11, C22, C23 of the linear theory for Poisson's ratio nu and semi-axes
+// ratio aob: interpolation in the table, the asymptotes of slender ellipses (g < 0.1)
+__device__ void linrol(double nu, double aob, double &cxx, double &cyy, double &cyz) {
+    const double pi = 3.14159265358979323846;
+    int icase;
+    double g;
+    if (aob <= 1.0) { g = aob; icase = 0; } else { g = 1.0 / aob; icase = 1; }
+    if (icase == 0 && g < 0.101) {
+        cxx = pi * pi / 4.0 / (1.0 - nu);
+        cyy = pi * pi / 4.0;
+        cyz = pi * sqrt(g) / 3.0 / (1.0 - nu) * (1.0 + nu * (log(16.0 / g) - 5.0));
+    } else if (icase == 1 && g < 0.101) {
+        const double al = log(16.0 / (g * g));
+        cxx = 2.0 * pi / (al - 2.0 * nu) / g * (1.0 + (3.0 - log(4.0)) / (al - 2.0 * nu));
+        cyy = 2.0 * pi / g * (1.0 + (1.0 - nu) * (3.0 - log(4.0)) / ((1.0 - nu) * al + 2.0 * nu)) /
+              ((1.0 - nu) * al + 2.0 * nu);
+        cyz = 2.0 * pi / 3.0 / pow(g, 1.5) / ((1.0 - nu) * al - 2.0 + 4.0 * nu);
+    } else {
+        const int irow = (int)(10.0 * g - 0.005);
+        const double fac = 10.0 * g - (double)(float)irow;
+        double cc[3];
+        for (int ic = 0; ic < 3; ic++) {
+            double cn[3];
+            for (int in = 0; in < 3; in++)
+                cn[in] = fac * (double)c_kalker[icase][irow][ic][in] + (1.0 - fac) * (double)c_kalker[icase][irow - 1][ic][in];
+            cc[ic] = (nu - 0.25) * (nu - 0.50) * 8.0 / cn[0] - (nu - 0.50) * nu * 16.0 / cn[1] +
+                     nu * (nu - 0.25) * 8.0 / cn[2];
+        }
+        cxx = 1.0 / cc[0]; cyy = 1.0 / cc[1]; cyz = 1.0 / cc[2];
+    }
+}
+
+// char_creep, m_solvpt.f90:497-540: characteristic creepages of the linear theory, with the
+// contact's radius from its area and its semi-axes from the bounding box of its elements
+__device__ __noinline__ void char_creep(const PView &P, double fntrue, double ch[3]) {
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx, n = P.n;
+    const int *igs = P.igs();
+    int c = 0, ix0 = mx + 1, ix1 = 0, iy0 = P.my + 1, iy1 = 0;
+    FOR_I(i, n) if (igs[i] >= Adhes) {
+        c++;
+        const int ix = i % mx + 1, iy = i / mx + 1;
+        ix0 = min(ix0, ix); ix1 = max(ix1, ix); iy0 = min(iy0, iy); iy1 = max(iy1, iy);
+    }
+    RedSmem &red = P.sm->red;
+    c = block_sumi1(red, c);
+    ix0 = (int)block_min1(red, (double)ix0); ix1 = (int)block_max1(red, (double)ix1);
+    iy0 = (int)block_min1(red, (double)iy0); iy1 = (int)block_max1(red, (double)iy1);
+    if (c == 0) { ix0 = mx; ix1 = 1; iy0 = P.my; iy1 = 1; }
+    const double pi = 3.14159265358979323846;
+    const double rc = sqrt((double)(float)c * d.dx * d.dy / pi);
+    const double a = (double)(float)max(1, ix1 - ix0 + 1) * d.dx * 0.5;
+    const double b = (double)(float)max(1, iy1 - iy0 + 1) * d.dy * 0.5;
+    double c11, c22, c23;
+    linrol(d.nu, a / b, c11, c22, c23);
+    ch[0] = d.fstat * fntrue / (rc * rc * d.ga * c11);
+    ch[1] = d.fstat * fntrue / (rc * rc * d.ga * c22);
+    ch[2] = d.fstat * fntrue / (rc * rc * rc * d.ga * c23);
+}
+
+// Mz of the current tangential tractions
+__device__ inline double moment_z(const PView &P) {
+    const PatchDesc &d = *P.d;
+    const double *px = P.c(W_PX), *py = P.c(W_PY);
+    double a[2] = {0.0, 0.0};
+    FOR_I(i, P.n) {
+        const double x = d.xc1 + (i % P.mx) * d.dx, y = d.yc1 + (i / P.mx) * d.dy;
+        a[0] += px[i] * y; a[1] += py[i] * x;
+    }
+    block_sum<2>(P.sm->red, a);
+    return d.dxdy * (-a[0] + a[1]);
+}
+
+// sens_norm, m_solvpn.f90:531-650: d Fn / d pen from one NormCG solve with the approach raised by
+// 0.67 % of the largest normal displacement in contact, started from the solution (which is
+// restored afterwards), with the stopping rule on the change from that start.  unn: the normal
+// displacements of the solution (W_DD).  False when that solve diverges.
+__device__ __noinline__ bool sens_norm(const PView &P, const Ops<double> &op, double pen, double fntrue, int &nconv,
+                                       double &sens_fn_pen) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n;
+    RedSmem &red = P.sm->red;
+    int *igs = P.igs();
+    double *pn = P.c(W_PN), *pn0 = P.c(W_RX), *ig0 = P.c(W_RY);
+    const double *unn = P.c(W_DD);
+    double m = -1e300;
+    FOR_I(i, n) { if (igs[i] >= Adhes) m = fmax(m, unn[i]); pn0[i] = pn[i]; ig0[i] = (double)igs[i]; }
+    const double pentru = block_max1(red, m);
+    const double dpen = 0.0067 * pentru;
+    double penloc = pen + dpen, err = 0.0;
+    const int it = normcg<double>(P, op, d.mxsens, d.epsens, penloc, err, nconv, 0, pn0);
+    double s = 0.0;
+    FOR_I(i, n) s += pn[i];
+    const double fnloc = d.dxdy * block_sum1(red, s);
+    sens_fn_pen = (fnloc - fntrue) / dpen;
+    FOR_I(i, n) { pn[i] = pn0[i]; igs[i] = (int)ig0[i]; }
+    gsync();
+    return it >= 0;
+}
+
+// sens_tang, m_solvpt.f90:544-796: d(Fx, Fy, Mz) / d(cksi, ceta, cphi) from one extra tangential
+// solve per creepage, perturbed by 1e-4 of its characteristic size and started from the solution
+// (restored afterwards), with the sensitivity solves' iterations, tolerance and stopping rule.
+// Returns false when a solve failed.
+__device__ __noinline__ bool sens_tang(const PView &P, TangRun &T) {
+    const PatchDesc &d = *P.d;
+    const int n = P.n, mx = P.mx, f3 = d.force3;
+    int *igs = P.igs();
+    const int *iel = P.ci(I_IEL);
+    double *px = P.c(W_PX), *py = P.c(W_PY), *sx = P.c(W_SX), *sy = P.c(W_SY);
+    double *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+    const double *wfx = P.c(W_WFX), *wfy = P.c(W_WFY), *facdt = P.c(W_FACDT);
+    double *px0 = P.c(W_RES), *py0 = P.c(W_RPRV), *sx0 = P.c(W_Z), *sy0 = P.c(W_V), *ig0 = P.c(W_Q);
+    double fxrel, fyrel;
+    rel_forces(P, T, fxrel, fyrel);
+    const double mztrue = moment_z(P);
+    double ch[3];
+    char_creep(P, T.fntrue, ch);
+    FOR_I(i, n) { px0[i] = px[i]; py0[i] = py[i]; sx0[i] = sx[i]; sy0[i] = sy[i]; ig0[i] = (double)igs[i]; }
+    gsync();
+    const int maxgs0 = T.maxgs;
+    const double eps0 = T.eps;
+    bool ok = true;
+    for (int icrp = 1; icrp <= 3 && ok; icrp++) {
+        const double dcrp = 0.0001 * ch[icrp - 1];
+        FOR_I(i, n) {
+            double wx = wfx[i], wy = wfy[i];
+            if (iel[i]) {
+                if (f3 >= 1) wx += facdt[i] * T.cksi * d.dq;
+                if (f3 >= 2) wy += facdt[i] * T.ceta * d.dq;
+                if (icrp == 1) wx += facdt[i] * dcrp * d.dq;
+                else if (icrp == 2) wy += facdt[i] * dcrp * d.dq;
+                else {
+                    const double x = d.xc1 + (i % mx) * d.dx, y = d.yc1 + (i / mx) * d.dy;
+                    wx -= facdt[i] * dcrp * y * d.dq;
+                    wy += facdt[i] * dcrp * x * d.dq;
+                }
+            }
+            wsx[i] = wx; wsy[i] = wy;
+        }
+        gsync();
+        T.maxgs = d.mxsens; T.eps = d.epsens; T.p0x = px0; T.p0y = py0;
+        int info = 0;
+        double err = 0.0;
+        const int it = tang_solver(P, T, info, err);
+        T.maxgs = maxgs0; T.eps = eps0; T.p0x = nullptr; T.p0y = nullptr;
+        if (it < 0) ok = false;
+        double fxloc, fyloc;
+        rel_forces(P, T, fxloc, fyloc);
+        const double mzloc = moment_z(P);
+        T.sens[1 * 4 + icrp] = (fxloc - fxrel) / dcrp;
+        T.sens[2 * 4 + icrp] = (fyloc - fyrel) / dcrp;
+        T.sens[3 * 4 + icrp] = (mzloc - mztrue) / dcrp;
+        FOR_I(i, n) { px[i] = px0[i]; py[i] = py0[i]; sx[i] = sx0[i]; sy[i] = sy0[i]; igs[i] = (int)ig0[i]; }
+        gsync();
+    }
+    return ok;
 }
 
 // TANG, m_stang.f90:28-746 for Coulomb friction, creepages or total forces prescribed.
@@ -839,6 +1032,7 @@ __device__ __noinline__ int stang(const PView &P, TangRun &T, int &itgs_out) {
     }
     if (!zready) ittang = -1;
     itgs_out = itgs;
+    if (d.sens >= 3 && !sens_tang(P, T)) return -2000;
     return ittang;
 }
 
@@ -915,13 +1109,9 @@ __device__ __noinline__ int count_atbnd(const PView &P) {
 // ------------------------------------------------------------------------------------------
 // the patch solve
 // ------------------------------------------------------------------------------------------
-// grid: one CTA per listed patch (group == 0), or the nblk CTAs of one patch group (group
-// != 0, cooperative launch, list[0] is the patch)
-__global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, const int *list, int group) {
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ SolverSmem sm;
-    const PatchDesc &d = descs[list[group ? 0 : blockIdx.x]];
-    const bool blk = group != 0;
+// the solve of one patch by this CTA (blk false) or by this CTA and the others of its patch
+// group (blk true)
+__device__ __noinline__ void solve_patch(const PatchDesc &d, bool blk, unsigned char *smraw, SolverSmem &sm) {
     group_init(blk ? d.nblk : 1, blk ? (int)blockIdx.x : 0, d.gscr);
     const SmemPlan sp = smem_plan(d.fx, d.fy, blk);
     PView P;
@@ -966,6 +1156,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, c
     gsync();
     setup_patch(P);
     double pen = d.pen, fntrue = d.fntrue;
+    // sensitivities [out * 4 + in] (out Fn, Fx, Fy, Mz; in pen, cksi, ceta, cphi): those of the
+    // previous solve on a warm start, with the reference's resets (m_sdis.f90:754-766)
+    double sens[16];
+    for (int k = 0; k < 16; k++) sens[k] = d.sens0[k];
+    if (d.iestim == 0) for (int io = 1; io < 4; io++) sens[io * 4] = 0.0;
+    if (d.iestim == 0 && (d.norm != 1 || d.ihertz != 0)) sens[0] = 0.0;
+    if (d.iestim == 0 || d.iestim == 2)
+        for (int io = 0; io < 4; io++) for (int ji = 1; ji < 4; ji++) sens[io * 4 + ji] = 0.0;
     int itnorm = 0, ittang = 0, itcg = 0, itgs = 0, solver = 0, nconv32 = 0, nconv64 = 0, nls = 0;
     // NORM (skipped for Hertzian traction bounds B = 2, 3)
     long long t_norm0 = clock64();
@@ -980,6 +1178,14 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, c
         if (d.norm == 0) {
             double s = 0; FOR_I(i, d.npot) s += P.c(W_PN)[i];
             fntrue = d.dxdy * block_sum1(sm.red, s);
+        }
+        // d Fn / d pen (S >= 2, m_snorm.f90:357-368); the reference re-evaluates the normal
+        // displacements of the final pressures on small grids (npot < 700)
+        if (it != -2 && d.sens >= 2) {
+            if (d.npot < 700) prod_n<double>(op64, P.c(W_PN), P.c(W_DD), OUT_ALL, P.igs(), 3);
+            if (!sens_norm(P, op64, pen, fntrue, nconv64, sens[0])) { status |= ST_NORMCG_DIV; itnorm = -1; }
+        } else if (it != -2) {
+            sens[0] = 0.0;
         }
     }
     if (threadIdx.x == 0) sm.t[O_T_NORM - O_T_TOTAL] = clock64() - t_norm0;
@@ -1002,11 +1208,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, c
     T.nconv = 0; T.nconv32 = 0; T.nls = 0;
     T.solver = 0; T.fntrue = fntrue;
     T.cksi = d.cksi; T.ceta = d.ceta;
-    for (int k = 0; k < 4; k++) T.sens[k] = d.sens0[k];
+    T.sens = sens;
+    T.maxgs = d.maxgs; T.p0x = nullptr; T.p0y = nullptr;
     if (d.iestim == 0 || d.iestim == 2) {
         if (d.force3 >= 1) T.cksi = 1e-6;
         if (d.force3 == 2) T.ceta = 0.0;
-        for (int k = 0; k < 4; k++) T.sens[k] = 0.0;
     }
     if (d.tang != 0 && ncon > 0 && itnorm >= 0) {
         int itg = 0;
@@ -1057,8 +1263,32 @@ __global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, c
         out[O_TEND] = (double)g_end;
         out[O_CKSI] = T.cksi;
         out[O_CETA] = T.ceta;
-        for (int k = 0; k < 4; k++) out[O_SENS + k] = T.sens[k];
+        for (int k = 0; k < 16; k++) out[O_SENS + k] = sens[k];
     }
+}
+
+// grid: one CTA per listed patch (mode 0); the nblk CTAs of one patch group (mode 1, cooperative
+// launch, list[0] is the patch); or a persistent grid (mode 2) whose CTAs take the nlist listed
+// patches in list order from the queue counter *queue until none is left, so that the SMs that
+// finish early take the next patch instead of idling
+__global__ void __launch_bounds__(kThreads, 2) k_solve(const PatchDesc *descs, const int *list, int mode, int nlist,
+                                                       int *queue) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ SolverSmem sm;
+    __shared__ int next;
+    if (mode == 2) {
+        for (;;) {
+            if (threadIdx.x == 0) next = atomicAdd(queue, 1);
+            __syncthreads();
+            const int k = next;
+            __syncthreads();
+            if (k >= nlist) break;
+            solve_patch(descs[list[k]], false, smraw, sm);
+            __syncthreads();
+        }
+        return;
+    }
+    solve_patch(descs[list[mode ? 0 : blockIdx.x]], mode != 0, smraw, sm);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1192,33 +1422,8 @@ int group_size(int mx, int my, int fx, int fy, int requested) {
     return std::max(2, std::min(want, cap));
 }
 
-// side streams of the calling host thread, one set per concurrent pass (created on first use,
-// never destroyed before exit)
-struct SideStreams {
-    static constexpr int kN = 16;
-    cudaStream_t s[kN];
-    cudaEvent_t fork, join[kN];
-    bool init = false, ok = false;
-};
-
-static SideStreams &side_streams(int set) {
-    thread_local SideStreams sets[kMaxPassSets];
-    SideStreams &ss = sets[set];
-    if (!ss.init) {
-        ss.init = true;
-        bool ok = cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) == cudaSuccess;
-        for (int k = 0; k < SideStreams::kN && ok; k++) {
-            ok = cudaStreamCreateWithFlags(&ss.s[k], cudaStreamNonBlocking) == cudaSuccess &&
-                 cudaEventCreateWithFlags(&ss.join[k], cudaEventDisableTiming) == cudaSuccess;
-        }
-        ss.ok = ok;
-    }
-    return ss;
-}
-
 int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
-               int *d_list, cudaStream_t stream, EngineTimer *timer, int pass_set) {
-    if (pass_set < 0 || pass_set >= kMaxPassSets) return (int)cudaErrorInvalidValue;
+               int *d_list, cudaStream_t stream, EngineTimer *timer) {
     if (timer) timer->nlaunch = 0;
     if (n <= 0) return 0;
     auto mark = [&](int kind, bool after) {
@@ -1227,18 +1432,14 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
         if (after) { timer->kind[timer->nlaunch] = kind; timer->nlaunch++; }
     };
     auto smem_of = [&](int i) { return solve_smem_bytes(hdesc[i].fx, hdesc[i].fy, hdesc[i].nblk > 1); };
-    // order: influence list first, then the single-CTA patches grouped by shared-memory class,
-    // largest first, then the patch groups
+    // order: influence list first, then the single-CTA patches, largest first (the queue of the
+    // persistent solve), then the patch groups
     std::vector<int> ic_list, ic_single, order, groups;
     for (int i = 0; i < n; i++) {
         if (compute_ic[i]) { ic_list.push_back(i); if (hdesc[i].nblk <= 1) ic_single.push_back(i); }
         if (hdesc[i].nblk > 1) groups.push_back(i); else order.push_back(i);
     }
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        size_t sa = smem_of(a), sb = smem_of(b);
-        if (sa != sb) return sa > sb;
-        return hdesc[a].npot > hdesc[b].npot;
-    });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hdesc[a].npot > hdesc[b].npot; });
     const int nsingle = (int)order.size();
     order.insert(order.end(), groups.begin(), groups.end());
     std::vector<int> all(ic_list);
@@ -1274,34 +1475,23 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
             g_launches += 1;
         }
     }
-    // one launch per shared-memory class (requirement within 25% of the class's first, largest
-    // member); the classes run concurrently on side streams so that the SMs freed by one class
-    // take CTAs of the others instead of idling until the slowest patch of a class finishes
-    std::vector<std::pair<int, int>> classes;
-    for (int start = 0; start < nsingle;) {
-        const size_t sm0 = smem_of(order[start]);
-        int end = start + 1;
-        while (end < nsingle && smem_of(order[end]) * 5 >= sm0 * 4) end++;
-        classes.push_back({start, end});
-        start = end;
-    }
+    // the single-CTA patches: one persistent launch of (co-resident CTAs of the device) CTAs that
+    // take the patches from a queue in device memory, largest first; the queue counter follows
+    // the lists in d_list
     mark(2, false);
-    if (!classes.empty()) {
-        SideStreams &ss = side_streams(pass_set);
-        if (!ss.ok) return (int)cudaErrorNotReady;
-        if ((e = cudaEventRecord(ss.fork, stream)) != cudaSuccess) return (int)e;
-        for (size_t c = 0; c < classes.size(); c++) {
-            cudaStream_t sc = ss.s[c % SideStreams::kN];
-            if (c < (size_t)SideStreams::kN && (e = cudaStreamWaitEvent(sc, ss.fork, 0)) != cudaSuccess) return (int)e;
-            const int start = classes[c].first, cnt = classes[c].second - classes[c].first;
-            const size_t sm0 = smem_of(order[start]);
-            k_solve<<<cnt, kThreads, sm0, sc>>>(ddesc, d_order + start, 0);
-            g_launches += 1;
-        }
-        for (int k = 0; k < SideStreams::kN && k < (int)classes.size(); k++) {
-            if ((e = cudaEventRecord(ss.join[k], ss.s[k])) != cudaSuccess) return (int)e;
-            if ((e = cudaStreamWaitEvent(stream, ss.join[k], 0)) != cudaSuccess) return (int)e;
-        }
+    if (nsingle > 0) {
+        size_t sm1 = 0;
+        for (int k = 0; k < nsingle; k++) sm1 = std::max(sm1, smem_of(order[k]));
+        int dev = 0, nsm = 0, occ = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
+        if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solve, kThreads, sm1)) != cudaSuccess)
+            return (int)e;
+        const int grid = std::max(1, std::min(nsingle, nsm * std::max(1, occ)));
+        int *queue = d_list + all.size();
+        if ((e = cudaMemsetAsync(queue, 0, sizeof(int), stream)) != cudaSuccess) return (int)e;
+        k_solve<<<grid, kThreads, sm1, stream>>>(ddesc, d_order, 2, nsingle, queue);
+        g_launches += 1;
     }
     // patch groups: cooperative launches, one patch at a time on the caller's stream after
     // all single-CTA work, so that nothing else of this library shares the SMs with them
@@ -1311,8 +1501,9 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
         const size_t sm = smem_of(i);
         if ((e = cudaMemsetAsync(h.gscr, 0, 256, stream)) != cudaSuccess) return (int)e;
         const int *lp = d_order + k;
-        int grp = 1;
-        void *args[3] = {(void *)&ddesc, (void *)&lp, (void *)&grp};
+        int grp = 1, nl = 1;
+        int *noq = nullptr;
+        void *args[5] = {(void *)&ddesc, (void *)&lp, (void *)&grp, (void *)&nl, (void *)&noq};
         if (compute_ic[i]) {
             e = cudaLaunchCooperativeKernel((const void *)k_spectra, dim3(h.nblk), dim3(kThreads), args, sm, stream);
             if (e != cudaSuccess) return (int)e;

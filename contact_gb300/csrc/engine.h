@@ -34,8 +34,8 @@ enum OutScalar {
     O_ALGB,                                // algorithmic bytes of the convolutions (inputs, spectra, outputs)
     O_TSTART, O_TEND,                      // global timer (ns) at the start and end of the solve
     O_CKSI, O_CETA,                        // creepages (solved for when total forces are prescribed)
-    O_SENS,                                // 4: dFx/dcksi, dFy/dcksi, dFx/deta, dFy/deta of the Newton-Raphson
-    O_NSCAL = O_SENS + 4
+    O_SENS,                                // 16: d(Fn, Fx, Fy, Mz) / d(pen, cksi, ceta, cphi), [out * 4 + in]
+    O_NSCAL = O_SENS + 16
 };
 
 // solver status bits (O_STATUS)
@@ -63,7 +63,10 @@ struct PatchDesc {
     double eps32;                     // tolerance of the FP32 phase
     int maxnr;                        // Newton-Raphson iterations on prescribed total forces
     double fxrel, fyrel;              // prescribed Fx / (mu Fn), Fy / (mu Fn) (force3 >= 1, >= 2)
-    double sens0[4];                  // Newton-Raphson sensitivities of the previous solve (warm start)
+    double sens0[16];                 // sensitivities of the previous solve (warm start), [out * 4 + in]
+    int sens;                         // S digit: >= 2 d Fn / d pen, >= 3 also the creepage sensitivities
+    int mxsens;                       // iterations and tolerance of the sensitivity solves
+    double epsens;
     int pvtime;                       // P digit: 0 previous time instance, 1 its normal part, 2 none
     int pad3_;
     // previous solution of the problem in device memory (prev_block layout), or nullptr: the

@@ -36,9 +36,9 @@ int group_size(int mx, int my, int fx, int fy, int requested);
 
 // Launch the engine for n patches whose descriptors live in device memory (ddesc) and
 // host memory (hdesc, same order).  compute_ic[i] != 0 requests influence coefficients and
-// spectra for patch i.  Patches are grouped by shared-memory class internally.
-// d_list is caller-owned device scratch for 3*n ints and must stay untouched until the
-// launched work has finished.  Returns a cudaError_t value.
+// spectra for patch i.  The single-CTA patches are solved by one persistent launch, largest first.
+// d_list is caller-owned device scratch for 3*n + 1 ints (the launch lists and the queue counter
+// of the persistent solve) and must stay untouched until the launched work has finished.  Returns a cudaError_t value.
 // Optional per-launch timing: when given, engine_run records ev[2k] before and ev[2k+1]
 // after its k-th kernel launch on 'stream' and sets kind[k] (0 influence coefficients,
 // 1 spectra, 2 patch solve).  The events are created by the caller.
@@ -49,12 +49,9 @@ struct EngineTimer {
     int nlaunch = 0;
 };
 
-// pass_set: which of the calling thread's kMaxPassSets side-stream sets the pass launches its
-// shared-memory classes on; passes that run concurrently (on different caller streams) use
-// different sets so that no class of one waits for a class of the other.
-constexpr int kMaxPassSets = 4;
+// All launches of a pass go to 'stream', so passes on different streams run concurrently.
 int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
-               int *d_list, cudaStream_t stream, EngineTimer *timer = nullptr, int pass_set = 0);
+               int *d_list, cudaStream_t stream, EngineTimer *timer = nullptr);
 
 // smallest 2^a 3^b 5^c 7^d >= n, following opt_fft_size (src/m_aijpj.f90:1022-1119)
 int opt_fft_size(int n);

@@ -183,32 +183,94 @@ __device__ __forceinline__ void stockham_stage_generic(const C<T> *src, C<T> *ds
 // batched transforms: nl lines of length n at buf + l * ld, all butterflies of a stage spread
 // over the threads of the CTA
 // ---------------------------------------------------------------------------------------------
+// Threads and (line, index) pairs of a batch: for rows no longer than the CTA, each thread
+// keeps one index i of a row and visits every G-th line (G rows of the batch side by side);
+// longer rows are strided over the CTA line by line.  Index arithmetic happens once per thread.
+template <typename F>
+__device__ __forceinline__ void for_lines(int nl, int len, F body) {
+    const int bd = blockDim.x;
+    if (len <= bd) {
+        const int G = bd / len, l0 = threadIdx.x / len, i = threadIdx.x - l0 * len;
+        if (l0 < G)
+            for (int l = l0; l < nl; l += G) body(l, i);
+    } else {
+        for (int l = 0; l < nl; l++)
+            for (int i = threadIdx.x; i < len; i += bd) body(l, i);
+    }
+}
+
+// the same visit for a transfer from global to shared memory: four loads in flight per thread
+// before their stores.  load(l, i) returns the value, store(l, i, v) places it.
+template <typename V, typename FL, typename FS>
+__device__ __forceinline__ void copy_lines(int nl, int len, FL load, FS store) {
+    constexpr int U = 4;
+    const int bd = blockDim.x;
+    if (len <= bd) {
+        const int G = bd / len, l0 = threadIdx.x / len, i = threadIdx.x - l0 * len;
+        if (l0 >= G) return;
+        for (int l = l0; l < nl; l += U * G) {
+            V v[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) if (l + u * G < nl) v[u] = load(l + u * G, i);
+#pragma unroll
+            for (int u = 0; u < U; u++) if (l + u * G < nl) store(l + u * G, i, v[u]);
+        }
+    } else {
+        for (int l = 0; l < nl; l++)
+            for (int i0 = threadIdx.x; i0 < len; i0 += U * bd) {
+                V v[U];
+#pragma unroll
+                for (int u = 0; u < U; u++) if (i0 + u * bd < len) v[u] = load(l, i0 + u * bd);
+#pragma unroll
+                for (int u = 0; u < U; u++) if (i0 + u * bd < len) store(l, i0 + u * bd, v[u]);
+            }
+    }
+}
+
+// one radix-R Stockham stage over nl lines: each thread keeps its butterfly j of a line and
+// the twiddles of j in registers
 template <typename T, int R>
 __device__ __forceinline__ void batch_stage(const C<T> *src, C<T> *dst, int ld, int n, int Ns, int nl,
                                             const C<T> *tw, int dir) {
     const int nb = n / R;
     const int tstep = n / (Ns * R);
-    const int total = nl * nb;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int l = t / nb, j = t - l * nb;
+    auto bfly = [&](int l, int j, const C<T> (&w)[8], int jm) {
         const C<T> *sl = src + (size_t)l * ld;
         C<T> *dl = dst + (size_t)l * ld;
         C<T> v[8];
-        const int jm = j % Ns;
 #pragma unroll
         for (int r = 0; r < R; r++) {
             C<T> a = sl[j + r * nb];
-            if (r > 0 && jm > 0) {
-                C<T> w = tw[r * jm * tstep];          // r * jm * tstep < n
-                if (dir > 0) w = cconj<T>(w);
-                a = cmul<T>(a, w);
-            }
+            if (r > 0 && jm > 0) a = cmul<T>(a, w[r]);
             v[r] = a;
         }
         dft_small<T, R>(v, dir);
         const int idx = (j - jm) * R + jm;           // (j / Ns) Ns R + jm
 #pragma unroll
         for (int r = 0; r < R; r++) dl[idx + r * Ns] = v[r];
+    };
+    auto twiddles = [&](int jm, C<T> (&w)[8]) {
+#pragma unroll
+        for (int r = 1; r < R; r++) {
+            C<T> t = tw[r * jm * tstep];                 // r * jm * tstep < n
+            w[r] = (dir > 0) ? cconj<T>(t) : t;
+        }
+    };
+    const int bd = blockDim.x;
+    if (nb <= bd) {
+        const int G = bd / nb, l0 = threadIdx.x / nb, j = threadIdx.x - l0 * nb;
+        if (l0 >= G) return;
+        const int jm = j % Ns;
+        C<T> w[8];
+        twiddles(jm, w);
+        for (int l = l0; l < nl; l += G) bfly(l, j, w, jm);
+    } else {
+        for (int j = threadIdx.x; j < nb; j += bd) {
+            const int jm = j % Ns;
+            C<T> w[8];
+            twiddles(jm, w);
+            for (int l = 0; l < nl; l++) bfly(l, j, w, jm);
+        }
     }
 }
 
@@ -354,9 +416,6 @@ struct Conv {
     double *bacc;           // shared accumulator of algorithmic bytes (may be null)
 };
 
-// loads each thread keeps in flight when it moves data from global to shared memory
-constexpr int kLoadUnroll = 4;
-
 // batches of the convolution go round the CTAs of the patch group (one CTA: all batches)
 #define FOR_BATCH(bt, nbat) for (int bt = g_grp.rank; bt < (nbat); bt += g_grp.nblk)
 
@@ -375,38 +434,26 @@ __device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, con
         C<T> *R = comp == 0 ? cv.R0 : cv.R1;
         FOR_BATCH(bt, nbat) {
             const int p0 = bt * cap, nl = min(cap, npair - p0);
-            // kLoadUnroll loads in flight per thread before their shared-memory stores
-            for (int t0 = threadIdx.x; t0 < nl * NX; t0 += kLoadUnroll * blockDim.x) {
-                C<T> v[kLoadUnroll];
-#pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int t = t0 + u * blockDim.x;
+            copy_lines<C<T>>(nl, NX,
+                [&](int l, int ix) {
+                    const int iy0 = 2 * (p0 + l);
                     T re = 0, im = 0;
-                    if (t < nl * NX) {
-                        const int l = t / NX, ix = t - l * NX;
-                        const int iy0 = 2 * (p0 + l);
-                        if (ix < mx) {
-                            re = (T)in[iy0 * mx + ix];
-                            if (iy0 + 1 < my) im = (T)in[(iy0 + 1) * mx + ix];
-                        }
+                    if (ix < mx) {
+                        re = (T)in[iy0 * mx + ix];
+                        if (iy0 + 1 < my) im = (T)in[(iy0 + 1) * mx + ix];
                     }
-                    v[u] = mkc<T>(re, im);
-                }
-#pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int t = t0 + u * blockDim.x;
-                    if (t < nl * NX) { const int l = t / NX; a[(size_t)l * ld + (t - l * NX)] = v[u]; }
-                }
-            }
+                    return mkc<T>(re, im);
+                },
+                [&](int l, int ix, C<T> v) { a[(size_t)l * ld + ix] = v; });
             C<T> *z = batch_fft<T>(a, b, ld, nl, cv.px, cv.twx, -1);
-            // A = (Z[k] + conj Z[n-k]) / 2 ; B = (Z[k] - conj Z[n-k]) / (2i); rows of the batch fastest
-            for (int t = threadIdx.x; t < nkx * nl; t += blockDim.x) {
-                const int k = t / nl, l = t - k * nl;
+            // A = (Z[k] + conj Z[n-k]) / 2 ; B = (Z[k] - conj Z[n-k]) / (2i); rows of the batch
+            // fastest, so that consecutive threads store consecutive rows of a column
+            for_lines(nkx, nl, [&](int k, int l) {
                 const int iy0 = 2 * (p0 + l);
                 const C<T> zk = z[(size_t)l * ld + k], zn = z[(size_t)l * ld + (k ? NX - k : 0)];
                 R[(size_t)k * my + iy0] = mkc<T>((T)0.5 * (zk.x + zn.x), (T)0.5 * (zk.y - zn.y));
                 if (iy0 + 1 < my) R[(size_t)k * my + iy0 + 1] = mkc<T>((T)0.5 * (zk.y + zn.y), (T)0.5 * (zn.x - zk.x));
-            }
+            });
             __syncthreads();
         }
     }
@@ -425,27 +472,14 @@ __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0
     const int nbat = (nkx + cap - 1) / cap;
     FOR_BATCH(bt, nbat) {
         const int k0 = bt * cap, nc = min(cap, nkx - k0), nl = nc * ncomp;
-        for (int t0 = threadIdx.x; t0 < nl * NY; t0 += kLoadUnroll * blockDim.x) {
-            C<T> v[kLoadUnroll];
-#pragma unroll
-            for (int u = 0; u < kLoadUnroll; u++) {
-                const int t = t0 + u * blockDim.x;
-                v[u] = mkc<T>(0, 0);
-                if (t < nl * NY) {
-                    const int line = t / NY, iy = t - line * NY;
-                    const int c = line / ncomp, comp = line - c * ncomp;
-                    if (iy < my) v[u] = ((comp == 0 ? cv.R0 : cv.R1) + (size_t)(k0 + c) * my)[iy];
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kLoadUnroll; u++) {
-                const int t = t0 + u * blockDim.x;
-                if (t < nl * NY) { const int line = t / NY; a[(size_t)line * ld + (t - line * NY)] = v[u]; }
-            }
-        }
+        copy_lines<C<T>>(nl, NY,
+            [&](int line, int iy) {
+                const int c = line / ncomp, comp = line - c * ncomp;
+                return iy < my ? ((comp == 0 ? cv.R0 : cv.R1) + (size_t)(k0 + c) * my)[iy] : mkc<T>(0, 0);
+            },
+            [&](int line, int iy, C<T> v) { a[(size_t)line * ld + iy] = v; });
         C<T> *z = batch_fft<T>(a, b, ld, nl, cv.py, cv.twy, -1);
-        for (int t = threadIdx.x; t < nc * NY; t += blockDim.x) {
-            const int c = t / NY, ky = t - c * NY;
+        for_lines(nc, NY, [&](int c, int ky) {
             const size_t kb = (size_t)(k0 + c) * (fy + 1);
             const int kq = ky <= fy ? ky : NY - ky;
             if (ncomp == 1) {
@@ -458,15 +492,13 @@ __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0
                 z0[ky] = cadd<T>(cscale<T>(p0, kxx), cscale<T>(p1, kxy));
                 z1[ky] = cadd<T>(cscale<T>(p0, kxy), cscale<T>(p1, kyy));
             }
-        }
+        });
         C<T> *o = (z == a) ? b : a;
         C<T> *r = batch_fft<T>(z, o, ld, nl, cv.py, cv.twy, +1);
-        for (int t = threadIdx.x; t < nl * my; t += blockDim.x) {
-            const int line = t / my, iy = t - line * my;
+        for_lines(nl, my, [&](int line, int iy) {
             const int c = line / ncomp, comp = line - c * ncomp;
-            C<T> *col = (comp == 0 ? cv.R0 : cv.R1) + (size_t)(k0 + c) * my;
-            col[iy] = r[(size_t)line * ld + iy];
-        }
+            ((comp == 0 ? cv.R0 : cv.R1) + (size_t)(k0 + c) * my)[iy] = r[(size_t)line * ld + iy];
+        });
         __syncthreads();
     }
 }
@@ -493,37 +525,23 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1
         FOR_BATCH(bt, nbat) {
             const int p0 = bt * cap, nl = min(cap, npair - p0);
             // Z = A + i B from the half spectra of rows iy0, iy0 + 1 (rows of the batch fastest)
-            for (int t0 = threadIdx.x; t0 < NX * nl; t0 += kLoadUnroll * blockDim.x) {
-                C<T> v[kLoadUnroll];
-#pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int t = t0 + u * blockDim.x;
-                    v[u] = mkc<T>(0, 0);
-                    if (t < NX * nl) {
-                        const int k = t / nl, l = t - k * nl;
-                        const int iy0 = 2 * (p0 + l);
-                        const bool has1 = iy0 + 1 < my;
-                        C<T> A, B;
-                        if (k < nkx) {
-                            A = R[(size_t)k * my + iy0];
-                            B = has1 ? R[(size_t)k * my + iy0 + 1] : mkc<T>(0, 0);
-                        } else {
-                            A = cconj<T>(R[(size_t)(NX - k) * my + iy0]);
-                            B = has1 ? cconj<T>(R[(size_t)(NX - k) * my + iy0 + 1]) : mkc<T>(0, 0);
-                        }
-                        v[u] = mkc<T>(A.x - B.y, A.y + B.x);
+            copy_lines<C<T>>(NX, nl,
+                [&](int k, int l) {
+                    const int iy0 = 2 * (p0 + l);
+                    const bool has1 = iy0 + 1 < my;
+                    C<T> A, B;
+                    if (k < nkx) {
+                        A = R[(size_t)k * my + iy0];
+                        B = has1 ? R[(size_t)k * my + iy0 + 1] : mkc<T>(0, 0);
+                    } else {
+                        A = cconj<T>(R[(size_t)(NX - k) * my + iy0]);
+                        B = has1 ? cconj<T>(R[(size_t)(NX - k) * my + iy0 + 1]) : mkc<T>(0, 0);
                     }
-                }
-#pragma unroll
-                for (int u = 0; u < kLoadUnroll; u++) {
-                    const int t = t0 + u * blockDim.x;
-                    if (t < NX * nl) { const int k = t / nl; a[(size_t)(t - k * nl) * ld + k] = v[u]; }
-                }
-            }
+                    return mkc<T>(A.x - B.y, A.y + B.x);
+                },
+                [&](int k, int l, C<T> v) { a[(size_t)l * ld + k] = v; });
             C<T> *z = batch_fft<T>(a, b, ld, nl, cv.px, cv.twx, +1);
-#pragma unroll 4
-            for (int t = threadIdx.x; t < nl * mx; t += blockDim.x) {
-                const int l = t / mx, ix = t - l * mx;
+            for_lines(nl, mx, [&](int l, int ix) {
                 const int iy0 = 2 * (p0 + l);
                 const C<T> zz = z[(size_t)l * ld + ix];
                 const int i0 = iy0 * mx + ix;
@@ -539,7 +557,7 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1
                     if (g0 >= Adhes) out[i0] = (mode == OUT_INT) ? v0 : o0 + v0;
                     if (g1 >= Adhes) out[i0 + mx] = (mode == OUT_INT) ? v1 : o1 + v1;
                 }
-            }
+            });
             __syncthreads();
         }
     }

@@ -163,9 +163,11 @@ __device__ inline void prod_t(const Ops<T> &op, const IO *inx, const IO *iny, IO
 // ------------------------------------------------------------------------------------------
 // NormCG, m_solvpn.f90:24-461.  Returns itcg, or -1 when the reference would abort.
 // ------------------------------------------------------------------------------------------
+// norm: the N digit of this solve (0 approach prescribed, 1 total force); p0 (sensitivity
+// solve, m_solvpn.f90:92-97, 281-290): the tolerance is relative to the change from p0
 template <typename T>
 __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, double eps, double &pen, double &err,
-                      int &nconv) {
+                      int &nconv, int norm, const double *p0 = nullptr) {
     const PatchDesc &d = *P.d;
     const int n = P.n;
     RedSmem &red = P.sm->red;
@@ -174,12 +176,12 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
     double *dd = P.c(W_DD), *z = P.c(W_Z), *v = P.c(W_V), *q = P.c(W_Q);
     const double dxdy = d.dxdy, fntrue = d.fntrue;
     const int numinn = (n <= 150) ? 3 : (n <= 400) ? 2 : 1;
-    if (d.norm == 1) pen = 0.0;
+    if (norm == 1) pen = 0.0;
     FOR_I(i, n) { rhs[i] = pen - hstot[i]; }
     double davg = 0.0;
     int ncon = 0;
     { int c = 0; FOR_I(i, n) if (igs[i] >= Adhes) c++; ncon = block_sumi1(red, c); }
-    if (d.norm == 0) {
+    if (norm == 0) {
         double hmin = 1e20; FOR_I(i, n) hmin = fmin(hmin, hstot[i]);
         hmin = block_min1(red, hmin) - pen;
         if (hmin >= 0.0) {
@@ -212,7 +214,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
     {
         double s = 0; int c = 0;
         FOR_I(i, n) if (igs[i] >= Adhes) { res[i] = rhs[i] - res[i]; s += res[i]; c++; }
-        if (d.norm == 1) {
+        if (norm == 1) {
             double a[1] = {s}; block_sum<1>(red, a); int cc = block_sumi1(red, c);
             double avg = a[0] / (double)(float)max(1, cc);
             FOR_I(i, n) if (igs[i] >= Adhes) res[i] -= avg;
@@ -226,7 +228,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
     while ((lchanged || rms_upd > eps * rms_xk) && itcg < maxcg) {
         itcg++; itinn++;
         prod_n<T>(op, res, z, OUT_INT, igs, 4); nconv++;
-        if (d.norm == 1) {
+        if (norm == 1) {
             double s = 0; int c = 0;
             FOR_I(i, n) if (igs[i] >= Adhes) { s += z[i]; c++; }
             s = block_sum1(red, s); c = block_sumi1(red, c);
@@ -247,7 +249,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
                 FOR_I(i, n) if (igs[i] >= Adhes) v[i] = beta * v[i] + z[i];
             }
         }
-        if (d.norm == 1) {
+        if (norm == 1) {
             double s = 0; int c = 0;
             FOR_I(i, n) if (igs[i] >= Adhes) { s += v[i]; c++; }
             s = block_sum1(red, s); c = block_sumi1(red, c);
@@ -255,7 +257,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
             FOR_I(i, n) if (igs[i] >= Adhes) v[i] -= avg;
         }
         prod_n<T>(op, v, q, OUT_INT, igs, 3); nconv++;
-        if (d.norm == 1) {
+        if (norm == 1) {
             double s = 0; int c = 0;
             FOR_I(i, n) if (igs[i] >= Adhes) { s += q[i]; c++; }
             s = block_sum1(red, s); c = block_sumi1(red, c);
@@ -276,7 +278,9 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
             double a[2] = {0, 0};
             FOR_I(i, n) if (igs[i] >= Adhes) {
                 pn[i] += alpha * v[i];
-                a[0] += v[i] * v[i]; a[1] += pn[i] * pn[i];
+                a[0] += v[i] * v[i];
+                const double e = p0 ? pn[i] - p0[i] : pn[i];
+                a[1] += e * e;
             }
             int c = 0; FOR_I(i, n) if (igs[i] >= Adhes) c++;
             block_sum<2>(red, a);
@@ -306,7 +310,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
                 ncon += c;
                 if (c > 0) lchg_negpn = true;
             }
-            if (d.norm == 1 && lchg_negpn) {
+            if (norm == 1 && lchg_negpn) {
                 double s = 0; FOR_I(i, n) s += pn[i];
                 double fk = dxdy * block_sum1(red, s);
                 if (fabs(fk) < (double)1e-3f * fntrue) {
@@ -319,7 +323,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
             // dd = A ps - rhs on all elements
             prod_n<T>(op, pn, dd, OUT_ALL, igs, 3); nconv++;
             FOR_I(i, n) dd[i] -= rhs[i];
-            if (d.norm == 1) {
+            if (norm == 1) {
                 double s = 0; FOR_I(i, n) if (igs[i] >= Adhes) s += dd[i];
                 s = block_sum1(red, s);
                 davg = s / (double)(float)ncon;
@@ -340,7 +344,7 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
             lchanged = (nin > 0) || lchg_negpn;
         }
     }
-    if (d.norm == 1) pen = davg;
+    if (norm == 1) pen = davg;
     double conv = 1.0;
     if (rms_upd * rms_upd1 > 0.0 && itcg > 1) conv = exp(log(rms_upd / rms_upd1) / (itcg - 1));
     err = rms_upd;
@@ -367,7 +371,7 @@ __device__ __noinline__ int snorm(const PView &P, const Ops<T> &op, int maxgs, i
         FOR_I(i, n) if (igs[i] < Adhes) pn[i] = 0.0;
         gsync();
         double errpn;
-        int it = normcg<T>(P, op, maxgs, eps, pen, errpn, nconv);
+        int it = normcg<T>(P, op, maxgs, eps, pen, errpn, nconv, P.d->norm);
         if (it < 0) { itcg_out = itcg; return -2; }
         itcg += it;
         int newext = 0;
@@ -567,6 +571,19 @@ __device__ inline GsBox gs_box(const PView &P) {
     return box;
 }
 
+// rms over all elements of the tangential tractions, or of their change from p0 (the stopping
+// rule of the sensitivity solves, m_solvpt.f90:2893-2899, 3138-3145)
+__device__ inline double rms_from(const PView &P, const double *px, const double *py, const double *p0x,
+                                  const double *p0y) {
+    double a = 0;
+    FOR_I(i, P.n) {
+        const double ex = p0x ? px[i] - p0x[i] : px[i], ey = p0y ? py[i] - p0y[i] : py[i];
+        a += ex * ex + ey * ey;
+    }
+    a = block_sum1(P.sm->red, a);
+    return sqrt(a / (2 * P.n));
+}
+
 // FP32 row sum of the change of dp within the current sweep (mixed-precision SteadyGS):
 // ga_inv * sum_j A(ii, j) delta(j) over the row extents, coefficients and changes in FP32
 // (per-thread sums), combined across the group in FP64
@@ -604,7 +621,8 @@ __device__ inline void stdygs_rowsum32(const PView &P, const GsBox &b, int ii, c
 // adhesion: that element keeps its traction and absorbs the change in its dp, so the elements
 // behind it keep the values that the last carry through it gave them.
 __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double omegah, double omegas, int &info,
-                                   double &err, const Ops<double> *o64 = nullptr) {
+                                   double &err, const Ops<double> *o64 = nullptr, const double *p0x = nullptr,
+                                   const double *p0y = nullptr) {
     PHASE_START(tgs);
     const PatchDesc &d = *P.d;
     const int mx = P.mx, my = P.my, n = P.n;
@@ -716,9 +734,7 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
         }
         // the lead thread's sum, broadcast to the group (the other threads add zeros)
         dif = sqrt(block_sum1(red, glead() ? difacc : 0.0) / (2.0 * k));
-        double a = 0; FOR_I(i, n) a += px[i] * px[i] + py[i] * py[i];
-        a = block_sum1(red, a);
-        double rms = sqrt(a / (2 * n));
+        const double rms = rms_from(P, px, py, p0x, p0y);
         difid = eps * fmax(1e-6, facnel * rms);
         if (itgs == 1) dif1 = dif;
     }
@@ -746,7 +762,7 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
 // ------------------------------------------------------------------------------------------
 __device__ __noinline__ int cnvxgs(const PView &P, const Ops<double> &op, const double *csv, const int *edge,
                                    bool any_edge, double eps, int maxgs, double omegah, double omegas, int &info,
-                                   double &err) {
+                                   double &err, const double *p0x = nullptr, const double *p0y = nullptr) {
     PHASE_START(tgs);
     const PatchDesc &d = *P.d;
     const int mx = P.mx, my = P.my, n = P.n;
@@ -807,9 +823,7 @@ __device__ __noinline__ int cnvxgs(const PView &P, const Ops<double> &op, const 
             gsync();
         }
         dif = sqrt(block_sum1(red, glead() ? difacc : 0.0) / (2.0 * k));
-        double a = 0; FOR_I(i, n) a += px[i] * px[i] + py[i] * py[i];
-        a = block_sum1(red, a);
-        const double rms = sqrt(a / (2 * n));
+        const double rms = rms_from(P, px, py, p0x, p0y);
         difid = eps * fmax(1e-6, facnel * rms);
         if (itgs == 1) dif1 = dif;
     }
@@ -1781,9 +1795,11 @@ __device__ __noinline__ int gdsteady(const PView &P, const Ops<T> &op, int maxgd
 // TangCG, m_solvpt.f90:1841-2442 (elastic).  The FFT preconditioner uses blocks xx, yy of
 // the preconditioner spectra, evaluated at the convolution's FFT size.
 // ------------------------------------------------------------------------------------------
+// p0x, p0y (sensitivity solves, m_solvpt.f90:1908-1914): the tolerance is relative to the change
+// of the tractions from p0 instead of to the tractions
 template <typename T>
 __device__ __noinline__ int tangcg(const PView &P, const Ops<T> &op, const T *Mxx, const T *Myy, int maxcg, double eps,
-                      double &err, int &nconv) {
+                      double &err, int &nconv, const double *p0x = nullptr, const double *p0y = nullptr) {
     const PatchDesc &d = *P.d;
     const int n = P.n, my = P.my, mx = P.mx;
     RedSmem &red = P.sm->red;
@@ -1891,7 +1907,12 @@ __device__ __noinline__ int tangcg(const PView &P, const Ops<T> &op, const T *Mx
                     px[i] = px[i] * g[i] / ptabs; py[i] = py[i] * g[i] / ptabs;
                 }
                 a[0] += vx[i] * vx[i] + vy[i] * vy[i];
-                a[1] += px[i] * px[i] + py[i] * py[i];
+                if (p0x) {
+                    const double ex = px[i] - p0x[i], ey = py[i] - p0y[i];
+                    a[1] += ex * ex + ey * ey;
+                } else {
+                    a[1] += px[i] * px[i] + py[i] * py[i];
+                }
             }
             block_sum<2>(red, a);
             dif = alpha * facnel * sqrt(a[0] / (2 * n));

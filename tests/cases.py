@@ -339,6 +339,10 @@ def to_oracle(case):
         pb.gg3, pb.laythk, pb.tau_c0, pb.k_tau = case["gg3"], case["laythk"], case["tau_c0"], case["k_tau"]
     pb.fxrel, pb.fyrel = case.get("fxrel", 0.0), case.get("fyrel", 0.0)
     pb.sens = case.get("sens", 1)
+    if "mxsens" in case:
+        pb.mxsens = case["mxsens"]
+    if "epsens" in case:
+        pb.epsens = case["epsens"]
     pb.standalone = int(case.get("standalone", False))
     pb.pvtime = case.get("pvtime", 2)
     if "iestim" in case:
