@@ -18,8 +18,16 @@ pytestmark = pytest.mark.gpu
 
 
 def _replay_gpu(cntc, seq, ire):
+    """The sequence through the C-ABI on one problem.  A case that prescribes total forces and
+    gives no creepage keeps the creepage of the previous solve (the stand-alone program's
+    carry-over, as the oracle replay does), which the Newton-Raphson starts from."""
     out = []
     for c in seq:
+        c = dict(c)
+        if out and c.get("force3", 0) >= 1 and "cksi" not in c:
+            c["cksi"] = out[-1]["creep"][0]
+        if out and c.get("force3", 0) >= 2 and "ceta" not in c:
+            c["ceta"] = out[-1]["creep"][1]
         out.append(run_gpu(cntc, c, ire=ire))
         out[-1]["creep"] = cntc.getcreepages(ire, 1)
     return out
