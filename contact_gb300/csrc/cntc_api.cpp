@@ -886,8 +886,10 @@ int calculate_async(int ire, int icp) {
     {
         std::lock_guard<std::mutex> lk(S.mu);
         const long long key = pkey2(ire, icp);
-        auto it = S.pending.find(key);
-        if (it != S.pending.end() && !it->second->done) return CNTC_err_other;   // already queued
+        // one request per problem at a time, as the reference locks a problem for the duration
+        // of a call (m_caddon_data.f90:336-413): a request holds its problem until cntc_wait
+        // has returned for it
+        if (S.pending.find(key) != S.pending.end()) return CNTC_err_other;
         S.ensure_started();
         S.pending[key] = r;
         S.queue.push_back(r);

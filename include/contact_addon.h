@@ -93,7 +93,8 @@ void cntc_calculate_noalloc(int *ire, int *icp, int *ierror);
 /* extension (serving): queue the solve of (ire, icp) and return at once (ierror 0 when
  * queued).  Queued solves are batched by free worker lanes as they arrive, up to a device
  * memory admission budget, and run concurrently with earlier batches.  The problem's
- * settings must not change until cntc_wait has returned for it. */
+ * settings must not change until cntc_wait has returned for it; a second request for the
+ * same problem before then is refused with CNTC_err_other. */
 void cntc_calculate_async(int *ire, int *icp, int *ierror);
 /* extension (serving): wait for a queued solve; ierror as cntc_calculate */
 void cntc_wait(int *ire, int *icp, int *ierror);
