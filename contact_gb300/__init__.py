@@ -117,6 +117,7 @@ _PROTOS = {
     "cntc_gb300_resident_collect": [_IP, _IP],
     "cntc_gb300_resident_release": [],
     "cntc_gb300_resident_depth": [_IP],
+    "cntc_gb300_resident_graphs": [],
     "cntc_gb300_lastcopybytes": [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "cntc_gb300_fmapeaks": [_DP],
 }
@@ -135,7 +136,8 @@ def load(path=None):
     for name, args in _PROTOS.items():
         f = getattr(lib, name)
         f.argtypes = args
-        f.restype = {"cntc_gb300_kernel_launches": ctypes.c_longlong, "cntc_gb300_fmapeaks": ctypes.c_int}.get(name)
+        f.restype = {"cntc_gb300_kernel_launches": ctypes.c_longlong, "cntc_gb300_fmapeaks": ctypes.c_int,
+                     "cntc_gb300_resident_graphs": ctypes.c_int}.get(name)
     _lib = lib
     return lib
 
@@ -456,6 +458,10 @@ class ResidentBatch:
         if err.value != 0:
             raise RuntimeError("resident solve failed (%d)" % err.value)
         return t
+
+    def graphs(self):
+        """Buffer sets whose pass replays a captured CUDA graph."""
+        return int(load().cntc_gb300_resident_graphs())
 
     def collect(self):
         err = np.zeros(self.n, dtype=np.int32)

@@ -1422,15 +1422,9 @@ int group_size(int mx, int my, int fx, int fy, int requested) {
     return std::max(2, std::min(want, cap));
 }
 
-int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
-               int *d_list, cudaStream_t stream, EngineTimer *timer) {
-    if (timer) timer->nlaunch = 0;
+int engine_plan(const PatchDesc *hdesc, int n, const unsigned char *compute_ic, EnginePlan &pl) {
+    pl = EnginePlan();
     if (n <= 0) return 0;
-    auto mark = [&](int kind, bool after) {
-        if (!timer || timer->nlaunch >= EngineTimer::kMax) return;
-        cudaEventRecord(timer->ev[2 * timer->nlaunch + (after ? 1 : 0)], stream);
-        if (after) { timer->kind[timer->nlaunch] = kind; timer->nlaunch++; }
-    };
     auto smem_of = [&](int i) { return solve_smem_bytes(hdesc[i].fx, hdesc[i].fy, hdesc[i].nblk > 1); };
     // order: influence list first, then the single-CTA patches, largest first (the queue of the
     // persistent solve), then the patch groups
@@ -1440,82 +1434,110 @@ int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned c
         if (hdesc[i].nblk > 1) groups.push_back(i); else order.push_back(i);
     }
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hdesc[a].npot > hdesc[b].npot; });
-    const int nsingle = (int)order.size();
+    pl.nsingle = (int)order.size();
     order.insert(order.end(), groups.begin(), groups.end());
-    std::vector<int> all(ic_list);
-    all.insert(all.end(), ic_single.begin(), ic_single.end());
-    all.insert(all.end(), order.begin(), order.end());
-    cudaError_t e = cudaMemcpyAsync(d_list, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
-    if (e != cudaSuccess) return (int)e;
-    // the host vector must outlive the asynchronous copy
-    e = cudaStreamSynchronize(stream);
-    if (e != cudaSuccess) return (int)e;
-    const int *d_ic = d_list;
-    const int *d_ics = d_list + ic_list.size();
-    const int *d_order = d_ics + ic_single.size();
-    size_t maxsm = 0;
-    for (int i = 0; i < n; i++) maxsm = std::max(maxsm, smem_of(i));
-    e = ensure_smem_attr(maxsm);
+    pl.all = ic_list;
+    pl.all.insert(pl.all.end(), ic_single.begin(), ic_single.end());
+    pl.all.insert(pl.all.end(), order.begin(), order.end());
+    pl.n_ic = (int)ic_list.size();
+    pl.n_ics = (int)ic_single.size();
+    for (int i = 0; i < n; i++) pl.maxsm = std::max(pl.maxsm, smem_of(i));
+    cudaError_t e = ensure_smem_attr(pl.maxsm);
     if (e != cudaSuccess) return (int)e;
     if (!ic_list.empty()) {
         int maxn = 0;
-        size_t smax = 0;
         for (int i : ic_list) maxn = std::max(maxn, 4 * hdesc[i].mx * hdesc[i].my);
-        dim3 g((maxn + kThreads - 1) / kThreads, (unsigned)ic_list.size());
-        if (g.x > 64) g.x = 64;
+        pl.ginf = dim3(std::min(64, (maxn + kThreads - 1) / kThreads), (unsigned)ic_list.size());
+        for (int i : ic_single) pl.sm_spec = std::max(pl.sm_spec, smem_of(i));
+    }
+    if (pl.nsingle > 0) {
+        for (int k = 0; k < pl.nsingle; k++) pl.sm_solve = std::max(pl.sm_solve, smem_of(order[k]));
+        int dev = 0, nsm = 0, occ = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
+        if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solve, kThreads, pl.sm_solve)) != cudaSuccess)
+            return (int)e;
+        pl.grid_solve = std::max(1, std::min(pl.nsingle, nsm * std::max(1, occ)));
+    }
+    for (int k = pl.nsingle; k < (int)order.size(); k++) {
+        const int i = order[k];
+        EnginePlan::Group g;
+        g.k = k; g.nblk = hdesc[i].nblk; g.sm = smem_of(i); g.gscr = hdesc[i].gscr; g.ic = compute_ic[i] != 0;
+        pl.groups.push_back(g);
+    }
+    pl.kernels = (pl.n_ic > 0) + (pl.n_ics > 0) + (pl.nsingle > 0);
+    for (const auto &g : pl.groups) pl.kernels += 1 + (g.ic ? 1 : 0);
+    return 0;
+}
+
+int engine_launch(const EnginePlan &pl, PatchDesc *ddesc, int *d_list, cudaStream_t stream, EngineTimer *timer) {
+    if (timer) timer->nlaunch = 0;
+    if (pl.all.empty()) return 0;
+    auto mark = [&](int kind, bool after) {
+        if (!timer || timer->nlaunch >= EngineTimer::kMax) return;
+        cudaEventRecord(timer->ev[2 * timer->nlaunch + (after ? 1 : 0)], stream);
+        if (after) { timer->kind[timer->nlaunch] = kind; timer->nlaunch++; }
+    };
+    cudaError_t e;
+    const int *d_ic = d_list;
+    const int *d_ics = d_list + pl.n_ic;
+    const int *d_order = d_ics + pl.n_ics;
+    if (pl.n_ic > 0) {
         mark(0, false);
-        k_influence<<<g, kThreads, 0, stream>>>(ddesc, d_ic);
+        k_influence<<<pl.ginf, kThreads, 0, stream>>>(ddesc, d_ic);
         mark(0, true);
-        g_launches += 1;
-        if (!ic_single.empty()) {
-            for (int i : ic_single) smax = std::max(smax, smem_of(i));
+        if (pl.n_ics > 0) {
             mark(1, false);
-            k_spectra<<<(unsigned)ic_single.size(), kThreads, smax, stream>>>(ddesc, d_ics, 0);
+            k_spectra<<<(unsigned)pl.n_ics, kThreads, pl.sm_spec, stream>>>(ddesc, d_ics, 0);
             mark(1, true);
-            g_launches += 1;
         }
     }
     // the single-CTA patches: one persistent launch of (co-resident CTAs of the device) CTAs that
     // take the patches from a queue in device memory, largest first; the queue counter follows
     // the lists in d_list
     mark(2, false);
-    if (nsingle > 0) {
-        size_t sm1 = 0;
-        for (int k = 0; k < nsingle; k++) sm1 = std::max(sm1, smem_of(order[k]));
-        int dev = 0, nsm = 0, occ = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return (int)e;
-        if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_solve, kThreads, sm1)) != cudaSuccess)
-            return (int)e;
-        const int grid = std::max(1, std::min(nsingle, nsm * std::max(1, occ)));
-        int *queue = d_list + all.size();
+    if (pl.nsingle > 0) {
+        int *queue = d_list + pl.all.size();
         if ((e = cudaMemsetAsync(queue, 0, sizeof(int), stream)) != cudaSuccess) return (int)e;
-        k_solve<<<grid, kThreads, sm1, stream>>>(ddesc, d_order, 2, nsingle, queue);
-        g_launches += 1;
+        k_solve<<<pl.grid_solve, kThreads, pl.sm_solve, stream>>>(ddesc, d_order, 2, pl.nsingle, queue);
     }
     // patch groups: cooperative launches, one patch at a time on the caller's stream after
     // all single-CTA work, so that nothing else of this library shares the SMs with them
-    for (int k = nsingle; k < (int)order.size(); k++) {
-        const int i = order[k];
-        const PatchDesc &h = hdesc[i];
-        const size_t sm = smem_of(i);
-        if ((e = cudaMemsetAsync(h.gscr, 0, 256, stream)) != cudaSuccess) return (int)e;
-        const int *lp = d_order + k;
+    for (const auto &g : pl.groups) {
+        if ((e = cudaMemsetAsync(g.gscr, 0, 256, stream)) != cudaSuccess) return (int)e;
+        const int *lp = d_order + g.k;
         int grp = 1, nl = 1;
         int *noq = nullptr;
         void *args[5] = {(void *)&ddesc, (void *)&lp, (void *)&grp, (void *)&nl, (void *)&noq};
-        if (compute_ic[i]) {
-            e = cudaLaunchCooperativeKernel((const void *)k_spectra, dim3(h.nblk), dim3(kThreads), args, sm, stream);
+        if (g.ic) {
+            e = cudaLaunchCooperativeKernel((const void *)k_spectra, dim3(g.nblk), dim3(kThreads), args, g.sm, stream);
             if (e != cudaSuccess) return (int)e;
-            if ((e = cudaMemsetAsync(h.gscr, 0, 256, stream)) != cudaSuccess) return (int)e;
-            g_launches += 1;
+            if ((e = cudaMemsetAsync(g.gscr, 0, 256, stream)) != cudaSuccess) return (int)e;
         }
-        e = cudaLaunchCooperativeKernel((const void *)k_solve, dim3(h.nblk), dim3(kThreads), args, sm, stream);
+        e = cudaLaunchCooperativeKernel((const void *)k_solve, dim3(g.nblk), dim3(kThreads), args, g.sm, stream);
         if (e != cudaSuccess) return (int)e;
-        g_launches += 1;
     }
     mark(2, true);
     return (int)cudaGetLastError();
+}
+
+void count_launches(long long k) { g_launches += k; }
+
+int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
+               int *d_list, cudaStream_t stream, EngineTimer *timer) {
+    if (timer) timer->nlaunch = 0;
+    if (n <= 0) return 0;
+    EnginePlan pl;
+    int rc = engine_plan(hdesc, n, compute_ic, pl);
+    if (rc != 0) return rc;
+    cudaError_t e = cudaMemcpyAsync(d_list, pl.all.data(), pl.all.size() * sizeof(int), cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) return (int)e;
+    // the host vector must outlive the asynchronous copy
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return (int)e;
+    rc = engine_launch(pl, ddesc, d_list, stream, timer);
+    if (rc == 0) g_launches += pl.kernels;
+    return rc;
 }
 
 } // namespace cgb

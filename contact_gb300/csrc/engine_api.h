@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <vector>
 #include "engine.h"
 
 namespace cgb {
@@ -52,6 +53,24 @@ struct EngineTimer {
 // All launches of a pass go to 'stream', so passes on different streams run concurrently.
 int engine_run(const PatchDesc *hdesc, PatchDesc *ddesc, int n, const unsigned char *compute_ic,
                int *d_list, cudaStream_t stream, EngineTimer *timer = nullptr);
+
+// engine_run in two parts, for passes that repeat on the same descriptors (the resident batch):
+// engine_plan orders the patches and sizes the launches on the host (plan.all is the content of
+// d_list, to be copied there by the caller); engine_launch only enqueues the pass's kernels on
+// 'stream', with no host synchronisation, so that it can be captured into a CUDA graph.
+struct EnginePlan {
+    std::vector<int> all;               // d_list: influence list, spectra list, solve order
+    int n_ic = 0, n_ics = 0, nsingle = 0, grid_solve = 0, kernels = 0;
+    size_t maxsm = 0, sm_spec = 0, sm_solve = 0;
+    dim3 ginf;
+    struct Group { int k, nblk; size_t sm; void *gscr; bool ic; };
+    std::vector<Group> groups;          // patch groups (cooperative launches)
+};
+int engine_plan(const PatchDesc *hdesc, int n, const unsigned char *compute_ic, EnginePlan &plan);
+int engine_launch(const EnginePlan &plan, PatchDesc *ddesc, int *d_list, cudaStream_t stream,
+                  EngineTimer *timer = nullptr);
+// adds k to the count of kernel launches (launches replayed from a captured graph)
+void count_launches(long long k);
 
 // smallest 2^a 3^b 5^c 7^d >= n, following opt_fft_size (src/m_aijpj.f90:1022-1119)
 int opt_fft_size(int n);

@@ -942,15 +942,50 @@ __device__ inline R dscl_adhesion(const PatchDesc &d, int ix, int jx, R old) {
     return fmin(R(50) * old, dn);
 }
 
+// angle from a to b in (-pi, pi], atan2 of cross and dot product.  For angles below 0.01 rad
+// (the usual case near convergence) the odd series of atan in r = cross / dot up to r^7: its
+// truncation, r^9 / 9, is below 1.2e-17 of the angle, so the value is that of atan2 to rounding
+// at a fraction of its FP64 instructions.
+template <typename R>
+__device__ inline R vec_angle(R ax, R ay, R bx, R by) {
+    const R cr = ax * by - ay * bx, dt = ax * bx + ay * by;
+    if constexpr (sizeof(R) == 8) {
+        if (dt > 0.0 && fabs(cr) < 0.01 * dt) {
+            const double r = cr / dt, r2 = r * r;
+            return r * (1.0 - r2 * (1.0 / 3.0 - r2 * (1.0 / 5.0 - r2 * (1.0 / 7.0))));
+        }
+    }
+    return atan2(cr, dt);
+}
+
+// x^p of the diagonal scaling.  For the default exponent p = 0.9 and moderate x: an FP32 start
+// exp2(0.9 log2 x) refined by two Newton steps on y^10 = x^9 in FP64 (quadratic convergence from
+// ~3e-7: the result is x^0.9 to rounding), in place of the FP64 pow; pow otherwise.
+template <typename R>
+__device__ inline R pow_scaling(R x, R p) {
+    if constexpr (sizeof(R) == 8) {
+        if (p == 0.9 && x >= 1e-30 && x <= 1e30) {
+            const double x2 = x * x, x4 = x2 * x2, c = x4 * x4 * x;
+            double y = (double)exp2f(0.9f * log2f((float)x));
+            for (int k = 0; k < 2; k++) {
+                const double y2 = y * y, y4 = y2 * y2, y9 = y4 * y4 * y, y10 = y9 * y;
+                y = y - (y10 - c) / (10.0 * y9);
+            }
+            return y;
+        }
+    }
+    return pow(x, p);
+}
+
 // angle error of a slip element (perturbed once when it is tiny); returns false if it stays tiny
 template <typename R>
 __device__ inline bool slip_element(const PatchDesc &d, const R coefs[2][2], R px, R py, R pn, R sx, R sy, int &elnew,
                                     R &fac_s) {
     const R tiny_err = R(1e-6), pi = R(3.14159265358979323846), two = R(2);
     const R fstat = (R)d.fstat;
-    // angle from a to b in (-pi, pi]: one atan2 of cross and dot product (the reference takes
-    // the difference of two atan2 values and wraps it)
-    auto angle = [](R ax, R ay, R bx, R by) { return atan2(ax * by - ay * bx, ax * bx + ay * by); };
+    // angle from a to b in (-pi, pi] (the reference takes the difference of two atan2 values
+    // and wraps it)
+    auto angle = [](R ax, R ay, R bx, R by) { return vec_angle<R>(ax, ay, bx, by); };
     (void)pi; (void)two;
     R pr[3] = {px, py, pn};
     R si[2] = {sx, sy};
@@ -1471,7 +1506,7 @@ __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, 
             int elnew = Slip;
             R fac_s = R(0);
             if (!slip_element<R>(d, coefs, (R)C.px[ii], (R)C.py[ii], (R)C.pn[ii], (R)C.sx[ii], (R)C.sy[ii], elnew, fac_s)) ndeg++;
-            else if (elnew == Slip) dscl[ii] = (S)(d_slp * pow(fac_s, pow_s));
+            else if (elnew == Slip) dscl[ii] = (S)(d_slp * pow_scaling<R>(fac_s, pow_s));
             else dscl[ii] = (S)dscl_adhesion<R>(d, ii % mx + 1, jxc[ii], (R)dscl[ii]);
         } else if (el == Adhes) {
             dscl[ii] = (S)dscl_adhesion<R>(d, ii % mx + 1, jxc[ii], (R)dscl[ii]);
@@ -1493,7 +1528,7 @@ __device__ __noinline__ void gd_diagscaling(const PView &P, const GdCols<S> &C, 
                     elnew = e2; fac_s = f2;
                 }
             }
-            if (el == Slip && elnew == Slip) dscl[ii] = (S)(d_slp * pow(fac_s, pow_s));
+            if (el == Slip && elnew == Slip) dscl[ii] = (S)(d_slp * pow_scaling<R>(fac_s, pow_s));
             else if (el == Adhes || elnew == Adhes) dscl[ii] = (S)dscl_adhesion<R>(d, ii % mx + 1, jxc[ii], (R)dscl[ii]);
             else dscl[ii] = S(0);
         }

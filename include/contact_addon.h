@@ -220,6 +220,10 @@ void cntc_gb300_resident_release(void);
  * pass leave idle take the next passes' patches (continuous batching).  times[4r] is then the
  * device time of all nrep passes divided by nrep. */
 void cntc_gb300_resident_depth(int *depth);
+/* extension (no reference counterpart): number of buffer sets of the resident batch whose pass
+ * is replayed from a captured CUDA graph (influence coefficients, spectra and the persistent
+ * solve launch); sets with patch groups launch directly. */
+int cntc_gb300_resident_graphs(void);
 /* extension (no reference counterpart): FMA peaks of the current device, measured with CUDA
  * events: out[0] FP64, out[1] FP32, in TFLOP/s.  The denominators of the patch-solve kernel's
  * arithmetic roofline.  Returns 0, or -1 when a measurement failed. */
