@@ -393,7 +393,7 @@ def kernel_launches():
 
 
 STAT_NAMES = ("nconv32", "nconv64", "nls", "status", "t_total", "t_conv", "t_ls", "t_diag", "t_gs", "t_norm",
-              "t_tang", "t_scan", "t_conv32", "conv_bytes", "t_start_ns", "t_end_ns", "ctas")
+              "t_tang", "t_scan", "t_conv32", "t_gsser", "conv_bytes", "t_start_ns", "t_end_ns", "ctas")
 
 
 def lastcopybytes():

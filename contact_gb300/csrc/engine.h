@@ -31,6 +31,7 @@ enum OutScalar {
     O_NCONV32, O_NCONV64, O_NLS, O_STATUS,
     O_T_TOTAL, O_T_CONV, O_T_LS, O_T_DIAG, O_T_GS, O_T_NORM, O_T_TANG, O_T_SCAN,   // SM clock cycles
     O_T_CONV32,                            // SM cycles in FP32 convolutions (part of O_T_CONV)
+    O_T_GSSER,                             // SM cycles of the serial element steps of SteadyGS (part of O_T_GS)
     O_ALGB,                                // algorithmic bytes of the convolutions (inputs, spectra, outputs)
     O_TSTART, O_TEND,                      // global timer (ns) at the start and end of the solve
     O_CKSI, O_CETA,                        // creepages (solved for when total forces are prescribed)
@@ -91,7 +92,7 @@ struct PatchDesc {
     void *gscr;
 };
 
-constexpr int kNumPhaseTimers = 9;   // O_T_TOTAL .. O_T_CONV32
+constexpr int kNumPhaseTimers = 10;  // O_T_TOTAL .. O_T_GSSER
 constexpr int kIoCols = W_HSTOT;      // W_H .. W_SN live in the io block
 
 __host__ __device__ inline size_t io_doubles(int npot) {

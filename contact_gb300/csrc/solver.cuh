@@ -612,14 +612,281 @@ __device__ inline void stdygs_rowsum32(const PView &P, const GsBox &b, int ii, c
     s[1] = a[1] / d.ga;
 }
 
+constexpr int kGsPad = 16;
+
+// Warp-cooperative SteadyGS element step of the row-blocked form, run by the lead warp for
+// element ii (column ix, row iy) with its shift s0, s1 (valid in lane 0, without the rigid
+// shift):
+//   - the column jx that closes the element's coefficient (the nearest column behind ix whose
+//     element is not in adhesion, the trailing column if there is none) by a warp ballot;
+//   - the element solve (plstrc) by lane 0 with the coefficients of its column offset ix - jx,
+//     taken from the table ctab (the reference's expression, evaluated once per offset);
+//   - the carry of the new traction towards the trailing edge through the adhesion elements
+//     behind it, up to and including the first element that is not in adhesion (which keeps its
+//     traction and absorbs the change in its dp): the carried tractions are FP64 prefix sums of
+//     dp over 32 columns at a time; at the first column whose carried traction exceeds its bound
+//     the traction is clipped, that column takes a new dp and the sums restart behind it.
+// Every change of dp is recorded in the row's FP32 change rd (dp - dp_b).  GB300 charges an
+// FP64 instruction per warp whatever the number of active lanes, so the carry costs a few
+// warp-wide FP64 instructions per 32 columns instead of several per column.  Returns (lane 0)
+// the squared change of the element's traction.
+__device__ inline double gs_element_warp(const PView &P, int ii, int ix, int iy, double s0, double s1, double eps,
+                                         double omegah, double omegas, const double *ctab, float *rdx, float *rdy,
+                                         const double *dbx, const double *dby, int lane) {
+    const PatchDesc &d = *P.d;
+    const int mx = P.mx;
+    const int ixsta = 1;
+    int *igs = P.igs();
+    double *px = P.c(W_PX), *py = P.c(W_PY);
+    const double *pn = P.c(W_PN);
+    double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY);
+    const double *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+    double *sx = P.c(W_SX), *sy = P.c(W_SY);
+    const double mus = d.fstat;
+    const int row0 = (iy - 1) * mx - 1;        // element index of column kx: row0 + kx
+    const unsigned all = 0xffffffffu;
+    int jx = ixsta;
+    for (int base = ix - 1; base >= ixsta; base -= 32) {
+        const int kx = base - lane;
+        const unsigned b = __ballot_sync(all, kx >= ixsta && igs[row0 + kx] != Adhes);
+        if (b) { jx = base - (__ffs(b) - 1); break; }
+    }
+    double dif2 = 0.0, pxn = 0.0, pyn = 0.0;
+    int eln = 0;
+    if (lane == 0) {
+        const int o = ix - jx;
+        double coef[2][2];
+        coef[0][0] = ctab[o];
+        coef[0][1] = ctab[mx + o];
+        coef[1][0] = coef[0][1];
+        coef[1][1] = ctab[2 * mx + o];
+        double s[2] = {s0 + wsx[ii], s1 + wsy[ii]};
+        double pr[3] = {px[ii], py[ii], pn[ii]};
+        int el = igs[ii];
+        elm_solve(el, coef, eps, omegah, omegas, pr, mus, s);
+        igs[ii] = el;
+        dif2 = (pr[0] - px[ii]) * (pr[0] - px[ii]) + (pr[1] - py[ii]) * (pr[1] - py[ii]);
+        dpx[ii] += pr[0] - px[ii];
+        dpy[ii] += pr[1] - py[ii];
+        px[ii] = pr[0]; py[ii] = pr[1];
+        sx[ii] = s[0]; sy[ii] = s[1];
+        rdx[kGsPad + ix - 1] = (float)(dpx[ii] - dbx[ii]);
+        rdy[kGsPad + ix - 1] = (float)(dpy[ii] - dby[ii]);
+        pxn = pr[0]; pyn = pr[1]; eln = el;
+    }
+    pxn = __shfl_sync(all, pxn, 0);
+    pyn = __shfl_sync(all, pyn, 0);
+    eln = __shfl_sync(all, eln, 0);
+    __syncwarp();
+    int base = ix - 1;
+    while (base >= ixsta) {
+        const int kx = base - lane;
+        const bool valid = kx >= ixsta;
+        const int kk = row0 + kx;
+        const int ek = valid ? igs[kk] : Exter;
+        // the chain: the lanes before the first one that is not in adhesion (or past the edge)
+        const unsigned stop = __ballot_sync(all, !valid || ek != Adhes);
+        const int e = stop ? __ffs(stop) - 1 : 32;
+        const bool chain = lane < e;
+        double ax = chain ? dpx[kk] : 0.0, ay = chain ? dpy[kk] : 0.0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double tx = __shfl_up_sync(all, ax, o), ty = __shfl_up_sync(all, ay, o);
+            if (lane >= o) { ax += tx; ay += ty; }
+        }
+        const double qx = pxn + ax, qy = pyn + ay;
+        // traction in front of each lane: the carried traction of the lane before it
+        double fx = __shfl_up_sync(all, qx, 1), fy = __shfl_up_sync(all, qy, 1);
+        if (lane == 0) { fx = pxn; fy = pyn; }
+        double ptbnd = 0.0;
+        bool viol = false;
+        if (chain) {
+            ptbnd = mus * pn[kk];
+            viol = qx * qx + qy * qy > ptbnd * ptbnd;
+        }
+        const unsigned vb = __ballot_sync(all, viol);
+        const int v = vb ? __ffs(vb) - 1 : 32;
+        if (chain && lane < v) { px[kk] = qx; py[kk] = qy; }
+        if (v < e) {
+            // clipped to the traction bound (|p| > bound compared in squares)
+            double cx = 0.0, cy = 0.0;
+            if (lane == v) {
+                const double f = ptbnd * inv_sqrt(qx * qx + qy * qy);
+                cx = qx * f; cy = qy * f;
+                px[kk] = cx; py[kk] = cy;
+                dpx[kk] = cx - fx; dpy[kk] = cy - fy;
+                rdx[kGsPad + kx - 1] = (float)(dpx[kk] - dbx[kk]);
+                rdy[kGsPad + kx - 1] = (float)(dpy[kk] - dby[kk]);
+            }
+            pxn = __shfl_sync(all, cx, v);
+            pyn = __shfl_sync(all, cy, v);
+            eln = Adhes;
+            base -= v + 1;
+            __syncwarp();
+            continue;
+        }
+        if (e < 32) {
+            // lane e ends the carry
+            const int efront = e == 0 ? eln : Adhes;
+            if (lane == e && valid) {
+                bool ch = false;
+                if (ek == Slip || ek == Plast) { dpx[kk] = px[kk] - fx; dpy[kk] = py[kk] - fy; ch = true; }
+                else if (efront >= Adhes) { dpx[kk] = -fx; dpy[kk] = -fy; ch = true; }
+                if (ch) {
+                    rdx[kGsPad + kx - 1] = (float)(dpx[kk] - dbx[kk]);
+                    rdy[kGsPad + kx - 1] = (float)(dpy[kk] - dby[kk]);
+                }
+            }
+            break;
+        }
+        // all 32 columns in adhesion and within their bounds: on to the next 32
+        pxn = __shfl_sync(all, qx, 31);
+        pyn = __shfl_sync(all, qy, 31);
+        eln = Adhes;
+        base -= 32;
+        __syncwarp();
+    }
+    __syncwarp();
+    return dif2;
+}
+
+// Row-blocked form of the mixed-precision SteadyGS sweep.  An element's shift within a sweep is
+// s_b (the FP64 product of dp_b at the start of the sweep) plus A times the change dp - dp_b
+// made so far in the sweep.  That change lives in the rows already swept and in the current
+// row only, so the shift splits into
+//   - the rows above: after a row is finished, its change is applied to an FP32 accumulator of
+//     every element of the rows below it (gs_row_update, spread over the whole patch group,
+//     register tiles of kGsTile elements along x with a sliding window of coefficients), and
+//   - the current row: a sum over that row's change, held in shared memory, by one warp
+//     (gs_inrow_sum), with no block-wide barrier per element.
+// Both parts are FP32 products of the sweep's change (which tends to zero as the sweep
+// converges); they are added to the FP64 s_b in FP64.  Shared memory (the convolution's batch buffer, free between products):
+// coefficient row dy = 0 of blocks xx, xy, yy (3 x 2 mx floats) and the current row's change
+// (2 x (mx + 2 kGsPad) floats, zero outside the row).
+constexpr int kGsTile = 8;
+
+// bytes: ctab (3 mx doubles), c0 (6 mx floats), rdx and rdy (mx + 2 kGsPad floats each)
+__host__ __device__ inline size_t gs_rows_smem_bytes(int mx) {
+    return (size_t)24 * mx + 4 * ((size_t)6 * mx + 2 * ((size_t)mx + 2 * kGsPad));
+}
+
+// (s0, s1) = sum over jx in [j0, j1] of A(ix - jx, 0) dd(jx) (without the factor ga_inv), FP32
+// products and sums; lane 0 returns the sum
+__device__ inline void gs_inrow_sum(const float *c0, const float *rdx, const float *rdy, int ix, int j0, int j1, int mx,
+                                    int lane, float &s0, float &s1) {
+    const float *cxx = c0, *cxy = c0 + 2 * mx, *cyy = c0 + 4 * mx;
+    float a0 = 0.f, a1 = 0.f;
+    for (int jx = j0 + lane; jx <= j1; jx += 32) {
+        const int k = ix - jx + mx;
+        const float vx = rdx[kGsPad + jx - 1], vy = rdy[kGsPad + jx - 1], c01 = cxy[k];
+        a0 = fmaf(cxx[k], vx, fmaf(c01, vy, a0));
+        a1 = fmaf(c01, vx, fmaf(cyy[k], vy, a1));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_down_sync(0xffffffffu, a0, o);
+        a1 += __shfl_down_sync(0xffffffffu, a1, o);
+    }
+    s0 = a0; s1 = a1;
+}
+
+// four coefficients c[k .. k + 3] of one coefficient row (k + q outside [0, kmax] read as 0;
+// a float4 load when all four are inside and aligned, which the caller arranges)
+__device__ inline float4 gs_coef4(const float *r, int k, int kmax) {
+    if (k >= 0 && k + 3 <= kmax) return *reinterpret_cast<const float4 *>(r + k);
+    float4 v;
+    v.x = (k + 0 >= 0 && k + 0 <= kmax) ? r[k + 0] : 0.f;
+    v.y = (k + 1 >= 0 && k + 1 <= kmax) ? r[k + 1] : 0.f;
+    v.z = (k + 2 >= 0 && k + 2 <= kmax) ? r[k + 2] : 0.f;
+    v.w = (k + 3 >= 0 && k + 3 <= kmax) ? r[k + 3] : 0.f;
+    return v;
+}
+
+// acc(t) += sum_jx A(t - (jx, iy)) dd(jx) for the elements t of the rows below iy within
+// the box, row by row in tiles of kGsTile elements along x.  Per tile the sum runs over jx from
+// high to low, so that the coefficient index k = tx - jx + mx rises by one per step and member m
+// of the tile reads c[k + m]: the coefficients sit in a window of kGsWin registers per block
+// (xx, xy, yy), refilled four at a time (float4 loads) right after their last use.  The loads
+// are aligned by starting the sum up to three columns above j1.  Columns outside [j0, j1] carry
+// dd = 0 (the zero padding of the row buffer), so their coefficients only need to be finite:
+// they are read inside the coefficient row or as zeros.
+constexpr int kGsWin = 2 * kGsTile;
+
+__device__ __noinline__ void gs_row_update(const PView &P, const GsBox &box, int iy, int j0, int j1, const float *rdx,
+                                           const float *rdy, const float *cf32, float *accx, float *accy) {
+    const int mx = P.mx, my = P.my;
+    const int *ext = P.ci(I_EXT);
+    const size_t bsz = (size_t)4 * mx * my;
+    const int jy1 = box.jy0 + box.cnt / max(box.w, 1) - 1;
+    if (box.cnt == 0 || iy >= jy1) return;
+    const int ntile = (box.w + kGsTile - 1) / kGsTile;
+    const int items = (jy1 - iy) * ntile;
+    const int kmax = 2 * mx - 1;
+    const int m0 = (int)(((uintptr_t)cf32 >> 2) & 3);
+    for (int it = gtid(); it < items; it += gstride()) {
+        const int ty = iy + 1 + it / ntile;
+        const int tx0 = box.jx0 + kGsTile * (it % ntile);
+        const int t0 = ext[ty - 1], t1 = ext[my + ty - 1];
+        if (t1 < t0 || tx0 > t1 || tx0 + kGsTile - 1 < t0) continue;
+        const int rb = (ty - iy + my) * 2 * mx;
+        const float *rxx = cf32 + rb, *rxy = cf32 + bsz + rb, *ryy = cf32 + 2 * bsz + rb;
+        const int e = (((m0 + rb + tx0 - j1 + mx) % 4) + 4) % 4;
+        const int jstart = j1 + e;
+        const int nround = (jstart - j0 + kGsWin) / kGsWin;
+        int k = tx0 - jstart + mx;
+        float wxx[kGsWin], wxy[kGsWin], wyy[kGsWin], a0[kGsTile], a1[kGsTile];
+#pragma unroll
+        for (int q = 0; q < kGsWin; q += 4) {
+            const float4 u = gs_coef4(rxx, k + q, kmax), v = gs_coef4(rxy, k + q, kmax), w = gs_coef4(ryy, k + q, kmax);
+            wxx[q] = u.x; wxx[q + 1] = u.y; wxx[q + 2] = u.z; wxx[q + 3] = u.w;
+            wxy[q] = v.x; wxy[q + 1] = v.y; wxy[q + 2] = v.z; wxy[q + 3] = v.w;
+            wyy[q] = w.x; wyy[q + 1] = w.y; wyy[q + 2] = w.z; wyy[q + 3] = w.w;
+        }
+#pragma unroll
+        for (int m = 0; m < kGsTile; m++) { a0[m] = 0.f; a1[m] = 0.f; }
+        const float *vxp = rdx + kGsPad + jstart - 1, *vyp = rdy + kGsPad + jstart - 1;
+        for (int r = 0; r < nround; r++) {
+#pragma unroll
+            for (int s = 0; s < kGsWin; s++) {
+                const float vx = vxp[-s], vy = vyp[-s];
+#pragma unroll
+                for (int m = 0; m < kGsTile; m++) {
+                    const int q = (s + m) % kGsWin;
+                    a0[m] = fmaf(wxx[q], vx, fmaf(wxy[q], vy, a0[m]));
+                    a1[m] = fmaf(wxy[q], vx, fmaf(wyy[q], vy, a1[m]));
+                }
+                if (s % 4 == 3) {
+                    // slots s - 3 .. s (offsets s - 3 .. s) are used for the last time at this
+                    // step; they take offsets kGsWin + s - 3 .. kGsWin + s
+                    const int q0 = s - 3;
+                    const int kk = k + kGsWin + q0;
+                    const float4 u = gs_coef4(rxx, kk, kmax), v = gs_coef4(rxy, kk, kmax), w = gs_coef4(ryy, kk, kmax);
+                    wxx[q0] = u.x; wxx[q0 + 1] = u.y; wxx[q0 + 2] = u.z; wxx[q0 + 3] = u.w;
+                    wxy[q0] = v.x; wxy[q0 + 1] = v.y; wxy[q0 + 2] = v.z; wxy[q0 + 3] = v.w;
+                    wyy[q0] = w.x; wyy[q0 + 1] = w.y; wyy[q0 + 2] = w.z; wyy[q0 + 3] = w.w;
+                }
+            }
+            vxp -= kGsWin; vyp -= kGsWin;
+            k += kGsWin;
+        }
+#pragma unroll
+        for (int m = 0; m < kGsTile; m++) {
+            const int tx = tx0 + m;
+            if (tx >= t0 && tx <= t1) {
+                const size_t t = (size_t)(tx - 1) + (size_t)(ty - 1) * mx;
+                accx[t] += a0[m];
+                accy[t] += a1[m];
+            }
+        }
+    }
+}
+
 // SteadyGS, m_solvpt.f90:2825-3254.  o64 (mixed precision): each sweep starts from an FP64
 // product s_b = A dp_b of the current dp (one FFT convolution); an element's shift within the
-// sweep is s_b plus the FP32 row sum of the change dp - dp_b made so far in the sweep, so that
-// the shift keeps FP64 accuracy up to the FP32 rounding of that change.
-// After an element is solved its new traction is carried towards the trailing edge through
-// the adhesion elements behind it, up to and including the first element that is not in
-// adhesion: that element keeps its traction and absorbs the change in its dp, so the elements
-// behind it keep the values that the last carry through it gave them.
+// sweep is s_b plus the FP32 product of the change dp - dp_b made so far in the sweep, so that
+// the shift keeps FP64 accuracy up to the FP32 rounding of that change.  The mixed form runs
+// row-blocked (gs_row_update) when the row buffers fit the convolution's shared batch buffer,
+// element-wise (one group-wide row sum per element) otherwise and in the FP64 form.
 __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double omegah, double omegas, int &info,
                                    double &err, const Ops<double> *o64 = nullptr, const double *p0x = nullptr,
                                    const double *p0y = nullptr) {
@@ -628,11 +895,9 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
     const int mx = P.mx, my = P.my, n = P.n;
     RedSmem &red = P.sm->red;
     int *igs = P.igs();
-    double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN);
-    double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY), *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
-    double *sx = P.c(W_SX), *sy = P.c(W_SY);
+    double *px = P.c(W_PX), *py = P.c(W_PY);
+    double *dpx = P.c(W_DPX), *dpy = P.c(W_DPY);
     const size_t bsz = (size_t)4 * mx * my;
-    const double mus = d.fstat;
     const int ixsta = 1, ixinc = 1, ixend = mx;
     const bool mix = o64 != nullptr;
     // mixed: FP32 coefficients xx, xy, yy (6 double columns from W_FST), the FP32 change (one
@@ -640,6 +905,17 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
     float *cf32 = (float *)P.c(W_FST);
     float *ddx = (float *)P.c(W_FST + 6), *ddy = ddx + n;
     double *dbx = P.c(W_DBX), *dby = P.c(W_DBY), *sbx = P.c(W_SBX), *sby = P.c(W_SBY);
+    // row-blocked form: FP32 sums of the rows' changes so far in the sweep (column W_TX)
+    float *accx = (float *)P.c(W_TX), *accy = accx + n;
+    const bool rows = mix && gs_rows_smem_bytes(mx) <= (size_t)o64->cv.ccap * sizeof(C<double>);
+    double *ctab = nullptr;
+    float *c0 = nullptr, *rdx = nullptr, *rdy = nullptr;
+    if (rows) {
+        ctab = (double *)o64->cv.cbuf;
+        c0 = (float *)(ctab + 3 * mx);
+        rdx = c0 + 6 * mx;
+        rdy = rdx + mx + 2 * kGsPad;
+    }
     if (mix) {
         for (int t = gtid(); t < (int)(3 * bsz); t += gstride()) cf32[t] = (float)d.cf[t];
     }
@@ -654,82 +930,139 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
     double facnel = sqrt((double)(float)n / (double)(float)k);
     // bounding box of the row extents (constant: the contact area does not change in TANG)
     const GsBox box = gs_box(P);
+    const int *ext = P.ci(I_EXT);
     int itgs = 0;
     double dif = 2.0, difid = 1.0, dif1 = 0.0;
     while (dif >= difid && itgs < maxgs) {
         itgs++;
         if (mix) {
-            FOR_I(i, n) { dbx[i] = dpx[i]; dby[i] = dpy[i]; ddx[i] = 0.f; ddy[i] = 0.f; }
+            FOR_I(i, n) { dbx[i] = dpx[i]; dby[i] = dpy[i]; ddx[i] = 0.f; ddy[i] = 0.f; accx[i] = 0.f; accy[i] = 0.f; }
             prod_t<double>(*o64, dbx, dby, sbx, sby, OUT_ALL, igs);
         }
         double difacc = 0.0;      // held by the group's lead thread
-        for (int iy = 1; iy <= my; iy++) {
-            for (int ix = ixsta; ix <= ixend; ix++) {
-                int ii = (ix - 1) + (iy - 1) * mx;
-                if (igs[ii] < Adhes) continue;
-                double s[2];
-                if (mix) stdygs_rowsum32(P, box, ii, cf32, ddx, ddy, s);
-                else stdygs_rowsum(P, box, ii, dpx, dpy, s);
-                if (glead() && ix > ixsta) {
-                    if (mix) { s[0] += sbx[ii]; s[1] += sby[ii]; }
-                    // the solver choice keeps the trailing column ix = 1 outside the contact area
-                    int jx = ix - ixinc;
-                    int jj = (jx - 1) + (iy - 1) * mx;
-                    while (igs[jj] == Adhes && jx != ixsta) { jx -= ixinc; jj = (jx - 1) + (iy - 1) * mx; }
-                    const size_t o0 = (size_t)(0 + mx) + (size_t)(0 + my) * 2 * mx;
-                    const size_t oj = (size_t)(jx - ix + mx) + (size_t)(0 + my) * 2 * mx;
-                    double coef[2][2];
-                    coef[0][0] = (d.cf[0 * bsz + o0] - d.cf[0 * bsz + oj]) / d.ga;
-                    coef[0][1] = (d.cf[1 * bsz + o0] - d.cf[1 * bsz + oj]) / d.ga;
-                    coef[1][0] = coef[0][1];
-                    coef[1][1] = (d.cf[2 * bsz + o0] - d.cf[2 * bsz + oj]) / d.ga;
-                    s[0] += wsx[ii]; s[1] += wsy[ii];
-                    double pr[3] = {px[ii], py[ii], pn[ii]};
-                    int el = igs[ii];
-                    elm_solve(el, coef, eps, omegah, omegas, pr, mus, s);
-                    igs[ii] = el;
-                    difacc += (pr[0] - px[ii]) * (pr[0] - px[ii]) + (pr[1] - py[ii]) * (pr[1] - py[ii]);
-                    dpx[ii] += pr[0] - px[ii];
-                    dpy[ii] += pr[1] - py[ii];
-                    px[ii] = pr[0]; py[ii] = pr[1];
-                    sx[ii] = s[0]; sy[ii] = s[1];
-                    if (mix) { ddx[ii] = (float)(dpx[ii] - dbx[ii]); ddy[ii] = (float)(dpy[ii] - dby[ii]); }
-                    // carry the new traction of element ii towards the trailing edge: p of an
-                    // adhesion element is the sum of the p in front of it and its dp (clipped to
-                    // the bound); the first element that is not in adhesion takes a new dp and
-                    // ends the carry.  The traction in front (pxn, pyn) and its element type are
-                    // carried in registers.
-                    double pxn = px[ii], pyn = py[ii];
-                    int eln = igs[ii];
-                    for (int kx = ix - ixinc; kx >= ixsta; kx -= ixinc) {
-                        const int kk = (kx - 1) + (iy - 1) * mx;
-                        const int el = igs[kk];
-                        if (el == Adhes) {
-                            const double qx = pxn + dpx[kk], qy = pyn + dpy[kk];
-                            const double pp = qx * qx + qy * qy, ptbnd = mus * pn[kk];
-                            if (pp > ptbnd * ptbnd) {
-                                // clipped to the traction bound (|p| > bound compared in squares)
-                                const double f = ptbnd * inv_sqrt(pp);
-                                const double cx = qx * f, cy = qy * f;
-                                px[kk] = cx; py[kk] = cy;
-                                dpx[kk] = cx - pxn; dpy[kk] = cy - pyn;
-                                pxn = cx; pyn = cy;
-                            } else {
-                                px[kk] = qx; py[kk] = qy;
-                                pxn = qx; pyn = qy;
-                            }
-                        } else if (el == Slip || el == Plast) {
-                            const double cx = px[kk], cy = py[kk];
-                            dpx[kk] = cx - pxn; dpy[kk] = cy - pyn;
-                        } else if (eln >= Adhes) {
-                            dpx[kk] = -pxn; dpy[kk] = -pyn;
+        if (rows) {
+            // coefficient row dy = 0 in shared memory (the product above used the buffer), and the
+            // element coefficients per column offset o = ix - jx (1 .. mx - 1)
+            const float *cr = cf32 + (size_t)my * 2 * mx;
+            for (int t = threadIdx.x; t < 2 * mx; t += blockDim.x) {
+                c0[t] = cr[t]; c0[2 * mx + t] = cr[bsz + t]; c0[4 * mx + t] = cr[2 * bsz + t];
+            }
+            {
+                const size_t o0 = (size_t)(0 + mx) + (size_t)(0 + my) * 2 * mx;
+                for (int t = threadIdx.x; t < 3 * mx; t += blockDim.x) {
+                    const int c = t / mx, o = t % mx;
+                    const size_t oj = (size_t)(-o + mx) + (size_t)(0 + my) * 2 * mx;
+                    ctab[t] = o == 0 ? 0.0 : (d.cf[c * bsz + o0] - d.cf[c * bsz + oj]) / d.ga;
+                }
+            }
+            const double gainv = 1.0 / d.ga;
+            const bool lead_warp = g_grp.rank == 0 && threadIdx.x < 32;
+            const int lane = threadIdx.x & 31;
+            for (int iy = 1; iy <= my; iy++) {
+                const int j0 = max(1, ext[iy - 1] - 1), j1 = min(mx, ext[my + iy - 1] + 1);
+                if (j0 > j1) continue;
+                for (int t = threadIdx.x; t < mx + 2 * kGsPad; t += blockDim.x) { rdx[t] = 0.f; rdy[t] = 0.f; }
+                __syncthreads();
+                if (lead_warp) {
+                    const long long tser = clock64();
+                    for (int ix = max(j0, ixsta + 1); ix <= j1; ix++) {
+                        const int ii = (ix - 1) + (iy - 1) * mx;
+                        if (igs[ii] < Adhes) continue;
+                        float r0, r1;
+                        gs_inrow_sum(c0, rdx, rdy, ix, j0, j1, mx, lane, r0, r1);
+                        double s0 = 0.0, s1 = 0.0;
+                        if (lane == 0) {
+                            s0 = ((double)accx[ii] + (double)r0) * gainv + sbx[ii];
+                            s1 = ((double)accy[ii] + (double)r1) * gainv + sby[ii];
                         }
-                        if (mix) { ddx[kk] = (float)(dpx[kk] - dbx[kk]); ddy[kk] = (float)(dpy[kk] - dby[kk]); }
-                        if (el != Adhes) break;
-                        eln = el;
+                        difacc += gs_element_warp(P, ii, ix, iy, s0, s1, eps, omegah, omegas, ctab, rdx, rdy, dbx,
+                                                  dby, lane);
                     }
+                    // a patch group: the row's change goes to the other CTAs through global memory
+                    if (g_grp.nblk > 1)
+                        for (int jx = j0 + lane; jx <= j1; jx += 32) {
+                            const int jj = (jx - 1) + (iy - 1) * mx;
+                            ddx[jj] = rdx[kGsPad + jx - 1]; ddy[jj] = rdy[kGsPad + jx - 1];
+                        }
+                    if (lane == 0) P.sm->t[O_T_GSSER - O_T_TOTAL] += clock64() - tser;
                 }
                 gsync();
+                if (g_grp.nblk > 1 && g_grp.rank != 0) {
+                    for (int jx = j0 + (int)threadIdx.x; jx <= j1; jx += blockDim.x) {
+                        const int jj = (jx - 1) + (iy - 1) * mx;
+                        rdx[kGsPad + jx - 1] = ddx[jj]; rdy[kGsPad + jx - 1] = ddy[jj];
+                    }
+                    __syncthreads();
+                }
+                gs_row_update(P, box, iy, j0, j1, rdx, rdy, cf32, accx, accy);
+                gsync();
+            }
+        } else {
+            for (int iy = 1; iy <= my; iy++) {
+                for (int ix = ixsta; ix <= ixend; ix++) {
+                    int ii = (ix - 1) + (iy - 1) * mx;
+                    if (igs[ii] < Adhes) continue;
+                    double s[2];
+                    if (mix) stdygs_rowsum32(P, box, ii, cf32, ddx, ddy, s);
+                    else stdygs_rowsum(P, box, ii, dpx, dpy, s);
+                    if (glead() && ix > ixsta) {
+                        if (mix) { s[0] += sbx[ii]; s[1] += sby[ii]; }
+                        double *pn = P.c(W_PN), *sx = P.c(W_SX), *sy = P.c(W_SY);
+                        const double *wsx = P.c(W_WSX), *wsy = P.c(W_WSY);
+                        const double mus = d.fstat;
+                        // the solver choice keeps the trailing column ix = 1 outside the contact area
+                        int jx = ix - ixinc;
+                        int jj = (jx - 1) + (iy - 1) * mx;
+                        while (igs[jj] == Adhes && jx != ixsta) { jx -= ixinc; jj = (jx - 1) + (iy - 1) * mx; }
+                        const size_t o0 = (size_t)(0 + mx) + (size_t)(0 + my) * 2 * mx;
+                        const size_t oj = (size_t)(jx - ix + mx) + (size_t)(0 + my) * 2 * mx;
+                        double coef[2][2];
+                        coef[0][0] = (d.cf[0 * bsz + o0] - d.cf[0 * bsz + oj]) / d.ga;
+                        coef[0][1] = (d.cf[1 * bsz + o0] - d.cf[1 * bsz + oj]) / d.ga;
+                        coef[1][0] = coef[0][1];
+                        coef[1][1] = (d.cf[2 * bsz + o0] - d.cf[2 * bsz + oj]) / d.ga;
+                        s[0] += wsx[ii]; s[1] += wsy[ii];
+                        double pr[3] = {px[ii], py[ii], pn[ii]};
+                        int el = igs[ii];
+                        elm_solve(el, coef, eps, omegah, omegas, pr, mus, s);
+                        igs[ii] = el;
+                        difacc += (pr[0] - px[ii]) * (pr[0] - px[ii]) + (pr[1] - py[ii]) * (pr[1] - py[ii]);
+                        dpx[ii] += pr[0] - px[ii];
+                        dpy[ii] += pr[1] - py[ii];
+                        px[ii] = pr[0]; py[ii] = pr[1];
+                        sx[ii] = s[0]; sy[ii] = s[1];
+                        if (mix) { ddx[ii] = (float)(dpx[ii] - dbx[ii]); ddy[ii] = (float)(dpy[ii] - dby[ii]); }
+                        double pxn = px[ii], pyn = py[ii];
+                        int eln = igs[ii];
+                        for (int kx = ix - ixinc; kx >= ixsta; kx -= ixinc) {
+                            const int kk = (kx - 1) + (iy - 1) * mx;
+                            const int ek = igs[kk];
+                            if (ek == Adhes) {
+                                const double qx = pxn + dpx[kk], qy = pyn + dpy[kk];
+                                const double pp = qx * qx + qy * qy, ptbnd = mus * pn[kk];
+                                if (pp > ptbnd * ptbnd) {
+                                    const double f = ptbnd * inv_sqrt(pp);
+                                    const double cx = qx * f, cy = qy * f;
+                                    px[kk] = cx; py[kk] = cy;
+                                    dpx[kk] = cx - pxn; dpy[kk] = cy - pyn;
+                                    pxn = cx; pyn = cy;
+                                } else {
+                                    px[kk] = qx; py[kk] = qy;
+                                    pxn = qx; pyn = qy;
+                                }
+                            } else if (ek == Slip || ek == Plast) {
+                                const double cx = px[kk], cy = py[kk];
+                                dpx[kk] = cx - pxn; dpy[kk] = cy - pyn;
+                            } else if (eln >= Adhes) {
+                                dpx[kk] = -pxn; dpy[kk] = -pyn;
+                            }
+                            if (mix) { ddx[kk] = (float)(dpx[kk] - dbx[kk]); ddy[kk] = (float)(dpy[kk] - dby[kk]); }
+                            if (ek != Adhes) break;
+                            eln = ek;
+                        }
+                    }
+                    gsync();
+                }
             }
         }
         // the lead thread's sum, broadcast to the group (the other threads add zeros)

@@ -24,9 +24,10 @@ def ctas(cntc, ire, icp=1):
     return int(cntc.getsolverstats(ire, icp)["ctas"])
 
 
-@pytest.mark.parametrize("gausei,eps,mixed", [(5, 1e-10, 0), (5, 1e-10, 1), (0, 1e-6, 0)])
+@pytest.mark.parametrize("gausei,eps,mixed", [(5, 1e-10, 0), (5, 1e-10, 1), (0, 1e-6, 0), (0, 1e-10, 1)])
 def test_group_hertz_51_matches_oracle(cntc, oracle, gausei, eps, mixed):
-    """The 51x51 Hertzian case (GDsteady, GDsteady mixed, SteadyGS) solved by 8 CTAs."""
+    """The 51x51 Hertzian case (GDsteady, GDsteady mixed, SteadyGS, SteadyGS mixed) solved by 8
+    CTAs."""
     case = C.config0(gausei=gausei, eps=eps, mixed=mixed)
     g = run_gpu(cntc, dict(case, group=GROUP), ire=70)
     assert ctas(cntc, 70) == GROUP

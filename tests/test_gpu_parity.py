@@ -81,6 +81,21 @@ def test_hertz_steady_rolling_mixed(cntc, oracle):
     assert st["nconv32"] > 0 and st["nconv64"] > 0
 
 
+@pytest.mark.parametrize("mx,my", [(51, 51), (64, 40), (33, 97)])
+def test_steadygs_mixed_rows(cntc, oracle, mx, my):
+    """SteadyGS in the mixed form (an FP64 product per sweep, the sweep's own change applied in
+    FP32 row by row) against the FP64 oracle: same classification, forces within 1e-8."""
+    case = C.config0(gausei=0, eps=1e-10, mx=mx, my=my, mixed=1)
+    g = run_gpu(cntc, case)
+    o = C.oracle_solve(dict(case, mixed=0))
+    assert o["ierror"] == 0 and o["solver"] == 4 and g["solver"] == 4
+    assert_parity(g, o, case, force_tol=MIXED_FORCE_TOL, trac_tol=TRAC_TOL, iterations=False)
+    assert cntc.getsolverstats(1, 1)["t_gs"] > 0
+    # the sweeps are the reference's: the sweep count follows the FP64 one (a sweep that dropped
+    # part of the in-sweep update would still converge, but in many more sweeps)
+    assert abs(g["itgs"] - o["itgs"]) <= 2, (g["itgs"], o["itgs"])
+
+
 @pytest.mark.parametrize("tang,dq", [(1, None), (2, 0.2)])
 def test_tangcg_shift_and_transient(cntc, oracle, tang, dq):
     """TangCG for shift (T=1) and transient rolling (T=2)."""
