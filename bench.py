@@ -330,6 +330,7 @@ def run_gb300(args, dist):
     kernels_per_pass = int(round(times[-1, 3]))
     graph_sets = rb.graphs()
     peak, peak_kind = measured_peaks()
+    fmap = cg.fma_peaks()
     achieved = alg / (solve_ms / 1e3) / 1e9
     rb.release()
 
@@ -404,10 +405,13 @@ def run_gb300(args, dist):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "kernel": "k_solve",
                      "kernels_per_step": kernels_per_pass, "peak_source": peak_kind,
-                     "note": "k_solve is bound by the FP64 pipe (53 % busy in profiles/"
-                             "k_solve_batch8_side64_full.md), not by HBM: one patch's working set stays in L1/L2; "
+                     "note": "k_solve is bound by the FP64 pipe (49 % busy with one CTA per SM in profiles/"
+                             "k_solve_mixed_side64_full.md), not by HBM: one patch's working set stays in L1/L2; "
                              "achieved = algorithmic bytes (convolution inputs, spectra and outputs, and the "
                              "iterations' vector passes) / patch-solve kernel time"},
+        "fma_peaks": dict(fmap, note="FMA-chain peaks of this GPU timed with CUDA events on all SMs; k_solve's "
+                                   "FP64 pipe is 49 % active with one CTA per SM (ncu, profiles/"
+                                   "k_solve_mixed_side64_full.md)"),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                 "errors": int((np.asarray(e_err) < 0).sum()),

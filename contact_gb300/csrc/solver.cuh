@@ -409,8 +409,13 @@ __device__ __noinline__ int snorm(const PView &P, const Ops<T> &op, int maxgs, i
 // single-element solver plstrc for an elastic element (m_solvpt.f90:3278-3807, no plasticity;
 // the plastic trial of the reference cannot succeed there and leaves the element in adhesion)
 // ------------------------------------------------------------------------------------------
-template <typename R>
-__device__ __noinline__ void elm_solve(int &el, const R coef[2][2], R eps, R omegah, R omegas, R pr[3], R mus, R s[2]) {
+// kF32Start (the mixed-precision SteadyGS): the slip Newton-Raphson first runs in FP32 from the
+// reference's starting point to FP32 accuracy, and the FP64 iteration continues from there with
+// the reference's stopping rule (one or two FP64 steps instead of several); detinv_pre, when
+// non-zero, is the element's 1 / det(coef), evaluated once per column offset by the caller.
+template <typename R, bool kF32Start = false>
+__device__ __noinline__ void elm_solve(int &el, const R coef[2][2], R eps, R omegah, R omegas, R pr[3], R mus, R s[2],
+                                       R detinv_pre = R(0)) {
     const int maxnr = 10;
     const R prc = R(0.0001);
     const R taucs = R(1e20);
@@ -425,7 +430,8 @@ __device__ __noinline__ void elm_solve(int &el, const R coef[2][2], R eps, R ome
         itry++;
         if (el == Adhes) {
             trc_bound = mus * pr[2];
-            R detinv = R(1) / (coef[0][0] * coef[1][1] - coef[0][1] * coef[1][0]);
+            const R detinv =
+                detinv_pre != R(0) ? detinv_pre : R(1) / (coef[0][0] * coef[1][1] - coef[0][1] * coef[1][0]);
             dp[0] = (-coef[1][1] * s[0] + coef[0][1] * s[1]) * detinv;
             dp[1] = (coef[1][0] * s[0] - coef[0][0] * s[1]) * detinv;
             pr[0] = pold1 + omegah * dp[0];
@@ -443,9 +449,33 @@ __device__ __noinline__ void elm_solve(int &el, const R coef[2][2], R eps, R ome
         } else if (el == Slip) {
             violat = 0;
             trc_bound = mus * pr[2];
-            R sabs = sqrt(si0[0] * si0[0] + si0[1] * si0[1]);
-            pr[0] = -trc_bound * si0[0] / sabs;
-            pr[1] = -trc_bound * si0[1] / sabs;
+            bool start = false;
+            if constexpr (kF32Start) {
+                const float c00 = (float)coef[0][0], c01 = (float)coef[0][1], c10 = (float)coef[1][0],
+                            c11 = (float)coef[1][1];
+                const float t0 = (float)si0[0], t1 = (float)si0[1], tb = (float)trc_bound;
+                const float sa = sqrtf(t0 * t0 + t1 * t1);
+                float qx = -tb * t0 / sa, qy = -tb * t1 / sa;
+                for (int it = 0; it < maxnr; it++) {
+                    const float ux = t0 + c00 * qx + c01 * qy, uy = t1 + c10 * qx + c11 * qy;
+                    const float g0 = qy * ux - qx * uy, g1 = qx * qx + qy * qy - tb * tb;
+                    const float a00 = -2.f * c10 * qx - t1 + (c00 - c11) * qy;
+                    const float a01 = 2.f * c01 * qy + t0 + (c00 - c11) * qx;
+                    const float a10 = 2.f * qx, a11 = 2.f * qy;
+                    const float det = a00 * a11 - a01 * a10;
+                    if (det == 0.f) break;
+                    const float rd = 1.f / det;
+                    const float ex = -(a11 * g0 - a01 * g1) * rd, ey = -(-a10 * g0 + a00 * g1) * rd;
+                    qx += ex; qy += ey;
+                    if (fabsf(ex) + fabsf(ey) <= 1e-6f * tb) break;
+                }
+                if (isfinite(qx) && isfinite(qy)) { pr[0] = (R)qx; pr[1] = (R)qy; start = true; }
+            }
+            if (!start) {
+                R sabs = sqrt(si0[0] * si0[0] + si0[1] * si0[1]);
+                pr[0] = -trc_bound * si0[0] / sabs;
+                pr[1] = -trc_bound * si0[1] / sabs;
+            }
             si[0] = si0[0] + coef[0][0] * pr[0] + coef[0][1] * pr[1];
             si[1] = si0[1] + coef[1][0] * pr[0] + coef[1][1] * pr[1];
             fk[0] = pr[1] * si[0] - pr[0] * si[1];
@@ -663,7 +693,7 @@ __device__ inline double gs_element_warp(const PView &P, int ii, int ix, int iy,
         double s[2] = {s0 + wsx[ii], s1 + wsy[ii]};
         double pr[3] = {px[ii], py[ii], pn[ii]};
         int el = igs[ii];
-        elm_solve(el, coef, eps, omegah, omegas, pr, mus, s);
+        elm_solve<double, true>(el, coef, eps, omegah, omegas, pr, mus, s, ctab[3 * mx + o]);
         igs[ii] = el;
         dif2 = (pr[0] - px[ii]) * (pr[0] - px[ii]) + (pr[1] - py[ii]) * (pr[1] - py[ii]);
         dpx[ii] += pr[0] - px[ii];
@@ -765,9 +795,9 @@ __device__ inline double gs_element_warp(const PView &P, int ii, int ix, int iy,
 // (2 x (mx + 2 kGsPad) floats, zero outside the row).
 constexpr int kGsTile = 8;
 
-// bytes: ctab (3 mx doubles), c0 (6 mx floats), rdx and rdy (mx + 2 kGsPad floats each)
+// bytes: ctab (4 mx doubles), c0 (6 mx floats), rdx and rdy (mx + 2 kGsPad floats each)
 __host__ __device__ inline size_t gs_rows_smem_bytes(int mx) {
-    return (size_t)24 * mx + 4 * ((size_t)6 * mx + 2 * ((size_t)mx + 2 * kGsPad));
+    return (size_t)32 * mx + 4 * ((size_t)6 * mx + 2 * ((size_t)mx + 2 * kGsPad));
 }
 
 // (s0, s1) = sum over jx in [j0, j1] of A(ix - jx, 0) dd(jx) (without the factor ga_inv), FP32
@@ -912,7 +942,7 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
     float *c0 = nullptr, *rdx = nullptr, *rdy = nullptr;
     if (rows) {
         ctab = (double *)o64->cv.cbuf;
-        c0 = (float *)(ctab + 3 * mx);
+        c0 = (float *)(ctab + 4 * mx);
         rdx = c0 + 6 * mx;
         rdy = rdx + mx + 2 * kGsPad;
     }
@@ -942,7 +972,8 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
         double difacc = 0.0;      // held by the group's lead thread
         if (rows) {
             // coefficient row dy = 0 in shared memory (the product above used the buffer), and the
-            // element coefficients per column offset o = ix - jx (1 .. mx - 1)
+            // element coefficients xx, xy, yy per column offset o = ix - jx (1 .. mx - 1) with
+            // 1 / det of each offset's 2 x 2 block
             const float *cr = cf32 + (size_t)my * 2 * mx;
             for (int t = threadIdx.x; t < 2 * mx; t += blockDim.x) {
                 c0[t] = cr[t]; c0[2 * mx + t] = cr[bsz + t]; c0[4 * mx + t] = cr[2 * bsz + t];
@@ -954,6 +985,10 @@ __device__ __noinline__ int stdygs(const PView &P, double eps, int maxgs, double
                     const size_t oj = (size_t)(-o + mx) + (size_t)(0 + my) * 2 * mx;
                     ctab[t] = o == 0 ? 0.0 : (d.cf[c * bsz + o0] - d.cf[c * bsz + oj]) / d.ga;
                 }
+                __syncthreads();
+                for (int o = threadIdx.x; o < mx; o += blockDim.x)
+                    ctab[3 * mx + o] = o == 0 ? 0.0
+                                              : 1.0 / (ctab[o] * ctab[2 * mx + o] - ctab[mx + o] * ctab[mx + o]);
             }
             const double gainv = 1.0 / d.ga;
             const bool lead_warp = g_grp.rank == 0 && threadIdx.x < 32;
