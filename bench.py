@@ -372,12 +372,20 @@ def run_gb300(args, dist):
             ft = math.hypot(b["fx"], b["fy"])
             ferr.append(math.hypot(a["fx"] - b["fx"], a["fy"] - b["fy"]) / max(ft, 1e-3 * c["fstat"] * abs(b["fn"])))
         ferr = np.array(ferr)
+        # the per-call FP64 drop-in (one cntc_calculate per patch, one CTA each): the sum of the
+        # patches' own solve times, measured in SM cycles by each patch's CTA in this pass (an
+        # upper bound: there two CTAs share an SM)
+        mhz = clk["sm_mhz"] if clk and clk.get("sm_mhz") else 2070.0
+        cta_s = sum(cg.getsolverstats(i, 2)["t_total"] for i in pire) / (mhz * 1e6)
         plain = {"patches": len(pc), "solves_per_s": len(pc) / (float(pt[0, 0]) / 1e3),
+                 "per_call_solves_per_s": len(pc) / cta_s,
                  "mixed_solves_per_s_same_sample": len(pc) / (mixed_sample_ms / 1e3),
                  "mixed_force_rel_err": {"max": float(ferr.max()), "p99": float(np.percentile(ferr, 99)),
                                          "median": float(np.median(ferr)), "above_1e-8": int((ferr > 1e-8).sum())},
-                 "note": "first %d patches of the workload, eps 1e-8, FP64 throughout; force error = |dF_t| / "
-                         "max(|F_t|, 1e-3 mu Fn) of the mixed form against this FP64 form" % len(pc)}
+                 "note": "first %d patches of the workload, eps 1e-8, FP64 throughout, batched (solves_per_s) and "
+                         "as per-call drop-in (per_call_solves_per_s: patches / sum of each patch's single-CTA "
+                         "solve time in that pass); force error = |dF_t| / max(|F_t|, 1e-3 mu Fn) of the mixed "
+                         "form against this FP64 form" % len(pc)}
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         rate, thr, desc, _ = cpu_sample_rate(cases, args.seed, threads=args.cpu_threads or None)

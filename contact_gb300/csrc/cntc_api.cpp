@@ -97,7 +97,7 @@ struct Problem {
     // device cache of the influence coefficients and spectra (cntc_calculate, _batch, _async):
     // they depend only on the grid, dx, dy and the material, and are reused while that key
     // stays the same
-    char key[128] = {0};          // geometry key of the cached influence coefficients
+    char key[256] = {0};          // geometry key of the cached influence coefficients
     bool ic_valid = false;
     void *d_ic = nullptr;
     size_t cap_ic = 0;
@@ -163,6 +163,15 @@ void select_units(Problem &p, int units) {
 // preparation of one patch: Hertz solution, potential contact, flags -> PatchDesc.
 // Returns 0 or an error code (cntc ierror convention).
 // ------------------------------------------------------------------------------------------
+// coefficient blocks of a problem's patch (PatchDesc::ncf): 4, or 6 / 8 for non-identical
+// materials (K != 0) in shifts / steady rolling
+int ncf_of(const Problem &p) {
+    const double ga = 2.0 / (1.0 / p.gg[0] + 1.0 / p.gg[1]);
+    const double ak = (ga / 4.0) * ((1.0 - 2.0 * p.poiss[0]) / p.gg[0] - (1.0 - 2.0 * p.poiss[1]) / p.gg[1]);
+    if (std::fabs(ak) < 1e-6) return 4;
+    return p.tang == 3 ? 8 : 6;
+}
+
 struct Prep {
     PatchDesc d;
     bool ic_needed;
@@ -176,7 +185,13 @@ int prepare(Problem &p, Prep &out) {
     const double ga = 2.0 / (1.0 / p.gg[0] + 1.0 / p.gg[1]);
     const double nu = ga * (p.poiss[0] / p.gg[0] + p.poiss[1] / p.gg[1]) / 2.0;
     const double ak = (ga / 4.0) * ((1.0 - 2.0 * p.poiss[0]) / p.gg[0] - (1.0 - 2.0 * p.poiss[1]) / p.gg[1]);
-    if (std::fabs(ak) >= 1e-6) { log_msg("non-identical materials (K != 0) are not supported"); return CNTC_err_other; }
+    // K != 0 couples the normal and tangential problems (|K| >= 1e-6, m_visc.f90:431-604): shifts
+    // and steady rolling are solved; transient rolling with coupling is not provided here
+    const bool cpl = std::fabs(ak) >= 1e-6;
+    if (cpl && p.tang == 2) {
+        log_msg("transient rolling (T=2) of non-identical materials (K != 0) is not supported");
+        return CNTC_err_other;
+    }
     if (p.mater != 0 || p.frclaw != 0 || p.rztang != 0 || p.varfrc != 0) {
         log_msg("only M=0, L=0, E=0 are supported");
         return CNTC_err_other;
@@ -244,7 +259,8 @@ int prepare(Problem &p, Prep &out) {
     d.gd_meth = p.gd_meth; d.kdown = p.kdown; d.kdowfb = p.kdowfb;
     d.fdecay = p.fdecay; d.betath = p.betath; d.d_ifc = p.d_ifc; d.d_lin = p.d_lin; d.d_cns = p.d_cns;
     d.d_slp = p.d_slp; d.pow_s = p.pow_s;
-    d.ga = ga; d.nu = nu; d.fstat = p.fstat;
+    d.ga = ga; d.nu = nu; d.ak = cpl ? ak : 0.0; d.fstat = p.fstat;
+    d.ncf = ncf_of(p);
     d.chi = chi; d.dq = dq; d.cksi = p.cksi; d.ceta = p.ceta; d.cphi = p.cphi;
     d.fntrue = fn; d.pen = pen;
     d.ihertz = ihertz; d.aa = p.hz_aa; d.bb = p.hz_bb;
@@ -266,8 +282,9 @@ int prepare(Problem &p, Prep &out) {
     for (int k = 0; k < 16; k++) d.sens0[k] = p.sens_all[k];
     d.sens = p.sens; d.mxsens = p.mxsens; d.epsens = p.epsens;
     // geometry key for reuse of influence coefficients and spectra
-    char key[128];
-    std::snprintf(key, sizeof(key), "%d %d %.17g %.17g %.17g %.17g", mx, my, dx, dy, ga, nu);
+    char key[256];
+    std::snprintf(key, sizeof(key), "%d %d %.17g %.17g %.17g %.17g %.17g %d %.17g", mx, my, dx, dy, ga, nu, d.ak,
+                  d.ncf, d.ncf == 8 ? dq : 0.0);
     if (std::strcmp(key, p.key) != 0) p.ic_valid = false;    // the cache holds another geometry
     out.ic_needed = !p.ic_valid;
     std::strcpy(p.key, key);
@@ -393,7 +410,7 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
     bool any_upload = false;
     for (int k = 0; k < n; k++) {
         const PatchDesc &d = b.preps[live[k]].d;
-        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk);
+        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk, d.ncf);
         off_io[k] = tot_io; tot_io += s.io;
         off_work[k] = tot_work; tot_work += s.work;
         any_upload |= b.preps[live[k]].upload;
@@ -418,7 +435,7 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
             // the geometry is unchanged, computed into it otherwise (without a buffer, when
             // the allocation fails, they are computed in the pass's work area as before)
             Problem &p = *b.probs[live[k]];
-            const PatchSizes ps = patch_sizes(hd[k].mx, hd[k].my, hd[k].fx, hd[k].fy, hd[k].nblk);
+            const PatchSizes ps = patch_sizes(hd[k].mx, hd[k].my, hd[k].fx, hd[k].fy, hd[k].nblk, hd[k].ncf);
             const size_t icb = ps.cf + ps.spec64 + ps.spec32;
             const bool hit = p.ic_valid && !b.preps[live[k]].ic_needed && p.d_ic && p.ic_dev == dev && p.cap_ic >= icb;
             if (!hit) {
@@ -602,7 +619,7 @@ int resident_setup(int n, const int *ire, const int *icp, int *ierror) {
     size_t tot_work = 0;
     for (int k = 0; k < m; k++) {
         const PatchDesc &d = b.preps[R->live[k]].d;
-        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk);
+        PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk, d.ncf);
         R->off_io[k] = R->tot_io; R->tot_io += s.io;
         off_work[k] = tot_work; tot_work += s.work;
     }
@@ -793,7 +810,7 @@ int calculate_noalloc(int ire, int icp) {
         p->have = false;
         return CNTC_err_other;
     }
-    const PatchSizes s = patch_sizes(hd.mx, hd.my, hd.fx, hd.fy, hd.nblk);
+    const PatchSizes s = patch_sizes(hd.mx, hd.my, hd.fx, hd.fy, hd.nblk, hd.ncf);
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t off_list = up(sizeof(PatchDesc)), off_io = off_list + 256, off_work = off_io + up(s.io);
     if (off_work + s.work > kNoAllocBytes || s.io > sizeof(g_noalloc_host)) {
@@ -925,7 +942,7 @@ int calculate_async(int ire, int icp) {
     auto r = std::make_shared<AsyncReq>();
     r->ire = ire; r->icp = icp;
     const int fx = opt_fft_size(std::max(1, p->mx)), fy = opt_fft_size(std::max(1, p->my));
-    const PatchSizes ps = patch_sizes(std::max(1, p->mx), std::max(1, p->my), fx, fy);
+    const PatchSizes ps = patch_sizes(std::max(1, p->mx), std::max(1, p->my), fx, fy, 1, ncf_of(*p));
     r->bytes = ps.io + ps.work + sizeof(PatchDesc);
     r->t_submit = std::chrono::steady_clock::now();
     {
@@ -1079,6 +1096,11 @@ void cntc_setmaterialparameters(int *ire, int *icp, int *imeth, int *nparam, dou
     p->poiss[0] = rparam[0]; p->poiss[1] = rparam[1];
     p->gg[0] = rparam[2] * p->s_forc / p->s_area;
     p->gg[1] = rparam[3] * p->s_forc / p->s_area;
+    // MAXOUT for quasi-identical and other material pairs (src/contact_addon.f90:1458-1462)
+    const double ga = 2.0 / (1.0 / p->gg[0] + 1.0 / p->gg[1]);
+    const double ak = (ga / 4.0) * ((1.0 - 2.0 * p->poiss[0]) / p->gg[0] - (1.0 - 2.0 * p->poiss[1]) / p->gg[1]);
+    if (p->maxout >= 2 && std::fabs(ak) < 1e-4) p->maxout = 1;
+    if (p->maxout <= 1 && std::fabs(ak) >= 1e-4) p->maxout = 10;
 }
 
 // H digit (cntc_setTemperatureData, src/contact_addon.f90:1477-1550): the method is recorded

@@ -38,12 +38,14 @@ __device__ inline void corner(int ix, int iy, double dx, double dy, double xsh, 
 // influence coefficients xx, xy (= yx), yy, zz of offset (ix, iy) for piecewise-constant
 // loading (elascf_pcwcns, m_visc.f90:431-604) on grids shifted by (xsh, ysh); zero for rows
 // below iy0 (single-row grids)
+// c[0..3]: xx, xy, yy, zz; with cpl (K != 0, |ak| >= 1e-6 as in the reference) also c[4], c[5]:
+// xz and yz (the terms with K of m_visc.f90:431-604, in its order of summation)
 __device__ inline void influence_at(int ix, int iy, int iy0, double dx, double dy, double nu, double xsh, double ysh,
-                                    double c[4]) {
+                                    double c[6], double ak = 0.0, bool cpl = false) {
     const double pi = 3.14159265358979323846;
     const double e1 = (1.0 - nu) / pi, e2 = 1.0 / pi, e3 = nu / pi;
-    const double tolx = dx * 1e-10;
-    double c11 = 0, c12 = 0, c22 = 0, c33 = 0;
+    const double tolx = dx * 1e-10, tolx2 = dx * 1e-20;
+    double c11 = 0, c12 = 0, c22 = 0, c33 = 0, c13 = 0, c23 = 0;
     if (iy >= iy0) {
         double x00, y00, r00, x01, y01, r01, x10, y10, r10, x11, y11, r11;
         corner(ix, iy, dx, dy, xsh, ysh, x00, y00, r00);
@@ -65,8 +67,23 @@ __device__ inline void influence_at(int ix, int iy, int iy0, double dx, double d
         c11 = c11 + (e1 * X1 + e2 * Y1);
         c22 = 0.0 - (e1 * Y0 + e2 * X0);
         c22 = c22 + (e1 * Y1 + e2 * X1);
+        if (cpl) {
+            // y log r + x atan(y / x) and x log r + y atan(x / y) at the four corners
+            auto j5 = [&](double x, double y, double r) { return y * log(r) + x * atan(y / (x + tolx2)); };
+            auto j6 = [&](double x, double y, double r) { return x * log(r) + y * atan(x / (y + tolx2)); };
+            const double f = e2 * ak;
+            c13 = 0.0 - f * j5(x00, y00, r00);
+            c13 = c13 + f * j5(x01, y01, r01);
+            c13 = c13 + f * j5(x10, y10, r10);
+            c13 = c13 - f * j5(x11, y11, r11);
+            c23 = 0.0 - f * j6(x00, y00, r00);
+            c23 = c23 + f * j6(x01, y01, r01);
+            c23 = c23 + f * j6(x10, y10, r10);
+            c23 = c23 - f * j6(x11, y11, r11);
+        }
     }
     c[0] = c11; c[1] = c12; c[2] = c22; c[3] = c33;
+    if (cpl) { c[4] = c13; c[5] = c23; }
 }
 
 // grid: (blocks per patch, number of listed patches); list[] gives the patch indices
@@ -79,12 +96,25 @@ __global__ void __launch_bounds__(kThreads) k_influence(const PatchDesc *descs, 
     const size_t bsz = (size_t)total;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
         const int ix = t % (2 * mx) - mx, iy = t / (2 * mx) - my;
-        double c[4];
-        influence_at(ix, iy, iy0, d.dx, d.dy, d.nu, 0.0, 0.0, c);
+        double c[6];
+        const bool cpl = d.ncf >= 6;
+        influence_at(ix, iy, iy0, d.dx, d.dy, d.nu, 0.0, 0.0, c, d.ak, cpl);
         cf[0 * bsz + t] = c[0];
         cf[1 * bsz + t] = c[1];
         cf[2 * bsz + t] = c[2];
         cf[3 * bsz + t] = c[3];
+        if (cpl) {
+            cf[4 * bsz + t] = c[4];
+            cf[5 * bsz + t] = c[5];
+        }
+        if (d.ncf == 8) {
+            // steady rolling: the coupling blocks of cs - cv, cv the grid shifted by one rolling
+            // step (m_visc.f90:289-354), for u'(pn) of stang_rhs
+            double v[6];
+            influence_at(ix, iy, iy0, d.dx, d.dy, d.nu, cos(d.chi) * d.dq, sin(d.chi) * d.dq, v, d.ak, true);
+            cf[6 * bsz + t] = c[4] - v[4];
+            cf[7 * bsz + t] = c[5] - v[5];
+        }
     }
 }
 
@@ -98,7 +128,7 @@ __device__ __noinline__ void steady_coefs(const PatchDesc &d, double *csv) {
     const double xsh = cos(d.chi) * d.dq, ysh = sin(d.chi) * d.dq;
     for (int t = gtid(); t < total; t += gstride()) {
         const int ix = t % (2 * mx) - mx, iy = t / (2 * mx) - my;
-        double c[4];
+        double c[6];
         influence_at(ix, iy, iy0, d.dx, d.dy, d.nu, xsh, ysh, c);
         csv[0 * (size_t)total + t] = d.cf[0 * (size_t)total + t] - c[0];
         csv[1 * (size_t)total + t] = d.cf[1 * (size_t)total + t] - c[1];
@@ -117,7 +147,7 @@ __device__ __noinline__ void transient_coefs(const PatchDesc &d, double *cv) {
     const double xsh = cos(d.chi) * d.dq, ysh = sin(d.chi) * d.dq;
     for (int t = gtid(); t < total; t += gstride()) {
         const int ix = t % (2 * mx) - mx, iy = t / (2 * mx) - my;
-        double c[4];
+        double c[6];
         influence_at(ix, iy, iy0, d.dx, d.dy, d.nu, xsh, ysh, c);
         for (int k = 0; k < 3; k++) {
             const double cs = d.cf[k * (size_t)total + t];
@@ -234,7 +264,7 @@ __device__ inline void make_ops(Ops<T> &op, const PatchDesc &d, unsigned char *s
     op.cv = make_conv<T>(d, smraw, sp);
     const size_t ksz = (size_t)(d.fx + 1) * (d.fy + 1);
     const T *base = (sizeof(T) == 8) ? (const T *)(const void *)d.spec64 : (const T *)(const void *)d.spec32;
-    for (int b = 0; b < 7; b++) op.K[b] = base + b * ksz;
+    for (int b = 0; b < kMaxSpectra; b++) op.K[b] = b < d.ncf + 3 ? base + b * ksz : nullptr;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -243,8 +273,10 @@ __device__ inline void make_ops(Ops<T> &op, const PatchDesc &d, unsigned char *s
 // real, quadrant-symmetric conv-size spectrum of a spatial block src (layout of cf:
 // (dx + mx) + (dy + my) * 2mx); offsets |dx| <= mx-1, |dy| <= my-1 are placed at
 // (dx mod NX, dy mod NY).  S: scratch of nkx * NY complex.
+// imag: the block is odd in exactly one of x, y (the coupling blocks xz, yz), so that its
+// spectrum is imaginary: the imaginary part is stored.
 __device__ __noinline__ void block_spectrum(const Conv<double> &cv, const double *src, double2 *S, double *K64,
-                                            float *K32, double2 *a, double2 *b) {
+                                            float *K32, double2 *a, double2 *b, bool imag = false) {
     const int mx = cv.mx, my = cv.my, NX = cv.NX, NY = cv.NY, nkx = cv.nkx, fy = cv.fy;
     const Lines &L = cv.L;
     const int lane = L.lane, nl = L.nl;
@@ -277,8 +309,9 @@ __device__ __noinline__ void block_spectrum(const Conv<double> &cv, const double
         double2 *z = line_fft<double>(a, b, cv.py, cv.twy, -1, lane, nl, L.blk);
         for (int ky = lane; ky <= fy; ky += nl) {
             const size_t o = (size_t)kx * (fy + 1) + ky;
-            K64[o] = z[ky].x;
-            K32[o] = (float)z[ky].x;
+            const double v = imag ? z[ky].y : z[ky].x;
+            K64[o] = v;
+            K32[o] = (float)v;
         }
         line_sync(L.blk);
     }
@@ -392,6 +425,15 @@ __global__ void __launch_bounds__(kThreads) k_spectra(const PatchDesc *descs, co
             make_twiddles<double>(cv.twy, cv.NY);
         }
         block_spectrum(cv, msp, S, K64 + (4 + k) * ksz, K32 + (4 + k) * ksz, a, b);
+    }
+    // coupling blocks (K != 0): cf blocks 4 .. ncf - 1 -> spectra 7 .. ncf + 2
+    for (int blkc = 4; blkc < d.ncf; blkc++) {
+        gsync();
+        if (!blk) {
+            make_twiddles<double>(cv.twx, cv.NX);
+            make_twiddles<double>(cv.twy, cv.NY);
+        }
+        block_spectrum(cv, d.cf + blkc * bsz, S, K64 + (blkc + 3) * ksz, K32 + (blkc + 3) * ksz, a, b, true);
     }
 }
 
@@ -937,6 +979,22 @@ __device__ __noinline__ int stang(const PView &P, TangRun &T, int &itgs_out) {
         wfy[i] = iel[i] ? -facdt[i] * wy[i] : 0.0;
     }
     gsync();
+    // K != 0: the tangential displacement of the normal pressure, u(ps_n) - u'(pv_n) (stang_rhs,
+    // m_stang.f90:749-951): in steady rolling through the coupling blocks of cs - cv applied to
+    // the current pressure; for shifts through cs applied to the pressure minus that of the
+    // previous time instance (P = 0, 1), or to the pressure alone (P = 2)
+    if (d.ncf >= 6) {
+        double *ux = P.c(W_UX), *uy = P.c(W_UY), *un = P.c(W_UN);
+        const double *src = pn;
+        if (d.tang == 1 && d.pvtime <= 1 && d.prev) {
+            const double *pvn = d.prev + 2 * (size_t)n;
+            FOR_I(i, n) un[i] = pn[i] - pvn[i];
+            src = un;
+        }
+        prod_tz(*T.op, src, ux, uy, OUT_ALL, igs, d.tang == 3 ? 9 : 7);
+        FOR_I(i, n) if (iel[i]) { wfx[i] += ux[i]; wfy[i] += uy[i]; }
+        gsync();
+    }
     // shifts and transient rolling continuing from the previous time instance (P = 0):
     // wsfix -= u' of the previous tangential tractions, through cs for shifts and through cv
     // (one rolling step) for transient rolling, where elements within one rolling step of
@@ -1049,6 +1107,11 @@ __device__ __noinline__ void soutpt(const PView &P, const Ops<T> &op, double pen
     FOR_I(i, n) { ux[i] = 0.0; uy[i] = 0.0; un[i] = 0.0; }
     prod_n<T>(op, pn, un, OUT_INT, igs, 3);
     prod_t<T>(op, px, py, ux, uy, OUT_INT, igs);
+    // K != 0: the coupling terms of u = A p (all components, m_soutpt.f90:377-511)
+    if (d.ncf >= 6) {
+        prod_zt(op, px, py, un, true, igs);
+        prod_tz(op, pn, ux, uy, OUT_ADDINT, igs, 7);
+    }
     double a[4] = {0, 0, 0, 0};
     double b[2] = {0, 0};
     double pmax = -1e20;
@@ -1165,42 +1228,6 @@ __device__ __noinline__ void solve_patch(const PatchDesc &d, bool blk, unsigned 
     if (d.iestim == 0 || d.iestim == 2)
         for (int io = 0; io < 4; io++) for (int ji = 1; ji < 4; ji++) sens[io * 4 + ji] = 0.0;
     int itnorm = 0, ittang = 0, itcg = 0, itgs = 0, solver = 0, nconv32 = 0, nconv64 = 0, nls = 0;
-    // NORM (skipped for Hertzian traction bounds B = 2, 3)
-    long long t_norm0 = clock64();
-    if (!(d.bound >= 2 && d.bound <= 4 && d.ihertz >= 1)) {
-        // the normal problem is a small part of a solve: FP64 in both forms, so that the mixed
-        // form starts its tangential iteration from exactly the same pressures
-        int it = 0, itc = 0;
-        it = snorm<double>(P, op64, d.maxgs, d.maxin, d.eps, pen, itc, nconv64);
-        itcg += itc;
-        if (it == -2) status |= ST_NORMCG_DIV;
-        itnorm = it >= 0 ? it : -1;
-        if (d.norm == 0) {
-            double s = 0; FOR_I(i, d.npot) s += P.c(W_PN)[i];
-            fntrue = d.dxdy * block_sum1(sm.red, s);
-        }
-        // d Fn / d pen (S >= 2, m_snorm.f90:357-368); the reference re-evaluates the normal
-        // displacements of the final pressures on small grids (npot < 700)
-        if (it != -2 && d.sens >= 2) {
-            if (d.npot < 700) prod_n<double>(op64, P.c(W_PN), P.c(W_DD), OUT_ALL, P.igs(), 3);
-            if (!sens_norm(P, op64, pen, fntrue, nconv64, sens[0])) { status |= ST_NORMCG_DIV; itnorm = -1; }
-        } else if (it != -2) {
-            sens[0] = 0.0;
-        }
-    }
-    if (threadIdx.x == 0) sm.t[O_T_NORM - O_T_TOTAL] = clock64() - t_norm0;
-    // clear the exterior tractions, count the contact area
-    int ncon = 0;
-    {
-        int *igs = P.igs();
-        double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN);
-        FOR_I(i, d.npot) {
-            if (igs[i] <= Exter) { pn[i] = 0.0; px[i] = 0.0; py[i] = 0.0; }
-            else ncon++;
-        }
-        ncon = block_sumi1(sm.red, ncon);
-    }
-    long long t_tang0 = clock64();
     // creepages and Newton-Raphson sensitivities: a fresh start takes cksi = 1e-6 (and ceta = 0
     // for F = 2) and zero sensitivities when total forces are prescribed (m_sdis.f90:754-766)
     TangRun T;
@@ -1214,17 +1241,99 @@ __device__ __noinline__ void solve_patch(const PatchDesc &d, bool blk, unsigned 
         if (d.force3 >= 1) T.cksi = 1e-6;
         if (d.force3 == 2) T.ceta = 0.0;
     }
-    if (d.tang != 0 && ncon > 0 && itnorm >= 0) {
-        int itg = 0;
-        const int it = stang(P, T, itg);
-        solver = T.solver;
-        nconv64 += T.nconv; nconv32 += T.nconv32; nls += T.nls;
-        itgs += itg;
-        if (it == -1000) status |= ST_UNSUPPORTED;
-        if (it == -2000) status |= ST_NOBRACKET;
-        ittang = it >= 0 ? it : -1;
+    // the Panagiotopoulos process (panprc, m_scontc.f90:356-553): NORM and TANG alternately until
+    // the tractions change by less than 5 eps (rms) between two passes, at most maxout passes; one
+    // pass for identical materials (K = 0, maxout = 1)
+    const int n = d.npot;
+    int *igs = P.igs();
+    double *px = P.c(W_PX), *py = P.c(W_PY), *pn = P.c(W_PN);
+    double *o1x = P.c(W_O1X), *o1y = P.c(W_O1Y), *o1n = P.c(W_O1N);
+    const bool outer = d.maxout > 1;
+    if (outer) {
+        FOR_I(i, n) { o1x[i] = px[i]; o1y[i] = py[i]; o1n[i] = pn[i]; }
+        gsync();
     }
-    if (threadIdx.x == 0) sm.t[O_T_TANG - O_T_TOTAL] = clock64() - t_tang0;
+    int itout = 0;
+    double difid = 1.0, dif = 200.0 * difid;
+    while (dif > difid && itout < d.maxout && itnorm >= 0 && ittang >= 0) {
+        itout++;
+        // NORM (skipped for Hertzian traction bounds B = 2, 3)
+        const long long t_norm0 = clock64();
+        if (!(d.bound >= 2 && d.bound <= 4 && d.ihertz >= 1)) {
+            // the normal problem is a small part of a solve: FP64 in both forms, so that the mixed
+            // form starts its tangential iteration from exactly the same pressures.  K != 0: the
+            // normal displacement of the current tangential tractions joins the undeformed
+            // distance
+            const double *htang = nullptr;
+            if (d.ncf >= 6) {
+                double *un = P.c(W_UN);
+                prod_zt(op64, px, py, un, false, igs);
+                htang = un;
+            }
+            int it = 0, itc = 0;
+            it = snorm<double>(P, op64, d.maxgs, d.maxin, d.eps, pen, itc, nconv64, htang);
+            itcg = itc;
+            if (it == -2) status |= ST_NORMCG_DIV;
+            if (it >= 0) itnorm += it; else itnorm = -1;
+            if (d.norm == 0) {
+                double s = 0; FOR_I(i, n) s += pn[i];
+                fntrue = d.dxdy * block_sum1(sm.red, s);
+                T.fntrue = fntrue;
+            }
+            // d Fn / d pen (S >= 2, m_snorm.f90:357-368); the reference re-evaluates the normal
+            // displacements of the final pressures on small grids (npot < 700)
+            if (it != -2 && d.sens >= 2) {
+                if (d.npot < 700) prod_n<double>(op64, pn, P.c(W_DD), OUT_ALL, igs, 3);
+                if (!sens_norm(P, op64, pen, fntrue, nconv64, sens[0])) { status |= ST_NORMCG_DIV; itnorm = -1; }
+            } else if (it != -2) {
+                sens[0] = 0.0;
+            }
+        }
+        if (threadIdx.x == 0) sm.t[O_T_NORM - O_T_TOTAL] += clock64() - t_norm0;
+        if (status != ST_OK) break;
+        // clear the exterior tractions, count the contact area (TANG follows NORM also when NORM
+        // reached maxin, as in the reference; the loop then ends)
+        int ncon = 0;
+        FOR_I(i, n) {
+            if (igs[i] <= Exter) { pn[i] = 0.0; px[i] = 0.0; py[i] = 0.0; }
+            else ncon++;
+        }
+        ncon = block_sumi1(sm.red, ncon);
+        if (d.tang == 0 || ncon <= 0) {
+            dif = 0.0;
+        } else {
+            const long long t_tang0 = clock64();
+            int itg = 0;
+            const int it = stang(P, T, itg);
+            solver = T.solver;
+            itgs = itg;
+            if (it == -1000) status |= ST_UNSUPPORTED;
+            if (it == -2000) status |= ST_NOBRACKET;
+            if (it >= 0) ittang += it; else ittang = -1;
+            if (threadIdx.x == 0) sm.t[O_T_TANG - O_T_TOTAL] += clock64() - t_tang0;
+            if (status != ST_OK) break;
+            if (outer) {
+                // change of the tractions over the contact area, all components (gf3_rms AllInt)
+                double a[2] = {0.0, 0.0};
+                int c = 0;
+                FOR_I(i, n) {
+                    if (igs[i] < Adhes) continue;
+                    const double ex = px[i] - o1x[i], ey = py[i] - o1y[i], en = pn[i] - o1n[i];
+                    a[0] += ex * ex + ey * ey + en * en;
+                    a[1] += px[i] * px[i] + py[i] * py[i] + pn[i] * pn[i];
+                    c += 3;
+                }
+                block_sum<2>(sm.red, a);
+                c = block_sumi1(sm.red, c);
+                dif = sqrt(a[0] / max(1, c));
+                difid = 5.0 * d.eps * sqrt(a[1] / max(1, c));
+                FOR_I(i, n) { o1x[i] = px[i]; o1y[i] = py[i]; o1n[i] = pn[i]; }
+                gsync();
+            }
+        }
+        if (status != ST_OK) break;
+    }
+    nconv64 += T.nconv; nconv32 += T.nconv32; nls += T.nls;
     soutpt<double>(P, op64, pen, fntrue, out);
     int atb = count_atbnd(P);
     // the solution, kept in device memory for the problem's next warm start or time instance
@@ -1324,14 +1433,14 @@ int opt_fft_size(int fft_size) {
     return (int)prod;
 }
 
-PatchSizes patch_sizes(int mx, int my, int fx, int fy, int nblk) {
+PatchSizes patch_sizes(int mx, int my, int fx, int fy, int nblk, int ncf) {
     PatchSizes s;
     const size_t n = (size_t)mx * my;
     const size_t ksz = (size_t)(fx + 1) * (fy + 1);
     s.io = align256(io_doubles((int)n) * sizeof(double));
-    s.cf = align256(16 * n * sizeof(double));
-    s.spec64 = align256(7 * ksz * sizeof(double));
-    s.spec32 = align256(7 * ksz * sizeof(float));
+    s.cf = align256((size_t)ncf * 4 * n * sizeof(double));
+    s.spec64 = align256((size_t)(ncf + 3) * ksz * sizeof(double));
+    s.spec32 = align256((size_t)(ncf + 3) * ksz * sizeof(float));
     size_t wkn = (size_t)(W_NCOL - kIoCols) * n;
     const size_t specscratch = spectra_scratch_doubles(mx, my, fx, fy) + 4 * n;   // k_spectra
     if (wkn < specscratch) wkn = specscratch;
@@ -1344,7 +1453,7 @@ PatchSizes patch_sizes(int mx, int my, int fx, int fy, int nblk) {
 }
 
 void carve_patch(PatchDesc &d, char *io, char *work) {
-    const PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk);
+    const PatchSizes s = patch_sizes(d.mx, d.my, d.fx, d.fy, d.nblk, d.ncf);
     d.io = (double *)io;
     char *p = work;
     d.cf = (const double *)p; p += s.cf;

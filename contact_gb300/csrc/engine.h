@@ -18,6 +18,7 @@ enum WsCol {
     W_POX, W_POY, W_WFX, W_WFY, W_PNX, W_PNY, W_TRC, W_ZX, W_ZY, W_ONE,   // W_WF*: fixed shift wsfix
     W_DBX, W_DBY, W_SBX, W_SBY, W_TX, W_TY,                  // mixed precision: base dp, A dp_base, change
     W_FACDT,                                                 // leading-edge fraction of the rolling step
+    W_O1X, W_O1Y, W_O1N,                                     // tractions of the previous outer (NORM/TANG) iteration
     W_FLS,                                                   // 9 columns: 18 float columns of the line search
     W_FST = W_FLS + 9,                                       // 14 columns: 28 float columns of the FP32 GD state
     W_NCOL = W_FST + 14
@@ -52,7 +53,7 @@ struct PatchDesc {
     double omegah, omegas;
     int gd_meth, kdown, kdowfb;
     double fdecay, betath, d_ifc, d_lin, d_cns, d_slp, pow_s;
-    double ga, nu;
+    double ga, nu, ak;                // combined modulus, Poisson ratio and difference parameter K
     double fstat;
     double chi, dq, cksi, ceta, cphi;
     double fntrue, pen;
@@ -69,7 +70,7 @@ struct PatchDesc {
     int mxsens;                       // iterations and tolerance of the sensitivity solves
     double epsens;
     int pvtime;                       // P digit: 0 previous time instance, 1 its normal part, 2 none
-    int pad3_;
+    int ncf;                          // coefficient blocks in cf: 4 (K = 0), 6 (K != 0), 8 (K != 0, steady rolling)
     // previous solution of the problem in device memory (prev_block layout), or nullptr: the
     // initial estimate when iestim != 0 and the previous time instance when pvtime <= 1.
     // save: where the solve leaves its own solution in the same layout (may equal prev), or nullptr.
@@ -81,8 +82,13 @@ struct PatchDesc {
     double *io;
     double *wk;                       // work columns W_HSTOT .. (W_NCOL - kIoCols) * npot doubles
     int *wki;                         // int columns I_OLD .. ((I_NCOL - 1) * npot ints)
-    const double *cf;                 // spatial influence coefficients [4][2my][2mx]: xx, xy, yy, zz
-    const double *spec64;             // spectra [7][fx+1][fy+1]: xx, xy, yy, zz, M_zz, M_xx, M_yy
+    // spatial influence coefficients [ncf][2my][2mx]: xx, xy, yy, zz; with K != 0 also xz, yz
+    // (zx = -xz, zy = -yz) and, in steady rolling, xz and yz of cs - cv (cv: the grid shifted by
+    // one rolling step)
+    const double *cf;
+    // spectra [nspec][fx+1][fy+1]: xx, xy, yy, zz, M_zz, M_xx, M_yy, then the imaginary parts of
+    // the spectra of the coupling blocks of cf (nspec = 3 + ncf)
+    const double *spec64;
     const float *spec32;
     void *rbuf;                       // 2 * (fx+1) * my complex doubles
     // patch group: nblk CTAs solve the patch together (1: a single CTA); gscr holds their

@@ -15,8 +15,9 @@ struct PatchSizes {
     size_t io, cf, spec64, spec32, wk, wki, rbuf, gscr, work;
 };
 
-// nblk: CTAs of the patch group (1: the patch is solved by one CTA)
-PatchSizes patch_sizes(int mx, int my, int fx, int fy, int nblk = 1);
+// nblk: CTAs of the patch group (1: the patch is solved by one CTA); ncf: coefficient blocks
+// (PatchDesc::ncf)
+PatchSizes patch_sizes(int mx, int my, int fx, int fy, int nblk = 1, int ncf = 4);
 
 // Assign the device pointers of d: io block at 'io' (patch_sizes().io bytes) and the work
 // buffers inside [work, work + patch_sizes().work).

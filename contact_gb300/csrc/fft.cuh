@@ -463,8 +463,12 @@ __device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, con
 // ncomp == 1: u = K0 p ; ncomp == 2: (ux,uy) = [[Kxx, Kxy],[Kxy, Kyy]] (px,py) with
 // K = {Kxx, Kxy, Kyy}.  Kernel blocks are (fx+1) x (fy+1) real, [kx][ky].  A batch holds cap
 // columns, each as ncomp lines (stride NY + 1 complex).
+// One component (ncomp = 1) may take a coupling kernel (kkind 1: odd in x, even in y; 2: even
+// in x, odd in y) whose spectrum is imaginary; K0 then holds its imaginary part, and ksign
+// scales the product (the blocks zx = -xz, zy = -yz).
 template <typename T>
-__device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0, const T *K1, const T *K2) {
+__device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0, const T *K1, const T *K2,
+                                       int kkind = 0, T ksign = T(1)) {
     const int NY = cv.NY, my = cv.my, nkx = cv.nkx, fy = cv.fy;
     const int ld = NY + 1;
     const int cap = cv.ccap / (2 * ld * ncomp);
@@ -482,8 +486,13 @@ __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0
         for_lines(nc, NY, [&](int c, int ky) {
             const size_t kb = (size_t)(k0 + c) * (fy + 1);
             const int kq = ky <= fy ? ky : NY - ky;
-            if (ncomp == 1) {
+            if (ncomp == 1 && kkind == 0) {
                 z[(size_t)c * ld + ky] = cscale<T>(z[(size_t)c * ld + ky], K0[kb + kq]);
+            } else if (ncomp == 1) {
+                // i s z, s odd in ky for kkind 2
+                const T sv = ksign * ((kkind == 2 && ky > fy) ? -K0[kb + kq] : K0[kb + kq]);
+                const C<T> v = z[(size_t)c * ld + ky];
+                z[(size_t)c * ld + ky] = mkc<T>(-sv * v.y, sv * v.x);
             } else {
                 // the xy kernel is odd in y: its real spectrum is odd in ky
                 const T kxx = K0[kb + kq], kxy = (ky <= fy) ? K1[kb + kq] : -K1[kb + kq], kyy = K2[kb + kq];
@@ -507,6 +516,7 @@ __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0
 constexpr int OUT_ALL = 0;      // u[i] = val for all elements
 constexpr int OUT_INT = 1;      // u[i] = val where igs >= Adhes (AllInt), others untouched
 constexpr int OUT_ADDINT = 2;   // u[i] += val where igs >= Adhes
+constexpr int OUT_ADDALL = 3;   // u[i] += val for all elements
 
 // step C: inverse row transforms, writes u (element-major)
 template <typename T, typename IO>
@@ -550,6 +560,9 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1
                 if (mode == OUT_ALL) {
                     out[i0] = v0;
                     if (has1) out[i0 + mx] = v1;
+                } else if (mode == OUT_ADDALL) {
+                    out[i0] += v0;
+                    if (has1) out[i0 + mx] += v1;
                 } else {
                     const int g0 = igs[i0], g1 = has1 ? igs[i0 + mx] : Exter;
                     const IO o0 = (mode == OUT_ADDINT && g0 >= Adhes) ? out[i0] : IO(0);
@@ -566,12 +579,13 @@ __device__ __noinline__ void conv_rows_inv(const Conv<T> &cv, IO *out0, IO *out1
 // full product u = A p.  Synchronises the patch group before and after.
 template <typename T, typename IO = double>
 __device__ void convolve(const Conv<T> &cv, const IO *in0, const IO *in1, IO *out0, IO *out1,
-                         int ncomp, const T *K0, const T *K1, const T *K2, int mode, const int *igs) {
+                         int ncomp, const T *K0, const T *K1, const T *K2, int mode, const int *igs,
+                         int kkind = 0, T ksign = T(1)) {
     gsync();
     long long t0 = clock64();
     conv_rows_fwd<T, IO>(cv, in0, in1, ncomp);
     gsync();
-    conv_cols<T>(cv, ncomp, K0, K1, K2);
+    conv_cols<T>(cv, ncomp, K0, K1, K2, kkind, ksign);
     gsync();
     conv_rows_inv<T, IO>(cv, out0, out1, ncomp, mode, igs);
     gsync();

@@ -141,18 +141,37 @@ __device__ __noinline__ void direct_rowsum(const PView &P, int ii, int nterm, co
 }
 
 // ------------------------------------------------------------------------------------------
-// products with A.  Spectra K[0..6] = xx, xy, yy, zz and the preconditioners zz, xx, yy.
+// products with A.  Spectra K[0..6] = xx, xy, yy, zz and the preconditioners zz, xx, yy;
+// K[7..10] the coupling blocks of K != 0.
 // ------------------------------------------------------------------------------------------
+constexpr int kMaxSpectra = 11;
+
 template <typename T>
 struct Ops {
     Conv<T> cv;
-    const T *K[7];          // xx, xy, yy, zz, M_zz, M_xx, M_yy
+    // xx, xy, yy, zz, M_zz, M_xx, M_yy; with K != 0 the imaginary spectra of xz, yz, and in
+    // steady rolling those of xz, yz of cs - cv (null when absent)
+    const T *K[kMaxSpectra];
 };
 
 // normal product out = A_zz in (kind 3) or M in (kind 4)
 template <typename T>
 __device__ inline void prod_n(const Ops<T> &op, const double *in, double *out, int mode, const int *igs, int kind) {
     convolve<T, double>(op.cv, in, nullptr, out, nullptr, 1, op.K[kind], nullptr, nullptr, mode, igs);
+}
+// coupling products (K != 0), FP64: (outx, outy) = A_tz in (xz, yz: spectra K[base], K[base + 1];
+// base 7 for cs, 9 for cs - cv of steady rolling), or out (+)= A_zt (inx, iny) = -(xz inx + yz iny)
+__device__ inline void prod_tz(const Ops<double> &op, const double *in, double *ox, double *oy, int mode,
+                               const int *igs, int base) {
+    convolve<double, double>(op.cv, in, nullptr, ox, nullptr, 1, op.K[base], nullptr, nullptr, mode, igs, 1);
+    convolve<double, double>(op.cv, in, nullptr, oy, nullptr, 1, op.K[base + 1], nullptr, nullptr, mode, igs, 2);
+}
+__device__ inline void prod_zt(const Ops<double> &op, const double *inx, const double *iny, double *out, bool add,
+                               const int *igs) {
+    convolve<double, double>(op.cv, inx, nullptr, out, nullptr, 1, op.K[7], nullptr, nullptr,
+                             add ? OUT_ADDINT : OUT_ALL, igs, 1, -1.0);
+    convolve<double, double>(op.cv, iny, nullptr, out, nullptr, 1, op.K[8], nullptr, nullptr,
+                             add ? OUT_ADDINT : OUT_ADDALL, igs, 2, -1.0);
 }
 // tangential product (outx, outy) = A_tt (inx, iny)
 template <typename T, typename IO = double>
@@ -355,14 +374,16 @@ __device__ __noinline__ int normcg(const PView &P, const Ops<T> &op, int maxcg, 
 // ------------------------------------------------------------------------------------------
 // snorm, m_snorm.f90:31-378.  Returns itnorm (-1 maxin, -2 NormCG divergence).
 // ------------------------------------------------------------------------------------------
+// htang (K != 0): the normal displacement A_zt p_t of the current tangential tractions, added to
+// the undeformed distance (m_snorm.f90:31-378)
 template <typename T>
 __device__ __noinline__ int snorm(const PView &P, const Ops<T> &op, int maxgs, int maxin, double eps, double &pen,
-                     int &itcg_out, int &nconv) {
+                     int &itcg_out, int &nconv, const double *htang = nullptr) {
     const int n = P.n, mx = P.mx, my = P.my;
     RedSmem &red = P.sm->red;
     int *igs = P.igs();
     double *pn = P.c(W_PN), *hstot = P.c(W_HSTOT), *h = P.c(W_H), *unn = P.c(W_DD), *one = P.c(W_ONE);
-    FOR_I(i, n) { hstot[i] = h[i]; one[i] = 1.0; }
+    FOR_I(i, n) { hstot[i] = htang ? h[i] + htang[i] : h[i]; one[i] = 1.0; }
     int itnorm = 0, itcg = 0;
     bool zready;
     do {
