@@ -22,6 +22,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <functional>
 #include <string>
 #include <vector>
 #include "../../include/contact_addon.h"
@@ -383,6 +384,11 @@ struct Arena {
     size_t cap_list = 0;
     double *h_io = nullptr;      // pinned staging
     size_t cap_hio = 0;
+    // per-patch completion flags in host-mapped memory (h_flags, seen by the device as
+    // d_flags) and the stream that copies finished patches back while the pass runs
+    int *h_flags = nullptr, *d_flags = nullptr;
+    size_t cap_flags = 0;
+    cudaStream_t copy_st = nullptr;
 };
 
 cudaError_t grow(void **ptr, size_t &cap, size_t need, bool pinned) {
@@ -398,8 +404,11 @@ thread_local Arena t_arena;
 // bytes moved by the last host<->device batch copy of this thread
 thread_local long long t_h2d_bytes = 0, t_d2h_bytes = 0;
 
-// runs the engine for all prepared entries with status 0; results go to the problems
-int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
+// runs the engine for all prepared entries with status 0; results go to the problems.
+// on_done (serving): called with the batch index of each patch as soon as its results are in
+// its problem, while the rest of the pass still runs; patches the pass leaves without a
+// completion flag (early returns) are collected when the pass has ended
+int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed, const std::function<void(int)> *on_done = nullptr) {
     const auto tb0 = std::chrono::steady_clock::now();
     std::vector<int> live;
     for (size_t i = 0; i < b.probs.size(); i++) if (b.status[i] == 0) live.push_back((int)i);
@@ -485,6 +494,17 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
         if (b.preps[live[k]].upload)
             stage_inputs(*b.probs[live[k]], hd[k], (double *)((char *)A.h_io + off_io[k]), !dev_prev[k]);
     }
+    if (on_done) {
+        if (A.cap_flags < (size_t)n) {
+            if (A.h_flags) { cudaFreeHost(A.h_flags); A.h_flags = A.d_flags = nullptr; A.cap_flags = 0; }
+            const size_t c = (size_t)n + n / 4 + 64;
+            if ((e = cudaHostAlloc((void **)&A.h_flags, c * sizeof(int), cudaHostAllocMapped)) != cudaSuccess) return (int)e;
+            if ((e = cudaHostGetDevicePointer((void **)&A.d_flags, A.h_flags, 0)) != cudaSuccess) return (int)e;
+            A.cap_flags = c;
+        }
+        if (!A.copy_st && (e = cudaStreamCreateWithFlags(&A.copy_st, cudaStreamNonBlocking)) != cudaSuccess) return (int)e;
+        for (int k = 0; k < n; k++) { ((volatile int *)A.h_flags)[k] = 0; hd[k].done = A.d_flags + k; }
+    }
     cudaStream_t st = cudaStreamPerThread;
     const auto tb1 = std::chrono::steady_clock::now();
     t_h2d_bytes = (long long)(n * sizeof(PatchDesc));
@@ -496,6 +516,48 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
         return (int)e;
     int rc = engine_run(hd.data(), A.d_desc, n, need_ic.data(), A.d_list, st);
     if (rc != 0) return rc;
+    if (on_done) {
+        std::vector<char> fin(n, 0);
+        std::vector<char> icf(n, 0);
+        for (int k : ic_fill) icf[k] = 1;
+        t_d2h_bytes = 0;
+        auto finish = [&](int k) -> cudaError_t {
+            const size_t bytes = patch_sizes(hd[k].mx, hd[k].my, hd[k].fx, hd[k].fy, hd[k].nblk, hd[k].ncf).io;
+            cudaError_t ce = cudaMemcpyAsync((char *)A.h_io + off_io[k], A.d_io + off_io[k], bytes,
+                                             cudaMemcpyDeviceToHost, A.copy_st);
+            if (ce == cudaSuccess) ce = cudaStreamSynchronize(A.copy_st);
+            if (ce != cudaSuccess) return ce;
+            t_d2h_bytes += (long long)bytes;
+            Problem &p = *b.probs[live[k]];
+            if (icf[k]) p.ic_valid = true;
+            if (hd[k].save) p.prev_valid = true;
+            collect(p, hd[k], (const double *)((const char *)A.h_io + off_io[k]));
+            fin[k] = 1;
+            (*on_done)(live[k]);
+            return cudaSuccess;
+        };
+        int left = n;
+        for (;;) {
+            bool any = false;
+            for (int k = 0; k < n; k++) {
+                if (fin[k] || ((volatile int *)A.h_flags)[k] == 0) continue;
+                if ((e = finish(k)) != cudaSuccess) return (int)e;
+                left--;
+                any = true;
+            }
+            if (left == 0) break;
+            if (!any) {
+                const cudaError_t q = cudaStreamQuery(st);
+                if (q == cudaSuccess) break;
+                if (q != cudaErrorNotReady) return (int)q;
+                std::this_thread::sleep_for(std::chrono::microseconds(200));
+            }
+        }
+        if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return (int)e;
+        for (int k = 0; k < n; k++)
+            if (!fin[k] && (e = finish(k)) != cudaSuccess) return (int)e;
+        return 0;
+    }
     if ((e = cudaMemcpyAsync(A.h_io, A.d_io, tot_io, cudaMemcpyDeviceToHost, st)) != cudaSuccess) return (int)e;
     t_d2h_bytes = (long long)tot_io;
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return (int)e;
@@ -512,18 +574,23 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed) {
     return 0;
 }
 
-int calculate_many(int n, const int *ire, const int *icp, int *ierror) {
+// on_done (serving): called with (batch index, ierror) for each entry as soon as it is
+// finished, after its problem has been released; entries refused before the pass are finished
+// before it starts
+int calculate_many(int n, const int *ire, const int *icp, int *ierror,
+                   const std::function<void(int, int)> *on_done = nullptr) {
     Batch b;
     b.probs.resize(n); b.preps.resize(n); b.status.assign(n, 0);
     auto t0 = std::chrono::steady_clock::now();
-    std::vector<std::unique_lock<std::mutex>> locks;
+    std::vector<std::unique_lock<std::mutex>> locks(n);
+    std::vector<char> fin(n, 0);
     for (int i = 0; i < n; i++) {
         Problem *p = lookup(ire[i], icp[i], true);
         b.probs[i] = p;
         if (!p) { b.status[i] = CNTC_err_icp; continue; }
         std::unique_lock<std::mutex> lk(p->busy, std::try_to_lock);
         if (!lk.owns_lock()) { b.status[i] = CNTC_err_other; continue; }   // same problem in use
-        locks.push_back(std::move(lk));
+        locks[i] = std::move(lk);
         p->ncase++;
         b.status[i] = prepare(*p, b.preps[i]);
         if (b.status[i] != 0) p->have = false;
@@ -531,15 +598,29 @@ int calculate_many(int n, const int *ire, const int *icp, int *ierror) {
     if (g_debug >= 2)
         std::fprintf(stderr, "contact_gb300: batch prepare %.3f s\n",
                      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
-    int rc = run_batch(b, t_arena, true);
+    // an entry's result: its problem's wall time (the pass's share, or the time until the entry
+    // finished in serving), then the problem is released
+    auto finish = [&](int i, int e, double dt) {
+        ierror[i] = e;
+        if (b.probs[i] && b.status[i] == 0) { b.probs[i]->twall += dt; b.probs[i]->tcpu += dt; }
+        if (locks[i].owns_lock()) locks[i].unlock();
+        fin[i] = 1;
+        if (on_done) (*on_done)(i, e);
+    };
+    if (on_done)
+        for (int i = 0; i < n; i++)
+            if (b.status[i] != 0) finish(i, b.status[i], 0.0);
+    std::function<void(int)> cb = [&](int i) {
+        finish(i, b.probs[i]->ierror,
+               std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count());
+    };
+    int rc = run_batch(b, t_arena, true, on_done ? &cb : nullptr);
     auto t1 = std::chrono::steady_clock::now();
     const double dt = std::chrono::duration<double>(t1 - t0).count();
     for (int i = 0; i < n; i++) {
-        if (!b.probs[i]) { ierror[i] = b.status[i]; continue; }
-        if (b.status[i] != 0) { ierror[i] = b.status[i]; continue; }
-        ierror[i] = (rc != 0) ? CNTC_err_other : b.probs[i]->ierror;
-        b.probs[i]->twall += dt / n;
-        b.probs[i]->tcpu += dt / n;
+        if (fin[i]) continue;
+        if (!b.probs[i] || b.status[i] != 0) { finish(i, b.status[i], 0.0); continue; }
+        finish(i, (rc != 0) ? CNTC_err_other : b.probs[i]->ierror, dt / n);
     }
     if (rc != 0 && g_debug >= 1) std::fprintf(stderr, "contact_gb300: engine error %d (%s)\n", rc, cudaGetErrorString((cudaError_t)rc));
     return rc;
@@ -856,7 +937,11 @@ struct AsyncReq {
 };
 
 struct Server {
-    static constexpr int kLanes = 4;
+    // a solve keeps its CTA for a long time (seconds for the larger patches), so the device is
+    // filled by many passes in flight, not by large ones: up to kLanes passes of at most
+    // kMaxPass requests each
+    static constexpr int kLanes = 64;
+    static constexpr size_t kMaxPass = 16;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<std::shared_ptr<AsyncReq>> queue;
@@ -880,7 +965,7 @@ struct Server {
                 cv_work.wait(lk, [&] { return stop || (!queue.empty() && held() + queue.front()->bytes <= budget) ||
                                              (!queue.empty() && in_flight == 0); });
                 if (stop && queue.empty()) return;
-                while (!queue.empty()) {
+                while (!queue.empty() && batch.size() < kMaxPass) {
                     const size_t b = queue.front()->bytes;
                     // a single request larger than the budget runs alone
                     if (held() + bytes + b > budget && !(batch.empty() && in_flight == 0)) break;
@@ -893,7 +978,17 @@ struct Server {
             std::vector<int> ire(batch.size()), icp(batch.size()), err(batch.size(), 0);
             for (size_t k = 0; k < batch.size(); k++) { ire[k] = batch[k]->ire; icp[k] = batch[k]->icp; }
             const auto t_start = std::chrono::steady_clock::now();
-            calculate_many((int)batch.size(), ire.data(), icp.data(), err.data());
+            // each request completes when its own patch has finished, not at the end of the pass
+            std::function<void(int, int)> done = [&](int k, int e) {
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    batch[k]->ierror = e;
+                    batch[k]->done = true;
+                    batch[k]->t_done = std::chrono::steady_clock::now();
+                }
+                cv_done.notify_all();
+            };
+            calculate_many((int)batch.size(), ire.data(), icp.data(), err.data(), &done);
             const auto now = std::chrono::steady_clock::now();
             if (g_debug >= 2)
                 std::fprintf(stderr, "contact_gb300: serving pass of %zu requests (%.1f MB) took %.3f s\n", batch.size(),
@@ -901,13 +996,7 @@ struct Server {
             {
                 std::lock_guard<std::mutex> lk(mu);
                 in_flight -= bytes;
-                for (size_t k = 0; k < batch.size(); k++) {
-                    batch[k]->ierror = err[k];
-                    batch[k]->done = true;
-                    batch[k]->t_done = now;
-                }
             }
-            cv_done.notify_all();
             cv_work.notify_all();
         }
     }

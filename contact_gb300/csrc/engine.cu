@@ -264,7 +264,7 @@ __device__ inline void make_ops(Ops<T> &op, const PatchDesc &d, unsigned char *s
     op.cv = make_conv<T>(d, smraw, sp);
     const size_t ksz = (size_t)(d.fx + 1) * (d.fy + 1);
     const T *base = (sizeof(T) == 8) ? (const T *)(const void *)d.spec64 : (const T *)(const void *)d.spec32;
-    for (int b = 0; b < kMaxSpectra; b++) op.K[b] = b < d.ncf + 3 ? base + b * ksz : nullptr;
+    for (int b = 0; b < kMaxSpectra; b++) op.K[b] = b < spectra_count(d.ncf) ? base + b * ksz : nullptr;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -273,8 +273,9 @@ __device__ inline void make_ops(Ops<T> &op, const PatchDesc &d, unsigned char *s
 // real, quadrant-symmetric conv-size spectrum of a spatial block src (layout of cf:
 // (dx + mx) + (dy + my) * 2mx); offsets |dx| <= mx-1, |dy| <= my-1 are placed at
 // (dx mod NX, dy mod NY).  S: scratch of nkx * NY complex.
-// imag: the block is odd in exactly one of x, y (the coupling blocks xz, yz), so that its
-// spectrum is imaginary: the imaginary part is stored.
+// imag: store the imaginary part instead of the real part (a block odd in exactly one of x, y,
+// such as the coupling blocks xz, yz, has an imaginary spectrum; the coupling blocks of cs - cv,
+// which have no parity in x, need both parts).
 __device__ __noinline__ void block_spectrum(const Conv<double> &cv, const double *src, double2 *S, double *K64,
                                             float *K32, double2 *a, double2 *b, bool imag = false) {
     const int mx = cv.mx, my = cv.my, NX = cv.NX, NY = cv.NY, nkx = cv.nkx, fy = cv.fy;
@@ -426,14 +427,18 @@ __global__ void __launch_bounds__(kThreads) k_spectra(const PatchDesc *descs, co
         }
         block_spectrum(cv, msp, S, K64 + (4 + k) * ksz, K32 + (4 + k) * ksz, a, b);
     }
-    // coupling blocks (K != 0): cf blocks 4 .. ncf - 1 -> spectra 7 .. ncf + 2
-    for (int blkc = 4; blkc < d.ncf; blkc++) {
+    // coupling blocks (K != 0): xz, yz (odd in x, resp. y: imaginary spectra) -> spectra 7, 8;
+    // in steady rolling xz, yz of cs - cv (no parity in x: real and imaginary parts) -> 9, 10
+    // and 11, 12
+    for (int q = 0; q < spectra_count(d.ncf) - 7; q++) {
+        const int blkc = q < 2 ? 4 + q : 6 + (q - 2) / 2;
+        const bool im = q < 2 ? true : ((q - 2) % 2 == 1);
         gsync();
         if (!blk) {
             make_twiddles<double>(cv.twx, cv.NX);
             make_twiddles<double>(cv.twy, cv.NY);
         }
-        block_spectrum(cv, d.cf + blkc * bsz, S, K64 + (blkc + 3) * ksz, K32 + (blkc + 3) * ksz, a, b, true);
+        block_spectrum(cv, d.cf + blkc * bsz, S, K64 + (7 + q) * ksz, K32 + (7 + q) * ksz, a, b, im);
     }
 }
 
@@ -991,7 +996,7 @@ __device__ __noinline__ int stang(const PView &P, TangRun &T, int &itgs_out) {
             FOR_I(i, n) un[i] = pn[i] - pvn[i];
             src = un;
         }
-        prod_tz(*T.op, src, ux, uy, OUT_ALL, igs, d.tang == 3 ? 9 : 7);
+        prod_tz(*T.op, src, ux, uy, OUT_ALL, igs, d.tang == 3);
         FOR_I(i, n) if (iel[i]) { wfx[i] += ux[i]; wfy[i] += uy[i]; }
         gsync();
     }
@@ -1110,7 +1115,7 @@ __device__ __noinline__ void soutpt(const PView &P, const Ops<T> &op, double pen
     // K != 0: the coupling terms of u = A p (all components, m_soutpt.f90:377-511)
     if (d.ncf >= 6) {
         prod_zt(op, px, py, un, true, igs);
-        prod_tz(op, pn, ux, uy, OUT_ADDINT, igs, 7);
+        prod_tz(op, pn, ux, uy, OUT_ADDINT, igs, false);
     }
     double a[4] = {0, 0, 0, 0};
     double b[2] = {0, 0};
@@ -1374,6 +1379,15 @@ __device__ __noinline__ void solve_patch(const PatchDesc &d, bool blk, unsigned 
         out[O_CETA] = T.ceta;
         for (int k = 0; k < 16; k++) out[O_SENS + k] = sens[k];
     }
+    // completion signal for the host: after the group barrier every result of the patch is in
+    // its io block; the system-scope fence orders them before the flag
+    if (d.done) {
+        gsync();
+        if (glead()) {
+            __threadfence_system();
+            *(volatile int *)d.done = 1;
+        }
+    }
 }
 
 // grid: one CTA per listed patch (mode 0); the nblk CTAs of one patch group (mode 1, cooperative
@@ -1439,8 +1453,8 @@ PatchSizes patch_sizes(int mx, int my, int fx, int fy, int nblk, int ncf) {
     const size_t ksz = (size_t)(fx + 1) * (fy + 1);
     s.io = align256(io_doubles((int)n) * sizeof(double));
     s.cf = align256((size_t)ncf * 4 * n * sizeof(double));
-    s.spec64 = align256((size_t)(ncf + 3) * ksz * sizeof(double));
-    s.spec32 = align256((size_t)(ncf + 3) * ksz * sizeof(float));
+    s.spec64 = align256((size_t)spectra_count(ncf) * ksz * sizeof(double));
+    s.spec32 = align256((size_t)spectra_count(ncf) * ksz * sizeof(float));
     size_t wkn = (size_t)(W_NCOL - kIoCols) * n;
     const size_t specscratch = spectra_scratch_doubles(mx, my, fx, fy) + 4 * n;   // k_spectra
     if (wkn < specscratch) wkn = specscratch;

@@ -76,6 +76,9 @@ struct PatchDesc {
     // save: where the solve leaves its own solution in the same layout (may equal prev), or nullptr.
     const double *prev;
     double *save;
+    // completion flag of the patch in host-mapped memory (serving), or nullptr: set to 1 after
+    // all results of the patch are in its io block and fenced at system scope
+    int *done;
     // io block: columns W_H .. W_SN (kIoCols * npot doubles), then O_NSCAL output scalars,
     // then the element division (npot ints).  Inputs (element-wise h, warm-start tractions
     // and element division) arrive and all results leave through this block.
@@ -86,8 +89,9 @@ struct PatchDesc {
     // (zx = -xz, zy = -yz) and, in steady rolling, xz and yz of cs - cv (cv: the grid shifted by
     // one rolling step)
     const double *cf;
-    // spectra [nspec][fx+1][fy+1]: xx, xy, yy, zz, M_zz, M_xx, M_yy, then the imaginary parts of
-    // the spectra of the coupling blocks of cf (nspec = 3 + ncf)
+    // spectra [spectra_count(ncf)][fx+1][fy+1]: xx, xy, yy, zz, M_zz, M_xx, M_yy; with K != 0 the
+    // imaginary parts of xz, yz, and in steady rolling the real and imaginary parts of xz and of
+    // yz of cs - cv
     const double *spec64;
     const float *spec32;
     void *rbuf;                       // 2 * (fx+1) * my complex doubles
@@ -100,6 +104,9 @@ struct PatchDesc {
 
 constexpr int kNumPhaseTimers = 10;  // O_T_TOTAL .. O_T_GSSER
 constexpr int kIoCols = W_HSTOT;      // W_H .. W_SN live in the io block
+
+// spectra of a patch with ncf coefficient blocks (PatchDesc::spec64)
+__host__ __device__ inline int spectra_count(int ncf) { return ncf >= 8 ? 13 : (ncf >= 6 ? 9 : 7); }
 
 __host__ __device__ inline size_t io_doubles(int npot) {
     return (size_t)kIoCols * npot + O_NSCAL + (size_t)(npot + 1) / 2;

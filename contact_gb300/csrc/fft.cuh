@@ -463,9 +463,10 @@ __device__ __noinline__ void conv_rows_fwd(const Conv<T> &cv, const IO *in0, con
 // ncomp == 1: u = K0 p ; ncomp == 2: (ux,uy) = [[Kxx, Kxy],[Kxy, Kyy]] (px,py) with
 // K = {Kxx, Kxy, Kyy}.  Kernel blocks are (fx+1) x (fy+1) real, [kx][ky].  A batch holds cap
 // columns, each as ncomp lines (stride NY + 1 complex).
-// One component (ncomp = 1) may take a coupling kernel (kkind 1: odd in x, even in y; 2: even
-// in x, odd in y) whose spectrum is imaginary; K0 then holds its imaginary part, and ksign
-// scales the product (the blocks zx = -xz, zy = -yz).
+// One component (ncomp = 1) may take a coupling kernel: kkind 1 (odd in x, even in y) and 2
+// (even in x, odd in y) have imaginary spectra, K0 holds the imaginary part; kkind 3 (even in
+// y) and 4 (odd in y) have no parity in x and complex spectra, K0 and K1 hold the real and
+// imaginary parts.  ksign scales the product (the blocks zx = -xz, zy = -yz).
 template <typename T>
 __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0, const T *K1, const T *K2,
                                        int kkind = 0, T ksign = T(1)) {
@@ -488,11 +489,17 @@ __device__ __noinline__ void conv_cols(const Conv<T> &cv, int ncomp, const T *K0
             const int kq = ky <= fy ? ky : NY - ky;
             if (ncomp == 1 && kkind == 0) {
                 z[(size_t)c * ld + ky] = cscale<T>(z[(size_t)c * ld + ky], K0[kb + kq]);
-            } else if (ncomp == 1) {
+            } else if (ncomp == 1 && kkind <= 2) {
                 // i s z, s odd in ky for kkind 2
                 const T sv = ksign * ((kkind == 2 && ky > fy) ? -K0[kb + kq] : K0[kb + kq]);
                 const C<T> v = z[(size_t)c * ld + ky];
                 z[(size_t)c * ld + ky] = mkc<T>(-sv * v.y, sv * v.x);
+            } else if (ncomp == 1) {
+                // (kr + i ki) z, the spectrum mirrored in ky with the kernel's parity in y
+                const T sg = (kkind == 4 && ky > fy) ? -ksign : ksign;
+                const T kr = sg * K0[kb + kq], ki = sg * K1[kb + kq];
+                const C<T> v = z[(size_t)c * ld + ky];
+                z[(size_t)c * ld + ky] = mkc<T>(kr * v.x - ki * v.y, kr * v.y + ki * v.x);
             } else {
                 // the xy kernel is odd in y: its real spectrum is odd in ky
                 const T kxx = K0[kb + kq], kxy = (ky <= fy) ? K1[kb + kq] : -K1[kb + kq], kyy = K2[kb + kq];

@@ -144,13 +144,13 @@ __device__ __noinline__ void direct_rowsum(const PView &P, int ii, int nterm, co
 // products with A.  Spectra K[0..6] = xx, xy, yy, zz and the preconditioners zz, xx, yy;
 // K[7..10] the coupling blocks of K != 0.
 // ------------------------------------------------------------------------------------------
-constexpr int kMaxSpectra = 11;
+constexpr int kMaxSpectra = 13;
 
 template <typename T>
 struct Ops {
     Conv<T> cv;
     // xx, xy, yy, zz, M_zz, M_xx, M_yy; with K != 0 the imaginary spectra of xz, yz, and in
-    // steady rolling those of xz, yz of cs - cv (null when absent)
+    // steady rolling the real and imaginary parts of xz and of yz of cs - cv (null when absent)
     const T *K[kMaxSpectra];
 };
 
@@ -159,12 +159,18 @@ template <typename T>
 __device__ inline void prod_n(const Ops<T> &op, const double *in, double *out, int mode, const int *igs, int kind) {
     convolve<T, double>(op.cv, in, nullptr, out, nullptr, 1, op.K[kind], nullptr, nullptr, mode, igs);
 }
-// coupling products (K != 0), FP64: (outx, outy) = A_tz in (xz, yz: spectra K[base], K[base + 1];
-// base 7 for cs, 9 for cs - cv of steady rolling), or out (+)= A_zt (inx, iny) = -(xz inx + yz iny)
+// coupling products (K != 0), FP64: (outx, outy) = A_tz in through the xz, yz blocks of cs
+// (imaginary spectra K[7], K[8]; csv false) or, in steady rolling, of cs - cv (complex spectra
+// K[9], K[10] and K[11], K[12]; csv true); or out (+)= A_zt (inx, iny) = -(xz inx + yz iny)
 __device__ inline void prod_tz(const Ops<double> &op, const double *in, double *ox, double *oy, int mode,
-                               const int *igs, int base) {
-    convolve<double, double>(op.cv, in, nullptr, ox, nullptr, 1, op.K[base], nullptr, nullptr, mode, igs, 1);
-    convolve<double, double>(op.cv, in, nullptr, oy, nullptr, 1, op.K[base + 1], nullptr, nullptr, mode, igs, 2);
+                               const int *igs, bool csv) {
+    if (!csv) {
+        convolve<double, double>(op.cv, in, nullptr, ox, nullptr, 1, op.K[7], nullptr, nullptr, mode, igs, 1);
+        convolve<double, double>(op.cv, in, nullptr, oy, nullptr, 1, op.K[8], nullptr, nullptr, mode, igs, 2);
+    } else {
+        convolve<double, double>(op.cv, in, nullptr, ox, nullptr, 1, op.K[9], op.K[10], nullptr, mode, igs, 3);
+        convolve<double, double>(op.cv, in, nullptr, oy, nullptr, 1, op.K[11], op.K[12], nullptr, mode, igs, 4);
+    }
 }
 __device__ inline void prod_zt(const Ops<double> &op, const double *inx, const double *iny, double *out, bool add,
                                const int *igs) {
