@@ -120,6 +120,7 @@ _PROTOS = {
     "cntc_gb300_resident_graphs": [],
     "cntc_gb300_lastcopybytes": [ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)],
     "cntc_gb300_fmapeaks": [_DP],
+    "cntc_gb300_latencyshapes": [_IP, _IP, _IP],
 }
 
 
@@ -137,7 +138,7 @@ def load(path=None):
         f = getattr(lib, name)
         f.argtypes = args
         f.restype = {"cntc_gb300_kernel_launches": ctypes.c_longlong, "cntc_gb300_fmapeaks": ctypes.c_int,
-                     "cntc_gb300_resident_graphs": ctypes.c_int}.get(name)
+                     "cntc_gb300_resident_graphs": ctypes.c_int, "cntc_gb300_latencyshapes": ctypes.c_int}.get(name)
     _lib = lib
     return lib
 
@@ -401,6 +402,16 @@ def lastcopybytes():
     a, b = ctypes.c_longlong(), ctypes.c_longlong()
     load().cntc_gb300_lastcopybytes(ctypes.byref(a), ctypes.byref(b))
     return a.value, b.value
+
+
+def latency_shapes():
+    """Launch shapes tuned so far for single-patch calls: {size class c: True (patch group) or
+    False (one CTA)} for grids of 2**c .. 2**(c+1) - 1 elements."""
+    cls = (ctypes.c_int * 32)()
+    grp = (ctypes.c_int * 32)()
+    cap = ctypes.c_int(32)
+    k = load().cntc_gb300_latencyshapes(ctypes.cast(cls, _IP), ctypes.cast(grp, _IP), ctypes.byref(cap))
+    return {int(cls[i]): bool(grp[i]) for i in range(k)}
 
 
 def fma_peaks():

@@ -179,7 +179,11 @@ struct Prep {
     bool upload;          // io block carries inputs (element-wise h or warm start)
 };
 
-int prepare(Problem &p, Prep &out) {
+int latency_ctas(int mx, int my, int fx, int fy);
+
+// latency: the call solves this patch alone (a single cntc_calculate), so that a cooperative
+// group of CTAs may take it (latency_ctas) when the grid is large enough to pay for the group
+int prepare(Problem &p, Prep &out, bool latency = false) {
     std::memset(&out.d, 0, sizeof(PatchDesc));
     PatchDesc &d = out.d;
     // combined material constants, combin_mater (m_hierarch_data.f90:1543-1553)
@@ -244,7 +248,7 @@ int prepare(Problem &p, Prep &out) {
     const int fx = cgb::opt_fft_size(mx), fy = cgb::opt_fft_size(my);
     // one CTA per patch while its FFT lines fit the per-warp buffers, a cooperative group of
     // CTAs for larger grids (or when CNTC_if_groupctas asks for one)
-    const int nblk = cgb::group_size(mx, my, fx, fy, p.group);
+    const int nblk = (latency && p.group == 0) ? latency_ctas(mx, my, fx, fy) : cgb::group_size(mx, my, fx, fy, p.group);
     if (nblk < 1) { log_msg("patch too large for the device (shared memory of one FFT line)"); return CNTC_err_other; }
     d.nblk = nblk;
     d.mx = mx; d.my = my; d.npot = mx * my; d.fx = fx; d.fy = fy;
@@ -389,13 +393,25 @@ struct Arena {
     int *h_flags = nullptr, *d_flags = nullptr;
     size_t cap_flags = 0;
     cudaStream_t copy_st = nullptr;
+    // pinned host buffers replaced by larger ones: freeing pinned memory synchronises the whole
+    // device, which would stall every other pass in flight, so they are kept until the thread
+    // that owns the arena exits
+    std::vector<void *> retired_host;
+    ~Arena() { for (void *q : retired_host) cudaFreeHost(q); }
 };
 
-cudaError_t grow(void **ptr, size_t &cap, size_t need, bool pinned) {
+// Device buffers come from the stream-ordered allocator on the caller's stream: a replaced
+// buffer is released after the work queued before it on that stream, without the device-wide
+// synchronisation of cudaFree (other threads' passes keep running).
+cudaError_t grow(void **ptr, size_t &cap, size_t need, bool pinned, cudaStream_t st, std::vector<void *> &retired) {
     if (need <= cap) return cudaSuccess;
-    if (*ptr) { if (pinned) cudaFreeHost(*ptr); else cudaFree(*ptr); *ptr = nullptr; cap = 0; }
+    if (*ptr) {
+        if (pinned) retired.push_back(*ptr);
+        else cudaFreeAsync(*ptr, st);
+        *ptr = nullptr; cap = 0;
+    }
     size_t c = need + need / 4 + 4096;
-    cudaError_t e = pinned ? cudaMallocHost(ptr, c) : cudaMalloc(ptr, c);
+    cudaError_t e = pinned ? cudaMallocHost(ptr, c) : cudaMallocAsync(ptr, c, st);
     if (e == cudaSuccess) cap = c;
     return e;
 }
@@ -425,11 +441,14 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed, const std::function<voi
         any_upload |= b.preps[live[k]].upload;
     }
     cudaError_t e;
-    if ((e = grow((void **)&A.d_io, A.cap_io, tot_io, false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.d_work, A.cap_work, tot_work, false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.d_desc, A.cap_desc, n * sizeof(PatchDesc), false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.d_list, A.cap_list, 3 * n * sizeof(int) + 64, false)) != cudaSuccess) return (int)e;
-    if ((e = grow((void **)&A.h_io, A.cap_hio, tot_io, true)) != cudaSuccess) return (int)e;
+    const cudaStream_t gst = cudaStreamPerThread;
+    auto &rt = A.retired_host;
+    if ((e = grow((void **)&A.d_io, A.cap_io, tot_io, false, gst, rt)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_work, A.cap_work, tot_work, false, gst, rt)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_desc, A.cap_desc, n * sizeof(PatchDesc), false, gst, rt)) != cudaSuccess) return (int)e;
+    if ((e = grow((void **)&A.d_list, A.cap_list, 3 * n * sizeof(int) + 64, false, gst, rt)) != cudaSuccess)
+        return (int)e;
+    if ((e = grow((void **)&A.h_io, A.cap_hio, tot_io, true, gst, rt)) != cudaSuccess) return (int)e;
     std::vector<PatchDesc> hd(n);
     std::vector<unsigned char> need_ic(n, 1);
     std::vector<int> ic_fill;     // patches whose coefficient cache this pass fills
@@ -496,7 +515,7 @@ int run_batch(Batch &b, Arena &A, bool reuse_ic_allowed, const std::function<voi
     }
     if (on_done) {
         if (A.cap_flags < (size_t)n) {
-            if (A.h_flags) { cudaFreeHost(A.h_flags); A.h_flags = A.d_flags = nullptr; A.cap_flags = 0; }
+            if (A.h_flags) { A.retired_host.push_back(A.h_flags); A.h_flags = A.d_flags = nullptr; A.cap_flags = 0; }
             const size_t c = (size_t)n + n / 4 + 64;
             if ((e = cudaHostAlloc((void **)&A.h_flags, c * sizeof(int), cudaHostAllocMapped)) != cudaSuccess) return (int)e;
             if ((e = cudaHostGetDevicePointer((void **)&A.d_flags, A.h_flags, 0)) != cudaSuccess) return (int)e;
@@ -592,7 +611,7 @@ int calculate_many(int n, const int *ire, const int *icp, int *ierror,
         if (!lk.owns_lock()) { b.status[i] = CNTC_err_other; continue; }   // same problem in use
         locks[i] = std::move(lk);
         p->ncase++;
-        b.status[i] = prepare(*p, b.preps[i]);
+        b.status[i] = prepare(*p, b.preps[i], n == 1 && !on_done);
         if (b.status[i] != 0) p->have = false;
     }
     if (g_debug >= 2)
@@ -624,6 +643,85 @@ int calculate_many(int n, const int *ire, const int *icp, int *ierror,
     }
     if (rc != 0 && g_debug >= 1) std::fprintf(stderr, "contact_gb300: engine error %d (%s)\n", rc, cudaGetErrorString((cudaError_t)rc));
     return rc;
+}
+
+// ------------------------------------------------------------------------------------------
+// launch shape of a single-patch call, tuned per size class.  A patch solved alone by one CTA
+// uses one SM of the device; a cooperative group of CTAs (one per 256 elements) solves it
+// sooner once the grid is large enough for the group barriers to pay.  For each size class
+// (element count in a factor-of-two band, from kLatencyMinElements to kMaxGroupGsElements, the
+// largest group that still runs SteadyGS) the first single-patch call on a device times a
+// synthetic normal problem of that class (Hertzian, square grid, the middle of the band) in both
+// shapes and keeps the faster one.  Batches and serving passes keep one CTA per patch, which
+// is the throughput form.
+// ------------------------------------------------------------------------------------------
+constexpr int kLatencyMinElements = 4096;
+constexpr int kElementsPerCta = 256;                 // group_size: one element per thread of a CTA
+
+struct ShapeTuner {
+    std::mutex mu;
+    std::map<std::pair<int, int>, int> group;      // (device, size class) -> 1: group, 0: one CTA
+};
+ShapeTuner &shape_tuner() {
+    static ShapeTuner t;
+    return t;
+}
+
+// seconds of one warm pass of the synthetic problem (side x side) with group request req
+double time_shape(int side, int req) {
+    Problem q;
+    q.tang = 0; q.norm = 1; q.fn = 1.0; q.eps = 1e-6;
+    q.ipotcn = -3; q.mx = side; q.my = side; q.hz_aa = 1.0; q.hz_bb = 1.0; q.hz_scale = 1.1;
+    q.group = req;
+    double best = 1e30;
+    for (int rep = 0; rep < 3; rep++) {
+        Batch b;
+        b.probs = {&q}; b.preps.resize(1); b.status = {0};
+        if (prepare(q, b.preps[0]) != 0) return 1e30;
+        const auto t0 = std::chrono::steady_clock::now();
+        const int rc = run_batch(b, t_arena, false);
+        const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (rc != 0) { cudaGetLastError(); return 1e30; }
+        if (rep > 0) best = std::min(best, t);      // the first pass includes first-use costs
+    }
+    return best;
+}
+
+int latency_ctas(int mx, int my, int fx, int fy) {
+    const int n = mx * my;
+    const int automatic = cgb::group_size(mx, my, fx, fy, 0);
+    if (n < kLatencyMinElements || n > kMaxGroupGsElements || automatic != 1) return automatic;
+    int cls = 0;
+    while ((2 << cls) <= n) cls++;                   // 2^cls <= n < 2^(cls + 1)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    ShapeTuner &t = shape_tuner();
+    std::lock_guard<std::mutex> lk(t.mu);
+    auto it = t.group.find({dev, cls});
+    if (it == t.group.end()) {
+        const int side = (int)std::lround(std::sqrt(1.5 * (double)(1 << cls)));
+        const int g = std::max(2, (side * side + kElementsPerCta - 1) / kElementsPerCta);
+        const double t1 = time_shape(side, 1), tg = time_shape(side, g);
+        if (g_debug >= 1)
+            std::fprintf(stderr, "contact_gb300: single-patch calls of %d..%d elements: one CTA %.4f s, "
+                                 "a group of %d CTAs %.4f s\n", 1 << cls, (2 << cls) - 1, t1, g, tg);
+        it = t.group.emplace(std::make_pair(dev, cls), tg < t1 ? 1 : 0).first;
+    }
+    if (!it->second) return 1;
+    const int g = cgb::group_size(mx, my, fx, fy, std::max(2, (n + kElementsPerCta - 1) / kElementsPerCta));
+    return g >= 2 ? g : 1;
+}
+
+// the sizes chosen so far, for the diagnostics of cntc_gb300_latencyshapes
+int latency_shapes(int *cls, int *grp, int cap) {
+    ShapeTuner &t = shape_tuner();
+    std::lock_guard<std::mutex> lk(t.mu);
+    int k = 0;
+    for (const auto &e : t.group) {
+        if (k >= cap) break;
+        cls[k] = e.first.second; grp[k] = e.second; k++;
+    }
+    return k;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1724,6 +1822,8 @@ void cntc_gb300_resident_solve(int *nrep, double *times, int *ierror) {
         if (g_debug >= 1) std::fprintf(stderr, "contact_gb300: resident solve error %d\n", rc);
     }
 }
+
+int cntc_gb300_latencyshapes(int *cls, int *group, int *cap) { return latency_shapes(cls, group, *cap); }
 
 int cntc_gb300_resident_graphs(void) {
     std::lock_guard<std::mutex> lk(g_res_mu);

@@ -577,7 +577,6 @@ __device__ __noinline__ void compute_facdt(const PView &P, int solver, double *f
     gsync();
 }
 
-constexpr int kMaxGroupGsElements = 40000;
 
 // state of TANG shared by the solver dispatch and the Newton-Raphson on total forces
 struct TangRun {

@@ -105,6 +105,10 @@ struct PatchDesc {
 constexpr int kNumPhaseTimers = 10;  // O_T_TOTAL .. O_T_GSSER
 constexpr int kIoCols = W_HSTOT;      // W_H .. W_SN live in the io block
 
+// SteadyGS and ConvexGS visit the elements one after another: a patch group refuses them above
+// this many elements (a sweep would take seconds)
+constexpr int kMaxGroupGsElements = 40000;
+
 // spectra of a patch with ncf coefficient blocks (PatchDesc::spec64)
 __host__ __device__ inline int spectra_count(int ncf) { return ncf >= 8 ? 13 : (ncf >= 6 ? 9 : 7); }
 

@@ -14,6 +14,7 @@
  *   cntc_gb300_getsolverstats   convolution counts and per-phase cycle counts of the last solve
  *   cntc_gb300_resident_*       solve a staged batch repeatedly on device-resident inputs
  *   cntc_gb300_fmapeaks         measured FP64 / FP32 FMA peaks of the device
+ *   cntc_gb300_latencyshapes    launch shapes tuned per size class for single-patch calls
  *   flag CNTC_if_mixedprec      (cntc_setflags) 1: FP32 convolutions + FP64 refinement
  *   flag CNTC_if_groupctas      (cntc_setflags) CTAs per patch: one, or a cooperative group
  */
@@ -228,6 +229,11 @@ int cntc_gb300_resident_graphs(void);
  * events: out[0] FP64, out[1] FP32, in TFLOP/s.  The denominators of the patch-solve kernel's
  * arithmetic roofline.  Returns 0, or -1 when a measurement failed. */
 int cntc_gb300_fmapeaks(double *out);
+/* extension (no reference counterpart): launch shapes chosen so far for single-patch calls
+ * (cntc_calculate): per entry the size class c (grids of 2^c .. 2^(c+1) - 1 elements) and
+ * whether a cooperative group of CTAs (1) or one CTA (0) solves it, as timed on the device the
+ * first time the class was met.  Returns the number of entries written (at most *cap). */
+int cntc_gb300_latencyshapes(int *cls, int *group, int *cap);
 
 #ifdef __cplusplus
 }

@@ -125,3 +125,16 @@ def test_large_256_mixed_against_fp64(large256):
     fe = force_err(mixed, plain, case["fstat"])
     assert fe["fn"] <= 1e-10 and fe["ft"] <= MIXED_FORCE_TOL * 10, fe
     assert int((mixed["igs"] != plain["igs"]).sum()) <= 2
+
+
+def test_single_call_launch_shape(cntc, oracle):
+    """A single cntc_calculate of a 96 x 96 patch (size class 2^13 elements) takes the launch
+    shape timed fastest for that class on this device, one CTA or a patch group; either way the
+    result is the oracle's."""
+    case = C.config0(gausei=5, eps=1e-8, mx=96, my=96)
+    g = run_gpu(cntc, case, ire=130)
+    shapes = cntc.latency_shapes()
+    assert 13 in shapes, shapes
+    assert (ctas(cntc, 130) > 1) == shapes[13]
+    o = C.oracle_solve(case)
+    assert_parity(g, o, case, iterations=False)
