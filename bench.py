@@ -676,19 +676,31 @@ def run_perfc(args, dist):
     cg.setup_case(199, 1, inp.materialize(gold[0]["case"]))
     cg.calculate(199, 1)
     cg.finalize(199)
-    for k, g in enumerate(gold):
-        case = inp.materialize(g["case"])
-        ire = 200 + k
+    def timed(ire, case):
         cg.setup_case(ire, 2, case)
         torch.cuda.synchronize()
         t = time.perf_counter()
         ierr = cg.calculate(ire, 2)
         torch.cuda.synchronize()
-        dt = time.perf_counter() - t
+        return ierr, time.perf_counter() - t
+
+    for k, g in enumerate(gold):
+        case = inp.materialize(g["case"])
+        ire = 200 + k
+        ierr, dt = timed(ire, case)
         r = cg.results(ire, 2)
         ref = g["reference"]
         row = {"name": g["name"], "grid": case["potprm"][:2], "ierror": ierr, "s": dt, "ref_s": ref["wall_s"],
                "speedup": ref["wall_s"] / dt if dt > 0 else None, "ctas": int(cg.getsolverstats(ire, 2)["ctas"])}
+        # the launch shape tuned per size class (CNTC_if_groupctas = -1): the first call of a
+        # class times both shapes, so a warm-up call on another problem precedes the timed one
+        tcase = dict(case, group=-1)
+        timed(400 + k, tcase)
+        cg.finalize(400 + k)
+        ierr_t, dt_t = timed(600 + k, tcase)
+        row.update(s_tuned=dt_t, speedup_tuned=ref["wall_s"] / dt_t if dt_t > 0 else None,
+                   ctas_tuned=int(cg.getsolverstats(600 + k, 2)["ctas"]), ierror_tuned=ierr_t)
+        cg.finalize(600 + k)
         if "ncon" in ref:
             row.update(ncon=r["ncon"], itcg=r["itcg"], ref_ncon=ref["ncon"], ref_itcg=ref["itcg"])
         else:
@@ -698,12 +710,14 @@ def run_perfc(args, dist):
     if dist.rank != 0:
         return None
     tot, tot_ref = sum(r["s"] for r in rows), sum(r["ref_s"] for r in rows)
+    tot_tuned = sum(r["s_tuned"] for r in rows)
     return {"metric": METRIC, "value": len(rows) / tot, "unit": UNIT, "n_gpus": dist.world, "steps": 1,
             "warmup": 1, "ms_per_step": tot * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "the reference's performance inputs (perfc_test)", "mode": "perfc",
             "config": {"workload": "perfc_test normal problems 1p-8p, 1f-4f and shift problems 1s-8s, FP64, "
-                                   "one cntc_calculate each"},
-            "total_s": tot, "reference_total_s": tot_ref, "cases": rows}
+                                   "one cntc_calculate each; s: default launch shape, s_tuned: the shape "
+                                   "tuned per size class (CNTC_if_groupctas = -1)"},
+            "total_s": tot, "total_s_tuned": tot_tuned, "reference_total_s": tot_ref, "cases": rows}
 
 
 def main():

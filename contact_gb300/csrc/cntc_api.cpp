@@ -181,8 +181,9 @@ struct Prep {
 
 int latency_ctas(int mx, int my, int fx, int fy);
 
-// latency: the call solves this patch alone (a single cntc_calculate), so that a cooperative
-// group of CTAs may take it (latency_ctas) when the grid is large enough to pay for the group
+// latency: the call solves this patch alone (a single cntc_calculate); with CNTC_if_groupctas
+// = -1 a cooperative group of CTAs then takes it when that was timed faster for its size class
+// (latency_ctas).  Batches, serving passes and the default (0) keep one CTA per patch.
 int prepare(Problem &p, Prep &out, bool latency = false) {
     std::memset(&out.d, 0, sizeof(PatchDesc));
     PatchDesc &d = out.d;
@@ -248,7 +249,8 @@ int prepare(Problem &p, Prep &out, bool latency = false) {
     const int fx = cgb::opt_fft_size(mx), fy = cgb::opt_fft_size(my);
     // one CTA per patch while its FFT lines fit the per-warp buffers, a cooperative group of
     // CTAs for larger grids (or when CNTC_if_groupctas asks for one)
-    const int nblk = (latency && p.group == 0) ? latency_ctas(mx, my, fx, fy) : cgb::group_size(mx, my, fx, fy, p.group);
+    const int nblk = (latency && p.group == -1) ? latency_ctas(mx, my, fx, fy)
+                                                : cgb::group_size(mx, my, fx, fy, std::max(0, p.group));
     if (nblk < 1) { log_msg("patch too large for the device (shared memory of one FFT line)"); return CNTC_err_other; }
     d.nblk = nblk;
     d.mx = mx; d.my = my; d.npot = mx * my; d.fx = fx; d.fy = fy;
@@ -646,9 +648,11 @@ int calculate_many(int n, const int *ire, const int *icp, int *ierror,
 }
 
 // ------------------------------------------------------------------------------------------
-// launch shape of a single-patch call, tuned per size class.  A patch solved alone by one CTA
-// uses one SM of the device; a cooperative group of CTAs (one per 256 elements) solves it
-// sooner once the grid is large enough for the group barriers to pay.  For each size class
+// launch shape of a single-patch call, tuned per size class (CNTC_if_groupctas = -1).  A patch
+// solved alone by one CTA uses one SM of the device; a cooperative group of CTAs (one per 256
+// elements) solves it sooner once the grid is large enough for the group barriers to pay.  The
+// group's reductions sum in another order, so its results agree with the one-CTA form to
+// rounding, not bit for bit; the default therefore keeps one CTA.  For each size class
 // (element count in a factor-of-two band, from kLatencyMinElements to kMaxGroupGsElements, the
 // largest group that still runs SteadyGS) the first single-patch call on a device times a
 // synthetic normal problem of that class (Hertzian, square grid, the middle of the band) in both
@@ -1222,7 +1226,7 @@ void cntc_setflags(int *ire, int *icp, int *lenflg, int *params, int *values) {
             case CNTC_ic_return: p->ret = std::max(0, std::min(3, v)); break;
             case CNTC_if_ncase: p->ncase = std::max(0, v - 1); break;
             case CNTC_if_mixedprec: p->mixed = (v >= 0 && v <= 4) ? v : 1; break;
-            case CNTC_if_groupctas: p->group = std::max(0, v); break;
+            case CNTC_if_groupctas: p->group = std::max(-1, v); break;
             default: break;   // output, debugging and module-1 flags have no effect here
         }
     }
