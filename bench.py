@@ -251,6 +251,40 @@ def cpu_sample_rate(cases, seed, threads=None, nstrata=None):
     return rate, threads, desc, wall
 
 
+def small_patch_latency(cg, reps=5):
+    """One small patch in a single call: the 21 x 21 Hertzian steady-rolling case of the smoke
+    test (GDsteady, FP64, eps 1e-10) through cntc_calculate (wall time, host buffers, median of
+    reps calls on a fresh problem each, after one warm-up call), beside the oracle's baseline
+    build on one core."""
+    import torch
+    case = C.config0(gausei=5, eps=1e-10, mx=21, my=21)
+    gpu = []
+    for r in range(reps + 1):
+        cg.setup_case(900 + r, 1, case)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        cg.calculate(900 + r, 1)
+        torch.cuda.synchronize()
+        if r > 0:
+            gpu.append(time.perf_counter() - t)
+        st, it = cg.getsolverstats(900 + r, 1), cg.getiterationcounts(900 + r, 1)
+        cg.finalize(900 + r)
+    tot = max(st["t_total"], 1.0)
+    phases = {k[2:]: round(st[k] / tot, 3) for k in ("t_norm", "t_tang", "t_conv", "t_ls", "t_scan", "t_diag")}
+    import pyoracle as po
+    po.build()
+    cpu = []
+    for r in range(reps):
+        t = time.perf_counter()
+        C.oracle_solve(case, fast=True)
+        cpu.append(time.perf_counter() - t)
+    return {"case": "21 x 21 Hertzian steady rolling, GDsteady, FP64, eps 1e-10, one cntc_calculate",
+            "gpu_ms": float(np.median(gpu) * 1e3), "cpu_one_core_ms": float(np.median(cpu) * 1e3),
+            "kernel_ms": st["t_total"] / 2.07e6, "gd_iterations": it["itgs"], "nconv64": st["nconv64"],
+            "phase_share_of_sm_cycles": phases,
+            "note": "single-call latency of one small patch (one CTA); the CPU is the oracle's baseline build"}
+
+
 # ------------------------------------------------------------------------------------------
 # GB300 arm
 # ------------------------------------------------------------------------------------------
@@ -387,9 +421,11 @@ def run_gb300(args, dist):
                          "solve time in that pass); force error = |dF_t| / max(|F_t|, 1e-3 mu Fn) of the mixed "
                          "form against this FP64 form" % len(pc)}
     cpu = None
+    small = None
     if dist.rank == 0 and not args.no_cpu_baseline:
         rate, thr, desc, _ = cpu_sample_rate(cases, args.seed, threads=args.cpu_threads or None)
         cpu = {"value": rate, "unit": UNIT, "cores": thr, "kind": "port", "sample": desc}
+        small = small_patch_latency(cg)
     if dist.rank != 0:
         return None
     out = {
@@ -425,6 +461,7 @@ def run_gb300(args, dist):
                 "errors": int((np.asarray(e_err) < 0).sum()),
                 "note": "one cntc_calculate_batch call, including the first-call allocation of its staging arena"},
         "plain_fp64": plain,
+        "small_patch": small,
         "clocks": clk,
         "gpu_launches": int(gpu_launches),
     }
