@@ -287,6 +287,48 @@ def setadmissionbudget(gbytes):
     load().cntc_gb300_setadmissionbudget(ctypes.byref(ctypes.c_double(float(gbytes))))
 
 
+# ------------------------------------------------------------------------------------------
+# subsurface stresses (subs_addBlock, subs_calculate, subs_getBlocksize, subs_getResults)
+# ------------------------------------------------------------------------------------------
+SUBS_COLUMNS = ("x", "y", "z", "ux", "uy", "uz", "sighyd", "sigvm", "sigtr", "sigma1", "sigma2", "sigma3",
+                "sigxx", "sigyx", "sigzx", "sigxy", "sigyy", "sigzy", "sigxz", "sigyz", "sigzz")
+
+
+def subs_addblock(ire, icp, iblk, isubs, xparam=(), yparam=(), zparam=()):
+    """Block iblk of subsurface points (types 1-3, 5-7: element centres; 9: x, y lists)."""
+    xa = np.ascontiguousarray(xparam, dtype=np.float64).reshape(-1)
+    ya = np.ascontiguousarray(yparam, dtype=np.float64).reshape(-1)
+    za = np.ascontiguousarray(zparam, dtype=np.float64).reshape(-1)
+    dummy = np.zeros(1)
+    ptr = lambda a: (a if a.size else dummy).ctypes.data_as(_DP)
+    load().subs_addblock(_i(ire), _i(icp), _i(iblk), _i(isubs), _i(xa.size), _i(ya.size), _i(za.size),
+                         ptr(xa), ptr(ya), ptr(za))
+
+
+def subs_calculate(ire, icp):
+    """Subsurface field of the last solution at all blocks of (ire, icp); returns ierror."""
+    e = ctypes.c_int(0)
+    load().subs_calculate(_i(ire), _i(icp), ctypes.byref(e))
+    return e.value
+
+
+def subs_getblocksize(ire, icp, iblk):
+    nx, ny, nz = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+    load().subs_getblocksize(_i(ire), _i(icp), _i(iblk), ctypes.byref(nx), ctypes.byref(ny), ctypes.byref(nz))
+    return nx.value, ny.value, nz.value
+
+
+def subs_getresults(ire, icp, iblk, cols=SUBS_COLUMNS):
+    """Results of block iblk as {column name: array of nx*ny*nz values (x fastest)}."""
+    nx, ny, nz = subs_getblocksize(ire, icp, iblk)
+    npt = nx * ny * nz
+    icol = np.array([SUBS_COLUMNS.index(c) + 1 for c in cols], dtype=np.int32)
+    vals = np.zeros((len(cols), max(npt, 1)))
+    load().subs_getresults(_i(ire), _i(icp), _i(iblk), _i(max(npt, 1)), _i(len(cols)), icol.ctypes.data_as(_IP),
+                           vals.ctypes.data_as(_DP))
+    return {c: vals[k, :npt].copy() for k, c in enumerate(cols)}
+
+
 def calculate_batch(ire_list, icp_list):
     _require_gpu()
     a, ap = _iarr(ire_list)

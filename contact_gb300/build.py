@@ -15,7 +15,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcontact_addon.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo", "--expt-relaxed-constexpr"]
-UNITS = ["engine.cu", "cntc_api.cpp", "peaks.cu"]
+UNITS = ["engine.cu", "cntc_api.cpp", "peaks.cu", "subsurf.cu"]
 
 
 def _nvcc():

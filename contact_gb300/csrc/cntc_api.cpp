@@ -50,6 +50,22 @@ constexpr int CNTC_err_norm = -27, CNTC_err_tang = -28, CNTC_err_icp = -31, CNTC
 constexpr int kMaxReid = 100, kMaxCpid = 9;
 constexpr int kCaddonVersion = 100 * 25 + 10 * 2 + 0;     // version 25.2.0 of the interface
 
+// one block of subsurface points (subs_addBlock, src/contact_addon.f90:3330-3515, and
+// expand_xb, m_subsurf.f90:440-620): element centres selected by index (types 1-3, 5-7) or
+// explicit x, y lists (type 9), at a regular (1-3) or listed (5-7, 9) set of depths z
+struct SubsBlock {
+    int isubs = 0;
+    int ixl = 1, ixinc = 1, ixh = 99999, iyl = 1, iyinc = 1, iyh = 99999;
+    std::vector<int> ixlist, iylist;      // types 3, 7: sorted unique positive indices
+    std::vector<double> x, y, z;          // type 9: x, y; types 5-7, 9: z (internal units)
+    int nz = 1;
+    double zl = 0.0, dz = 1.0;            // types 1-3
+    // filled by subs_calculate: effective point counts and the results, npoint rows of 21
+    // columns (x, y, z, ux, uy, uz, sighyd, sigvm, sigtr, sigma1..3, the stress tensor by columns)
+    int nx_eff = 0, ny_eff = 0;
+    std::vector<double> table;
+};
+
 struct Problem {
     int ire = 0, icp = 0, ncase = 0;
     // unit scaling (cntc_select_units, src/m_global_data.f90:463-526)
@@ -111,6 +127,8 @@ struct Problem {
     int prev_dev = -1;
     bool prev_valid = false;
     char prev_key[160] = {0};
+    // subsurface stress blocks (subs_addBlock) and their results (subs_calculate)
+    std::vector<SubsBlock> subs;
     std::mutex busy;
     // frees the device caches (cntc_finalize, cntc_finalizelast; not at process exit, when
     // the CUDA runtime may already be gone and the driver reclaims the memory)
@@ -1226,7 +1244,7 @@ void cntc_setflags(int *ire, int *icp, int *lenflg, int *params, int *values) {
             case CNTC_ic_return: p->ret = std::max(0, std::min(3, v)); break;
             case CNTC_if_ncase: p->ncase = std::max(0, v - 1); break;
             case CNTC_if_mixedprec: p->mixed = (v >= 0 && v <= 4) ? v : 1; break;
-            case CNTC_if_groupctas: p->group = std::max(-1, v); break;
+            case CNTC_if_groupctas: p->group = (v == -1) ? -1 : std::max(0, v); break;
             default: break;   // output, debugging and module-1 flags have no effect here
         }
     }
@@ -1769,20 +1787,180 @@ void cntc_getglobalforces(int *, int *, int *lenarr, double *values) {
     not_supported("cntc_getglobalforces");
     zero(lenarr, values);
 }
-void subs_addblock(int *, int *, int *, int *, int *, int *, int *, double *, double *, double *) {
-    not_supported("subs_addblock");
+// ------------------------------------------------------------------------------------------
+// subsurface stresses (module 3): subs_addBlock 3330-3515, subs_calculate 3904-3997,
+// subs_getBlocksize 6071-6109, subs_getResults 6113-6187 of src/contact_addon.f90
+// ------------------------------------------------------------------------------------------
+constexpr int kMaxSubsBlocks = 10, kMaxSubsPoints = 9999;      // MXBLCK, MXSUBS (m_globals.f90:32-33)
+
+void subs_addblock(int *ire, int *icp, int *iblk, int *isubs, int *npx, int *npy, int *npz, double *xparam,
+                   double *yparam, double *zparam) {
+    static const int npx_loc[10] = {0, 0, 3, -1, 0, 0, 3, -1, 0, -1}, npz_loc[10] = {0, 3, 3, 3, 0, -1, -1, -1, 0, -1};
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) return;
+    const int t = *isubs, b = *iblk;
+    if (b < 0 || b > std::min(kMaxSubsBlocks, (int)p->subs.size() + 1)) { log_msg("subs_addblock: invalid block"); return; }
+    if (t < 1 || t == 4 || t == 8 || t > 9) { log_msg("subs_addblock: block type does not exist"); return; }
+    if ((npx_loc[t] > 0 && *npx != npx_loc[t]) || (npx_loc[t] > 0 && *npy != npx_loc[t]) ||
+        (npz_loc[t] > 0 && *npz != npz_loc[t])) {
+        log_msg("subs_addblock: wrong number of parameters for the block type");
+        return;
+    }
+    // blocks iblk and higher are replaced; iblk <= 0 clears the list
+    p->subs.resize(std::max(0, b - 1));
+    if (b <= 0) return;
+    SubsBlock s;
+    s.isubs = t;
+    auto clamp_n = [](int n) { return std::max(1, std::min(n, kMaxSubsPoints)); };
+    auto unique_positive = [&](int n, const double *v) {
+        std::vector<int> r;
+        for (int i = 0; i < clamp_n(n); i++) { const int k = (int)std::lround(v[i]); if (k > 0) r.push_back(k); }
+        std::sort(r.begin(), r.end());
+        r.erase(std::unique(r.begin(), r.end()), r.end());
+        return r;
+    };
+    if (t == 2 || t == 6) {
+        s.ixl = std::max((int)std::lround(xparam[0]), 1);
+        s.ixinc = std::max((int)std::lround(xparam[1]), 1);
+        s.ixh = std::min((int)std::lround(xparam[2]), 999999);
+        s.iyl = std::max((int)std::lround(yparam[0]), 1);
+        s.iyinc = std::max((int)std::lround(yparam[1]), 1);
+        s.iyh = std::min((int)std::lround(yparam[2]), 999999);
+    } else if (t == 3 || t == 7) {
+        s.ixlist = unique_positive(*npx, xparam);
+        s.iylist = unique_positive(*npy, yparam);
+    }
+    if (t >= 1 && t <= 3) {
+        s.nz = clamp_n((int)std::lround(zparam[0]));
+        s.zl = zparam[1] * p->s_len;
+        s.dz = std::max(zparam[2] * p->s_len, 1e-9);
+    } else {
+        s.nz = clamp_n(*npz);
+        s.z.assign(zparam, zparam + s.nz);
+        for (double &v : s.z) v *= p->s_len;
+        std::sort(s.z.begin(), s.z.end());
+    }
+    if (t == 9) {
+        s.x.assign(xparam, xparam + clamp_n(*npx));
+        s.y.assign(yparam, yparam + clamp_n(*npy));
+        for (double &v : s.x) v *= p->s_len;
+        for (double &v : s.y) v *= p->s_len;
+        std::sort(s.x.begin(), s.x.end());
+        std::sort(s.y.begin(), s.y.end());
+    }
+    p->subs.push_back(s);
 }
-void subs_calculate(int *, int *, int *ierror) {
-    not_supported("subs_calculate");
-    *ierror = CNTC_err_other;
+
+// one block (expand_xb, m_subsurf.f90:440-620, then the field at its points): element centres
+// depth by depth, explicit points in one pass
+static int subs_block(const Problem &p, SubsBlock &s) {
+    const int mx = p.r_mx, my = p.r_my, n = mx * my;
+    std::vector<int> ixs, iys;
+    std::vector<double> xs, ys;
+    if (s.isubs == 9) {
+        xs = s.x; ys = s.y;
+    } else {
+        if (s.isubs == 3 || s.isubs == 7) {
+            for (int k : s.ixlist) if (k >= 1 && k <= mx) ixs.push_back(k);
+            for (int k : s.iylist) if (k >= 1 && k <= my) iys.push_back(k);
+        } else {
+            for (int k = std::max(s.ixl, 1); k <= std::min(s.ixh, mx); k += s.ixinc) ixs.push_back(k);
+            for (int k = std::max(s.iyl, 1); k <= std::min(s.iyh, my); k += s.iyinc) iys.push_back(k);
+        }
+        for (int k : ixs) xs.push_back(p.r_xc1 + (double)(float)(k - 1) * p.r_dx);
+        for (int k : iys) ys.push_back(p.r_yc1 + (double)(float)(k - 1) * p.r_dy);
+    }
+    std::vector<double> zs = s.z;
+    if (s.isubs >= 1 && s.isubs <= 3) {
+        zs.resize(s.nz);
+        for (int k = 0; k < s.nz; k++) zs[k] = s.zl + (double)(float)k * s.dz;
+    }
+    s.nx_eff = (int)xs.size(); s.ny_eff = (int)ys.size();
+    const int nxy = s.nx_eff * s.ny_eff, nz = (int)zs.size(), npt = nxy * nz;
+    s.table.assign((size_t)npt * 21, 0.0);
+    if (npt == 0) return 0;
+    cgb::SubsLoad L;
+    L.mx = mx; L.my = my; L.dx = p.r_dx; L.dy = p.r_dy; L.xc1 = p.r_xc1; L.yc1 = p.r_yc1;
+    L.pn = p.fields.data() + (size_t)W_PN * n;
+    L.px = p.fields.data() + (size_t)W_PX * n;
+    L.py = p.fields.data() + (size_t)W_PY * n;
+    L.gg[0] = p.gg[0]; L.gg[1] = p.gg[1]; L.poiss[0] = p.poiss[0]; L.poiss[1] = p.poiss[1];
+    std::vector<double> res((size_t)npt * cgb::kSubsCols);
+    int rc = 0;
+    if (s.isubs == 9) {
+        std::vector<double> xyz((size_t)npt * 3);
+        for (int iz = 0, q = 0; iz < nz; iz++)
+            for (int iy = 0; iy < s.ny_eff; iy++)
+                for (int ix = 0; ix < s.nx_eff; ix++, q++) {
+                    xyz[3 * q] = xs[ix]; xyz[3 * q + 1] = ys[iy]; xyz[3 * q + 2] = zs[iz];
+                }
+        rc = cgb::subs_points(L, npt, xyz.data(), res.data());
+    } else {
+        for (int iz = 0; iz < nz && rc == 0; iz++)
+            rc = cgb::subs_depth(L, zs[iz], s.nx_eff, ixs.data(), s.ny_eff, iys.data(),
+                                 res.data() + (size_t)iz * nxy * cgb::kSubsCols);
+    }
+    if (rc != 0) return rc;
+    for (int iz = 0, q = 0; iz < nz; iz++)
+        for (int iy = 0; iy < s.ny_eff; iy++)
+            for (int ix = 0; ix < s.nx_eff; ix++, q++) {
+                double *row = s.table.data() + (size_t)q * 21;
+                const double *o = res.data() + (size_t)q * cgb::kSubsCols;
+                row[0] = xs[ix]; row[1] = ys[iy]; row[2] = zs[iz];
+                for (int c = 0; c < 9; c++) row[3 + c] = o[c];
+                // the stress tensor by columns: sigxx, sigyx, sigzx, sigxy, ...
+                for (int j = 0; j < 3; j++)
+                    for (int i = 0; i < 3; i++) row[12 + i + 3 * j] = o[9 + 3 * i + j];
+            }
+    return 0;
 }
-void subs_getblocksize(int *, int *, int *, int *nx, int *ny, int *nz) {
-    not_supported("subs_getblocksize");
+
+void subs_calculate(int *ire, int *icp, int *ierror) {
+    *ierror = 0;
+    Problem *p = lookup(*ire, *icp, true);
+    if (!p) { *ierror = CNTC_err_icp; return; }
+    std::unique_lock<std::mutex> lk(p->busy, std::try_to_lock);
+    if (!lk.owns_lock()) { *ierror = CNTC_err_other; return; }
+    // the tractions of the last solve on its grid (the reference takes the problem's current
+    // output without a check; here a problem without a solution is refused)
+    if (!p->have || (int)p->fields.size() < kIoCols * p->r_mx * p->r_my) {
+        log_msg("subs_calculate: no solution to evaluate");
+        *ierror = CNTC_err_other;
+        return;
+    }
+    for (SubsBlock &s : p->subs) {
+        const int rc = subs_block(*p, s);
+        if (rc != 0) {
+            if (g_debug >= 1) std::fprintf(stderr, "contact_gb300: subsurface error %d\n", rc);
+            *ierror = CNTC_err_other;
+            return;
+        }
+    }
+}
+
+void subs_getblocksize(int *ire, int *icp, int *iblk, int *nx, int *ny, int *nz) {
     *nx = 0; *ny = 0; *nz = 0;
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p || *iblk <= 0 || *iblk > (int)p->subs.size()) return;
+    const SubsBlock &s = p->subs[*iblk - 1];
+    if (s.table.empty() && s.nx_eff * s.ny_eff == 0) return;
+    *nx = s.nx_eff; *ny = s.ny_eff;
+    *nz = (s.nx_eff * s.ny_eff > 0) ? (int)(s.table.size() / 21) / (s.nx_eff * s.ny_eff) : 0;
 }
-void subs_getresults(int *, int *, int *, int *lenarr, int *ncol, int *, double *values) {
-    not_supported("subs_getresults");
-    for (int i = 0; i < *lenarr * std::max(0, *ncol); i++) values[i] = 0.0;
+
+void subs_getresults(int *ire, int *icp, int *iblk, int *lenarr, int *ncol, int *icol, double *values) {
+    Problem *p = lookup(*ire, *icp, false);
+    if (!p || *iblk <= 0 || *iblk > (int)p->subs.size()) return;
+    const SubsBlock &s = p->subs[*iblk - 1];
+    const int npnt = (int)(s.table.size() / 21);
+    for (int jc = 0; jc < *ncol; jc++) {
+        double *out = values + (size_t)jc * std::max(0, *lenarr);
+        const int c = icol[jc];
+        if (c <= 0 || c > 21) { for (int i = 0; i < *lenarr; i++) out[i] = -999.0; continue; }
+        // lengths and displacements in the caller's length unit, stresses in its stress unit
+        const double f = c <= 6 ? 1.0 / p->s_len : p->s_area / p->s_forc;
+        for (int i = 0; i < std::min(npnt, *lenarr); i++) out[i] = s.table[(size_t)i * 21 + (c - 1)] * f;
+    }
 }
 
 void cntc_finalize(int *ire) {

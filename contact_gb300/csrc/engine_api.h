@@ -79,4 +79,19 @@ int opt_fft_size(int n);
 // count of this library's kernels launched since load (for benchmark accounting)
 long long kernel_launch_count();
 
+// subsurface elastic field of the surface tractions (subsurf.cu, m_subsurf.f90).  Host arrays;
+// per point kSubsCols values: ux, uy, uz, sighyd, sigvm, sigtr, sigma1..3, sig[3][3] row by row.
+// Points with z >= 0 lie in body 1, z < 0 in body 2.
+struct SubsLoad {
+    int mx, my;
+    double dx, dy, xc1, yc1;          // grid: spacing and centre of the first element
+    const double *pn, *px, *py;       // tractions of body 1, mx*my each (x fastest)
+    double gg[2], poiss[2];           // the two bodies
+};
+constexpr int kSubsCols = 18;
+// at npts arbitrary points xyz[3 q ..]
+int subs_points(const SubsLoad &L, int npts, const double *xyz, double *out);
+// at the element centres (ixs[a], iys[b]) (1-based, x fastest) at depth zw
+int subs_depth(const SubsLoad &L, double zw, int nx, const int *ixs, int ny, const int *iys, double *out);
+
 } // namespace cgb

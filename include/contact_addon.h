@@ -146,11 +146,12 @@ void cntc_setmetadata(int *ire, int *icp, int *lenmta, int *params, double *valu
  * returns 0, 0 as the reference does without a temperature solution */
 void cntc_getmaximumtemperature(int *ire, int *icp, double *t1max, double *t2max);
 
-/* Entry points of the wheel-rail module (module 1), the input-file reader and subsurface
- * stresses.  They lie outside this library's solve path; they are exported so that hosts
- * binding the reference's full interface load this library unchanged.  Each logs that it is
- * not supported and returns: setters without effect, getters with zero outputs, and
- * ierror = CNTC_err_other where the call has one.  Fortran implementations:
+/* Entry points of the wheel-rail module (module 1) and the input-file reader.  They lie
+ * outside this library's solve path; they are exported so that hosts binding the reference's
+ * full interface load this library unchanged.  Each logs that it is not supported and returns:
+ * setters without effect, getters with zero outputs, and ierror = CNTC_err_other where the
+ * call has one.  The subsurface entry points (subs_*) below them are implemented for module 3
+ * (see their own comment).  Fortran implementations:
  * cntc_readInpFile 729-776, cntc_setVerticalForce 2261-2290, cntc_setProfileInputFname
  * 2654-2749, cntc_setProfileInputValues 2753-2829, cntc_setTrackDimensions 2833-2985,
  * cntc_setWheelsetDimensions 2989-3063, cntc_setWheelsetPosition 3067-3132,
@@ -180,6 +181,14 @@ void cntc_getwheelsetvelocity(int *ire, int *lenarr, double *values);
 void cntc_getnumcontactpatches(int *ire, int *npatch);
 void cntc_getcontactlocation(int *ire, int *icp, int *lenarr, double *values);
 void cntc_getglobalforces(int *ire, int *icp, int *lenarr, double *values);
+/* Subsurface stresses of module 3 (src/contact_addon.f90 subs_addBlock 3330-3515,
+ * subs_calculate 3904-3997, subs_getBlocksize 6071-6109, subs_getResults 6113-6187;
+ * m_subsurf.f90): blocks of points (types 1-3, 5-7: element centres selected by index ranges or
+ * lists at regular or listed depths; 9: x, y, z lists), evaluated on the GPU for the tractions
+ * of the problem's last solve (z >= 0 in body 1, z < 0 in body 2).  Results per point: x, y, z,
+ * displacements, hydrostatic / von Mises / Tresca stress, principal stresses and the stress
+ * tensor by columns (21 columns, points x fastest, then y, then z).  subs_calculate on a
+ * problem without a solution returns CNTC_err_other. */
 void subs_addblock(int *ire, int *icp, int *iblk, int *isubs, int *nx, int *ny, int *nz, double *xparam,
                    double *yparam, double *zparam);
 void subs_calculate(int *ire, int *icp, int *ierror);

@@ -72,6 +72,8 @@ def test_flags_roundtrip(lib):
     assert getflags(ire, icp, flags) == [1, 2, 3, 1, 12]
     cg.setflags(ire, icp, [cg.CNTC_if_groupctas], [-4])          # negative: automatic
     assert getflags(ire, icp, [cg.CNTC_if_groupctas]) == [0]
+    cg.setflags(ire, icp, [cg.CNTC_if_groupctas], [-1])          # -1: tuned per size class
+    assert getflags(ire, icp, [cg.CNTC_if_groupctas]) == [-1]
     cg.finalize(ire)
 
 
@@ -161,8 +163,10 @@ def test_getparameters_material_friction_kinematics(lib):
 
 
 def test_entry_points_outside_the_solve_path(lib):
-    """Wheel-rail, input-file and subsurface entry points exist and report 'not supported':
-    outputs zeroed, ierror CNTC_err_other; metadata is accepted; temperatures are zero."""
+    """Wheel-rail and input-file entry points exist and report 'not supported': outputs zeroed,
+    ierror CNTC_err_other; metadata is accepted; temperatures are zero.  Subsurface stresses of
+    a problem without a solution are refused (CNTC_err_other); an unknown block has no points
+    and leaves the output array as it was (src/contact_addon.f90:6147-6150)."""
     ire, icp = 907, 1
     cg.setnormalforce(ire, icp, 1e4)
     ierr = ctypes.c_int(0)
@@ -183,7 +187,7 @@ def test_entry_points_outside_the_solve_path(lib):
     w = np.full((2, 3), 4.0)
     icol = np.zeros(2, dtype=np.int32)
     lib.subs_getresults(_i(ire), _i(icp), _i(1), _i(3), _i(2), icol.ctypes.data_as(cg._IP), w.ctypes.data_as(cg._DP))
-    assert np.all(w == 0.0)
+    assert np.all(w == 4.0)
     params = np.array([1], dtype=np.int32)
     vals = np.array([0.5])
     lib.cntc_setmetadata(_i(ire), _i(icp), _i(1), params.ctypes.data_as(cg._IP), vals.ctypes.data_as(cg._DP))

@@ -1,0 +1,113 @@
+"""Subsurface stresses on the GPU (subs_addBlock / subs_calculate / subs_getResults, module 3)
+against the reference's printed field of its own example (examples/subsurf.ref_subs, fixture
+tests/golden/subsurf.json) and against the oracle's two forms on the same tractions: the direct
+sum at arbitrary points, and the influence-coefficient path at element centres."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import cases as C
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+# oracle column of each library column (oracle: ux uy uz sighyd sigvm sigtr sigma1..3 sig row by row)
+ORC = {"ux": 0, "uy": 1, "uz": 2, "sighyd": 3, "sigvm": 4, "sigtr": 5, "sigma1": 6, "sigma2": 7, "sigma3": 8,
+       "sigxx": 9, "sigxy": 10, "sigxz": 11, "sigyx": 12, "sigyy": 13, "sigyz": 14, "sigzx": 15, "sigzy": 16,
+       "sigzz": 17}
+FIELD = [c for c in ORC]
+
+
+def _half_unit(tok):
+    t = tok.upper()
+    if "E" in t:
+        mant, ex = t.split("E")
+        return 0.5 * 10.0 ** (int(ex) - (len(mant.split(".")[1]) if "." in mant else 0))
+    return 0.5 * 10.0 ** (-(len(t.split(".")[1]) if "." in t else 0))
+
+
+def test_example_against_printed_table(cntc):
+    """examples/subsurf.inp case 2 solved on the GPU (pressure and Fx = 0.999 mu Fn on one
+    element, ConvexGS inside the Newton-Raphson), then its field at the printed points: block 1
+    (a column below the centre) and the 7 x 7 printed subgrid of block 2, within half a unit of
+    the last printed digit (components that vanish at the free surface: 1e-12 of the column's
+    largest value)."""
+    with open(os.path.join(GOLD, "subsurf.json")) as f:
+        g = json.load(f)
+    ire, icp = 140, 1
+    cntc.setup_case(ire, icp, C.subsurf_case(2))
+    assert cntc.calculate(ire, icp) >= 0
+    b1 = np.array([[float(v) for v in r[:3]] for r in g["block1"]])
+    cntc.subs_addblock(ire, icp, 1, 9, [b1[0, 0]], [b1[0, 1]], b1[:, 2])
+    cntc.subs_addblock(ire, icp, 2, 9, g["block2_x"], g["block2_y"], g["block2_z"])
+    assert cntc.subs_calculate(ire, icp) == 0
+    assert cntc.subs_getblocksize(ire, icp, 1) == (1, 1, len(b1))
+    nx, ny, nz = len(g["block2_x"]), len(g["block2_y"]), len(g["block2_z"])
+    assert cntc.subs_getblocksize(ire, icp, 2) == (nx, ny, nz)
+    cols = [c.lower() for c in g["columns"][3:]]
+    r1 = cntc.subs_getresults(ire, icp, 1)
+    r2 = cntc.subs_getresults(ire, icp, 2)
+    pick = g["block2_pick"]
+    sel = [ix + nx * (iy + ny * iz) for iz in range(nz) for iy in pick for ix in pick]
+    for rows, res, idx in ((g["block1"], r1, range(len(g["block1"]))), (g["block2_subgrid"], r2, sel)):
+        gv = np.array([[float(v) for v in r[3:]] for r in rows])
+        scale = np.abs(gv).max(axis=0)
+        for q, (r, k) in enumerate(zip(rows, idx)):
+            for c, name in enumerate(cols):
+                tol = max(_half_unit(r[3 + c]) * (1 + 1e-9), 1e-12 * scale[c])
+                assert abs(res[name][k] - gv[q, c]) <= tol, (r[:3], name, res[name][k], r[3 + c])
+            assert (res["x"][k], res["y"][k], res["z"][k]) == pytest.approx([float(v) for v in r[:3]])
+
+
+def test_element_centres_and_points_against_oracle(cntc, oracle):
+    """Hertzian steady rolling on 51 x 51 (GDsteady, FP64), then its field on the GPU: every
+    element centre at four listed depths from the surface (block type 5), a subgrid of centres at listed
+    depths (type 6), and explicit points in both bodies (type 9, z < 0 below the surface of body
+    2).  Centres: the oracle's influence-coefficient path on the same tractions, within 1e-10 of
+    each column's largest value (the GPU sums the tabulated coefficients directly, the oracle by
+    FFT); points: the oracle's direct sum within 1e-11."""
+    ire, icp = 141, 1
+    case = C.config0(gausei=5, eps=1e-10)
+    cntc.setup_case(ire, icp, case)
+    assert cntc.calculate(ire, icp) >= 0
+    res = cntc.results(ire, icp)
+    mx, my = res["mx"], res["my"]
+    zc = [0.0, 0.4, 1.0, 2.5]
+    cntc.subs_addblock(ire, icp, 1, 5, [], [], zc)
+    cntc.subs_addblock(ire, icp, 2, 6, [3, 4, 49], [10, 7, 40], [0.3, 1.2])
+    px_, py_, pz_ = [-3.0, 0.1, 2.2], [-1.5, 0.0, 2.0], [-0.8, 0.05, 0.7]
+    cntc.subs_addblock(ire, icp, 3, 9, px_, py_, pz_)
+    assert cntc.subs_calculate(ire, icp) == 0
+    r1 = cntc.subs_getresults(ire, icp, 1)
+    assert cntc.subs_getblocksize(ire, icp, 1) == (mx, my, len(zc))
+    xc1, yc1 = r1["x"][0], r1["y"][0]
+    grid = (mx, my, res["dx"], res["dy"], xc1, yc1)
+    gg, nu = case["gg"], case["poiss"]
+    f = oracle.subsurf_depths(grid, res["pn"], res["px"], res["py"], gg, nu, np.array(zc))   # (nz, n, 18)
+    for name in FIELD:
+        got = r1[name].reshape(len(zc), mx * my)
+        ref = f[:, :, ORC[name]]
+        scale = np.abs(ref).max() + 1e-300
+        assert np.abs(got - ref).max() <= 1e-10 * scale, (name, np.abs(got - ref).max() / scale)
+    # type 6: ix 3, 7, ..., 47; iy 10, 17, ..., 38 at z 0.3, 1.2
+    r2 = cntc.subs_getresults(ire, icp, 2)
+    ixs, iys = list(range(3, 50, 4)), list(range(10, 41, 7))
+    assert cntc.subs_getblocksize(ire, icp, 2) == (len(ixs), len(iys), 2)
+    f2 = oracle.subsurf_depths(grid, res["pn"], res["px"], res["py"], gg, nu, np.array([0.3, 1.2]))
+    sel = [(ix - 1) + (iy - 1) * mx for iy in iys for ix in ixs]
+    for name in FIELD:
+        ref = f2[:, sel, ORC[name]].ravel()
+        scale = np.abs(ref).max() + 1e-300
+        assert np.abs(r2[name] - ref).max() <= 1e-10 * scale, name
+    # type 9: explicit points, x fastest, then y, then z (sorted)
+    r3 = cntc.subs_getresults(ire, icp, 3)
+    X, Y, Z = np.meshgrid(sorted(px_), sorted(py_), sorted(pz_), indexing="ij")
+    pts = np.stack([X.transpose(2, 1, 0).ravel(), Y.transpose(2, 1, 0).ravel(), Z.transpose(2, 1, 0).ravel()], 1)
+    assert np.allclose(np.stack([r3["x"], r3["y"], r3["z"]], 1), pts)
+    d = oracle.subsurf_points(grid, res["pn"], res["px"], res["py"], gg, nu, pts)
+    for name in FIELD:
+        scale = np.abs(d[:, ORC[name]]).max() + 1e-300
+        assert np.abs(r3[name] - d[:, ORC[name]]).max() <= 1e-11 * scale, name
