@@ -261,9 +261,13 @@ int prepare(Problem &p, Prep &out, bool latency = false) {
     if (!is_roll) { chi = 0.0; dq = 1.0; veloc = 1.0; }
     if (is_roll && std::fabs(chi) > 0.01) { log_msg("rolling direction chi != 0 is not supported"); return CNTC_err_other; }
     p.dt = dq / std::max(1e-10, veloc);
-    // a single column in rolling direction: steady rolling would select ConvexGS (-99 here as
-    // well); single rows (my = 1) are solved
-    if (mx < 2 || my < 1) { log_msg("grids with mx < 2 are not supported"); return CNTC_err_other; }
+    // a single column in rolling direction is solved for the normal problem alone (FFT length 2
+    // in x, as for single rows in y); with a tangential problem the reference selects ConvexGS
+    // there, which is not on the device
+    if ((mx < 2 && p.tang != 0) || mx < 1 || my < 1) {
+        log_msg("grids with mx < 2 are supported for the normal problem only");
+        return CNTC_err_other;
+    }
     const int fx = cgb::opt_fft_size(mx), fy = cgb::opt_fft_size(my);
     // one CTA per patch while its FFT lines fit the per-warp buffers, a cooperative group of
     // CTAs for larger grids (or when CNTC_if_groupctas asks for one)

@@ -222,3 +222,25 @@ def test_unsupported_options_refused_before_any_device_work(lib):
     cg.setflags(ire, 4, [cg.CNTC_ic_force], [1])
     assert _calc(lib, ire, 4) == cg.CNTC_err_other
     cg.finalize(ire)
+
+
+def test_single_column_refused_for_tangential_problems(lib, capfd):
+    """A grid of one column in rolling direction (mx = 1) is refused by the set-up for a
+    tangential problem (the reference selects ConvexGS there) but passes it for the normal
+    problem alone, which then reaches the engine (no device here)."""
+    ire = 909
+    roll = C.subsurf_case(2)
+    roll.pop("force3"), roll.pop("fxrel")
+    roll["cksi"] = 0.0
+    cg.setglobalflags([cg.CNTC_if_idebug], [1])
+    try:
+        cg.setup_case(ire, 1, roll)
+        capfd.readouterr()
+        assert _calc(lib, ire, 1) == cg.CNTC_err_other
+        assert "mx < 2" in capfd.readouterr().err
+        cg.setup_case(ire, 2, C.subsurf_case(1))
+        _calc(lib, ire, 2)
+        assert "mx < 2" not in capfd.readouterr().err
+    finally:
+        cg.setglobalflags([cg.CNTC_if_idebug], [0])
+        cg.finalize(ire)

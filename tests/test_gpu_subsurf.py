@@ -1,9 +1,8 @@
 """Subsurface stresses on the GPU (subs_addBlock / subs_calculate / subs_getResults, module 3)
-against the reference's printed field of its own example (examples/subsurf.ref_subs, fixture
+against the reference's printed maxima of its own example (examples/subsurf.ref_out, fixture
 tests/golden/subsurf.json) and against the oracle's two forms on the same tractions: the direct
 sum at arbitrary points, and the influence-coefficient path at element centres."""
 import json
-import math
 import os
 
 import numpy as np
@@ -19,27 +18,34 @@ ORC = {"ux": 0, "uy": 1, "uz": 2, "sighyd": 3, "sigvm": 4, "sigtr": 5, "sigma1":
        "sigxx": 9, "sigxy": 10, "sigxz": 11, "sigyx": 12, "sigyy": 13, "sigyz": 14, "sigzx": 15, "sigzy": 16,
        "sigzz": 17}
 FIELD = [c for c in ORC]
+# The principal stresses come from the trigonometric (Cardano) solution of the characteristic
+# cubic, as in the reference (m_subsurf.f90:2440-2490, Cardano's algorithm): near a
+# repeated eigenvalue (sigma1 = sigma2 on the axis below a symmetric load) acos(r) with r
+# close to +-1 turns a rounding difference dr into an angle of order sqrt(dr), so two
+# evaluations of the same formula agree to about 1e-8 of the stresses there, not to 1e-11.
+PRINCIPAL_TOL = {"sigma1": 5e-8, "sigma2": 5e-8, "sigma3": 5e-8, "sigtr": 5e-8}
 
 
-def _half_unit(tok):
-    t = tok.upper()
-    if "E" in t:
-        mant, ex = t.split("E")
-        return 0.5 * 10.0 ** (int(ex) - (len(mant.split(".")[1]) if "." in mant else 0))
-    return 0.5 * 10.0 ** (-(len(t.split(".")[1]) if "." in t else 0))
-
-
-def test_example_against_printed_table(cntc):
-    """examples/subsurf.inp case 2 solved on the GPU (pressure and Fx = 0.999 mu Fn on one
-    element, ConvexGS inside the Newton-Raphson), then its field at the printed points: block 1
-    (a column below the centre) and the 7 x 7 printed subgrid of block 2, within half a unit of
-    the last printed digit (components that vanish at the free surface: 1e-12 of the column's
-    largest value)."""
+def test_example_against_printed_table(cntc, oracle):
+    """examples/subsurf.inp case 1 solved on the GPU (the normal problem on its single element:
+    pressure 1 on 1 x 1 mm), then its field on the GPU at the example's two blocks: block 1 (a
+    column below the centre) and block 2 (21 x 21 x 15 points).  The printed maxima of case 1
+    (largest hydrostatic stress, von Mises, Tresca, principal stresses, sigma_xx, yy, zz) to
+    the printed 3 decimals and at the printed position; every point within 1e-11 of the
+    largest displacement (stress) of the oracle's direct sum of the same pressure (principal
+    stresses near a repeated eigenvalue: 5e-8).  (Case 2 adds a
+    traction found by ConvexGS on a single column, which is not on the device; its printed
+    table is held against the oracle's own solve on the CPU.)"""
+    import pyoracle as po
     with open(os.path.join(GOLD, "subsurf.json")) as f:
         g = json.load(f)
     ire, icp = 140, 1
-    cntc.setup_case(ire, icp, C.subsurf_case(2))
+    cntc.setup_case(ire, icp, C.subsurf_case(1))
     assert cntc.calculate(ire, icp) >= 0
+    res = cntc.results(ire, icp)
+    assert (res["mx"], res["my"]) == (1, 1)
+    solve = [s for s in g["solves"] if s["case"] == 1][0]
+    assert abs(res["pn"].max() - solve["pmax"]) <= 0.5e-4
     b1 = np.array([[float(v) for v in r[:3]] for r in g["block1"]])
     cntc.subs_addblock(ire, icp, 1, 9, [b1[0, 0]], [b1[0, 1]], b1[:, 2])
     cntc.subs_addblock(ire, icp, 2, 9, g["block2_x"], g["block2_y"], g["block2_z"])
@@ -47,19 +53,29 @@ def test_example_against_printed_table(cntc):
     assert cntc.subs_getblocksize(ire, icp, 1) == (1, 1, len(b1))
     nx, ny, nz = len(g["block2_x"]), len(g["block2_y"]), len(g["block2_z"])
     assert cntc.subs_getblocksize(ire, icp, 2) == (nx, ny, nz)
-    cols = [c.lower() for c in g["columns"][3:]]
-    r1 = cntc.subs_getresults(ire, icp, 1)
-    r2 = cntc.subs_getresults(ire, icp, 2)
-    pick = g["block2_pick"]
-    sel = [ix + nx * (iy + ny * iz) for iz in range(nz) for iy in pick for ix in pick]
-    for rows, res, idx in ((g["block1"], r1, range(len(g["block1"]))), (g["block2_subgrid"], r2, sel)):
-        gv = np.array([[float(v) for v in r[3:]] for r in rows])
-        scale = np.abs(gv).max(axis=0)
-        for q, (r, k) in enumerate(zip(rows, idx)):
-            for c, name in enumerate(cols):
-                tol = max(_half_unit(r[3 + c]) * (1 + 1e-9), 1e-12 * scale[c])
-                assert abs(res[name][k] - gv[q, c]) <= tol, (r[:3], name, res[name][k], r[3 + c])
-            assert (res["x"][k], res["y"][k], res["z"][k]) == pytest.approx([float(v) for v in r[:3]])
+    out = {1: cntc.subs_getresults(ire, icp, 1), 2: cntc.subs_getresults(ire, icp, 2)}
+    pot = C.subsurf_case(1)["potprm"]                       # first corner, element size
+    grid = (res["mx"], res["my"], res["dx"], res["dy"], pot[2] + 0.5 * pot[4], pot[3] + 0.5 * pot[5])
+    for blk, r in out.items():
+        pts = np.stack([r["x"], r["y"], r["z"]], 1)
+        d = po.subsurf_points(grid, res["pn"], res["px"], res["py"], g["gg"], g["poiss"], pts)
+        for name in FIELD:
+            # against the largest value of the column's group (displacements, stresses): a
+            # column that nearly vanishes (ux on the axis) carries the group's rounding
+            grp = FIELD[:3] if name in FIELD[:3] else FIELD[3:]
+            scale = max(np.abs(d[:, ORC[c]]).max() for c in grp)
+            assert np.abs(r[name] - d[:, ORC[name]]).max() <= PRINCIPAL_TOL.get(name, 1e-11) * scale, (blk, name)
+    # block 2 points: x fastest, then y, then z
+    assert np.allclose(out[2]["x"][:nx], sorted(g["block2_x"]))
+    summ = [s for s in g["summaries"] if s["case"] == 1]
+    assert len(summ) == 16
+    for s in summ:
+        r = out[s["block"]]
+        col = r[s["quantity"].lower()]
+        i = int(np.argmax(np.abs(col)) if s["kind"] == "ABSMAX" else np.argmax(col) if s["kind"] == "MAX"
+                else np.argmin(col))
+        assert abs(col[i] - s["value"]) <= 0.5e-3 * (1 + 1e-9), s
+        assert np.allclose(np.round([r["x"][i], r["y"][i], r["z"][i]], 3), s["at"]), s
 
 
 def test_element_centres_and_points_against_oracle(cntc, oracle):
