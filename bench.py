@@ -72,6 +72,10 @@ def parse():
     ap.add_argument("--perfc", action="store_true",
                     help="the reference's own performance inputs (perfc_test: normal problems 71x81 to 575x647, "
                          "shift problems), FP64, each through cntc_calculate, against the published 2016 timings")
+    ap.add_argument("--accuracy", action="store_true",
+                    help="errors of the mixed and FP64 forms at the workload's eps and at --tight-eps, each against "
+                         "the others, on the first --plain-sample patches")
+    ap.add_argument("--tight-eps", type=float, default=1e-11)
     ap.add_argument("--large-side", type=int, default=1024)
     ap.add_argument("--large-maxgs", type=int, default=3000)
     ap.add_argument("--large-eps", type=float, default=1e-6,
@@ -288,6 +292,42 @@ def small_patch_latency(cg, reps=5):
 # ------------------------------------------------------------------------------------------
 # GB300 arm
 # ------------------------------------------------------------------------------------------
+def _fields(cg, ire, icp):
+    fn, fx, fy, _ = cg.getcontactforces(ire, icp)
+    pn, px, py = cg.gettractions(ire, icp)
+    return dict(fn=fn, fx=fx, fy=fy, pmax=cg.getmaximumpressure(ire, icp), pn=pn, px=px, py=py,
+                igs=np.asarray(cg.getelementdivision(ire, icp)).ravel())
+
+
+def form_errors(cg, ire, icp_a, icp_b, fstat):
+    """Per patch, form a (icp_a) against form b (icp_b) of the same problems: tangential force
+    |dF_t| / max(|F_t|, 1e-3 mu Fn), normal force |dFn| / Fn, maximum pressure |dpmax| / pmax,
+    traction field max |dp| / pmax over the three components, and the elements whose class
+    differs."""
+    out = {k: [] for k in ("ft", "fn", "pmax", "tractions", "eldiv")}
+    for i, mu in zip(ire, fstat):
+        a, b = _fields(cg, i, icp_a), _fields(cg, i, icp_b)
+        ft = math.hypot(b["fx"], b["fy"])
+        out["ft"].append(math.hypot(a["fx"] - b["fx"], a["fy"] - b["fy"]) / max(ft, 1e-3 * mu * abs(b["fn"])))
+        out["fn"].append(abs(a["fn"] - b["fn"]) / max(abs(b["fn"]), 1e-300))
+        out["pmax"].append(abs(a["pmax"] - b["pmax"]) / max(b["pmax"], 1e-300))
+        dp = max(float(np.abs(a[k] - b[k]).max()) for k in ("pn", "px", "py"))
+        out["tractions"].append(dp / max(b["pmax"], 1e-300))
+        out["eldiv"].append(int((a["igs"] != b["igs"]).sum()))
+    return {k: np.array(v) for k, v in out.items()}
+
+
+def summarize_errors(errs, bound=1e-8):
+    out = {}
+    for k, v in errs.items():
+        if k == "eldiv":
+            out[k] = {"patches_differing": int((v > 0).sum()), "max_elements": int(v.max())}
+        else:
+            out[k] = {"median": float(np.median(v)), "p99": float(np.percentile(v, 99)), "max": float(v.max()),
+                      "above_%g" % bound: int((v > bound).sum())}
+    return out
+
+
 def setup_problems(cg, cases, ire0=1):
     ire = list(range(ire0, ire0 + len(cases)))
     for i, c in zip(ire, cases):
@@ -399,13 +439,9 @@ def run_gb300(args, dist):
         mrb.collect()
         mrb.release()
         mixed_sample_ms = float(mt[0, 0])
-        # force error of the mixed form against the FP64 form on the same patches
-        ferr = []
-        for i, c in zip(pire, pc):
-            a, b = cg.results(i, 1), cg.results(i, 2)
-            ft = math.hypot(b["fx"], b["fy"])
-            ferr.append(math.hypot(a["fx"] - b["fx"], a["fy"] - b["fy"]) / max(ft, 1e-3 * c["fstat"] * abs(b["fn"])))
-        ferr = np.array(ferr)
+        # errors of the mixed form against the FP64 form on the same patches
+        errs = form_errors(cg, pire, 1, 2, [c["fstat"] for c in pc])
+        ferr = errs["ft"]
         # the per-call FP64 drop-in (one cntc_calculate per patch, one CTA each): the sum of the
         # patches' own solve times, measured in SM cycles by each patch's CTA in this pass (an
         # upper bound: there two CTAs share an SM)
@@ -416,6 +452,7 @@ def run_gb300(args, dist):
                  "mixed_solves_per_s_same_sample": len(pc) / (mixed_sample_ms / 1e3),
                  "mixed_force_rel_err": {"max": float(ferr.max()), "p99": float(np.percentile(ferr, 99)),
                                          "median": float(np.median(ferr)), "above_1e-8": int((ferr > 1e-8).sum())},
+                 "mixed_err_vs_fp64": summarize_errors(errs),
                  "note": "first %d patches of the workload, eps 1e-8, FP64 throughout, batched (solves_per_s) and "
                          "as per-call drop-in (per_call_solves_per_s: patches / sum of each patch's single-CTA "
                          "solve time in that pass); force error = |dF_t| / max(|F_t|, 1e-3 mu Fn) of the mixed "
@@ -757,6 +794,58 @@ def run_perfc(args, dist):
             "total_s": tot, "total_s_tuned": tot_tuned, "reference_total_s": tot_ref, "cases": rows}
 
 
+# ------------------------------------------------------------------------------------------
+# accuracy of the forms on a sample of the batched workload: the mixed and the FP64 form at the
+# workload's tolerance and at a tight one, each against the others
+# ------------------------------------------------------------------------------------------
+def run_accuracy(args, dist):
+    import torch
+    import contact_gb300 as cg
+    torch.cuda.set_device(dist.local)
+    cg.load()
+    n = args.plain_sample
+    cases = workload(n, args.seed)
+    ire = list(range(1, n + 1))
+    eps = cases[0]["eps"]
+    forms = {1: ("mixed", eps, {}), 2: ("fp64", eps, {"mixed": 0}),
+             3: ("fp64", args.tight_eps, {"mixed": 0, "eps": args.tight_eps}),
+             4: ("mixed", args.tight_eps, {"eps": args.tight_eps})}
+    rates, iters = {}, {}
+    for icp, (name, e, over) in forms.items():
+        for i, c in zip(ire, cases):
+            cg.setup_case(i, icp, dict(c, **over))
+        rb = cg.ResidentBatch(ire, [icp] * n)
+        t = rb.solve(1)
+        rb.collect()
+        rb.release()
+        key = "%s_eps%g" % (name, e)
+        rates[key] = n / (float(t[0, 0]) / 1e3)
+        iters[key] = float(np.mean([cg.getiterationcounts(i, icp)["itgs"] for i in ire]))
+    fstat = [c["fstat"] for c in cases]
+    pairs = {"mixed_vs_fp64_same_eps": (1, 2), "fp64_eps_vs_fp64_tight": (2, 3),
+             "mixed_eps_vs_fp64_tight": (1, 3), "mixed_tight_vs_fp64_tight": (4, 3)}
+    errs = {k: form_errors(cg, ire, a, b, fstat) for k, (a, b) in pairs.items()}
+    table = {k: summarize_errors(v) for k, v in errs.items()}
+    # the patches where mixed and FP64 differ most at the workload's eps, with the distance of
+    # each form from the tightly converged FP64 answer
+    worst = []
+    for k in np.argsort(-errs["mixed_vs_fp64_same_eps"]["ft"])[:8]:
+        worst.append({"patch": int(k), "grid": cases[k]["potprm"][:2],
+                      "ft_mixed_vs_fp64": float(errs["mixed_vs_fp64_same_eps"]["ft"][k]),
+                      "ft_fp64_vs_tight": float(errs["fp64_eps_vs_fp64_tight"]["ft"][k]),
+                      "ft_mixed_vs_tight": float(errs["mixed_eps_vs_fp64_tight"]["ft"][k]),
+                      "ft_mixed_tight_vs_tight": float(errs["mixed_tight_vs_fp64_tight"]["ft"][k])})
+    if dist.rank != 0:
+        return None
+    return {"metric": METRIC, "value": rates["mixed_eps%g" % eps], "unit": UNIT, "n_gpus": dist.world,
+            "steps": 1, "warmup": 0, "ms_per_step": n / rates["mixed_eps%g" % eps] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic", "mode": "accuracy",
+            "config": {"workload": "first %d patches of the batched workload (seed %d), mixed tier %d and FP64, "
+                                   "at eps %g and at eps %g" % (n, args.seed, MIXED_TIER, eps, args.tight_eps)},
+            "solves_per_s": rates, "mean_gd_iterations": iters, "errors": table, "worst_patches": worst}
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -767,6 +856,8 @@ def main():
             out = run_large(args, dist)
         elif args.perfc and args.impl != "reference":
             out = run_perfc(args, dist)
+        elif args.accuracy and args.impl != "reference":
+            out = run_accuracy(args, dist)
         else:
             out = run_reference(args, dist) if args.impl == "reference" else run_gb300(args, dist)
         if out is not None:
