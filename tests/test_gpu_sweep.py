@@ -1,9 +1,9 @@
 """The non-Hertzian grid sweep (seeded sinusoidal roughness on a quadratic gap, Fn 100 kN,
 creepages (0.002, 0.001, 0.2 rad/m), mu 0.3) at its configured grid sizes, against the oracle.
 
-128 x 128 is solved by the oracle inside the test (a few seconds); 256 x 256 (a patch group on
-the GPU) against the committed oracle fixture tests/golden/config1_256.npz, made by
-tests/golden/make_config1.py.  The bar is the FP64 parity bar of the other tests: identical
+128 x 128 is solved by the oracle inside the test (a few seconds); 256 x 256 and 512 x 512
+(patch groups on the GPU) against the committed oracle fixtures tests/golden/config1_256.npz
+and config1_512.npz, made by tests/golden/make_config1.py.  The bar is the FP64 parity bar of the other tests: identical
 element division and iteration counts, forces within 1e-10, tractions within 1e-8 of pmax.
 The case with the large patch's parameters (seed 4, Fn 150 kN, creepages (0.003, 0, 0.3
 rad/m), mu 0.25) is held to the same bar at 128 x 128.
@@ -41,9 +41,10 @@ def test_large_patch_parameters_128_against_oracle(cntc, oracle):
     assert_parity(g, o, case)
 
 
-def test_sweep_256_against_fixture(cntc):
-    f = np.load(os.path.join(GOLD, "config1_256.npz"))
-    m = int(f["m"])
+@pytest.mark.parametrize("m", [256, 512])
+def test_sweep_against_fixture(cntc, m):
+    f = np.load(os.path.join(GOLD, "config1_%d.npz" % m))
+    assert int(f["m"]) == m
     case = C.config1(m, seed=int(f["seed"]), eps=float(f["eps"]), maxgs=int(f["maxgs"]))
     g = run_gpu(cntc, case, ire=102)
     assert int(cntc.getsolverstats(102, 1)["ctas"]) > 1          # a patch group
