@@ -262,8 +262,8 @@ int prepare(Problem &p, Prep &out, bool latency = false) {
     if (is_roll && std::fabs(chi) > 0.01) { log_msg("rolling direction chi != 0 is not supported"); return CNTC_err_other; }
     p.dt = dq / std::max(1e-10, veloc);
     // a single column in rolling direction is solved for the normal problem alone (FFT length 2
-    // in x, as for single rows in y); with a tangential problem the reference selects ConvexGS
-    // there, which is not on the device
+    // in x, as for single rows in y); with a tangential problem (ConvexGS in the reference) the
+    // one-column tangential operators are not verified, so it is refused
     if ((mx < 2 && p.tang != 0) || mx < 1 || my < 1) {
         log_msg("grids with mx < 2 are supported for the normal problem only");
         return CNTC_err_other;
