@@ -85,6 +85,11 @@ def parse():
 
 
 MIXED_TIER = 1     # FP32 convolution products along the FP64 iteration path
+# DRAM bytes (read + write) per algorithmic byte of k_solve, from one ncu capture of the
+# persistent solve on 304 patches with sides <= 64, two CTAs per SM: 41.5 GB of DRAM traffic
+# against 71.4 GB of algorithmic bytes in the same launch (the bench's own count).  The full
+# workload is too large to capture; its traffic is estimated with this ratio.
+TRAFFIC_PER_ALG_BYTE = 41.5 / 71.4
 
 
 def workload(n, seed, mixed=MIXED_TIER, max_side=0):
@@ -484,15 +489,19 @@ def run_gb300(args, dist):
         "phase_share_of_sm_cycles": phases,
         "steadygs_fallbacks": n_fallback,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "kernel": "k_solve",
+                     "frac": achieved / peak, "traffic": alg * TRAFFIC_PER_ALG_BYTE, "algorithmic_bytes": alg,
+                     "traffic_unit": "bytes per launch", "kernel": "k_solve",
                      "kernels_per_step": kernels_per_pass, "peak_source": peak_kind,
-                     "note": "k_solve is bound by the FP64 pipe (49 % busy with one CTA per SM in profiles/"
-                             "k_solve_mixed_side64_full.md), not by HBM: one patch's working set stays in L1/L2; "
-                             "achieved = algorithmic bytes (convolution inputs, spectra and outputs, and the "
-                             "iterations' vector passes) / patch-solve kernel time"},
+                     "traffic_source": "DRAM bytes per algorithmic byte of the ncu capture of k_solve on 304 "
+                                       "patches (profiles/k_solve_batch304_side64_full.md: 41.5 GB for 71.4 GB "
+                                       "algorithmic), times this launch's algorithmic bytes: an estimate",
+                     "note": "k_solve is bound by the FP64 pipe (57.5 % of the active cycles with two CTAs per SM, "
+                             "profiles/k_solve_batch304_side64_full.md), not by HBM; achieved = algorithmic bytes "
+                             "(convolution inputs, spectra and outputs, and the iterations' vector passes) / "
+                             "patch-solve kernel time"},
         "fma_peaks": dict(fmap, note="FMA-chain peaks of this GPU timed with CUDA events on all SMs; k_solve's "
-                                   "FP64 pipe is 49 % active with one CTA per SM (ncu, profiles/"
-                                   "k_solve_mixed_side64_full.md)"),
+                                   "FP64 pipe is 57.5 % active with two CTAs per SM (ncu, profiles/"
+                                   "k_solve_batch304_side64_full.md)"),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                 "errors": int((np.asarray(e_err) < 0).sum()),
