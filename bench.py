@@ -492,16 +492,14 @@ def run_gb300(args, dist):
                      "frac": achieved / peak, "traffic": alg * TRAFFIC_PER_ALG_BYTE, "algorithmic_bytes": alg,
                      "traffic_unit": "bytes per launch", "kernel": "k_solve",
                      "kernels_per_step": kernels_per_pass, "peak_source": peak_kind,
-                     "traffic_source": "DRAM bytes per algorithmic byte of the ncu capture of k_solve on 304 "
-                                       "patches (profiles/k_solve_batch304_side64_full.md: 41.5 GB for 71.4 GB "
-                                       "algorithmic), times this launch's algorithmic bytes: an estimate",
+                     "traffic_source": "DRAM bytes per algorithmic byte of one ncu capture of k_solve on 304 "
+                                       "patches with sides <= 64 (41.5 GB for 71.4 GB algorithmic), times this "
+                                       "launch's algorithmic bytes: an estimate",
                      "note": "k_solve is bound by the FP64 pipe (57.5 % of the active cycles with two CTAs per SM, "
-                             "profiles/k_solve_batch304_side64_full.md), not by HBM; achieved = algorithmic bytes "
-                             "(convolution inputs, spectra and outputs, and the iterations' vector passes) / "
-                             "patch-solve kernel time"},
+                             "ncu on 304 patches), not by HBM; achieved = algorithmic bytes (convolution inputs, "
+                             "spectra and outputs, and the iterations' vector passes) / patch-solve kernel time"},
         "fma_peaks": dict(fmap, note="FMA-chain peaks of this GPU timed with CUDA events on all SMs; k_solve's "
-                                   "FP64 pipe is 57.5 % active with two CTAs per SM (ncu, profiles/"
-                                   "k_solve_batch304_side64_full.md)"),
+                                   "FP64 pipe is 57.5 % active with two CTAs per SM (ncu on 304 patches)"),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes, "d2h_bytes_per_step": d2h_bytes,
                 "errors": int((np.asarray(e_err) < 0).sum()),
