@@ -6,11 +6,11 @@
 // :1519-1629).  Piecewise-constant tractions (C = 2).
 //
 // Two forms, as the reference:
-//   - arbitrary points (block type 9, sstres :1412-1515): one thread per point sums the field
+//   - arbitrary points (block type 9, sstres :1412-1515): one warp per point sums the field
 //     of every loaded element;
 //   - element centres at a depth (block types 1-7, sstres_inflcf + sstres_fft :1097-1408): the
 //     influence coefficients of one element at all grid offsets are tabulated once per depth
-//     (the quarter ix, iy <= 0 evaluated, the rest by the kernel's symmetries), then one thread
+//     (the quarter ix, iy <= 0 evaluated, the rest by the kernel's symmetries), then one warp
 //     per selected element centre sums table x tractions over the loaded elements.  The
 //     reference convolves the same table by FFT; the direct sum needs no spectra of the 36
 //     blocks and keeps the whole depth in one pass.
@@ -153,31 +153,42 @@ __device__ void subs_derived(double gg, double poiss, int neg, double vr[3][4], 
         for (int j = 0; j < 3; j++) out[9 + 3 * i + j] = fabs(sig[i][j]) < gg * tolsml ? 0.0 : sig[i][j];
 }
 
-// arbitrary points: the field of every element with positive pressure (sstres, :1412-1515)
+// the 12 sums of one output point, spread over the lanes of its warp, added up in a fixed
+// order (shuffles down to lane 0)
+__device__ inline void warp_sum12(double vr[3][4]) {
+    for (int j = 0; j < 3; j++)
+        for (int k = 0; k < 4; k++)
+            for (int o = 16; o > 0; o >>= 1) vr[j][k] += __shfl_down_sync(0xffffffffu, vr[j][k], o);
+}
+
+// arbitrary points: the field of every element with positive pressure (sstres, :1412-1515).
+// One warp per point; its lanes take every 32nd element of the grid, so that a few hundred
+// points still fill the device.
 __global__ void k_subs_points(SubsDev L, const double *xyz, int npts, double *out) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= npts) return;
+    const int q = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (q >= npts) return;                     // whole warps: blockDim is a multiple of 32
     double xw[3] = {xyz[3 * q], xyz[3 * q + 1], xyz[3 * q + 2]};
     const int ia = (xw[2] >= 0.0) ? 0 : 1, neg = (xw[2] >= 0.0) ? 1 : -1;
     xw[2] = neg * xw[2];
     xw[1] = neg * xw[1];
     double vr[3][4] = {};
     double v[3][3][4], vnu[3][3][4];
-    for (int iy = 0; iy < L.my; iy++)
-        for (int ix = 0; ix < L.mx; ix++) {
-            const int ii = ix + iy * L.mx;
-            if (!(L.pn[ii] > 0.0)) continue;
-            const double xp[2] = {L.xc1 + ix * L.dx, neg * (L.yc1 + iy * L.dy)};
-            stres1(L.dx, L.dy, L.gg[ia], v, vnu, xw, xp);
-            const double p[3] = {L.px[ii], L.py[ii], L.pn[ii]};
-            for (int j = 0; j < 3; j++)
-                for (int k = 0; k < 4; k++)
-                    for (int i = 0; i < 3; i++) {
-                        const int fi = (i == 0) ? neg : 1;
-                        vr[j][k] += fi * p[i] * (v[i][j][k] + L.poiss[ia] * vnu[i][j][k]);
-                    }
-        }
-    subs_derived(L.gg[ia], L.poiss[ia], neg, vr, out + (size_t)18 * q);
+    const int n = L.mx * L.my;
+    for (int ii = lane; ii < n; ii += 32) {
+        if (!(L.pn[ii] > 0.0)) continue;
+        const int ix = ii % L.mx, iy = ii / L.mx;
+        const double xp[2] = {L.xc1 + ix * L.dx, neg * (L.yc1 + iy * L.dy)};
+        stres1(L.dx, L.dy, L.gg[ia], v, vnu, xw, xp);
+        const double p[3] = {L.px[ii], L.py[ii], L.pn[ii]};
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 4; k++)
+                for (int i = 0; i < 3; i++) {
+                    const int fi = (i == 0) ? neg : 1;
+                    vr[j][k] += fi * p[i] * (v[i][j][k] + L.poiss[ia] * vnu[i][j][k]);
+                }
+    }
+    warp_sum12(vr);
+    if (lane == 0) subs_derived(L.gg[ia], L.poiss[ia], neg, vr, out + (size_t)18 * q);
 }
 
 // influence coefficients of one element at depth zw (sstres_inflcf, :1261-1408): tab[b][off],
@@ -213,29 +224,31 @@ __global__ void k_subs_table(SubsDev L, double zw, double *tab) {
 }
 
 // element centres (ixs[], iys[] 1-based) at depth zw: table x tractions summed over the
-// elements (sstres_fft, :1097-1257, here as a direct sum); the x traction is negated for body 2
+// elements (sstres_fft, :1097-1257, here as a direct sum); the x traction is negated for body
+// 2.  One warp per centre; its lanes take every 32nd element, so consecutive lanes read
+// consecutive table entries.
 __global__ void k_subs_conv(SubsDev L, double zw, const double *tab, const int *ixs, int nx, const int *iys, int ny,
                             double *out) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nx * ny) return;
+    const int q = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (q >= nx * ny) return;                  // whole warps: blockDim is a multiple of 32
     const int mx = L.mx, my = L.my;
     const int ixo = ixs[q % nx] - 1, iyo = iys[q / nx] - 1;
     const int ia = (zw >= 0.0) ? 0 : 1, neg = (zw >= 0.0) ? 1 : -1;
     const size_t bs = (size_t)4 * mx * my;
     double vr[3][4] = {};
-    for (int jy = 0; jy < my; jy++)
-        for (int jx = 0; jx < mx; jx++) {
-            const int jj = jx + jy * mx;
-            const double p[3] = {(ia == 1 ? -1.0 : 1.0) * L.px[jj], L.py[jj], L.pn[jj]};
-            if (p[0] == 0.0 && p[1] == 0.0 && p[2] == 0.0) continue;
-            const size_t o = (size_t)(ixo - jx + mx) + (size_t)(iyo - jy + my) * 2 * mx;
-            for (int k = 0; k < 4; k++)
-                for (int j = 0; j < 3; j++) {
-                    const double *b = tab + (size_t)(9 * k + 3 * j) * bs + o;
-                    vr[j][k] += b[0] * p[0] + b[bs] * p[1] + b[2 * bs] * p[2];
-                }
-        }
-    subs_derived(L.gg[ia], L.poiss[ia], neg, vr, out + (size_t)18 * q);
+    for (int jj = lane; jj < mx * my; jj += 32) {
+        const int jx = jj % mx, jy = jj / mx;
+        const double p[3] = {(ia == 1 ? -1.0 : 1.0) * L.px[jj], L.py[jj], L.pn[jj]};
+        if (p[0] == 0.0 && p[1] == 0.0 && p[2] == 0.0) continue;
+        const size_t o = (size_t)(ixo - jx + mx) + (size_t)(iyo - jy + my) * 2 * mx;
+        for (int k = 0; k < 4; k++)
+            for (int j = 0; j < 3; j++) {
+                const double *b = tab + (size_t)(9 * k + 3 * j) * bs + o;
+                vr[j][k] += b[0] * p[0] + b[bs] * p[1] + b[2 * bs] * p[2];
+            }
+    }
+    warp_sum12(vr);
+    if (lane == 0) subs_derived(L.gg[ia], L.poiss[ia], neg, vr, out + (size_t)18 * q);
 }
 
 } // namespace cgb
@@ -262,7 +275,9 @@ struct DevLoad {
     void release(cudaStream_t st) { if (buf) cudaFreeAsync(buf, st); buf = nullptr; }
 };
 
-constexpr int kSubsThreads = 128;
+// points per CTA of the summing kernels (one warp each); threads per CTA of the table kernel,
+// small so that the (mx + 1)(my + 1) table points of a modest grid spread over many SMs
+constexpr int kSubsWarps = 4, kSubsTableThreads = 32;
 
 } // namespace
 
@@ -279,7 +294,7 @@ int subs_points(const SubsLoad &L, int npts, const double *xyz, double *out) {
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(dxyz, xyz, (size_t)3 * npts * sizeof(double), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        k_subs_points<<<(npts + kSubsThreads - 1) / kSubsThreads, kSubsThreads, 0, st>>>(dl.d, dxyz, npts, dout);
+        k_subs_points<<<(npts + kSubsWarps - 1) / kSubsWarps, 32 * kSubsWarps, 0, st>>>(dl.d, dxyz, npts, dout);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)
@@ -310,9 +325,9 @@ int subs_depth(const SubsLoad &L, double zw, int nx, const int *ixs, int ny, con
     if (e == cudaSuccess) e = cudaMemcpyAsync(dix + nx, iys, (size_t)ny * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
         const int nq = (mx + 1) * (my + 1);
-        k_subs_table<<<(nq + kSubsThreads - 1) / kSubsThreads, kSubsThreads, 0, st>>>(dl.d, zw, tab);
-        k_subs_conv<<<(npts + kSubsThreads - 1) / kSubsThreads, kSubsThreads, 0, st>>>(dl.d, zw, tab, dix, nx,
-                                                                                      dix + nx, ny, dout);
+        k_subs_table<<<(nq + kSubsTableThreads - 1) / kSubsTableThreads, kSubsTableThreads, 0, st>>>(dl.d, zw, tab);
+        k_subs_conv<<<(npts + kSubsWarps - 1) / kSubsWarps, 32 * kSubsWarps, 0, st>>>(dl.d, zw, tab, dix, nx,
+                                                                                     dix + nx, ny, dout);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess)

@@ -84,7 +84,7 @@ def test_element_centres_and_points_against_oracle(cntc, oracle):
     depths (type 6), and explicit points in both bodies (type 9, z < 0 below the surface of body
     2).  Centres: the oracle's influence-coefficient path on the same tractions, within 1e-10 of
     each column's largest value (the GPU sums the tabulated coefficients directly, the oracle by
-    FFT); points: the oracle's direct sum within 1e-11."""
+    FFT); points: the oracle's direct sum within 1e-11 of the largest displacement (stress)."""
     ire, icp = 141, 1
     case = C.config0(gausei=5, eps=1e-10)
     cntc.setup_case(ire, icp, case)
@@ -125,5 +125,6 @@ def test_element_centres_and_points_against_oracle(cntc, oracle):
     assert np.allclose(np.stack([r3["x"], r3["y"], r3["z"]], 1), pts)
     d = oracle.subsurf_points(grid, res["pn"], res["px"], res["py"], gg, nu, pts)
     for name in FIELD:
-        scale = np.abs(d[:, ORC[name]]).max() + 1e-300
-        assert np.abs(r3[name] - d[:, ORC[name]]).max() <= 1e-11 * scale, name
+        grp = FIELD[:3] if name in FIELD[:3] else FIELD[3:]
+        scale = max(np.abs(d[:, ORC[c]]).max() for c in grp)
+        assert np.abs(r3[name] - d[:, ORC[name]]).max() <= PRINCIPAL_TOL.get(name, 1e-11) * scale, name
