@@ -26,73 +26,81 @@ struct SubsDev {
     double gg[2], poiss[2];
 };
 
-// Displacements v[i][j][0] in direction j and their gradients v[i][j][k] (d/dx_k) at xw due to a
-// unit traction in direction i on the dx x dy element centred at xp; vnu holds the parts
-// proportional to Poisson's ratio.  xw[2] >= 0.  The terms and their order of summation follow
-// m_subsurf.f90:1633-1852.
-__device__ __noinline__ void stres1(double dx, double dy, double gg, double v[3][3][4], double vnu[3][3][4],
-                                    const double xw[3], const double xp[2]) {
+// One corner (jx, jy = +-1) of the dx x dy element centred at xp, seen from xw (xw[2] >= 0):
+// its signed share of the displacements v[i][j][0] in direction j and their gradients
+// v[i][j][k] (d/dx_k) due to a unit traction in direction i, added to v; vnu collects the
+// parts proportional to Poisson's ratio.  The terms and their order of summation follow
+// m_subsurf.f90:1633-1852; the four corners together, divided by 4 pi gg, give the field.
+__device__ __noinline__ void stres1_corner(int jx, int jy, double dx, double dy, double v[3][3][4],
+                                           double vnu[3][3][4], const double xw[3], const double xp[2]) {
     const double epsrel = 5e-7;
     const int sgn[3] = {-1, -1, 1};
     const int nxt[3] = {1, 2, 0};
+    const double y[3] = {xp[0] + jx * dx / 2.0 - xw[0], xp[1] + jy * dy / 2.0 - xw[1], xw[2]};
+    const double w = fmax(1e-12, sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]));
+    // components moved away from zero to at least epsrel w (with their sign), so that the
+    // logarithms and quotients below stay finite on the element's edges
+    const double epsy = epsrel * w;
+    double ye[3];
+    for (int i = 0; i < 3; i++) ye[i] = (y[i] >= 0.0) ? fmax(epsy, y[i]) : fmin(-epsy, y[i]);
+    const double we = fmax(1e-12, sqrt(ye[0] * ye[0] + ye[1] * ye[1] + ye[2] * ye[2]));
+    double al[3], at[3], wm[4];
+    wm[0] = we;
+    for (int k = 0; k < 3; k++) {
+        al[k] = log(y[k] + we);
+        at[k] = atan((y[nxt[k]] + y[nxt[nxt[k]]] + w) / ye[k]);
+        wm[k + 1] = sgn[k] * y[k] / we;
+    }
+    double a[3][3][4], t[3][3][4];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            a[i][j][0] = y[i] * al[j];
+            t[i][j][0] = y[i] * at[j];
+            for (int k = 0; k < 3; k++) {
+                const double dik = i == k ? 1.0 : 0.0, djk = j == k ? 1.0 : 0.0;
+                a[i][j][k + 1] = sgn[k] * (dik * al[j] + y[i] * (djk * w + y[k]) / (we * (y[j] + we)));
+                t[i][j][k + 1] = sgn[k] * (dik * at[j] +
+                                           y[i] * (y[j] * (y[k] + w) - djk * w * (y[0] + y[1] + y[2] + w)) /
+                                               (2 * we * (y[nxt[j]] + we) * (y[nxt[nxt[j]]] + we)));
+            }
+        }
+    const double s = jx * jy;
+    for (int k = 0; k < 4; k++) {
+        for (int i = 0; i < 2; i++) {
+            const int l = 1 - i;
+            double q = a[i][l][k] + 2 * a[l][i][k] + 4 * t[2][2][k] + a[i][l][k] - 2 * t[2][i][k];
+            v[i][i][k] += s * q;
+            q = -2 * (a[i][l][k] - 2 * t[2][i][k]);
+            vnu[i][i][k] += q * s;
+            q = -a[2][2][k];
+            v[i][l][k] += s * q;
+            q = 2 * (a[2][2][k] - wm[k]);
+            vnu[i][l][k] += q * s;
+            q = 2 * (a[l][2][k] + a[2][l][k] + 2 * t[i][i][k]);
+            vnu[i][2][k] += q * s;
+            vnu[2][i][k] = -vnu[i][2][k];
+            q = -a[l][2][k] - 2 * t[i][i][k];
+            v[i][2][k] += q * s;
+            v[2][i][k] += (2 * a[2][l][k] - q) * s;
+        }
+        double q = -2 * (a[0][1][k] + a[1][0][k] + 2 * t[2][2][k]);
+        vnu[2][2][k] += q * s;
+        q = -2 * t[2][2][k] + 2 * (a[0][1][k] + a[1][0][k] + 2 * t[2][2][k]);
+        v[2][2][k] += q * s;
+    }
+}
+
+// Displacements v[i][j][0] in direction j and their gradients v[i][j][k] (d/dx_k) at xw due to a
+// unit traction in direction i on the dx x dy element centred at xp; vnu holds the parts
+// proportional to Poisson's ratio.  xw[2] >= 0.  The four corners in the reference's order
+// (m_subsurf.f90:1633-1852).
+__device__ __noinline__ void stres1(double dx, double dy, double gg, double v[3][3][4], double vnu[3][3][4],
+                                    const double xw[3], const double xp[2]) {
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
             for (int k = 0; k < 4; k++) { v[i][j][k] = 0.0; vnu[i][j][k] = 0.0; }
     for (int jx = -1; jx <= 1; jx += 2)
-        for (int jy = -1; jy <= 1; jy += 2) {
-            const double y[3] = {xp[0] + jx * dx / 2.0 - xw[0], xp[1] + jy * dy / 2.0 - xw[1], xw[2]};
-            const double w = fmax(1e-12, sqrt(y[0] * y[0] + y[1] * y[1] + y[2] * y[2]));
-            // components moved away from zero to at least epsrel w (with their sign), so that the
-            // logarithms and quotients below stay finite on the element's edges
-            const double epsy = epsrel * w;
-            double ye[3];
-            for (int i = 0; i < 3; i++) ye[i] = (y[i] >= 0.0) ? fmax(epsy, y[i]) : fmin(-epsy, y[i]);
-            const double we = fmax(1e-12, sqrt(ye[0] * ye[0] + ye[1] * ye[1] + ye[2] * ye[2]));
-            double al[3], at[3], wm[4];
-            wm[0] = we;
-            for (int k = 0; k < 3; k++) {
-                al[k] = log(y[k] + we);
-                at[k] = atan((y[nxt[k]] + y[nxt[nxt[k]]] + w) / ye[k]);
-                wm[k + 1] = sgn[k] * y[k] / we;
-            }
-            double a[3][3][4], t[3][3][4];
-            for (int i = 0; i < 3; i++)
-                for (int j = 0; j < 3; j++) {
-                    a[i][j][0] = y[i] * al[j];
-                    t[i][j][0] = y[i] * at[j];
-                    for (int k = 0; k < 3; k++) {
-                        const double dik = i == k ? 1.0 : 0.0, djk = j == k ? 1.0 : 0.0;
-                        a[i][j][k + 1] = sgn[k] * (dik * al[j] + y[i] * (djk * w + y[k]) / (we * (y[j] + we)));
-                        t[i][j][k + 1] = sgn[k] * (dik * at[j] +
-                                                   y[i] * (y[j] * (y[k] + w) - djk * w * (y[0] + y[1] + y[2] + w)) /
-                                                       (2 * we * (y[nxt[j]] + we) * (y[nxt[nxt[j]]] + we)));
-                    }
-                }
-            const double s = jx * jy;
-            for (int k = 0; k < 4; k++) {
-                for (int i = 0; i < 2; i++) {
-                    const int l = 1 - i;
-                    double q = a[i][l][k] + 2 * a[l][i][k] + 4 * t[2][2][k] + a[i][l][k] - 2 * t[2][i][k];
-                    v[i][i][k] += s * q;
-                    q = -2 * (a[i][l][k] - 2 * t[2][i][k]);
-                    vnu[i][i][k] += q * s;
-                    q = -a[2][2][k];
-                    v[i][l][k] += s * q;
-                    q = 2 * (a[2][2][k] - wm[k]);
-                    vnu[i][l][k] += q * s;
-                    q = 2 * (a[l][2][k] + a[2][l][k] + 2 * t[i][i][k]);
-                    vnu[i][2][k] += q * s;
-                    vnu[2][i][k] = -vnu[i][2][k];
-                    q = -a[l][2][k] - 2 * t[i][i][k];
-                    v[i][2][k] += q * s;
-                    v[2][i][k] += (2 * a[2][l][k] - q) * s;
-                }
-                double q = -2 * (a[0][1][k] + a[1][0][k] + 2 * t[2][2][k]);
-                vnu[2][2][k] += q * s;
-                q = -2 * t[2][2][k] + 2 * (a[0][1][k] + a[1][0][k] + 2 * t[2][2][k]);
-                v[2][2][k] += q * s;
-            }
-        }
+        for (int jy = -1; jy <= 1; jy += 2) stres1_corner(jx, jy, dx, dy, v, vnu, xw, xp);
     const double f = 4.0 * 3.14159265358979323846 * gg;
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++)
@@ -193,33 +201,54 @@ __global__ void k_subs_points(SubsDev L, const double *xyz, int npts, double *ou
 
 // influence coefficients of one element at depth zw (sstres_inflcf, :1261-1408): tab[b][off],
 // block b = 9 k + 3 j + i (quantity k: displacement or d/dx_k, output direction j, traction
-// direction i), offset (ix + mx) + (iy + my) 2mx for ix in [-mx, mx-1], iy in [-my, my-1].  One
-// thread per quarter offset ix, iy <= 0 evaluates the field and writes it with the signs of the
-// kernel's symmetry in x and in y to the mirrored offsets.
+// direction i), offset (ix + mx) + (iy + my) 2mx for ix in [-mx, mx-1], iy in [-my, my-1].
+// Four lanes per quarter offset ix, iy <= 0: lane c evaluates corner c of the element, the four
+// shares are added across the lanes, and lane c writes the field with the signs of the
+// kernel's symmetry in x and in y to mirror c of the offset (itself, in x, in y, in both).
 __global__ void k_subs_table(SubsDev L, double zw, double *tab) {
-    const int mx = L.mx, my = L.my;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (mx + 1) * (my + 1)) return;
+    const int mx = L.mx, my = L.my, nq = (mx + 1) * (my + 1);
+    const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int c = (int)(g & 3);
+    // no early exit: every lane of the grid takes part in the shuffles (the grid holds whole
+    // warps); lanes past the last offset compute the last one again and write nothing
+    const bool live = (g >> 2) < nq;
+    const int t = live ? (int)(g >> 2) : nq - 1;
     const int ix = -(t % (mx + 1)), iy = -(t / (mx + 1));
     const int ia = (zw >= 0.0) ? 0 : 1, neg = (zw >= 0.0) ? 1 : -1;
     const double xp[2] = {0.0, 0.0};
     const double xw[3] = {(double)(float)ix * L.dx, neg * (double)(float)iy * L.dy, neg * zw};
     double v[3][3][4], vnu[3][3][4];
-    stres1(L.dx, L.dy, L.gg[ia], v, vnu, xw, xp);
-    const size_t bs = (size_t)4 * mx * my;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 4; k++) { v[i][j][k] = 0.0; vnu[i][j][k] = 0.0; }
+    stres1_corner((c & 2) ? 1 : -1, (c & 1) ? 1 : -1, L.dx, L.dy, v, vnu, xw, xp);
+    const double f = 4.0 * 3.14159265358979323846 * L.gg[ia];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 4; k++) {
+                double a = v[i][j][k], b = vnu[i][j][k];
+                a += __shfl_xor_sync(0xffffffffu, a, 1);
+                b += __shfl_xor_sync(0xffffffffu, b, 1);
+                a += __shfl_xor_sync(0xffffffffu, a, 2);
+                b += __shfl_xor_sync(0xffffffffu, b, 2);
+                v[i][j][k] = a / f;
+                vnu[i][j][k] = b / f;
+            }
     const bool mirx = ix < 0 && -ix <= mx - 1, miry = iy < 0 && -iy <= my - 1;
-    auto off = [&](int ox, int oy) { return (size_t)(ox + mx) + (size_t)(oy + my) * 2 * mx; };
+    const bool wx = (c & 1) != 0, wy = (c & 2) != 0;
+    if (!live || (wx && !mirx) || (wy && !miry)) return;
+    const size_t bs = (size_t)4 * mx * my;
+    const size_t o = (size_t)((wx ? -ix : ix) + mx) + (size_t)((wy ? -iy : iy) + my) * 2 * mx;
     for (int k = 0; k < 4; k++)
         for (int j = 0; j < 3; j++)
             for (int i = 0; i < 3; i++) {
                 const double val = v[i][j][k] + L.poiss[ia] * vnu[i][j][k];
-                double *b = tab + (size_t)(9 * k + 3 * j + i) * bs;
                 const double fx = (k == 1 ? -1 : 1) * (j == 0 ? -1 : 1) * (i == 0 ? -1 : 1);
                 const double fy = (k == 2 ? -1 : 1) * (j == 1 ? -1 : 1) * (i == 1 ? -1 : 1);
-                b[off(ix, iy)] = val;
-                if (mirx) b[off(-ix, iy)] = fx * val;
-                if (miry) b[off(ix, -iy)] = fy * val;
-                if (mirx && miry) b[off(-ix, -iy)] = fy * (fx * val);
+                double w = val;
+                if (wx) w = fx * w;
+                if (wy) w = fy * w;
+                tab[(size_t)(9 * k + 3 * j + i) * bs + o] = w;
             }
 }
 
@@ -275,9 +304,9 @@ struct DevLoad {
     void release(cudaStream_t st) { if (buf) cudaFreeAsync(buf, st); buf = nullptr; }
 };
 
-// points per CTA of the summing kernels (one warp each); threads per CTA of the table kernel,
-// small so that the (mx + 1)(my + 1) table points of a modest grid spread over many SMs
-constexpr int kSubsWarps = 4, kSubsTableThreads = 32;
+// points per CTA of the summing kernels (one warp each); threads per CTA of the table kernel
+// (four per table offset; a multiple of 32, so that its shuffles see whole warps)
+constexpr int kSubsWarps = 4, kSubsTableThreads = 64;
 
 } // namespace
 
@@ -324,8 +353,9 @@ int subs_depth(const SubsLoad &L, double zw, int nx, const int *ixs, int ny, con
     if (e == cudaSuccess) e = cudaMemcpyAsync(dix, ixs, (size_t)nx * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dix + nx, iys, (size_t)ny * sizeof(int), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        const int nq = (mx + 1) * (my + 1);
-        k_subs_table<<<(nq + kSubsTableThreads - 1) / kSubsTableThreads, kSubsTableThreads, 0, st>>>(dl.d, zw, tab);
+        const long long nt = 4LL * (mx + 1) * (my + 1);
+        k_subs_table<<<(unsigned)((nt + kSubsTableThreads - 1) / kSubsTableThreads), kSubsTableThreads, 0, st>>>(
+            dl.d, zw, tab);
         k_subs_conv<<<(npts + kSubsWarps - 1) / kSubsWarps, 32 * kSubsWarps, 0, st>>>(dl.d, zw, tab, dix, nx,
                                                                                      dix + nx, ny, dout);
         e = cudaGetLastError();
