@@ -421,7 +421,16 @@ struct Arena {
     // device, which would stall every other pass in flight, so they are kept until the thread
     // that owns the arena exits
     std::vector<void *> retired_host;
-    ~Arena() { for (void *q : retired_host) cudaFreeHost(q); }
+    // at thread exit: the arena's passes have all completed (each call waits for its own), so
+    // its buffers and stream are released here, not leaked with the thread
+    ~Arena() {
+        for (void *q : retired_host) cudaFreeHost(q);
+        if (h_io) cudaFreeHost(h_io);
+        if (h_flags) cudaFreeHost(h_flags);
+        for (void *q : {(void *)d_io, (void *)d_work, (void *)d_desc, (void *)d_list})
+            if (q) cudaFree(q);
+        if (copy_st) cudaStreamDestroy(copy_st);
+    }
 };
 
 // Device buffers come from the stream-ordered allocator on the caller's stream: a replaced
