@@ -1824,7 +1824,8 @@ void subs_addblock(int *ire, int *icp, int *iblk, int *isubs, int *npx, int *npy
     if (b <= 0) return;
     SubsBlock s;
     s.isubs = t;
-    auto clamp_n = [](int n) { return std::max(1, std::min(n, kMaxSubsPoints)); };
+    // a list of n <= 0 values is empty (its array is not read): the block then has no points
+    auto clamp_n = [](int n) { return std::max(0, std::min(n, kMaxSubsPoints)); };
     auto unique_positive = [&](int n, const double *v) {
         std::vector<int> r;
         for (int i = 0; i < clamp_n(n); i++) { const int k = (int)std::lround(v[i]); if (k > 0) r.push_back(k); }

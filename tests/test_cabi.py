@@ -244,3 +244,24 @@ def test_single_column_refused_for_tangential_problems(lib, capfd):
     finally:
         cg.setglobalflags([cg.CNTC_if_idebug], [0])
         cg.finalize(ire)
+
+
+def test_subsurface_block_with_empty_list_reads_no_parameters(lib):
+    """subs_addBlock with a list of zero values (npx = 0 for explicit points) reads nothing
+    from that list: a null array does not crash the call.  An invalid block type (4) and a
+    wrong parameter count (type 2 needs three per direction) are refused without reading
+    their (null) arrays."""
+    ire, icp = 910, 1
+    cg.setnormalforce(ire, icp, 1e4)
+    y = np.array([0.0, 1.0])
+    z = np.array([0.5])
+    null = ctypes.POINTER(ctypes.c_double)()
+    lib.subs_addblock(_i(ire), _i(icp), _i(1), _i(9), _i(0), _i(2), _i(1), null, y.ctypes.data_as(cg._DP),
+                      z.ctypes.data_as(cg._DP))
+    lib.subs_addblock(_i(ire), _i(icp), _i(2), _i(4), _i(0), _i(0), _i(1), null, null, z.ctypes.data_as(cg._DP))
+    lib.subs_addblock(_i(ire), _i(icp), _i(2), _i(2), _i(2), _i(3), _i(1), null, null, z.ctypes.data_as(cg._DP))
+    # blocks beyond the list are unknown: no points, the output is left as it was
+    nx, ny, nz = ctypes.c_int(7), ctypes.c_int(7), ctypes.c_int(7)
+    lib.subs_getblocksize(_i(ire), _i(icp), _i(2), ctypes.byref(nx), ctypes.byref(ny), ctypes.byref(nz))
+    assert (nx.value, ny.value, nz.value) == (0, 0, 0)
+    cg.finalize(ire)
